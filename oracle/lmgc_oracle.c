@@ -1,0 +1,533 @@
+/* lmgc_oracle.c -- sequential C restatement of UG 3.12.1's lmgc path.
+ * TEST INFRASTRUCTURE ONLY (see lmgc_oracle.h).  Each function names the
+ * reference routine whose arithmetic it restates. */
+#include "lmgc_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ACTIVE_CLASS 3 /* gm/algebra.h: vectors the smoothers update */
+#define NEWDEF_CLASS 2 /* gm/algebra.h: vectors carrying a new defect */
+
+/* SolveSmallBlock, np/algebra/block.cc:104-224: n=1 division, n=2 Cramer
+ * with the inverted determinant, n=3 the reference's elimination formula,
+ * larger n Gaussian elimination with partial pivoting. */
+static int solve_small(int n, double *sol, const double *m, const double *rhs) {
+  if (n == 1) { sol[0] = rhs[0] / m[0]; return 0; }
+  if (n == 2) {
+    double det = m[0] * m[3] - m[1] * m[2];
+    if (det == 0.0) return 1;
+    det = 1.0 / det;
+    sol[0] = (rhs[0] * m[3] - rhs[1] * m[1]) * det;
+    sol[1] = (rhs[1] * m[0] - rhs[0] * m[2]) * det;
+    return 0;
+  }
+  if (n == 3) {
+    double M3div0 = m[3] / m[0], M6div0 = m[6] / m[0];
+    double aux = (m[7] - M6div0 * m[1]) / (m[4] - M3div0 * m[1]);
+    sol[2] = (rhs[2] - M6div0 * rhs[0] - aux * (rhs[1] - M3div0 * rhs[0])) /
+             (m[8] - M6div0 * m[2] - aux * (m[5] - M3div0 * m[2]));
+    sol[1] = (rhs[1] - m[3] / m[0] * rhs[0] - (m[5] - M3div0 * m[2]) * sol[2]) / (m[4] - M3div0 * m[1]);
+    sol[0] = (rhs[0] - m[1] * sol[1] - m[2] * sol[2]) / m[0];
+    return 0;
+  }
+  double a[ORC_MAX_S * ORC_MAX_S], b[ORC_MAX_S];
+  memcpy(a, m, sizeof(double) * n * n);
+  memcpy(b, rhs, sizeof(double) * n);
+  for (int i = 0; i < n; ++i) {
+    int p = i;
+    for (int k = i + 1; k < n; ++k) if (fabs(a[k * n + i]) > fabs(a[p * n + i])) p = k;
+    if (a[p * n + i] == 0.0) return 1;
+    if (p != i) {
+      for (int k = 0; k < n; ++k) { double t = a[i * n + k]; a[i * n + k] = a[p * n + k]; a[p * n + k] = t; }
+      double t = b[i]; b[i] = b[p]; b[p] = t;
+    }
+    for (int k = i + 1; k < n; ++k) {
+      double f = a[k * n + i] / a[i * n + i];
+      for (int j = i; j < n; ++j) a[k * n + j] -= f * a[i * n + j];
+      b[k] -= f * b[i];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = b[i];
+    for (int j = i + 1; j < n; ++j) s -= a[i * n + j] * sol[j];
+    sol[i] = s / a[i * n + i];
+  }
+  return 0;
+}
+
+/* InvertSmallBlock, block.cc:272-330 (n=1,2 closed form; larger n by
+ * solving against the unit vectors). */
+static int invert_small(int n, const double *m, double *inv) {
+  if (n == 1) {
+    if (fabs(m[0]) < 1e-25) return 1;
+    inv[0] = 1.0 / m[0];
+    return 0;
+  }
+  if (n == 2) {
+    double det = m[0] * m[3] - m[1] * m[2];
+    if (fabs(det) < 1e-25) return 1;
+    double id = 1.0 / det;
+    inv[0] = m[3] * id; inv[1] = -m[1] * id; inv[2] = -m[2] * id; inv[3] = m[0] * id;
+    return 0;
+  }
+  if (n == 3) {
+    double det = m[0] * m[4] * m[8] + m[1] * m[5] * m[6] + m[2] * m[3] * m[7] - m[2] * m[4] * m[6] -
+                 m[0] * m[5] * m[7] - m[1] * m[3] * m[8];
+    if (fabs(det) < 1e-25) return 1;
+    double id = 1.0 / det;
+    inv[0] = (m[4] * m[8] - m[5] * m[7]) * id;
+    inv[3] = (-m[3] * m[8] + m[5] * m[6]) * id;
+    inv[6] = (m[3] * m[7] - m[4] * m[6]) * id;
+    inv[1] = (-m[1] * m[8] + m[2] * m[7]) * id;
+    inv[4] = (m[0] * m[8] - m[2] * m[6]) * id;
+    inv[7] = (-m[0] * m[7] + m[1] * m[6]) * id;
+    inv[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+    inv[5] = (-m[0] * m[5] + m[2] * m[3]) * id;
+    inv[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+    return 0;
+  }
+  for (int c = 0; c < n; ++c) {
+    double e[ORC_MAX_S] = {0}, x[ORC_MAX_S];
+    e[c] = 1.0;
+    if (solve_small(n, x, m, e)) return 1;
+    for (int r = 0; r < n; ++r) inv[r * n + c] = x[r];
+  }
+  return 0;
+}
+
+/* dmatmul_minus, np/algebra/ugblas.cc:3997 (templates matfunc.ct /
+ * matloop.ct, MATMUL_rc macros ugblas.h:161-340): per row the products of
+ * all row entries (diagonal first) are summed, then subtracted once. */
+void orc_matmul_minus(const orc_level *L, double *x, const double *y) {
+  const int s = L->s, ss = s * s;
+  for (int i = 0; i < L->n; ++i) {
+    double acc[ORC_MAX_S] = {0};
+    for (int k = L->rowptr[i]; k < L->rowptr[i + 1]; ++k) {
+      const double *m = L->val + (size_t)k * ss;
+      const double *w = y + (size_t)L->col[k] * s;
+      for (int r = 0; r < s; ++r) {
+        double t = 0.0;
+        for (int c = 0; c < s; ++c) t += m[r * s + c] * w[c];
+        acc[r] += t;
+      }
+    }
+    for (int r = 0; r < s; ++r) x[(size_t)i * s + r] -= acc[r];
+  }
+}
+
+/* l_jac, np/algebra/ugiter.cc:271-356: v = D^{-1} d on ACTIVE vectors,
+ * zero elsewhere. */
+int orc_jac(const orc_level *L, double *v, const double *d) {
+  const int s = L->s, ss = s * s;
+  for (int i = 0; i < L->n; ++i) {
+    double *vi = v + (size_t)i * s;
+    if (L->vclass[i] < ACTIVE_CLASS) { for (int r = 0; r < s; ++r) vi[r] = 0.0; continue; }
+    const double *D = L->val + (size_t)L->rowptr[i] * ss;
+    if (s == 1) vi[0] = d[i] / D[0];
+    else if (solve_small(s, vi, D, d + (size_t)i * s)) return -(i + 1);
+  }
+  return 0;
+}
+
+/* l_lgs, ugiter.cc:412-612: forward solve of (D+L) v = d in list order,
+ * L = entries to ACTIVE vectors earlier in the list. */
+int orc_lgs(const orc_level *L, double *v, const double *d) {
+  const int s = L->s, ss = s * s;
+  for (int i = 0; i < L->n; ++i) {
+    double *vi = v + (size_t)i * s;
+    if (L->vclass[i] < ACTIVE_CLASS) { for (int r = 0; r < s; ++r) vi[r] = 0.0; continue; }
+    const int k0 = L->rowptr[i];
+    if (s == 1) {
+      double sum = 0.0;
+      for (int k = k0 + 1; k < L->rowptr[i + 1]; ++k) {
+        int j = L->col[k];
+        if (j < i && L->vclass[j] >= ACTIVE_CLASS) sum += L->val[k] * v[j];
+      }
+      vi[0] = (d[i] - sum) / L->val[k0];
+    } else {
+      double rhs[ORC_MAX_S], acc[ORC_MAX_S] = {0};
+      for (int r = 0; r < s; ++r) rhs[r] = d[(size_t)i * s + r];
+      for (int k = k0 + 1; k < L->rowptr[i + 1]; ++k) {
+        int j = L->col[k];
+        if (!(j < i && L->vclass[j] >= ACTIVE_CLASS)) continue;
+        const double *m = L->val + (size_t)k * ss, *w = v + (size_t)j * s;
+        for (int r = 0; r < s; ++r) {
+          double t = 0.0;
+          for (int c = 0; c < s; ++c) t += m[r * s + c] * w[c];
+          acc[r] += t;
+        }
+      }
+      for (int r = 0; r < s; ++r) rhs[r] -= acc[r];
+      if (solve_small(s, vi, L->val + (size_t)k0 * ss, rhs)) return -(i + 1);
+    }
+  }
+  return 0;
+}
+
+static int find_entry(const orc_level *L, int row, int col) {
+  for (int k = L->rowptr[row]; k < L->rowptr[row + 1]; ++k)
+    if (L->col[k] == col) return k;
+  return -1;
+}
+
+/* l_ilubthdecomp, ugiter.cc:2252-2625, without threshold / rest vector
+ * (as called by ILUPreProcess, np/procs/iter.cc:5444): in-place ILU(0) in
+ * list order.  Row i's diagonal block is replaced by its inverse
+ * (StoreInverse), each (j,i) below it by the pivot L_ji = A_ji D_i^{-1},
+ * and the pattern entries (j,k), k>i, are updated.  Off-pattern fill is
+ * dropped; beta adds it back to the diagonal (scalar: beta*|fill|,
+ * blocks: the diagonal's columns scaled by 1+beta*rowsum). */
+int orc_ilu_decomp(const orc_level *L, double *lu, const double *beta) {
+  const int s = L->s, ss = s * s, n = L->n;
+  memcpy(lu, L->val, sizeof(double) * (size_t)L->rowptr[n] * ss);
+  for (int i = 0; i < n; ++i) {
+    if (L->vclass[i] < ACTIVE_CLASS) continue;
+    const int kd = L->rowptr[i];
+    if (s == 1) {
+      double diag = lu[kd];
+      if (fabs(diag) < DBL_EPSILON * 10 * 1e-20) return -(i + 1);
+      double invdiag = 1.0 / diag;
+      lu[kd] = invdiag;
+      for (int kij = kd + 1; kij < L->rowptr[i + 1]; ++kij) {
+        int j = L->col[kij];
+        if (!(L->vclass[j] >= ACTIVE_CLASS && j > i)) continue;
+        int kji = find_entry(L, j, i);
+        double pivot = lu[kji] * invdiag;
+        lu[kji] = pivot;
+        if (pivot == 0.0) continue;
+        for (int kik = kd + 1; kik < L->rowptr[i + 1]; ++kik) {
+          int k = L->col[kik];
+          if (!(L->vclass[k] >= ACTIVE_CLASS && k > i)) continue;
+          int kjk = find_entry(L, j, k);
+          if (kjk >= 0) lu[kjk] -= pivot * lu[kik];
+          else if (beta) lu[L->rowptr[j]] += beta[0] * fabs(pivot * lu[kik]);
+        }
+      }
+    } else {
+      double inv[ORC_MAX_S * ORC_MAX_S];
+      if (invert_small(s, lu + (size_t)kd * ss, inv)) return -(i + 1);
+      memcpy(lu + (size_t)kd * ss, inv, sizeof(double) * ss);
+      for (int kij = kd + 1; kij < L->rowptr[i + 1]; ++kij) {
+        int j = L->col[kij];
+        if (!(L->vclass[j] >= ACTIVE_CLASS && i < j)) continue;
+        double rowsum[ORC_MAX_S] = {0};
+        int kji = find_entry(L, j, i);
+        double *piv = lu + (size_t)kji * ss, pm[ORC_MAX_S * ORC_MAX_S];
+        int zero = 1;
+        for (int r = 0; r < s; ++r)
+          for (int c = 0; c < s; ++c) {
+            double sum = 0.0;
+            for (int q = 0; q < s; ++q) sum += piv[r * s + q] * inv[q * s + c];
+            pm[r * s + c] = sum;
+            if (sum != 0.0) zero = 0;
+          }
+        memcpy(piv, pm, sizeof(double) * ss);
+        if (zero) continue;
+        for (int kik = kd + 1; kik < L->rowptr[i + 1]; ++kik) {
+          int k = L->col[kik];
+          if (!(L->vclass[k] >= ACTIVE_CLASS && i < k)) continue;
+          const double *elm = lu + (size_t)kik * ss;
+          double cor[ORC_MAX_S * ORC_MAX_S];
+          int cz = 1;
+          for (int r = 0; r < s; ++r)
+            for (int c = 0; c < s; ++c) {
+              double sum = 0.0;
+              for (int q = 0; q < s; ++q) sum += pm[r * s + q] * elm[q * s + c];
+              cor[r * s + c] = sum;
+              if (sum != 0.0) cz = 0;
+            }
+          if (cz) continue;
+          int kjk = find_entry(L, j, k);
+          if (kjk >= 0) {
+            double *mat = lu + (size_t)kjk * ss;
+            for (int q = 0; q < ss; ++q) mat[q] -= cor[q];
+          } else {
+            for (int r = 0; r < s; ++r)
+              for (int c = 0; c < s; ++c) rowsum[r] += fabs(cor[r * s + c]);
+          }
+        }
+        if (!beta) continue;
+        double *djj = lu + (size_t)L->rowptr[j] * ss;
+        for (int r = 0; r < s; ++r)
+          for (int c = 0; c < s; ++c) djj[r * s + c] *= 1.0 + beta[c] * rowsum[c];
+      }
+    }
+  }
+  return 0;
+}
+
+/* l_luiter, ugiter.cc:4444-4796: forward solve with the unit lower factor
+ * in list order, then backward solve with the upper factor in reverse list
+ * order, multiplying by the stored inverse diagonal. */
+int orc_luiter(const orc_level *L, const double *lu, double *v, const double *d) {
+  const int s = L->s, ss = s * s, n = L->n;
+  for (int i = 0; i < n; ++i) {
+    double *vi = v + (size_t)i * s;
+    if (L->vclass[i] < ACTIVE_CLASS) { for (int r = 0; r < s; ++r) vi[r] = 0.0; continue; }
+    double acc[ORC_MAX_S] = {0};
+    for (int k = L->rowptr[i] + 1; k < L->rowptr[i + 1]; ++k) {
+      int j = L->col[k];
+      if (!(j < i && L->vclass[j] >= ACTIVE_CLASS)) continue;
+      const double *m = lu + (size_t)k * ss, *w = v + (size_t)j * s;
+      if (s == 1) { acc[0] += m[0] * w[0]; continue; }
+      for (int r = 0; r < s; ++r) {
+        double t = 0.0;
+        for (int c = 0; c < s; ++c) t += m[r * s + c] * w[c];
+        acc[r] += t;
+      }
+    }
+    for (int r = 0; r < s; ++r) vi[r] = d[(size_t)i * s + r] - acc[r];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    if (L->vclass[i] < ACTIVE_CLASS) continue;
+    double *vi = v + (size_t)i * s;
+    double acc[ORC_MAX_S] = {0};
+    for (int k = L->rowptr[i] + 1; k < L->rowptr[i + 1]; ++k) {
+      int j = L->col[k];
+      if (!(j > i && L->vclass[j] >= ACTIVE_CLASS)) continue;
+      const double *m = lu + (size_t)k * ss, *w = v + (size_t)j * s;
+      if (s == 1) { acc[0] += m[0] * w[0]; continue; }
+      for (int r = 0; r < s; ++r) {
+        double t = 0.0;
+        for (int c = 0; c < s; ++c) t += m[r * s + c] * w[c];
+        acc[r] += t;
+      }
+    }
+    const double *dinv = lu + (size_t)L->rowptr[i] * ss;
+    if (s == 1) { vi[0] = (vi[0] - acc[0]) * dinv[0]; continue; }
+    double rhs[ORC_MAX_S];
+    for (int r = 0; r < s; ++r) rhs[r] = vi[r] - acc[r];
+    for (int r = 0; r < s; ++r) {
+      double sum = 0.0;
+      for (int c = 0; c < s; ++c) sum += dinv[r * s + c] * rhs[c];
+      vi[r] = sum;
+    }
+  }
+  return 0;
+}
+
+/* dnrm2x, ugblas.cc:3156: per-component Euclidean norms, summed in list
+ * order over the vectors with NEW_DEFECT (VCLASS >= 2), which is the
+ * ON_SURFACE set of the top level of a uniformly refined hierarchy. */
+void orc_nrm2x(const orc_level *L, const double *x, double *out) {
+  const int s = L->s;
+  for (int r = 0; r < s; ++r) out[r] = 0.0;
+  for (int i = 0; i < L->n; ++i) {
+    if (L->vclass[i] < NEWDEF_CLASS) continue;
+    for (int r = 0; r < s; ++r) { double v = x[(size_t)i * s + r]; out[r] += v * v; }
+  }
+  for (int r = 0; r < s; ++r) out[r] = sqrt(out[r]);
+}
+
+/* StandardRestrictNodeVector, np/algebra/transgrid.cc:117-232: reset the
+ * coarse vectors with VNCLASS >= NEWDEF_CLASS, then every fine vector with
+ * VCLASS >= NEWDEF_CLASS adds weight*damp*value to its coarse parents,
+ * except into components the coarse VECSKIP marks. */
+void orc_restrict(const orc_level *fine, const orc_level *coarse, double *to, const double *from,
+                  const double *damp) {
+  const int s = fine->s;
+  for (int c = 0; c < coarse->n; ++c)
+    if (coarse->vnclass[c] >= NEWDEF_CLASS)
+      for (int r = 0; r < s; ++r) to[(size_t)c * s + r] = 0.0;
+  for (int f = 0; f < fine->n; ++f) {
+    if (fine->vclass[f] < NEWDEF_CLASS) continue;
+    double sv[ORC_MAX_S];
+    for (int r = 0; r < s; ++r) sv[r] = damp[r] * from[(size_t)f * s + r];
+    for (int k = fine->prowptr[f]; k < fine->prowptr[f + 1]; ++k) {
+      int c = fine->pcol[k];
+      int sk = coarse->skip[c];
+      for (int r = 0; r < s; ++r)
+        if (!(sk & (1 << r))) to[(size_t)c * s + r] += fine->pw[k] * sv[r];
+    }
+  }
+}
+
+/* StandardIntCorNodeVector, transgrid.cc:235-347: reset the fine vector,
+ * then every fine vector not skipped in all components takes
+ * sum_i weight_i*damp*coarse_i in each component its VECSKIP leaves free. */
+void orc_interpolate(const orc_level *fine, double *to, const double *from, const double *damp) {
+  const int s = fine->s;
+  memset(to, 0, sizeof(double) * (size_t)fine->n * s);
+  for (int f = 0; f < fine->n; ++f) {
+    int sk = fine->skip[f];
+    if (sk == (1 << s) - 1) continue;
+    for (int r = 0; r < s; ++r) {
+      if (sk & (1 << r)) continue;
+      double acc = 0.0;
+      for (int k = fine->prowptr[f]; k < fine->prowptr[f + 1]; ++k)
+        acc += fine->pw[k] * damp[r] * from[(size_t)fine->pcol[k] * s + r];
+      to[(size_t)f * s + r] = acc;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- solver */
+typedef struct {
+  const orc_mg *mg;
+  double **c, **t, **b, **lu; /* per level */
+  double *base_lu;            /* dense LU of the base level (no pivoting) */
+  int base_n;
+} orc_ws;
+
+/* ex base solver, np/procs/iter.cc:8685-9068 with the band LU of
+ * gm/evm.cc (EXDecomposeMatrixDOUBLE / EXApplyLUDOUBLE): LU without
+ * pivoting in list order; the dense matrix here is the band with full width. */
+static int base_factor(orc_ws *w, const orc_level *L) {
+  const int s = L->s, n = L->n * s;
+  w->base_n = n;
+  w->base_lu = (double *)calloc((size_t)n * n, sizeof(double));
+  if (!w->base_lu) return -1;
+  double *M = w->base_lu;
+  for (int i = 0; i < L->n; ++i)
+    for (int k = L->rowptr[i]; k < L->rowptr[i + 1]; ++k)
+      for (int r = 0; r < s; ++r)
+        for (int c = 0; c < s; ++c) M[(size_t)(i * s + r) * n + L->col[k] * s + c] = L->val[(size_t)k * s * s + r * s + c];
+  for (int i = 0; i < n - 1; ++i) {
+    double d = M[(size_t)i * n + i];
+    if (d == 0.0) return -1;
+    for (int j = i + 1; j < n; ++j) {
+      double f = M[(size_t)j * n + i] / d;
+      M[(size_t)j * n + i] = f;
+      for (int k = i + 1; k < n; ++k) M[(size_t)j * n + k] -= f * M[(size_t)i * n + k];
+    }
+  }
+  return 0;
+}
+
+static void base_apply(const orc_ws *w, double *vec) {
+  const int n = w->base_n;
+  const double *M = w->base_lu;
+  for (int i = 1; i < n; ++i)
+    for (int j = 0; j < i; ++j) vec[i] -= M[(size_t)i * n + j] * vec[j];
+  for (int i = n - 1; i >= 0; --i) {
+    for (int j = i + 1; j < n; ++j) vec[i] -= M[(size_t)i * n + j] * vec[j];
+    vec[i] /= M[(size_t)i * n + i];
+  }
+}
+
+/* Smoother, iter.cc:817-842: t = Step(b); t *= damp; b -= A t. */
+static int smooth(orc_ws *w, int l, double *t, double *b) {
+  const orc_mg *mg = w->mg;
+  const orc_level *L = &mg->lev[l];
+  const int s = L->s;
+  int rc;
+  if (mg->smoother == ORC_JAC) rc = orc_jac(L, t, b);
+  else if (mg->smoother == ORC_GS) rc = orc_lgs(L, t, b);
+  else rc = orc_luiter(L, w->lu[l], t, b);
+  if (rc) return rc;
+  for (int i = 0; i < L->n; ++i)
+    for (int r = 0; r < s; ++r) t[(size_t)i * s + r] *= mg->damp[r];
+  orc_matmul_minus(L, b, t);
+  return 0;
+}
+
+static void vadd(double *x, const double *y, size_t n) { for (size_t i = 0; i < n; ++i) x[i] += y[i]; }
+
+/* Lmgc, iter.cc:7741-7949. */
+static int lmgc(orc_ws *w, int l) {
+  const orc_mg *mg = w->mg;
+  const orc_level *L = &mg->lev[l];
+  const size_t len = (size_t)L->n * L->s;
+  double *c = w->c[l], *b = w->b[l], *t = w->t[l];
+  int rc;
+  if (l <= mg->baselevel) {
+    /* base ls with $m 1 and the ex iteration: c += A^{-1} b; b -= A (A^{-1} b),
+     * skipped when the defect is already below the base abslimit */
+    double nb[ORC_MAX_S];
+    orc_nrm2x(L, b, nb);
+    int below = 1;
+    for (int r = 0; r < L->s; ++r)
+      if (fabs(nb[r]) >= fabs(mg->base_abslimit[r])) below = 0;
+    if (below) return 0;
+    memcpy(t, b, sizeof(double) * len);
+    base_apply(w, t);
+    orc_matmul_minus(L, b, t);
+    vadd(c, t, len);
+    return 0;
+  }
+  for (int i = 0; i < mg->nu1; ++i) {
+    if ((rc = smooth(w, l, t, b))) return rc;
+    vadd(c, t, len);
+  }
+  const orc_level *Lc = &mg->lev[l - 1];
+  double one[ORC_MAX_S];
+  for (int r = 0; r < ORC_MAX_S; ++r) one[r] = 1.0;
+  orc_restrict(L, Lc, w->b[l - 1], b, one);
+  memset(w->c[l - 1], 0, sizeof(double) * (size_t)Lc->n * Lc->s);
+  for (int g = 0; g < mg->gamma; ++g)
+    if ((rc = lmgc(w, l - 1))) return rc;
+  orc_interpolate(L, t, w->c[l - 1], mg->cdamp);
+  vadd(c, t, len);
+  orc_matmul_minus(L, b, t);
+  for (int i = 0; i < mg->nu2; ++i) {
+    if ((rc = smooth(w, l, t, b))) return rc;
+    vadd(c, t, len);
+  }
+  return 0;
+}
+
+/* sc_cmp, np/udm/npscan.cc:1027-1057: 1 iff every |x_i| < |y_i|. */
+static int sc_cmp(const double *x, const double *y, int s) {
+  for (int i = 0; i < s; ++i)
+    if (fabs(x[i]) >= fabs(y[i])) return 0;
+  return 1;
+}
+
+/* LinearSolver, np/procs/ls.cc:637-749, preceded by LinearDefect (562) and
+ * LinearResiduum (577); LSUpdate (869) adds c on levels baselevel..top. */
+int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
+                 double *hist, int *converged) {
+  const int top = mg->nlevels - 1;
+  const int s = mg->lev[top].s;
+  const int bl = mg->baselevel < top ? mg->baselevel : top;
+  orc_ws w;
+  memset(&w, 0, sizeof w);
+  w.mg = mg;
+  w.c = (double **)calloc(mg->nlevels, sizeof(double *));
+  w.t = (double **)calloc(mg->nlevels, sizeof(double *));
+  w.b = (double **)calloc(mg->nlevels, sizeof(double *));
+  w.lu = (double **)calloc(mg->nlevels, sizeof(double *));
+  int rc = 0, it = 0;
+  *converged = 0;
+  for (int l = bl; l <= top; ++l) {
+    size_t len = (size_t)mg->lev[l].n * s;
+    w.c[l] = (double *)calloc(len, sizeof(double));
+    w.t[l] = (double *)calloc(len, sizeof(double));
+    w.b[l] = (l == top) ? b : (double *)calloc(len, sizeof(double));
+    if (mg->smoother == ORC_ILU && l > bl) {
+      const orc_level *L = &mg->lev[l];
+      w.lu[l] = (double *)malloc(sizeof(double) * (size_t)L->rowptr[L->n] * s * s);
+      if ((rc = orc_ilu_decomp(L, w.lu[l], mg->beta))) goto done;
+    }
+  }
+  if (base_factor(&w, &mg->lev[bl])) { rc = -1000000; goto done; }
+  {
+    const orc_level *T = &mg->lev[top];
+    const size_t len = (size_t)T->n * s;
+    double first[ORC_MAX_S], last[ORC_MAX_S], reach[ORC_MAX_S];
+    orc_matmul_minus(T, b, x);
+    orc_nrm2x(T, b, first);
+    if (hist) for (int r = 0; r < s; ++r) hist[r] = first[r];
+    for (int r = 0; r < s; ++r) { reach[r] = first[r] * red[r]; if (reach[r] == 0.0) reach[r] = red[r]; }
+    *converged = sc_cmp(first, abslimit, s);
+    for (it = 0; it < maxit; ++it) {
+      if (*converged) break;
+      memset(w.c[top], 0, sizeof(double) * len);
+      if ((rc = lmgc(&w, top))) goto done;
+      vadd(x, w.c[top], len); /* coarse-level x copies are not materialised */
+      orc_nrm2x(T, b, last);
+      if (hist) for (int r = 0; r < s; ++r) hist[(size_t)(it + 1) * s + r] = last[r];
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) { *converged = 1; ++it; break; }
+    }
+  }
+done:
+  for (int l = bl; l <= top; ++l) {
+    free(w.c[l]); free(w.t[l]); free(w.lu[l]);
+    if (l != top) free(w.b[l]);
+  }
+  free(w.c); free(w.t); free(w.b); free(w.lu); free(w.base_lu);
+  return rc ? rc : it;
+}

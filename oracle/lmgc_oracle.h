@@ -1,0 +1,80 @@
+/* lmgc_oracle: a plain-C, sequential restatement of UG 3.12.1's linear
+ * multigrid path (ls + lmgc with jac / gs / ilu smoothers, the standard
+ * transfer and the ex base solver) on a flattened hierarchy.
+ *
+ * TEST INFRASTRUCTURE ONLY.  It is the checker the CUDA path is compared
+ * against (tests/, __graft_entry__.smoke, and bench.py's CPU baseline leg);
+ * the ug_gb300 product never calls it.  Its own correctness is pinned
+ * against golden vectors produced by the UG reference itself
+ * (oracle/ug_export.cc -> tests/golden/).
+ *
+ * Layout: one level = block CSR in UG's VECTOR-list order, each row's
+ * MATRIX list in VSTART/MNEXT order (diagonal block first), blocks stored
+ * row-major (s*s doubles), plus the VCLASS / VNCLASS / VECSKIP fields and
+ * the standard-transfer weights to the next coarser level as a CSR over the
+ * fine vectors.  Every function is re-entrant (no global state), so
+ * independent solves may run concurrently on different threads. */
+#ifndef LMGC_ORACLE_H
+#define LMGC_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_S 8
+
+typedef struct {
+  int n;              /* block rows (VECTORs) */
+  int s;              /* block size (components per VECTOR) */
+  const int *rowptr;  /* n+1 */
+  const int *col;     /* nnzb, diagonal first in each row */
+  const double *val;  /* nnzb*s*s */
+  const int *vclass;  /* VCLASS per vector (ACTIVE_CLASS = 3, NEWDEF_CLASS = 2) */
+  const int *vnclass; /* VNCLASS per vector */
+  const int *skip;    /* VECSKIP bit mask per vector */
+  /* standard transfer from level-1 to this level; NULL on the coarsest */
+  const int *prowptr; /* n+1 */
+  const int *pcol;    /* coarse vector index */
+  const double *pw;   /* weight (1 for a corner copy, else shape function) */
+} orc_level;
+
+enum { ORC_JAC = 0, ORC_GS = 1, ORC_ILU = 2 };
+
+typedef struct {
+  int nlevels;            /* levels 0..nlevels-1 */
+  const orc_level *lev;
+  int baselevel;          /* lmgc $b */
+  int nu1, nu2, gamma;    /* lmgc $n1 $n2 $g */
+  int smoother;           /* ORC_JAC / ORC_GS / ORC_ILU, same for pre and post */
+  double damp[ORC_MAX_S]; /* smoother $damp */
+  double beta[ORC_MAX_S]; /* ilu $beta */
+  double cdamp[ORC_MAX_S];/* lmgc $damp (interpolation damping) */
+  /* the base solver is an `ls` ($m 1, $I ex): it does nothing when every
+   * component of the base-level defect is already below its abslimit
+   * (default ABS_LIMIT = 1e-10, np/procs/ls.cc:66, 389-391, 689) */
+  double base_abslimit[ORC_MAX_S];
+} orc_mg;
+
+/* ---- kernels (one level) ---- */
+void orc_matmul_minus(const orc_level *L, double *x, const double *y);          /* x -= A y */
+int orc_jac(const orc_level *L, double *v, const double *d);                      /* l_jac */
+int orc_lgs(const orc_level *L, double *v, const double *d);                      /* l_lgs */
+int orc_ilu_decomp(const orc_level *L, double *lu, const double *beta);           /* l_ilubthdecomp */
+int orc_luiter(const orc_level *L, const double *lu, double *v, const double *d); /* l_luiter */
+void orc_nrm2x(const orc_level *L, const double *x, double *out);                 /* dnrm2x */
+void orc_restrict(const orc_level *fine, const orc_level *coarse, double *to_coarse,
+                  const double *from_fine, const double *damp);                   /* StandardRestrict */
+void orc_interpolate(const orc_level *fine, double *to_fine, const double *from_coarse,
+                     const double *damp);                                         /* StandardInterpolateCorrection */
+
+/* ---- solver ----
+ * Solves A x = b on level top = nlevels-1 with ls + lmgc.  x (finest, n*s)
+ * is the start value and receives the solution; b is overwritten by the
+ * final defect.  hist (may be NULL) receives s*(maxit+1) defect norms.
+ * Returns the number of iterations, or a negative error code. */
+int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit,
+                 int maxit, double *hist, int *converged);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,207 @@
+"""ctypes front end of the C restatement of UG's lmgc path (lmgc_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker the CUDA path is compared against.
+The ug_gb300 product never imports this module.
+
+Also reads the UGFX container written by oracle/ug_export.cc (the UG
+reference driven as an oracle) into a dict of numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import struct
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "liblmgc_oracle.so")
+
+JAC, GS, ILU = 0, 1, 2
+SMOOTHERS = {"jac": JAC, "gs": GS, "ilu": ILU}
+MAX_S = 8
+
+
+def read_ugfx(path: str) -> dict:
+    """Parse the named-array container written by ug_export."""
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:6] != b"UGFX1\n":
+        raise ValueError(f"{path}: not a UGFX file")
+    p = 6
+    while p < len(data):
+        e = data.index(b"\0", p)
+        name = data[p:e].decode()
+        t = chr(data[e + 1])
+        (n,) = struct.unpack_from("<q", data, e + 2)
+        p = e + 10
+        if t == "d":
+            out[name] = np.frombuffer(data, np.float64, n, p).copy(); p += 8 * n
+        elif t == "i":
+            out[name] = np.frombuffer(data, np.int32, n, p).copy(); p += 4 * n
+        elif t == "s":
+            out[name] = data[p:p + n].decode(); p += n
+        else:
+            raise ValueError(f"bad record type {t!r}")
+    return out
+
+
+def build(quiet: bool = True) -> str:
+    """Compile liblmgc_oracle.so (plain C, no dependency on the reference)."""
+    cmd = ["make", "-C", HERE, "oracle_lib"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
+    return LIB_PATH
+
+
+class _Level(C.Structure):
+    _fields_ = [("n", C.c_int), ("s", C.c_int), ("rowptr", C.c_void_p), ("col", C.c_void_p),
+                ("val", C.c_void_p), ("vclass", C.c_void_p), ("vnclass", C.c_void_p),
+                ("skip", C.c_void_p), ("prowptr", C.c_void_p), ("pcol", C.c_void_p),
+                ("pw", C.c_void_p)]
+
+
+class _MG(C.Structure):
+    _fields_ = [("nlevels", C.c_int), ("lev", C.c_void_p), ("baselevel", C.c_int),
+                ("nu1", C.c_int), ("nu2", C.c_int), ("gamma", C.c_int), ("smoother", C.c_int),
+                ("damp", C.c_double * MAX_S), ("beta", C.c_double * MAX_S),
+                ("cdamp", C.c_double * MAX_S), ("base_abslimit", C.c_double * MAX_S)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.orc_matmul_minus.argtypes = [P, P, P]
+        L.orc_jac.argtypes = [P, P, P]
+        L.orc_lgs.argtypes = [P, P, P]
+        L.orc_ilu_decomp.argtypes = [P, P, P]
+        L.orc_luiter.argtypes = [P, P, P, P]
+        L.orc_nrm2x.argtypes = [P, P, P]
+        L.orc_restrict.argtypes = [P, P, P, P, P]
+        L.orc_interpolate.argtypes = [P, P, P, P]
+        L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve"):
+            getattr(L, f).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Hierarchy:
+    """Levels of a flattened multigrid hierarchy, as plain numpy arrays.
+
+    ``levels[l]`` is a dict with n, s, rowptr, col, val, vclass, vnclass, skip
+    and (l >= 1) prowptr, pcol, pw.  The C structs point into these arrays, so
+    the object keeps them alive."""
+
+    def __init__(self, levels: list[dict]):
+        self.levels = []
+        for L in levels:
+            d = {"n": int(L["n"]), "s": int(L["s"])}
+            for k in ("rowptr", "col", "vclass", "vnclass", "skip", "prowptr", "pcol"):
+                d[k] = None if L.get(k) is None else np.ascontiguousarray(L[k], np.int32)
+            for k in ("val", "pw"):
+                d[k] = None if L.get(k) is None else np.ascontiguousarray(L[k], np.float64)
+            self.levels.append(d)
+        self._c = (_Level * len(self.levels))()
+        for i, d in enumerate(self.levels):
+            self._c[i] = _Level(d["n"], d["s"], _p(d["rowptr"]), _p(d["col"]), _p(d["val"]),
+                                _p(d["vclass"]), _p(d["vnclass"]), _p(d["skip"]), _p(d["prowptr"]),
+                                _p(d["pcol"]), _p(d["pw"]))
+
+    @classmethod
+    def from_ugfx(cls, fx: dict) -> "Hierarchy":
+        s = int(fx["blocksize"][0])
+        levels = []
+        for l in range(int(fx["nlevels"][0])):
+            p = f"L{l}_"
+            L = {"n": int(fx[p + "n"][0]), "s": s, "rowptr": fx[p + "rowptr"], "col": fx[p + "col"],
+                 "val": fx[p + "val"], "vclass": fx[p + "vclass"], "vnclass": fx[p + "vnclass"],
+                 "skip": fx[p + "skip"]}
+            if l > 0:
+                q = f"P{l}_"
+                L.update(prowptr=fx[q + "rowptr"], pcol=fx[q + "col"], pw=fx[q + "w"])
+            levels.append(L)
+        return cls(levels)
+
+    def lev(self, l):
+        return C.byref(self._c[l])
+
+    # ---- kernels
+    def matmul_minus(self, l, x, y):
+        x = np.array(x, np.float64); y = np.ascontiguousarray(y, np.float64)
+        lib().orc_matmul_minus(self.lev(l), _p(x), _p(y)); return x
+
+    def jac(self, l, d):
+        v = np.zeros_like(d, dtype=np.float64); d = np.ascontiguousarray(d, np.float64)
+        rc = lib().orc_jac(self.lev(l), _p(v), _p(d)); assert rc == 0, rc; return v
+
+    def lgs(self, l, d):
+        v = np.zeros_like(d, dtype=np.float64); d = np.ascontiguousarray(d, np.float64)
+        rc = lib().orc_lgs(self.lev(l), _p(v), _p(d)); assert rc == 0, rc; return v
+
+    def ilu_decomp(self, l, beta=None):
+        L = self.levels[l]
+        lu = np.empty_like(L["val"])
+        b = None if beta is None else np.ascontiguousarray(np.resize(beta, MAX_S), np.float64)
+        rc = lib().orc_ilu_decomp(self.lev(l), _p(lu), _p(b)); assert rc == 0, rc; return lu
+
+    def luiter(self, l, lu, d):
+        v = np.zeros_like(d, dtype=np.float64); d = np.ascontiguousarray(d, np.float64)
+        lu = np.ascontiguousarray(lu, np.float64)
+        rc = lib().orc_luiter(self.lev(l), _p(lu), _p(v), _p(d)); assert rc == 0, rc; return v
+
+    def nrm2x(self, l, x):
+        out = np.zeros(MAX_S); x = np.ascontiguousarray(x, np.float64)
+        lib().orc_nrm2x(self.lev(l), _p(x), _p(out)); return out[: self.levels[l]["s"]]
+
+    def restrict(self, l, to_coarse, from_fine, damp=None):
+        to = np.array(to_coarse, np.float64); fr = np.ascontiguousarray(from_fine, np.float64)
+        dm = np.ones(MAX_S) if damp is None else np.resize(np.asarray(damp, np.float64), MAX_S)
+        lib().orc_restrict(self.lev(l), self.lev(l - 1), _p(to), _p(fr), _p(dm)); return to
+
+    def interpolate(self, l, from_coarse, damp=None):
+        L = self.levels[l]
+        to = np.zeros(L["n"] * L["s"]); fr = np.ascontiguousarray(from_coarse, np.float64)
+        dm = np.ones(MAX_S) if damp is None else np.resize(np.asarray(damp, np.float64), MAX_S)
+        lib().orc_interpolate(self.lev(l), _p(to), _p(fr), _p(dm)); return to
+
+    # ---- solver
+    def ls_solve(self, rhs, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None,
+                 beta=None, cdamp=None, red=1e-10, abslimit=1e-50, maxit=100, x0=None,
+                 base_abslimit=1e-10):
+        """ls + lmgc as configured by `npinit lmgc $n1 $n2 $g $b` and `npinit ls
+        $red $abslimit $m`.  Returns (x, iterations, converged, history)."""
+        top = len(self.levels) - 1
+        s = self.levels[top]["s"]
+        mg = _MG()
+        mg.nlevels = len(self.levels); mg.lev = C.addressof(self._c)
+        mg.baselevel, mg.nu1, mg.nu2, mg.gamma = baselevel, nu1, nu2, gamma
+        mg.smoother = SMOOTHERS[smoother] if isinstance(smoother, str) else smoother
+        for i in range(MAX_S):
+            mg.damp[i] = 1.0 if damp is None else float(np.resize(damp, MAX_S)[i])
+            mg.beta[i] = 0.0 if beta is None else float(np.resize(beta, MAX_S)[i])
+            mg.cdamp[i] = 1.0 if cdamp is None else float(np.resize(cdamp, MAX_S)[i])
+            mg.base_abslimit[i] = float(np.resize(base_abslimit, MAX_S)[i])
+        x = np.zeros(self.levels[top]["n"] * s) if x0 is None else np.array(x0, np.float64)
+        b = np.array(rhs, np.float64)
+        redv = np.resize(np.asarray(red, np.float64), MAX_S)
+        absv = np.resize(np.asarray(abslimit, np.float64), MAX_S)
+        hist = np.zeros((maxit + 1) * s)
+        conv = C.c_int(0)
+        it = lib().orc_ls_solve(C.byref(mg), _p(x), _p(b), _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
+        if it < 0:
+            raise RuntimeError(f"oracle ls failed: {it}")
+        return x, it, bool(conv.value), hist[: (it + 1) * s].reshape(it + 1, s)

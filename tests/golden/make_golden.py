@@ -1,0 +1,56 @@
+"""Regenerate the golden fixtures in this directory from the UG reference.
+
+Builds the reference with oracle/Makefile (needs the UG 3.12.1 sources at
+$REF, default /root/reference), runs oracle/_ref/ug_export{2d,3d} for each
+case below and stores every record as a compressed .npz.  Each fixture holds
+the hierarchy exactly as UG's grid manager and assembly produced it, the
+known-answer vectors of UG's kernels on the finest level, and UG's own ls +
+lmgc solve (iteration count, defect history, solution).
+
+    python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle  # noqa: E402
+
+# name: (dimension, problem, nref, baselevel, smoother, seed)
+CASES = {
+    "q1_jac": (2, "poisson", 5, 2, "jac", 11),
+    "q1_gs": (2, "poisson", 5, 2, "gs", 11),
+    "q1_ilu": (2, "poisson", 5, 2, "ilu", 11),
+    "p1_gs": (3, "poisson", 3, 0, "gs", 12),
+    "p1k_jac": (3, "diffusion", 3, 0, "jac", 13),
+    "p1k_gs": (3, "diffusion", 3, 0, "gs", 13),
+    "p1k_ilu": (3, "diffusion", 3, 0, "ilu", 13),
+    "el_jac": (2, "elasticity", 4, 1, "jac", 14),
+    "el_gs": (2, "elasticity", 4, 1, "gs", 14),
+    "el_ilu": (2, "elasticity", 4, 1, "ilu", 14),
+}
+
+
+def main():
+    env = dict(os.environ)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"], check=True, env=env)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (dim, problem, nref, base, sm, seed) in CASES.items():
+            exe = os.path.join(ROOT, "oracle", "_ref", f"ug_export{dim}d")
+            raw = os.path.join(tmp, name + ".bin")
+            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw], check=True,
+                           stdout=subprocess.DEVNULL)
+            fx = oracle.read_ugfx(raw)
+            arrays = {k: (np.array(v) if not isinstance(v, str) else np.array(v)) for k, v in fx.items()}
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+            print(f"{name}: levels={int(fx['nlevels'][0])} n_top={int(fx['L%d_n' % (int(fx['nlevels'][0]) - 1)][0])}"
+                  f" ug_iters={int(fx['ls_iters'][0])}")
+
+
+if __name__ == "__main__":
+    main()
