@@ -1,0 +1,342 @@
+"""Benchmark of the lmgc hot path on GB300.
+
+Workload (one step = one complete linear solve): 3D variable-coefficient
+diffusion -div(k grad u) = f, P1 tetrahedra on the unit cube, six Kuhn
+tetrahedra red-refined 6 times (65^3 = 274,625 unknowns, 4,018,753
+nonzeros), k = exp(g) per element with g a seeded Gaussian field
+(exponential covariance, correlation length 0.1, variance 1), seeded
+uniform[-1,1] right-hand side; ls + lmgc V(2,2) with multicolour
+Gauss-Seidel, base level 0, to 1e-8 relative defect.  Two precisions:
+plain FP64 and the FP32 V-cycle inside FP64 iterative refinement (the
+headline `value`).  Inputs are synthetic (seeded), generated on the host.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: the path does not shard (a single solve has no partition), so N
+ranks run independent replicas of the workload; value = all ranks' solves
+divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s to 1e-8 rel defect, mixed vs FP64 GPU; HBM GB/s; serve p50/p99 ms"
+NREF, SEED, CORR, VAR = 6, 2026, 0.1, 1.0
+RED = 1e-8
+
+
+def workload_config(extra=None):
+    c = {"workload": "3D P1 diffusion k=exp(g) (corr 0.1, var 1), unit cube 6 Kuhn tets red x6, "
+                     "65^3=274625 unknowns, lmgc V(2,2) multicolour GS, base level 0, ls to 1e-8 rel defect",
+         "unknowns": 274625, "nnz": 4018753, "levels": NREF + 1, "smoother": "gs (multicolour)",
+         "l2": "flushed between timed steps (256 MB write); the hierarchy itself (~60 MB FP64) fits in L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0])); mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the roofline kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch"):
+                return float(line.split("=")[1])
+    return None
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args):
+    """The reference's CPU implementation of the path on the host cores.
+
+    The UG reference itself cannot run here (its sources are not present on
+    this host, and it does not build for aarch64 from this tree), so the
+    oracle port -- the C restatement of UG's ls + lmgc, pinned bit-for-bit
+    to UG's kernels and solves -- runs the same workload, one independent
+    solve per host thread, each step a batch of concurrent solves."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import ctypes  # noqa: F401
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import ug_gb300 as G
+    oracle.build()
+    gen = G.Generator(G.Generator.DIFFUSION3D, NREF, seed=SEED, corr=CORR, var=VAR)
+    # UG's own order: the VECTOR list (lexicographic here), as l_lgs sweeps it
+    H = oracle.Hierarchy(gen.levels())
+    rhs = gen.rhs
+    threads = max(1, min(os.cpu_count() or 1, 16))
+
+    # warm-up: one complete solve gives the iteration count of the workload
+    t0 = time.perf_counter()
+    _, iters, conv, _ = H.ls_solve(rhs, smoother="gs", baselevel=0, red=RED)
+    t_full = time.perf_counter() - t0
+    # each timed step: `threads` concurrent solves of one ls iteration (defect,
+    # norm, one V-cycle), scaled by the iteration count of a complete solve
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        th = [threading.Thread(target=lambda: H.ls_solve(rhs, smoother="gs", baselevel=0, red=RED, maxit=1))
+              for _ in range(threads)]
+        [t.start() for t in th]
+        [t.join() for t in th]
+        times.append(time.perf_counter() - t0)
+    per_step = float(np.mean(times)) * iters  # one batch of `threads` complete solves
+    value = threads / per_step
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": workload_config({"iterations": iters}),
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{threads} concurrent FP64 solves (one per thread), each step one ls "
+                                       f"iteration of each, scaled by the {iters} iterations of a complete "
+                                       f"solve (single-thread complete solve: {t_full:.1f} s)"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    import ug_gb300 as G
+
+    gen = G.Generator(G.Generator.DIFFUSION3D, NREF, seed=SEED, corr=CORR, var=VAR)
+    mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True, autotune=True, device=local)
+    G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
+    mg.createvector("sol", "rhs", "rhs0")
+    G.setup_lmgc(mg, "gs", baselevel=0, red=RED, abslimit=1e-50, name="mgs64")
+    mg.npcreate("mgs32", "linear_solver.gls")
+    mg.npinit("mgs32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    top = mg.top
+    mg.upload("rhs0", top, gen.rhs)
+    mg.ls_preprocess("mgs64", top, "sol", "rhs")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def step(solver):
+        lr = G.LResult()
+        mg.dcopy(top, "rhs", "rhs0")
+        mg.dset(top, "sol", 0.0)
+        mg.ls_defect(solver, top, "sol", "rhs")
+        mg.ls_residuum(solver, 0, top, "sol", "rhs", lr)
+        mg.ls_solver(solver, top, "sol", "rhs", lr)
+        return lr
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    results = {}
+    for solver in ("mgs64", "mgs32"):
+        for _ in range(args.warmup):
+            step(solver)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        launches = 0
+        iters = []
+        with ClockSampler(local) as clk:
+            barrier(); torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(args.steps):
+                flush.zero_()
+                mg.launch_count(reset=True)
+                ev[k][0].record(stream)
+                lr = step(solver)
+                ev[k][1].record(stream)
+                launches += mg.launch_count()
+                iters.append(lr.iters)
+                assert lr.converged, f"{solver} did not converge"
+            torch.cuda.synchronize(); barrier()
+            wall = time.perf_counter() - t0
+        ms = [a.elapsed_time(b) for a, b in ev]
+        ms_step = float(np.mean(ms))
+        if world > 1:
+            t = torch.tensor([ms_step], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_step = float(t.item())
+        results[solver] = {"ms_per_step": ms_step, "iters": iters[-1], "launches_per_step": launches / args.steps,
+                           "clocks": clk.summary(), "wall_s": wall}
+
+    # end to end through the C ABI: host b -> solve -> host x, mixed precision
+    b_host = np.ascontiguousarray(gen.rhs)
+    x_host = np.empty_like(b_host)
+    lr = G.LResult()
+    mg.solve_host("mgs32", b_host, x_host)  # warm
+    torch.cuda.synchronize()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_(); torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mg.solve_host("mgs32", b_host, x_host)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = float(np.mean(e2e_t)) * 1e3
+
+    # roofline: finest-level dmatmul_minus (the defect / smoother-update pass), HBM-cold
+    n, s, nnz = mg.size(top)
+    mg.createvector("ry", "rx")
+    mg.createvector("ry32", "rx32", prec=G.FP32)
+    algo = {64: nnz * (8 + 4) + (n + 1) * 4 + 3 * n * 8, 32: nnz * (4 + 4) + (n + 1) * 4 + 3 * n * 4}
+    kms = {}
+    for bits, (x, y) in ((64, ("rx", "ry")), (32, ("rx32", "ry32"))):
+        ts = []
+        for k in range(20):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            mg.dmatmul_minus(top, x, y)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if k >= 3:
+                ts.append(a.elapsed_time(b))
+        kms[bits] = float(np.mean(ts))
+    peak, peak_kind = measured_peak()
+    ach32 = algo[32] / (kms[32] * 1e-3) / 1e9
+    ach64 = algo[64] / (kms[64] * 1e-3) / 1e9
+
+    # CPU baseline: the oracle port, one FP64 solve on one core, bounded sample
+    cpu = None
+    if rank == 0:
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build()
+            H = oracle.Hierarchy(gen.levels())
+            t0 = time.perf_counter()
+            _, it_cpu, conv, _ = H.ls_solve(gen.rhs, smoother="gs", baselevel=0, red=RED)
+            dt = time.perf_counter() - t0
+            cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                   "sample": f"one full FP64 solve of the workload in UG's list order ({it_cpu} iterations, {dt:.1f} s)"}
+        except Exception as e:  # reported, not fatal
+            cpu = {"value": None, "unit": "solves/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        r32, r64 = results["mgs32"], results["mgs64"]
+        value = world * 1e3 / r32["ms_per_step"]
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-in-f64 (mixed); f64 reported beside",
+            "data": "synthetic (seeded)",
+            "config": workload_config({"iterations_mixed": r32["iters"], "iterations_fp64": r64["iters"],
+                                       "parallelism": "replicas" if world > 1 else "1 GPU"}),
+            "fp64": {"value": world * 1e3 / r64["ms_per_step"], "unit": "solves/s", "ms_per_step": r64["ms_per_step"],
+                     "iterations": r64["iters"]},
+            "mixed_over_fp64": r64["ms_per_step"] / r32["ms_per_step"],
+            "e2e": {"value": world * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": int(n * s * 8),
+                    "d2h_bytes_per_step": int(n * s * 8), "ms_per_step": e2e_ms},
+            "roofline": {"bound": "hbm", "kernel": "spmv_minus_kernel<float> (finest level, HBM-cold)",
+                         "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
+                         "peak_kind": peak_kind, "traffic": profiled_traffic(),
+                         "algorithmic_bytes": algo[32], "launch_ms": kms[32],
+                         "fp64": {"achieved": ach64, "frac": ach64 / peak, "algorithmic_bytes": algo[64],
+                                  "launch_ms": kms[64]}},
+            "gpu_launches": int(r32["launches_per_step"] * args.steps),
+            "clocks": r32["clocks"],
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    mg.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * ug_gb300.h -- C ABI of the GB300 (sm_103a) implementation of UG's linear
+ * multigrid hot path: lmgc with the jac / gs / ilu smoothers, the standard
+ * grid transfer, the ex base solver and the ls outer iteration.
+ *
+ * The boundary mirrors UG 3.12.1's numproc plugin interface
+ * (np/udm/numproc.h, np/procs/iter.h, transfer.h, ls.h): a UG build adds
+ * numproc classes whose function pointers forward to the gmg_iter_* /
+ * gmg_transfer_* / gmg_ls_* entry points below, after flattening its
+ * VECTOR/MATRIX lists into gmg_level_desc arrays at every grid change.
+ *
+ * Conventions (those of the reference):
+ *   - every entry point returns 0 on success and nonzero on failure, never
+ *     aborts; gmg_last_error() describes the last failure of this thread;
+ *   - `result` out-parameters receive an error code as NP_RETURN does
+ *     (np/np.h:89); a failed decomposition reports -(row index+1);
+ *   - levels are numbered 0 (coarsest) .. nlevels-1 (finest);
+ *   - host arrays are in UG's VECTOR-list order; each MATRIX row lists the
+ *     diagonal block first (VSTART), then the off-diagonal blocks (MNEXT);
+ *     blocks are row-major s*s; vectors hold s components per VECTOR.
+ * All pointers are plain host pointers unless the name says _dev.
+ */
+#ifndef UG_GB300_H
+#define UG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GMG_MAX_S 8   /* largest block size (components per VECTOR) */
+
+typedef struct gmg_mg gmg_mg;   /* multigrid: device hierarchy + user data + numprocs (MULTIGRID) */
+typedef struct gmg_vec gmg_vec; /* vector data descriptor, one array per level (VECDATA_DESC) */
+typedef struct gmg_mat gmg_mat; /* matrix data descriptor (MATDATA_DESC) */
+typedef struct gmg_np gmg_np;   /* numproc object (NP_BASE and derived) */
+
+/* LRESULT, np/procs/ls.h:71-77 */
+typedef struct {
+  int error_code;
+  int converged;
+  double first_defect[GMG_MAX_S];
+  double last_defect[GMG_MAX_S];
+  int number_of_linear_iterations;
+} gmg_lresult;
+
+/* One level of the flattened hierarchy (host arrays, UG VECTOR-list order).
+ * Produced from VSTART/MNEXT/MDEST/MVALUE (gm/gm.h:601-672), VCLASS/VNCLASS
+ * (gm.h:2200-2207), VECSKIP (gm.h:2286) and the standard transfer weights
+ * (corner node -> father copy with weight 1, other nodes -> father element
+ * corners with the shape functions GNs at LCVECT, np/algebra/transgrid.cc:117). */
+typedef struct {
+  int n;               /* VECTORs on the level */
+  int s;               /* components per VECTOR (block size), 1..GMG_MAX_S */
+  const int *rowptr;   /* n+1 */
+  const int *col;      /* rowptr[n] block column indices, diagonal first in each row */
+  const double *val;   /* rowptr[n]*s*s values */
+  const int *vclass;   /* n, or NULL for all 3 (ACTIVE_CLASS) */
+  const int *vnclass;  /* n, or NULL for all 3 */
+  const int *skip;     /* n VECSKIP masks, or NULL for none */
+  const int *prowptr;  /* standard transfer from level-1: n+1 (NULL on level 0) */
+  const int *pcol;     /* coarse VECTOR index per weight */
+  const double *pw;    /* weight */
+} gmg_level_desc;
+
+/* processing order of every level (the `order` numproc, np/procs/order.cc) */
+#define GMG_ORDER_LIST 0  /* UG's VECTOR-list order: gs / ilu reproduce l_lgs / l_luiter */
+#define GMG_ORDER_COLOR 1 /* multicolour order (greedy colouring of the matrix graph) */
+
+#define GMG_PREC_FP64 0
+#define GMG_PREC_FP32 1
+
+typedef struct {
+  int order;        /* GMG_ORDER_* */
+  int fp32_copy;    /* also keep FP32 copies of matrices/transfers (mixed precision) */
+  int autotune;     /* time SpMV variants per level at creation and keep the fastest */
+  int device;       /* CUDA device ordinal */
+} gmg_mg_opts;
+
+/* ---------------------------------------------------------------- setup */
+/* Flattened hierarchy -> device (a grid change: AdaptMultiGrid, gm/refine.cc:6482,
+ * followed by assembly).  Creates the system matrix descriptor "MAT". */
+int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *opts, gmg_mg **out);
+int gmg_mg_destroy(gmg_mg *mg);
+/* Runs all of mg's work on this CUDA stream (cudaStream_t; NULL = legacy default). */
+int gmg_mg_set_stream(gmg_mg *mg, void *stream);
+int gmg_mg_nlevels(const gmg_mg *mg);
+int gmg_mg_level_size(const gmg_mg *mg, int level, int *n, int *s, long long *nnzb);
+/* perm[i] = UG list position of the VECTOR processed i-th on this level */
+int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm);
+/* The matrix as stored on the device, in processing order (for checking). */
+int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val);
+/* Number of multicolour classes (wavefronts of the gs/ilu schedule) on a level. */
+int gmg_mg_num_waves(const gmg_mg *mg, int level);
+/* Device bytes held by the hierarchy. */
+long long gmg_mg_device_bytes(const gmg_mg *mg);
+/* Kernel launches issued by mg since creation (or the last reset). */
+long long gmg_mg_launch_count(const gmg_mg *mg, int reset);
+const char *gmg_last_error(void);
+/* Synchronise mg's stream; returns nonzero if a kernel failed. */
+int gmg_mg_sync(gmg_mg *mg);
+
+/* ------------------------------------------------ user data (udm.h) */
+/* createvector: one array per level, GMG_PREC_FP64 or GMG_PREC_FP32 */
+int gmg_vec_create(gmg_mg *mg, const char *name, int precision, gmg_vec **out);
+gmg_vec *gmg_vec_by_name(gmg_mg *mg, const char *name);
+gmg_mat *gmg_mat_by_name(gmg_mg *mg, const char *name);
+/* host (UG list order, n*s doubles) <-> device, on mg's stream, synchronous */
+int gmg_vec_upload(gmg_vec *v, int level, const double *host);
+int gmg_vec_download(gmg_vec *v, int level, double *host);
+/* device array of a level (processing order) */
+int gmg_vec_device_ptr(gmg_vec *v, int level, void **ptr_dev);
+
+/* ------------------------------------------------ numprocs (numproc.h) */
+/* npcreate <objname> $c <classname>; classes: "iter.gjac", "iter.ggs",
+ * "iter.gilu", "iter.glmgc", "iter.gex", "transfer.gtransfer", "linear_solver.gls" */
+int gmg_np_create(gmg_mg *mg, const char *objname, const char *classname);
+/* npinit <objname> <args>, e.g. "$damp 0.8", "$S pre post base $T transfer $n1 2 $n2 2 $b 2";
+ * returns NP_EXECUTABLE (3), NP_ACTIVE (2) or NP_NOT_ACTIVE (1) in *status (numproc.h:54-57) */
+int gmg_np_init(gmg_mg *mg, const char *objname, const char *args, int *status);
+/* npexecute <objname> <args> ("$i $d $r $s $p") on the current (finest) level */
+int gmg_np_execute(gmg_mg *mg, const char *objname, const char *args);
+gmg_np *gmg_np_by_name(gmg_mg *mg, const char *objname);
+/* Display: writes the configuration (as `npdisplay`) into buf */
+int gmg_np_display(gmg_np *np, char *buf, int buflen);
+
+/* NP_ITER (np/procs/iter.h:68-101). Iter: c <- correction, b <- b - A c. */
+int gmg_iter_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result);
+int gmg_iter_iter(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result);
+int gmg_iter_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+
+/* NP_TRANSFER (np/procs/transfer.h:79-166) */
+int gmg_transfer_preprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+int gmg_transfer_restrict_defect(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A,
+                                 const double *damp, int *result);
+int gmg_transfer_interpolate_correction(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A,
+                                        const double *damp, int *result);
+int gmg_transfer_postprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+
+/* NP_LINEAR_SOLVER (np/procs/ls.h:79-132); Solver takes (abslimit, reduction)
+ * in the order of np/procs/ls.cc:637. */
+int gmg_ls_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result);
+int gmg_ls_defect(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+int gmg_ls_residuum(gmg_np *np, int fromlevel, int tolevel, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr);
+int gmg_ls_solver(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
+                  const double *reduction, gmg_lresult *lr);
+int gmg_ls_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+
+/* ------------------------------------------------ level kernels (ugblas.cc, ugiter.cc, transgrid.cc) */
+int gmg_dset(gmg_mg *mg, int level, gmg_vec *x, double a);                              /* dset 2291 */
+int gmg_dcopy(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y);                            /* dcopy: x = y */
+int gmg_dadd(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y);                             /* dadd 2586: x += y */
+int gmg_dmatmul_minus(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *A, gmg_vec *y);        /* 3997: x -= A y */
+int gmg_dnrm2x(gmg_mg *mg, int level, gmg_vec *x, double *norms);                        /* 3156 */
+int gmg_l_jac(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);                /* ugiter.cc:271 */
+int gmg_l_lgs(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);                /* ugiter.cc:412 */
+int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *M, const double *beta);            /* ugiter.cc:2252 */
+int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);             /* ugiter.cc:4444 */
+int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp);            /* 462 */
+int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp); /* 529 */
+
+/* ------------------------------------------------ one-call solve from host buffers */
+/* Uploads b (finest level, list order), runs ls `solver` ($i $d $r $s $p, with the x/b
+ * given to npinit), downloads x. */
+int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double *x_host, gmg_lresult *lr);
+
+/* ------------------------------------------------ structured hierarchies */
+/* Builds, on the host, the hierarchy UG's grid manager produces for the
+ * unit square (one Q1 quad) / unit cube (six Kuhn tets) refined `nref` times
+ * with `mark $a; refine`, assembled as in the workloads:
+ *   kind 0: 2D Q1 Poisson;   kind 1: 3D P1 diffusion, k = exp(g) per element
+ *   (exponential covariance, correlation `corr`, variance `var`; var=0 gives k=1);
+ *   kind 2: 2D P1 plane-strain elasticity (E=1, nu=0.3) on two triangles, 2x2 blocks.
+ * Homogeneous Dirichlet boundary (unit rows, VECSKIP); the right-hand side is
+ * uniform[-1,1] keyed by lattice position and `seed`, scaled by h^dim.
+ * Node order per level: lexicographic.  The generator owns all arrays. */
+typedef struct gmg_gen gmg_gen;
+int gmg_gen_create(int kind, int nref, unsigned long long seed, double corr, double var, gmg_gen **out);
+int gmg_gen_levels(gmg_gen *g, const gmg_level_desc **levels, int *nlevels);
+int gmg_gen_rhs(gmg_gen *g, const double **rhs, int *len);
+int gmg_gen_coords(gmg_gen *g, int level, const double **xyz);
+int gmg_gen_destroy(gmg_gen *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UG_GB300_H */

@@ -30,3 +30,33 @@ def oracle_mod():
     import oracle
     oracle.build()
     return oracle
+
+
+def permuted_levels(levels, mg):
+    """The hierarchy as the device processes it (processing order of every
+    level), as plain arrays for the oracle: rows, columns, transfer rows and
+    transfer columns renumbered by mg.order(level)."""
+    out = []
+    inv_prev = None
+    for l, d in enumerate(levels):
+        perm = mg.order(l)
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(len(perm), dtype=perm.dtype)
+        rp, col, val = mg.matrix(l)
+        e = {"n": d["n"], "s": d["s"], "rowptr": rp, "col": col, "val": val,
+             "vclass": np.asarray(d["vclass"])[perm], "vnclass": np.asarray(d["vnclass"])[perm],
+             "skip": np.asarray(d["skip"])[perm]}
+        if l > 0:
+            prp, pcol, pw = np.asarray(d["prowptr"]), np.asarray(d["pcol"]), np.asarray(d["pw"])
+            rows = [np.arange(prp[o], prp[o + 1]) for o in perm]
+            newrp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+            idx = np.concatenate(rows) if rows else np.zeros(0, int)
+            e.update(prowptr=newrp, pcol=inv_prev[pcol[idx]].astype(np.int32), pw=pw[idx])
+        out.append(e)
+        inv_prev = inv
+    return out
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64); b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))

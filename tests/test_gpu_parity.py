@@ -1,0 +1,193 @@
+"""GPU parity of the lmgc path against the UG reference and its C restatement.
+
+* Kernels: every level kernel called through the C ABI on UG's own hierarchies
+  (tests/golden) reproduces UG's known-answer vectors; tolerance 1e-12
+  relative (FP64; only the summation order inside a row differs).
+* Solves: ls + lmgc with jac / gs / ilu in UG's VECTOR-list order takes UG's
+  iteration count and reaches UG's solution (jac 1e-10, gs / ilu 1e-8
+  relative, iterations +-1 allowed by the contract, equal in practice);
+  in multicolour order it matches the oracle run on the same (reordered)
+  hierarchy.
+* Mixed precision: an FP32 V-cycle inside FP64 iterative refinement meets
+  the FP64 stopping test; its error against a tightly converged FP64 oracle
+  solution is bounded by 1e-6 relative.
+* Full-size workloads: the 2D Q1 257x257 and 3D P1 65^3 hierarchies.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, permuted_levels, rel
+
+pytestmark = pytest.mark.gpu
+NAMES = golden_names()
+
+
+@pytest.fixture(scope="module")
+def G():
+    import ug_gb300
+    ug_gb300.lib()
+    return ug_gb300
+
+
+def _setup(G, fx, order=0, fp32=False):
+    levels = G.levels_from_ugfx(fx)
+    mg = G.MultiGrid(levels, order=order, fp32=fp32)
+    return mg, levels
+
+
+def _damp(sm):
+    return 0.8 if sm == "jac" else 1.0
+
+
+@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("name", NAMES)
+def test_kernels_match_ug(G, oracle_mod, name, order):
+    fx = load_golden(name)
+    mg, levels = _setup(G, fx, order)
+    top = mg.top
+    mg.createvector("x", "y", "d", "v", "c", "t")
+    mg.upload("x", top, fx["kat_x"]); mg.upload("y", top, fx["kat_y"])
+    mg.dmatmul_minus(top, "x", "y")
+    assert rel(mg.download("x", top), fx["kat_matmul"]) <= 1e-12
+    mg.upload("d", top, fx["kat_d"])
+    mg.l_jac(top, "v", "d")
+    assert rel(mg.download("v", top), fx["kat_jac"]) <= 1e-12
+    assert rel(mg.dnrm2x(top, "d"), fx["kat_nrm"]) <= 1e-12
+    mg.upload("c", top - 1, fx["kat_restrict_pre"])
+    mg.standard_restrict(top, "c", "d")
+    assert rel(mg.download("c", top - 1), fx["kat_restrict"]) <= 1e-12
+    mg.upload("c", top - 1, fx["kat_interp_coarse"])
+    mg.upload("t", top, np.full(fx["kat_d"].size, 7.0))
+    mg.standard_interpolate_correction(top, "t", "c")
+    assert rel(mg.download("t", top), fx["kat_interp"]) <= 1e-12
+    mg.l_lgs(top, "v", "d")
+    gs = mg.download("v", top)
+    mg.l_ilu_decomp(top)
+    mg.l_luiter(top, "v", "d")
+    ilu = mg.download("v", top)
+    if order == 0:  # UG's own list order: UG's numbers
+        assert rel(gs, fx["kat_gs"]) <= 1e-12
+        assert rel(ilu, fx["kat_ilu"]) <= 1e-12
+    else:  # multicolour order: the reference algorithm on the reordered grid
+        H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+        perm = mg.order(top)
+        s = levels[top]["s"]
+        d_p = fx["kat_d"].reshape(-1, s)[perm].ravel()
+        ref_gs = np.empty((len(perm), s)); ref_gs[perm] = H.lgs(top, d_p).reshape(-1, s)
+        assert rel(gs, ref_gs.ravel()) <= 1e-12
+        lu = H.ilu_decomp(top)
+        ref_ilu = np.empty((len(perm), s)); ref_ilu[perm] = H.luiter(top, lu, d_p).reshape(-1, s)
+        assert rel(ilu, ref_ilu.ravel()) <= 1e-12
+    mg.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_solve_matches_ug(G, name):
+    fx = load_golden(name)
+    mg, _ = _setup(G, fx, 0)
+    sm = fx["smoother"]
+    G.setup_lmgc(mg, sm, baselevel=int(fx["baselevel"][0]), damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    x, lr = mg.solve_host("mgs", fx["rhs"])
+    it_ug = int(fx["ls_iters"][0])
+    assert lr.converged
+    assert abs(lr.first_defect[0] - fx["ls_hist"][0]) <= 1e-12 * fx["ls_hist"][0]
+    if sm == "jac":
+        assert lr.iters == it_ug
+        assert rel(x, fx["ls_x"]) <= 1e-10
+    else:
+        assert abs(lr.iters - it_ug) <= 1
+        assert rel(x, fx["ls_x"]) <= 1e-8
+    # a second solve on the same device state is bitwise reproducible
+    x2, lr2 = mg.solve_host("mgs", fx["rhs"])
+    assert lr2.iters == lr.iters and np.array_equal(x, x2)
+    mg.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_solve_multicolour_matches_oracle(G, oracle_mod, name):
+    fx = load_golden(name)
+    mg, levels = _setup(G, fx, 1)
+    sm = fx["smoother"]
+    bl = int(fx["baselevel"][0])
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    x, lr = mg.solve_host("mgs", fx["rhs"])
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    top = mg.top
+    perm = mg.order(top)
+    s = levels[top]["s"]
+    xo, ito, conv, _ = H.ls_solve(fx["rhs"].reshape(-1, s)[perm].ravel(), smoother=sm, baselevel=bl,
+                                  damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    xr = np.empty((len(perm), s)); xr[perm] = xo.reshape(-1, s)
+    assert conv and lr.converged and lr.iters == ito
+    assert rel(x, xr.ravel()) <= 1e-10
+    mg.close()
+
+
+@pytest.mark.parametrize("name", ["q1_jac", "p1k_gs", "el_ilu", "q1_ilu"])
+def test_mixed_precision_refinement(G, oracle_mod, name):
+    fx = load_golden(name)
+    mg, levels = _setup(G, fx, 0, fp32=True)
+    sm = fx["smoother"]
+    bl = int(fx["baselevel"][0])
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-8, abslimit=1e-50, mixed=True)
+    x, lr = mg.solve_host("mgs", fx["rhs"])
+    assert lr.converged
+    H = oracle_mod.Hierarchy(levels)
+    top = mg.top
+    # the FP64 defect of the mixed solution meets the stopping test
+    d = H.matmul_minus(top, fx["rhs"], x)
+    d0 = H.nrm2x(top, fx["rhs"])
+    assert np.all(H.nrm2x(top, d) <= 1.01e-8 * d0)
+    xo, ito, _, _ = H.ls_solve(fx["rhs"], smoother=sm, baselevel=bl, damp=_damp(sm), red=1e-13, abslimit=1e-50)
+    assert rel(x, xo) <= 1e-6
+    mg.close()
+
+
+def test_numproc_status_and_errors(G):
+    fx = load_golden("q1_jac")
+    mg, _ = _setup(G, fx, 0)
+    mg.createvector("sol", "rhs")
+    mg.npcreate("lmgc", "iter.glmgc")
+    assert mg.npinit("lmgc", "$n1 2") == G.NP_NOT_ACTIVE          # no $S / $T
+    mg.npcreate("ls", "linear_solver.gls")
+    assert mg.npinit("ls", "$m 5") == G.NP_NOT_ACTIVE             # no $I
+    with pytest.raises(G.GmgError):
+        mg.npcreate("bad", "iter.nosuchclass")
+    with pytest.raises(G.GmgError):
+        mg.npexecute("lmgc", "$s")                                  # not executable
+    G.setup_lmgc(mg, "jac", baselevel=2)
+    assert "n1 = 2" in mg.npdisplay("lmgc") and "baselevel = 2" in mg.npdisplay("lmgc")
+    mg.upload("rhs", mg.top, fx["rhs"])
+    mg.npexecute("mgs", "$i $d $r $s $p")
+    assert rel(mg.download("sol", mg.top), fx["ls_x"]) <= 1e-10
+    mg.close()
+
+
+def test_full_size_q1_jacobi(G, oracle_mod):
+    """2D Q1 Poisson 257x257 (66,049 unknowns), V(2,2) jac 0.8, base 4x4, red 1e-10."""
+    gen = G.Generator(0, 8, seed=1)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels)
+    G.setup_lmgc(mg, "jac", baselevel=2, red=1e-10)
+    x, lr = mg.solve_host("mgs", gen.rhs)
+    H = oracle_mod.Hierarchy(levels)
+    xo, ito, conv, _ = H.ls_solve(gen.rhs, smoother="jac", baselevel=2, damp=0.8, red=1e-10)
+    assert lr.converged and conv and lr.iters == ito
+    assert rel(x, xo) <= 1e-10
+    mg.close()
+
+
+def test_full_size_p1_diffusion_gs(G, oracle_mod):
+    """3D P1 diffusion 65^3 (274,625 unknowns), k = exp(g), multicolour GS V(2,2), red 1e-8."""
+    gen = G.Generator(1, 6, seed=2, corr=0.1, var=1.0)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=G.ORDER_COLOR)
+    G.setup_lmgc(mg, "gs", baselevel=0, red=1e-8)
+    x, lr = mg.solve_host("mgs", gen.rhs)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    perm = mg.order(mg.top)
+    xo, ito, conv, _ = H.ls_solve(gen.rhs[perm], smoother="gs", baselevel=0, red=1e-8)
+    xr = np.empty_like(xo); xr[perm] = xo
+    assert lr.converged and conv and lr.iters == ito
+    assert rel(x, xr) <= 1e-10
+    mg.close()

@@ -1,0 +1,492 @@
+"""ug_gb300: UG's linear multigrid hot path (lmgc with jac / gs / ilu, the
+standard transfer, ex and ls) as hand-written CUDA for GB300 (sm_103a).
+
+This module is the host-side mirror of UG's numproc interface over the C ABI
+in include/ug_gb300.h (libug_gb300.so, built in tree by ug_gb300/build.py):
+a ``MultiGrid`` holds the device-resident hierarchy, its vectors ("createvector")
+and numproc objects ("npcreate" / "npinit" / "npexecute"), with the same
+class roles, argument syntax and error behaviour as UG 3.12.1:
+
+    mg = MultiGrid(levels)                   # flattened hierarchy (grid change)
+    mg.createvector("sol", "rhs")
+    mg.npcreate("transfer", "transfer.gtransfer"); mg.npinit("transfer", "")
+    mg.npcreate("smooth", "iter.gjac");     mg.npinit("smooth", "$damp 0.8")
+    ...
+    mg.npexecute("mgs", "$i $d $r $s $p")
+
+There is no CPU fallback: without the library or a CUDA device every call
+that needs the GPU raises GmgError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["GmgError", "Generator", "MultiGrid", "LResult", "lib", "LIB_PATH",
+           "ORDER_LIST", "ORDER_COLOR", "FP64", "FP32"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libug_gb300.so")
+MAX_S = 8
+ORDER_LIST, ORDER_COLOR = 0, 1
+FP64, FP32 = 0, 1
+NP_NOT_INIT, NP_NOT_ACTIVE, NP_ACTIVE, NP_EXECUTABLE = 0, 1, 2, 3
+
+
+class GmgError(RuntimeError):
+    pass
+
+
+class LevelDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("s", C.c_int), ("rowptr", C.c_void_p), ("col", C.c_void_p),
+                ("val", C.c_void_p), ("vclass", C.c_void_p), ("vnclass", C.c_void_p), ("skip", C.c_void_p),
+                ("prowptr", C.c_void_p), ("pcol", C.c_void_p), ("pw", C.c_void_p)]
+
+
+class MgOpts(C.Structure):
+    _fields_ = [("order", C.c_int), ("fp32_copy", C.c_int), ("autotune", C.c_int), ("device", C.c_int)]
+
+
+class LResult(C.Structure):
+    """LRESULT (np/procs/ls.h:71-77)."""
+    _fields_ = [("error_code", C.c_int), ("converged", C.c_int), ("first_defect", C.c_double * MAX_S),
+                ("last_defect", C.c_double * MAX_S), ("number_of_linear_iterations", C.c_int)]
+
+    @property
+    def iters(self):
+        return self.number_of_linear_iterations
+
+
+_lib = None
+
+
+def lib(build_if_missing: bool = True):
+    """Load libug_gb300.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise GmgError(f"{LIB_PATH} is missing: run python -m ug_gb300.build")
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(LIB_PATH)
+    P, I, D, LL = C.c_void_p, C.c_int, C.c_double, C.c_longlong
+    sig = {
+        "gmg_last_error": ([], C.c_char_p),
+        "gmg_mg_create": ([P, I, P, P], I), "gmg_mg_destroy": ([P], I), "gmg_mg_set_stream": ([P, P], I),
+        "gmg_mg_nlevels": ([P], I), "gmg_mg_level_size": ([P, I, P, P, P], I), "gmg_mg_get_order": ([P, I, P], I),
+        "gmg_mg_get_matrix": ([P, I, P, P, P], I), "gmg_mg_num_waves": ([P, I], I),
+        "gmg_mg_device_bytes": ([P], LL), "gmg_mg_launch_count": ([P, I], LL), "gmg_mg_sync": ([P], I),
+        "gmg_vec_create": ([P, C.c_char_p, I, P], I), "gmg_vec_by_name": ([P, C.c_char_p], P),
+        "gmg_mat_by_name": ([P, C.c_char_p], P), "gmg_vec_upload": ([P, I, P], I),
+        "gmg_vec_download": ([P, I, P], I), "gmg_vec_device_ptr": ([P, I, P], I),
+        "gmg_np_create": ([P, C.c_char_p, C.c_char_p], I), "gmg_np_init": ([P, C.c_char_p, C.c_char_p, P], I),
+        "gmg_np_execute": ([P, C.c_char_p, C.c_char_p], I), "gmg_np_by_name": ([P, C.c_char_p], P),
+        "gmg_np_display": ([P, C.c_char_p, I], I),
+        "gmg_iter_preprocess": ([P, I, P, P, P, P, P], I), "gmg_iter_iter": ([P, I, P, P, P, P], I),
+        "gmg_iter_postprocess": ([P, I, P, P, P, P], I),
+        "gmg_transfer_preprocess": ([P, P, I, P, P, P, P], I),
+        "gmg_transfer_restrict_defect": ([P, I, P, P, P, P, P], I),
+        "gmg_transfer_interpolate_correction": ([P, I, P, P, P, P, P], I),
+        "gmg_transfer_postprocess": ([P, P, I, P, P, P, P], I),
+        "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
+        "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
+        "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
+        "gmg_dset": ([P, I, P, D], I), "gmg_dcopy": ([P, I, P, P], I), "gmg_dadd": ([P, I, P, P], I),
+        "gmg_dmatmul_minus": ([P, I, P, P, P], I), "gmg_dnrm2x": ([P, I, P, P], I),
+        "gmg_l_jac": ([P, I, P, P, P], I), "gmg_l_lgs": ([P, I, P, P, P], I),
+        "gmg_l_ilu_decomp": ([P, I, P, P], I), "gmg_l_luiter": ([P, I, P, P, P], I),
+        "gmg_standard_restrict": ([P, I, P, P, P], I), "gmg_standard_interpolate_correction": ([P, I, P, P, P], I),
+        "gmg_solve_host": ([P, C.c_char_p, P, P, P], I),
+        "gmg_gen_create": ([I, I, C.c_ulonglong, D, D, P], I), "gmg_gen_levels": ([P, P, P], I),
+        "gmg_gen_rhs": ([P, P, P], I), "gmg_gen_coords": ([P, I, P], I), "gmg_gen_destroy": ([P], I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _err(what: str):
+    msg = lib().gmg_last_error()
+    raise GmgError(f"{what}: {msg.decode() if msg else 'failed'}")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _sc(v, default=1.0):
+    a = np.full(MAX_S, default, np.float64)
+    if v is not None:
+        v = np.atleast_1d(np.asarray(v, np.float64))
+        a[:] = np.resize(v, MAX_S)
+    return a
+
+
+class Generator:
+    """Structured hierarchy of a workload, built on the host (no GPU needed).
+
+    kind 0: 2D Q1 Poisson on the unit square (one quad refined nref times);
+    kind 1: 3D P1 diffusion on the unit cube (six Kuhn tets refined nref
+    times), k = exp(g) with correlation ``corr`` and variance ``var``;
+    kind 2: 2D P1 plane-strain elasticity, 2x2 blocks."""
+
+    POISSON2D, DIFFUSION3D, ELASTICITY2D = 0, 1, 2
+
+    def __init__(self, kind: int, nref: int, seed: int = 1, corr: float = 0.1, var: float = 0.0):
+        L = lib()
+        h = C.c_void_p()
+        if L.gmg_gen_create(kind, nref, seed, corr, var, C.byref(h)):
+            _err("gmg_gen_create")
+        self._h = h
+        self.kind, self.nref = kind, nref
+        lev = C.POINTER(LevelDesc)()
+        nl = C.c_int()
+        L.gmg_gen_levels(h, C.byref(lev), C.byref(nl))
+        self._desc = lev
+        self.nlevels = nl.value
+        rp = C.POINTER(C.c_double)()
+        ln = C.c_int()
+        L.gmg_gen_rhs(h, C.byref(rp), C.byref(ln))
+        self.rhs = np.ctypeslib.as_array(rp, (ln.value,)).copy()
+
+    def level(self, l: int) -> dict:
+        """Numpy copies of one level's arrays (UG list order)."""
+        d = self._desc[l]
+        n, s = d.n, d.s
+
+        def arr(p, cnt, ct):
+            return np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), (cnt,)).copy() if p and cnt else None
+
+        rowptr = arr(d.rowptr, n + 1, C.c_int)
+        nnz = int(rowptr[-1])
+        out = {"n": n, "s": s, "rowptr": rowptr, "col": arr(d.col, nnz, C.c_int),
+               "val": arr(d.val, nnz * s * s, C.c_double), "vclass": arr(d.vclass, n, C.c_int),
+               "vnclass": arr(d.vnclass, n, C.c_int), "skip": arr(d.skip, n, C.c_int)}
+        if l > 0:
+            prow = arr(d.prowptr, n + 1, C.c_int)
+            out.update(prowptr=prow, pcol=arr(d.pcol, int(prow[-1]), C.c_int), pw=arr(d.pw, int(prow[-1]), C.c_double))
+        xp = C.POINTER(C.c_double)()
+        lib().gmg_gen_coords(self._h, l, C.byref(xp))
+        out["xyz"] = np.ctypeslib.as_array(xp, (n * 3,)).copy().reshape(n, 3)
+        return out
+
+    def levels(self):
+        return [self.level(l) for l in range(self.nlevels)]
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.gmg_gen_destroy(self._h)
+            self._h = None
+
+
+def levels_from_ugfx(fx: dict) -> list[dict]:
+    """Level dicts from an exported UG hierarchy (golden fixture)."""
+    s = int(np.asarray(fx["blocksize"]).ravel()[0])
+    out = []
+    for l in range(int(np.asarray(fx["nlevels"]).ravel()[0])):
+        p = f"L{l}_"
+        d = {"n": int(np.asarray(fx[p + "n"]).ravel()[0]), "s": s, "rowptr": fx[p + "rowptr"], "col": fx[p + "col"],
+             "val": fx[p + "val"], "vclass": fx[p + "vclass"], "vnclass": fx[p + "vnclass"], "skip": fx[p + "skip"]}
+        if l > 0:
+            q = f"P{l}_"
+            d.update(prowptr=fx[q + "rowptr"], pcol=fx[q + "col"], pw=fx[q + "w"])
+        out.append(d)
+    return out
+
+
+class MultiGrid:
+    """Device-resident multigrid hierarchy with UG-style user data and numprocs."""
+
+    def __init__(self, levels, order: int = ORDER_LIST, fp32: bool = False, autotune: bool = False, device: int = 0):
+        L = lib()
+        if isinstance(levels, Generator):
+            desc_arr = levels._desc
+            nl = levels.nlevels
+            self._keep = [levels]
+        else:
+            nl = len(levels)
+            desc_arr = (LevelDesc * nl)()
+            self._keep = []
+            for i, d in enumerate(levels):
+                ints = {k: (None if d.get(k) is None else np.ascontiguousarray(d[k], np.int32))
+                        for k in ("rowptr", "col", "vclass", "vnclass", "skip", "prowptr", "pcol")}
+                dbl = {k: (None if d.get(k) is None else np.ascontiguousarray(d[k], np.float64)) for k in ("val", "pw")}
+                self._keep += list(ints.values()) + list(dbl.values())
+                desc_arr[i] = LevelDesc(int(d["n"]), int(d["s"]), _ptr(ints["rowptr"]), _ptr(ints["col"]),
+                                        _ptr(dbl["val"]), _ptr(ints["vclass"]), _ptr(ints["vnclass"]),
+                                        _ptr(ints["skip"]), _ptr(ints["prowptr"]), _ptr(ints["pcol"]),
+                                        _ptr(dbl["pw"]))
+        opts = MgOpts(order, int(fp32), int(autotune), device)
+        h = C.c_void_p()
+        if L.gmg_mg_create(C.cast(desc_arr, C.c_void_p), nl, C.byref(opts), C.byref(h)):
+            _err("gmg_mg_create")
+        self._h = h
+        self.nlevels = nl
+        self.top = nl - 1
+        self._keep = None  # the device holds its own copies
+
+    # ---- hierarchy
+    def size(self, level: int):
+        n, s, nnz = C.c_int(), C.c_int(), C.c_longlong()
+        if lib().gmg_mg_level_size(self._h, level, C.byref(n), C.byref(s), C.byref(nnz)):
+            _err("gmg_mg_level_size")
+        return n.value, s.value, nnz.value
+
+    def order(self, level: int) -> np.ndarray:
+        n, _, _ = self.size(level)
+        p = np.empty(n, np.int32)
+        lib().gmg_mg_get_order(self._h, level, _ptr(p))
+        return p
+
+    def matrix(self, level: int):
+        n, s, nnz = self.size(level)
+        rp, col, val = np.empty(n + 1, np.int32), np.empty(nnz, np.int32), np.empty(nnz * s * s)
+        lib().gmg_mg_get_matrix(self._h, level, _ptr(rp), _ptr(col), _ptr(val))
+        return rp, col, val
+
+    def num_waves(self, level: int) -> int:
+        return lib().gmg_mg_num_waves(self._h, level)
+
+    def device_bytes(self) -> int:
+        return lib().gmg_mg_device_bytes(self._h)
+
+    def launch_count(self, reset: bool = False) -> int:
+        return lib().gmg_mg_launch_count(self._h, int(reset))
+
+    def sync(self):
+        if lib().gmg_mg_sync(self._h):
+            _err("gmg_mg_sync")
+
+    # ---- user data
+    def createvector(self, *names, prec: int = FP64):
+        for n in names:
+            if lib().gmg_vec_create(self._h, n.encode(), prec, None):
+                _err(f"createvector {n}")
+
+    def vec(self, name: str):
+        v = lib().gmg_vec_by_name(self._h, name.encode())
+        if not v:
+            raise GmgError(f"no vector {name}")
+        return v
+
+    def mat(self, name: str = "MAT"):
+        m = lib().gmg_mat_by_name(self._h, name.encode())
+        if not m:
+            raise GmgError(f"no matrix {name}")
+        return m
+
+    def upload(self, name: str, level: int, data):
+        n, s, _ = self.size(level)
+        a = np.ascontiguousarray(data, np.float64).ravel()
+        if a.size != n * s:
+            raise GmgError(f"upload {name}: {a.size} values for {n}x{s}")
+        if lib().gmg_vec_upload(self.vec(name), level, _ptr(a)):
+            _err(f"upload {name}")
+
+    def download(self, name: str, level: int) -> np.ndarray:
+        n, s, _ = self.size(level)
+        a = np.empty(n * s)
+        if lib().gmg_vec_download(self.vec(name), level, _ptr(a)):
+            _err(f"download {name}")
+        return a
+
+    def device_ptr(self, name: str, level: int) -> int:
+        p = C.c_void_p()
+        if lib().gmg_vec_device_ptr(self.vec(name), level, C.byref(p)):
+            _err("device_ptr")
+        return p.value
+
+    # ---- numprocs
+    def npcreate(self, obj: str, cls: str):
+        if lib().gmg_np_create(self._h, obj.encode(), cls.encode()):
+            _err(f"npcreate {obj} $c {cls}")
+
+    def npinit(self, obj: str, args: str = "") -> int:
+        st = C.c_int()
+        rc = lib().gmg_np_init(self._h, obj.encode(), args.encode(), C.byref(st))
+        if rc and st.value != NP_NOT_ACTIVE:
+            _err(f"npinit {obj}")
+        return st.value
+
+    def npexecute(self, obj: str, args: str):
+        if lib().gmg_np_execute(self._h, obj.encode(), args.encode()):
+            _err(f"npexecute {obj} {args}")
+
+    def np(self, obj: str):
+        p = lib().gmg_np_by_name(self._h, obj.encode())
+        if not p:
+            raise GmgError(f"no numproc {obj}")
+        return p
+
+    def npdisplay(self, obj: str) -> str:
+        buf = C.create_string_buffer(4096)
+        lib().gmg_np_display(self.np(obj), buf, 4096)
+        return buf.value.decode()
+
+    # NP_ITER
+    def iter_preprocess(self, obj, level, x, b, A="MAT"):
+        bl, res = C.c_int(), C.c_int()
+        if lib().gmg_iter_preprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(bl), C.byref(res)):
+            _err(f"{obj} PreProcess")
+        return bl.value
+
+    def iter_iter(self, obj, level, c, b, A="MAT"):
+        res = C.c_int()
+        if lib().gmg_iter_iter(self.np(obj), level, self.vec(c), self.vec(b), self.mat(A), C.byref(res)):
+            _err(f"{obj} Iter")
+
+    def iter_postprocess(self, obj, level, x, b, A="MAT"):
+        res = C.c_int()
+        if lib().gmg_iter_postprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(res)):
+            _err(f"{obj} PostProcess")
+
+    # NP_TRANSFER
+    def restrict_defect(self, obj, level, to, frm, damp=None, A="MAT"):
+        res = C.c_int()
+        d = _sc(damp)
+        if lib().gmg_transfer_restrict_defect(self.np(obj), level, self.vec(to), self.vec(frm), self.mat(A), _ptr(d), C.byref(res)):
+            _err(f"{obj} RestrictDefect")
+
+    def interpolate_correction(self, obj, level, to, frm, damp=None, A="MAT"):
+        res = C.c_int()
+        d = _sc(damp)
+        if lib().gmg_transfer_interpolate_correction(self.np(obj), level, self.vec(to), self.vec(frm), self.mat(A), _ptr(d), C.byref(res)):
+            _err(f"{obj} InterpolateCorrection")
+
+    # NP_LINEAR_SOLVER
+    def ls_preprocess(self, obj, level, x, b, A="MAT"):
+        bl, res = C.c_int(), C.c_int()
+        if lib().gmg_ls_preprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(bl), C.byref(res)):
+            _err(f"{obj} PreProcess")
+        return bl.value
+
+    def ls_defect(self, obj, level, x, b, A="MAT"):
+        res = C.c_int()
+        if lib().gmg_ls_defect(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(res)):
+            _err(f"{obj} Defect")
+
+    def ls_residuum(self, obj, fl, tl, x, b, lr: LResult, A="MAT"):
+        if lib().gmg_ls_residuum(self.np(obj), fl, tl, self.vec(x), self.vec(b), self.mat(A), C.byref(lr)):
+            _err(f"{obj} Residuum")
+        return lr
+
+    def ls_solver(self, obj, level, x, b, lr: LResult, abslimit=None, reduction=None, A="MAT"):
+        a = None if abslimit is None else _sc(abslimit)
+        r = None if reduction is None else _sc(reduction)
+        if lib().gmg_ls_solver(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), _ptr(a), _ptr(r), C.byref(lr)):
+            _err(f"{obj} Solver")
+        return lr
+
+    def ls_postprocess(self, obj, level, x, b, A="MAT"):
+        res = C.c_int()
+        if lib().gmg_ls_postprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(res)):
+            _err(f"{obj} PostProcess")
+
+    # level kernels (ugblas / ugiter / transgrid)
+    def dset(self, level, x, a):
+        if lib().gmg_dset(self._h, level, self.vec(x), float(a)):
+            _err("dset")
+
+    def dcopy(self, level, x, y):
+        if lib().gmg_dcopy(self._h, level, self.vec(x), self.vec(y)):
+            _err("dcopy")
+
+    def dadd(self, level, x, y):
+        if lib().gmg_dadd(self._h, level, self.vec(x), self.vec(y)):
+            _err("dadd")
+
+    def dmatmul_minus(self, level, x, y, A="MAT"):
+        if lib().gmg_dmatmul_minus(self._h, level, self.vec(x), self.mat(A), self.vec(y)):
+            _err("dmatmul_minus")
+
+    def dnrm2x(self, level, x):
+        out = np.zeros(MAX_S)
+        if lib().gmg_dnrm2x(self._h, level, self.vec(x), _ptr(out)):
+            _err("dnrm2x")
+        return out[: self.size(level)[1]]
+
+    def l_jac(self, level, v, d, M="MAT"):
+        if lib().gmg_l_jac(self._h, level, self.vec(v), self.mat(M), self.vec(d)):
+            _err("l_jac")
+
+    def l_lgs(self, level, v, d, M="MAT"):
+        if lib().gmg_l_lgs(self._h, level, self.vec(v), self.mat(M), self.vec(d)):
+            _err("l_lgs")
+
+    def l_ilu_decomp(self, level, beta=None, M="MAT"):
+        b = _sc(beta, 0.0)
+        if lib().gmg_l_ilu_decomp(self._h, level, self.mat(M), _ptr(b)):
+            _err("l_ilubthdecomp")
+
+    def l_luiter(self, level, v, d, M="MAT"):
+        if lib().gmg_l_luiter(self._h, level, self.vec(v), self.mat(M), self.vec(d)):
+            _err("l_luiter")
+
+    def standard_restrict(self, level, to, frm, damp=None):
+        d = _sc(damp)
+        if lib().gmg_standard_restrict(self._h, level, self.vec(to), self.vec(frm), _ptr(d)):
+            _err("StandardRestrict")
+
+    def standard_interpolate_correction(self, level, to, frm, damp=None):
+        d = _sc(damp)
+        if lib().gmg_standard_interpolate_correction(self._h, level, self.vec(to), self.vec(frm), _ptr(d)):
+            _err("StandardInterpolateCorrection")
+
+    def solve_host(self, solver: str, b, x=None):
+        """gmg_solve_host: b (finest level, list order) -> (x, LResult)."""
+        n, s, _ = self.size(self.top)
+        bb = np.ascontiguousarray(b, np.float64).ravel()
+        xx = np.empty(n * s) if x is None else x
+        lr = LResult()
+        if lib().gmg_solve_host(self._h, solver.encode(), _ptr(bb), _ptr(xx), C.byref(lr)):
+            _err(f"solve {solver}")
+        return xx, lr
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gmg_mg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: int = 2, nu2: int = 2,
+               damp: float | None = None, red: float = 1e-10, abslimit: float = 1e-50, maxit: int = 100,
+               mixed: bool = False, x: str = "sol", b: str = "rhs", name: str = "mgs") -> str:
+    """The standard script of the workloads, as UG numproc commands:
+
+        npcreate transfer $c gtransfer; npcreate smooth $c g<smoother>;
+        npcreate base $c gex; npcreate basesolver $c gls ($red 1e-14 $m 1 $I base);
+        npcreate lmgc $c glmgc ($S smooth smooth basesolver $T transfer $n1 $n2 $b);
+        npcreate mgs $c gls ($A MAT $x sol $b rhs $red $abslimit $m $I lmgc)."""
+    for v in (x, b):
+        try:
+            mg.vec(v)
+        except GmgError:
+            mg.createvector(v)
+    mg.npcreate("transfer", "transfer.gtransfer"); mg.npinit("transfer", "")
+    mg.npcreate("smooth", f"iter.g{smoother}")
+    if damp is None:
+        damp = 0.8 if smoother == "jac" else 1.0
+    mg.npinit("smooth", f"$damp {damp}")
+    mg.npcreate("base", "iter.gex"); mg.npinit("base", "")
+    mg.npcreate("basesolver", "linear_solver.gls"); mg.npinit("basesolver", "$red 1e-14 $m 1 $I base")
+    mg.npcreate("lmgc", "iter.glmgc")
+    mg.npinit("lmgc", f"$S smooth smooth basesolver $T transfer $n1 {nu1} $n2 {nu2} $b {baselevel}")
+    mg.npcreate(name, "linear_solver.gls")
+    st = mg.npinit(name, f"$A MAT $x {x} $b {b} $red {red} $abslimit {abslimit} $m {maxit} $I lmgc"
+                         f" $mixed {int(mixed)}")
+    if st != NP_EXECUTABLE:
+        raise GmgError(f"{name} not executable (status {st})")
+    return name

@@ -1,0 +1,182 @@
+// Internal data structures of the GB300 lmgc library (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ug_gb300.h"
+
+namespace gmg {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+const char *last_error();
+
+#define GMG_CUDA(call)                                                                              \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) {                                                                        \
+      ::gmg::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));          \
+      return 1;                                                                                     \
+    }                                                                                               \
+  } while (0)
+
+#define GMG_CHECK(cond, ...)             \
+  do {                                   \
+    if (!(cond)) {                       \
+      ::gmg::set_error(__VA_ARGS__);     \
+      return 1;                          \
+    }                                    \
+  } while (0)
+
+// VECTOR flags kept per row on the device (bits)
+enum : uint8_t {
+  F_ACTIVE = 1,  // VCLASS >= ACTIVE_CLASS (3): updated by the smoothers
+  F_NEWDEF = 2,  // VCLASS >= NEWDEF_CLASS (2): restricted into the coarse grid
+  F_RESET = 4,   // VNCLASS >= NEWDEF_CLASS (2): reset before restriction
+};
+
+// ---------------------------------------------------------------- device memory
+// All arrays of one hierarchy live in one allocation; sub-arrays are 256-byte
+// aligned so every row / block access can use 128-bit loads.
+struct Arena {
+  char *base = nullptr;
+  size_t size = 0, used = 0;
+  int alloc(size_t bytes);
+  void *take(size_t bytes);
+  template <class T> T *take_n(size_t n) { return static_cast<T *>(take(n * sizeof(T))); }
+  void release();
+};
+
+// sparse rows on the device, one precision pair
+struct DevCSR {
+  int nrows = 0;
+  long long nnz = 0;
+  int *rowptr = nullptr, *col = nullptr;
+  double *v64 = nullptr;
+  float *v32 = nullptr;
+};
+
+// wavefront schedule: rows[ptr[w]..ptr[w+1]) are independent
+struct Sched {
+  std::vector<int> ptr;
+  int *rows = nullptr;
+  int nwave() const { return ptr.empty() ? 0 : int(ptr.size()) - 1; }
+};
+
+struct Level {
+  int n = 0, s = 1;
+  long long nnzb = 0;
+  bool all_active = true;   // every row ACTIVE
+  bool any_skip = false;
+  // host copies in processing order
+  std::vector<int> perm;       // perm[i] = UG list position of processed row i
+  std::vector<int> h_rowptr, h_col;
+  std::vector<double> h_val;   // blocks row-major
+  std::vector<uint8_t> h_flags, h_skip;
+  std::vector<int> h_prow, h_pcol;  // transfer from level-1 (processing orders)
+  std::vector<double> h_pw;
+  // device
+  DevCSR A;                     // system matrix
+  double *dinv64 = nullptr;     // inverse diagonal blocks (n*s*s)
+  float *dinv32 = nullptr;
+  uint8_t *flags = nullptr, *skip = nullptr;
+  int *perm_dev = nullptr;
+  Sched lower;                  // forward wavefronts (gs, ilu forward)
+  Sched upper;                  // backward wavefronts (ilu backward)
+  // ILU(0) factors in processing order (filled by the ilu numproc's PreProcess)
+  bool ilu_ready = false;
+  DevCSR L, U;                  // strict lower (unit diagonal) / strict upper parts
+  double *udinv64 = nullptr;    // inverted diagonal blocks of U
+  float *udinv32 = nullptr;
+  std::vector<void *> own;      // cudaMalloc'd arrays owned outside the arena
+  // transfer from level-1: P (rows = this level), R (rows = level-1 VECTORs)
+  DevCSR P, R;
+  // base solve: explicit inverse of the level matrix (filled by ex PreProcess)
+  double *ainv = nullptr;
+  int base_dim = 0;
+  // SpMV variant: threads cooperating on one row
+  int tpr = 8;
+};
+
+struct Vec {
+  std::string name;
+  int prec = GMG_PREC_FP64;
+  std::vector<void *> lev;  // one device array per level (n*s elements)
+};
+
+struct Mat {
+  std::string name;
+};
+
+
+}  // namespace gmg
+
+struct gmg_vec : gmg::Vec {
+  gmg_mg *mg = nullptr;
+};
+struct gmg_mat : gmg::Mat {
+  gmg_mg *mg = nullptr;
+};
+
+struct gmg_mg {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  gmg_mg_opts opts{};
+  gmg::Arena arena;
+  std::vector<gmg::Level> lev;
+  std::map<std::string, std::unique_ptr<gmg_vec>> vecs;
+  std::map<std::string, std::unique_ptr<gmg_mat>> mats;
+  std::map<std::string, std::unique_ptr<gmg_np>> nps;
+  bool own_stream = false;
+  // scratch: reduction partials, pinned host mirror of norms, staging buffers
+  double *partial = nullptr;   // GMG_REDUCE_BLOCKS * GMG_MAX_S
+  double *norms_dev = nullptr; // GMG_MAX_S
+  double *norms_host = nullptr;// pinned
+  void *stage_dev = nullptr;   // n_top*s doubles
+  double *stage_host = nullptr;// pinned, n_top*s doubles
+  long long launches = 0;
+  ~gmg_mg();
+};
+
+namespace gmg {
+
+constexpr int REDUCE_BLOCKS = 304;  // 2 x 152 SMs
+
+// ---------------------------------------------------------------- kernels (gmg_kernels.cu)
+// All launchers enqueue on `st`, count launches in mg->launches, return 0 / 1.
+int k_set(gmg_mg *mg, int prec, void *x, long long len, double a);
+int k_copy(gmg_mg *mg, int prec, void *x, const void *y, long long len);
+int k_add(gmg_mg *mg, int prec, void *x, const void *y, long long len);
+int k_scale(gmg_mg *mg, int prec, void *x, int n, int s, const double *damp);
+int k_convert(gmg_mg *mg, int dst_prec, void *dst, int src_prec, const void *src, long long len);
+int k_add_mixed(gmg_mg *mg, double *x64, int src_prec, const void *c, long long len);  // x64 += c
+// x -= A y (A in the precision of x/y); if acc != null also acc += y
+int k_matmul_minus(gmg_mg *mg, const Level &L, int prec, void *x, const void *y, void *acc);
+// FP64 x -= A64 y with y of precision yprec (iterative-refinement defect)
+int k_matmul_minus_mixed(gmg_mg *mg, const Level &L, double *x, int yprec, const void *y);
+// t = damp * D^{-1} b on ACTIVE rows, 0 elsewhere
+int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp);
+// forward Gauss-Seidel in processing order over the wavefronts; t is overwritten
+int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
+// ILU forward / backward solve with the factors of L
+int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
+// coarse = (reset ? 0 : coarse) + R (damp*fine), honouring coarse VECSKIP
+int k_restrict(gmg_mg *mg, const Level &fine, const Level &coarse, int prec, void *to, const void *from,
+               const double *damp);
+// fine t = P (damp*coarse) honouring fine VECSKIP; acc += t if acc != null
+int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void *from, const double *damp,
+                  void *acc);
+// per-component 2-norms of the NEW_DEFECT rows into mg->norms_dev (device)
+int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x);
+// base level: if |b| >= abslimit in some component: t = Ainv b; b -= A t; c += t
+int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit);
+// permutations between UG list order and processing order
+int k_gather(gmg_mg *mg, int prec, void *dst, const double *src_list, const int *perm, int n, int s);
+int k_scatter(gmg_mg *mg, int prec, double *dst_list, const void *src, const int *perm, int n, int s);
+
+}  // namespace gmg

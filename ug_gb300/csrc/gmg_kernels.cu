@@ -1,0 +1,803 @@
+// CUDA kernels of the lmgc hot path for GB300 (sm_103a).
+//
+// Every kernel is a memory-bound sparse or vector pass; none of them maps to
+// tensor cores.  Layout: block-CSR in processing order, 256-byte aligned
+// arrays in one arena.  Rows are handled by groups of TPR consecutive threads
+// (TPR = threads per row) so that a warp reads 32 consecutive (column,
+// value) pairs -- coalesced -- and the TPR partial sums are combined with
+// warp shuffles.  Block sizes S = 1, 2, 3 are compiled as templates so every
+// block product is unrolled in registers.
+//
+// The arithmetic of each kernel follows the UG routine named in its comment;
+// results agree with the reference to rounding (the summation order inside a
+// row follows the shuffle tree instead of the MATRIX list).
+#include <cstdio>
+
+#include "gmg_internal.h"
+
+namespace gmg {
+
+namespace {
+
+constexpr int BLK = 256;
+
+template <class T>
+struct Damp {
+  T d[GMG_MAX_S];
+};
+
+template <class T>
+Damp<T> make_damp(const double *damp, int s) {
+  Damp<T> r;
+  for (int i = 0; i < GMG_MAX_S; ++i) r.d[i] = T(damp ? damp[i < s ? i : 0] : 1.0);
+  return r;
+}
+
+inline unsigned grid_for(long long threads) {
+  long long g = (threads + BLK - 1) / BLK;
+  return unsigned(g < 1 ? 1 : g);
+}
+
+template <int TPR, class T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int off = TPR / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// ------------------------------------------------------------ BLAS-1 kernels
+template <class T>
+__global__ void set_kernel(T *x, long long len, T a) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    x[i] = a;
+}
+template <class T>
+__global__ void copy_kernel(T *x, const T *__restrict__ y, long long len) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    x[i] = y[i];
+}
+template <class T>
+__global__ void add_kernel(T *x, const T *__restrict__ y, long long len) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    x[i] += y[i];
+}
+template <class TD, class TS>
+__global__ void convert_kernel(TD *x, const TS *__restrict__ y, long long len) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    x[i] = TD(y[i]);
+}
+template <class TS>
+__global__ void add_mixed_kernel(double *x, const TS *__restrict__ y, long long len) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    x[i] += double(y[i]);
+}
+// dscalx: x_i,r *= damp_r
+template <class T, int S>
+__global__ void scale_kernel(T *x, int n, Damp<T> dm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int r = 0; r < S; ++r) x[(size_t)i * S + r] *= dm.d[r];
+}
+
+// ------------------------------------------------------------ dmatmul_minus
+// ugblas.cc:3997: x -= A y, row sums formed before the subtraction.
+// ACC: additionally acc += y (the lmgc `dadd(c, t)` that follows every
+// smoothing step and the coarse-grid correction, iter.cc:7811-7816, 7903).
+template <class T, class TY, int S, int TPR, bool ACC>
+__global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__restrict__ rowptr,
+                                                         const int *__restrict__ col, const T *__restrict__ val,
+                                                         const TY *__restrict__ y, T *__restrict__ x,
+                                                         TY *__restrict__ acc) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = gt / TPR, lane = gt & (TPR - 1);
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  if (row < n) {
+    const int k1 = __ldg(rowptr + row + 1);
+    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+      const int j = __ldg(col + k);
+      const T *m = val + (size_t)k * (S * S);
+      T yv[S];
+#pragma unroll
+      for (int c = 0; c < S; ++c) yv[c] = T(__ldg(y + (size_t)j * S + c));
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+  if (row < n && lane == 0) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      x[(size_t)row * S + r] -= s[r];
+      if (ACC) acc[(size_t)row * S + r] += y[(size_t)row * S + r];
+    }
+  }
+}
+
+// ------------------------------------------------------------ l_jac
+// ugiter.cc:271: t = D^{-1} b on ACTIVE rows (0 elsewhere), then the
+// smoother's dscalx by damp (iter.cc:836).  D^{-1} is stored per row.
+template <class T, int S, bool ALL_ACTIVE>
+__global__ void jac_kernel(int n, const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
+                           const T *__restrict__ b, T *__restrict__ t, Damp<T> dm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!ALL_ACTIVE && !(flags[i] & F_ACTIVE)) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) t[(size_t)i * S + r] = T(0);
+    return;
+  }
+  T bv[S];
+#pragma unroll
+  for (int c = 0; c < S; ++c) bv[c] = b[(size_t)i * S + c];
+  const T *D = dinv + (size_t)i * S * S;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    T v = T(0);
+#pragma unroll
+    for (int c = 0; c < S; ++c) v = fma(D[r * S + c], bv[c], v);
+    t[(size_t)i * S + r] = v * dm.d[r];
+  }
+}
+
+// ------------------------------------------------------------ l_lgs
+// ugiter.cc:412: forward solve (D+L) t = b in processing order.  Rows of one
+// wavefront depend only on rows of earlier wavefronts; t is zero before the
+// sweep, so summing every off-diagonal entry picks up exactly the rows that
+// precede the current one (later rows still hold 0).  Inactive rows stay 0.
+template <class T, int S, int TPR, bool ALL_ACTIVE>
+__global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ rows, int nrows,
+                                                      const int *__restrict__ rowptr, const int *__restrict__ col,
+                                                      const T *__restrict__ val, const T *__restrict__ dinv,
+                                                      const uint8_t *__restrict__ flags, const T *__restrict__ b,
+                                                      T *__restrict__ t) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = gt / TPR, lane = gt & (TPR - 1);
+  const bool valid = idx < nrows;
+  const int row = valid ? __ldg(rows + idx) : 0;
+  const bool work = valid && (ALL_ACTIVE || (flags[row] & F_ACTIVE));
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  if (work) {
+    const int k1 = __ldg(rowptr + row + 1);
+    for (int k = __ldg(rowptr + row) + 1 + lane; k < k1; k += TPR) {
+      const int j = __ldg(col + k);
+      const T *m = val + (size_t)k * (S * S);
+      T yv[S];
+#pragma unroll
+      for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+  if (work && lane == 0) {
+    T rhs[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) rhs[r] = b[(size_t)row * S + r] - s[r];
+    const T *D = dinv + (size_t)row * S * S;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      T v = T(0);
+#pragma unroll
+      for (int c = 0; c < S; ++c) v = fma(D[r * S + c], rhs[c], v);
+      t[(size_t)row * S + r] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------ l_luiter
+// ugiter.cc:4444: forward with the unit lower factor, then backward with the
+// strict upper factor and the stored inverse diagonal (StoreInverse).
+template <class T, int S, int TPR, bool ALL_ACTIVE>
+__global__ void __launch_bounds__(BLK) ilu_fwd_kernel(const int *__restrict__ rows, int nrows,
+                                                      const int *__restrict__ rowptr, const int *__restrict__ col,
+                                                      const T *__restrict__ val, const uint8_t *__restrict__ flags,
+                                                      const T *__restrict__ b, T *__restrict__ t) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = gt / TPR, lane = gt & (TPR - 1);
+  const bool valid = idx < nrows;
+  const int row = valid ? __ldg(rows + idx) : 0;
+  const bool active = ALL_ACTIVE || (valid && (flags[row] & F_ACTIVE));
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  if (valid && active) {
+    const int k1 = __ldg(rowptr + row + 1);
+    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+      const int j = __ldg(col + k);
+      const T *m = val + (size_t)k * (S * S);
+      T yv[S];
+#pragma unroll
+      for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+  if (valid && lane == 0) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) t[(size_t)row * S + r] = active ? b[(size_t)row * S + r] - s[r] : T(0);
+  }
+}
+
+template <class T, int S, int TPR, bool ALL_ACTIVE>
+__global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ rows, int nrows,
+                                                      const int *__restrict__ rowptr, const int *__restrict__ col,
+                                                      const T *__restrict__ val, const T *__restrict__ dinv,
+                                                      const uint8_t *__restrict__ flags, T *__restrict__ t) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = gt / TPR, lane = gt & (TPR - 1);
+  const bool valid = idx < nrows;
+  const int row = valid ? __ldg(rows + idx) : 0;
+  const bool work = valid && (ALL_ACTIVE || (flags[row] & F_ACTIVE));
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  if (work) {
+    const int k1 = __ldg(rowptr + row + 1);
+    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+      const int j = __ldg(col + k);
+      const T *m = val + (size_t)k * (S * S);
+      T yv[S];
+#pragma unroll
+      for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+  if (work && lane == 0) {
+    T rhs[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) rhs[r] = t[(size_t)row * S + r] - s[r];
+    const T *D = dinv + (size_t)row * S * S;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      T v = T(0);
+#pragma unroll
+      for (int c = 0; c < S; ++c) v = fma(D[r * S + c], rhs[c], v);
+      t[(size_t)row * S + r] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------ StandardRestrict
+// transgrid.cc:117-232 as a gather over R = P^T: coarse rows with VNCLASS >= 2
+// start from 0, the others keep their value; each contribution is
+// weight * (damp * fine defect); components set in the coarse VECSKIP get none.
+template <class T, int S>
+__global__ void restrict_kernel(int nc, const int *__restrict__ rrow, const int *__restrict__ rcol,
+                                const T *__restrict__ rw, const uint8_t *__restrict__ cflags,
+                                const uint8_t *__restrict__ cskip, const T *__restrict__ from, T *__restrict__ to,
+                                Damp<T> dm) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const bool reset = cflags[c] & F_RESET;
+  const int sk = cskip[c];
+  T acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = reset ? T(0) : to[(size_t)c * S + r];
+  const int k1 = __ldg(rrow + c + 1);
+  for (int k = __ldg(rrow + c); k < k1; ++k) {
+    const int f = __ldg(rcol + k);
+    const T w = __ldg(rw + k);
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc[r] = fma(w, dm.d[r] * from[(size_t)f * S + r], acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r)
+    to[(size_t)c * S + r] = (sk & (1 << r)) ? (reset ? T(0) : to[(size_t)c * S + r]) : acc[r];
+}
+
+// ------------------------------------------------------------ StandardInterpolateCorrection
+// transgrid.cc:235-347: t_f = sum_i (weight_i * damp) * c_i in every component
+// the fine VECSKIP leaves free; rows skipped in all components stay 0.
+template <class T, int S, bool ACC>
+__global__ void interp_kernel(int nf, const int *__restrict__ prow, const int *__restrict__ pcol,
+                              const T *__restrict__ pw, const uint8_t *__restrict__ fskip,
+                              const T *__restrict__ from, T *__restrict__ to, Damp<T> dm, T *__restrict__ acc) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int sk = fskip[f];
+  T v[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) v[r] = T(0);
+  if (sk != (1 << S) - 1) {
+    const int k1 = __ldg(prow + f + 1);
+    for (int k = __ldg(prow + f); k < k1; ++k) {
+      const int c = __ldg(pcol + k);
+      const T w = __ldg(pw + k);
+#pragma unroll
+      for (int r = 0; r < S; ++r) v[r] = fma(w * dm.d[r], from[(size_t)c * S + r], v[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < S; ++r)
+      if (sk & (1 << r)) v[r] = T(0);
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    to[(size_t)f * S + r] = v[r];
+    if (ACC) acc[(size_t)f * S + r] += v[r];
+  }
+}
+
+// ------------------------------------------------------------ dnrm2x
+// ugblas.cc:3156: per-component sums of squares over the NEW_DEFECT rows,
+// accumulated in FP64 whatever the vector precision, in two deterministic
+// stages (fixed grid, fixed reduction tree), then square roots.
+template <class T, int S, bool ALL>
+__global__ void __launch_bounds__(BLK) nrm_stage1(int n, const T *__restrict__ x, const uint8_t *__restrict__ flags,
+                                                  double *__restrict__ partial) {
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!ALL && !(flags[i] & F_NEWDEF)) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      double v = double(x[(size_t)i * S + r]);
+      acc[r] = fma(v, v, acc[r]);
+    }
+  }
+  __shared__ double sh[BLK / 32][S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * S + threadIdx.x] = v;
+  }
+}
+
+template <int S>
+__global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, double *__restrict__ out) {
+  __shared__ double sh[1024];
+  for (int r = 0; r < S; ++r) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += partial[(size_t)b * S + r];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[r] = sqrt(sh[0]);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ base solver
+// The lmgc base solver `ls $m 1 $I ex` (np/procs/ls.cc:637, iter.cc:8972):
+// nothing happens when every component of |b| is below the base abslimit;
+// otherwise t = A^{-1} b (the exact solve of the band LU, here an explicit
+// FP64 inverse), b -= A t, c += t.  One CTA: the base level is tiny.
+template <class T, int S>
+__global__ void __launch_bounds__(1024) base_kernel(int n, const double *__restrict__ ainv, const int *__restrict__ rowptr,
+                                                    const int *__restrict__ col, const T *__restrict__ val,
+                                                    T *__restrict__ c, T *__restrict__ b, T *__restrict__ t,
+                                                    Damp<double> abslimit) {
+  __shared__ double red[S][32];
+  __shared__ int skip;
+  const int N = n * S;
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+#pragma unroll
+    for (int r = 0; r < S; ++r) { double v = double(b[(size_t)i * S + r]); acc[r] += v * v; }
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[r][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int below = 1;
+    for (int r = 0; r < S; ++r) {
+      double v = 0.0;
+      for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) v += red[r][w];
+      if (fabs(sqrt(v)) >= fabs(abslimit.d[r])) below = 0;
+    }
+    skip = below;
+  }
+  __syncthreads();
+  if (skip) return;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double v = 0.0;
+    for (int j = 0; j < N; ++j) v = fma(ainv[(size_t)i * N + j], double(b[j]), v);
+    t[i] = T(v);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    T s[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) s[r] = T(0);
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = col[k];
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int cc = 0; cc < S; ++cc) s[r] = fma(val[(size_t)k * S * S + r * S + cc], t[(size_t)j * S + cc], s[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      b[(size_t)i * S + r] -= s[r];
+      c[(size_t)i * S + r] += t[(size_t)i * S + r];
+    }
+  }
+}
+
+// ------------------------------------------------------------ permutations
+template <class T>
+__global__ void gather_kernel(T *dst, const double *__restrict__ src, const int *__restrict__ perm, int n, int s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = perm[i];
+  for (int r = 0; r < s; ++r) dst[(size_t)i * s + r] = T(src[(size_t)p * s + r]);
+}
+template <class T>
+__global__ void scatter_kernel(double *dst, const T *__restrict__ src, const int *__restrict__ perm, int n, int s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = perm[i];
+  for (int r = 0; r < s; ++r) dst[(size_t)p * s + r] = double(src[(size_t)i * s + r]);
+}
+
+// ------------------------------------------------------------ dispatch helpers
+#define LAUNCH_CHECK(mg)                                                         \
+  do {                                                                           \
+    (mg)->launches++;                                                            \
+    cudaError_t e_ = cudaGetLastError();                                         \
+    if (e_ != cudaSuccess) {                                                     \
+      set_error("%s:%d kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_)); \
+      return 1;                                                                  \
+    }                                                                            \
+  } while (0)
+
+inline int vec_grid(long long len) {
+  long long g = (len + BLK - 1) / BLK;
+  return int(g > 4 * 152 * 8 ? 4 * 152 * 8 : (g < 1 ? 1 : g));
+}
+
+template <class T, class TY, int S, bool ACC>
+int spmv_dispatch_tpr(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, TY *acc) {
+  const int n = L.n;
+  switch (L.tpr) {
+#define CASE(TP)                                                                                           \
+  case TP:                                                                                                 \
+    spmv_minus_kernel<T, TY, S, TP, ACC><<<grid_for((long long)n * TP), BLK, 0, mg->stream>>>(n, L.A.rowptr, \
+                                                                                           L.A.col, val, y, x, acc); \
+    break;
+    CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32)
+#undef CASE
+    default: set_error("bad threads-per-row %d", L.tpr); return 1;
+  }
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+template <class T, class TY, bool ACC>
+int spmv_dispatch(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, TY *acc) {
+  switch (L.s) {
+    case 1: return spmv_dispatch_tpr<T, TY, 1, ACC>(mg, L, val, x, y, acc);
+    case 2: return spmv_dispatch_tpr<T, TY, 2, ACC>(mg, L, val, x, y, acc);
+    case 3: return spmv_dispatch_tpr<T, TY, 3, ACC>(mg, L, val, x, y, acc);
+    default: set_error("block size %d not compiled", L.s); return 1;
+  }
+}
+
+template <class T>
+const T *mval(const DevCSR &M);
+template <>
+const double *mval<double>(const DevCSR &M) { return M.v64; }
+template <>
+const float *mval<float>(const DevCSR &M) { return M.v32; }
+template <class T>
+const T *dinv_of(const Level &L);
+template <>
+const double *dinv_of<double>(const Level &L) { return L.dinv64; }
+template <>
+const float *dinv_of<float>(const Level &L) { return L.dinv32; }
+template <class T>
+const T *udinv_of(const Level &L);
+template <>
+const double *udinv_of<double>(const Level &L) { return L.udinv64; }
+template <>
+const float *udinv_of<float>(const Level &L) { return L.udinv32; }
+
+template <class T, int S, int TPR>
+int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
+  const T *val = mval<T>(L.A), *dinv = dinv_of<T>(L);
+  for (int w = 0; w < L.lower.nwave(); ++w) {
+    const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
+    if (nr <= 0) continue;
+    if (L.all_active)
+      gs_wave_kernel<T, S, TPR, true><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+          L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv, L.flags, b, t);
+    else
+      gs_wave_kernel<T, S, TPR, false><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+          L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv, L.flags, b, t);
+    LAUNCH_CHECK(mg);
+  }
+  return 0;
+}
+
+template <class T, int S, int TPR>
+int ilu_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
+  const T *lv = mval<T>(L.L), *uv = mval<T>(L.U), *ud = udinv_of<T>(L);
+  for (int w = 0; w < L.lower.nwave(); ++w) {
+    const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
+    if (nr <= 0) continue;
+    if (L.all_active)
+      ilu_fwd_kernel<T, S, TPR, true><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+          L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
+    else
+      ilu_fwd_kernel<T, S, TPR, false><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+          L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
+    LAUNCH_CHECK(mg);
+  }
+  for (int w = 0; w < L.upper.nwave(); ++w) {
+    const int r0 = L.upper.ptr[w], nr = L.upper.ptr[w + 1] - r0;
+    if (nr <= 0) continue;
+    if (L.all_active)
+      ilu_bwd_kernel<T, S, TPR, true><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+          L.upper.rows + r0, nr, L.U.rowptr, L.U.col, uv, ud, L.flags, t);
+    else
+      ilu_bwd_kernel<T, S, TPR, false><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+          L.upper.rows + r0, nr, L.U.rowptr, L.U.col, uv, ud, L.flags, t);
+    LAUNCH_CHECK(mg);
+  }
+  return 0;
+}
+
+// threads per row for the triangular sweeps: short rows, so at most 8
+inline int tri_tpr(const Level &L) { return L.tpr > 8 ? 8 : (L.tpr < 4 ? 4 : L.tpr); }
+
+}  // namespace
+
+// ============================================================ launchers
+int k_set(gmg_mg *mg, int prec, void *x, long long len, double a) {
+  if (len <= 0) return 0;
+  if (prec == GMG_PREC_FP64) set_kernel<double><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)x, len, a);
+  else set_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)x, len, float(a));
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_copy(gmg_mg *mg, int prec, void *x, const void *y, long long len) {
+  if (len <= 0) return 0;
+  if (prec == GMG_PREC_FP64) copy_kernel<double><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)x, (const double *)y, len);
+  else copy_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)x, (const float *)y, len);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_add(gmg_mg *mg, int prec, void *x, const void *y, long long len) {
+  if (len <= 0) return 0;
+  if (prec == GMG_PREC_FP64) add_kernel<double><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)x, (const double *)y, len);
+  else add_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)x, (const float *)y, len);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_scale(gmg_mg *mg, int prec, void *x, int n, int s, const double *damp) {
+  bool unit = true;
+  for (int r = 0; r < s; ++r) unit = unit && damp[r] == 1.0;
+  if (unit || n <= 0) return 0;  // dscalx by 1 is the identity
+#define SC(TT, SS) scale_kernel<TT, SS><<<grid_for(n), BLK, 0, mg->stream>>>((TT *)x, n, make_damp<TT>(damp, SS))
+  if (prec == GMG_PREC_FP64) {
+    if (s == 1) SC(double, 1); else if (s == 2) SC(double, 2); else if (s == 3) SC(double, 3);
+    else { set_error("block size %d not compiled", s); return 1; }
+  } else {
+    if (s == 1) SC(float, 1); else if (s == 2) SC(float, 2); else if (s == 3) SC(float, 3);
+    else { set_error("block size %d not compiled", s); return 1; }
+  }
+#undef SC
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long len) {
+  if (len <= 0) return 0;
+  if (dp == sp) return k_copy(mg, dp, dst, src, len);
+  if (dp == GMG_PREC_FP32)
+    convert_kernel<float, double><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)dst, (const double *)src, len);
+  else
+    convert_kernel<double, float><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)dst, (const float *)src, len);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_add_mixed(gmg_mg *mg, double *x, int sp, const void *c, long long len) {
+  if (len <= 0) return 0;
+  if (sp == GMG_PREC_FP64) return k_add(mg, GMG_PREC_FP64, x, c, len);
+  add_mixed_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>(x, (const float *)c, len);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_matmul_minus(gmg_mg *mg, const Level &L, int prec, void *x, const void *y, void *acc) {
+  if (L.n == 0) return 0;
+  if (prec == GMG_PREC_FP64) {
+    if (acc) return spmv_dispatch<double, double, true>(mg, L, L.A.v64, (double *)x, (const double *)y, (double *)acc);
+    return spmv_dispatch<double, double, false>(mg, L, L.A.v64, (double *)x, (const double *)y, nullptr);
+  }
+  GMG_CHECK(L.A.v32, "FP32 matrix copy not built (gmg_mg_opts.fp32_copy)");
+  if (acc) return spmv_dispatch<float, float, true>(mg, L, L.A.v32, (float *)x, (const float *)y, (float *)acc);
+  return spmv_dispatch<float, float, false>(mg, L, L.A.v32, (float *)x, (const float *)y, nullptr);
+}
+
+int k_matmul_minus_mixed(gmg_mg *mg, const Level &L, double *x, int yprec, const void *y) {
+  if (yprec == GMG_PREC_FP64) return k_matmul_minus(mg, L, GMG_PREC_FP64, x, y, nullptr);
+  return spmv_dispatch<double, float, false>(mg, L, L.A.v64, x, (const float *)y, nullptr);
+}
+
+int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp) {
+  if (L.n == 0) return 0;
+#define JK(TT, SS, ALL)                                                                                     \
+  jac_kernel<TT, SS, ALL><<<grid_for(L.n), BLK, 0, mg->stream>>>(L.n, dinv_of<TT>(L), L.flags, (const TT *)b, \
+                                                                 (TT *)t, make_damp<TT>(damp, SS))
+#define JS(TT)                                                                      \
+  if (L.s == 1) { if (L.all_active) JK(TT, 1, true); else JK(TT, 1, false); }       \
+  else if (L.s == 2) { if (L.all_active) JK(TT, 2, true); else JK(TT, 2, false); }  \
+  else if (L.s == 3) { if (L.all_active) JK(TT, 3, true); else JK(TT, 3, false); }  \
+  else { set_error("block size %d not compiled", L.s); return 1; }
+  if (prec == GMG_PREC_FP64) { JS(double) }
+  else { GMG_CHECK(L.dinv32, "FP32 copy not built"); JS(float) }
+#undef JS
+#undef JK
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
+  if (L.n == 0) return 0;
+  if (k_set(mg, prec, t, (long long)L.n * L.s, 0.0)) return 1;
+  const int tp = tri_tpr(L);
+#define GS(TT, SS)                                                                      \
+  return tp == 4 ? gs_waves<TT, SS, 4>(mg, L, (TT *)t, (const TT *)b)                   \
+                 : gs_waves<TT, SS, 8>(mg, L, (TT *)t, (const TT *)b);
+  if (prec == GMG_PREC_FP64) {
+    if (L.s == 1) { GS(double, 1) } else if (L.s == 2) { GS(double, 2) } else if (L.s == 3) { GS(double, 3) }
+  } else {
+    GMG_CHECK(L.A.v32 && L.dinv32, "FP32 copy not built");
+    if (L.s == 1) { GS(float, 1) } else if (L.s == 2) { GS(float, 2) } else if (L.s == 3) { GS(float, 3) }
+  }
+#undef GS
+  set_error("block size %d not compiled", L.s);
+  return 1;
+}
+
+int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
+  if (L.n == 0) return 0;
+  GMG_CHECK(L.ilu_ready, "ILU factors of level not computed (ilu PreProcess)");
+  const int tp = tri_tpr(L);
+#define IL(TT, SS)                                                                       \
+  return tp == 4 ? ilu_waves<TT, SS, 4>(mg, L, (TT *)t, (const TT *)b)                   \
+                 : ilu_waves<TT, SS, 8>(mg, L, (TT *)t, (const TT *)b);
+  if (prec == GMG_PREC_FP64) {
+    if (L.s == 1) { IL(double, 1) } else if (L.s == 2) { IL(double, 2) } else if (L.s == 3) { IL(double, 3) }
+  } else {
+    GMG_CHECK(L.L.v32, "FP32 ILU factors not built");
+    if (L.s == 1) { IL(float, 1) } else if (L.s == 2) { IL(float, 2) } else if (L.s == 3) { IL(float, 3) }
+  }
+#undef IL
+  set_error("block size %d not compiled", L.s);
+  return 1;
+}
+
+int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp) {
+  if (C.n == 0) return 0;
+#define RK(TT, SS)                                                                                            \
+  restrict_kernel<TT, SS><<<grid_for(C.n), BLK, 0, mg->stream>>>(C.n, F.R.rowptr, F.R.col, mval<TT>(F.R), C.flags, \
+                                                                 C.skip, (const TT *)from, (TT *)to,            \
+                                                                 make_damp<TT>(damp, SS))
+#define RS(TT)                                  \
+  if (F.s == 1) RK(TT, 1);                      \
+  else if (F.s == 2) RK(TT, 2);                 \
+  else if (F.s == 3) RK(TT, 3);                 \
+  else { set_error("block size %d not compiled", F.s); return 1; }
+  if (prec == GMG_PREC_FP64) { RS(double) }
+  else { GMG_CHECK(F.R.v32, "FP32 transfer not built"); RS(float) }
+#undef RS
+#undef RK
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_interpolate(gmg_mg *mg, const Level &F, int prec, void *to, const void *from, const double *damp, void *acc) {
+  if (F.n == 0) return 0;
+#define IK(TT, SS, A)                                                                                              \
+  interp_kernel<TT, SS, A><<<grid_for(F.n), BLK, 0, mg->stream>>>(F.n, F.P.rowptr, F.P.col, mval<TT>(F.P), F.skip, \
+                                                                  (const TT *)from, (TT *)to,                        \
+                                                                  make_damp<TT>(damp, SS), (TT *)acc)
+#define IS(TT)                                                                \
+  if (F.s == 1) { if (acc) IK(TT, 1, true); else IK(TT, 1, false); }         \
+  else if (F.s == 2) { if (acc) IK(TT, 2, true); else IK(TT, 2, false); }    \
+  else if (F.s == 3) { if (acc) IK(TT, 3, true); else IK(TT, 3, false); }    \
+  else { set_error("block size %d not compiled", F.s); return 1; }
+  if (prec == GMG_PREC_FP64) { IS(double) }
+  else { GMG_CHECK(F.P.v32, "FP32 transfer not built"); IS(float) }
+#undef IS
+#undef IK
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x) {
+  const int nb = REDUCE_BLOCKS;
+  bool all = L.all_active;  // every row ACTIVE implies every row NEW_DEFECT
+#define N1(TT, SS)                                                                                            \
+  { if (all) nrm_stage1<TT, SS, true><<<nb, BLK, 0, mg->stream>>>(L.n, (const TT *)x, L.flags, mg->partial);  \
+    else nrm_stage1<TT, SS, false><<<nb, BLK, 0, mg->stream>>>(L.n, (const TT *)x, L.flags, mg->partial);     \
+    LAUNCH_CHECK(mg);                                                                                         \
+    nrm_stage2<SS><<<1, 1024, 0, mg->stream>>>(nb, mg->partial, mg->norms_dev);                               \
+    LAUNCH_CHECK(mg); return 0; }
+  if (prec == GMG_PREC_FP64) {
+    if (L.s == 1) N1(double, 1) if (L.s == 2) N1(double, 2) if (L.s == 3) N1(double, 3)
+  } else {
+    if (L.s == 1) N1(float, 1) if (L.s == 2) N1(float, 2) if (L.s == 3) N1(float, 3)
+  }
+#undef N1
+  set_error("block size %d not compiled", L.s);
+  return 1;
+}
+
+int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit) {
+  GMG_CHECK(L.ainv, "base level inverse not computed (ex PreProcess)");
+  Damp<double> al = make_damp<double>(abslimit, L.s);
+#define BK(TT, SS)                                                                                             \
+  base_kernel<TT, SS><<<1, 1024, 0, mg->stream>>>(L.n, L.ainv, L.A.rowptr, L.A.col, mval<TT>(L.A), (TT *)c,    \
+                                                  (TT *)b, (TT *)t, al)
+#define BS(TT)                                   \
+  if (L.s == 1) BK(TT, 1);                       \
+  else if (L.s == 2) BK(TT, 2);                  \
+  else if (L.s == 3) BK(TT, 3);                  \
+  else { set_error("block size %d not compiled", L.s); return 1; }
+  if (prec == GMG_PREC_FP64) { BS(double) }
+  else { GMG_CHECK(L.A.v32, "FP32 copy not built"); BS(float) }
+#undef BS
+#undef BK
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_gather(gmg_mg *mg, int prec, void *dst, const double *src, const int *perm, int n, int s) {
+  if (n == 0) return 0;
+  if (prec == GMG_PREC_FP64) gather_kernel<double><<<grid_for(n), BLK, 0, mg->stream>>>((double *)dst, src, perm, n, s);
+  else gather_kernel<float><<<grid_for(n), BLK, 0, mg->stream>>>((float *)dst, src, perm, n, s);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *perm, int n, int s) {
+  if (n == 0) return 0;
+  if (prec == GMG_PREC_FP64) scatter_kernel<double><<<grid_for(n), BLK, 0, mg->stream>>>(dst, (const double *)src, perm, n, s);
+  else scatter_kernel<float><<<grid_for(n), BLK, 0, mg->stream>>>(dst, (const float *)src, perm, n, s);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+}  // namespace gmg

@@ -1,0 +1,536 @@
+// Hierarchy construction: the flattened UG hierarchy (gmg_level_desc, UG
+// VECTOR-list order) becomes a device-resident set of block-CSR levels in
+// processing order, with the standard transfer as P (interpolation, rows =
+// fine VECTORs) and R = P^T (restriction, rows = coarse VECTORs, gathered
+// instead of scattered so no atomics are needed), inverse diagonal blocks,
+// per-row VECTOR flags and the wavefront schedules of the triangular sweeps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+
+#include "gmg_internal.h"
+#include "gmg_np.h"
+
+namespace gmg {
+
+static thread_local char g_err[1024] = "";
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+const char *last_error() { return g_err; }
+
+int Arena::alloc(size_t bytes) {
+  size = bytes;
+  used = 0;
+  if (bytes == 0) return 0;
+  GMG_CUDA(cudaMalloc(&base, bytes));
+  return 0;
+}
+void *Arena::take(size_t bytes) {
+  size_t b = (bytes + 255) & ~size_t(255);
+  if (used + b > size) return nullptr;
+  void *p = base + used;
+  used += b;
+  return p;
+}
+void Arena::release() {
+  if (base) cudaFree(base);
+  base = nullptr;
+  size = used = 0;
+}
+
+// ------------------------------------------------------------ small dense algebra
+// Inverse of an s x s block by Gauss-Jordan with partial pivoting; s <= 2
+// in closed form as InvertSmallBlock (np/algebra/block.cc:272).
+int invert_block(int s, const double *m, double *inv) {
+  if (s == 1) {
+    if (m[0] == 0.0) return 1;
+    inv[0] = 1.0 / m[0];
+    return 0;
+  }
+  if (s == 2) {
+    double det = m[0] * m[3] - m[1] * m[2];
+    if (det == 0.0) return 1;
+    double id = 1.0 / det;
+    inv[0] = m[3] * id; inv[1] = -m[1] * id; inv[2] = -m[2] * id; inv[3] = m[0] * id;
+    return 0;
+  }
+  std::vector<double> a(m, m + s * s);
+  for (int i = 0; i < s * s; ++i) inv[i] = 0.0;
+  for (int i = 0; i < s; ++i) inv[i * s + i] = 1.0;
+  for (int c = 0; c < s; ++c) {
+    int p = c;
+    for (int r = c + 1; r < s; ++r) if (std::fabs(a[r * s + c]) > std::fabs(a[p * s + c])) p = r;
+    if (a[p * s + c] == 0.0) return 1;
+    if (p != c)
+      for (int k = 0; k < s; ++k) { std::swap(a[p * s + k], a[c * s + k]); std::swap(inv[p * s + k], inv[c * s + k]); }
+    double d = 1.0 / a[c * s + c];
+    for (int k = 0; k < s; ++k) { a[c * s + k] *= d; inv[c * s + k] *= d; }
+    for (int r = 0; r < s; ++r) {
+      if (r == c) continue;
+      double f = a[r * s + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < s; ++k) { a[r * s + k] -= f * a[c * s + k]; inv[r * s + k] -= f * inv[c * s + k]; }
+    }
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------ orderings and schedules
+// Greedy colouring of the (symmetrised) matrix graph in list order; returns
+// the colour of every VECTOR.
+static std::vector<int> greedy_colour(int n, const std::vector<std::vector<int>> &adj, int *ncol) {
+  std::vector<int> colour(n, -1), mark;
+  int nc = 0;
+  for (int i = 0; i < n; ++i) {
+    mark.assign(nc + 1, 0);
+    for (int j : adj[i])
+      if (colour[j] >= 0) mark[colour[j]] = 1;
+    int c = 0;
+    while (c < nc && mark[c]) ++c;
+    colour[i] = c;
+    if (c == nc) ++nc;
+  }
+  *ncol = nc;
+  return colour;
+}
+
+static std::vector<std::vector<int>> sym_adjacency(int n, const int *rowptr, const int *col) {
+  std::vector<std::vector<int>> adj(n);
+  for (int i = 0; i < n; ++i)
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      int j = col[k];
+      if (j == i) continue;
+      adj[i].push_back(j);
+      adj[j].push_back(i);
+    }
+  for (auto &a : adj) {
+    std::sort(a.begin(), a.end());
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+  }
+  return adj;
+}
+
+// Level sets of the triangular dependency graph in processing order.
+// forward: row i waits for its neighbours j < i; backward: for j > i.
+static void wavefronts(int n, const std::vector<std::vector<int>> &adj, bool forward, std::vector<int> &ptr,
+                       std::vector<int> &rows) {
+  std::vector<int> w(n, 0);
+  int nw = 0;
+  if (forward) {
+    for (int i = 0; i < n; ++i) {
+      int m = -1;
+      for (int j : adj[i]) if (j < i) m = std::max(m, w[j]);
+      w[i] = m + 1;
+      nw = std::max(nw, w[i] + 1);
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      int m = -1;
+      for (int j : adj[i]) if (j > i) m = std::max(m, w[j]);
+      w[i] = m + 1;
+      nw = std::max(nw, w[i] + 1);
+    }
+  }
+  ptr.assign(nw + 1, 0);
+  for (int i = 0; i < n; ++i) ptr[w[i] + 1]++;
+  for (int k = 0; k < nw; ++k) ptr[k + 1] += ptr[k];
+  rows.assign(n, 0);
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  if (forward) {
+    for (int i = 0; i < n; ++i) rows[fill[w[i]]++] = i;
+  } else {
+    for (int i = n - 1; i >= 0; --i) rows[fill[w[i]]++] = i;
+  }
+}
+
+// ------------------------------------------------------------ device uploads
+template <class T>
+static int upload(T *dst, const T *src, size_t n) {
+  if (n) GMG_CUDA(cudaMemcpy(dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+static std::vector<float> to_f32(const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); }
+
+static size_t al(size_t b) { return (b + 255) & ~size_t(255); }
+
+// host-side build of one level (processing order), no device work
+struct HostLevel {
+  int n = 0, s = 1;
+  std::vector<int> perm, iperm, rowptr, col;
+  std::vector<double> val, dinv;
+  std::vector<uint8_t> flags, skip;
+  std::vector<int> lptr, lrows, uptr, urows;
+  std::vector<int> prow, pcol, rrow, rcol;
+  std::vector<double> pw, rw;
+  bool all_active = true, any_skip = false;
+  int ncolour = 0;
+};
+
+static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H) {
+  const int n = d.n, s = d.s, ss = s * s;
+  H.n = n; H.s = s;
+  GMG_CHECK(n >= 0 && s >= 1 && s <= GMG_MAX_S, "bad level size n=%d s=%d", n, s);
+  GMG_CHECK(n == 0 || (d.rowptr && d.col && d.val), "level arrays missing");
+  for (int i = 0; i < n; ++i) {
+    GMG_CHECK(d.rowptr[i + 1] > d.rowptr[i], "row %d has no diagonal entry", i);
+    GMG_CHECK(d.col[d.rowptr[i]] == i, "row %d: first entry is not the diagonal (VSTART)", i);
+  }
+  auto adj = sym_adjacency(n, d.rowptr, d.col);
+  H.perm.resize(n);
+  std::iota(H.perm.begin(), H.perm.end(), 0);
+  if (order == GMG_ORDER_COLOR && n > 0) {
+    std::vector<int> colour = greedy_colour(n, adj, &H.ncolour);
+    std::stable_sort(H.perm.begin(), H.perm.end(), [&](int a, int b) { return colour[a] < colour[b]; });
+  }
+  H.iperm.resize(n);
+  for (int i = 0; i < n; ++i) H.iperm[H.perm[i]] = i;
+  // matrix rows in processing order, entries in MATRIX-list order, diagonal first
+  H.rowptr.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) H.rowptr[i + 1] = H.rowptr[i] + (d.rowptr[H.perm[i] + 1] - d.rowptr[H.perm[i]]);
+  H.col.resize(H.rowptr[n]);
+  H.val.resize(size_t(H.rowptr[n]) * ss);
+  for (int i = 0; i < n; ++i) {
+    int o = H.perm[i], k0 = d.rowptr[o], k1 = d.rowptr[o + 1], q = H.rowptr[i];
+    for (int k = k0; k < k1; ++k, ++q) {
+      GMG_CHECK(d.col[k] >= 0 && d.col[k] < n, "row %d: column %d out of range", o, d.col[k]);
+      H.col[q] = H.iperm[d.col[k]];
+      std::memcpy(&H.val[size_t(q) * ss], &d.val[size_t(k) * ss], sizeof(double) * ss);
+    }
+  }
+  H.flags.resize(n);
+  H.skip.resize(n);
+  for (int i = 0; i < n; ++i) {
+    int o = H.perm[i];
+    int vc = d.vclass ? d.vclass[o] : 3, vn = d.vnclass ? d.vnclass[o] : 3, sk = d.skip ? d.skip[o] : 0;
+    uint8_t f = 0;
+    if (vc >= 3) f |= F_ACTIVE; else H.all_active = false;
+    if (vc >= 2) f |= F_NEWDEF;
+    if (vn >= 2) f |= F_RESET;
+    H.flags[i] = f;
+    H.skip[i] = uint8_t(sk & 0xff);
+    if (sk) H.any_skip = true;
+  }
+  // inverse diagonal blocks (Jacobi, Gauss-Seidel)
+  H.dinv.assign(size_t(n) * ss, 0.0);
+  for (int i = 0; i < n; ++i) {
+    if (!(H.flags[i] & F_ACTIVE)) continue;
+    GMG_CHECK(!invert_block(s, &H.val[size_t(H.rowptr[i]) * ss], &H.dinv[size_t(i) * ss]),
+              "singular diagonal block in row %d", H.perm[i]);
+  }
+  // wavefronts in processing order
+  std::vector<std::vector<int>> padj(n);
+  for (int i = 0; i < n; ++i) {
+    for (int j : adj[H.perm[i]]) padj[i].push_back(H.iperm[j]);
+  }
+  wavefronts(n, padj, true, H.lptr, H.lrows);
+  wavefronts(n, padj, false, H.uptr, H.urows);
+  return 0;
+}
+
+// transfer from the coarser level `C` to `F` (processing orders of both)
+static int build_host_transfer(const gmg_level_desc &d, const HostLevel &C, HostLevel &F) {
+  const int n = F.n;
+  GMG_CHECK(d.prowptr && d.pcol && d.pw, "transfer arrays missing on a fine level");
+  F.prow.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    int o = F.perm[i];
+    F.prow[i + 1] = F.prow[i] + (d.prowptr[o + 1] - d.prowptr[o]);
+  }
+  F.pcol.resize(F.prow[n]);
+  F.pw.resize(F.prow[n]);
+  for (int i = 0; i < n; ++i) {
+    int o = F.perm[i], q = F.prow[i];
+    for (int k = d.prowptr[o]; k < d.prowptr[o + 1]; ++k, ++q) {
+      GMG_CHECK(d.pcol[k] >= 0 && d.pcol[k] < C.n, "transfer: coarse index %d out of range", d.pcol[k]);
+      F.pcol[q] = C.iperm[d.pcol[k]];
+      F.pw[q] = d.pw[k];
+    }
+  }
+  // R = P^T over the fine rows with NEW_DEFECT (transgrid.cc:153)
+  F.rrow.assign(C.n + 1, 0);
+  for (int i = 0; i < n; ++i)
+    if (F.flags[i] & F_NEWDEF)
+      for (int k = F.prow[i]; k < F.prow[i + 1]; ++k) F.rrow[F.pcol[k] + 1]++;
+  for (int c = 0; c < C.n; ++c) F.rrow[c + 1] += F.rrow[c];
+  F.rcol.resize(F.rrow[C.n]);
+  F.rw.resize(F.rrow[C.n]);
+  std::vector<int> fill(F.rrow.begin(), F.rrow.end() - 1);
+  for (int i = 0; i < n; ++i)
+    if (F.flags[i] & F_NEWDEF)
+      for (int k = F.prow[i]; k < F.prow[i + 1]; ++k) {
+        int q = fill[F.pcol[k]]++;
+        F.rcol[q] = i;
+        F.rw[q] = F.pw[k];
+      }
+  return 0;
+}
+
+static int pick_tpr(const HostLevel &H) {
+  if (H.n == 0) return 8;
+  double avg = double(H.rowptr[H.n]) / H.n * (H.s > 1 ? 2.0 : 1.0);
+  int t = avg <= 2 ? 2 : avg <= 5 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32;
+  if (H.s > 1 && t > 8) t = 8;
+  return t;
+}
+
+// ------------------------------------------------------------ autotuner
+// Times dmatmul_minus with 4, 8 and 16 threads per row on the level's own
+// matrix (CUDA events, median of 5) and keeps the fastest.
+static int autotune_level(gmg_mg *mg, Level &L) {
+  if (L.n < 4096) return 0;
+  void *x = nullptr, *y = nullptr;
+  size_t len = size_t(L.n) * L.s;
+  GMG_CUDA(cudaMalloc(&x, len * sizeof(double)));
+  GMG_CUDA(cudaMalloc(&y, len * sizeof(double)));
+  cudaMemsetAsync(x, 0, len * sizeof(double), mg->stream);
+  cudaMemsetAsync(y, 0, len * sizeof(double), mg->stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = L.tpr;
+  float best_ms = 1e30f;
+  const int cands[3] = {4, 8, 16};
+  for (int c : cands) {
+    if (L.s > 1 && c > 8) continue;
+    L.tpr = c;
+    std::vector<float> ts;
+    for (int rep = 0; rep < 6; ++rep) {
+      cudaEventRecord(e0, mg->stream);
+      if (k_matmul_minus(mg, L, GMG_PREC_FP64, x, y, nullptr)) break;
+      cudaEventRecord(e1, mg->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep) ts.push_back(ms);
+    }
+    if (ts.empty()) continue;
+    std::sort(ts.begin(), ts.end());
+    if (ts[ts.size() / 2] < best_ms) { best_ms = ts[ts.size() / 2]; best = c; }
+  }
+  L.tpr = best;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(x);
+  cudaFree(y);
+  return 0;
+}
+
+}  // namespace gmg
+
+using namespace gmg;
+
+gmg_mg::~gmg_mg() {
+  nps.clear();
+  if (own_stream && stream) cudaStreamDestroy(stream);
+  for (auto &kv : vecs)
+    for (void *p : kv.second->lev) cudaFree(p);
+  for (auto &L : lev) {
+    for (void *p : L.own) cudaFree(p);
+    if (L.ainv) cudaFree(L.ainv);
+  }
+  arena.release();
+  if (norms_host) cudaFreeHost(norms_host);
+  if (stage_host) cudaFreeHost(stage_host);
+}
+
+extern "C" {
+
+const char *gmg_last_error(void) { return gmg::last_error(); }
+
+int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *opts_in, gmg_mg **out) {
+  if (!out || !levels || nlevels < 1) { set_error("gmg_mg_create: bad arguments"); return 1; }
+  *out = nullptr;
+  gmg_mg_opts opts{};
+  if (opts_in) opts = *opts_in;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return 1; }
+  GMG_CUDA(cudaSetDevice(opts.device));
+  const int s = levels[0].s;
+  std::vector<HostLevel> H(nlevels);
+  for (int l = 0; l < nlevels; ++l) {
+    GMG_CHECK(levels[l].s == s, "all levels must have the same block size");
+    if (build_host_level(levels[l], opts.order, H[l])) return 1;
+    if (l > 0 && build_host_transfer(levels[l], H[l - 1], H[l])) return 1;
+  }
+  // plan the arena
+  const bool f32 = opts.fp32_copy != 0;
+  size_t bytes = 0;
+  for (int l = 0; l < nlevels; ++l) {
+    const HostLevel &h = H[l];
+    size_t nnz = h.rowptr[h.n], ss = size_t(s) * s;
+    bytes += al((h.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * 8) + (f32 ? al(nnz * ss * 4) : 0);
+    bytes += al(h.n * ss * 8) + (f32 ? al(h.n * ss * 4) : 0) + 2 * al(h.n) + 3 * al(h.n * 4);
+    if (l > 0) {
+      size_t pn = h.pcol.size(), rn = h.rcol.size();
+      bytes += al((h.n + 1) * 4) + al(pn * 4) + al(pn * 8) + (f32 ? al(pn * 4) : 0);
+      bytes += al((H[l - 1].n + 1) * 4) + al(rn * 4) + al(rn * 8) + (f32 ? al(rn * 4) : 0);
+    }
+  }
+  auto mg = std::make_unique<gmg_mg>();
+  mg->device = opts.device;
+  mg->opts = opts;
+  // a stream of its own: the legacy default stream cannot be captured into graphs
+  GMG_CUDA(cudaStreamCreateWithFlags(&mg->stream, cudaStreamNonBlocking));
+  mg->own_stream = true;
+  if (mg->arena.alloc(bytes)) return 1;
+  mg->lev.resize(nlevels);
+  for (int l = 0; l < nlevels; ++l) {
+    HostLevel &h = H[l];
+    Level &L = mg->lev[l];
+    const size_t nnz = h.rowptr[h.n], ss = size_t(s) * s;
+    L.n = h.n; L.s = s; L.nnzb = nnz;
+    L.all_active = h.all_active; L.any_skip = h.any_skip;
+    L.A.nrows = h.n; L.A.nnz = nnz;
+    L.A.rowptr = mg->arena.take_n<int>(h.n + 1);
+    L.A.col = mg->arena.take_n<int>(nnz);
+    L.A.v64 = mg->arena.take_n<double>(nnz * ss);
+    if (upload(L.A.rowptr, h.rowptr.data(), h.n + 1) || upload(L.A.col, h.col.data(), nnz) ||
+        upload(L.A.v64, h.val.data(), nnz * ss))
+      return 1;
+    L.dinv64 = mg->arena.take_n<double>(h.n * ss);
+    if (upload(L.dinv64, h.dinv.data(), h.n * ss)) return 1;
+    if (f32) {
+      L.A.v32 = mg->arena.take_n<float>(nnz * ss);
+      L.dinv32 = mg->arena.take_n<float>(h.n * ss);
+      auto v = to_f32(h.val), dv = to_f32(h.dinv);
+      if (upload(L.A.v32, v.data(), v.size()) || upload(L.dinv32, dv.data(), dv.size())) return 1;
+    }
+    L.flags = mg->arena.take_n<uint8_t>(h.n);
+    L.skip = mg->arena.take_n<uint8_t>(h.n);
+    L.perm_dev = mg->arena.take_n<int>(h.n);
+    L.lower.rows = mg->arena.take_n<int>(h.n);
+    L.upper.rows = mg->arena.take_n<int>(h.n);
+    L.lower.ptr = h.lptr;
+    L.upper.ptr = h.uptr;
+    if (upload(L.flags, h.flags.data(), h.n) || upload(L.skip, h.skip.data(), h.n) ||
+        upload(L.perm_dev, h.perm.data(), h.n) || upload(L.lower.rows, h.lrows.data(), h.n) ||
+        upload(L.upper.rows, h.urows.data(), h.n))
+      return 1;
+    if (l > 0) {
+      const int nc = H[l - 1].n;
+      L.P.nrows = h.n; L.P.nnz = h.pcol.size();
+      L.P.rowptr = mg->arena.take_n<int>(h.n + 1);
+      L.P.col = mg->arena.take_n<int>(h.pcol.size());
+      L.P.v64 = mg->arena.take_n<double>(h.pw.size());
+      L.R.nrows = nc; L.R.nnz = h.rcol.size();
+      L.R.rowptr = mg->arena.take_n<int>(nc + 1);
+      L.R.col = mg->arena.take_n<int>(h.rcol.size());
+      L.R.v64 = mg->arena.take_n<double>(h.rw.size());
+      if (upload(L.P.rowptr, h.prow.data(), h.n + 1) || upload(L.P.col, h.pcol.data(), h.pcol.size()) ||
+          upload(L.P.v64, h.pw.data(), h.pw.size()) || upload(L.R.rowptr, h.rrow.data(), nc + 1) ||
+          upload(L.R.col, h.rcol.data(), h.rcol.size()) || upload(L.R.v64, h.rw.data(), h.rw.size()))
+        return 1;
+      if (f32) {
+        L.P.v32 = mg->arena.take_n<float>(h.pw.size());
+        L.R.v32 = mg->arena.take_n<float>(h.rw.size());
+        auto pw = to_f32(h.pw), rw = to_f32(h.rw);
+        if (upload(L.P.v32, pw.data(), pw.size()) || upload(L.R.v32, rw.data(), rw.size())) return 1;
+      }
+    }
+    L.tpr = pick_tpr(h);
+    // keep host copies for the ILU / base factorisations and for export
+    L.perm = std::move(h.perm);
+    L.h_rowptr = std::move(h.rowptr);
+    L.h_col = std::move(h.col);
+    L.h_val = std::move(h.val);
+    L.h_flags = std::move(h.flags);
+    L.h_skip = std::move(h.skip);
+  }
+  GMG_CHECK(mg->arena.used <= mg->arena.size, "arena overflow");
+  // scratch
+  GMG_CUDA(cudaMalloc(&mg->partial, sizeof(double) * (REDUCE_BLOCKS * GMG_MAX_S + GMG_MAX_S)));
+  mg->norms_dev = mg->partial + REDUCE_BLOCKS * GMG_MAX_S;
+  GMG_CUDA(cudaMallocHost(&mg->norms_host, sizeof(double) * GMG_MAX_S));
+  mg->lev.back().own.push_back(mg->partial);
+  size_t top_len = size_t(mg->lev.back().n) * s;
+  GMG_CUDA(cudaMallocHost(&mg->stage_host, sizeof(double) * (top_len ? top_len : 1)));
+  GMG_CUDA(cudaMalloc(&mg->stage_dev, sizeof(double) * (top_len ? top_len : 1)));
+  mg->lev.back().own.push_back(mg->stage_dev);
+  mg->mats["MAT"] = std::make_unique<gmg_mat>();
+  mg->mats["MAT"]->name = "MAT";
+  mg->mats["MAT"]->mg = mg.get();
+  if (opts.autotune)
+    for (auto &L : mg->lev)
+      if (autotune_level(mg.get(), L)) return 1;
+  GMG_CUDA(cudaDeviceSynchronize());
+  *out = mg.release();
+  return 0;
+}
+
+int gmg_mg_destroy(gmg_mg *mg) {
+  delete mg;
+  return 0;
+}
+
+int gmg_mg_set_stream(gmg_mg *mg, void *stream) {
+  if (!mg) return 1;
+  if (mg->own_stream && mg->stream) cudaStreamDestroy(mg->stream);
+  mg->own_stream = false;
+  mg->stream = (cudaStream_t)stream;
+  return 0;
+}
+
+int gmg_mg_nlevels(const gmg_mg *mg) { return mg ? int(mg->lev.size()) : 0; }
+
+int gmg_mg_level_size(const gmg_mg *mg, int level, int *n, int *s, long long *nnzb) {
+  if (!mg || level < 0 || level >= (int)mg->lev.size()) { set_error("bad level"); return 1; }
+  const Level &L = mg->lev[level];
+  if (n) *n = L.n;
+  if (s) *s = L.s;
+  if (nnzb) *nnzb = L.nnzb;
+  return 0;
+}
+
+int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm) {
+  if (!mg || level < 0 || level >= (int)mg->lev.size()) { set_error("bad level"); return 1; }
+  std::copy(mg->lev[level].perm.begin(), mg->lev[level].perm.end(), perm);
+  return 0;
+}
+
+int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val) {
+  if (!mg || level < 0 || level >= (int)mg->lev.size()) { set_error("bad level"); return 1; }
+  const Level &L = mg->lev[level];
+  if (rowptr) std::copy(L.h_rowptr.begin(), L.h_rowptr.end(), rowptr);
+  if (col) std::copy(L.h_col.begin(), L.h_col.end(), col);
+  if (val) std::copy(L.h_val.begin(), L.h_val.end(), val);
+  return 0;
+}
+
+int gmg_mg_num_waves(const gmg_mg *mg, int level) {
+  if (!mg || level < 0 || level >= (int)mg->lev.size()) return -1;
+  return mg->lev[level].lower.nwave();
+}
+
+long long gmg_mg_device_bytes(const gmg_mg *mg) {
+  if (!mg) return 0;
+  long long b = (long long)mg->arena.size;
+  for (auto &kv : mg->vecs)
+    for (size_t l = 0; l < kv.second->lev.size(); ++l)
+      b += (long long)mg->lev[l].n * mg->lev[l].s * (kv.second->prec == GMG_PREC_FP64 ? 8 : 4);
+  return b;
+}
+
+long long gmg_mg_launch_count(const gmg_mg *mg, int reset) {
+  if (!mg) return 0;
+  long long c = mg->launches;
+  if (reset) const_cast<gmg_mg *>(mg)->launches = 0;
+  return c;
+}
+
+int gmg_mg_sync(gmg_mg *mg) {
+  if (!mg) return 1;
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  GMG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+}  // extern "C"

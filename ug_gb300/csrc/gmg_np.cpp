@@ -1,0 +1,1112 @@
+// Numprocs of the GB300 lmgc path and the C ABI around them.
+//
+// Each class restates the control flow of the UG numproc it mirrors (cited
+// per method); the arithmetic runs in the kernels of gmg_kernels.cu on the
+// multigrid's stream.  Nothing here synchronises with the device except the
+// ls convergence test (one 8-byte-per-component read per iteration) and the
+// explicit upload / download calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <sstream>
+
+#include "gmg_internal.h"
+#include "gmg_np.h"
+
+namespace gmg {
+
+int invert_block(int s, const double *m, double *inv);  // gmg_mg.cpp
+
+// ------------------------------------------------------------ arguments
+Args::Args(const char *s) {
+  std::string cur;
+  bool in = false;
+  for (const char *p = s ? s : ""; *p; ++p) {
+    if (*p == '$') {
+      if (in) argv.push_back(cur);
+      cur.clear();
+      in = true;
+    } else if (in && *p != ';') {
+      cur += *p;
+    }
+  }
+  if (in) argv.push_back(cur);
+  for (auto &a : argv) {
+    size_t b = a.find_first_not_of(" \t\n"), e = a.find_last_not_of(" \t\n");
+    a = (b == std::string::npos) ? std::string() : a.substr(b, e - b + 1);
+  }
+}
+
+const std::string *Args::find(const char *name) const {
+  const size_t ln = strlen(name);
+  for (auto &a : argv)
+    if (a.compare(0, ln, name) == 0 && (a.size() == ln || a[ln] == ' ' || a[ln] == '\t')) return &a;
+  return nullptr;
+}
+
+bool Args::get_int(const char *name, int *v) const {
+  const std::string *a = find(name);
+  if (!a) return false;
+  return sscanf(a->c_str() + strlen(name), "%d", v) == 1;
+}
+
+bool Args::get_double(const char *name, double *v) const {
+  const std::string *a = find(name);
+  if (!a) return false;
+  return sscanf(a->c_str() + strlen(name), "%lf", v) == 1;
+}
+
+bool Args::get_word(const char *name, std::string *v) const {
+  const std::string *a = find(name);
+  if (!a) return false;
+  std::istringstream is(a->substr(strlen(name)));
+  return bool(is >> *v);
+}
+
+bool Args::get_sc(const char *name, double *v) const {
+  const std::string *a = find(name);
+  if (!a) return false;
+  std::istringstream is(a->substr(strlen(name)));
+  std::string tok;
+  if (!(is >> tok)) return false;
+  if (tok == "nd" || tok == "ed" || tok == "el" || tok == "si")
+    if (!(is >> tok)) return false;
+  std::vector<double> vals;
+  size_t p = 0;
+  while (p <= tok.size()) {
+    size_t q = tok.find(':', p);
+    std::string part = tok.substr(p, q == std::string::npos ? std::string::npos : q - p);
+    char *end = nullptr;
+    double d = strtod(part.c_str(), &end);
+    if (end == part.c_str()) return false;
+    vals.push_back(d);
+    if (q == std::string::npos) break;
+    p = q + 1;
+  }
+  for (int i = 0; i < GMG_MAX_S; ++i) v[i] = vals[std::min<size_t>(i, vals.size() - 1)];
+  return true;
+}
+
+// ------------------------------------------------------------ helpers
+void *vlev(gmg_vec *v, int level) { return v->lev[level]; }
+
+static gmg_vec *read_vec(gmg_mg *mg, const Args &a, const char *opt) {
+  std::string n;
+  if (!a.get_word(opt, &n)) return nullptr;
+  auto it = mg->vecs.find(n);
+  return it == mg->vecs.end() ? nullptr : it->second.get();
+}
+static gmg_mat *read_mat(gmg_mg *mg, const Args &a, const char *opt) {
+  std::string n;
+  if (!a.get_word(opt, &n)) return nullptr;
+  auto it = mg->mats.find(n);
+  return it == mg->mats.end() ? nullptr : it->second.get();
+}
+static gmg_np *read_np(gmg_mg *mg, const std::string &n, int kind) {
+  auto it = mg->nps.find(n);
+  if (it == mg->nps.end() || it->second->kind() != kind) return nullptr;
+  return it->second.get();
+}
+
+static int alloc_vec(gmg_mg *mg, gmg_vec *v) {
+  v->lev.assign(mg->lev.size(), nullptr);
+  for (size_t l = 0; l < mg->lev.size(); ++l) {
+    size_t len = size_t(mg->lev[l].n) * mg->lev[l].s;
+    size_t bytes = (len ? len : 1) * (v->prec == GMG_PREC_FP64 ? 8 : 4);
+    GMG_CUDA(cudaMalloc(&v->lev[l], bytes));
+    GMG_CUDA(cudaMemsetAsync(v->lev[l], 0, bytes, mg->stream));
+  }
+  return 0;
+}
+
+gmg_vec *temp_vec(gmg_mg *mg, const std::string &name, int prec) {
+  auto it = mg->vecs.find(name);
+  if (it != mg->vecs.end()) return it->second->prec == prec ? it->second.get() : nullptr;
+  auto v = std::make_unique<gmg_vec>();
+  v->name = name;
+  v->prec = prec;
+  v->mg = mg;
+  if (alloc_vec(mg, v.get())) return nullptr;
+  gmg_vec *r = v.get();
+  mg->vecs[name] = std::move(v);
+  return r;
+}
+
+static long long vlen(gmg_mg *mg, int level) { return (long long)mg->lev[level].n * mg->lev[level].s; }
+
+static int check_level(gmg_mg *mg, int level) {
+  GMG_CHECK(level >= 0 && level < (int)mg->lev.size(), "level %d out of range", level);
+  return 0;
+}
+
+static std::string fmt_sc(const double *v, int s) {
+  std::ostringstream o;
+  for (int i = 0; i < s; ++i) o << (i ? ":" : "") << v[i];
+  return o.str();
+}
+
+// ------------------------------------------------------------ NP_ITER
+int NPIter::InitIter(const Args &a) {
+  A = read_mat(mg, a, "A");
+  c = read_vec(mg, a, "c");
+  b = read_vec(mg, a, "r");
+  return (A && b && c) ? NP_EXECUTABLE : NP_ACTIVE;
+}
+
+int NPIter::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *) {
+  *baselevel = level;
+  return 0;
+}
+
+int NPIter::PostProcess(int, gmg_vec *, gmg_vec *, gmg_mat *, int *) { return 0; }
+
+int NPIter::IterAcc(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int *result) {
+  if (Iter(level, cv, bv, Am, result)) return 1;
+  return k_add(mg, acc->prec, vlev(acc, level), vlev(cv, level), vlen(mg, level));
+}
+
+// NPIterExecute, iter.cc:702-760
+int NPIter::Execute(const Args &a) {
+  const int level = int(mg->lev.size()) - 1;
+  int result = 0, bl = 0;
+  GMG_CHECK(c && b && A, "NPIterExecute: vectors c, b or matrix A missing");
+  if (a.option("i") && PreProcess(level, c, b, A, &bl, &result)) return 1;
+  if (a.option("s") && Iter(level, c, b, A, &result)) return 1;
+  if (a.option("p") && PostProcess(level, c, b, A, &result)) return 1;
+  return 0;
+}
+
+std::string NPIter::Display() const {
+  std::ostringstream o;
+  o << "class " << cls << "\n";
+  if (A) o << "A = " << A->name << "\n";
+  if (b) o << "r = " << b->name << "\n";
+  if (c) o << "c = " << c->name << "\n";
+  return o.str();
+}
+
+// ------------------------------------------------------------ smoothers
+int NPSmoother::Init(const Args &a) {  // SmootherInit, iter.cc:763
+  for (double &d : damp) d = 1.0;
+  a.get_sc("damp", damp);
+  return InitIter(a);
+}
+
+std::string NPSmoother::Display() const {
+  return NPIter::Display() + "damp = " + fmt_sc(damp, mg->lev.empty() ? 1 : mg->lev[0].s) + "\n";
+}
+
+// Smoother, iter.cc:817-842
+int NPSmoother::Iter(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, int *result) {
+  if (check_level(mg, level)) return 1;
+  GMG_CHECK(x->prec == bv->prec, "smoother: c and b differ in precision");
+  if (Step(level, x, bv, Am, result)) return 1;
+  const Level &L = mg->lev[level];
+  if (k_scale(mg, x->prec, vlev(x, level), L.n, L.s, damp)) return 1;
+  return k_matmul_minus(mg, L, x->prec, vlev(bv, level), vlev(x, level), nullptr);
+}
+
+int NPSmoother::IterAcc(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int *result) {
+  if (check_level(mg, level)) return 1;
+  if (acc->prec != x->prec) return NPIter::IterAcc(level, x, bv, Am, acc, result);
+  if (Step(level, x, bv, Am, result)) return 1;
+  const Level &L = mg->lev[level];
+  if (k_scale(mg, x->prec, vlev(x, level), L.n, L.s, damp)) return 1;
+  return k_matmul_minus(mg, L, x->prec, vlev(bv, level), vlev(x, level), vlev(acc, level));
+}
+
+// jac: l_jac (ugiter.cc:271) with the damping folded into the same pass
+int NPJac::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
+  return k_jac(mg, mg->lev[level], x->prec, vlev(x, level), vlev(bv, level), one);
+}
+int NPJac::Iter(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
+  if (check_level(mg, level)) return 1;
+  const Level &L = mg->lev[level];
+  if (k_jac(mg, L, x->prec, vlev(x, level), vlev(bv, level), damp)) return 1;
+  return k_matmul_minus(mg, L, x->prec, vlev(bv, level), vlev(x, level), nullptr);
+}
+int NPJac::IterAcc(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int *result) {
+  if (check_level(mg, level)) return 1;
+  if (acc->prec != x->prec) return NPIter::IterAcc(level, x, bv, Am, acc, result);
+  const Level &L = mg->lev[level];
+  if (k_jac(mg, L, x->prec, vlev(x, level), vlev(bv, level), damp)) return 1;
+  return k_matmul_minus(mg, L, x->prec, vlev(bv, level), vlev(x, level), vlev(acc, level));
+}
+
+// gs: l_lgs (ugiter.cc:412) in the hierarchy's processing order
+int NPGs::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
+  return k_gs(mg, mg->lev[level], x->prec, vlev(x, level), vlev(bv, level));
+}
+
+// ilu: ILUInit (iter.cc:5415) reads $beta (and $mindiag, unused by the decomposition)
+int NPIlu::Init(const Args &a) {
+  for (double &d : beta) d = 0.0;
+  a.get_sc("beta", beta);
+  return NPSmoother::Init(a);
+}
+
+std::string NPIlu::Display() const {
+  return NPSmoother::Display() + "beta = " + fmt_sc(beta, mg->lev.empty() ? 1 : mg->lev[0].s) + "\n";
+}
+
+// l_ilubthdecomp (ugiter.cc:2252-2625) without threshold / rest vector, on a
+// copy of A (ILUPreProcess, iter.cc:5444), in processing order.  The row's
+// diagonal block becomes its inverse (StoreInverse), each block (j,i) below
+// it the pivot A_ji D_i^{-1}, and pattern blocks (j,k), k>i, are updated.
+static int ilu_factor_host(const Level &L, const double *beta, std::vector<double> &lu) {
+  const int n = L.n, s = L.s, ss = s * s;
+  lu = L.h_val;
+  auto active = [&](int i) { return (L.h_flags[i] & F_ACTIVE) != 0; };
+  auto find = [&](int row, int col) {
+    for (int k = L.h_rowptr[row]; k < L.h_rowptr[row + 1]; ++k)
+      if (L.h_col[k] == col) return k;
+    return -1;
+  };
+  std::vector<double> inv(ss), pm(ss), cor(ss), rowsum(s);
+  for (int i = 0; i < n; ++i) {
+    if (!active(i)) continue;
+    const int kd = L.h_rowptr[i];
+    if (s == 1) {
+      double diag = lu[kd];
+      if (std::fabs(diag) < 2.220446049250313e-16 * 10 * 1e-20) return -(i + 1);
+      double invdiag = 1.0 / diag;
+      lu[kd] = invdiag;
+      for (int kij = kd + 1; kij < L.h_rowptr[i + 1]; ++kij) {
+        int j = L.h_col[kij];
+        if (!(active(j) && j > i)) continue;
+        int kji = find(j, i);
+        if (kji < 0) return -(i + 1);
+        double pivot = lu[kji] * invdiag;
+        lu[kji] = pivot;
+        if (pivot == 0.0) continue;
+        for (int kik = kd + 1; kik < L.h_rowptr[i + 1]; ++kik) {
+          int k = L.h_col[kik];
+          if (!(active(k) && k > i)) continue;
+          int kjk = find(j, k);
+          if (kjk >= 0) lu[kjk] -= pivot * lu[kik];
+          else lu[L.h_rowptr[j]] += beta[0] * std::fabs(pivot * lu[kik]);
+        }
+      }
+      continue;
+    }
+    if (invert_block(s, &lu[size_t(kd) * ss], inv.data())) return -(i + 1);
+    std::copy(inv.begin(), inv.end(), lu.begin() + size_t(kd) * ss);
+    for (int kij = kd + 1; kij < L.h_rowptr[i + 1]; ++kij) {
+      int j = L.h_col[kij];
+      if (!(active(j) && i < j)) continue;
+      std::fill(rowsum.begin(), rowsum.end(), 0.0);
+      int kji = find(j, i);
+      if (kji < 0) return -(i + 1);
+      double *piv = &lu[size_t(kji) * ss];
+      bool zero = true;
+      for (int r = 0; r < s; ++r)
+        for (int c = 0; c < s; ++c) {
+          double sum = 0.0;
+          for (int q = 0; q < s; ++q) sum += piv[r * s + q] * inv[q * s + c];
+          pm[r * s + c] = sum;
+          if (sum != 0.0) zero = false;
+        }
+      std::copy(pm.begin(), pm.end(), piv);
+      if (zero) continue;
+      for (int kik = kd + 1; kik < L.h_rowptr[i + 1]; ++kik) {
+        int k = L.h_col[kik];
+        if (!(active(k) && i < k)) continue;
+        const double *elm = &lu[size_t(kik) * ss];
+        bool cz = true;
+        for (int r = 0; r < s; ++r)
+          for (int c = 0; c < s; ++c) {
+            double sum = 0.0;
+            for (int q = 0; q < s; ++q) sum += pm[r * s + q] * elm[q * s + c];
+            cor[r * s + c] = sum;
+            if (sum != 0.0) cz = false;
+          }
+        if (cz) continue;
+        int kjk = find(j, k);
+        if (kjk >= 0) {
+          double *mat = &lu[size_t(kjk) * ss];
+          for (int q = 0; q < ss; ++q) mat[q] -= cor[q];
+        } else {
+          for (int r = 0; r < s; ++r)
+            for (int c = 0; c < s; ++c) rowsum[r] += std::fabs(cor[r * s + c]);
+        }
+      }
+      double *djj = &lu[size_t(L.h_rowptr[j]) * ss];
+      for (int r = 0; r < s; ++r)
+        for (int c = 0; c < s; ++c) djj[r * s + c] *= 1.0 + beta[c] * rowsum[c];
+    }
+  }
+  return 0;
+}
+
+template <class T>
+static int dev_copy(gmg::Level &L, T **dst, const std::vector<T> &src) {
+  size_t n = src.empty() ? 1 : src.size();
+  GMG_CUDA(cudaMalloc(dst, n * sizeof(T)));
+  L.own.push_back(*dst);
+  if (!src.empty()) GMG_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// ILUPreProcess, iter.cc:5444: factor a copy of A and split it into the unit
+// lower factor, the strict upper factor and the inverted diagonal blocks.
+int NPIlu::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *result) {
+  if (check_level(mg, level)) return 1;
+  Level &L = mg->lev[level];
+  *baselevel = level;
+  if (L.ilu_ready) return 0;
+  std::vector<double> lu;
+  int rc = ilu_factor_host(L, beta, lu);
+  if (rc) {
+    *result = rc;
+    set_error("ILU decomposition failed in row %d of level %d", -rc - 1, level);
+    return 1;
+  }
+  const int n = L.n, s = L.s, ss = s * s;
+  std::vector<int> lr(n + 1, 0), ur(n + 1, 0), lc, uc;
+  std::vector<double> lv, uv, ud(size_t(n) * ss, 0.0);
+  for (int i = 0; i < n; ++i) {
+    const bool act = L.h_flags[i] & F_ACTIVE;
+    for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k) {
+      int j = L.h_col[k];
+      if (j == i) {
+        if (act) std::copy(&lu[size_t(k) * ss], &lu[size_t(k) * ss] + ss, &ud[size_t(i) * ss]);
+        continue;
+      }
+      if (!act || !(L.h_flags[j] & F_ACTIVE)) continue;
+      if (j < i) { lc.push_back(j); lv.insert(lv.end(), &lu[size_t(k) * ss], &lu[size_t(k) * ss] + ss); }
+      else { uc.push_back(j); uv.insert(uv.end(), &lu[size_t(k) * ss], &lu[size_t(k) * ss] + ss); }
+    }
+    lr[i + 1] = int(lc.size());
+    ur[i + 1] = int(uc.size());
+  }
+  L.L.nrows = L.U.nrows = n;
+  L.L.nnz = lc.size();
+  L.U.nnz = uc.size();
+  if (dev_copy(L, &L.L.rowptr, lr) || dev_copy(L, &L.L.col, lc) || dev_copy(L, &L.L.v64, lv) ||
+      dev_copy(L, &L.U.rowptr, ur) || dev_copy(L, &L.U.col, uc) || dev_copy(L, &L.U.v64, uv) ||
+      dev_copy(L, &L.udinv64, ud))
+    return 1;
+  if (mg->opts.fp32_copy) {
+    std::vector<float> lv32(lv.begin(), lv.end()), uv32(uv.begin(), uv.end()), ud32(ud.begin(), ud.end());
+    if (dev_copy(L, &L.L.v32, lv32) || dev_copy(L, &L.U.v32, uv32) || dev_copy(L, &L.udinv32, ud32)) return 1;
+  }
+  L.ilu_ready = true;
+  return 0;
+}
+
+int NPIlu::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
+  return k_luiter(mg, mg->lev[level], x->prec, vlev(x, level), vlev(bv, level));
+}
+
+// ex: EXPreProcess (iter.cc:8685) decomposes the level matrix once; here the
+// decomposition is an explicit FP64 inverse (Gauss-Jordan, partial pivoting).
+int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *result) {
+  if (check_level(mg, level)) return 1;
+  Level &L = mg->lev[level];
+  *baselevel = level;
+  if (L.ainv) return 0;
+  const int N = L.n * L.s, s = L.s;
+  GMG_CHECK(N <= 4096, "ex: level %d has %d unknowns, above the dense base-solver limit 4096", level, N);
+  std::vector<double> a(size_t(N) * N, 0.0), inv(size_t(N) * N, 0.0);
+  for (int i = 0; i < L.n; ++i)
+    for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k)
+      for (int r = 0; r < s; ++r)
+        for (int c = 0; c < s; ++c)
+          a[size_t(i * s + r) * N + L.h_col[k] * s + c] = L.h_val[size_t(k) * s * s + r * s + c];
+  for (int i = 0; i < N; ++i) inv[size_t(i) * N + i] = 1.0;
+  for (int c = 0; c < N; ++c) {
+    int p = c;
+    for (int r = c + 1; r < N; ++r)
+      if (std::fabs(a[size_t(r) * N + c]) > std::fabs(a[size_t(p) * N + c])) p = r;
+    if (a[size_t(p) * N + c] == 0.0) {
+      *result = -(c + 1);
+      set_error("ex: singular base-level matrix");
+      return 1;
+    }
+    if (p != c)
+      for (int k = 0; k < N; ++k) {
+        std::swap(a[size_t(p) * N + k], a[size_t(c) * N + k]);
+        std::swap(inv[size_t(p) * N + k], inv[size_t(c) * N + k]);
+      }
+    double d = 1.0 / a[size_t(c) * N + c];
+    for (int k = 0; k < N; ++k) { a[size_t(c) * N + k] *= d; inv[size_t(c) * N + k] *= d; }
+    for (int r = 0; r < N; ++r) {
+      if (r == c) continue;
+      double f = a[size_t(r) * N + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < N; ++k) {
+        a[size_t(r) * N + k] -= f * a[size_t(c) * N + k];
+        inv[size_t(r) * N + k] -= f * inv[size_t(c) * N + k];
+      }
+    }
+  }
+  GMG_CUDA(cudaMalloc(&L.ainv, inv.size() * sizeof(double)));
+  GMG_CUDA(cudaMemcpy(L.ainv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
+  L.base_dim = N;
+  return 0;
+}
+
+int NPEx::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, int *result) {
+  // x = A^{-1} b without touching b: run the exact solve on a scratch defect
+  gmg_vec *tb = temp_vec(mg, "__ex_b" + std::to_string(x->prec), x->prec);
+  gmg_vec *tt = temp_vec(mg, "__ex_t" + std::to_string(x->prec), x->prec);
+  GMG_CHECK(tb && tt, "ex: temporary vectors");
+  const long long len = vlen(mg, level);
+  const double never[GMG_MAX_S] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (k_copy(mg, x->prec, vlev(tb, level), vlev(bv, level), len) || k_set(mg, x->prec, vlev(x, level), len, 0.0))
+    return 1;
+  return k_base_solve(mg, mg->lev[level], x->prec, vlev(x, level), vlev(tb, level), vlev(tt, level), never);
+}
+
+// EXSmoother, iter.cc:8972-9068: x = A^{-1} b, x *= damp, b -= A x
+int NPEx::Iter(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, int *result) {
+  if (check_level(mg, level)) return 1;
+  bool unit = true;
+  for (int r = 0; r < mg->lev[level].s; ++r) unit = unit && damp[r] == 1.0;
+  if (!unit) return NPSmoother::Iter(level, x, bv, Am, result);
+  gmg_vec *tt = temp_vec(mg, "__ex_t" + std::to_string(x->prec), x->prec);
+  GMG_CHECK(tt, "ex: temporary vector");
+  const double never[GMG_MAX_S] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (k_set(mg, x->prec, vlev(x, level), vlen(mg, level), 0.0)) return 1;
+  return k_base_solve(mg, mg->lev[level], x->prec, vlev(x, level), vlev(bv, level), vlev(tt, level), never);
+}
+
+// ------------------------------------------------------------ transfer
+int NPTransfer::Init(const Args &a) {  // TransferInit / NPTransferInit
+  A = read_mat(mg, a, "A");
+  x = read_vec(mg, a, "x");
+  c = read_vec(mg, a, "c");
+  b = read_vec(mg, a, "b");
+  baselevel = 0;
+  a.get_int("baselevel", &baselevel);
+  for (double &d : damp) d = 1.0;
+  a.get_sc("damp", damp);
+  GMG_CHECK(!a.option("M") && !a.option("S") && !a.option("D"),
+            "transfer: only the standard (shape-function) mode is implemented");
+  return (!A && !b && !x && !c) ? NP_ACTIVE : NP_EXECUTABLE;
+}
+
+int NPTransfer::PreProcess(int *, int, gmg_vec *, gmg_vec *, gmg_mat *, int *) { return 0; }
+int NPTransfer::PostProcess(int *, int, gmg_vec *, gmg_vec *, gmg_mat *, int *) { return 0; }
+
+// RestrictDefect, transfer.cc:724: level -> level-1 with StandardRestrict
+int NPTransfer::RestrictDefect(int level, gmg_vec *to, gmg_vec *from, gmg_mat *, const double *dmp, int *result) {
+  if (check_level(mg, level)) return 1;
+  GMG_CHECK(level >= 1, "RestrictDefect: no coarser grid below level %d", level);
+  GMG_CHECK(to->prec == from->prec, "RestrictDefect: precision mismatch");
+  return k_restrict(mg, mg->lev[level], mg->lev[level - 1], to->prec, vlev(to, level - 1), vlev(from, level), dmp);
+}
+
+// InterpolateCorrection, transfer.cc:747: level-1 -> level with StandardInterpolateCorrection
+int NPTransfer::InterpolateCorrection(int level, gmg_vec *to, gmg_vec *from, gmg_mat *, const double *dmp,
+                                      int *result) {
+  if (check_level(mg, level)) return 1;
+  GMG_CHECK(level >= 1, "InterpolateCorrection: no coarser grid below level %d", level);
+  GMG_CHECK(to->prec == from->prec, "InterpolateCorrection: precision mismatch");
+  return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), dmp, nullptr);
+}
+
+int NPTransfer::Execute(const Args &a) {
+  const int level = int(mg->lev.size()) - 1;
+  int result = 0, fl = baselevel;
+  if (a.option("i") && PreProcess(&fl, level, x, b, A, &result)) return 1;
+  if (a.option("R")) {
+    GMG_CHECK(b, "transfer: no vector b");
+    if (RestrictDefect(level, b, b, A, damp, &result)) return 1;
+  }
+  if (a.option("I")) {
+    GMG_CHECK(c, "transfer: no vector c");
+    if (InterpolateCorrection(level, c, c, A, damp, &result)) return 1;
+  }
+  if (a.option("p") && PostProcess(&fl, level, x, b, A, &result)) return 1;
+  return 0;
+}
+
+std::string NPTransfer::Display() const {
+  return "class " + cls + "\nRestrict = StandardRestrict\nInterpolateCor = StandardInterpolateCorrection\n";
+}
+
+// ------------------------------------------------------------ lmgc
+int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
+  std::string tn;
+  Transfer = a.get_word("T", &tn) ? static_cast<NPTransfer *>(read_np(mg, tn, NPK_TRANSFER)) : nullptr;
+  for (auto &arg : a.argv) {
+    if (arg.empty() || arg[0] != 'S') continue;
+    char pre[256], post[256], base[256];
+    if (sscanf(arg.c_str(), "S %255s %255s %255s", pre, post, base) != 3) continue;
+    PreSmooth = static_cast<NPIter *>(read_np(mg, pre, NPK_ITER));
+    PostSmooth = static_cast<NPIter *>(read_np(mg, post, NPK_ITER));
+    BaseSolver = static_cast<NPLinearSolver *>(read_np(mg, base, NPK_LS));
+    break;
+  }
+  if (!a.get_int("g", &gamma)) gamma = 1;
+  if (!a.get_int("n1", &nu1)) nu1 = 1;
+  if (!a.get_int("n2", &nu2)) nu2 = 1;
+  if (!a.get_int("b", &baselevel)) baselevel = 0;
+  if (baselevel < 0) {  // $b -N: the finest level with at most N vectors
+    int i;
+    for (i = int(mg->lev.size()) - 1; i > 0; --i)
+      if (mg->lev[i].n <= -baselevel) break;
+    baselevel = i;
+  }
+  if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return NP_NOT_ACTIVE;
+  int ret = InitIter(a);
+  for (double &d : damp) d = 1.0;
+  a.get_sc("damp", damp);
+  return ret;
+}
+
+std::string NPLmgc::Display() const {
+  std::ostringstream o;
+  o << NPIter::Display() << "g = " << gamma << "\nn1 = " << nu1 << "\nn2 = " << nu2 << "\nbaselevel = " << baselevel
+    << "\nT = " << (Transfer ? Transfer->name : "---") << "\npre = " << (PreSmooth ? PreSmooth->name : "---")
+    << "\npost = " << (PostSmooth ? PostSmooth->name : "---") << "\nbase = " << (BaseSolver ? BaseSolver->name : "---")
+    << "\n";
+  return o.str();
+}
+
+bool NPLmgc::capturable() const {
+  if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return false;
+  const NPLs *bls = dynamic_cast<const NPLs *>(BaseSolver);
+  bool base_ok = (bls && bls->is_exact_base()) || (gamma == 0);
+  return base_ok && Transfer->capturable() && PreSmooth->capturable() && PostSmooth->capturable();
+}
+
+// LmgcPreProcess, iter.cc:7707-7739
+int NPLmgc::PreProcess(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, int *bl, int *result) {
+  if (Transfer->PreProcess(&baselevel, level, x, bv, Am, result)) return 1;
+  for (int i = baselevel + 1; i <= level; ++i)
+    if (PreSmooth->PreProcess(i, x, bv, Am, bl, result)) return 1;
+  if (PreSmooth != PostSmooth)
+    for (int i = baselevel + 1; i <= level; ++i)
+      if (PostSmooth->PreProcess(i, x, bv, Am, bl, result)) return 1;
+  *bl = std::min(baselevel, level);
+  if (gamma > 0 && BaseSolver->PreProcess(*bl, x, bv, Am, bl, result)) return 1;
+  return 0;
+}
+
+// Lmgc, iter.cc:7741-7949
+int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) {
+  if (check_level(mg, level)) return 1;
+  GMG_CHECK(cv->prec == bv->prec, "lmgc: c and b differ in precision");
+  const int prec = cv->prec;
+  if (level <= baselevel) {
+    NPLs *bls = dynamic_cast<NPLs *>(BaseSolver);
+    if (bls && bls->is_exact_base()) {
+      // `ls $m 1 $I ex`: one kernel with the solver's abslimit test on the device
+      gmg_vec *tt = temp_vec(mg, "__lmgc_base_t" + std::to_string(prec), prec);
+      GMG_CHECK(tt, "lmgc: temporary vector");
+      return k_base_solve(mg, mg->lev[level], prec, vlev(cv, level), vlev(bv, level), vlev(tt, level),
+                          BaseSolver->abslimit);
+    }
+    gmg_lresult lr{};
+    if (BaseSolver->Residuum(std::min(level, baselevel), level, cv, bv, Am, &lr)) return 1;
+    return BaseSolver->Solver(level, cv, bv, Am, BaseSolver->abslimit, BaseSolver->reduction, &lr);
+  }
+  gmg_vec *&t = prec == GMG_PREC_FP64 ? t64 : t32;
+  if (!t) t = temp_vec(mg, name + "__t" + std::to_string(prec), prec);
+  GMG_CHECK(t, "lmgc: temporary vector");
+  for (int i = 0; i < nu1; ++i)
+    if (PreSmooth->IterAcc(level, t, bv, Am, cv, result)) return 1;
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};  // Factor_One
+  if (Transfer->RestrictDefect(level, bv, bv, Am, one, result)) return 1;
+  if (k_set(mg, prec, vlev(cv, level - 1), vlen(mg, level - 1), 0.0)) return 1;
+  for (int i = 0; i < gamma; ++i)
+    if (Iter(level - 1, cv, bv, Am, result)) return 1;
+  // t = P c_{l-1} * damp; c += t (fused); b -= A t
+  if (dynamic_cast<NPTransfer *>(Transfer) && typeid(*Transfer) == typeid(NPTransfer)) {
+    if (k_interpolate(mg, mg->lev[level], prec, vlev(t, level), vlev(cv, level - 1), damp, vlev(cv, level))) return 1;
+  } else {
+    if (Transfer->InterpolateCorrection(level, t, cv, Am, damp, result)) return 1;
+    if (k_add(mg, prec, vlev(cv, level), vlev(t, level), vlen(mg, level))) return 1;
+  }
+  if (k_matmul_minus(mg, mg->lev[level], prec, vlev(bv, level), vlev(t, level), nullptr)) return 1;
+  for (int i = 0; i < nu2; ++i)
+    if (PostSmooth->IterAcc(level, t, bv, Am, cv, result)) return 1;
+  return 0;
+}
+
+// LmgcPostProcess, iter.cc:7951
+int NPLmgc::PostProcess(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, int *result) {
+  if (gamma > 0 && BaseSolver->PostProcess(baselevel, x, bv, Am, result)) return 1;
+  if (PreSmooth != PostSmooth)
+    for (int i = level; i >= baselevel + 1; --i)
+      if (PostSmooth->PostProcess(i, x, bv, Am, result)) return 1;
+  for (int i = level; i >= baselevel + 1; --i)
+    if (PreSmooth->PostProcess(i, x, bv, Am, result)) return 1;
+  int fl = baselevel;
+  return Transfer->PostProcess(&fl, level, x, bv, Am, result);
+}
+
+// ------------------------------------------------------------ linear solver
+int NPLinearSolver::InitLS(const Args &a) {  // NPLinearSolverInit, ls.cc:382
+  A = read_mat(mg, a, "A");
+  x = read_vec(mg, a, "x");
+  b = read_vec(mg, a, "b");
+  if (!a.get_sc("abslimit", abslimit))
+    for (double &d : abslimit) d = 1e-10;  // ABS_LIMIT, ls.cc:66
+  if (!a.get_sc("red", reduction)) return NP_ACTIVE;
+  if (!x || !b || !A) return NP_ACTIVE;
+  return NP_EXECUTABLE;
+}
+
+// NPLinearSolverExecute, ls.cc:436-537
+int NPLinearSolver::Execute(const Args &a) {
+  const int level = int(mg->lev.size()) - 1;
+  int result = 0, bl = 0;
+  GMG_CHECK(x && b && A, "NPLinearSolverExecute: x, b or A missing");
+  gmg_lresult lr{};
+  if (a.option("i") && PreProcess(level, x, b, A, &bl, &result)) return 1;
+  if (a.option("d") && Defect(level, x, b, A, &result)) return 1;
+  if (a.option("r") && Residuum(bl, level, x, b, A, &lr)) return 1;
+  if (a.option("s") && Solver(level, x, b, A, abslimit, reduction, &lr)) return 1;
+  if (a.option("p") && PostProcess(level, x, b, A, &result)) return 1;
+  return 0;
+}
+
+NPLs::~NPLs() {
+  if (graph) cudaGraphExecDestroy(graph);
+}
+
+int NPLs::Init(const Args &a) {  // LinearSolverInit, ls.cc:788
+  if (!a.get_int("m", &maxiter)) return NP_NOT_ACTIVE;
+  std::string itn;
+  IterNp = a.get_word("I", &itn) ? static_cast<NPIter *>(read_np(mg, itn, NPK_ITER)) : nullptr;
+  if (!IterNp) return NP_NOT_ACTIVE;
+  baselevel = 0;
+  cvec = read_vec(mg, a, "c");
+  std::string d;
+  display = a.get_word("d", &d) ? (d == "full" ? 2 : d == "red" ? 1 : 0) : 0;
+  if (!a.get_int("mixed", &mixed)) mixed = 0;
+  if (!a.get_int("graph", &use_graph)) use_graph = 1;
+  if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+  return InitLS(a);
+}
+
+std::string NPLs::Display() const {
+  std::ostringstream o;
+  o << "class " << cls << "\nm = " << maxiter << "\nbaselevel = " << baselevel
+    << "\nIter = " << (IterNp ? IterNp->name : "---") << "\nmixed = " << mixed << "\nred = "
+    << fmt_sc(reduction, 1) << "\nabslimit = " << fmt_sc(abslimit, 1) << "\n";
+  return o.str();
+}
+
+bool NPLs::is_exact_base() const {
+  if (maxiter != 1 || !IterNp) return false;
+  const NPEx *ex = dynamic_cast<const NPEx *>(IterNp);
+  if (!ex) return false;
+  for (int r = 0; r < GMG_MAX_S; ++r)
+    if (ex->damp[r] != 1.0) return false;
+  return true;
+}
+
+// LinearSolverPreProcess, ls.cc:539
+int NPLs::PreProcess(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *bl, int *result) {
+  if (IterNp->PreProcess(level, xv, bv, Am, bl, result)) return 1;
+  baselevel = std::min(*bl, level);
+  preprocessed = true;
+  return 0;
+}
+
+// LinearDefect, ls.cc:562: b -= A x on the surface, which is the top level
+// of a uniformly refined hierarchy
+int NPLs::Defect(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *, int *) {
+  if (check_level(mg, level)) return 1;
+  if (bv->prec == GMG_PREC_FP64)
+    return k_matmul_minus_mixed(mg, mg->lev[level], (double *)vlev(bv, level), xv->prec, vlev(xv, level));
+  GMG_CHECK(xv->prec == bv->prec, "ls: precision mismatch");
+  return k_matmul_minus(mg, mg->lev[level], bv->prec, vlev(bv, level), vlev(xv, level), nullptr);
+}
+
+// LinearResiduum, ls.cc:577: per-component norms of b
+int NPLs::Residuum(int, int tl, gmg_vec *, gmg_vec *bv, gmg_mat *, gmg_lresult *lr) {
+  if (check_level(mg, tl)) return 1;
+  const int s = mg->lev[tl].s;
+  if (k_nrm2x(mg, mg->lev[tl], bv->prec, vlev(bv, tl))) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
+  return 0;
+}
+
+// the body of one ls iteration (ls.cc:694-701), enqueued without host work:
+// dset(c, 0); Iter(c, b); LSUpdate x += c; norm of b into mg->norms_dev.
+// Mixed: the iteration runs on FP32 copies (b32 = b; c32) and the FP64 defect
+// is updated as b -= A c with the FP64 matrix (iterative refinement).
+int NPLs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const Level &L = mg->lev[level];
+  const long long len = vlen(mg, level);
+  if (!mixed) {
+    if (k_set(mg, cvec->prec, vlev(cvec, level), len, 0.0)) return 1;
+    if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
+    if (xv->prec == GMG_PREC_FP64) {
+      if (k_add_mixed(mg, (double *)vlev(xv, level), cvec->prec, vlev(cvec, level), len)) return 1;
+    } else if (k_add(mg, xv->prec, vlev(xv, level), vlev(cvec, level), len)) {
+      return 1;
+    }
+  } else {
+    if (k_convert(mg, GMG_PREC_FP32, vlev(b32, level), bv->prec, vlev(bv, level), len)) return 1;
+    if (k_set(mg, GMG_PREC_FP32, vlev(cvec, level), len, 0.0)) return 1;
+    if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    if (k_add_mixed(mg, (double *)vlev(xv, level), GMG_PREC_FP32, vlev(cvec, level), len)) return 1;
+    if (k_matmul_minus_mixed(mg, L, (double *)vlev(bv, level), GMG_PREC_FP32, vlev(cvec, level))) return 1;
+  }
+  if (k_nrm2x(mg, L, bv->prec, vlev(bv, level))) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
+  return 0;
+}
+
+static int sc_cmp(const double *x, const double *y, int s) {  // npscan.cc:1027
+  for (int i = 0; i < s; ++i)
+    if (std::fabs(x[i]) >= std::fabs(y[i])) return 0;
+  return 1;
+}
+
+// LinearSolver, ls.cc:637-749
+int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double *abs_, const double *red,
+                 gmg_lresult *lr) {
+  if (check_level(mg, level)) return 1;
+  const int s = mg->lev[level].s;
+  for (int i = 0; i < GMG_MAX_S; ++i) { reduction[i] = red[i]; abslimit[i] = abs_[i]; }
+  GMG_CHECK(!mixed || (xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64 && mg->opts.fp32_copy),
+            "ls $mixed needs FP64 x and b and a hierarchy with FP32 copies");
+  const int cprec = mixed ? GMG_PREC_FP32 : bv->prec;
+  if (!cvec || cvec->prec != cprec) cvec = temp_vec(mg, name + "__c" + std::to_string(cprec), cprec);
+  if (mixed && !b32) b32 = temp_vec(mg, name + "__b32", GMG_PREC_FP32);
+  GMG_CHECK(cvec && (!mixed || b32), "ls: temporary vectors");
+  double reach[GMG_MAX_S];
+  for (int i = 0; i < s; ++i) {
+    lr->first_defect[i] = lr->last_defect[i];
+    reach[i] = lr->first_defect[i] * red[i];  // sc_mul_check, npscan.cc:1151
+    if (reach[i] == 0.0) reach[i] = red[i];
+  }
+  lr->converged = sc_cmp(lr->first_defect, abs_, s);
+  lr->number_of_linear_iterations = 0;
+  const bool graph_ok = use_graph && IterNp->capturable();
+  if (graph && (graph_level != level || graph_x != xv || graph_b != bv)) {
+    cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
+  int i;
+  for (i = 0; i < maxiter; ++i) {
+    if (lr->converged) break;
+    int err = 0;
+    // the first iteration runs eagerly (it creates the numprocs' temporaries);
+    // the following ones replay one captured graph of the iteration
+    if (graph_ok && (graph || i > 0)) {
+      if (!graph) {
+        cudaGraph_t g;
+        const long long before = mg->launches;
+        GMG_CUDA(cudaStreamBeginCapture(mg->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = iteration(level, xv, bv, Am, &err);
+        cudaError_t ce = cudaStreamEndCapture(mg->stream, &g);
+        if (rc) { if (ce == cudaSuccess) cudaGraphDestroy(g); return 1; }
+        GMG_CUDA(ce);
+        GMG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+        cudaGraphDestroy(g);
+        graph_level = level; graph_x = xv; graph_b = bv;
+        graph_kernels = mg->launches - before;  // captured, not yet run
+        mg->launches = before;
+      }
+      GMG_CUDA(cudaGraphLaunch(graph, mg->stream));
+      mg->launches += graph_kernels;
+    } else if (iteration(level, xv, bv, Am, &err)) {
+      lr->error_code = err;
+      return 1;
+    }
+    GMG_CUDA(cudaStreamSynchronize(mg->stream));
+    for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
+    for (int r = 0; r < s; ++r)
+      GMG_CHECK(std::isfinite(lr->last_defect[r]), "ls: defect is not finite in iteration %d", i + 1);
+    if (sc_cmp(lr->last_defect, abs_, s) || sc_cmp(lr->last_defect, reach, s)) {
+      lr->converged = 1;
+      lr->number_of_linear_iterations = i + 1;
+      break;
+    }
+  }
+  if (!lr->converged) lr->number_of_linear_iterations = i;
+  return 0;
+}
+
+int NPLs::PostProcess(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *result) {
+  if (IterNp && IterNp->PostProcess(level, xv, bv, Am, result)) return 1;
+  return 0;
+}
+
+// ------------------------------------------------------------ class registry (CreateClass)
+static gmg_np *construct(const std::string &cls) {
+  // the class name's last component selects the constructor (GetConstructor, numproc.cc:145)
+  std::string c = cls.substr(cls.rfind('.') == std::string::npos ? 0 : cls.rfind('.') + 1);
+  if (c == "gjac") return new NPJac;
+  if (c == "ggs") return new NPGs;
+  if (c == "gilu") return new NPIlu;
+  if (c == "gex") return new NPEx;
+  if (c == "glmgc") return new NPLmgc;
+  if (c == "gtransfer") return new NPTransfer;
+  if (c == "gls") return new NPLs;
+  return nullptr;
+}
+
+}  // namespace gmg
+
+using namespace gmg;
+
+// ============================================================ C ABI
+extern "C" {
+
+int gmg_vec_create(gmg_mg *mg, const char *name, int precision, gmg_vec **out) {
+  if (!mg || !name) { set_error("gmg_vec_create: bad arguments"); return 1; }
+  GMG_CHECK(precision == GMG_PREC_FP64 || (precision == GMG_PREC_FP32), "bad precision %d", precision);
+  GMG_CHECK(!mg->vecs.count(name), "vector %s exists", name);
+  gmg_vec *v = temp_vec(mg, name, precision);
+  if (!v) return 1;
+  if (out) *out = v;
+  return 0;
+}
+
+gmg_vec *gmg_vec_by_name(gmg_mg *mg, const char *name) {
+  if (!mg || !name) return nullptr;
+  auto it = mg->vecs.find(name);
+  return it == mg->vecs.end() ? nullptr : it->second.get();
+}
+
+gmg_mat *gmg_mat_by_name(gmg_mg *mg, const char *name) {
+  if (!mg || !name) return nullptr;
+  auto it = mg->mats.find(name);
+  return it == mg->mats.end() ? nullptr : it->second.get();
+}
+
+int gmg_vec_upload(gmg_vec *v, int level, const double *host) {
+  if (!v || !host) { set_error("gmg_vec_upload: bad arguments"); return 1; }
+  gmg_mg *mg = v->mg;
+  if (check_level(mg, level)) return 1;
+  const Level &L = mg->lev[level];
+  const size_t len = size_t(L.n) * L.s;
+  std::memcpy(mg->stage_host, host, len * sizeof(double));
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+  if (k_gather(mg, v->prec, vlev(v, level), (const double *)mg->stage_dev, L.perm_dev, L.n, L.s)) return 1;
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  return 0;
+}
+
+int gmg_vec_download(gmg_vec *v, int level, double *host) {
+  if (!v || !host) { set_error("gmg_vec_download: bad arguments"); return 1; }
+  gmg_mg *mg = v->mg;
+  if (check_level(mg, level)) return 1;
+  const Level &L = mg->lev[level];
+  const size_t len = size_t(L.n) * L.s;
+  if (k_scatter(mg, v->prec, (double *)mg->stage_dev, vlev(v, level), L.perm_dev, L.n, L.s)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, len * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  std::memcpy(host, mg->stage_host, len * sizeof(double));
+  return 0;
+}
+
+int gmg_vec_device_ptr(gmg_vec *v, int level, void **ptr) {
+  if (!v || !ptr) { set_error("gmg_vec_device_ptr: bad arguments"); return 1; }
+  if (check_level(v->mg, level)) return 1;
+  *ptr = v->lev[level];
+  return 0;
+}
+
+int gmg_np_create(gmg_mg *mg, const char *objname, const char *classname) {
+  if (!mg || !objname || !classname) { set_error("gmg_np_create: bad arguments"); return 1; }
+  gmg_np *np = construct(classname);
+  GMG_CHECK(np, "no numproc class %s", classname);
+  np->mg = mg;
+  np->name = objname;
+  np->cls = classname;
+  mg->nps[objname].reset(np);
+  return 0;
+}
+
+int gmg_np_init(gmg_mg *mg, const char *objname, const char *args, int *status) {
+  gmg_np *np = gmg_np_by_name(mg, objname);
+  GMG_CHECK(np, "no numproc %s", objname ? objname : "(null)");
+  np->status = np->Init(Args(args));
+  if (status) *status = np->status;
+  return np->status == NP_NOT_ACTIVE ? 1 : 0;
+}
+
+int gmg_np_execute(gmg_mg *mg, const char *objname, const char *args) {
+  gmg_np *np = gmg_np_by_name(mg, objname);
+  GMG_CHECK(np, "no numproc %s", objname ? objname : "(null)");
+  GMG_CHECK(np->status == NP_EXECUTABLE, "numproc %s is not executable", objname);
+  return np->Execute(Args(args));
+}
+
+gmg_np *gmg_np_by_name(gmg_mg *mg, const char *objname) {
+  if (!mg || !objname) return nullptr;
+  auto it = mg->nps.find(objname);
+  return it == mg->nps.end() ? nullptr : it->second.get();
+}
+
+int gmg_np_display(gmg_np *np, char *buf, int buflen) {
+  if (!np || !buf || buflen <= 0) return 1;
+  std::string s = np->Display();
+  snprintf(buf, buflen, "%s", s.c_str());
+  return 0;
+}
+
+#define AS(T, np, k)                                                  \
+  T *p = (np && np->kind() == k) ? static_cast<T *>(np) : nullptr;    \
+  if (!p) { set_error("%s: numproc of the wrong class", __func__); return 1; }
+
+int gmg_iter_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *bl, int *result) {
+  AS(NPIter, np, NPK_ITER);
+  int dummy;
+  return p->PreProcess(level, x, b, A, bl ? bl : &dummy, result ? result : &dummy);
+}
+int gmg_iter_iter(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPIter, np, NPK_ITER);
+  int dummy;
+  return p->Iter(level, c, b, A, result ? result : &dummy);
+}
+int gmg_iter_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPIter, np, NPK_ITER);
+  int dummy;
+  return p->PostProcess(level, x, b, A, result ? result : &dummy);
+}
+int gmg_transfer_preprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy = 0, f0 = 0;
+  return p->PreProcess(fl ? fl : &f0, tl, x, b, A, result ? result : &dummy);
+}
+int gmg_transfer_restrict_defect(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A, const double *damp,
+                                 int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy;
+  return p->RestrictDefect(level, to, from, A, damp ? damp : p->damp, result ? result : &dummy);
+}
+int gmg_transfer_interpolate_correction(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A,
+                                        const double *damp, int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy;
+  return p->InterpolateCorrection(level, to, from, A, damp ? damp : p->damp, result ? result : &dummy);
+}
+int gmg_transfer_postprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy = 0, f0 = 0;
+  return p->PostProcess(fl ? fl : &f0, tl, x, b, A, result ? result : &dummy);
+}
+int gmg_ls_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *bl, int *result) {
+  AS(NPLinearSolver, np, NPK_LS);
+  int dummy = 0;
+  return p->PreProcess(level, x, b, A, bl ? bl : &dummy, result ? result : &dummy);
+}
+int gmg_ls_defect(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPLinearSolver, np, NPK_LS);
+  int dummy;
+  return p->Defect(level, x, b, A, result ? result : &dummy);
+}
+int gmg_ls_residuum(gmg_np *np, int fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr) {
+  AS(NPLinearSolver, np, NPK_LS);
+  GMG_CHECK(lr, "gmg_ls_residuum: lr is NULL");
+  return p->Residuum(fl, tl, x, b, A, lr);
+}
+int gmg_ls_solver(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
+                  const double *reduction, gmg_lresult *lr) {
+  AS(NPLinearSolver, np, NPK_LS);
+  GMG_CHECK(lr, "gmg_ls_solver: lr is NULL");
+  return p->Solver(level, x, b, A, abslimit ? abslimit : p->abslimit, reduction ? reduction : p->reduction, lr);
+}
+int gmg_ls_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPLinearSolver, np, NPK_LS);
+  int dummy;
+  return p->PostProcess(level, x, b, A, result ? result : &dummy);
+}
+
+// ------------------------------------------------ level kernels
+#define MGV(mg, level)                                        \
+  if (!mg) { set_error("%s: no multigrid", __func__); return 1; } \
+  if (check_level(mg, level)) return 1;
+
+int gmg_dset(gmg_mg *mg, int level, gmg_vec *x, double a) {
+  MGV(mg, level);
+  return k_set(mg, x->prec, vlev(x, level), vlen(mg, level), a);
+}
+int gmg_dcopy(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y) {
+  MGV(mg, level);
+  return k_convert(mg, x->prec, vlev(x, level), y->prec, vlev(y, level), vlen(mg, level));
+}
+int gmg_dadd(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y) {
+  MGV(mg, level);
+  if (x->prec == GMG_PREC_FP64) return k_add_mixed(mg, (double *)vlev(x, level), y->prec, vlev(y, level), vlen(mg, level));
+  GMG_CHECK(y->prec == x->prec, "dadd: precision mismatch");
+  return k_add(mg, x->prec, vlev(x, level), vlev(y, level), vlen(mg, level));
+}
+int gmg_dmatmul_minus(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) {
+  MGV(mg, level);
+  if (x->prec == GMG_PREC_FP64) return k_matmul_minus_mixed(mg, mg->lev[level], (double *)vlev(x, level), y->prec, vlev(y, level));
+  GMG_CHECK(y->prec == x->prec, "dmatmul_minus: precision mismatch");
+  return k_matmul_minus(mg, mg->lev[level], x->prec, vlev(x, level), vlev(y, level), nullptr);
+}
+int gmg_dnrm2x(gmg_mg *mg, int level, gmg_vec *x, double *norms) {
+  MGV(mg, level);
+  if (k_nrm2x(mg, mg->lev[level], x->prec, vlev(x, level))) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * mg->lev[level].s, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  for (int r = 0; r < mg->lev[level].s; ++r) norms[r] = mg->norms_host[r];
+  return 0;
+}
+int gmg_l_jac(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
+  MGV(mg, level);
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
+  return k_jac(mg, mg->lev[level], v->prec, vlev(v, level), vlev(d, level), one);
+}
+int gmg_l_lgs(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
+  MGV(mg, level);
+  return k_gs(mg, mg->lev[level], v->prec, vlev(v, level), vlev(d, level));
+}
+int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *, const double *beta) {
+  MGV(mg, level);
+  NPIlu tmp;
+  tmp.mg = mg;
+  for (int i = 0; i < GMG_MAX_S; ++i) tmp.beta[i] = beta ? beta[i] : 0.0;
+  mg->lev[level].ilu_ready = false;
+  int bl = 0, res = 0;
+  return tmp.PreProcess(level, nullptr, nullptr, nullptr, &bl, &res);
+}
+int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
+  MGV(mg, level);
+  return k_luiter(mg, mg->lev[level], v->prec, vlev(v, level), vlev(d, level));
+}
+int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
+  MGV(mg, level);
+  GMG_CHECK(level >= 1, "no coarser grid");
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
+  return k_restrict(mg, mg->lev[level], mg->lev[level - 1], to->prec, vlev(to, level - 1), vlev(from, level),
+                    damp ? damp : one);
+}
+int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
+  MGV(mg, level);
+  GMG_CHECK(level >= 1, "no coarser grid");
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
+  return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), damp ? damp : one, nullptr);
+}
+
+int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double *x_host, gmg_lresult *lr) {
+  if (!mg || !solver || !b_host || !x_host || !lr) { set_error("gmg_solve_host: bad arguments"); return 1; }
+  gmg_np *np = gmg_np_by_name(mg, solver);
+  GMG_CHECK(np && np->kind() == NPK_LS, "no linear solver %s", solver);
+  NPLinearSolver *ls = static_cast<NPLinearSolver *>(np);
+  NPLs *gls = dynamic_cast<NPLs *>(ls);
+  GMG_CHECK(ls->x && ls->b && ls->A, "solver %s has no x, b or A", solver);
+  const int top = int(mg->lev.size()) - 1;
+  int bl = 0, res = 0;
+  if (!(gls && gls->preprocessed) && ls->PreProcess(top, ls->x, ls->b, ls->A, &bl, &res)) return 1;
+  *lr = gmg_lresult{};
+  if (gmg_vec_upload(ls->b, top, b_host)) return 1;
+  if (k_set(mg, ls->x->prec, vlev(ls->x, top), vlen(mg, top), 0.0)) return 1;
+  if (ls->Defect(top, ls->x, ls->b, ls->A, &res)) return 1;
+  if (ls->Residuum(gls ? gls->baselevel : 0, top, ls->x, ls->b, ls->A, lr)) return 1;
+  if (ls->Solver(top, ls->x, ls->b, ls->A, ls->abslimit, ls->reduction, lr)) return 1;
+  return gmg_vec_download(ls->x, top, x_host);
+}
+
+}  // extern "C"

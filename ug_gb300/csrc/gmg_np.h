@@ -1,0 +1,179 @@
+// Numproc classes of the GB300 lmgc path: C++ mirrors of UG's NP_BASE /
+// NP_ITER / NP_TRANSFER / NP_LINEAR_SOLVER objects (np/udm/numproc.h:75-87,
+// np/procs/iter.h:68-101, transfer.h:79-166, ls.h:79-132) whose methods
+// enqueue CUDA kernels on the multigrid's stream instead of walking VECTOR
+// lists.  Argument parsing follows npinit's `$name value` syntax.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "gmg_internal.h"
+
+// numproc status (np/udm/numproc.h:54-57)
+enum { NP_NOT_INIT = 0, NP_NOT_ACTIVE = 1, NP_ACTIVE = 2, NP_EXECUTABLE = 3 };
+enum { NPK_ITER = 1, NPK_TRANSFER = 2, NPK_LS = 3 };
+
+namespace gmg {
+
+// npinit / npexecute arguments: "$A MAT $x sol $red 1e-10 $i" -> {"A MAT", "x sol", "red 1e-10", "i"}
+struct Args {
+  std::vector<std::string> argv;
+  explicit Args(const char *s);
+  const std::string *find(const char *name) const;     // argument whose first word is name
+  bool option(const char *name) const { return find(name) != nullptr; }
+  bool get_int(const char *name, int *v) const;
+  bool get_double(const char *name, double *v) const;
+  bool get_word(const char *name, std::string *v) const;
+  // sc_read (np/udm/npscan.cc): "$damp 0.8" (all components) or "$damp 0.8:0.5" [nd prefix allowed]
+  bool get_sc(const char *name, double *v) const;
+};
+
+}  // namespace gmg
+
+struct gmg_np {
+  gmg_mg *mg = nullptr;
+  std::string name, cls;
+  int status = NP_NOT_INIT;
+  virtual ~gmg_np() = default;
+  virtual int kind() const = 0;
+  virtual int Init(const gmg::Args &a) = 0;  // returns the status
+  virtual std::string Display() const { return "class " + cls + "\n"; }
+  virtual int Execute(const gmg::Args &a) = 0;
+  // true when every call enqueues device work only (no host synchronisation),
+  // so a whole cycle can be captured into a CUDA graph
+  virtual bool capturable() const { return true; }
+};
+
+namespace gmg {
+
+struct NPIter : gmg_np {
+  gmg_vec *c = nullptr, *b = nullptr;
+  gmg_mat *A = nullptr;
+  int kind() const override { return NPK_ITER; }
+  int InitIter(const Args &a);  // NPIterInit, iter.cc:674
+  virtual int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result);
+  virtual int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) = 0;
+  virtual int PostProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+  // Iter followed by acc += c (lmgc's dadd after each smoothing step);
+  // smoothers fuse the addition into their defect update
+  virtual int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result);
+  int Execute(const Args &a) override;  // NPIterExecute, iter.cc:702
+  std::string Display() const override;
+};
+
+// NP_SMOOTHER, iter.cc:152-177: Step, then dscalx(damp), then b -= A x
+struct NPSmoother : NPIter {
+  double damp[GMG_MAX_S];
+  int Init(const Args &a) override;  // SmootherInit, iter.cc:763
+  virtual int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) = 0;
+  int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) override;  // Smoother, iter.cc:817
+  int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result) override;
+  std::string Display() const override;
+};
+
+struct NPJac : NPSmoother {  // jac, iter.cc:894-942
+  int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) override;
+  int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result) override;
+};
+
+struct NPGs : NPSmoother {  // gs, iter.cc:974-1086
+  int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+};
+
+struct NPIlu : NPSmoother {  // ilu, iter.cc:5383-5524
+  double beta[GMG_MAX_S];
+  int Init(const Args &a) override;
+  int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) override;
+  int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  std::string Display() const override;
+};
+
+struct NPEx : NPSmoother {  // ex, iter.cc:8218-9130 (exact solve on one level)
+  int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) override;
+  int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) override;
+};
+
+struct NPTransfer : gmg_np {
+  gmg_vec *x = nullptr, *c = nullptr, *b = nullptr;
+  gmg_mat *A = nullptr;
+  double damp[GMG_MAX_S];
+  int baselevel = 0;
+  int kind() const override { return NPK_TRANSFER; }
+  int Init(const Args &a) override;  // TransferInit + NPTransferInit, transfer.cc:553, 296
+  virtual int PreProcess(int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+  virtual int RestrictDefect(int level, gmg_vec *to, gmg_vec *from, gmg_mat *A, const double *damp, int *result);
+  virtual int InterpolateCorrection(int level, gmg_vec *to, gmg_vec *from, gmg_mat *A, const double *damp,
+                                    int *result);
+  virtual int PostProcess(int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+  int Execute(const Args &a) override;
+  std::string Display() const override;
+};
+
+struct NPLinearSolver;
+
+struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
+  int gamma = 1, nu1 = 1, nu2 = 1, baselevel = 0;
+  NPTransfer *Transfer = nullptr;
+  NPIter *PreSmooth = nullptr, *PostSmooth = nullptr;
+  NPLinearSolver *BaseSolver = nullptr;
+  double damp[GMG_MAX_S];
+  gmg_vec *t64 = nullptr, *t32 = nullptr;  // the temporary t of Lmgc (AllocVDFromVD)
+  int Init(const Args &a) override;
+  int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) override;
+  int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) override;
+  int PostProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  bool capturable() const override;
+  std::string Display() const override;
+};
+
+struct NPLinearSolver : gmg_np {
+  gmg_vec *x = nullptr, *b = nullptr;
+  gmg_mat *A = nullptr;
+  double reduction[GMG_MAX_S], abslimit[GMG_MAX_S];
+  int kind() const override { return NPK_LS; }
+  int InitLS(const Args &a);  // NPLinearSolverInit, ls.cc:382
+  virtual int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) = 0;
+  virtual int Defect(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) = 0;
+  virtual int Residuum(int fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr) = 0;
+  virtual int Solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
+                     const double *reduction, gmg_lresult *lr) = 0;
+  virtual int PostProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) = 0;
+  int Execute(const Args &a) override;  // NPLinearSolverExecute, ls.cc:436
+};
+
+// ls, np/procs/ls.cc:79-109, 539-900.  $mixed 1 runs the iteration's
+// vectors in FP32 inside FP64 iterative refinement.
+struct NPLs : NPLinearSolver {
+  int maxiter = 0, baselevel = 0, display = 0, mixed = 0, use_graph = 1;
+  NPIter *IterNp = nullptr;
+  gmg_vec *cvec = nullptr;                   // correction c (precision of x, or FP32 in mixed mode)
+  gmg_vec *b32 = nullptr;                    // FP32 defect in mixed mode
+  bool preprocessed = false;
+  // CUDA graph of one iteration (dset c; Iter; update; norm)
+  cudaGraphExec_t graph = nullptr;
+  int graph_level = -1;
+  gmg_vec *graph_x = nullptr, *graph_b = nullptr;
+  long long graph_kernels = 0;  // kernels per replay (for the launch counter)
+  ~NPLs() override;
+  int Init(const Args &a) override;
+  int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) override;
+  int Defect(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  int Residuum(int fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr) override;
+  int Solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit, const double *reduction,
+             gmg_lresult *lr) override;
+  int PostProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  bool capturable() const override { return false; }
+  std::string Display() const override;
+  // one iteration without the host-side test: dset c, Iter, update x, norm into mg->norms_dev
+  int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
+  // the base-solver shortcut of lmgc: `ls $m 1 $I ex` as one kernel
+  bool is_exact_base() const;
+};
+
+// helpers shared by the numprocs and the C ABI
+gmg_vec *temp_vec(gmg_mg *mg, const std::string &name, int prec);
+void *vlev(gmg_vec *v, int level);
+
+}  // namespace gmg
