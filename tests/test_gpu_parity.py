@@ -81,12 +81,15 @@ def test_kernels_match_ug(G, oracle_mod, name, order):
     mg.close()
 
 
+@pytest.mark.parametrize("fuse", [0, None])
 @pytest.mark.parametrize("name", NAMES)
-def test_solve_matches_ug(G, name):
+def test_solve_matches_ug(G, name, fuse):
+    """fuse=0: one kernel per level operation; None: the small levels run as
+    one fused cluster kernel (here the whole hierarchy)."""
     fx = load_golden(name)
     mg, _ = _setup(G, fx, 0)
     sm = fx["smoother"]
-    G.setup_lmgc(mg, sm, baselevel=int(fx["baselevel"][0]), damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    G.setup_lmgc(mg, sm, baselevel=int(fx["baselevel"][0]), damp=_damp(sm), red=1e-10, abslimit=1e-50, fuse=fuse)
     x, lr = mg.solve_host("mgs", fx["rhs"])
     it_ug = int(fx["ls_iters"][0])
     assert lr.converged
@@ -103,13 +106,14 @@ def test_solve_matches_ug(G, name):
     mg.close()
 
 
+@pytest.mark.parametrize("fuse", [0, None])
 @pytest.mark.parametrize("name", NAMES)
-def test_solve_multicolour_matches_oracle(G, oracle_mod, name):
+def test_solve_multicolour_matches_oracle(G, oracle_mod, name, fuse):
     fx = load_golden(name)
     mg, levels = _setup(G, fx, 1)
     sm = fx["smoother"]
     bl = int(fx["baselevel"][0])
-    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50, fuse=fuse)
     x, lr = mg.solve_host("mgs", fx["rhs"])
     H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
     top = mg.top

@@ -64,6 +64,7 @@ struct DevCSR {
 // wavefront schedule: rows[ptr[w]..ptr[w+1]) are independent
 struct Sched {
   std::vector<int> ptr;
+  int *ptr_dev = nullptr;  // device copy of ptr (fused coarse cycle)
   int *rows = nullptr;
   int nwave() const { return ptr.empty() ? 0 : int(ptr.size()) - 1; }
 };
@@ -175,6 +176,12 @@ int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void 
 int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x);
 // base level: if |b| >= abslimit in some component: t = Ainv b; b -= A t; c += t
 int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit);
+// the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
+struct CoarseCfg {
+  int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;
+  double damp[GMG_MAX_S], cdamp[GMG_MAX_S], abslimit[GMG_MAX_S];
+};
+int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t);
 // permutations between UG list order and processing order
 int k_gather(gmg_mg *mg, int prec, void *dst, const double *src_list, const int *perm, int n, int s);
 int k_scatter(gmg_mg *mg, int prec, double *dst_list, const void *src, const int *perm, int n, int s);

@@ -146,10 +146,9 @@ __global__ void jac_kernel(int n, const T *__restrict__ dinv, const uint8_t *__r
 }
 
 // ------------------------------------------------------------ l_lgs
-// ugiter.cc:412: forward solve (D+L) t = b in processing order.  Rows of one
-// wavefront depend only on rows of earlier wavefronts; t is zero before the
-// sweep, so summing every off-diagonal entry picks up exactly the rows that
-// precede the current one (later rows still hold 0).  Inactive rows stay 0.
+// ugiter.cc:412: forward solve (D+L) t = b in processing order: row i uses
+// the entries to rows j < i (VINDEX(w) < VINDEX(v)), all of which belong to
+// earlier wavefronts and are final.  Inactive rows get 0.
 template <class T, int S, int TPR, bool ALL_ACTIVE>
 __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ rows, int nrows,
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
@@ -160,7 +159,8 @@ __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ ro
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
   const int row = valid ? __ldg(rows + idx) : 0;
-  const bool work = valid && (ALL_ACTIVE || (flags[row] & F_ACTIVE));
+  const bool active = ALL_ACTIVE || (valid && (flags[row] & F_ACTIVE));
+  const bool work = valid && active;
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ ro
     const int k1 = __ldg(rowptr + row + 1);
     for (int k = __ldg(rowptr + row) + 1 + lane; k < k1; k += TPR) {
       const int j = __ldg(col + k);
+      if (j >= row) continue;
       const T *m = val + (size_t)k * (S * S);
       T yv[S];
 #pragma unroll
@@ -180,6 +181,10 @@ __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ ro
   }
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+  if (valid && !active && lane == 0) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) t[(size_t)row * S + r] = T(0);
+  }
   if (work && lane == 0) {
     T rhs[S];
 #pragma unroll
@@ -674,7 +679,6 @@ int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const do
 
 int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
   if (L.n == 0) return 0;
-  if (k_set(mg, prec, t, (long long)L.n * L.s, 0.0)) return 1;
   const int tp = tri_tpr(L);
 #define GS(TT, SS)                                                                      \
   return tp == 4 ? gs_waves<TT, SS, 4>(mg, L, (TT *)t, (const TT *)b)                   \

@@ -369,6 +369,7 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
     size_t nnz = h.rowptr[h.n], ss = size_t(s) * s;
     bytes += al((h.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * 8) + (f32 ? al(nnz * ss * 4) : 0);
     bytes += al(h.n * ss * 8) + (f32 ? al(h.n * ss * 4) : 0) + 2 * al(h.n) + 3 * al(h.n * 4);
+    bytes += al(h.lptr.size() * 4) + al(h.uptr.size() * 4);
     if (l > 0) {
       size_t pn = h.pcol.size(), rn = h.rcol.size();
       bytes += al((h.n + 1) * 4) + al(pn * 4) + al(pn * 8) + (f32 ? al(pn * 4) : 0);
@@ -411,6 +412,10 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
     L.upper.rows = mg->arena.take_n<int>(h.n);
     L.lower.ptr = h.lptr;
     L.upper.ptr = h.uptr;
+    L.lower.ptr_dev = mg->arena.take_n<int>(h.lptr.size());
+    L.upper.ptr_dev = mg->arena.take_n<int>(h.uptr.size());
+    if (upload(L.lower.ptr_dev, h.lptr.data(), h.lptr.size()) || upload(L.upper.ptr_dev, h.uptr.data(), h.uptr.size()))
+      return 1;
     if (upload(L.flags, h.flags.data(), h.n) || upload(L.skip, h.skip.data(), h.n) ||
         upload(L.perm_dev, h.perm.data(), h.n) || upload(L.lower.rows, h.lrows.data(), h.n) ||
         upload(L.upper.rows, h.urows.data(), h.n))

@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <sstream>
+#include <typeinfo>
 
 #include "gmg_internal.h"
 #include "gmg_np.h"
@@ -554,6 +555,8 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
       if (mg->lev[i].n <= -baselevel) break;
     baselevel = i;
   }
+  if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 40000;
+  if (!a.get_int("cluster", &cluster)) cluster = 16;
   if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return NP_NOT_ACTIVE;
   int ret = InitIter(a);
   for (double &d : damp) d = 1.0;
@@ -564,10 +567,28 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
 std::string NPLmgc::Display() const {
   std::ostringstream o;
   o << NPIter::Display() << "g = " << gamma << "\nn1 = " << nu1 << "\nn2 = " << nu2 << "\nbaselevel = " << baselevel
+    << "\nfuse = " << fuse_rows << " (" << (fusable_smoother() >= 0 ? "fused coarse cycle" : "not fusable")
+    << ")\ncluster = " << cluster
     << "\nT = " << (Transfer ? Transfer->name : "---") << "\npre = " << (PreSmooth ? PreSmooth->name : "---")
     << "\npost = " << (PostSmooth ? PostSmooth->name : "---") << "\nbase = " << (BaseSolver ? BaseSolver->name : "---")
     << "\n";
   return o.str();
+}
+
+int NPLmgc::fusable_smoother() const {
+  if (fuse_rows <= 0 || gamma != 1 || !Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return -1;
+  if (typeid(*Transfer) != typeid(NPTransfer)) return -1;
+  const NPLs *bls = dynamic_cast<const NPLs *>(BaseSolver);
+  if (!bls || !bls->is_exact_base()) return -1;
+  if (typeid(*PreSmooth) != typeid(*PostSmooth)) return -1;
+  const NPSmoother *pre = dynamic_cast<const NPSmoother *>(PreSmooth);
+  const NPSmoother *post = dynamic_cast<const NPSmoother *>(PostSmooth);
+  for (int r = 0; r < GMG_MAX_S; ++r)
+    if (pre->damp[r] != post->damp[r]) return -1;
+  if (typeid(*PreSmooth) == typeid(NPJac)) return 0;
+  if (typeid(*PreSmooth) == typeid(NPGs)) return 1;
+  if (typeid(*PreSmooth) == typeid(NPIlu)) return 2;
+  return -1;
 }
 
 bool NPLmgc::capturable() const {
@@ -611,6 +632,20 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   gmg_vec *&t = prec == GMG_PREC_FP64 ? t64 : t32;
   if (!t) t = temp_vec(mg, name + "__t" + std::to_string(prec), prec);
   GMG_CHECK(t, "lmgc: temporary vector");
+  const int smo = fusable_smoother();
+  if (smo >= 0 && mg->lev[level].n <= fuse_rows) {
+    // this level and everything below it: one cluster kernel
+    CoarseCfg cfg;
+    cfg.bl = baselevel; cfg.lc = level; cfg.smoother = smo;
+    cfg.nu1 = nu1; cfg.nu2 = nu2; cfg.cluster = cluster;
+    const NPSmoother *sm = static_cast<const NPSmoother *>(PreSmooth);
+    for (int r = 0; r < GMG_MAX_S; ++r) {
+      cfg.damp[r] = sm->damp[r];
+      cfg.cdamp[r] = damp[r];
+      cfg.abslimit[r] = BaseSolver->abslimit[r];
+    }
+    return k_coarse_cycle(mg, prec, cfg, cv, bv, t);
+  }
   for (int i = 0; i < nu1; ++i)
     if (PreSmooth->IterAcc(level, t, bv, Am, cv, result)) return 1;
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};  // Factor_One

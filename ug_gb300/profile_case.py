@@ -1,0 +1,33 @@
+"""Small driver for profiling the lmgc path with Nsight Compute.
+
+One solve of the 3D P1 diffusion workload (unit cube, six Kuhn tetrahedra
+refined --nref times, k = exp(g), multicolour Gauss-Seidel V(2,2)), limited
+to --cycles ls iterations, with CUDA graphs off so that every kernel is an
+individual launch in the profiler's launch list.
+
+    python -m ug_gb300.profile_case --cycles 2 [--fp64] [--nref 6] [--fuse 40000]
+"""
+import argparse
+
+import ug_gb300 as G
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cycles", type=int, default=2)
+    ap.add_argument("--nref", type=int, default=6)
+    ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--fuse", type=int, default=40000)
+    a = ap.parse_args()
+    gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
+    mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
+    G.setup_lmgc(mg, "gs", baselevel=0, red=1e-8, maxit=a.cycles, mixed=not a.fp64, graph=False, fuse=a.fuse)
+    mg.launch_count(reset=True)
+    x, lr = mg.solve_host("mgs", gen.rhs)
+    print(f"cycles={lr.iters} defect {lr.first_defect[0]:.3e} -> {lr.last_defect[0]:.3e}, "
+          f"{mg.launch_count()} kernel launches")
+    mg.close()
+
+
+if __name__ == "__main__":
+    main()
