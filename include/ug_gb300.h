@@ -74,6 +74,7 @@ typedef struct {
   int fp32_copy;    /* also keep FP32 copies of matrices/transfers (mixed precision) */
   int autotune;     /* time SpMV variants per level at creation and keep the fastest */
   int device;       /* CUDA device ordinal */
+  int disable_pdl;  /* 1: launch without programmatic dependent launch */
 } gmg_mg_opts;
 
 /* ---------------------------------------------------------------- setup */

@@ -46,7 +46,8 @@ class LevelDesc(C.Structure):
 
 
 class MgOpts(C.Structure):
-    _fields_ = [("order", C.c_int), ("fp32_copy", C.c_int), ("autotune", C.c_int), ("device", C.c_int)]
+    _fields_ = [("order", C.c_int), ("fp32_copy", C.c_int), ("autotune", C.c_int), ("device", C.c_int),
+                ("disable_pdl", C.c_int)]
 
 
 class LResult(C.Structure):
@@ -204,7 +205,8 @@ def levels_from_ugfx(fx: dict) -> list[dict]:
 class MultiGrid:
     """Device-resident multigrid hierarchy with UG-style user data and numprocs."""
 
-    def __init__(self, levels, order: int = ORDER_LIST, fp32: bool = False, autotune: bool = False, device: int = 0):
+    def __init__(self, levels, order: int = ORDER_LIST, fp32: bool = False, autotune: bool = False, device: int = 0,
+                 pdl: bool = True):
         L = lib()
         if isinstance(levels, Generator):
             desc_arr = levels._desc
@@ -223,7 +225,7 @@ class MultiGrid:
                                         _ptr(dbl["val"]), _ptr(ints["vclass"]), _ptr(ints["vnclass"]),
                                         _ptr(ints["skip"]), _ptr(ints["prowptr"]), _ptr(ints["pcol"]),
                                         _ptr(dbl["pw"]))
-        opts = MgOpts(order, int(fp32), int(autotune), device)
+        opts = MgOpts(order, int(fp32), int(autotune), device, int(not pdl))
         h = C.c_void_p()
         if L.gmg_mg_create(C.cast(desc_arr, C.c_void_p), nl, C.byref(opts), C.byref(h)):
             _err("gmg_mg_create")

@@ -1,19 +1,23 @@
 // Fused coarse-grid cycle: the lmgc recursion (gamma = 1) over the small
-// levels bl..lc run by ONE thread-block cluster in a single launch.
+// levels bl..lc, run by ONE thread block out of shared memory.
 //
-// Below a few tens of thousands of unknowns a level's kernels are far
-// shorter than a launch, so a V-cycle there is launch-latency bound (each
-// level needs ~40 dependent kernels per visit).  Here every phase of
-// Lmgc (np/procs/iter.cc:7741) -- smoothing step, defect update, dadd,
-// restriction, coarse reset, base solve, interpolation -- is a
-// cluster-strided loop over the level's rows, separated from the next
-// phase by the hardware cluster barrier (barrier.cluster, release/acquire
-// at cluster scope) instead of a kernel boundary.  Data written inside the
-// kernel (b, c, t) is read through L2 (ld.global.cg) so that no SM reads a
-// stale L1 line written by another SM of the cluster; matrix data is
-// read-only and uses the read-only path.  The arithmetic of each phase is
-// that of the per-level kernels in gmg_kernels.cu.
-#include <cooperative_groups.h>
+// On the coarse levels a V-cycle is pure latency: each level visit needs
+// ~25 dependent phases (smoothing waves, defect updates, dadd, restriction,
+// interpolation) of a few hundred rows each, so separate kernel launches or
+// grid-wide barriers cost far more than the arithmetic.  Here the matrices,
+// transfer operators, schedules and vectors of all levels bl..lc (a few
+// hundred KB at most) are copied into shared memory once per cycle, every
+// phase of Lmgc (np/procs/iter.cc:7741) is a block-strided loop over a
+// level's rows, and phases are separated by __syncthreads.  The arithmetic
+// of each phase is that of the per-level kernels in gmg_kernels.cu.
+//
+// The static data of the fused levels is packed once into a contiguous
+// device image (16-byte aligned sections) that the kernel copies with
+// 128-bit loads; the vectors b and c of every fused level are read at the
+// start and written back at the end (c of the top fused level is the
+// coarse-grid correction the caller interpolates; b is written back because
+// restriction keeps the old defect on rows with VNCLASS < 2).
+#include <cstring>
 
 #include "gmg_internal.h"
 #include "gmg_np.h"
@@ -23,250 +27,267 @@ namespace gmg {
 namespace {
 
 constexpr int MAXCL = 12;
-constexpr int CBLK = 512;
+constexpr int CBLK = 1024;
 
+// level description: byte offsets into the shared-memory image
+struct SLev {
+  int n, all_active, nwave, nuwave;
+  int o_rowptr, o_col, o_val, o_dinv, o_flags, o_skip;
+  int o_wptr, o_wrows, o_uptr, o_urows;
+  int o_lrow, o_lcol, o_lval, o_urow, o_ucol, o_uval, o_udinv;
+  int o_prow, o_pcol, o_pw, o_rrow, o_rcol, o_rw;
+  int o_b, o_c, o_t;  // vectors (after the static image)
+  void *gb, *gc;      // the level's b and c in global memory
+};
+
+struct SArgs {
+  int nl, nu1, nu2, unit_damp, smem_bytes, image_bytes;
+  const int4 *image;  // static part, image_bytes (multiple of 16)
+  double damp[GMG_MAX_S], cdamp[GMG_MAX_S], abslimit[GMG_MAX_S];
+  int o_ainv, base_dim;
+  SLev L[MAXCL];
+};
+
+// pointers into shared memory for one level
 template <class T>
-struct CLev {
-  int n, all_active;
-  const int *rowptr, *col;
-  const T *val, *dinv;
+struct PL {
+  int n, all_active, nwave, nuwave;
+  const int *rowptr, *col, *wptr, *wrows, *uptr, *urows, *lrow, *lcol, *urow, *ucol, *prow, *pcol, *rrow, *rcol;
+  const T *val, *dinv, *lval, *uval, *udinv, *pw, *rw;
   const uint8_t *flags, *skip;
-  int nwave, nuwave;
-  const int *wptr, *wrows, *uptr, *urows;
-  const int *lrow, *lcol, *urow, *ucol;
-  const T *lval, *uval, *udinv;
-  const int *prow, *pcol, *rrow, *rcol;  // P (rows: this level), R (rows: level below)
-  const T *pw, *rw;
-  T *c, *b, *t;
+  T *b, *c, *t;
 };
 
 template <class T>
-struct CArgs {
-  int nl;  // levels in the fused range; L[0] is the base level
-  int nu1, nu2, unit_damp;
-  T damp[GMG_MAX_S], cdamp[GMG_MAX_S];
-  const double *ainv;
-  double abslimit[GMG_MAX_S];
-  CLev<T> L[MAXCL];
-};
-
-__device__ __forceinline__ void cluster_sync() {
-  __threadfence();
-  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
-  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+__device__ PL<T> make_pl(const SLev &s, char *sm) {
+  PL<T> p;
+  p.n = s.n; p.all_active = s.all_active; p.nwave = s.nwave; p.nuwave = s.nuwave;
+  auto I = [&](int o) { return o >= 0 ? (const int *)(sm + o) : nullptr; };
+  auto V = [&](int o) { return o >= 0 ? (const T *)(sm + o) : nullptr; };
+  p.rowptr = I(s.o_rowptr); p.col = I(s.o_col); p.wptr = I(s.o_wptr); p.wrows = I(s.o_wrows);
+  p.uptr = I(s.o_uptr); p.urows = I(s.o_urows); p.lrow = I(s.o_lrow); p.lcol = I(s.o_lcol);
+  p.urow = I(s.o_urow); p.ucol = I(s.o_ucol); p.prow = I(s.o_prow); p.pcol = I(s.o_pcol);
+  p.rrow = I(s.o_rrow); p.rcol = I(s.o_rcol);
+  p.val = V(s.o_val); p.dinv = V(s.o_dinv); p.lval = V(s.o_lval); p.uval = V(s.o_uval);
+  p.udinv = V(s.o_udinv); p.pw = V(s.o_pw); p.rw = V(s.o_rw);
+  p.flags = (const uint8_t *)(sm + s.o_flags); p.skip = (const uint8_t *)(sm + s.o_skip);
+  p.b = (T *)(sm + s.o_b); p.c = (T *)(sm + s.o_c); p.t = (T *)(sm + s.o_t);
+  return p;
 }
 
-template <class T>
-__device__ __forceinline__ T ldv(const T *p) { return __ldcg(p); }
+template <int S>
+struct GL {
+  static constexpr int G = S == 1 ? 4 : 2;  // lanes per row
+};
+
+template <int G, class T>
+__device__ __forceinline__ T gsum(T v) {
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// s += sum over the lane's share of `row` (entries j < lim when LOWER) of m_k * v_j
+template <class T, int S, int G, bool LOWER>
+__device__ __forceinline__ void row_dot(const int *rowptr, const int *col, const T *val, const T *v, int row,
+                                        int first, int lane, bool on, T *s) {
+  const int k1 = on ? rowptr[row + 1] : 0;
+  for (int k = on ? rowptr[row] + first + lane : 0; k < k1; k += G) {
+    const int j = col[k];
+    if (LOWER && j >= row) continue;
+    const T *m = val + (size_t)k * S * S;
+#pragma unroll
+    for (int r = 0; r < S; ++r)
+#pragma unroll
+      for (int c = 0; c < S; ++c) s[r] = fma(m[r * S + c], v[j * S + c], s[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = gsum<G>(s[r]);
+}
 
 struct Team {
-  int tid, nth, rank;
+  int lane, grp, ngrp;
 };
 
 // x -= A y ; acc += y (dmatmul_minus + dadd)
 template <class T, int S>
-__device__ void c_spmv(const CLev<T> &L, T *x, const T *y, T *acc, const Team &tm) {
-  for (int i = tm.tid; i < L.n; i += tm.nth) {
+__device__ void c_spmv(const PL<T> &L, T *x, const T *y, T *acc, const Team &tm) {
+  constexpr int G = GL<S>::G;
+  for (int base = 0; base < L.n; base += tm.ngrp) {
+    const int i = base + tm.grp;
+    const bool valid = i < L.n;
     T s[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) s[r] = T(0);
-    const int k1 = __ldg(L.rowptr + i + 1);
-    for (int k = __ldg(L.rowptr + i); k < k1; ++k) {
-      const int j = __ldg(L.col + k);
-      const T *m = L.val + (size_t)k * S * S;
+    row_dot<T, S, G, false>(L.rowptr, L.col, L.val, y, i, 0, tm.lane, valid, s);
+    if (valid && tm.lane == 0) {
 #pragma unroll
-      for (int r = 0; r < S; ++r)
-#pragma unroll
-        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), ldv(y + (size_t)j * S + c), s[r]);
-    }
-#pragma unroll
-    for (int r = 0; r < S; ++r) {
-      x[(size_t)i * S + r] = ldv(x + (size_t)i * S + r) - s[r];
-      if (acc) acc[(size_t)i * S + r] = ldv(acc + (size_t)i * S + r) + ldv(y + (size_t)i * S + r);
+      for (int r = 0; r < S; ++r) {
+        x[i * S + r] -= s[r];
+        if (acc) acc[i * S + r] += y[i * S + r];
+      }
     }
   }
 }
 
 // t = damp * D^{-1} b (l_jac + dscalx)
 template <class T, int S>
-__device__ void c_jac(const CLev<T> &L, const CArgs<T> &a, const Team &tm) {
-  for (int i = tm.tid; i < L.n; i += tm.nth) {
+__device__ void c_jac(const PL<T> &L, const SArgs &a) {
+  for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
     if (!L.all_active && !(L.flags[i] & F_ACTIVE)) {
 #pragma unroll
-      for (int r = 0; r < S; ++r) L.t[(size_t)i * S + r] = T(0);
+      for (int r = 0; r < S; ++r) L.t[i * S + r] = T(0);
       continue;
     }
-    T bv[S];
-#pragma unroll
-    for (int c = 0; c < S; ++c) bv[c] = ldv(L.b + (size_t)i * S + c);
 #pragma unroll
     for (int r = 0; r < S; ++r) {
       T v = T(0);
 #pragma unroll
-      for (int c = 0; c < S; ++c) v = fma(__ldg(L.dinv + (size_t)i * S * S + r * S + c), bv[c], v);
-      L.t[(size_t)i * S + r] = v * a.damp[r];
+      for (int c = 0; c < S; ++c) v = fma(L.dinv[i * S * S + r * S + c], L.b[i * S + c], v);
+      L.t[i * S + r] = v * T(a.damp[r]);
     }
   }
 }
 
-// (D+L) t = b over the wavefronts, L = entries to rows earlier in processing order (l_lgs)
+// (D+L) t = b over the wavefronts (l_lgs)
 template <class T, int S>
-__device__ void c_gs(const CLev<T> &L, const Team &tm) {
+__device__ void c_gs(const PL<T> &L, const Team &tm) {
+  constexpr int G = GL<S>::G;
   for (int w = 0; w < L.nwave; ++w) {
-    const int r0 = __ldg(L.wptr + w), r1 = __ldg(L.wptr + w + 1);
-    for (int q = r0 + tm.tid; q < r1; q += tm.nth) {
-      const int i = __ldg(L.wrows + q);
-      if (!L.all_active && !(L.flags[i] & F_ACTIVE)) {
-#pragma unroll
-        for (int r = 0; r < S; ++r) L.t[(size_t)i * S + r] = T(0);
-        continue;
-      }
+    const int r0 = L.wptr[w], r1 = L.wptr[w + 1];
+    for (int base = r0; base < r1; base += tm.ngrp) {
+      const int q = base + tm.grp;
+      const bool valid = q < r1;
+      const int i = valid ? L.wrows[q] : 0;
+      const bool act = valid && (L.all_active || (L.flags[i] & F_ACTIVE));
       T s[S];
 #pragma unroll
-      for (int r = 0; r < S; ++r) s[r] = ldv(L.b + (size_t)i * S + r);
-      const int k1 = __ldg(L.rowptr + i + 1);
-      for (int k = __ldg(L.rowptr + i) + 1; k < k1; ++k) {
-        const int j = __ldg(L.col + k);
-        if (j >= i) continue;
-        const T *m = L.val + (size_t)k * S * S;
+      for (int r = 0; r < S; ++r) s[r] = T(0);
+      row_dot<T, S, G, true>(L.rowptr, L.col, L.val, L.t, i, 1, tm.lane, act, s);
+      if (valid && tm.lane == 0) {
+        T rhs[S];
 #pragma unroll
-        for (int r = 0; r < S; ++r)
+        for (int r = 0; r < S; ++r) rhs[r] = L.b[i * S + r] - s[r];
 #pragma unroll
-          for (int c = 0; c < S; ++c) s[r] = fma(-__ldg(m + r * S + c), ldv(L.t + (size_t)j * S + c), s[r]);
-      }
+        for (int r = 0; r < S; ++r) {
+          T v = T(0);
 #pragma unroll
-      for (int r = 0; r < S; ++r) {
-        T v = T(0);
-#pragma unroll
-        for (int c = 0; c < S; ++c) v = fma(__ldg(L.dinv + (size_t)i * S * S + r * S + c), s[c], v);
-        L.t[(size_t)i * S + r] = v;
-      }
-    }
-    cluster_sync();
-  }
-}
-
-// L U t = b (l_luiter): forward waves with the unit lower factor, backward with U and D^{-1}
-template <class T, int S>
-__device__ void c_ilu(const CLev<T> &L, const Team &tm) {
-  for (int w = 0; w < L.nwave; ++w) {
-    const int r0 = __ldg(L.wptr + w), r1 = __ldg(L.wptr + w + 1);
-    for (int q = r0 + tm.tid; q < r1; q += tm.nth) {
-      const int i = __ldg(L.wrows + q);
-      const bool act = L.all_active || (L.flags[i] & F_ACTIVE);
-      T s[S];
-#pragma unroll
-      for (int r = 0; r < S; ++r) s[r] = act ? ldv(L.b + (size_t)i * S + r) : T(0);
-      if (act) {
-        const int k1 = __ldg(L.lrow + i + 1);
-        for (int k = __ldg(L.lrow + i); k < k1; ++k) {
-          const int j = __ldg(L.lcol + k);
-          const T *m = L.lval + (size_t)k * S * S;
-#pragma unroll
-          for (int r = 0; r < S; ++r)
-#pragma unroll
-            for (int c = 0; c < S; ++c) s[r] = fma(-__ldg(m + r * S + c), ldv(L.t + (size_t)j * S + c), s[r]);
+          for (int c = 0; c < S; ++c) v = fma(L.dinv[i * S * S + r * S + c], rhs[c], v);
+          L.t[i * S + r] = act ? v : T(0);
         }
       }
-#pragma unroll
-      for (int r = 0; r < S; ++r) L.t[(size_t)i * S + r] = s[r];
     }
-    cluster_sync();
+    __syncthreads();
   }
-  for (int w = 0; w < L.nuwave; ++w) {
-    const int r0 = __ldg(L.uptr + w), r1 = __ldg(L.uptr + w + 1);
-    for (int q = r0 + tm.tid; q < r1; q += tm.nth) {
-      const int i = __ldg(L.urows + q);
-      if (!L.all_active && !(L.flags[i] & F_ACTIVE)) continue;
+}
+
+// L U t = b (l_luiter)
+template <class T, int S>
+__device__ void c_ilu(const PL<T> &L, const Team &tm) {
+  constexpr int G = GL<S>::G;
+  for (int w = 0; w < L.nwave; ++w) {
+    const int r0 = L.wptr[w], r1 = L.wptr[w + 1];
+    for (int base = r0; base < r1; base += tm.ngrp) {
+      const int q = base + tm.grp;
+      const bool valid = q < r1;
+      const int i = valid ? L.wrows[q] : 0;
+      const bool act = valid && (L.all_active || (L.flags[i] & F_ACTIVE));
       T s[S];
 #pragma unroll
-      for (int r = 0; r < S; ++r) s[r] = ldv(L.t + (size_t)i * S + r);
-      const int k1 = __ldg(L.urow + i + 1);
-      for (int k = __ldg(L.urow + i); k < k1; ++k) {
-        const int j = __ldg(L.ucol + k);
-        const T *m = L.uval + (size_t)k * S * S;
+      for (int r = 0; r < S; ++r) s[r] = T(0);
+      row_dot<T, S, G, false>(L.lrow, L.lcol, L.lval, L.t, i, 0, tm.lane, act, s);
+      if (valid && tm.lane == 0)
 #pragma unroll
-        for (int r = 0; r < S; ++r)
+        for (int r = 0; r < S; ++r) L.t[i * S + r] = act ? L.b[i * S + r] - s[r] : T(0);
+    }
+    __syncthreads();
+  }
+  for (int w = 0; w < L.nuwave; ++w) {
+    const int r0 = L.uptr[w], r1 = L.uptr[w + 1];
+    for (int base = r0; base < r1; base += tm.ngrp) {
+      const int q = base + tm.grp;
+      const bool valid = q < r1;
+      const int i = valid ? L.urows[q] : 0;
+      const bool act = valid && (L.all_active || (L.flags[i] & F_ACTIVE));
+      T s[S];
 #pragma unroll
-          for (int c = 0; c < S; ++c) s[r] = fma(-__ldg(m + r * S + c), ldv(L.t + (size_t)j * S + c), s[r]);
-      }
+      for (int r = 0; r < S; ++r) s[r] = T(0);
+      row_dot<T, S, G, false>(L.urow, L.ucol, L.uval, L.t, i, 0, tm.lane, act, s);
+      if (act && tm.lane == 0) {
+        T rhs[S];
 #pragma unroll
-      for (int r = 0; r < S; ++r) {
-        T v = T(0);
+        for (int r = 0; r < S; ++r) rhs[r] = L.t[i * S + r] - s[r];
 #pragma unroll
-        for (int c = 0; c < S; ++c) v = fma(__ldg(L.udinv + (size_t)i * S * S + r * S + c), s[c], v);
-        L.t[(size_t)i * S + r] = v;
+        for (int r = 0; r < S; ++r) {
+          T v = T(0);
+#pragma unroll
+          for (int c = 0; c < S; ++c) v = fma(L.udinv[i * S * S + r * S + c], rhs[c], v);
+          L.t[i * S + r] = v;
+        }
       }
     }
-    cluster_sync();
+    __syncthreads();
   }
 }
 
-template <class T, int S>
-__device__ void c_scale(const CLev<T> &L, const CArgs<T> &a, const Team &tm) {
-  for (int i = tm.tid; i < L.n; i += tm.nth)
-#pragma unroll
-    for (int r = 0; r < S; ++r) L.t[(size_t)i * S + r] = ldv(L.t + (size_t)i * S + r) * a.damp[r];
-}
-
-// one smoothing step of Smoother (iter.cc:817) followed by lmgc's dadd(c, t)
+// one step of Smoother (iter.cc:817) followed by lmgc's dadd(c, t)
 template <class T, int S, int SMO>
-__device__ void c_smooth(const CLev<T> &L, const CArgs<T> &a, const Team &tm) {
+__device__ void c_smooth(const PL<T> &L, const SArgs &a, const Team &tm) {
   if (SMO == 0) {
-    c_jac<T, S>(L, a, tm);
-    cluster_sync();
+    c_jac<T, S>(L, a);
+    __syncthreads();
   } else {
     if (SMO == 1) c_gs<T, S>(L, tm);
     else c_ilu<T, S>(L, tm);
     if (!a.unit_damp) {
-      c_scale<T, S>(L, a, tm);
-      cluster_sync();
+      for (int i = threadIdx.x; i < L.n; i += blockDim.x)
+#pragma unroll
+        for (int r = 0; r < S; ++r) L.t[i * S + r] *= T(a.damp[r]);
+      __syncthreads();
     }
   }
   c_spmv<T, S>(L, L.b, L.t, L.c, tm);
-  cluster_sync();
+  __syncthreads();
 }
 
 // StandardRestrict into the level below, fused with lmgc's dset(c_{l-1}, 0)
 template <class T, int S>
-__device__ void c_restrict(const CLev<T> &F, const CLev<T> &Cl, const Team &tm) {
-  for (int c = tm.tid; c < Cl.n; c += tm.nth) {
+__device__ void c_restrict(const PL<T> &F, const PL<T> &Cl) {
+  for (int c = threadIdx.x; c < Cl.n; c += blockDim.x) {
     const bool reset = Cl.flags[c] & F_RESET;
     const int sk = Cl.skip[c];
     T acc[S];
 #pragma unroll
-    for (int r = 0; r < S; ++r) acc[r] = reset ? T(0) : ldv(Cl.b + (size_t)c * S + r);
-    const int k1 = __ldg(F.rrow + c + 1);
-    for (int k = __ldg(F.rrow + c); k < k1; ++k) {
-      const int f = __ldg(F.rcol + k);
-      const T w = __ldg(F.rw + k);
+    for (int r = 0; r < S; ++r) acc[r] = reset ? T(0) : Cl.b[c * S + r];
+    for (int k = F.rrow[c]; k < F.rrow[c + 1]; ++k) {
+      const int f = F.rcol[k];
+      const T w = F.rw[k];
 #pragma unroll
-      for (int r = 0; r < S; ++r) acc[r] = fma(w, ldv(F.b + (size_t)f * S + r), acc[r]);
+      for (int r = 0; r < S; ++r) acc[r] = fma(w, F.b[f * S + r], acc[r]);
     }
 #pragma unroll
     for (int r = 0; r < S; ++r) {
-      if (!(sk & (1 << r))) Cl.b[(size_t)c * S + r] = acc[r];
-      else if (reset) Cl.b[(size_t)c * S + r] = T(0);
-      Cl.c[(size_t)c * S + r] = T(0);
+      if (!(sk & (1 << r))) Cl.b[c * S + r] = acc[r];
+      else if (reset) Cl.b[c * S + r] = T(0);
+      Cl.c[c * S + r] = T(0);
     }
   }
 }
 
 // StandardInterpolateCorrection into t, fused with lmgc's dadd(c, t)
 template <class T, int S>
-__device__ void c_interp(const CLev<T> &F, const CLev<T> &Cl, const CArgs<T> &a, const Team &tm) {
-  for (int f = tm.tid; f < F.n; f += tm.nth) {
+__device__ void c_interp(const PL<T> &F, const PL<T> &Cl, const SArgs &a) {
+  for (int f = threadIdx.x; f < F.n; f += blockDim.x) {
     const int sk = F.skip[f];
     T v[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) v[r] = T(0);
     if (sk != (1 << S) - 1) {
-      const int k1 = __ldg(F.prow + f + 1);
-      for (int k = __ldg(F.prow + f); k < k1; ++k) {
-        const int c = __ldg(F.pcol + k);
-        const T w = __ldg(F.pw + k);
+      for (int k = F.prow[f]; k < F.prow[f + 1]; ++k) {
+        const int c = F.pcol[k];
+        const T w = F.pw[k];
 #pragma unroll
-        for (int r = 0; r < S; ++r) v[r] = fma(w * a.cdamp[r], ldv(Cl.c + (size_t)c * S + r), v[r]);
+        for (int r = 0; r < S; ++r) v[r] = fma(w * T(a.cdamp[r]), Cl.c[c * S + r], v[r]);
       }
 #pragma unroll
       for (int r = 0; r < S; ++r)
@@ -274,15 +295,15 @@ __device__ void c_interp(const CLev<T> &F, const CLev<T> &Cl, const CArgs<T> &a,
     }
 #pragma unroll
     for (int r = 0; r < S; ++r) {
-      F.t[(size_t)f * S + r] = v[r];
-      F.c[(size_t)f * S + r] = ldv(F.c + (size_t)f * S + r) + v[r];
+      F.t[f * S + r] = v[r];
+      F.c[f * S + r] += v[r];
     }
   }
 }
 
-// base solver `ls $m 1 $I ex` on the cluster's first CTA
+// base solver `ls $m 1 $I ex`: skip below the abslimit, else t = A^{-1} b; b -= A t; c += t
 template <class T, int S>
-__device__ void c_base(const CLev<T> &B, const CArgs<T> &a) {
+__device__ void c_base(const PL<T> &B, const SArgs &a, const double *ainv, const Team &tm) {
   __shared__ double red[S][CBLK / 32];
   __shared__ int skip;
   double acc[S];
@@ -291,7 +312,7 @@ __device__ void c_base(const CLev<T> &B, const CArgs<T> &a) {
   for (int i = threadIdx.x; i < B.n; i += blockDim.x)
 #pragma unroll
     for (int r = 0; r < S; ++r) {
-      double v = double(ldv(B.b + (size_t)i * S + r));
+      double v = double(B.b[i * S + r]);
       acc[r] += v * v;
     }
 #pragma unroll
@@ -305,7 +326,7 @@ __device__ void c_base(const CLev<T> &B, const CArgs<T> &a) {
     int below = 1;
     for (int r = 0; r < S; ++r) {
       double v = 0.0;
-      for (int w = 0; w < CBLK / 32; ++w) v += red[r][w];
+      for (int w = 0; w < (int)(blockDim.x / 32); ++w) v += red[r][w];
       if (fabs(sqrt(v)) >= fabs(a.abslimit[r])) below = 0;
     }
     skip = below;
@@ -315,158 +336,280 @@ __device__ void c_base(const CLev<T> &B, const CArgs<T> &a) {
   const int N = B.n * S;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     double v = 0.0;
-    for (int j = 0; j < N; ++j) v = fma(a.ainv[(size_t)i * N + j], double(ldv(B.b + j)), v);
+    for (int j = 0; j < N; ++j) v = fma(ainv[i * N + j], double(B.b[j]), v);
     B.t[i] = T(v);
   }
   __syncthreads();
-  Team one{int(threadIdx.x), int(blockDim.x), 0};
-  c_spmv<T, S>(B, B.b, B.t, B.c, one);
+  c_spmv<T, S>(B, B.b, B.t, B.c, tm);
+  __syncthreads();
 }
 
 template <class T, int S, int SMO>
-__global__ void __launch_bounds__(CBLK, 1) coarse_cycle_kernel(const __grid_constant__ CArgs<T> a) {
-  namespace cg = cooperative_groups;
-  cg::cluster_group cl = cg::this_cluster();
-  Team tm;
-  tm.rank = int(cl.block_rank());
-  tm.nth = int(cl.num_blocks()) * blockDim.x;
-  tm.tid = tm.rank * blockDim.x + threadIdx.x;
-  // down: pre-smoothing and restriction, from the top of the fused range
-  for (int k = a.nl - 1; k >= 1; --k) {
-    for (int it = 0; it < a.nu1; ++it) c_smooth<T, S, SMO>(a.L[k], a, tm);
-    c_restrict<T, S>(a.L[k], a.L[k - 1], tm);
-    cluster_sync();
+__global__ void __launch_bounds__(CBLK, 1) coarse_cycle_kernel(const __grid_constant__ SArgs a) {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");  // programmatic dependent launch
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+  extern __shared__ int4 smem4[];
+  char *sm = reinterpret_cast<char *>(smem4);
+  // static image: 128-bit copies
+  for (int i = threadIdx.x; i < a.image_bytes / 16; i += blockDim.x) smem4[i] = __ldg(a.image + i);
+  // vectors: b and c of every fused level
+  for (int k = 0; k < a.nl; ++k) {
+    const SLev &s = a.L[k];
+    T *b = (T *)(sm + s.o_b), *c = (T *)(sm + s.o_c);
+    const T *gb = (const T *)s.gb, *gc = (const T *)s.gc;
+    for (int i = threadIdx.x; i < s.n * S; i += blockDim.x) {
+      b[i] = gb[i];
+      c[i] = gc[i];
+    }
   }
-  if (tm.rank == 0) c_base<T, S>(a.L[0], a);
-  cluster_sync();
+  __syncthreads();
+  constexpr int G = GL<S>::G;
+  Team tm{int(threadIdx.x & (G - 1)), int(threadIdx.x / G), int(blockDim.x / G)};
+  // down: pre-smoothing and restriction
+  for (int k = a.nl - 1; k >= 1; --k) {
+    const PL<T> L = make_pl<T>(a.L[k], sm);
+    for (int it = 0; it < a.nu1; ++it) c_smooth<T, S, SMO>(L, a, tm);
+    c_restrict<T, S>(L, make_pl<T>(a.L[k - 1], sm));
+    __syncthreads();
+  }
+  c_base<T, S>(make_pl<T>(a.L[0], sm), a, reinterpret_cast<const double *>(sm + a.o_ainv), tm);
   // up: interpolation, coarse-grid correction, post-smoothing
   for (int k = 1; k < a.nl; ++k) {
-    c_interp<T, S>(a.L[k], a.L[k - 1], a, tm);
-    cluster_sync();
-    c_spmv<T, S>(a.L[k], a.L[k].b, a.L[k].t, nullptr, tm);
-    cluster_sync();
-    for (int it = 0; it < a.nu2; ++it) c_smooth<T, S, SMO>(a.L[k], a, tm);
+    const PL<T> L = make_pl<T>(a.L[k], sm);
+    c_interp<T, S>(L, make_pl<T>(a.L[k - 1], sm), a);
+    __syncthreads();
+    c_spmv<T, S>(L, L.b, L.t, nullptr, tm);
+    __syncthreads();
+    for (int it = 0; it < a.nu2; ++it) c_smooth<T, S, SMO>(L, a, tm);
+  }
+  // write back b and c of every fused level
+  for (int k = 0; k < a.nl; ++k) {
+    const SLev &s = a.L[k];
+    const T *b = (const T *)(sm + s.o_b), *c = (const T *)(sm + s.o_c);
+    T *gb = (T *)s.gb, *gc = (T *)s.gc;
+    for (int i = threadIdx.x; i < s.n * S; i += blockDim.x) {
+      gb[i] = b[i];
+      gc[i] = c[i];
+    }
   }
 }
 
-template <class T>
-const T *pick(const double *d, const float *f);
-template <>
-const double *pick<double>(const double *d, const float *) { return d; }
-template <>
-const float *pick<float>(const double *, const float *f) { return f; }
+// ---------------------------------------------------------------- host: the image
+struct Image {
+  std::vector<char> host;
+  int add(const void *p, size_t bytes) {
+    if (!p || bytes == 0) return -1;
+    size_t o = (host.size() + 15) & ~size_t(15);
+    host.resize(o + ((bytes + 15) & ~size_t(15)), 0);
+    std::memcpy(host.data() + o, p, bytes);
+    return int(o);
+  }
+};
 
 template <class T>
-int fill_args(gmg_mg *mg, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t, CArgs<T> &a) {
-  a.nl = cfg.lc - cfg.bl + 1;
+std::vector<T> conv(const double *d, size_t n) {
+  return std::vector<T>(d, d + n);
+}
+
+struct CachedImage : CoarseImageBase {
+  int bl = -1, lc = -1, prec = -1, smo = -1;
+  void *dev = nullptr;
+  SArgs args{};
+  ~CachedImage() override {
+    if (dev) cudaFree(dev);
+  }
+};
+
+// device-to-host copies of the level's device-only data (ILU factors)
+template <class T>
+static int d2h(std::vector<char> &out, const T *dev, size_t n) {
+  out.resize(n * sizeof(T));
+  if (n) GMG_CUDA(cudaMemcpy(out.data(), dev, n * sizeof(T), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+template <class T>
+int build_image(gmg_mg *mg, int bl, int lc, int smo, SArgs &a, std::vector<char> &img, int *smem_total) {
+  Image im;
+  const int s = mg->lev[bl].s, ss = s * s;
+  a.nl = lc - bl + 1;
   GMG_CHECK(a.nl >= 1 && a.nl <= MAXCL, "fused coarse cycle: %d levels (max %d)", a.nl, MAXCL);
+  for (int k = 0; k < a.nl; ++k) {
+    const Level &L = mg->lev[bl + k];
+    SLev &d = a.L[k];
+    std::memset(&d, 0xff, sizeof d);  // all offsets -1
+    d.n = L.n; d.all_active = L.all_active;
+    d.nwave = L.lower.nwave(); d.nuwave = L.upper.nwave();
+    const size_t nnz = L.h_rowptr[L.n];
+    d.o_rowptr = im.add(L.h_rowptr.data(), (L.n + 1) * 4);
+    d.o_col = im.add(L.h_col.data(), nnz * 4);
+    auto v = conv<T>(L.h_val.data(), nnz * ss);
+    d.o_val = im.add(v.data(), v.size() * sizeof(T));
+    std::vector<double> dinv(size_t(L.n) * ss);
+    GMG_CUDA(cudaMemcpy(dinv.data(), L.dinv64, dinv.size() * 8, cudaMemcpyDeviceToHost));
+    auto dv = conv<T>(dinv.data(), dinv.size());
+    d.o_dinv = im.add(dv.data(), dv.size() * sizeof(T));
+    d.o_flags = im.add(L.h_flags.data(), L.n);
+    d.o_skip = im.add(L.h_skip.data(), L.n);
+    d.o_wptr = im.add(L.lower.ptr.data(), L.lower.ptr.size() * 4);
+    d.o_uptr = im.add(L.upper.ptr.data(), L.upper.ptr.size() * 4);
+    std::vector<char> tmp;
+    if (d2h(tmp, L.lower.rows, L.n)) return 1;
+    d.o_wrows = im.add(tmp.data(), tmp.size());
+    if (d2h(tmp, L.upper.rows, L.n)) return 1;
+    d.o_urows = im.add(tmp.data(), tmp.size());
+    if (smo == 2 && k > 0) {
+      GMG_CHECK(L.ilu_ready, "ILU factors missing on level %d", bl + k);
+      if (d2h(tmp, L.L.rowptr, L.n + 1)) return 1;
+      d.o_lrow = im.add(tmp.data(), tmp.size());
+      if (d2h(tmp, L.L.col, L.L.nnz)) return 1;
+      d.o_lcol = im.add(tmp.data(), tmp.size());
+      if (d2h(tmp, L.U.rowptr, L.n + 1)) return 1;
+      d.o_urow = im.add(tmp.data(), tmp.size());
+      if (d2h(tmp, L.U.col, L.U.nnz)) return 1;
+      d.o_ucol = im.add(tmp.data(), tmp.size());
+      std::vector<double> lv(L.L.nnz * ss), uv(L.U.nnz * ss), ud(size_t(L.n) * ss);
+      if (!lv.empty()) GMG_CUDA(cudaMemcpy(lv.data(), L.L.v64, lv.size() * 8, cudaMemcpyDeviceToHost));
+      if (!uv.empty()) GMG_CUDA(cudaMemcpy(uv.data(), L.U.v64, uv.size() * 8, cudaMemcpyDeviceToHost));
+      GMG_CUDA(cudaMemcpy(ud.data(), L.udinv64, ud.size() * 8, cudaMemcpyDeviceToHost));
+      auto lt = conv<T>(lv.data(), lv.size()), ut = conv<T>(uv.data(), uv.size()), dt = conv<T>(ud.data(), ud.size());
+      d.o_lval = im.add(lt.data(), lt.size() * sizeof(T));
+      d.o_uval = im.add(ut.data(), ut.size() * sizeof(T));
+      d.o_udinv = im.add(dt.data(), dt.size() * sizeof(T));
+    }
+    if (k > 0) {  // transfer from the level below
+      if (d2h(tmp, L.P.rowptr, L.n + 1)) return 1;
+      d.o_prow = im.add(tmp.data(), tmp.size());
+      if (d2h(tmp, L.P.col, L.P.nnz)) return 1;
+      d.o_pcol = im.add(tmp.data(), tmp.size());
+      std::vector<double> pw(L.P.nnz), rw(L.R.nnz);
+      if (!pw.empty()) GMG_CUDA(cudaMemcpy(pw.data(), L.P.v64, pw.size() * 8, cudaMemcpyDeviceToHost));
+      auto pt = conv<T>(pw.data(), pw.size());
+      d.o_pw = im.add(pt.data(), pt.size() * sizeof(T));
+      if (d2h(tmp, L.R.rowptr, mg->lev[bl + k - 1].n + 1)) return 1;
+      d.o_rrow = im.add(tmp.data(), tmp.size());
+      if (d2h(tmp, L.R.col, L.R.nnz)) return 1;
+      d.o_rcol = im.add(tmp.data(), tmp.size());
+      if (!rw.empty()) GMG_CUDA(cudaMemcpy(rw.data(), L.R.v64, rw.size() * 8, cudaMemcpyDeviceToHost));
+      auto rt = conv<T>(rw.data(), rw.size());
+      d.o_rw = im.add(rt.data(), rt.size() * sizeof(T));
+    }
+  }
+  const Level &B = mg->lev[bl];
+  GMG_CHECK(B.ainv, "base level inverse not computed (ex PreProcess)");
+  std::vector<double> ainv(size_t(B.base_dim) * B.base_dim);
+  GMG_CUDA(cudaMemcpy(ainv.data(), B.ainv, ainv.size() * 8, cudaMemcpyDeviceToHost));
+  a.o_ainv = im.add(ainv.data(), ainv.size() * 8);
+  a.base_dim = B.base_dim;
+  a.image_bytes = int((im.host.size() + 15) & ~size_t(15));
+  im.host.resize(a.image_bytes, 0);
+  // vectors after the image
+  size_t off = im.host.size();
+  for (int k = 0; k < a.nl; ++k) {
+    const size_t vb = ((size_t(mg->lev[bl + k].n) * s * sizeof(T)) + 15) & ~size_t(15);
+    a.L[k].o_b = int(off); off += vb;
+    a.L[k].o_c = int(off); off += vb;
+    a.L[k].o_t = int(off); off += vb;
+  }
+  *smem_total = int(off);
+  img.swap(im.host);
+  return 0;
+}
+
+}  // namespace
+
+// shared-memory bytes the fused cycle needs for levels bl..lc (no device work)
+long long coarse_smem_bytes(const gmg_mg *mg, int bl, int lc, int prec, int smo) {
+  const int s = mg->lev[bl].s, ss = s * s;
+  const size_t T = prec == GMG_PREC_FP64 ? 8 : 4;
+  auto al = [](size_t b) { return (b + 15) & ~size_t(15); };
+  size_t b = 0;
+  for (int l = bl; l <= lc; ++l) {
+    const Level &L = mg->lev[l];
+    const size_t nnz = L.h_rowptr[L.n];
+    b += al((L.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * T) + al(size_t(L.n) * ss * T) + 2 * al(L.n);
+    b += al(L.lower.ptr.size() * 4) + al(L.upper.ptr.size() * 4) + 2 * al(size_t(L.n) * 4);
+    if (smo == 2 && l > bl) b += 2 * (al((L.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * T)) + al(size_t(L.n) * ss * T);
+    if (l > bl)
+      b += al((L.n + 1) * 4) + al(L.P.nnz * 4) + al(L.P.nnz * T) + al((mg->lev[l - 1].n + 1) * 4) +
+           al(L.R.nnz * 4) + al(L.R.nnz * T);
+    b += 3 * al(size_t(L.n) * s * T);
+  }
+  const size_t N = size_t(mg->lev[bl].n) * s;
+  b += al(N * N * 8);
+  return (long long)b;
+}
+
+int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t) {
+  (void)t;
+  // the packed image is built once per (levels, precision, smoother), on the
+  // first (eager, uncaptured) call, and lives as long as the multigrid
+  auto &lst = mg->coarse_images;
+  CachedImage *ci = nullptr;
+  for (auto &b0 : lst) {
+    CachedImage *e = static_cast<CachedImage *>(b0.get());
+    if (e->bl == cfg.bl && e->lc == cfg.lc && e->prec == prec && e->smo == cfg.smoother) ci = e;
+  }
+  if (!ci) {
+    auto e = std::make_unique<CachedImage>();
+    std::vector<char> img;
+    int smem = 0;
+    int rc = prec == GMG_PREC_FP64 ? build_image<double>(mg, cfg.bl, cfg.lc, cfg.smoother, e->args, img, &smem)
+                                   : build_image<float>(mg, cfg.bl, cfg.lc, cfg.smoother, e->args, img, &smem);
+    if (rc) return 1;
+    GMG_CHECK(smem <= 227 * 1024, "fused coarse cycle needs %d bytes of shared memory", smem);
+    GMG_CUDA(cudaMalloc(&e->dev, img.size()));
+    GMG_CUDA(cudaMemcpy(e->dev, img.data(), img.size(), cudaMemcpyHostToDevice));
+    e->args.image = (const int4 *)e->dev;
+    e->args.smem_bytes = smem;
+    e->bl = cfg.bl; e->lc = cfg.lc; e->prec = prec; e->smo = cfg.smoother;
+    ci = e.get();
+    lst.push_back(std::move(e));
+  }
+  SArgs a = ci->args;
   a.nu1 = cfg.nu1;
   a.nu2 = cfg.nu2;
   a.unit_damp = 1;
   const int s = mg->lev[cfg.bl].s;
   for (int r = 0; r < GMG_MAX_S; ++r) {
-    a.damp[r] = T(cfg.damp[r]);
-    a.cdamp[r] = T(cfg.cdamp[r]);
+    a.damp[r] = cfg.damp[r];
+    a.cdamp[r] = cfg.cdamp[r];
     a.abslimit[r] = cfg.abslimit[r];
     if (r < s && cfg.damp[r] != 1.0) a.unit_damp = 0;
   }
-  const Level &B = mg->lev[cfg.bl];
-  GMG_CHECK(B.ainv, "base level inverse not computed (ex PreProcess)");
-  a.ainv = B.ainv;
   for (int k = 0; k < a.nl; ++k) {
-    const Level &L = mg->lev[cfg.bl + k];
-    CLev<T> &d = a.L[k];
-    d.n = L.n;
-    d.all_active = L.all_active;
-    d.rowptr = L.A.rowptr; d.col = L.A.col;
-    d.val = pick<T>(L.A.v64, L.A.v32);
-    d.dinv = pick<T>(L.dinv64, L.dinv32);
-    GMG_CHECK(d.val && d.dinv, "fused coarse cycle: precision copy missing");
-    d.flags = L.flags; d.skip = L.skip;
-    d.nwave = L.lower.nwave(); d.wptr = L.lower.ptr_dev; d.wrows = L.lower.rows;
-    d.nuwave = L.upper.nwave(); d.uptr = L.upper.ptr_dev; d.urows = L.upper.rows;
-    d.lrow = L.L.rowptr; d.lcol = L.L.col; d.lval = pick<T>(L.L.v64, L.L.v32);
-    d.urow = L.U.rowptr; d.ucol = L.U.col; d.uval = pick<T>(L.U.v64, L.U.v32);
-    d.udinv = pick<T>(L.udinv64, L.udinv32);
-    if (cfg.smoother == 2 && k > 0) GMG_CHECK(L.ilu_ready && d.lval && d.uval, "ILU factors missing on level %d", cfg.bl + k);
-    d.prow = L.P.rowptr; d.pcol = L.P.col; d.pw = pick<T>(L.P.v64, L.P.v32);
-    d.rrow = L.R.rowptr; d.rcol = L.R.col; d.rw = pick<T>(L.R.v64, L.R.v32);
-    d.c = (T *)c->lev[cfg.bl + k];
-    d.b = (T *)b->lev[cfg.bl + k];
-    d.t = (T *)t->lev[cfg.bl + k];
+    a.L[k].gb = b->lev[cfg.bl + k];
+    a.L[k].gc = c->lev[cfg.bl + k];
   }
-  return 0;
-}
-
-template <class T, int S, int SMO>
-int launch(gmg_mg *mg, const CArgs<T> &a, int want_cluster) {
-  auto kern = coarse_cycle_kernel<T, S, SMO>;
-  // the cluster size is chosen once per kernel variant, outside any stream
-  // capture: the largest power of two <= want_cluster that fits
-  static int chosen[2][4][3][6] = {};
-  int wi = 0;
-  while ((1 << wi) < want_cluster && wi < 5) ++wi;
-  int &csz = chosen[sizeof(T) == 8 ? 0 : 1][S][SMO][wi];
-  if (!csz) {
-    GMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    for (int c = 1 << wi; c >= 1; c /= 2) {
-      cudaLaunchConfig_t cfg = {};
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = c;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.gridDim = dim3(c);
-      cfg.blockDim = dim3(CBLK);
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1) {
-        csz = c;
-        break;
-      }
-      cudaGetLastError();
-    }
-    GMG_CHECK(csz, "fused coarse cycle: no cluster size fits");
+  void (*kern)(const SArgs) = nullptr;
+#define PICK(TT, SS)                                                     \
+  if (s == SS) {                                                         \
+    if (cfg.smoother == 0) kern = coarse_cycle_kernel<TT, SS, 0>;        \
+    else if (cfg.smoother == 1) kern = coarse_cycle_kernel<TT, SS, 1>;   \
+    else kern = coarse_cycle_kernel<TT, SS, 2>;                          \
   }
-  cudaLaunchConfig_t cfg = {};
+  if (prec == GMG_PREC_FP64) { PICK(double, 1) PICK(double, 2) PICK(double, 3) }
+  else { PICK(float, 1) PICK(float, 2) PICK(float, 3) }
+#undef PICK
+  GMG_CHECK(kern, "block size %d not compiled", s);
+  static thread_local std::map<void *, int> smem_set;
+  if (smem_set[(void *)kern] < a.smem_bytes) {
+    GMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes));
+    smem_set[(void *)kern] = a.smem_bytes;
+  }
+  cudaLaunchConfig_t lc = {};
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = csz;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3(csz);
-  cfg.blockDim = dim3(CBLK);
-  cfg.stream = mg->stream;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  GMG_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  lc.gridDim = dim3(1);
+  lc.blockDim = dim3(CBLK);
+  lc.dynamicSmemBytes = a.smem_bytes;
+  lc.stream = mg->stream;
+  lc.attrs = attr;
+  lc.numAttrs = mg->opts.disable_pdl ? 0 : 1;
+  GMG_CUDA(cudaLaunchKernelEx(&lc, kern, a));
   mg->launches++;
   return 0;
-}
-
-template <class T>
-int dispatch(gmg_mg *mg, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t) {
-  CArgs<T> a;
-  if (fill_args<T>(mg, cfg, c, b, t, a)) return 1;
-  const int s = mg->lev[cfg.bl].s;
-#define L3(SS)                                                                  \
-  if (s == SS) {                                                                \
-    if (cfg.smoother == 0) return launch<T, SS, 0>(mg, a, cfg.cluster);         \
-    if (cfg.smoother == 1) return launch<T, SS, 1>(mg, a, cfg.cluster);         \
-    return launch<T, SS, 2>(mg, a, cfg.cluster);                                \
-  }
-  L3(1) L3(2) L3(3)
-#undef L3
-  set_error("block size %d not compiled", s);
-  return 1;
-}
-
-}  // namespace
-
-int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t) {
-  if (prec == GMG_PREC_FP64) return dispatch<double>(mg, cfg, c, b, t);
-  return dispatch<float>(mg, cfg, c, b, t);
 }
 
 }  // namespace gmg

@@ -114,6 +114,11 @@ struct Mat {
   std::string name;
 };
 
+// packed device image of fused coarse levels (gmg_coarse.cu), owned by the multigrid
+struct CoarseImageBase {
+  virtual ~CoarseImageBase() = default;
+};
+
 
 }  // namespace gmg
 
@@ -141,6 +146,7 @@ struct gmg_mg {
   void *stage_dev = nullptr;   // n_top*s doubles
   double *stage_host = nullptr;// pinned, n_top*s doubles
   long long launches = 0;
+  std::vector<std::unique_ptr<gmg::CoarseImageBase>> coarse_images;
   ~gmg_mg();
 };
 
@@ -182,6 +188,9 @@ struct CoarseCfg {
   double damp[GMG_MAX_S], cdamp[GMG_MAX_S], abslimit[GMG_MAX_S];
 };
 int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t);
+// shared memory the fused cycle needs for levels bl..lc
+long long coarse_smem_bytes(const gmg_mg *mg, int bl, int lc, int prec, int smoother);
+constexpr long long COARSE_SMEM_BUDGET = 220 * 1024;
 // permutations between UG list order and processing order
 int k_gather(gmg_mg *mg, int prec, void *dst, const double *src_list, const int *perm, int n, int s);
 int k_scatter(gmg_mg *mg, int prec, double *dst_list, const void *src, const int *perm, int n, int s);

@@ -12,6 +12,7 @@
 // results agree with the reference to rounding (the summation order inside a
 // row follows the shuffle tree instead of the MATRIX list).
 #include <cstdio>
+#include <utility>
 
 #include "gmg_internal.h"
 
@@ -20,6 +21,33 @@ namespace gmg {
 namespace {
 
 constexpr int BLK = 256;
+
+// Programmatic dependent launch: every kernel is launched with programmatic
+// stream serialisation, waits for its predecessor's memory before touching
+// any data (griddepcontrol.wait) and immediately allows its successor to be
+// launched (griddepcontrol.launch_dependents), so the successor's launch
+// and scheduling overlap this kernel's tail.  Without the launch attribute
+// both instructions are no-ops.
+__device__ __forceinline__ void pdl_prologue() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+template <typename... KP, typename... A>
+inline void pdl_launch(gmg_mg *mg, void (*kern)(KP...), dim3 grid, dim3 block, A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = mg->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = mg->opts.disable_pdl ? 0 : 1;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+#define GMG_LAUNCH(K, G, B, ...) pdl_launch(mg, K, dim3(G), dim3(B), __VA_ARGS__)
 
 template <class T>
 struct Damp {
@@ -48,32 +76,38 @@ __device__ __forceinline__ T group_sum(T v) {
 // ------------------------------------------------------------ BLAS-1 kernels
 template <class T>
 __global__ void set_kernel(T *x, long long len, T a) {
+  pdl_prologue();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
     x[i] = a;
 }
 template <class T>
 __global__ void copy_kernel(T *x, const T *__restrict__ y, long long len) {
+  pdl_prologue();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
     x[i] = y[i];
 }
 template <class T>
 __global__ void add_kernel(T *x, const T *__restrict__ y, long long len) {
+  pdl_prologue();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
     x[i] += y[i];
 }
 template <class TD, class TS>
 __global__ void convert_kernel(TD *x, const TS *__restrict__ y, long long len) {
+  pdl_prologue();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
     x[i] = TD(y[i]);
 }
 template <class TS>
 __global__ void add_mixed_kernel(double *x, const TS *__restrict__ y, long long len) {
+  pdl_prologue();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
     x[i] += double(y[i]);
 }
 // dscalx: x_i,r *= damp_r
 template <class T, int S>
 __global__ void scale_kernel(T *x, int n, Damp<T> dm) {
+  pdl_prologue();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
 #pragma unroll
@@ -89,6 +123,7 @@ __global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__res
                                                          const int *__restrict__ col, const T *__restrict__ val,
                                                          const TY *__restrict__ y, T *__restrict__ x,
                                                          TY *__restrict__ acc) {
+  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int row = gt / TPR, lane = gt & (TPR - 1);
   T s[S];
@@ -125,6 +160,7 @@ __global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__res
 template <class T, int S, bool ALL_ACTIVE>
 __global__ void jac_kernel(int n, const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
                            const T *__restrict__ b, T *__restrict__ t, Damp<T> dm) {
+  pdl_prologue();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (!ALL_ACTIVE && !(flags[i] & F_ACTIVE)) {
@@ -155,6 +191,7 @@ __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ ro
                                                       const T *__restrict__ val, const T *__restrict__ dinv,
                                                       const uint8_t *__restrict__ flags, const T *__restrict__ b,
                                                       T *__restrict__ t) {
+  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
@@ -208,6 +245,7 @@ __global__ void __launch_bounds__(BLK) ilu_fwd_kernel(const int *__restrict__ ro
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
                                                       const T *__restrict__ val, const uint8_t *__restrict__ flags,
                                                       const T *__restrict__ b, T *__restrict__ t) {
+  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
@@ -243,6 +281,7 @@ __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ ro
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
                                                       const T *__restrict__ val, const T *__restrict__ dinv,
                                                       const uint8_t *__restrict__ flags, T *__restrict__ t) {
+  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
@@ -291,6 +330,7 @@ __global__ void restrict_kernel(int nc, const int *__restrict__ rrow, const int 
                                 const T *__restrict__ rw, const uint8_t *__restrict__ cflags,
                                 const uint8_t *__restrict__ cskip, const T *__restrict__ from, T *__restrict__ to,
                                 Damp<T> dm) {
+  pdl_prologue();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const bool reset = cflags[c] & F_RESET;
@@ -317,6 +357,7 @@ template <class T, int S, bool ACC>
 __global__ void interp_kernel(int nf, const int *__restrict__ prow, const int *__restrict__ pcol,
                               const T *__restrict__ pw, const uint8_t *__restrict__ fskip,
                               const T *__restrict__ from, T *__restrict__ to, Damp<T> dm, T *__restrict__ acc) {
+  pdl_prologue();
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const int sk = fskip[f];
@@ -349,6 +390,7 @@ __global__ void interp_kernel(int nf, const int *__restrict__ prow, const int *_
 template <class T, int S, bool ALL>
 __global__ void __launch_bounds__(BLK) nrm_stage1(int n, const T *__restrict__ x, const uint8_t *__restrict__ flags,
                                                   double *__restrict__ partial) {
+  pdl_prologue();
   double acc[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = 0.0;
@@ -377,6 +419,7 @@ __global__ void __launch_bounds__(BLK) nrm_stage1(int n, const T *__restrict__ x
 
 template <int S>
 __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, double *__restrict__ out) {
+  pdl_prologue();
   __shared__ double sh[1024];
   for (int r = 0; r < S; ++r) {
     double v = 0.0;
@@ -402,6 +445,7 @@ __global__ void __launch_bounds__(1024) base_kernel(int n, const double *__restr
                                                     const int *__restrict__ col, const T *__restrict__ val,
                                                     T *__restrict__ c, T *__restrict__ b, T *__restrict__ t,
                                                     Damp<double> abslimit) {
+  pdl_prologue();
   __shared__ double red[S][32];
   __shared__ int skip;
   const int N = n * S;
@@ -457,6 +501,7 @@ __global__ void __launch_bounds__(1024) base_kernel(int n, const double *__restr
 // ------------------------------------------------------------ permutations
 template <class T>
 __global__ void gather_kernel(T *dst, const double *__restrict__ src, const int *__restrict__ perm, int n, int s) {
+  pdl_prologue();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int p = perm[i];
@@ -464,6 +509,7 @@ __global__ void gather_kernel(T *dst, const double *__restrict__ src, const int 
 }
 template <class T>
 __global__ void scatter_kernel(double *dst, const T *__restrict__ src, const int *__restrict__ perm, int n, int s) {
+  pdl_prologue();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int p = perm[i];
@@ -492,7 +538,7 @@ int spmv_dispatch_tpr(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *
   switch (L.tpr) {
 #define CASE(TP)                                                                                           \
   case TP:                                                                                                 \
-    spmv_minus_kernel<T, TY, S, TP, ACC><<<grid_for((long long)n * TP), BLK, 0, mg->stream>>>(n, L.A.rowptr, \
+    GMG_LAUNCH((spmv_minus_kernel<T, TY, S, TP, ACC>), grid_for((long long)n * TP), BLK, n, L.A.rowptr, \
                                                                                            L.A.col, val, y, x, acc); \
     break;
     CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32)
@@ -539,10 +585,10 @@ int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
     if (nr <= 0) continue;
     if (L.all_active)
-      gs_wave_kernel<T, S, TPR, true><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, true>), grid_for((long long)nr * TPR), BLK, 
           L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv, L.flags, b, t);
     else
-      gs_wave_kernel<T, S, TPR, false><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, false>), grid_for((long long)nr * TPR), BLK, 
           L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv, L.flags, b, t);
     LAUNCH_CHECK(mg);
   }
@@ -556,10 +602,10 @@ int ilu_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
     if (nr <= 0) continue;
     if (L.all_active)
-      ilu_fwd_kernel<T, S, TPR, true><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, true>), grid_for((long long)nr * TPR), BLK, 
           L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
     else
-      ilu_fwd_kernel<T, S, TPR, false><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, false>), grid_for((long long)nr * TPR), BLK, 
           L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
     LAUNCH_CHECK(mg);
   }
@@ -567,10 +613,10 @@ int ilu_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.upper.ptr[w], nr = L.upper.ptr[w + 1] - r0;
     if (nr <= 0) continue;
     if (L.all_active)
-      ilu_bwd_kernel<T, S, TPR, true><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+      GMG_LAUNCH((ilu_bwd_kernel<T, S, TPR, true>), grid_for((long long)nr * TPR), BLK, 
           L.upper.rows + r0, nr, L.U.rowptr, L.U.col, uv, ud, L.flags, t);
     else
-      ilu_bwd_kernel<T, S, TPR, false><<<grid_for((long long)nr * TPR), BLK, 0, mg->stream>>>(
+      GMG_LAUNCH((ilu_bwd_kernel<T, S, TPR, false>), grid_for((long long)nr * TPR), BLK, 
           L.upper.rows + r0, nr, L.U.rowptr, L.U.col, uv, ud, L.flags, t);
     LAUNCH_CHECK(mg);
   }
@@ -585,24 +631,24 @@ inline int tri_tpr(const Level &L) { return L.tpr > 8 ? 8 : (L.tpr < 4 ? 4 : L.t
 // ============================================================ launchers
 int k_set(gmg_mg *mg, int prec, void *x, long long len, double a) {
   if (len <= 0) return 0;
-  if (prec == GMG_PREC_FP64) set_kernel<double><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)x, len, a);
-  else set_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)x, len, float(a));
+  if (prec == GMG_PREC_FP64) GMG_LAUNCH((set_kernel<double>), vec_grid(len), BLK, (double *)x, len, a);
+  else GMG_LAUNCH((set_kernel<float>), vec_grid(len), BLK, (float *)x, len, float(a));
   LAUNCH_CHECK(mg);
   return 0;
 }
 
 int k_copy(gmg_mg *mg, int prec, void *x, const void *y, long long len) {
   if (len <= 0) return 0;
-  if (prec == GMG_PREC_FP64) copy_kernel<double><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)x, (const double *)y, len);
-  else copy_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)x, (const float *)y, len);
+  if (prec == GMG_PREC_FP64) GMG_LAUNCH((copy_kernel<double>), vec_grid(len), BLK, (double *)x, (const double *)y, len);
+  else GMG_LAUNCH((copy_kernel<float>), vec_grid(len), BLK, (float *)x, (const float *)y, len);
   LAUNCH_CHECK(mg);
   return 0;
 }
 
 int k_add(gmg_mg *mg, int prec, void *x, const void *y, long long len) {
   if (len <= 0) return 0;
-  if (prec == GMG_PREC_FP64) add_kernel<double><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)x, (const double *)y, len);
-  else add_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)x, (const float *)y, len);
+  if (prec == GMG_PREC_FP64) GMG_LAUNCH((add_kernel<double>), vec_grid(len), BLK, (double *)x, (const double *)y, len);
+  else GMG_LAUNCH((add_kernel<float>), vec_grid(len), BLK, (float *)x, (const float *)y, len);
   LAUNCH_CHECK(mg);
   return 0;
 }
@@ -611,7 +657,7 @@ int k_scale(gmg_mg *mg, int prec, void *x, int n, int s, const double *damp) {
   bool unit = true;
   for (int r = 0; r < s; ++r) unit = unit && damp[r] == 1.0;
   if (unit || n <= 0) return 0;  // dscalx by 1 is the identity
-#define SC(TT, SS) scale_kernel<TT, SS><<<grid_for(n), BLK, 0, mg->stream>>>((TT *)x, n, make_damp<TT>(damp, SS))
+#define SC(TT, SS) GMG_LAUNCH((scale_kernel<TT, SS>), grid_for(n), BLK, (TT *)x, n, make_damp<TT>(damp, SS))
   if (prec == GMG_PREC_FP64) {
     if (s == 1) SC(double, 1); else if (s == 2) SC(double, 2); else if (s == 3) SC(double, 3);
     else { set_error("block size %d not compiled", s); return 1; }
@@ -628,9 +674,9 @@ int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long 
   if (len <= 0) return 0;
   if (dp == sp) return k_copy(mg, dp, dst, src, len);
   if (dp == GMG_PREC_FP32)
-    convert_kernel<float, double><<<vec_grid(len), BLK, 0, mg->stream>>>((float *)dst, (const double *)src, len);
+    GMG_LAUNCH((convert_kernel<float, double>), vec_grid(len), BLK, (float *)dst, (const double *)src, len);
   else
-    convert_kernel<double, float><<<vec_grid(len), BLK, 0, mg->stream>>>((double *)dst, (const float *)src, len);
+    GMG_LAUNCH((convert_kernel<double, float>), vec_grid(len), BLK, (double *)dst, (const float *)src, len);
   LAUNCH_CHECK(mg);
   return 0;
 }
@@ -638,7 +684,7 @@ int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long 
 int k_add_mixed(gmg_mg *mg, double *x, int sp, const void *c, long long len) {
   if (len <= 0) return 0;
   if (sp == GMG_PREC_FP64) return k_add(mg, GMG_PREC_FP64, x, c, len);
-  add_mixed_kernel<float><<<vec_grid(len), BLK, 0, mg->stream>>>(x, (const float *)c, len);
+  GMG_LAUNCH((add_mixed_kernel<float>), vec_grid(len), BLK, x, (const float *)c, len);
   LAUNCH_CHECK(mg);
   return 0;
 }
@@ -662,7 +708,7 @@ int k_matmul_minus_mixed(gmg_mg *mg, const Level &L, double *x, int yprec, const
 int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp) {
   if (L.n == 0) return 0;
 #define JK(TT, SS, ALL)                                                                                     \
-  jac_kernel<TT, SS, ALL><<<grid_for(L.n), BLK, 0, mg->stream>>>(L.n, dinv_of<TT>(L), L.flags, (const TT *)b, \
+  GMG_LAUNCH((jac_kernel<TT, SS, ALL>), grid_for(L.n), BLK, L.n, dinv_of<TT>(L), L.flags, (const TT *)b, \
                                                                  (TT *)t, make_damp<TT>(damp, SS))
 #define JS(TT)                                                                      \
   if (L.s == 1) { if (L.all_active) JK(TT, 1, true); else JK(TT, 1, false); }       \
@@ -715,7 +761,7 @@ int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
 int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp) {
   if (C.n == 0) return 0;
 #define RK(TT, SS)                                                                                            \
-  restrict_kernel<TT, SS><<<grid_for(C.n), BLK, 0, mg->stream>>>(C.n, F.R.rowptr, F.R.col, mval<TT>(F.R), C.flags, \
+  GMG_LAUNCH((restrict_kernel<TT, SS>), grid_for(C.n), BLK, C.n, F.R.rowptr, F.R.col, mval<TT>(F.R), C.flags, \
                                                                  C.skip, (const TT *)from, (TT *)to,            \
                                                                  make_damp<TT>(damp, SS))
 #define RS(TT)                                  \
@@ -734,7 +780,7 @@ int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, c
 int k_interpolate(gmg_mg *mg, const Level &F, int prec, void *to, const void *from, const double *damp, void *acc) {
   if (F.n == 0) return 0;
 #define IK(TT, SS, A)                                                                                              \
-  interp_kernel<TT, SS, A><<<grid_for(F.n), BLK, 0, mg->stream>>>(F.n, F.P.rowptr, F.P.col, mval<TT>(F.P), F.skip, \
+  GMG_LAUNCH((interp_kernel<TT, SS, A>), grid_for(F.n), BLK, F.n, F.P.rowptr, F.P.col, mval<TT>(F.P), F.skip, \
                                                                   (const TT *)from, (TT *)to,                        \
                                                                   make_damp<TT>(damp, SS), (TT *)acc)
 #define IS(TT)                                                                \
@@ -754,10 +800,10 @@ int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x) {
   const int nb = REDUCE_BLOCKS;
   bool all = L.all_active;  // every row ACTIVE implies every row NEW_DEFECT
 #define N1(TT, SS)                                                                                            \
-  { if (all) nrm_stage1<TT, SS, true><<<nb, BLK, 0, mg->stream>>>(L.n, (const TT *)x, L.flags, mg->partial);  \
-    else nrm_stage1<TT, SS, false><<<nb, BLK, 0, mg->stream>>>(L.n, (const TT *)x, L.flags, mg->partial);     \
+  { if (all) GMG_LAUNCH((nrm_stage1<TT, SS, true>), nb, BLK, L.n, (const TT *)x, L.flags, mg->partial);  \
+    else GMG_LAUNCH((nrm_stage1<TT, SS, false>), nb, BLK, L.n, (const TT *)x, L.flags, mg->partial);     \
     LAUNCH_CHECK(mg);                                                                                         \
-    nrm_stage2<SS><<<1, 1024, 0, mg->stream>>>(nb, mg->partial, mg->norms_dev);                               \
+    GMG_LAUNCH((nrm_stage2<SS>), 1, 1024, nb, mg->partial, mg->norms_dev);                               \
     LAUNCH_CHECK(mg); return 0; }
   if (prec == GMG_PREC_FP64) {
     if (L.s == 1) N1(double, 1) if (L.s == 2) N1(double, 2) if (L.s == 3) N1(double, 3)
@@ -773,7 +819,7 @@ int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t
   GMG_CHECK(L.ainv, "base level inverse not computed (ex PreProcess)");
   Damp<double> al = make_damp<double>(abslimit, L.s);
 #define BK(TT, SS)                                                                                             \
-  base_kernel<TT, SS><<<1, 1024, 0, mg->stream>>>(L.n, L.ainv, L.A.rowptr, L.A.col, mval<TT>(L.A), (TT *)c,    \
+  GMG_LAUNCH((base_kernel<TT, SS>), 1, 1024, L.n, L.ainv, L.A.rowptr, L.A.col, mval<TT>(L.A), (TT *)c,    \
                                                   (TT *)b, (TT *)t, al)
 #define BS(TT)                                   \
   if (L.s == 1) BK(TT, 1);                       \
@@ -790,16 +836,16 @@ int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t
 
 int k_gather(gmg_mg *mg, int prec, void *dst, const double *src, const int *perm, int n, int s) {
   if (n == 0) return 0;
-  if (prec == GMG_PREC_FP64) gather_kernel<double><<<grid_for(n), BLK, 0, mg->stream>>>((double *)dst, src, perm, n, s);
-  else gather_kernel<float><<<grid_for(n), BLK, 0, mg->stream>>>((float *)dst, src, perm, n, s);
+  if (prec == GMG_PREC_FP64) GMG_LAUNCH((gather_kernel<double>), grid_for(n), BLK, (double *)dst, src, perm, n, s);
+  else GMG_LAUNCH((gather_kernel<float>), grid_for(n), BLK, (float *)dst, src, perm, n, s);
   LAUNCH_CHECK(mg);
   return 0;
 }
 
 int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *perm, int n, int s) {
   if (n == 0) return 0;
-  if (prec == GMG_PREC_FP64) scatter_kernel<double><<<grid_for(n), BLK, 0, mg->stream>>>(dst, (const double *)src, perm, n, s);
-  else scatter_kernel<float><<<grid_for(n), BLK, 0, mg->stream>>>(dst, (const float *)src, perm, n, s);
+  if (prec == GMG_PREC_FP64) GMG_LAUNCH((scatter_kernel<double>), grid_for(n), BLK, dst, (const double *)src, perm, n, s);
+  else GMG_LAUNCH((scatter_kernel<float>), grid_for(n), BLK, dst, (const float *)src, perm, n, s);
   LAUNCH_CHECK(mg);
   return 0;
 }

@@ -12,6 +12,8 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <queue>
+#include <tuple>
 
 #include "gmg_internal.h"
 #include "gmg_np.h"
@@ -85,19 +87,38 @@ int invert_block(int s, const double *m, double *inv) {
 }
 
 // ------------------------------------------------------------ orderings and schedules
-// Greedy colouring of the (symmetrised) matrix graph in list order; returns
-// the colour of every VECTOR.
+// Colouring of the (symmetrised) matrix graph by saturation degree (DSATUR,
+// Brelaz 1979): repeatedly colour the uncoloured VECTOR with the most
+// distinct colours among its neighbours (ties: larger degree, then smaller
+// list position) with the smallest free colour.  Fewer colours mean fewer
+// wavefronts per Gauss-Seidel sweep (4 instead of greedy's 8 on the
+// Freudenthal tetrahedral meshes, 3 on the triangle meshes).
 static std::vector<int> greedy_colour(int n, const std::vector<std::vector<int>> &adj, int *ncol) {
-  std::vector<int> colour(n, -1), mark;
+  std::vector<int> colour(n, -1);
+  std::vector<std::vector<char>> seen(n);
+  std::vector<int> sat(n, 0);
+  using Key = std::tuple<int, int, int>;  // (saturation, degree, -index), max first
+  std::priority_queue<Key> pq;
+  for (int i = 0; i < n; ++i) pq.push(Key(0, int(adj[i].size()), -i));
   int nc = 0;
-  for (int i = 0; i < n; ++i) {
-    mark.assign(nc + 1, 0);
-    for (int j : adj[i])
-      if (colour[j] >= 0) mark[colour[j]] = 1;
+  while (!pq.empty()) {
+    Key k = pq.top();
+    pq.pop();
+    int i = -std::get<2>(k);
+    if (colour[i] >= 0 || std::get<0>(k) != sat[i]) continue;
     int c = 0;
-    while (c < nc && mark[c]) ++c;
+    while (c < int(seen[i].size()) && seen[i][c]) ++c;
     colour[i] = c;
-    if (c == nc) ++nc;
+    nc = std::max(nc, c + 1);
+    for (int j : adj[i]) {
+      if (colour[j] >= 0) continue;
+      if (int(seen[j].size()) <= c) seen[j].resize(c + 1, 0);
+      if (!seen[j][c]) {
+        seen[j][c] = 1;
+        ++sat[j];
+        pq.push(Key(sat[j], int(adj[j].size()), -j));
+      }
+    }
   }
   *ncol = nc;
   return colour;

@@ -555,7 +555,7 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
       if (mg->lev[i].n <= -baselevel) break;
     baselevel = i;
   }
-  if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 40000;
+  if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 6000;
   if (!a.get_int("cluster", &cluster)) cluster = 16;
   if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return NP_NOT_ACTIVE;
   int ret = InitIter(a);
@@ -633,7 +633,8 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   if (!t) t = temp_vec(mg, name + "__t" + std::to_string(prec), prec);
   GMG_CHECK(t, "lmgc: temporary vector");
   const int smo = fusable_smoother();
-  if (smo >= 0 && mg->lev[level].n <= fuse_rows) {
+  if (smo >= 0 && mg->lev[level].n <= fuse_rows &&
+      coarse_smem_bytes(mg, baselevel, level, prec, smo) <= COARSE_SMEM_BUDGET) {
     // this level and everything below it: one cluster kernel
     CoarseCfg cfg;
     cfg.bl = baselevel; cfg.lc = level; cfg.smoother = smo;
@@ -1104,6 +1105,7 @@ int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *, const double *beta) {
   tmp.mg = mg;
   for (int i = 0; i < GMG_MAX_S; ++i) tmp.beta[i] = beta ? beta[i] : 0.0;
   mg->lev[level].ilu_ready = false;
+  mg->coarse_images.clear();  // fused images hold copies of the factors
   int bl = 0, res = 0;
   return tmp.PreProcess(level, nullptr, nullptr, nullptr, &bl, &res);
 }

@@ -122,7 +122,7 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   gmg_vec *t64 = nullptr, *t32 = nullptr;  // the temporary t of Lmgc (AllocVDFromVD)
   // levels with at most fuse_rows VECTORs run as one fused cluster kernel
   // (gmg_coarse.cu); 0 disables.  cluster = CTAs of that kernel's cluster.
-  int fuse_rows = 40000, cluster = 16;
+  int fuse_rows = 6000, cluster = 16;
   int Init(const Args &a) override;
   // smoother code of the fused kernel (0 jac, 1 gs, 2 ilu) or -1 if this
   // configuration cannot be fused
