@@ -195,3 +195,41 @@ def test_full_size_p1_diffusion_gs(G, oracle_mod):
     assert lr.converged and conv and lr.iters == ito
     assert rel(x, xr) <= 1e-10
     mg.close()
+
+
+MID = [  # generator kind, nref, smoother, baselevel, var
+    (0, 6, "jac", 2, 0.0), (0, 6, "gs", 2, 0.0), (0, 6, "ilu", 2, 0.0),
+    (1, 4, "gs", 0, 1.0), (1, 4, "ilu", 0, 1.0), (1, 4, "jac", 0, 1.0),
+    (2, 6, "gs", 1, 0.0), (2, 6, "ilu", 1, 0.0), (2, 6, "jac", 1, 0.0),
+]
+
+
+@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("kind,nref,sm,bl,var", MID)
+def test_midsize_vs_oracle(G, oracle_mod, kind, nref, sm, bl, var, order):
+    """Levels above 2048 VECTORs use the sliced-ELLPACK kernels (and, in
+    multicolour order, colour-range Gauss-Seidel waves); small levels the
+    shared-memory fused cycle.  Same iterations and solution as the oracle."""
+    gen = G.Generator(kind, nref, seed=5, corr=0.1, var=var)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=order, fp32=True)
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    x, lr = mg.solve_host("mgs", gen.rhs)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    perm = mg.order(mg.top)
+    s = levels[-1]["s"]
+    xo, ito, conv, _ = H.ls_solve(gen.rhs.reshape(-1, s)[perm].ravel(), smoother=sm, baselevel=bl,
+                                  damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    xr = np.empty((len(perm), s)); xr[perm] = xo.reshape(-1, s)
+    assert conv and lr.converged and lr.iters == ito
+    assert rel(x, xr.ravel()) <= 1e-10
+    # the mixed-precision solver on the same device hierarchy
+    mg.npcreate("mgs32", "linear_solver.gls")
+    mg.npinit("mgs32", "$A MAT $x sol $b rhs $red 1e-8 $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    x32, lr32 = mg.solve_host("mgs32", gen.rhs)
+    _, it8, _, _ = H.ls_solve(gen.rhs.reshape(-1, s)[perm].ravel(), smoother=sm, baselevel=bl,
+                              damp=_damp(sm), red=1e-8, abslimit=1e-50)
+    assert lr32.converged and abs(lr32.iters - it8) <= 1
+    d = H.matmul_minus(mg.top, gen.rhs.reshape(-1, s)[perm].ravel(), x32.reshape(-1, s)[perm].ravel())
+    assert np.all(H.nrm2x(mg.top, d) <= 1.01e-8 * H.nrm2x(mg.top, gen.rhs.reshape(-1, s)[perm].ravel()))
+    mg.close()

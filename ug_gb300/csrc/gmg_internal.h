@@ -102,6 +102,16 @@ struct Level {
   int base_dim = 0;
   // SpMV variant: threads cooperating on one row
   int tpr = 8;
+  // sliced ELLPACK copy of A (slices of 32 consecutive rows stored column by
+  // column, padded to the slice's longest row with zero blocks pointing at the
+  // row itself): one thread per row, coalesced 32-row loads, no reductions
+  bool sell = false;
+  int *sell_ptr = nullptr;  // nslices+1 entry offsets
+  int *sell_col = nullptr;
+  double *sell_v64 = nullptr;
+  float *sell_v32 = nullptr;
+  // the forward schedule's wavefronts are contiguous row ranges (multicolour order)
+  bool waves_contiguous = false;
 };
 
 struct Vec {

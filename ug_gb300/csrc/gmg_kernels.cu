@@ -154,6 +154,87 @@ __global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__res
   }
 }
 
+// Sliced-ELLPACK dmatmul_minus: one thread per row; entry k of the 32 rows
+// of a slice are adjacent, so a warp loads 32 consecutive columns and values
+// per step, all loads of a row are independent (no row-pointer chain, no
+// shuffle reduction: one FMA per stored entry, which matters for FP64 on
+// GB300).  Padding entries are zero blocks at the row itself.
+template <class T, class TY, int S, bool ACC>
+__global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__restrict__ sptr,
+                                                        const int *__restrict__ scol, const T *__restrict__ sval,
+                                                        const TY *__restrict__ y, T *__restrict__ x,
+                                                        TY *__restrict__ acc) {
+  pdl_prologue();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int e0 = __ldg(sptr + (i >> 5));
+  const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  int e = e0 + (i & 31);
+#pragma unroll 4
+  for (int k = 0; k < w; ++k, e += 32) {
+    const int j = __ldg(scol + e);
+    const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      const T yv = T(__ldg(y + (size_t)j * S + c));
+#pragma unroll
+      for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + c), yv, s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    x[(size_t)i * S + r] -= s[r];
+    if (ACC) acc[(size_t)i * S + r] += y[(size_t)i * S + r];
+  }
+}
+
+// Sliced-ELLPACK l_lgs wave over the contiguous rows [r0, r1) of one colour:
+// entries to rows j < i (earlier colours) are final, the diagonal (entry 0)
+// and the padding (j == i) are skipped.
+template <class T, int S, bool ALL_ACTIVE>
+__global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int *__restrict__ sptr,
+                                                      const int *__restrict__ scol, const T *__restrict__ sval,
+                                                      const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
+                                                      const T *__restrict__ b, T *__restrict__ t) {
+  pdl_prologue();
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  if (!ALL_ACTIVE && !(flags[i] & F_ACTIVE)) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) t[(size_t)i * S + r] = T(0);
+    return;
+  }
+  const int e0 = __ldg(sptr + (i >> 5));
+  const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = b[(size_t)i * S + r];
+  int e = e0 + (i & 31) + 32;
+#pragma unroll 4
+  for (int k = 1; k < w; ++k, e += 32) {
+    const int j = __ldg(scol + e);
+    if (j >= i) continue;
+    const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      const T tv = t[(size_t)j * S + c];
+#pragma unroll
+      for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + c), tv, s[r]);
+    }
+  }
+  const T *D = dinv + (size_t)i * S * S;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    T v = T(0);
+#pragma unroll
+    for (int c = 0; c < S; ++c) v = fma(D[r * S + c], s[c], v);
+    t[(size_t)i * S + r] = v;
+  }
+}
+
 // ------------------------------------------------------------ l_jac
 // ugiter.cc:271: t = D^{-1} b on ACTIVE rows (0 elsewhere), then the
 // smoother's dscalx by damp (iter.cc:836).  D^{-1} is stored per row.
@@ -549,8 +630,26 @@ int spmv_dispatch_tpr(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *
   return 0;
 }
 
+template <class T>
+const T *sell_val(const Level &L);
+template <>
+const double *sell_val<double>(const Level &L) { return L.sell_v64; }
+template <>
+const float *sell_val<float>(const Level &L) { return L.sell_v32; }
+
 template <class T, class TY, bool ACC>
 int spmv_dispatch(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, TY *acc) {
+  if (L.sell && sell_val<T>(L)) {
+    const T *sv = sell_val<T>(L);
+    switch (L.s) {
+      case 1: GMG_LAUNCH((sell_spmv_kernel<T, TY, 1, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      case 2: GMG_LAUNCH((sell_spmv_kernel<T, TY, 2, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      case 3: GMG_LAUNCH((sell_spmv_kernel<T, TY, 3, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      default: set_error("block size %d not compiled", L.s); return 1;
+    }
+    LAUNCH_CHECK(mg);
+    return 0;
+  }
   switch (L.s) {
     case 1: return spmv_dispatch_tpr<T, TY, 1, ACC>(mg, L, val, x, y, acc);
     case 2: return spmv_dispatch_tpr<T, TY, 2, ACC>(mg, L, val, x, y, acc);
@@ -723,8 +822,36 @@ int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const do
   return 0;
 }
 
+template <class T, int S>
+int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
+  const T *sv = sell_val<T>(L), *dinv = dinv_of<T>(L);
+  for (int w = 0; w < L.lower.nwave(); ++w) {
+    const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
+    if (r1 <= r0) continue;
+    if (L.all_active)
+      GMG_LAUNCH((sell_gs_kernel<T, S, true>), grid_for(r1 - r0), BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv,
+                 L.flags, b, t);
+    else
+      GMG_LAUNCH((sell_gs_kernel<T, S, false>), grid_for(r1 - r0), BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv,
+                 L.flags, b, t);
+    LAUNCH_CHECK(mg);
+  }
+  return 0;
+}
+
 int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
   if (L.n == 0) return 0;
+  if (L.sell && L.waves_contiguous) {
+    if (prec == GMG_PREC_FP64) {
+      if (L.s == 1) return sell_gs_waves<double, 1>(mg, L, (double *)t, (const double *)b);
+      if (L.s == 2) return sell_gs_waves<double, 2>(mg, L, (double *)t, (const double *)b);
+      if (L.s == 3) return sell_gs_waves<double, 3>(mg, L, (double *)t, (const double *)b);
+    } else if (L.sell_v32 && L.dinv32) {
+      if (L.s == 1) return sell_gs_waves<float, 1>(mg, L, (float *)t, (const float *)b);
+      if (L.s == 2) return sell_gs_waves<float, 2>(mg, L, (float *)t, (const float *)b);
+      if (L.s == 3) return sell_gs_waves<float, 3>(mg, L, (float *)t, (const float *)b);
+    }
+  }
   const int tp = tri_tpr(L);
 #define GS(TT, SS)                                                                      \
   return tp == 4 ? gs_waves<TT, SS, 4>(mg, L, (TT *)t, (const TT *)b)                   \

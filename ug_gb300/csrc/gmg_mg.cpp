@@ -192,9 +192,40 @@ struct HostLevel {
   std::vector<int> lptr, lrows, uptr, urows;
   std::vector<int> prow, pcol, rrow, rcol;
   std::vector<double> pw, rw;
-  bool all_active = true, any_skip = false;
+  bool all_active = true, any_skip = false, contiguous = false;
   int ncolour = 0;
+  std::vector<int> sptr, scol;  // sliced ELLPACK (32-row slices)
+  std::vector<double> sval;
 };
+
+constexpr int SELL_MIN_ROWS = 2048;  // smaller levels keep the CSR kernels
+
+static void build_sell(HostLevel &H) {
+  const int n = H.n, ss = H.s * H.s, ns = (n + 31) / 32;
+  H.sptr.assign(ns + 1, 0);
+  for (int sl = 0; sl < ns; ++sl) {
+    int w = 0;
+    for (int i = sl * 32; i < std::min(n, sl * 32 + 32); ++i) w = std::max(w, H.rowptr[i + 1] - H.rowptr[i]);
+    H.sptr[sl + 1] = H.sptr[sl] + 32 * w;
+  }
+  H.scol.assign(H.sptr[ns], 0);
+  H.sval.assign(size_t(H.sptr[ns]) * ss, 0.0);
+  for (int sl = 0; sl < ns; ++sl) {
+    const int w = (H.sptr[sl + 1] - H.sptr[sl]) / 32;
+    for (int lane = 0; lane < 32; ++lane) {
+      const int i = sl * 32 + lane;
+      for (int k = 0; k < w; ++k) {
+        const size_t e = size_t(H.sptr[sl]) + size_t(k) * 32 + lane;
+        if (i < n && k < H.rowptr[i + 1] - H.rowptr[i]) {
+          H.scol[e] = H.col[H.rowptr[i] + k];
+          std::memcpy(&H.sval[e * ss], &H.val[size_t(H.rowptr[i] + k) * ss], sizeof(double) * ss);
+        } else {
+          H.scol[e] = i < n ? i : 0;  // padding: zero block at the row itself
+        }
+      }
+    }
+  }
+}
 
 static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H) {
   const int n = d.n, s = d.s, ss = s * s;
@@ -211,6 +242,20 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H) {
   if (order == GMG_ORDER_COLOR && n > 0) {
     std::vector<int> colour = greedy_colour(n, adj, &H.ncolour);
     std::stable_sort(H.perm.begin(), H.perm.end(), [&](int a, int b) { return colour[a] < colour[b]; });
+    // the wavefronts are the colour classes: contiguous ranges of the processing order
+    H.lptr.assign(H.ncolour + 1, 0);
+    for (int i = 0; i < n; ++i) H.lptr[colour[i] + 1]++;
+    for (int c = 0; c < H.ncolour; ++c) H.lptr[c + 1] += H.lptr[c];
+    H.lrows.resize(n);
+    std::iota(H.lrows.begin(), H.lrows.end(), 0);
+    // backward sweeps take the colours last to first
+    H.uptr.assign(1, 0);
+    H.urows.clear();
+    for (int c = H.ncolour - 1; c >= 0; --c) {
+      for (int i = H.lptr[c]; i < H.lptr[c + 1]; ++i) H.urows.push_back(i);
+      H.uptr.push_back(int(H.urows.size()));
+    }
+    H.contiguous = true;
   }
   H.iperm.resize(n);
   for (int i = 0; i < n; ++i) H.iperm[H.perm[i]] = i;
@@ -247,13 +292,16 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H) {
     GMG_CHECK(!invert_block(s, &H.val[size_t(H.rowptr[i]) * ss], &H.dinv[size_t(i) * ss]),
               "singular diagonal block in row %d", H.perm[i]);
   }
-  // wavefronts in processing order
-  std::vector<std::vector<int>> padj(n);
-  for (int i = 0; i < n; ++i) {
-    for (int j : adj[H.perm[i]]) padj[i].push_back(H.iperm[j]);
+  // wavefronts (level sets) of the list order
+  if (!H.contiguous) {
+    std::vector<std::vector<int>> padj(n);
+    for (int i = 0; i < n; ++i) {
+      for (int j : adj[H.perm[i]]) padj[i].push_back(H.iperm[j]);
+    }
+    wavefronts(n, padj, true, H.lptr, H.lrows);
+    wavefronts(n, padj, false, H.uptr, H.urows);
   }
-  wavefronts(n, padj, true, H.lptr, H.lrows);
-  wavefronts(n, padj, false, H.uptr, H.urows);
+  if (n >= SELL_MIN_ROWS) build_sell(H);
   return 0;
 }
 
@@ -391,6 +439,8 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
     bytes += al((h.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * 8) + (f32 ? al(nnz * ss * 4) : 0);
     bytes += al(h.n * ss * 8) + (f32 ? al(h.n * ss * 4) : 0) + 2 * al(h.n) + 3 * al(h.n * 4);
     bytes += al(h.lptr.size() * 4) + al(h.uptr.size() * 4);
+    if (!h.sptr.empty())
+      bytes += al(h.sptr.size() * 4) + al(h.scol.size() * 4) + al(h.sval.size() * 8) + (f32 ? al(h.sval.size() * 4) : 0);
     if (l > 0) {
       size_t pn = h.pcol.size(), rn = h.rcol.size();
       bytes += al((h.n + 1) * 4) + al(pn * 4) + al(pn * 8) + (f32 ? al(pn * 4) : 0);
@@ -463,6 +513,24 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
       }
     }
     L.tpr = pick_tpr(h);
+    L.waves_contiguous = h.contiguous;
+    if (!h.sptr.empty()) {
+      L.sell = true;
+      L.sell_ptr = mg->arena.take_n<int>(h.sptr.size());
+      L.sell_col = mg->arena.take_n<int>(h.scol.size());
+      L.sell_v64 = mg->arena.take_n<double>(h.sval.size());
+      if (upload(L.sell_ptr, h.sptr.data(), h.sptr.size()) || upload(L.sell_col, h.scol.data(), h.scol.size()) ||
+          upload(L.sell_v64, h.sval.data(), h.sval.size()))
+        return 1;
+      if (f32) {
+        L.sell_v32 = mg->arena.take_n<float>(h.sval.size());
+        auto sv = to_f32(h.sval);
+        if (upload(L.sell_v32, sv.data(), sv.size())) return 1;
+      }
+      std::vector<int>().swap(h.sptr);
+      std::vector<int>().swap(h.scol);
+      std::vector<double>().swap(h.sval);
+    }
     // keep host copies for the ILU / base factorisations and for export
     L.perm = std::move(h.perm);
     L.h_rowptr = std::move(h.rowptr);
