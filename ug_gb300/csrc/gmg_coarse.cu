@@ -92,6 +92,7 @@ template <class T, int S, int G, bool LOWER>
 __device__ __forceinline__ void row_dot(const int *rowptr, const int *col, const T *val, const T *v, int row,
                                         int first, int lane, bool on, T *s) {
   const int k1 = on ? rowptr[row + 1] : 0;
+#pragma unroll 4
   for (int k = on ? rowptr[row] + first + lane : 0; k < k1; k += G) {
     const int j = col[k];
     if (LOWER && j >= row) continue;
@@ -350,8 +351,19 @@ __global__ void __launch_bounds__(CBLK, 1) coarse_cycle_kernel(const __grid_cons
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   extern __shared__ int4 smem4[];
   char *sm = reinterpret_cast<char *>(smem4);
-  // static image: 128-bit copies
-  for (int i = threadIdx.x; i < a.image_bytes / 16; i += blockDim.x) smem4[i] = __ldg(a.image + i);
+  // static image: 128-bit copies, eight loads in flight per thread
+  {
+    const int nv = a.image_bytes / 16, bd = blockDim.x;
+    int i = threadIdx.x;
+    for (; i + 7 * bd < nv; i += 8 * bd) {
+      int4 r[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) r[u] = __ldg(a.image + i + u * bd);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) smem4[i + u * bd] = r[u];
+    }
+    for (; i < nv; i += bd) smem4[i] = __ldg(a.image + i);
+  }
   // vectors: b and c of every fused level
   for (int k = 0; k < a.nl; ++k) {
     const SLev &s = a.L[k];

@@ -176,6 +176,8 @@ int k_add_mixed(gmg_mg *mg, double *x64, int src_prec, const void *c, long long 
 int k_matmul_minus(gmg_mg *mg, const Level &L, int prec, void *x, const void *y, void *acc);
 // FP64 x -= A64 y with y of precision yprec (iterative-refinement defect)
 int k_matmul_minus_mixed(gmg_mg *mg, const Level &L, double *x, int yprec, const void *y);
+// iterative-refinement update in one pass: b -= A64 c; x += c (c in FP32)
+int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const float *c);
 // t = damp * D^{-1} b on ACTIVE rows, 0 elsewhere
 int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp);
 // forward Gauss-Seidel in processing order over the wavefronts; t is overwritten
@@ -183,8 +185,11 @@ int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // ILU forward / backward solve with the factors of L
 int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // coarse = (reset ? 0 : coarse) + R (damp*fine), honouring coarse VECSKIP
+// (zero_coarse, if given, is set to 0 on the coarse level in the same pass)
 int k_restrict(gmg_mg *mg, const Level &fine, const Level &coarse, int prec, void *to, const void *from,
-               const double *damp);
+               const double *damp, void *zero_coarse = nullptr);
+// b32 = b64 and c32 = 0 in one pass (start of a mixed-precision iteration)
+int k_refine_prepare(gmg_mg *mg, float *b32, float *c32, const double *b64, long long len);
 // fine t = P (damp*coarse) honouring fine VECSKIP; acc += t if acc != null
 int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void *from, const double *damp,
                   void *acc);

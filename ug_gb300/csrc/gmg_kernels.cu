@@ -98,6 +98,13 @@ __global__ void convert_kernel(TD *x, const TS *__restrict__ y, long long len) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
     x[i] = TD(y[i]);
 }
+__global__ void refine_prepare_kernel(float *b32, float *c32, const double *__restrict__ b64, long long len) {
+  pdl_prologue();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    b32[i] = float(b64[i]);
+    c32[i] = 0.0f;
+  }
+}
 template <class TS>
 __global__ void add_mixed_kernel(double *x, const TS *__restrict__ y, long long len) {
   pdl_prologue();
@@ -158,12 +165,14 @@ __global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__res
 // of a slice are adjacent, so a warp loads 32 consecutive columns and values
 // per step, all loads of a row are independent (no row-pointer chain, no
 // shuffle reduction: one FMA per stored entry, which matters for FP64 on
-// GB300).  Padding entries are zero blocks at the row itself.
-template <class T, class TY, int S, bool ACC>
+// GB300).  Padding entries are zero blocks at the row itself.  (Loading a
+// row's column indices in one predicated batch before the gathers measured
+// slower on GB300 than this plain loop, which the compiler pipelines.)
+template <class T, class TY, class TA, int S, bool ACC>
 __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__restrict__ sptr,
                                                         const int *__restrict__ scol, const T *__restrict__ sval,
                                                         const TY *__restrict__ y, T *__restrict__ x,
-                                                        TY *__restrict__ acc) {
+                                                        TA *__restrict__ acc) {
   pdl_prologue();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -187,7 +196,7 @@ __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__rest
 #pragma unroll
   for (int r = 0; r < S; ++r) {
     x[(size_t)i * S + r] -= s[r];
-    if (ACC) acc[(size_t)i * S + r] += y[(size_t)i * S + r];
+    if (ACC) acc[(size_t)i * S + r] += TA(y[(size_t)i * S + r]);
   }
 }
 
@@ -410,10 +419,13 @@ template <class T, int S>
 __global__ void restrict_kernel(int nc, const int *__restrict__ rrow, const int *__restrict__ rcol,
                                 const T *__restrict__ rw, const uint8_t *__restrict__ cflags,
                                 const uint8_t *__restrict__ cskip, const T *__restrict__ from, T *__restrict__ to,
-                                Damp<T> dm) {
+                                Damp<T> dm, T *__restrict__ zero) {
   pdl_prologue();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
+  if (zero)  // lmgc's dset(c_{l-1}, 0), iter.cc:7873, in the same pass
+#pragma unroll
+    for (int r = 0; r < S; ++r) zero[(size_t)c * S + r] = T(0);
   const bool reset = cflags[c] & F_RESET;
   const int sk = cskip[c];
   T acc[S];
@@ -468,6 +480,62 @@ __global__ void interp_kernel(int nf, const int *__restrict__ prow, const int *_
 // ugblas.cc:3156: per-component sums of squares over the NEW_DEFECT rows,
 // accumulated in FP64 whatever the vector precision, in two deterministic
 // stages (fixed grid, fixed reduction tree), then square roots.
+// Both stages in one launch: every block writes its partial sums, takes a
+// ticket, and the block that draws the last ticket adds the partials in
+// block order (so the result does not depend on which block finishes last),
+// writes the norms and resets the ticket counter for the next call.
+template <class T, int S, bool ALL>
+__global__ void __launch_bounds__(BLK) nrm_kernel(int n, const T *__restrict__ x, const uint8_t *__restrict__ flags,
+                                                  double *__restrict__ partial, unsigned *__restrict__ ticket,
+                                                  double *__restrict__ out) {
+  pdl_prologue();
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!ALL && !(flags[i] & F_NEWDEF)) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      double v = double(x[(size_t)i * S + r]);
+      acc[r] = fma(v, v, acc[r]);
+    }
+  }
+  __shared__ double sh[BLK / 32][S];
+  __shared__ bool last;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * S + threadIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[BLK];
+  for (int r = 0; r < S; ++r) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(partial + (size_t)b * S + r);
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[r] = sqrt(red[0]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
 template <class T, int S, bool ALL>
 __global__ void __launch_bounds__(BLK) nrm_stage1(int n, const T *__restrict__ x, const uint8_t *__restrict__ flags,
                                                   double *__restrict__ partial) {
@@ -642,9 +710,9 @@ int spmv_dispatch(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, T
   if (L.sell && sell_val<T>(L)) {
     const T *sv = sell_val<T>(L);
     switch (L.s) {
-      case 1: GMG_LAUNCH((sell_spmv_kernel<T, TY, 1, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
-      case 2: GMG_LAUNCH((sell_spmv_kernel<T, TY, 2, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
-      case 3: GMG_LAUNCH((sell_spmv_kernel<T, TY, 3, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      case 1: GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, 1, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      case 2: GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, 2, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      case 3: GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, 3, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
       default: set_error("block size %d not compiled", L.s); return 1;
     }
     LAUNCH_CHECK(mg);
@@ -780,6 +848,13 @@ int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long 
   return 0;
 }
 
+int k_refine_prepare(gmg_mg *mg, float *b32, float *c32, const double *b64, long long len) {
+  if (len <= 0) return 0;
+  GMG_LAUNCH(refine_prepare_kernel, vec_grid(len), BLK, b32, c32, b64, len);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_add_mixed(gmg_mg *mg, double *x, int sp, const void *c, long long len) {
   if (len <= 0) return 0;
   if (sp == GMG_PREC_FP64) return k_add(mg, GMG_PREC_FP64, x, c, len);
@@ -802,6 +877,22 @@ int k_matmul_minus(gmg_mg *mg, const Level &L, int prec, void *x, const void *y,
 int k_matmul_minus_mixed(gmg_mg *mg, const Level &L, double *x, int yprec, const void *y) {
   if (yprec == GMG_PREC_FP64) return k_matmul_minus(mg, L, GMG_PREC_FP64, x, y, nullptr);
   return spmv_dispatch<double, float, false>(mg, L, L.A.v64, x, (const float *)y, nullptr);
+}
+
+int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const float *c) {
+  if (L.n == 0) return 0;
+  if (!L.sell) {  // small levels: two passes
+    if (k_add_mixed(mg, x, GMG_PREC_FP32, c, (long long)L.n * L.s)) return 1;
+    return k_matmul_minus_mixed(mg, L, b, GMG_PREC_FP32, c);
+  }
+  switch (L.s) {
+    case 1: GMG_LAUNCH((sell_spmv_kernel<double, float, double, 1, true>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, L.sell_v64, c, b, x); break;
+    case 2: GMG_LAUNCH((sell_spmv_kernel<double, float, double, 2, true>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, L.sell_v64, c, b, x); break;
+    case 3: GMG_LAUNCH((sell_spmv_kernel<double, float, double, 3, true>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, L.sell_v64, c, b, x); break;
+    default: set_error("block size %d not compiled", L.s); return 1;
+  }
+  LAUNCH_CHECK(mg);
+  return 0;
 }
 
 int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp) {
@@ -885,12 +976,13 @@ int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
   return 1;
 }
 
-int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp) {
+int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp,
+               void *zero_coarse) {
   if (C.n == 0) return 0;
 #define RK(TT, SS)                                                                                            \
   GMG_LAUNCH((restrict_kernel<TT, SS>), grid_for(C.n), BLK, C.n, F.R.rowptr, F.R.col, mval<TT>(F.R), C.flags, \
                                                                  C.skip, (const TT *)from, (TT *)to,            \
-                                                                 make_damp<TT>(damp, SS))
+                                                                 make_damp<TT>(damp, SS), (TT *)zero_coarse)
 #define RS(TT)                                  \
   if (F.s == 1) RK(TT, 1);                      \
   else if (F.s == 2) RK(TT, 2);                 \
@@ -926,11 +1018,12 @@ int k_interpolate(gmg_mg *mg, const Level &F, int prec, void *to, const void *fr
 int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x) {
   const int nb = REDUCE_BLOCKS;
   bool all = L.all_active;  // every row ACTIVE implies every row NEW_DEFECT
-#define N1(TT, SS)                                                                                            \
-  { if (all) GMG_LAUNCH((nrm_stage1<TT, SS, true>), nb, BLK, L.n, (const TT *)x, L.flags, mg->partial);  \
-    else GMG_LAUNCH((nrm_stage1<TT, SS, false>), nb, BLK, L.n, (const TT *)x, L.flags, mg->partial);     \
-    LAUNCH_CHECK(mg);                                                                                         \
-    GMG_LAUNCH((nrm_stage2<SS>), 1, 1024, nb, mg->partial, mg->norms_dev);                               \
+  unsigned *ticket = reinterpret_cast<unsigned *>(mg->norms_dev + GMG_MAX_S);
+#define N1(TT, SS)                                                                                                  \
+  { if (all) GMG_LAUNCH((nrm_kernel<TT, SS, true>), nb, BLK, L.n, (const TT *)x, L.flags, mg->partial, ticket,      \
+                        mg->norms_dev);                                                                             \
+    else GMG_LAUNCH((nrm_kernel<TT, SS, false>), nb, BLK, L.n, (const TT *)x, L.flags, mg->partial, ticket,         \
+                    mg->norms_dev);                                                                                 \
     LAUNCH_CHECK(mg); return 0; }
   if (prec == GMG_PREC_FP64) {
     if (L.s == 1) N1(double, 1) if (L.s == 2) N1(double, 2) if (L.s == 3) N1(double, 3)

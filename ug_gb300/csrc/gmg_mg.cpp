@@ -541,7 +541,10 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
   }
   GMG_CHECK(mg->arena.used <= mg->arena.size, "arena overflow");
   // scratch
-  GMG_CUDA(cudaMalloc(&mg->partial, sizeof(double) * (REDUCE_BLOCKS * GMG_MAX_S + GMG_MAX_S)));
+  // reduction scratch: per-block partial sums, the norms, and the norm kernel's ticket counter
+  const size_t scratch = sizeof(double) * (REDUCE_BLOCKS * GMG_MAX_S + GMG_MAX_S + 1);
+  GMG_CUDA(cudaMalloc(&mg->partial, scratch));
+  GMG_CUDA(cudaMemset(mg->partial, 0, scratch));
   mg->norms_dev = mg->partial + REDUCE_BLOCKS * GMG_MAX_S;
   GMG_CUDA(cudaMallocHost(&mg->norms_host, sizeof(double) * GMG_MAX_S));
   mg->lev.back().own.push_back(mg->partial);

@@ -650,8 +650,15 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   for (int i = 0; i < nu1; ++i)
     if (PreSmooth->IterAcc(level, t, bv, Am, cv, result)) return 1;
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};  // Factor_One
-  if (Transfer->RestrictDefect(level, bv, bv, Am, one, result)) return 1;
-  if (k_set(mg, prec, vlev(cv, level - 1), vlen(mg, level - 1), 0.0)) return 1;
+  if (typeid(*Transfer) == typeid(NPTransfer)) {
+    // StandardRestrict and dset(c_{l-1}, 0) in one pass
+    if (k_restrict(mg, mg->lev[level], mg->lev[level - 1], prec, vlev(bv, level - 1), vlev(bv, level), one,
+                   vlev(cv, level - 1)))
+      return 1;
+  } else {
+    if (Transfer->RestrictDefect(level, bv, bv, Am, one, result)) return 1;
+    if (k_set(mg, prec, vlev(cv, level - 1), vlen(mg, level - 1), 0.0)) return 1;
+  }
   for (int i = 0; i < gamma; ++i)
     if (Iter(level - 1, cv, bv, Am, result)) return 1;
   // t = P c_{l-1} * damp; c += t (fused); b -= A t
@@ -786,11 +793,12 @@ int NPLs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) 
       return 1;
     }
   } else {
-    if (k_convert(mg, GMG_PREC_FP32, vlev(b32, level), bv->prec, vlev(bv, level), len)) return 1;
-    if (k_set(mg, GMG_PREC_FP32, vlev(cvec, level), len, 0.0)) return 1;
+    if (k_refine_prepare(mg, (float *)vlev(b32, level), (float *)vlev(cvec, level), (const double *)vlev(bv, level),
+                         len))
+      return 1;
     if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
-    if (k_add_mixed(mg, (double *)vlev(xv, level), GMG_PREC_FP32, vlev(cvec, level), len)) return 1;
-    if (k_matmul_minus_mixed(mg, L, (double *)vlev(bv, level), GMG_PREC_FP32, vlev(cvec, level))) return 1;
+    if (k_refine_update(mg, L, (double *)vlev(bv, level), (double *)vlev(xv, level), (const float *)vlev(cvec, level)))
+      return 1;
   }
   if (k_nrm2x(mg, L, bv->prec, vlev(bv, level))) return 1;
   GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
