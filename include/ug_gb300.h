@@ -159,6 +159,19 @@ int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);    
 int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp);            /* 462 */
 int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp); /* 529 */
 
+/* ------------------------------------------------ allocation-free norm
+ * No counterpart in the reference.  Per-component 2-norms of a device array
+ * x_dev (n rows of s doubles, row-major) into norms_dev (s doubles, device),
+ * for callers that cannot let a library call cudaMalloc: a host framework
+ * whose memory manager owns all device memory and only hands buffers over,
+ * or a process with a spent device-memory budget.  The reduction's scratch is
+ * a fixed array inside the library (about 20 KB per device, held until the
+ * process exits); s above GMG_MAX_S is rejected.  The first call on a device
+ * looks up that array's address with the device current: make it before any
+ * stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race; order them on one stream.  Enqueued on `stream` (cudaStream_t). */
+int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev, void *stream);
+
 /* ------------------------------------------------ one-call solve from host buffers */
 /* Uploads b (finest level, list order), runs ls `solver` ($i $d $r $s $p, with the x/b
  * given to npinit), downloads x. */
