@@ -43,6 +43,7 @@ def test_generator_matches_ug(name, kind, nref, seed, corr, var):
         n = int(fx[f"L{l}_n"][0])
         assert g["n"] == n
         assert g["rowptr"][-1] == fx[f"L{l}_rowptr"][-1]
+        assert np.array_equal(np.unique(g["vnclass"]), np.unique(fx[f"L{l}_vnclass"]))
         if kind == 1 and l > 0:
             maps.append(None)
             continue

@@ -249,7 +249,8 @@ static int build_level(gmg_gen *G, int l, const ugfx::LogNormalField &field) {
   }
   // Dirichlet rows, classes
   L.vclass.assign(n, 3);
-  L.vnclass.assign(n, 3);
+  // VNCLASS: 3 under a refined level, 0 on the finest level (no sons), as UG sets it
+  L.vnclass.assign(n, l < G->nref ? 3 : 0);
   L.skip.assign(n, 0);
   for (int k = 0; k < (dim == 3 ? g.N : 1); ++k)
     for (int j = 0; j < g.N; ++j)
