@@ -166,13 +166,143 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-            "config": workload_config({"iterations": iters}),
+            "config": workload_config({"iterations": iters, "smoother": "gs (UG VECTOR-list order, as l_lgs)"}),
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"{threads} concurrent FP64 solves (one per thread), each step one ls "
                                        f"iteration of each, scaled by the {iters} iterations of a complete "
                                        f"solve (single-thread complete solve: {t_full:.1f} s)"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- batched workload
+BATCH_N, BATCH_SEED, BATCH_VAR = 512, 4242, 0.5
+
+
+def batch_instances(G, count):
+    """The batched workload: `count` independent 2D Q1 Poisson instances on the
+    unit square, instance k refined L_k ~ U{3..7} times ((2^L+1)^2 = 81 ..
+    16,641 unknowns), k = exp(g) with its own seeded field (corr 0.1,
+    variance 0.5) and its own seeded uniform[-1,1] right-hand side."""
+    rng = np.random.default_rng(BATCH_SEED)
+    nrefs = rng.integers(3, 8, size=count)
+    return [G.Generator(G.Generator.POISSON2D, int(L), seed=BATCH_SEED + k, corr=CORR, var=BATCH_VAR)
+            for k, L in enumerate(nrefs)], [int(L) for L in nrefs]
+
+
+def run_batched(args, stream, flush_l2, world, rank):
+    """All instances in one batched hierarchy: FP32 Jacobi V(2,2) inside FP64
+    iterative refinement to 1e-8 relative defect per instance (and the same
+    batch in plain FP64), against the plain FP64 GPU path that solves one
+    instance at a time (timed on a sample of instances)."""
+    import torch
+    import ug_gb300 as G
+    gens, nrefs = batch_instances(G, args.batch)
+    mg = G.MultiGrid(gens, batched=True, order=G.ORDER_COLOR, fp32=True, device=torch.cuda.current_device())
+    G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
+    G.setup_lmgc(mg, "jac", baselevel=0, red=RED, abslimit=1e-50, name="bat64")
+    mg.npcreate("bat32", "linear_solver.gls")
+    mg.npinit("bat32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    b = mg.pack([g.rhs for g in gens])
+    x = np.empty_like(b)
+    unknowns = int(b.size)
+    nnz = sum(mg.size(l)[2] for l in range(mg.nlevels))
+    out = {"workload": f"{args.batch} x 2D Q1 Poisson, levels U{{3..7}} (81..16641 unknowns), k=exp(g) var 0.5, "
+                       f"Jacobi V(2,2) omega 0.8, to 1e-8 rel defect per instance",
+           "instances": args.batch, "unknowns": unknowns, "nnz_all_levels": int(nnz),
+           "levels_histogram": {str(L): nrefs.count(L) for L in range(3, 8)}}
+
+    def timed(solver):
+        for _ in range(args.warmup):
+            mg.solve_host(solver, b, x)
+        ms, iters, launches = [], 0, 0
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            for _ in range(args.steps):
+                flush_l2(); torch.cuda.synchronize()
+                mg.launch_count(reset=True)
+                t0 = time.perf_counter()
+                _, lr = mg.solve_host(solver, b, x)
+                ms.append((time.perf_counter() - t0) * 1e3)
+                launches += mg.launch_count()
+                assert lr.converged, f"batched {solver} did not converge"
+                iters = lr.iters
+        return float(np.mean(ms)), iters, launches / args.steps, clk.summary()
+
+    ms32, it32, l32, clk32 = timed("bat32")
+    ms64, it64, l64, _ = timed("bat64")
+    # device-only: one solve from resident data (b already on the device)
+    top = mg.top
+    mg.createvector("b0")
+    mg.upload_packed("b0", b)
+    dev_ms = []
+    for k in range(args.warmup + args.steps):
+        lr = G.LResult()
+        flush_l2()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for l in range(mg.nlevels):
+            mg.dcopy(l, "rhs", "b0")
+            mg.dset(l, "sol", 0.0)
+        mg.ls_defect("bat32", top, "sol", "rhs")
+        mg.ls_residuum("bat32", 0, top, "sol", "rhs", lr)
+        mg.ls_solver("bat32", top, "sol", "rhs", lr)
+        e.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            dev_ms.append(a.elapsed_time(e))
+    mg.close()
+    # plain FP64 GPU path: one instance at a time, on a sample
+    rng = np.random.default_rng(1)
+    sample = sorted(rng.choice(args.batch, size=min(32, args.batch), replace=False).tolist())
+    solos = []
+    for k in sample:
+        m1 = G.MultiGrid(gens[k], order=G.ORDER_COLOR, fp32=False, device=torch.cuda.current_device())
+        G.lib().gmg_mg_set_stream(m1._h, stream.cuda_stream)
+        G.setup_lmgc(m1, "jac", baselevel=0, red=RED, abslimit=1e-50)
+        m1.solve_host("mgs", gens[k].rhs)
+        solos.append(m1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k, m1 in zip(sample, solos):
+        m1.solve_host("mgs", gens[k].rhs)
+    solo_s = time.perf_counter() - t0
+    for m1 in solos:
+        m1.close()
+    # the sample's share of the batch's work (unknowns) scales it to the whole batch
+    frac = sum(len(gens[k].rhs) for k in sample) / unknowns
+    solo_per_s = len(sample) / solo_s
+    solo_batch_s = solo_s / frac  # time to solve all instances one at a time
+    out.update({
+        "mixed": {"value": world * args.batch / (ms32 * 1e-3), "unit": "solves/s (e2e, host b -> host x)",
+                  "ms_per_batch": ms32, "iterations_max": it32, "launches_per_batch": l32, "clocks": clk32,
+                  "device_ms_per_batch": float(np.mean(dev_ms)),
+                  "device_value": world * args.batch / (float(np.mean(dev_ms)) * 1e-3)},
+        "fp64_batched": {"value": world * args.batch / (ms64 * 1e-3), "ms_per_batch": ms64, "iterations_max": it64,
+                         "launches_per_batch": l64},
+        "fp64_one_at_a_time": {"value": world * args.batch / solo_batch_s, "unit": "solves/s",
+                               "sample": f"{len(sample)} instances solved one after another "
+                                         f"({solo_per_s:.0f} instance solves/s), scaled to the batch by unknowns"},
+        "mixed_batched_over_fp64_one_at_a_time": solo_batch_s / (ms32 * 1e-3),
+        "h2d_bytes_per_batch": int(unknowns * 8), "d2h_bytes_per_batch": int(unknowns * 8),
+    })
+    if rank == 0:
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build()
+            cs = sample[:8]
+            t0 = time.perf_counter()
+            for k in cs:
+                oracle.Hierarchy(gens[k].levels()).ls_solve(gens[k].rhs, smoother="jac", baselevel=0, damp=0.8,
+                                                            red=RED)
+            dt = time.perf_counter() - t0
+            cfrac = sum(len(gens[k].rhs) for k in cs) / unknowns
+            out["cpu_baseline"] = {"value": args.batch / (dt / cfrac), "unit": "solves/s", "cores": 1,
+                                   "kind": "port", "sample": f"{len(cs)} instances, FP64, one core ({dt:.1f} s), "
+                                                             f"scaled to the batch by unknowns"}
+        except Exception as e:  # reported, not fatal
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    return out
 
 
 # ---------------------------------------------------------------- our arm
@@ -301,6 +431,10 @@ def run_ours(args):
         except Exception as e:  # reported, not fatal
             cpu = {"value": None, "unit": "solves/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
 
+    waves = [mg.num_waves(l) for l in range(mg.nlevels)]
+    mg.close()
+    batched = run_batched(args, stream, flush_l2, world, rank) if not args.no_batched else None
+
     if rank == 0:
         r32, r64 = results["mgs32"], results["mgs64"]
         value = world * 1e3 / r32["ms_per_step"]
@@ -311,7 +445,7 @@ def run_ours(args):
             "data": "synthetic (seeded)",
             "config": workload_config({"iterations_mixed": r32["iters"], "iterations_fp64": r64["iters"],
                                        "parallelism": "replicas" if world > 1 else "1 GPU",
-                                       "gs_waves_per_level": [mg.num_waves(l) for l in range(mg.nlevels)],
+                                       "gs_waves_per_level": waves,
                                        "launches_per_solve": r32["launches_per_step"]}),
             "fp64": {"value": world * 1e3 / r64["ms_per_step"], "unit": "solves/s", "ms_per_step": r64["ms_per_step"],
                      "iterations": r64["iters"]},
@@ -327,9 +461,9 @@ def run_ours(args):
             "gpu_launches": int(r32["launches_per_step"] * args.steps),
             "clocks": r32["clocks"],
             "cpu_baseline": cpu,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
-    mg.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -340,6 +474,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances workload")
+    ap.add_argument("--batch", type=int, default=BATCH_N, help="instances of the batched workload")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -100,6 +100,33 @@ const char *gmg_last_error(void);
 /* Synchronise mg's stream; returns nonzero if a kernel failed. */
 int gmg_mg_sync(gmg_mg *mg);
 
+/* ------------------------------------------------ batched hierarchies */
+/* `ninst` independent problems, instance k given as inst_nlevels[k] levels
+ * (instances[k][0..]), all with one block size, stored block-diagonally:
+ * level l of the result is the concatenation, in instance order, of level l
+ * of every instance that has one, so each instance advances through the
+ * same per-level kernels at once (no UG counterpart: UG solves one
+ * MULTIGRID at a time; each instance is what UG's ls would compute for it).
+ * Instance k's finest level inst_nlevels[k]-1 is its surface: every row there
+ * has VNCLASS < 2 (UG's top level) and every row below has VNCLASS >= 2
+ * (NULL vnclass arrays mean exactly that).  An ls on such a hierarchy, run
+ * at its deepest level, tests convergence per instance and leaves converged
+ * instances' x alone; vectors are passed packed (below). */
+int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *inst_nlevels, int ninst,
+                          const gmg_mg_opts *opts, gmg_mg **out);
+/* number of instances (0 for a hierarchy from gmg_mg_create) */
+int gmg_mg_num_instances(const gmg_mg *mg);
+/* instance k's finest level, its VECTORs there and its first VECTOR in the packed layout */
+int gmg_mg_instance_info(const gmg_mg *mg, int k, int *top, int *n_top, long long *pack_offset);
+/* packed vectors: every instance's finest-level values (its list order, s per
+ * VECTOR), instance after instance: sum_k n_top[k]*s doubles; synchronous */
+int gmg_vec_upload_packed(gmg_vec *v, const double *host);
+int gmg_vec_download_packed(gmg_vec *v, double *host);
+/* per-instance LRESULT of the last ls Solver on a batched hierarchy (its
+ * aggregate LRESULT holds the largest defects / iteration count over the
+ * instances and converged = all converged) */
+int gmg_ls_instance_result(gmg_np *ls, int k, gmg_lresult *lr);
+
 /* ------------------------------------------------ user data (udm.h) */
 /* createvector: one array per level, GMG_PREC_FP64 or GMG_PREC_FP32 */
 int gmg_vec_create(gmg_mg *mg, const char *name, int precision, gmg_vec **out);
@@ -173,8 +200,8 @@ int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_
 int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev, void *stream);
 
 /* ------------------------------------------------ one-call solve from host buffers */
-/* Uploads b (finest level, list order), runs ls `solver` ($i $d $r $s $p, with the x/b
- * given to npinit), downloads x. */
+/* Uploads b (finest level, list order; packed on a batched hierarchy), runs ls
+ * `solver` ($i $d $r $s $p, with the x/b given to npinit), downloads x. */
 int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double *x_host, gmg_lresult *lr);
 
 /* ------------------------------------------------ structured hierarchies */

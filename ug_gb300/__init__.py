@@ -102,6 +102,9 @@ def lib(build_if_missing: bool = True):
         "gmg_l_ilu_decomp": ([P, I, P, P], I), "gmg_l_luiter": ([P, I, P, P, P], I),
         "gmg_standard_restrict": ([P, I, P, P, P], I), "gmg_standard_interpolate_correction": ([P, I, P, P, P], I),
         "gmg_solve_host": ([P, C.c_char_p, P, P, P], I),
+        "gmg_mg_create_batched": ([P, P, I, P, P], I), "gmg_mg_num_instances": ([P], I),
+        "gmg_mg_instance_info": ([P, I, P, P, P], I), "gmg_vec_upload_packed": ([P, P], I),
+        "gmg_vec_download_packed": ([P, P], I), "gmg_ls_instance_result": ([P, I, P], I),
         "gmg_gen_create": ([I, I, C.c_ulonglong, D, D, P], I), "gmg_gen_levels": ([P, P, P], I),
         "gmg_gen_rhs": ([P, P, P], I), "gmg_gen_coords": ([P, I, P], I), "gmg_gen_destroy": ([P], I),
     }
@@ -202,37 +205,99 @@ def levels_from_ugfx(fx: dict) -> list[dict]:
     return out
 
 
+def _desc_array(levels, keep: list):
+    """gmg_level_desc array of a Generator or a list of level dicts; the numpy
+    arrays it points into are appended to ``keep``."""
+    if isinstance(levels, Generator):
+        keep.append(levels)
+        return levels._desc, levels.nlevels
+    nl = len(levels)
+    desc_arr = (LevelDesc * nl)()
+    for i, d in enumerate(levels):
+        ints = {k: (None if d.get(k) is None else np.ascontiguousarray(d[k], np.int32))
+                for k in ("rowptr", "col", "vclass", "vnclass", "skip", "prowptr", "pcol")}
+        dbl = {k: (None if d.get(k) is None else np.ascontiguousarray(d[k], np.float64)) for k in ("val", "pw")}
+        keep += list(ints.values()) + list(dbl.values())
+        desc_arr[i] = LevelDesc(int(d["n"]), int(d["s"]), _ptr(ints["rowptr"]), _ptr(ints["col"]),
+                                _ptr(dbl["val"]), _ptr(ints["vclass"]), _ptr(ints["vnclass"]),
+                                _ptr(ints["skip"]), _ptr(ints["prowptr"]), _ptr(ints["pcol"]),
+                                _ptr(dbl["pw"]))
+    keep.append(desc_arr)
+    return desc_arr, nl
+
+
 class MultiGrid:
-    """Device-resident multigrid hierarchy with UG-style user data and numprocs."""
+    """Device-resident multigrid hierarchy with UG-style user data and numprocs.
+
+    ``levels`` is a Generator or a list of level dicts; a list of several
+    such hierarchies (``batched=True``) builds one batched hierarchy of
+    independent instances (gmg_mg_create_batched), whose vectors move as
+    packed arrays (``upload_packed`` / ``download_packed`` / ``split``)."""
 
     def __init__(self, levels, order: int = ORDER_LIST, fp32: bool = False, autotune: bool = False, device: int = 0,
-                 pdl: bool = True):
+                 pdl: bool = True, batched: bool = False):
         L = lib()
-        if isinstance(levels, Generator):
-            desc_arr = levels._desc
-            nl = levels.nlevels
-            self._keep = [levels]
-        else:
-            nl = len(levels)
-            desc_arr = (LevelDesc * nl)()
-            self._keep = []
-            for i, d in enumerate(levels):
-                ints = {k: (None if d.get(k) is None else np.ascontiguousarray(d[k], np.int32))
-                        for k in ("rowptr", "col", "vclass", "vnclass", "skip", "prowptr", "pcol")}
-                dbl = {k: (None if d.get(k) is None else np.ascontiguousarray(d[k], np.float64)) for k in ("val", "pw")}
-                self._keep += list(ints.values()) + list(dbl.values())
-                desc_arr[i] = LevelDesc(int(d["n"]), int(d["s"]), _ptr(ints["rowptr"]), _ptr(ints["col"]),
-                                        _ptr(dbl["val"]), _ptr(ints["vclass"]), _ptr(ints["vnclass"]),
-                                        _ptr(ints["skip"]), _ptr(ints["prowptr"]), _ptr(ints["pcol"]),
-                                        _ptr(dbl["pw"]))
         opts = MgOpts(order, int(fp32), int(autotune), device, int(not pdl))
         h = C.c_void_p()
-        if L.gmg_mg_create(C.cast(desc_arr, C.c_void_p), nl, C.byref(opts), C.byref(h)):
-            _err("gmg_mg_create")
+        keep: list = []
+        if batched:
+            descs = [_desc_array(inst, keep) for inst in levels]
+            ninst = len(descs)
+            ptrs = (C.c_void_p * ninst)(*[C.cast(d, C.c_void_p).value for d, _ in descs])
+            nls = np.array([n for _, n in descs], np.int32)
+            if L.gmg_mg_create_batched(C.cast(ptrs, C.c_void_p), _ptr(nls), ninst, C.byref(opts), C.byref(h)):
+                _err("gmg_mg_create_batched")
+            nl = int(nls.max())
+        else:
+            desc_arr, nl = _desc_array(levels, keep)
+            if L.gmg_mg_create(C.cast(desc_arr, C.c_void_p), nl, C.byref(opts), C.byref(h)):
+                _err("gmg_mg_create")
         self._h = h
         self.nlevels = nl
         self.top = nl - 1
-        self._keep = None  # the device holds its own copies
+        self.ninst = L.gmg_mg_num_instances(h)
+        if self.ninst:
+            top, nt, po = C.c_int(), C.c_int(), C.c_longlong()
+            self.inst_top, self.inst_n, self.pack_off = [], [], []
+            for k in range(self.ninst):
+                L.gmg_mg_instance_info(h, k, C.byref(top), C.byref(nt), C.byref(po))
+                self.inst_top.append(top.value)
+                self.inst_n.append(nt.value)
+                self.pack_off.append(po.value)
+            self.block = self.size(0)[1]
+            self.packed_len = (self.pack_off[-1] + self.inst_n[-1]) * self.block
+        del keep  # the device holds its own copies
+
+    # ---- batched hierarchies
+    def split(self, packed) -> list:
+        """Per-instance views of a packed vector."""
+        s = self.block
+        return [packed[o * s:(o + n) * s] for o, n in zip(self.pack_off, self.inst_n)]
+
+    def pack(self, parts) -> np.ndarray:
+        out = np.concatenate([np.ascontiguousarray(p, np.float64).ravel() for p in parts])
+        if out.size != self.packed_len:
+            raise GmgError(f"pack: {out.size} values for {self.packed_len}")
+        return out
+
+    def upload_packed(self, name: str, data):
+        a = np.ascontiguousarray(data, np.float64).ravel()
+        if a.size != self.packed_len:
+            raise GmgError(f"upload_packed {name}: {a.size} values for {self.packed_len}")
+        if lib().gmg_vec_upload_packed(self.vec(name), _ptr(a)):
+            _err(f"upload_packed {name}")
+
+    def download_packed(self, name: str) -> np.ndarray:
+        a = np.empty(self.packed_len)
+        if lib().gmg_vec_download_packed(self.vec(name), _ptr(a)):
+            _err(f"download_packed {name}")
+        return a
+
+    def instance_result(self, ls: str, k: int) -> LResult:
+        lr = LResult()
+        if lib().gmg_ls_instance_result(self.np(ls), k, C.byref(lr)):
+            _err("gmg_ls_instance_result")
+        return lr
 
     # ---- hierarchy
     def size(self, level: int):
@@ -442,10 +507,14 @@ class MultiGrid:
             _err("StandardInterpolateCorrection")
 
     def solve_host(self, solver: str, b, x=None):
-        """gmg_solve_host: b (finest level, list order) -> (x, LResult)."""
+        """gmg_solve_host: b (finest level, list order; packed on a batched
+        hierarchy) -> (x, LResult)."""
         n, s, _ = self.size(self.top)
+        length = self.packed_len if self.ninst else n * s
         bb = np.ascontiguousarray(b, np.float64).ravel()
-        xx = np.empty(n * s) if x is None else x
+        if bb.size != length:
+            raise GmgError(f"solve {solver}: {bb.size} values for {length}")
+        xx = np.empty(length) if x is None else x
         lr = LResult()
         if lib().gmg_solve_host(self._h, solver.encode(), _ptr(bb), _ptr(xx), C.byref(lr)):
             _err(f"solve {solver}")

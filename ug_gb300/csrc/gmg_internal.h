@@ -100,6 +100,13 @@ struct Level {
   // base solve: explicit inverse of the level matrix (filled by ex PreProcess)
   double *ainv = nullptr;
   int base_dim = 0;
+  // block-diagonal levels (batched hierarchies): rows of independent block k
+  // are blk_rows[blk_ptr[k]..blk_ptr[k+1]) in processing order; the base
+  // solve then keeps one dense inverse per block (at ainv + blk_aoff[k])
+  std::vector<int> blk_ptr, blk_rows;
+  int nblk_dev = 0;
+  int *blk_ptr_dev = nullptr, *blk_rows_dev = nullptr;
+  long long *blk_aoff_dev = nullptr;
   // SpMV variant: threads cooperating on one row
   int tpr = 8;
   // sliced ELLPACK copy of A (slices of 32 consecutive rows stored column by
@@ -157,6 +164,28 @@ struct gmg_mg {
   double *stage_host = nullptr;// pinned, n_top*s doubles
   long long launches = 0;
   std::vector<std::unique_ptr<gmg::CoarseImageBase>> coarse_images;
+  // batched hierarchies (gmg_mg_create_batched): independent instances stored
+  // block-diagonally in every level; instance k's finest level is top[k]
+  struct Batch {
+    int ninst = 0;
+    std::vector<int> top;                    // per instance
+    std::vector<std::vector<int>> list_off;  // [level][instance] first row in list order (-1 if absent)
+    std::vector<int> nrows_top;              // rows of instance k on its top level
+    std::vector<long long> pack_off;         // first row of instance k in the packed layout
+    // per level that is some instance's top: instances with that top (local order)
+    struct TopLevel {
+      int level = 0, ninst = 0, nrows = 0;
+      std::vector<int> ids;                  // global instance ids
+      // instance-major row lists: rows_dev[ptr_dev[k]..ptr_dev[k+1]) are the
+      // processing-order rows of instance ids[k] in its own list order, and
+      // pack_dev[q] is row q's position in the packed host layout
+      int *ids_dev = nullptr, *ptr_dev = nullptr, *rows_dev = nullptr, *pack_dev = nullptr;
+    };
+    std::vector<TopLevel> tops;
+    uint8_t *conv_dev = nullptr;             // converged flag per instance
+    uint8_t *conv_host = nullptr;            // pinned mirror
+    double *norms_dev = nullptr, *norms_host = nullptr;  // ninst * GMG_MAX_S
+  } batch;
   ~gmg_mg();
 };
 
@@ -197,6 +226,11 @@ int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void 
 int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x);
 // base level: if |b| >= abslimit in some component: t = Ainv b; b -= A t; c += t
 int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit);
+// batched ls, on one top level: for each of its instances (one block each),
+// x += c on its rows unless converged[id], then the per-component norms of b
+// on its rows into norms[id*GMG_MAX_S + r]
+int k_batch_update_norm(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, const void *b, double *x,
+                        int cprec, const void *c, int s);
 // the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
 struct CoarseCfg {
   int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;
@@ -206,6 +240,9 @@ int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_v
 // shared memory the fused cycle needs for levels bl..lc
 long long coarse_smem_bytes(const gmg_mg *mg, int bl, int lc, int prec, int smoother);
 constexpr long long COARSE_SMEM_BUDGET = 220 * 1024;
+// packed instance vectors of a batched hierarchy <-> one top level's rows
+int k_pack_gather(gmg_mg *mg, int prec, void *dst, const double *packed, const gmg_mg::Batch::TopLevel &tl, int s);
+int k_pack_scatter(gmg_mg *mg, int prec, double *packed, const void *src, const gmg_mg::Batch::TopLevel &tl, int s);
 // permutations between UG list order and processing order
 int k_gather(gmg_mg *mg, int prec, void *dst, const double *src_list, const int *perm, int n, int s);
 int k_scatter(gmg_mg *mg, int prec, double *dst_list, const void *src, const int *perm, int n, int s);

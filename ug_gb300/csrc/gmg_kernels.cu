@@ -584,6 +584,48 @@ __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, doub
   }
 }
 
+// ------------------------------------------------------------ batched ls
+// One block per instance of a top level: LSUpdate (x += c, skipped once the
+// instance has converged, so its x stays the one of its own converged
+// iteration) and dnrm2x of its defect, summed in a fixed order.
+template <class TB, class TC, int S>
+__global__ void __launch_bounds__(BLK) batch_update_norm_kernel(const int *__restrict__ ids, const int *__restrict__ ptr,
+                                                                const int *__restrict__ rows,
+                                                                const uint8_t *__restrict__ flags,
+                                                                const uint8_t *__restrict__ conv,
+                                                                const TB *__restrict__ b, double *__restrict__ x,
+                                                                const TC *__restrict__ c, double *__restrict__ norms) {
+  pdl_prologue();
+  const int k = blockIdx.x, id = ids[k], r0 = ptr[k], r1 = ptr[k + 1];
+  const bool upd = c != nullptr && !conv[id];
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int q = r0 + threadIdx.x; q < r1; q += blockDim.x) {
+    const int i = rows[q];
+    const bool nd = flags[i] & F_NEWDEF;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      if (upd) x[(size_t)i * S + r] += double(c[(size_t)i * S + r]);
+      const double v = nd ? double(b[(size_t)i * S + r]) : 0.0;
+      acc[r] = fma(v, v, acc[r]);
+    }
+  }
+  __shared__ double sh[BLK / 32][S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    norms[(size_t)id * GMG_MAX_S + threadIdx.x] = sqrt(v);
+  }
+}
+
 // ------------------------------------------------------------ base solver
 // The lmgc base solver `ls $m 1 $I ex` (np/procs/ls.cc:637, iter.cc:8972):
 // nothing happens when every component of |b| is below the base abslimit;
@@ -647,7 +689,94 @@ __global__ void __launch_bounds__(1024) base_kernel(int n, const double *__restr
   }
 }
 
+// The same on a block-diagonal level (a batched hierarchy's base level): one
+// CTA per independent block, each with its own abslimit test and its own
+// dense inverse, so every instance is solved exactly as if it were alone.
+template <class T, int S>
+__global__ void __launch_bounds__(256) base_block_kernel(const int *__restrict__ bptr, const int *__restrict__ brows,
+                                                         const long long *__restrict__ aoff,
+                                                         const double *__restrict__ ainv,
+                                                         const int *__restrict__ rowptr, const int *__restrict__ col,
+                                                         const T *__restrict__ val, T *__restrict__ c,
+                                                         T *__restrict__ b, T *__restrict__ t, Damp<double> abslimit) {
+  pdl_prologue();
+  __shared__ double red[S][8];
+  __shared__ int skip;
+  const int r0 = bptr[blockIdx.x], m = bptr[blockIdx.x + 1] - r0, N = m * S;
+  const int *rows = brows + r0;
+  const double *A = ainv + aoff[blockIdx.x];
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int q = threadIdx.x; q < m; q += blockDim.x)
+#pragma unroll
+    for (int r = 0; r < S; ++r) { double v = double(b[(size_t)rows[q] * S + r]); acc[r] += v * v; }
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[r][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int below = 1;
+    for (int r = 0; r < S; ++r) {
+      double v = 0.0;
+      for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) v += red[r][w];
+      if (fabs(sqrt(v)) >= fabs(abslimit.d[r])) below = 0;
+    }
+    skip = below;
+  }
+  __syncthreads();
+  if (skip) return;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) {
+    double v = 0.0;
+    for (int j = 0; j < N; ++j) v = fma(A[(size_t)e * N + j], double(b[(size_t)rows[j / S] * S + j % S]), v);
+    t[(size_t)rows[e / S] * S + e % S] = T(v);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < m; q += blockDim.x) {
+    const int i = rows[q];
+    T s[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) s[r] = T(0);
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = col[k];
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int cc = 0; cc < S; ++cc) s[r] = fma(val[(size_t)k * S * S + r * S + cc], t[(size_t)j * S + cc], s[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      b[(size_t)i * S + r] -= s[r];
+      c[(size_t)i * S + r] += t[(size_t)i * S + r];
+    }
+  }
+}
+
 // ------------------------------------------------------------ permutations
+// packed instance vectors (instance-major, each in its own list order) <->
+// the rows of one top level of a batched hierarchy
+template <class T>
+__global__ void pack_gather_kernel(T *dst, const double *__restrict__ src, const int *__restrict__ rows,
+                                   const int *__restrict__ pack, int m, int s) {
+  pdl_prologue();
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const int i = rows[q], p = pack[q];
+  for (int r = 0; r < s; ++r) dst[(size_t)i * s + r] = T(src[(size_t)p * s + r]);
+}
+template <class T>
+__global__ void pack_scatter_kernel(double *dst, const T *__restrict__ src, const int *__restrict__ rows,
+                                    const int *__restrict__ pack, int m, int s) {
+  pdl_prologue();
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const int i = rows[q], p = pack[q];
+  for (int r = 0; r < s; ++r) dst[(size_t)p * s + r] = double(src[(size_t)i * s + r]);
+}
+
 template <class T>
 __global__ void gather_kernel(T *dst, const double *__restrict__ src, const int *__restrict__ perm, int n, int s) {
   pdl_prologue();
@@ -848,6 +977,29 @@ int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long 
   return 0;
 }
 
+int k_batch_update_norm(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, const void *b, double *x,
+                        int cprec, const void *c, int s) {
+  if (tl.ninst == 0) return 0;
+  const auto &B = mg->batch;
+#define BU(TB, TC, SS)                                                                                          \
+  GMG_LAUNCH((batch_update_norm_kernel<TB, TC, SS>), tl.ninst, BLK, tl.ids_dev, tl.ptr_dev, tl.rows_dev,        \
+             mg->lev[tl.level].flags, B.conv_dev, (const TB *)b, x, (const TC *)c, B.norms_dev)
+#define BS(TB, TC)                                       \
+  if (s == 1) BU(TB, TC, 1);                             \
+  else if (s == 2) BU(TB, TC, 2);                        \
+  else if (s == 3) BU(TB, TC, 3);                        \
+  else { set_error("block size %d not compiled", s); return 1; }
+  if (bprec == GMG_PREC_FP64) {
+    if (cprec == GMG_PREC_FP64) { BS(double, double) } else { BS(double, float) }
+  } else {
+    if (cprec == GMG_PREC_FP64) { BS(float, double) } else { BS(float, float) }
+  }
+#undef BS
+#undef BU
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_refine_prepare(gmg_mg *mg, float *b32, float *c32, const double *b64, long long len) {
   if (len <= 0) return 0;
   GMG_LAUNCH(refine_prepare_kernel, vec_grid(len), BLK, b32, c32, b64, len);
@@ -1039,8 +1191,14 @@ int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t
   GMG_CHECK(L.ainv, "base level inverse not computed (ex PreProcess)");
   Damp<double> al = make_damp<double>(abslimit, L.s);
 #define BK(TT, SS)                                                                                             \
-  GMG_LAUNCH((base_kernel<TT, SS>), 1, 1024, L.n, L.ainv, L.A.rowptr, L.A.col, mval<TT>(L.A), (TT *)c,    \
-                                                  (TT *)b, (TT *)t, al)
+  do {                                                                                                         \
+    if (L.nblk_dev > 0)                                                                                        \
+      GMG_LAUNCH((base_block_kernel<TT, SS>), L.nblk_dev, 256, L.blk_ptr_dev, L.blk_rows_dev, L.blk_aoff_dev,  \
+                 L.ainv, L.A.rowptr, L.A.col, mval<TT>(L.A), (TT *)c, (TT *)b, (TT *)t, al);                   \
+    else                                                                                                       \
+      GMG_LAUNCH((base_kernel<TT, SS>), 1, 1024, L.n, L.ainv, L.A.rowptr, L.A.col, mval<TT>(L.A), (TT *)c,     \
+                 (TT *)b, (TT *)t, al);                                                                        \
+  } while (0)
 #define BS(TT)                                   \
   if (L.s == 1) BK(TT, 1);                       \
   else if (L.s == 2) BK(TT, 2);                  \
@@ -1050,6 +1208,30 @@ int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t
   else { GMG_CHECK(L.A.v32, "FP32 copy not built"); BS(float) }
 #undef BS
 #undef BK
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_pack_gather(gmg_mg *mg, int prec, void *dst, const double *packed, const gmg_mg::Batch::TopLevel &tl, int s) {
+  if (tl.nrows == 0) return 0;
+  if (prec == GMG_PREC_FP64)
+    GMG_LAUNCH((pack_gather_kernel<double>), grid_for(tl.nrows), BLK, (double *)dst, packed, tl.rows_dev,
+               tl.pack_dev, tl.nrows, s);
+  else
+    GMG_LAUNCH((pack_gather_kernel<float>), grid_for(tl.nrows), BLK, (float *)dst, packed, tl.rows_dev,
+               tl.pack_dev, tl.nrows, s);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_pack_scatter(gmg_mg *mg, int prec, double *packed, const void *src, const gmg_mg::Batch::TopLevel &tl, int s) {
+  if (tl.nrows == 0) return 0;
+  if (prec == GMG_PREC_FP64)
+    GMG_LAUNCH((pack_scatter_kernel<double>), grid_for(tl.nrows), BLK, packed, (const double *)src, tl.rows_dev,
+               tl.pack_dev, tl.nrows, s);
+  else
+    GMG_LAUNCH((pack_scatter_kernel<float>), grid_for(tl.nrows), BLK, packed, (const float *)src, tl.rows_dev,
+               tl.pack_dev, tl.nrows, s);
   LAUNCH_CHECK(mg);
   return 0;
 }

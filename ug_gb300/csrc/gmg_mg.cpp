@@ -227,7 +227,10 @@ static void build_sell(HostLevel &H) {
   }
 }
 
-static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H) {
+// `colour_in`, if given, is the colouring to use in GMG_ORDER_COLOR (a batched
+// hierarchy passes the concatenation of its instances' own colourings)
+static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
+                            const std::vector<int> *colour_in = nullptr) {
   const int n = d.n, s = d.s, ss = s * s;
   H.n = n; H.s = s;
   GMG_CHECK(n >= 0 && s >= 1 && s <= GMG_MAX_S, "bad level size n=%d s=%d", n, s);
@@ -240,7 +243,14 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H) {
   H.perm.resize(n);
   std::iota(H.perm.begin(), H.perm.end(), 0);
   if (order == GMG_ORDER_COLOR && n > 0) {
-    std::vector<int> colour = greedy_colour(n, adj, &H.ncolour);
+    std::vector<int> colour;
+    if (colour_in) {
+      GMG_CHECK((int)colour_in->size() == n, "colouring of %zu rows for a level of %d", colour_in->size(), n);
+      colour = *colour_in;
+      H.ncolour = 1 + *std::max_element(colour.begin(), colour.end());
+    } else {
+      colour = greedy_colour(n, adj, &H.ncolour);
+    }
     std::stable_sort(H.perm.begin(), H.perm.end(), [&](int a, int b) { return colour[a] < colour[b]; });
     // the wavefronts are the colour classes: contiguous ranges of the processing order
     H.lptr.assign(H.ncolour + 1, 0);
@@ -409,17 +419,21 @@ gmg_mg::~gmg_mg() {
   arena.release();
   if (norms_host) cudaFreeHost(norms_host);
   if (stage_host) cudaFreeHost(stage_host);
+  if (batch.conv_host) cudaFreeHost(batch.conv_host);
+  if (batch.norms_host) cudaFreeHost(batch.norms_host);
 }
 
 extern "C" {
 
 const char *gmg_last_error(void) { return gmg::last_error(); }
 
-int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *opts_in, gmg_mg **out) {
-  if (!out || !levels || nlevels < 1) { set_error("gmg_mg_create: bad arguments"); return 1; }
-  *out = nullptr;
-  gmg_mg_opts opts{};
-  if (opts_in) opts = *opts_in;
+}  // extern "C"
+
+// the device hierarchy of `levels`; `colours` optionally fixes each level's
+// colouring, `stage_min` is the least staging length (doubles) to allocate
+static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts &opts,
+                            const std::vector<std::vector<int>> *colours, size_t stage_min,
+                            std::unique_ptr<gmg_mg> &out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return 1; }
   GMG_CUDA(cudaSetDevice(opts.device));
@@ -427,7 +441,7 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
   std::vector<HostLevel> H(nlevels);
   for (int l = 0; l < nlevels; ++l) {
     GMG_CHECK(levels[l].s == s, "all levels must have the same block size");
-    if (build_host_level(levels[l], opts.order, H[l])) return 1;
+    if (build_host_level(levels[l], opts.order, H[l], colours ? &(*colours)[l] : nullptr)) return 1;
     if (l > 0 && build_host_transfer(levels[l], H[l - 1], H[l])) return 1;
   }
   // plan the arena
@@ -548,7 +562,7 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
   mg->norms_dev = mg->partial + REDUCE_BLOCKS * GMG_MAX_S;
   GMG_CUDA(cudaMallocHost(&mg->norms_host, sizeof(double) * GMG_MAX_S));
   mg->lev.back().own.push_back(mg->partial);
-  size_t top_len = size_t(mg->lev.back().n) * s;
+  size_t top_len = std::max(size_t(mg->lev.back().n) * s, stage_min);
   GMG_CUDA(cudaMallocHost(&mg->stage_host, sizeof(double) * (top_len ? top_len : 1)));
   GMG_CUDA(cudaMalloc(&mg->stage_dev, sizeof(double) * (top_len ? top_len : 1)));
   mg->lev.back().own.push_back(mg->stage_dev);
@@ -559,7 +573,184 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
     for (auto &L : mg->lev)
       if (autotune_level(mg.get(), L)) return 1;
   GMG_CUDA(cudaDeviceSynchronize());
+  out = std::move(mg);
+  return 0;
+}
+
+template <class T>
+static int upload_owned(Level &L, T **dst, const std::vector<T> &src) {
+  GMG_CUDA(cudaMalloc(dst, sizeof(T) * (src.empty() ? 1 : src.size())));
+  L.own.push_back(*dst);
+  if (!src.empty()) GMG_CUDA(cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// rows of the union level that belong to instance k, in the instance's own
+// list order (as processing-order indices)
+static std::vector<int> instance_rows(const Level &L, int off, int n) {
+  std::vector<int> iperm(L.n), r(n);
+  for (int i = 0; i < L.n; ++i) iperm[L.perm[i]] = i;
+  for (int j = 0; j < n; ++j) r[j] = iperm[off + j];
+  return r;
+}
+
+extern "C" {
+
+int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *opts_in, gmg_mg **out) {
+  if (!out || !levels || nlevels < 1) { set_error("gmg_mg_create: bad arguments"); return 1; }
+  *out = nullptr;
+  gmg_mg_opts opts{};
+  if (opts_in) opts = *opts_in;
+  std::unique_ptr<gmg_mg> mg;
+  if (create_hierarchy(levels, nlevels, opts, nullptr, 0, mg)) return 1;
   *out = mg.release();
+  return 0;
+}
+
+// Independent instances (each a UG hierarchy with its own depth) stored
+// block-diagonally: union level l holds, in instance order, level l of every
+// instance that has one.  Instance k's finest level top[k] must be its surface
+// (VNCLASS < 2 on every row, as on UG's top level) and its lower levels must
+// be reset by the restriction (VNCLASS >= 2): then one lmgc cycle on the union
+// from the deepest level is, for every instance, the cycle it runs alone.
+int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *inst_nlevels, int ninst,
+                          const gmg_mg_opts *opts_in, gmg_mg **out) {
+  if (!out || !instances || !inst_nlevels || ninst < 1) { set_error("gmg_mg_create_batched: bad arguments"); return 1; }
+  *out = nullptr;
+  gmg_mg_opts opts{};
+  if (opts_in) opts = *opts_in;
+  int nl = 0;
+  for (int k = 0; k < ninst; ++k) {
+    GMG_CHECK(instances[k] && inst_nlevels[k] >= 1, "instance %d has no levels", k);
+    nl = std::max(nl, inst_nlevels[k]);
+  }
+  const int s = instances[0][0].s;
+  struct U {
+    std::vector<int> rowptr{0}, col, vclass, vnclass, skip, prow{0}, pcol;
+    std::vector<double> val, pw;
+  };
+  std::vector<U> u(nl);
+  std::vector<std::vector<int>> off(nl, std::vector<int>(ninst, -1)), colours;
+  if (opts.order == GMG_ORDER_COLOR) colours.resize(nl);
+  std::vector<gmg_level_desc> desc(nl);
+  for (int l = 0; l < nl; ++l) {
+    U &d = u[l];
+    int n = 0;
+    for (int k = 0; k < ninst; ++k) {
+      if (inst_nlevels[k] <= l) continue;
+      const gmg_level_desc &e = instances[k][l];
+      const bool top = l == inst_nlevels[k] - 1;
+      GMG_CHECK(e.s == s, "instance %d level %d: block size %d, expected %d", k, l, e.s, s);
+      GMG_CHECK(e.n >= 0 && (e.n == 0 || (e.rowptr && e.col && e.val)), "instance %d level %d: arrays missing", k, l);
+      GMG_CHECK(l == 0 || (e.prowptr && e.pcol && e.pw), "instance %d level %d: transfer arrays missing", k, l);
+      off[l][k] = n;
+      for (int i = 0; i < e.n; ++i) {
+        GMG_CHECK(e.rowptr[i + 1] > e.rowptr[i], "instance %d level %d row %d: no diagonal entry", k, l, i);
+        for (int q = e.rowptr[i]; q < e.rowptr[i + 1]; ++q) {
+          GMG_CHECK(e.col[q] >= 0 && e.col[q] < e.n, "instance %d level %d row %d: column out of range", k, l, i);
+          d.col.push_back(e.col[q] + n);
+        }
+        d.val.insert(d.val.end(), e.val + size_t(e.rowptr[i]) * s * s, e.val + size_t(e.rowptr[i + 1]) * s * s);
+        d.rowptr.push_back(int(d.col.size()));
+        const int vn = e.vnclass ? e.vnclass[i] : (top ? 0 : 3);
+        GMG_CHECK(top ? vn < 2 : vn >= 2,
+                  "instance %d level %d row %d: VNCLASS %d (a batched instance's top level is its surface)", k, l,
+                  i, vn);
+        d.vclass.push_back(e.vclass ? e.vclass[i] : 3);
+        d.vnclass.push_back(vn);
+        d.skip.push_back(e.skip ? e.skip[i] : 0);
+        if (l > 0) {
+          const int nc = instances[k][l - 1].n;
+          for (int q = e.prowptr[i]; q < e.prowptr[i + 1]; ++q) {
+            GMG_CHECK(e.pcol[q] >= 0 && e.pcol[q] < nc, "instance %d level %d: transfer index out of range", k, l);
+            d.pcol.push_back(e.pcol[q] + off[l - 1][k]);
+            d.pw.push_back(e.pw[q]);
+          }
+          d.prow.push_back(int(d.pcol.size()));
+        }
+      }
+      if (!colours.empty()) {
+        int nc = 0;
+        std::vector<int> c = greedy_colour(e.n, sym_adjacency(e.n, e.rowptr, e.col), &nc);
+        colours[l].insert(colours[l].end(), c.begin(), c.end());
+      }
+      n += e.n;
+    }
+    desc[l] = gmg_level_desc{n, s, d.rowptr.data(), d.col.data(), d.val.data(), d.vclass.data(), d.vnclass.data(),
+                             d.skip.data(), l ? d.prow.data() : nullptr, l ? d.pcol.data() : nullptr,
+                             l ? d.pw.data() : nullptr};
+  }
+  std::vector<long long> pack_off(ninst + 1, 0);
+  for (int k = 0; k < ninst; ++k) pack_off[k + 1] = pack_off[k] + instances[k][inst_nlevels[k] - 1].n;
+  std::unique_ptr<gmg_mg> mg;
+  if (create_hierarchy(desc.data(), nl, opts, colours.empty() ? nullptr : &colours, size_t(pack_off[ninst]) * s, mg))
+    return 1;
+  u.clear();
+  auto &B = mg->batch;
+  B.ninst = ninst;
+  B.list_off = off;
+  B.pack_off = pack_off;
+  for (int k = 0; k < ninst; ++k) {
+    B.top.push_back(inst_nlevels[k] - 1);
+    B.nrows_top.push_back(instances[k][inst_nlevels[k] - 1].n);
+  }
+  for (int l = 0; l < nl; ++l) {
+    Level &L = mg->lev[l];
+    // independent blocks of this level (block-diagonal base solves)
+    L.blk_ptr.assign(1, 0);
+    L.blk_rows.clear();
+    std::vector<int> iperm(L.n);
+    for (int i = 0; i < L.n; ++i) iperm[L.perm[i]] = i;
+    for (int k = 0; k < ninst; ++k) {
+      if (off[l][k] < 0) continue;
+      const int n = instances[k][l].n;
+      std::vector<int> r(n);
+      for (int j = 0; j < n; ++j) r[j] = iperm[off[l][k] + j];
+      std::sort(r.begin(), r.end());
+      L.blk_rows.insert(L.blk_rows.end(), r.begin(), r.end());
+      L.blk_ptr.push_back(int(L.blk_rows.size()));
+    }
+    gmg_mg::Batch::TopLevel tl;
+    tl.level = l;
+    std::vector<int> ptr{0}, rows, pack;
+    for (int k = 0; k < ninst; ++k) {
+      if (B.top[k] != l) continue;
+      tl.ids.push_back(k);
+      std::vector<int> r = instance_rows(L, off[l][k], B.nrows_top[k]);
+      for (int j = 0; j < B.nrows_top[k]; ++j) pack.push_back(int(pack_off[k] + j));
+      rows.insert(rows.end(), r.begin(), r.end());
+      ptr.push_back(int(rows.size()));
+    }
+    if (tl.ids.empty()) continue;
+    tl.ninst = int(tl.ids.size());
+    tl.nrows = int(rows.size());
+    if (upload_owned(L, &tl.ids_dev, tl.ids) || upload_owned(L, &tl.ptr_dev, ptr) || upload_owned(L, &tl.rows_dev, rows) ||
+        upload_owned(L, &tl.pack_dev, pack))
+      return 1;
+    B.tops.push_back(std::move(tl));
+  }
+  GMG_CHECK(pack_off[ninst] < (1LL << 31), "batched hierarchy: more than 2^31 top-level rows");
+  Level &T = mg->lev.back();
+  GMG_CUDA(cudaMalloc(&B.conv_dev, ninst));
+  T.own.push_back(B.conv_dev);
+  GMG_CUDA(cudaMemset(B.conv_dev, 0, ninst));
+  GMG_CUDA(cudaMallocHost(&B.conv_host, ninst));
+  std::memset(B.conv_host, 0, ninst);
+  GMG_CUDA(cudaMalloc(&B.norms_dev, sizeof(double) * ninst * GMG_MAX_S));
+  T.own.push_back(B.norms_dev);
+  GMG_CUDA(cudaMemset(B.norms_dev, 0, sizeof(double) * ninst * GMG_MAX_S));
+  GMG_CUDA(cudaMallocHost(&B.norms_host, sizeof(double) * ninst * GMG_MAX_S));
+  *out = mg.release();
+  return 0;
+}
+
+int gmg_mg_num_instances(const gmg_mg *mg) { return mg ? mg->batch.ninst : 0; }
+
+int gmg_mg_instance_info(const gmg_mg *mg, int k, int *top, int *n_top, long long *pack_offset) {
+  if (!mg || k < 0 || k >= mg->batch.ninst) { set_error("gmg_mg_instance_info: bad instance %d", k); return 1; }
+  if (top) *top = mg->batch.top[k];
+  if (n_top) *n_top = mg->batch.nrows_top[k];
+  if (pack_offset) *pack_offset = mg->batch.pack_off[k];
   return 0;
 }
 

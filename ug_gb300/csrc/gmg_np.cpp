@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <numeric>
 #include <sstream>
 #include <typeinfo>
 
@@ -406,29 +407,16 @@ int NPIlu::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
 
 // ex: EXPreProcess (iter.cc:8685) decomposes the level matrix once; here the
 // decomposition is an explicit FP64 inverse (Gauss-Jordan, partial pivoting).
-int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *result) {
-  if (check_level(mg, level)) return 1;
-  Level &L = mg->lev[level];
-  *baselevel = level;
-  if (L.ainv) return 0;
-  const int N = L.n * L.s, s = L.s;
-  GMG_CHECK(N <= 4096, "ex: level %d has %d unknowns, above the dense base-solver limit 4096", level, N);
-  std::vector<double> a(size_t(N) * N, 0.0), inv(size_t(N) * N, 0.0);
-  for (int i = 0; i < L.n; ++i)
-    for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k)
-      for (int r = 0; r < s; ++r)
-        for (int c = 0; c < s; ++c)
-          a[size_t(i * s + r) * N + L.h_col[k] * s + c] = L.h_val[size_t(k) * s * s + r * s + c];
+// Gauss-Jordan with partial pivoting: inv = a^{-1} (a is destroyed); returns
+// 0, or the 1-based column without a pivot
+static int gauss_jordan(std::vector<double> &a, std::vector<double> &inv, int N) {
+  inv.assign(size_t(N) * N, 0.0);
   for (int i = 0; i < N; ++i) inv[size_t(i) * N + i] = 1.0;
   for (int c = 0; c < N; ++c) {
     int p = c;
     for (int r = c + 1; r < N; ++r)
       if (std::fabs(a[size_t(r) * N + c]) > std::fabs(a[size_t(p) * N + c])) p = r;
-    if (a[size_t(p) * N + c] == 0.0) {
-      *result = -(c + 1);
-      set_error("ex: singular base-level matrix");
-      return 1;
-    }
+    if (a[size_t(p) * N + c] == 0.0) return c + 1;
     if (p != c)
       for (int k = 0; k < N; ++k) {
         std::swap(a[size_t(p) * N + k], a[size_t(c) * N + k]);
@@ -445,6 +433,73 @@ int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel,
         inv[size_t(r) * N + k] -= f * inv[size_t(c) * N + k];
       }
     }
+  }
+  return 0;
+}
+
+// dense copy of the rows `rows` (processing order, a closed block of the level)
+static void dense_block(const Level &L, const int *rows, int m, std::vector<double> &a) {
+  const int s = L.s, N = m * s;
+  a.assign(size_t(N) * N, 0.0);
+  std::map<int, int> local;
+  for (int q = 0; q < m; ++q) local[rows[q]] = q;
+  for (int q = 0; q < m; ++q) {
+    const int i = rows[q];
+    for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k) {
+      const int j = local.at(L.h_col[k]);
+      for (int r = 0; r < s; ++r)
+        for (int c = 0; c < s; ++c) a[size_t(q * s + r) * N + j * s + c] = L.h_val[size_t(k) * s * s + r * s + c];
+    }
+  }
+}
+
+int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *result) {
+  if (check_level(mg, level)) return 1;
+  Level &L = mg->lev[level];
+  *baselevel = level;
+  if (L.ainv) return 0;
+  const int s = L.s;
+  std::vector<double> a, inv, all;
+  if (L.blk_ptr.size() > 1) {
+    // block-diagonal level of a batched hierarchy: one inverse per instance
+    const int nb = int(L.blk_ptr.size()) - 1;
+    std::vector<long long> aoff(nb, 0);
+    for (int b = 0; b < nb; ++b) {
+      const int m = L.blk_ptr[b + 1] - L.blk_ptr[b], N = m * s;
+      GMG_CHECK(N <= 4096, "ex: level %d block %d has %d unknowns, above the dense base-solver limit 4096", level, b, N);
+      dense_block(L, L.blk_rows.data() + L.blk_ptr[b], m, a);
+      if (int c = gauss_jordan(a, inv, N)) {
+        *result = -c;
+        set_error("ex: singular base-level matrix of instance block %d", b);
+        return 1;
+      }
+      aoff[b] = (long long)all.size();
+      all.insert(all.end(), inv.begin(), inv.end());
+    }
+    GMG_CUDA(cudaMalloc(&L.ainv, std::max<size_t>(all.size(), 1) * sizeof(double)));
+    GMG_CUDA(cudaMemcpy(L.ainv, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+    GMG_CUDA(cudaMalloc(&L.blk_ptr_dev, L.blk_ptr.size() * sizeof(int)));
+    L.own.push_back(L.blk_ptr_dev);
+    GMG_CUDA(cudaMemcpy(L.blk_ptr_dev, L.blk_ptr.data(), L.blk_ptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    GMG_CUDA(cudaMalloc(&L.blk_rows_dev, std::max<size_t>(L.blk_rows.size(), 1) * sizeof(int)));
+    L.own.push_back(L.blk_rows_dev);
+    GMG_CUDA(cudaMemcpy(L.blk_rows_dev, L.blk_rows.data(), L.blk_rows.size() * sizeof(int), cudaMemcpyHostToDevice));
+    GMG_CUDA(cudaMalloc(&L.blk_aoff_dev, nb * sizeof(long long)));
+    L.own.push_back(L.blk_aoff_dev);
+    GMG_CUDA(cudaMemcpy(L.blk_aoff_dev, aoff.data(), nb * sizeof(long long), cudaMemcpyHostToDevice));
+    L.nblk_dev = nb;
+    L.base_dim = 0;  // no single dense inverse (the fused coarse cycle needs one)
+    return 0;
+  }
+  const int N = L.n * s;
+  GMG_CHECK(N <= 4096, "ex: level %d has %d unknowns, above the dense base-solver limit 4096", level, N);
+  std::vector<int> rows(L.n);
+  std::iota(rows.begin(), rows.end(), 0);
+  dense_block(L, rows.data(), L.n, a);
+  if (int c = gauss_jordan(a, inv, N)) {
+    *result = -c;
+    set_error("ex: singular base-level matrix");
+    return 1;
   }
   GMG_CUDA(cudaMalloc(&L.ainv, inv.size() * sizeof(double)));
   GMG_CUDA(cudaMemcpy(L.ainv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -633,7 +688,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   if (!t) t = temp_vec(mg, name + "__t" + std::to_string(prec), prec);
   GMG_CHECK(t, "lmgc: temporary vector");
   const int smo = fusable_smoother();
-  if (smo >= 0 && mg->lev[level].n <= fuse_rows &&
+  if (smo >= 0 && mg->batch.ninst == 0 && mg->lev[level].n <= fuse_rows &&
       coarse_smem_bytes(mg, baselevel, level, prec, smo) <= COARSE_SMEM_BUDGET) {
     // this level and everything below it: one cluster kernel
     CoarseCfg cfg;
@@ -756,10 +811,23 @@ int NPLs::PreProcess(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *bl, 
   return 0;
 }
 
+bool NPLs::batched(int level) const { return mg->batch.ninst > 0 && level == int(mg->lev.size()) - 1; }
+
 // LinearDefect, ls.cc:562: b -= A x on the surface, which is the top level
-// of a uniformly refined hierarchy
-int NPLs::Defect(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *, int *) {
+// of a uniformly refined hierarchy (on a batched hierarchy: every instance's
+// own top level; a level that is some instance's top is updated whole, which
+// only touches the other instances' restricted, reset rows there)
+int NPLs::Defect(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *res) {
   if (check_level(mg, level)) return 1;
+  if (batched(level)) {
+    for (const auto &tl : mg->batch.tops)
+      if (defect_level(tl.level, xv, bv)) return 1;
+    return 0;
+  }
+  return defect_level(level, xv, bv);
+}
+
+int NPLs::defect_level(int level, gmg_vec *xv, gmg_vec *bv) {
   if (bv->prec == GMG_PREC_FP64)
     return k_matmul_minus_mixed(mg, mg->lev[level], (double *)vlev(bv, level), xv->prec, vlev(xv, level));
   GMG_CHECK(xv->prec == bv->prec, "ls: precision mismatch");
@@ -770,6 +838,18 @@ int NPLs::Defect(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *, int *) {
 int NPLs::Residuum(int, int tl, gmg_vec *, gmg_vec *bv, gmg_mat *, gmg_lresult *lr) {
   if (check_level(mg, tl)) return 1;
   const int s = mg->lev[tl].s;
+  if (batched(tl)) {
+    // per-instance defect norms, each on the instance's own top level
+    const auto &B = mg->batch;
+    if (batch_norms(bv)) return 1;
+    GMG_CUDA(cudaStreamSynchronize(mg->stream));
+    inst_last.assign(B.norms_host, B.norms_host + size_t(B.ninst) * GMG_MAX_S);
+    for (int r = 0; r < s; ++r) {
+      lr->last_defect[r] = 0.0;
+      for (int k = 0; k < B.ninst; ++k) lr->last_defect[r] = std::max(lr->last_defect[r], inst_last[k * GMG_MAX_S + r]);
+    }
+    return 0;
+  }
   if (k_nrm2x(mg, mg->lev[tl], bv->prec, vlev(bv, tl))) return 1;
   GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
@@ -781,7 +861,54 @@ int NPLs::Residuum(int, int tl, gmg_vec *, gmg_vec *bv, gmg_mat *, gmg_lresult *
 // dset(c, 0); Iter(c, b); LSUpdate x += c; norm of b into mg->norms_dev.
 // Mixed: the iteration runs on FP32 copies (b32 = b; c32) and the FP64 defect
 // is updated as b -= A c with the FP64 matrix (iterative refinement).
+int NPLs::batch_norms(gmg_vec *bv) {
+  const auto &B = mg->batch;
+  for (const auto &tl : B.tops)
+    if (k_batch_update_norm(mg, tl, bv->prec, vlev(bv, tl.level), nullptr, GMG_PREC_FP64, nullptr, mg->lev[0].s))
+      return 1;
+  GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
+                           mg->stream));
+  return 0;
+}
+
+// one ls iteration of every instance of a batched hierarchy: the converged
+// flags go to the device first; one lmgc cycle on the union from the deepest
+// level is each instance's own cycle; then per top level x += c on the rows
+// of the instances that are still iterating and their defect norms.
+int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const auto &B = mg->batch;
+  const int s = mg->lev[level].s;
+  GMG_CUDA(cudaMemcpyAsync(B.conv_dev, B.conv_host, B.ninst, cudaMemcpyHostToDevice, mg->stream));
+  if (!mixed) {
+    // c below the deepest level is reset by every restriction of the cycle
+    if (k_set(mg, cvec->prec, vlev(cvec, level), vlen(mg, level), 0.0)) return 1;
+    if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
+    for (const auto &tl : B.tops)
+      if (k_batch_update_norm(mg, tl, bv->prec, vlev(bv, tl.level), (double *)vlev(xv, tl.level), cvec->prec,
+                              vlev(cvec, tl.level), s))
+        return 1;
+  } else {
+    for (const auto &tl : B.tops)
+      if (k_refine_prepare(mg, (float *)vlev(b32, tl.level), (float *)vlev(cvec, tl.level),
+                           (const double *)vlev(bv, tl.level), vlen(mg, tl.level)))
+        return 1;
+    if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    for (const auto &tl : B.tops) {
+      if (k_matmul_minus_mixed(mg, mg->lev[tl.level], (double *)vlev(bv, tl.level), GMG_PREC_FP32,
+                               vlev(cvec, tl.level)))
+        return 1;
+      if (k_batch_update_norm(mg, tl, GMG_PREC_FP64, vlev(bv, tl.level), (double *)vlev(xv, tl.level), GMG_PREC_FP32,
+                              vlev(cvec, tl.level), s))
+        return 1;
+    }
+  }
+  GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
+                           mg->stream));
+  return 0;
+}
+
 int NPLs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  if (batched(level)) return batch_iteration(level, xv, bv, Am, err);
   const Level &L = mg->lev[level];
   const long long len = vlen(mg, level);
   if (!mixed) {
@@ -831,39 +958,15 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   }
   lr->converged = sc_cmp(lr->first_defect, abs_, s);
   lr->number_of_linear_iterations = 0;
-  const bool graph_ok = use_graph && IterNp->capturable();
   if (graph && (graph_level != level || graph_x != xv || graph_b != bv)) {
     cudaGraphExecDestroy(graph);
     graph = nullptr;
   }
+  if (batched(level)) return batch_solver(level, xv, bv, Am, abs_, red, lr);
   int i;
   for (i = 0; i < maxiter; ++i) {
     if (lr->converged) break;
-    int err = 0;
-    // the first iteration runs eagerly (it creates the numprocs' temporaries);
-    // the following ones replay one captured graph of the iteration
-    if (graph_ok && (graph || i > 0)) {
-      if (!graph) {
-        cudaGraph_t g;
-        const long long before = mg->launches;
-        GMG_CUDA(cudaStreamBeginCapture(mg->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = iteration(level, xv, bv, Am, &err);
-        cudaError_t ce = cudaStreamEndCapture(mg->stream, &g);
-        if (rc) { if (ce == cudaSuccess) cudaGraphDestroy(g); return 1; }
-        GMG_CUDA(ce);
-        GMG_CUDA(cudaGraphInstantiate(&graph, g, 0));
-        cudaGraphDestroy(g);
-        graph_level = level; graph_x = xv; graph_b = bv;
-        graph_kernels = mg->launches - before;  // captured, not yet run
-        mg->launches = before;
-      }
-      GMG_CUDA(cudaGraphLaunch(graph, mg->stream));
-      mg->launches += graph_kernels;
-    } else if (iteration(level, xv, bv, Am, &err)) {
-      lr->error_code = err;
-      return 1;
-    }
-    GMG_CUDA(cudaStreamSynchronize(mg->stream));
+    if (step(i, level, xv, bv, Am, lr)) return 1;
     for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
     for (int r = 0; r < s; ++r)
       GMG_CHECK(std::isfinite(lr->last_defect[r]), "ls: defect is not finite in iteration %d", i + 1);
@@ -874,6 +977,100 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
     }
   }
   if (!lr->converged) lr->number_of_linear_iterations = i;
+  return 0;
+}
+
+// iteration i of the solver loop, synchronised: the first runs eagerly (it
+// creates the numprocs' temporaries), the following ones replay one captured
+// graph of the iteration
+int NPLs::step(int i, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, gmg_lresult *lr) {
+  int err = 0;
+  const bool graph_ok = use_graph && IterNp->capturable();
+  if (graph_ok && (graph || i > 0)) {
+    if (!graph) {
+      cudaGraph_t g;
+      const long long before = mg->launches;
+      GMG_CUDA(cudaStreamBeginCapture(mg->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = iteration(level, xv, bv, Am, &err);
+      cudaError_t ce = cudaStreamEndCapture(mg->stream, &g);
+      if (rc) { if (ce == cudaSuccess) cudaGraphDestroy(g); return 1; }
+      GMG_CUDA(ce);
+      GMG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+      cudaGraphDestroy(g);
+      graph_level = level; graph_x = xv; graph_b = bv;
+      graph_kernels = mg->launches - before;  // captured, not yet run
+      mg->launches = before;
+    }
+    GMG_CUDA(cudaGraphLaunch(graph, mg->stream));
+    mg->launches += graph_kernels;
+  } else if (iteration(level, xv, bv, Am, &err)) {
+    lr->error_code = err;
+    return 1;
+  }
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  return 0;
+}
+
+// LinearSolver on a batched hierarchy: every instance keeps its own first
+// defect, reduction target and convergence test (ls.cc:680-730); converged
+// instances stop updating x while the others iterate.  lr receives the
+// largest first / last defect over the instances, the largest iteration
+// count, and converged = all converged.
+int NPLs::batch_solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double *abs_, const double *red,
+                       gmg_lresult *lr) {
+  auto &B = mg->batch;
+  const int s = mg->lev[level].s, ni = B.ninst;
+  GMG_CHECK(xv->prec == GMG_PREC_FP64, "ls on a batched hierarchy needs an FP64 x");
+  GMG_CHECK((int)inst_last.size() == ni * GMG_MAX_S, "ls on a batched hierarchy: Residuum must run before Solver");
+  const int min_top = *std::min_element(B.top.begin(), B.top.end());
+  GMG_CHECK(baselevel <= min_top, "batched ls: base level %d above the shallowest instance's top level %d", baselevel,
+            min_top);
+  if (const NPLmgc *m = dynamic_cast<const NPLmgc *>(IterNp))
+    GMG_CHECK(m->gamma == 1, "batched ls: lmgc with gamma %d (only V-cycles advance every instance alike)", m->gamma);
+  inst_first = inst_last;
+  inst_iters.assign(ni, 0);
+  inst_conv.assign(ni, 0);
+  std::vector<double> reach(size_t(ni) * GMG_MAX_S, 0.0);
+  for (int k = 0; k < ni; ++k) {
+    for (int r = 0; r < s; ++r) {
+      reach[k * GMG_MAX_S + r] = inst_first[k * GMG_MAX_S + r] * red[r];
+      if (reach[k * GMG_MAX_S + r] == 0.0) reach[k * GMG_MAX_S + r] = red[r];
+    }
+    inst_conv[k] = sc_cmp(&inst_first[k * GMG_MAX_S], abs_, s);
+  }
+  int i;
+  for (i = 0; i < maxiter; ++i) {
+    bool all = true;
+    for (int k = 0; k < ni; ++k) {
+      B.conv_host[k] = uint8_t(inst_conv[k]);
+      all = all && inst_conv[k];
+    }
+    if (all) break;
+    if (step(i, level, xv, bv, Am, lr)) return 1;
+    for (int k = 0; k < ni; ++k) {
+      if (inst_conv[k]) continue;
+      const double *d = B.norms_host + size_t(k) * GMG_MAX_S;
+      for (int r = 0; r < s; ++r) {
+        GMG_CHECK(std::isfinite(d[r]), "ls: defect of instance %d is not finite in iteration %d", k, i + 1);
+        inst_last[k * GMG_MAX_S + r] = d[r];
+      }
+      if (sc_cmp(d, abs_, s) || sc_cmp(d, &reach[k * GMG_MAX_S], s)) {
+        inst_conv[k] = 1;
+        inst_iters[k] = i + 1;
+      }
+    }
+  }
+  lr->converged = 1;
+  lr->number_of_linear_iterations = 0;
+  for (int r = 0; r < s; ++r) lr->first_defect[r] = lr->last_defect[r] = 0.0;
+  for (int k = 0; k < ni; ++k) {
+    if (!inst_conv[k]) { inst_iters[k] = i; lr->converged = 0; }
+    lr->number_of_linear_iterations = std::max(lr->number_of_linear_iterations, inst_iters[k]);
+    for (int r = 0; r < s; ++r) {
+      lr->first_defect[r] = std::max(lr->first_defect[r], inst_first[k * GMG_MAX_S + r]);
+      lr->last_defect[r] = std::max(lr->last_defect[r], inst_last[k * GMG_MAX_S + r]);
+    }
+  }
   return 0;
 }
 
@@ -1146,12 +1343,65 @@ int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double 
   int bl = 0, res = 0;
   if (!(gls && gls->preprocessed) && ls->PreProcess(top, ls->x, ls->b, ls->A, &bl, &res)) return 1;
   *lr = gmg_lresult{};
-  if (gmg_vec_upload(ls->b, top, b_host)) return 1;
-  if (k_set(mg, ls->x->prec, vlev(ls->x, top), vlen(mg, top), 0.0)) return 1;
+  if (mg->batch.ninst > 0) {
+    // packed instance vectors; x = 0 on every instance's top level
+    if (gmg_vec_upload_packed(ls->b, b_host)) return 1;
+    for (const auto &tl : mg->batch.tops)
+      if (k_set(mg, ls->x->prec, vlev(ls->x, tl.level), vlen(mg, tl.level), 0.0)) return 1;
+  } else {
+    if (gmg_vec_upload(ls->b, top, b_host)) return 1;
+    if (k_set(mg, ls->x->prec, vlev(ls->x, top), vlen(mg, top), 0.0)) return 1;
+  }
   if (ls->Defect(top, ls->x, ls->b, ls->A, &res)) return 1;
   if (ls->Residuum(gls ? gls->baselevel : 0, top, ls->x, ls->b, ls->A, lr)) return 1;
   if (ls->Solver(top, ls->x, ls->b, ls->A, ls->abslimit, ls->reduction, lr)) return 1;
-  return gmg_vec_download(ls->x, top, x_host);
+  return mg->batch.ninst > 0 ? gmg_vec_download_packed(ls->x, x_host) : gmg_vec_download(ls->x, top, x_host);
+}
+
+static long long packed_len(const gmg_mg *mg) {
+  return mg->batch.pack_off.empty() ? 0 : mg->batch.pack_off.back() * mg->lev[0].s;
+}
+
+int gmg_vec_upload_packed(gmg_vec *v, const double *host) {
+  if (!v || !host) { set_error("gmg_vec_upload_packed: bad arguments"); return 1; }
+  gmg_mg *mg = v->mg;
+  GMG_CHECK(mg->batch.ninst > 0, "gmg_vec_upload_packed: not a batched hierarchy");
+  const size_t len = size_t(packed_len(mg));
+  std::memcpy(mg->stage_host, host, len * sizeof(double));
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+  for (const auto &tl : mg->batch.tops)
+    if (k_pack_gather(mg, v->prec, vlev(v, tl.level), (const double *)mg->stage_dev, tl, mg->lev[0].s)) return 1;
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  return 0;
+}
+
+int gmg_vec_download_packed(gmg_vec *v, double *host) {
+  if (!v || !host) { set_error("gmg_vec_download_packed: bad arguments"); return 1; }
+  gmg_mg *mg = v->mg;
+  GMG_CHECK(mg->batch.ninst > 0, "gmg_vec_download_packed: not a batched hierarchy");
+  const size_t len = size_t(packed_len(mg));
+  for (const auto &tl : mg->batch.tops)
+    if (k_pack_scatter(mg, v->prec, (double *)mg->stage_dev, vlev(v, tl.level), tl, mg->lev[0].s)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, len * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  std::memcpy(host, mg->stage_host, len * sizeof(double));
+  return 0;
+}
+
+int gmg_ls_instance_result(gmg_np *np, int k, gmg_lresult *lr) {
+  NPLs *ls = dynamic_cast<NPLs *>(np);
+  GMG_CHECK(ls && lr, "gmg_ls_instance_result: not an ls numproc");
+  const int ni = ls->mg->batch.ninst, s = ls->mg->lev[0].s;
+  GMG_CHECK(k >= 0 && k < ni, "gmg_ls_instance_result: bad instance %d", k);
+  GMG_CHECK((int)ls->inst_iters.size() == ni, "gmg_ls_instance_result: the solver has not run");
+  *lr = gmg_lresult{};
+  lr->converged = ls->inst_conv[k];
+  lr->number_of_linear_iterations = ls->inst_iters[k];
+  for (int r = 0; r < s; ++r) {
+    lr->first_defect[r] = ls->inst_first[k * GMG_MAX_S + r];
+    lr->last_defect[r] = ls->inst_last[k * GMG_MAX_S + r];
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -176,6 +176,17 @@ struct NPLs : NPLinearSolver {
   int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
   // the base-solver shortcut of lmgc: `ls $m 1 $I ex` as one kernel
   bool is_exact_base() const;
+  // iteration i of Solver's loop (graph replay after the first), synchronised
+  int step(int i, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr);
+  int defect_level(int level, gmg_vec *x, gmg_vec *b);
+  // batched hierarchies (gmg_mg_create_batched), solved on their deepest level
+  bool batched(int level) const;
+  std::vector<double> inst_first, inst_last;  // ninst * GMG_MAX_S, per-instance defects
+  std::vector<int> inst_iters, inst_conv;
+  int batch_norms(gmg_vec *b);  // per-instance defect norms into batch.norms_host (async)
+  int batch_iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
+  int batch_solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit, const double *reduction,
+                   gmg_lresult *lr);
 };
 
 // helpers shared by the numprocs and the C ABI
