@@ -176,18 +176,7 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- batched workload
-BATCH_N, BATCH_SEED, BATCH_VAR = 512, 4242, 0.5
-
-
-def batch_instances(G, count):
-    """The batched workload: `count` independent 2D Q1 Poisson instances on the
-    unit square, instance k refined L_k ~ U{3..7} times ((2^L+1)^2 = 81 ..
-    16,641 unknowns), k = exp(g) with its own seeded field (corr 0.1,
-    variance 0.5) and its own seeded uniform[-1,1] right-hand side."""
-    rng = np.random.default_rng(BATCH_SEED)
-    nrefs = rng.integers(3, 8, size=count)
-    return [G.Generator(G.Generator.POISSON2D, int(L), seed=BATCH_SEED + k, corr=CORR, var=BATCH_VAR)
-            for k, L in enumerate(nrefs)], [int(L) for L in nrefs]
+BATCH_N = 512
 
 
 def run_batched(args, stream, flush_l2, world, rank):
@@ -197,7 +186,8 @@ def run_batched(args, stream, flush_l2, world, rank):
     instance at a time (timed on a sample of instances)."""
     import torch
     import ug_gb300 as G
-    gens, nrefs = batch_instances(G, args.batch)
+    from ug_gb300.workloads import batch_instances
+    gens, nrefs = batch_instances(args.batch)
     mg = G.MultiGrid(gens, batched=True, order=G.ORDER_COLOR, fp32=True, device=torch.cuda.current_device())
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     G.setup_lmgc(mg, "jac", baselevel=0, red=RED, abslimit=1e-50, name="bat64")
@@ -290,7 +280,7 @@ def run_batched(args, stream, flush_l2, world, rank):
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import oracle
             oracle.build()
-            cs = sample[:8]
+            cs = sample
             t0 = time.perf_counter()
             for k in cs:
                 oracle.Hierarchy(gens[k].levels()).ls_solve(gens[k].rhs, smoother="jac", baselevel=0, damp=0.8,

@@ -63,13 +63,17 @@ BATCHES = [  # kind, nrefs of the instances, smoother, order, baselevel
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("bsmem", [None, 0, 200000])
 @pytest.mark.parametrize("kind,nrefs,sm,order,bl", BATCHES)
-def test_batched_equals_alone(G, oracle_mod, kind, nrefs, sm, order, bl):
+def test_batched_equals_alone(G, oracle_mod, kind, nrefs, sm, order, bl, bsmem):
+    """bsmem: the per-instance shared-memory budget of the batched fused
+    coarse cycle (None: default; 0: every level as separate launches;
+    200000: deep fusion, shallow instances run their whole cycle there)."""
     gens = _instances(G, kind, nrefs, var=0.5 if kind != 2 else 0.0)
     insts = [g.levels() for g in gens]
     mg = G.MultiGrid(insts, batched=True, order=order, fp32=True)
     assert mg.ninst == len(nrefs) and mg.inst_top == [len(l) - 1 for l in insts]
-    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50, bsmem=bsmem)
     b = mg.pack([g.rhs for g in gens])
     x, lr = mg.solve_host("mgs", b)
     assert lr.converged

@@ -6,6 +6,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/ug_gb300.h"
@@ -164,6 +165,7 @@ struct gmg_mg {
   double *stage_host = nullptr;// pinned, n_top*s doubles
   long long launches = 0;
   std::vector<std::unique_ptr<gmg::CoarseImageBase>> coarse_images;
+  std::map<std::tuple<int, int, int, int>, long long> coarse_smem_cache;  // (bl, lc, prec, smoother)
   // batched hierarchies (gmg_mg_create_batched): independent instances stored
   // block-diagonally in every level; instance k's finest level is top[k]
   struct Batch {
@@ -174,12 +176,17 @@ struct gmg_mg {
     std::vector<long long> pack_off;         // first row of instance k in the packed layout
     // per level that is some instance's top: instances with that top (local order)
     struct TopLevel {
-      int level = 0, ninst = 0, nrows = 0;
+      int level = 0, ninst = 0, nrows = 0, nchunks = 0;
       std::vector<int> ids;                  // global instance ids
       // instance-major row lists: rows_dev[ptr_dev[k]..ptr_dev[k+1]) are the
-      // processing-order rows of instance ids[k] in its own list order, and
-      // pack_dev[q] is row q's position in the packed host layout
+      // rows of instance ids[k] (ascending processing order), and pack_dev[q]
+      // is row q's position in the packed host layout
       int *ids_dev = nullptr, *ptr_dev = nullptr, *rows_dev = nullptr, *pack_dev = nullptr;
+      // chunks of at most BATCH_CHUNK rows of one instance: chunk h is rows
+      // chunk_q[h]..chunk_q[h+1] of instance chunk_k[h]; instance k owns chunks
+      // inst_cptr[k]..inst_cptr[k+1]; partial sums and per-instance tickets
+      int *chunk_k_dev = nullptr, *chunk_q_dev = nullptr, *inst_cptr_dev = nullptr, *ticket_dev = nullptr;
+      double *partial_dev = nullptr;
     };
     std::vector<TopLevel> tops;
     uint8_t *conv_dev = nullptr;             // converged flag per instance
@@ -192,6 +199,7 @@ struct gmg_mg {
 namespace gmg {
 
 constexpr int REDUCE_BLOCKS = 304;  // 2 x 152 SMs
+constexpr int BATCH_CHUNK = 256;    // rows per block of the batched ls update (one per thread)
 
 // ---------------------------------------------------------------- kernels (gmg_kernels.cu)
 // All launchers enqueue on `st`, count launches in mg->launches, return 0 / 1.
@@ -209,6 +217,9 @@ int k_matmul_minus_mixed(gmg_mg *mg, const Level &L, double *x, int yprec, const
 int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const float *c);
 // t = damp * D^{-1} b on ACTIVE rows, 0 elsewhere
 int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp);
+// one damped Jacobi smoothing step in one pass: t = damp D^{-1} bin (0 off
+// ACTIVE rows), bout = bin - A t, c += t (bout must not alias bin)
+int k_jac_step(gmg_mg *mg, const Level &L, int prec, void *bout, const void *bin, void *c, const double *damp);
 // forward Gauss-Seidel in processing order over the wavefronts; t is overwritten
 int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // ILU forward / backward solve with the factors of L
@@ -226,11 +237,12 @@ int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void 
 int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x);
 // base level: if |b| >= abslimit in some component: t = Ainv b; b -= A t; c += t
 int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit);
-// batched ls, on one top level: for each of its instances (one block each),
-// x += c on its rows unless converged[id], then the per-component norms of b
-// on its rows into norms[id*GMG_MAX_S + r]
-int k_batch_update_norm(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, const void *b, double *x,
-                        int cprec, const void *c, int s);
+// batched ls, the end of an iteration on one top level, over the rows of the
+// instances whose finest level it is: if spmv, b -= A c (FP64 matrix); x += c
+// unless the instance has converged (c != null); per-component norms of b
+// into batch.norms_dev[id*GMG_MAX_S + r]
+int k_batch_finish(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, void *b, double *x, int cprec,
+                   const void *c, bool spmv, int s);
 // the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
 struct CoarseCfg {
   int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;
@@ -240,6 +252,8 @@ int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_v
 // shared memory the fused cycle needs for levels bl..lc
 long long coarse_smem_bytes(const gmg_mg *mg, int bl, int lc, int prec, int smoother);
 constexpr long long COARSE_SMEM_BUDGET = 220 * 1024;
+// default per-instance budget of the batched fused cycle (several blocks per SM)
+constexpr long long BATCH_COARSE_SMEM_BUDGET = 64 * 1024;
 // packed instance vectors of a batched hierarchy <-> one top level's rows
 int k_pack_gather(gmg_mg *mg, int prec, void *dst, const double *packed, const gmg_mg::Batch::TopLevel &tl, int s);
 int k_pack_scatter(gmg_mg *mg, int prec, double *packed, const void *src, const gmg_mg::Batch::TopLevel &tl, int s);

@@ -271,6 +271,109 @@ __global__ void jac_kernel(int n, const T *__restrict__ dinv, const uint8_t *__r
   }
 }
 
+// ------------------------------------------------------------ fused Jacobi step
+// One damped Jacobi smoothing step of lmgc in one pass: l_jac with the
+// smoother's dscalx (t = damp D^{-1} b, 0 on rows that are not ACTIVE),
+// dmatmul_minus (b -= A t) and dadd (c += t).  Every t_j is recomputed where
+// it is used, from b_j and row j's inverse diagonal block with jac_kernel's
+// arithmetic, so the results are those of the two-pass step.  The new defect
+// goes to bout, which must not alias bin (rows read their neighbours' bin
+// while others write).
+template <class T, int S, bool ALL_ACTIVE>
+__device__ __forceinline__ void jac_value(const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
+                                          const T *__restrict__ b, int j, const Damp<T> &dm, T *t) {
+  if (!ALL_ACTIVE && !(__ldg(flags + j) & F_ACTIVE)) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) t[r] = T(0);
+    return;
+  }
+  T bv[S];
+#pragma unroll
+  for (int c = 0; c < S; ++c) bv[c] = __ldg(b + (size_t)j * S + c);
+  const T *D = dinv + (size_t)j * S * S;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    T v = T(0);
+#pragma unroll
+    for (int c = 0; c < S; ++c) v = fma(__ldg(D + r * S + c), bv[c], v);
+    t[r] = v * dm.d[r];
+  }
+}
+
+template <class T, int S, bool ALL_ACTIVE>
+__global__ void __launch_bounds__(BLK) sell_jac_step_kernel(int n, const int *__restrict__ sptr,
+                                                            const int *__restrict__ scol, const T *__restrict__ sval,
+                                                            const T *__restrict__ dinv,
+                                                            const uint8_t *__restrict__ flags,
+                                                            const T *__restrict__ bin, T *__restrict__ bout,
+                                                            T *__restrict__ c, Damp<T> dm) {
+  pdl_prologue();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int e0 = __ldg(sptr + (i >> 5));
+  const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  int e = e0 + (i & 31);
+#pragma unroll 4
+  for (int k = 0; k < w; ++k, e += 32) {
+    const int j = __ldg(scol + e);
+    const T *m = sval + (size_t)e * (S * S);
+    T tv[S];
+    jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, j, dm, tv);
+#pragma unroll
+    for (int cc = 0; cc < S; ++cc)
+#pragma unroll
+      for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + cc), tv[cc], s[r]);
+  }
+  T ti[S];
+  jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, i, dm, ti);
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    bout[(size_t)i * S + r] = bin[(size_t)i * S + r] - s[r];
+    c[(size_t)i * S + r] += ti[r];
+  }
+}
+
+template <class T, int S, int TPR, bool ALL_ACTIVE>
+__global__ void __launch_bounds__(BLK) jac_step_kernel(int n, const int *__restrict__ rowptr,
+                                                       const int *__restrict__ col, const T *__restrict__ val,
+                                                       const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
+                                                       const T *__restrict__ bin, T *__restrict__ bout,
+                                                       T *__restrict__ c, Damp<T> dm) {
+  pdl_prologue();
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = gt / TPR, lane = gt & (TPR - 1);
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+  if (row < n) {
+    const int k1 = __ldg(rowptr + row + 1);
+    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+      const int j = __ldg(col + k);
+      const T *m = val + (size_t)k * (S * S);
+      T tv[S];
+      jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, j, dm, tv);
+#pragma unroll
+      for (int r = 0; r < S; ++r)
+#pragma unroll
+        for (int cc = 0; cc < S; ++cc) s[r] = fma(__ldg(m + r * S + cc), tv[cc], s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+  if (row < n && lane == 0) {
+    T ti[S];
+    jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, row, dm, ti);
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      bout[(size_t)row * S + r] = bin[(size_t)row * S + r] - s[r];
+      c[(size_t)row * S + r] += ti[r];
+    }
+  }
+}
+
 // ------------------------------------------------------------ l_lgs
 // ugiter.cc:412: forward solve (D+L) t = b in processing order: row i uses
 // the entries to rows j < i (VINDEX(w) < VINDEX(v)), all of which belong to
@@ -585,33 +688,114 @@ __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, doub
 }
 
 // ------------------------------------------------------------ batched ls
-// One block per instance of a top level: LSUpdate (x += c, skipped once the
-// instance has converged, so its x stays the one of its own converged
-// iteration) and dnrm2x of its defect, summed in a fixed order.
-template <class TB, class TC, int S>
-__global__ void __launch_bounds__(BLK) batch_update_norm_kernel(const int *__restrict__ ids, const int *__restrict__ ptr,
-                                                                const int *__restrict__ rows,
-                                                                const uint8_t *__restrict__ flags,
-                                                                const uint8_t *__restrict__ conv,
-                                                                const TB *__restrict__ b, double *__restrict__ x,
-                                                                const TC *__restrict__ c, double *__restrict__ norms) {
+// The end of one ls iteration on one top level of a batched hierarchy, over
+// the rows of the instances whose finest level it is (no other rows):
+//   SPMV (mixed precision):  b -= A c with the FP64 matrix (refinement defect);
+//   LSUpdate:                x += c, unless the instance has converged (its x
+//                            then stays that of its converged iteration);
+//   dnrm2x:                  per-component norms of b on NEW_DEFECT rows.
+// One block per chunk of one instance's rows (processing order); the block
+// sums go to partial[], and the instance's last block to finish (a ticket
+// per instance, reset by that block) adds them in chunk order, so the norms
+// are deterministic.  c == nullptr: norms only.
+template <class TB, class TC, int S, bool SPMV>
+__global__ void __launch_bounds__(BLK) batch_finish_kernel(
+    const int *__restrict__ chunk_k, const int *__restrict__ chunk_q, const int *__restrict__ inst_cptr,
+    const int *__restrict__ ids, const int *__restrict__ rows, const uint8_t *__restrict__ flags,
+    const uint8_t *__restrict__ conv, const int *__restrict__ sptr, const int *__restrict__ scol,
+    const double *__restrict__ sval, const int *__restrict__ rowptr, const int *__restrict__ col,
+    const double *__restrict__ val, TB *__restrict__ b, double *__restrict__ x, const TC *__restrict__ c,
+    double *__restrict__ partial, int *__restrict__ ticket, double *__restrict__ norms) {
   pdl_prologue();
-  const int k = blockIdx.x, id = ids[k], r0 = ptr[k], r1 = ptr[k + 1];
+  const int ch = blockIdx.x, k = chunk_k[ch], q0 = chunk_q[ch], q1 = chunk_q[ch + 1];
+  const int id = ids[k];
   const bool upd = c != nullptr && !conv[id];
   double acc[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = 0.0;
-  for (int q = r0 + threadIdx.x; q < r1; q += blockDim.x) {
+  for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
     const int i = rows[q];
-    const bool nd = flags[i] & F_NEWDEF;
+    TB bi[S];
 #pragma unroll
-    for (int r = 0; r < S; ++r) {
-      if (upd) x[(size_t)i * S + r] += double(c[(size_t)i * S + r]);
-      const double v = nd ? double(b[(size_t)i * S + r]) : 0.0;
-      acc[r] = fma(v, v, acc[r]);
+    for (int r = 0; r < S; ++r) bi[r] = b[(size_t)i * S + r];
+    if (SPMV) {
+      double s[S];
+#pragma unroll
+      for (int r = 0; r < S; ++r) s[r] = 0.0;
+      if (sptr) {  // sliced ELLPACK row i: entries sptr[i/32] + 32 k + i%32
+        const int e0 = __ldg(sptr + (i >> 5));
+        const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+        int e = e0 + (i & 31);
+#pragma unroll 4
+        for (int kk = 0; kk < w; ++kk, e += 32) {
+          const int j = __ldg(scol + e);
+          const double *m = sval + (size_t)e * (S * S);
+#pragma unroll
+          for (int cc = 0; cc < S; ++cc) {
+            const double yv = double(__ldg(c + (size_t)j * S + cc));
+#pragma unroll
+            for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + cc), yv, s[r]);
+          }
+        }
+      } else {
+        for (int kk = __ldg(rowptr + i); kk < __ldg(rowptr + i + 1); ++kk) {
+          const int j = __ldg(col + kk);
+          const double *m = val + (size_t)kk * (S * S);
+#pragma unroll
+          for (int cc = 0; cc < S; ++cc) {
+            const double yv = double(__ldg(c + (size_t)j * S + cc));
+#pragma unroll
+            for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + cc), yv, s[r]);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < S; ++r) {
+        bi[r] -= s[r];
+        b[(size_t)i * S + r] = bi[r];
+      }
     }
+    if (upd)
+#pragma unroll
+      for (int r = 0; r < S; ++r) x[(size_t)i * S + r] += double(c[(size_t)i * S + r]);
+    if (flags[i] & F_NEWDEF)
+#pragma unroll
+      for (int r = 0; r < S; ++r) {
+        const double v = double(bi[r]);
+        acc[r] = fma(v, v, acc[r]);
+      }
   }
   __shared__ double sh[BLK / 32][S];
+  __shared__ bool last;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)ch * S + threadIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int n = inst_cptr[k + 1] - inst_cptr[k];
+    last = atomicAdd(ticket + k, 1) == n - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // the instance's chunk sums: thread t adds chunks t, t+BLK, ... in order,
+  // then a fixed-shape block reduction (deterministic for a given chunking)
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int q = inst_cptr[k] + threadIdx.x; q < inst_cptr[k + 1]; q += blockDim.x)
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc[r] += __ldcg(partial + (size_t)q * S + r);
+  __syncthreads();  // sh is reused
 #pragma unroll
   for (int r = 0; r < S; ++r) {
     double v = acc[r];
@@ -624,6 +808,7 @@ __global__ void __launch_bounds__(BLK) batch_update_norm_kernel(const int *__res
     for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
     norms[(size_t)id * GMG_MAX_S + threadIdx.x] = sqrt(v);
   }
+  if (threadIdx.x == 0) ticket[k] = 0;
 }
 
 // ------------------------------------------------------------ base solver
@@ -977,25 +1162,31 @@ int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long 
   return 0;
 }
 
-int k_batch_update_norm(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, const void *b, double *x,
-                        int cprec, const void *c, int s) {
-  if (tl.ninst == 0) return 0;
+int k_batch_finish(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, void *b, double *x, int cprec,
+                   const void *c, bool spmv, int s) {
+  if (tl.nchunks == 0) return 0;
   const auto &B = mg->batch;
-#define BU(TB, TC, SS)                                                                                          \
-  GMG_LAUNCH((batch_update_norm_kernel<TB, TC, SS>), tl.ninst, BLK, tl.ids_dev, tl.ptr_dev, tl.rows_dev,        \
-             mg->lev[tl.level].flags, B.conv_dev, (const TB *)b, x, (const TC *)c, B.norms_dev)
-#define BS(TB, TC)                                       \
-  if (s == 1) BU(TB, TC, 1);                             \
-  else if (s == 2) BU(TB, TC, 2);                        \
-  else if (s == 3) BU(TB, TC, 3);                        \
+  const Level &L = mg->lev[tl.level];
+  GMG_CHECK(!spmv || (bprec == GMG_PREC_FP64 && c), "batched refinement update needs an FP64 defect and c");
+#define BF(TB, TC, SS, SP)                                                                                        \
+  GMG_LAUNCH((batch_finish_kernel<TB, TC, SS, SP>), tl.nchunks, BLK, tl.chunk_k_dev, tl.chunk_q_dev,              \
+             tl.inst_cptr_dev, tl.ids_dev, tl.rows_dev, L.flags, B.conv_dev, L.sell ? L.sell_ptr : nullptr,       \
+             L.sell_col, L.sell_v64, L.A.rowptr, L.A.col, L.A.v64, (TB *)b, x, (const TC *)c, tl.partial_dev,     \
+             tl.ticket_dev, B.norms_dev)
+#define BS(TB, TC, SP)                         \
+  if (s == 1) BF(TB, TC, 1, SP);               \
+  else if (s == 2) BF(TB, TC, 2, SP);          \
+  else if (s == 3) BF(TB, TC, 3, SP);          \
   else { set_error("block size %d not compiled", s); return 1; }
-  if (bprec == GMG_PREC_FP64) {
-    if (cprec == GMG_PREC_FP64) { BS(double, double) } else { BS(double, float) }
+  if (spmv) {
+    if (cprec == GMG_PREC_FP32) { BS(double, float, true) } else { BS(double, double, true) }
+  } else if (bprec == GMG_PREC_FP64) {
+    if (cprec == GMG_PREC_FP64) { BS(double, double, false) } else { BS(double, float, false) }
   } else {
-    if (cprec == GMG_PREC_FP64) { BS(float, double) } else { BS(float, float) }
+    if (cprec == GMG_PREC_FP64) { BS(float, double, false) } else { BS(float, float, false) }
   }
 #undef BS
-#undef BU
+#undef BF
   LAUNCH_CHECK(mg);
   return 0;
 }
@@ -1063,6 +1254,52 @@ int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const do
 #undef JK
   LAUNCH_CHECK(mg);
   return 0;
+}
+
+template <class T, int S, bool ALL>
+int jac_step_dispatch(gmg_mg *mg, const Level &L, T *bout, const T *bin, T *c, Damp<T> dm) {
+  const T *dinv = dinv_of<T>(L);
+  if (L.sell && sell_val<T>(L)) {
+    GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sell_val<T>(L),
+               dinv, L.flags, bin, bout, c, dm);
+    LAUNCH_CHECK(mg);
+    return 0;
+  }
+  const T *val = mval<T>(L.A);
+  switch (L.tpr) {
+#define CASE(TP)                                                                                                 \
+  case TP:                                                                                                       \
+    GMG_LAUNCH((jac_step_kernel<T, S, TP, ALL>), grid_for((long long)L.n * TP), BLK, L.n, L.A.rowptr, L.A.col, val, \
+               dinv, L.flags, bin, bout, c, dm);                                                                 \
+    break;
+    CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32)
+#undef CASE
+    default: set_error("bad threads-per-row %d", L.tpr); return 1;
+  }
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_jac_step(gmg_mg *mg, const Level &L, int prec, void *bout, const void *bin, void *c, const double *damp) {
+  if (L.n == 0) return 0;
+#define JS(TT)                                                                                                  \
+  {                                                                                                             \
+    Damp<TT> dm = make_damp<TT>(damp, L.s);                                                                     \
+    TT *o = (TT *)bout, *cc = (TT *)c;                                                                          \
+    const TT *in = (const TT *)bin;                                                                             \
+    if (L.s == 1) return L.all_active ? jac_step_dispatch<TT, 1, true>(mg, L, o, in, cc, dm)                    \
+                                      : jac_step_dispatch<TT, 1, false>(mg, L, o, in, cc, dm);                  \
+    if (L.s == 2) return L.all_active ? jac_step_dispatch<TT, 2, true>(mg, L, o, in, cc, dm)                    \
+                                      : jac_step_dispatch<TT, 2, false>(mg, L, o, in, cc, dm);                  \
+    if (L.s == 3) return L.all_active ? jac_step_dispatch<TT, 3, true>(mg, L, o, in, cc, dm)                    \
+                                      : jac_step_dispatch<TT, 3, false>(mg, L, o, in, cc, dm);                  \
+    set_error("block size %d not compiled", L.s);                                                               \
+    return 1;                                                                                                   \
+  }
+  if (prec == GMG_PREC_FP64) JS(double)
+  GMG_CHECK(L.dinv32 && L.A.v32, "FP32 copy not built");
+  JS(float)
+#undef JS
 }
 
 template <class T, int S>

@@ -712,20 +712,36 @@ int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *ins
     }
     gmg_mg::Batch::TopLevel tl;
     tl.level = l;
-    std::vector<int> ptr{0}, rows, pack;
+    std::vector<int> ptr{0}, rows, pack, chunk_k, chunk_q{0}, inst_cptr{0};
     for (int k = 0; k < ninst; ++k) {
       if (B.top[k] != l) continue;
+      const int kl = int(tl.ids.size());
       tl.ids.push_back(k);
       std::vector<int> r = instance_rows(L, off[l][k], B.nrows_top[k]);
-      for (int j = 0; j < B.nrows_top[k]; ++j) pack.push_back(int(pack_off[k] + j));
-      rows.insert(rows.end(), r.begin(), r.end());
+      std::vector<std::pair<int, int>> rp(r.size());
+      for (int j = 0; j < B.nrows_top[k]; ++j) rp[j] = {r[j], int(pack_off[k] + j)};
+      std::sort(rp.begin(), rp.end());
+      for (auto &e : rp) { rows.push_back(e.first); pack.push_back(e.second); }
+      for (int q = ptr.back(); q < int(rows.size()); q += BATCH_CHUNK) {
+        chunk_k.push_back(kl);
+        chunk_q.push_back(std::min(q + BATCH_CHUNK, int(rows.size())));
+      }
+      if (rows.size() == size_t(ptr.back())) {  // an instance without rows still gets its norm
+        chunk_k.push_back(kl);
+        chunk_q.push_back(int(rows.size()));
+      }
       ptr.push_back(int(rows.size()));
+      inst_cptr.push_back(int(chunk_k.size()));
     }
     if (tl.ids.empty()) continue;
     tl.ninst = int(tl.ids.size());
     tl.nrows = int(rows.size());
+    tl.nchunks = int(chunk_k.size());
     if (upload_owned(L, &tl.ids_dev, tl.ids) || upload_owned(L, &tl.ptr_dev, ptr) || upload_owned(L, &tl.rows_dev, rows) ||
-        upload_owned(L, &tl.pack_dev, pack))
+        upload_owned(L, &tl.pack_dev, pack) || upload_owned(L, &tl.chunk_k_dev, chunk_k) ||
+        upload_owned(L, &tl.chunk_q_dev, chunk_q) || upload_owned(L, &tl.inst_cptr_dev, inst_cptr) ||
+        upload_owned(L, &tl.ticket_dev, std::vector<int>(tl.ninst, 0)) ||
+        upload_owned(L, &tl.partial_dev, std::vector<double>(size_t(tl.nchunks) * s, 0.0)))
       return 1;
     B.tops.push_back(std::move(tl));
   }

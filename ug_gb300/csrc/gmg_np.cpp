@@ -171,6 +171,12 @@ int NPIter::IterAcc(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, gmg_vec *a
   return k_add(mg, acc->prec, vlev(acc, level), vlev(cv, level), vlen(mg, level));
 }
 
+int NPIter::IterAccN(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result) {
+  for (int i = 0; i < steps; ++i)
+    if (IterAcc(level, cv, bv, Am, acc, result)) return 1;
+  return 0;
+}
+
 // NPIterExecute, iter.cc:702-760
 int NPIter::Execute(const Args &a) {
   const int level = int(mg->lev.size()) - 1;
@@ -238,6 +244,25 @@ int NPJac::IterAcc(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc
   const Level &L = mg->lev[level];
   if (k_jac(mg, L, x->prec, vlev(x, level), vlev(bv, level), damp)) return 1;
   return k_matmul_minus(mg, L, x->prec, vlev(bv, level), vlev(x, level), vlev(acc, level));
+}
+
+int NPJac::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result) {
+  if (check_level(mg, level)) return 1;
+  // FP32 only: recomputing D^{-1} b per stored entry triples the FP64
+  // arithmetic per entry, and GB300's FP64 rate makes that slower than the
+  // two-pass step
+  if (x->prec != GMG_PREC_FP32 || acc->prec != x->prec || bv->prec != x->prec || steps < 2)
+    return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
+  gmg_vec *pp = temp_vec(mg, "__jac_pp" + std::to_string(x->prec), x->prec);
+  GMG_CHECK(pp, "jac: temporary vector");
+  const Level &L = mg->lev[level];
+  void *src = vlev(bv, level), *dst = vlev(pp, level);
+  for (int i = 0; i < steps; ++i) {
+    if (k_jac_step(mg, L, x->prec, dst, src, vlev(acc, level), damp)) return 1;
+    std::swap(src, dst);
+  }
+  if (src != vlev(bv, level) && k_copy(mg, x->prec, vlev(bv, level), src, vlen(mg, level))) return 1;
+  return 0;
 }
 
 // gs: l_lgs (ugiter.cc:412) in the hierarchy's processing order
@@ -612,6 +637,8 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
   }
   if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 6000;
   if (!a.get_int("cluster", &cluster)) cluster = 16;
+  int bs = 0;
+  batch_smem = a.get_int("bsmem", &bs) ? bs : BATCH_COARSE_SMEM_BUDGET;
   if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return NP_NOT_ACTIVE;
   int ret = InitIter(a);
   for (double &d : damp) d = 1.0;
@@ -688,8 +715,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   if (!t) t = temp_vec(mg, name + "__t" + std::to_string(prec), prec);
   GMG_CHECK(t, "lmgc: temporary vector");
   const int smo = fusable_smoother();
-  if (smo >= 0 && mg->batch.ninst == 0 && mg->lev[level].n <= fuse_rows &&
-      coarse_smem_bytes(mg, baselevel, level, prec, smo) <= COARSE_SMEM_BUDGET) {
+  if (smo >= 0 && fuse_here(level, prec, smo)) {
     // this level and everything below it: one cluster kernel
     CoarseCfg cfg;
     cfg.bl = baselevel; cfg.lc = level; cfg.smoother = smo;
@@ -702,8 +728,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
     }
     return k_coarse_cycle(mg, prec, cfg, cv, bv, t);
   }
-  for (int i = 0; i < nu1; ++i)
-    if (PreSmooth->IterAcc(level, t, bv, Am, cv, result)) return 1;
+  if (PreSmooth->IterAccN(level, t, bv, Am, cv, nu1, result)) return 1;
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};  // Factor_One
   if (typeid(*Transfer) == typeid(NPTransfer)) {
     // StandardRestrict and dset(c_{l-1}, 0) in one pass
@@ -724,9 +749,14 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
     if (k_add(mg, prec, vlev(cv, level), vlev(t, level), vlen(mg, level))) return 1;
   }
   if (k_matmul_minus(mg, mg->lev[level], prec, vlev(bv, level), vlev(t, level), nullptr)) return 1;
-  for (int i = 0; i < nu2; ++i)
-    if (PostSmooth->IterAcc(level, t, bv, Am, cv, result)) return 1;
+  if (PostSmooth->IterAccN(level, t, bv, Am, cv, nu2, result)) return 1;
   return 0;
+}
+
+bool NPLmgc::fuse_here(int level, int prec, int smo) {
+  if (mg->batch.ninst == 0)
+    return mg->lev[level].n <= fuse_rows && coarse_smem_bytes(mg, baselevel, level, prec, smo) <= COARSE_SMEM_BUDGET;
+  return batch_smem > 0 && fuse_rows > 0 && coarse_smem_bytes(mg, baselevel, level, prec, smo) <= batch_smem;
 }
 
 // LmgcPostProcess, iter.cc:7951
@@ -864,7 +894,7 @@ int NPLs::Residuum(int, int tl, gmg_vec *, gmg_vec *bv, gmg_mat *, gmg_lresult *
 int NPLs::batch_norms(gmg_vec *bv) {
   const auto &B = mg->batch;
   for (const auto &tl : B.tops)
-    if (k_batch_update_norm(mg, tl, bv->prec, vlev(bv, tl.level), nullptr, GMG_PREC_FP64, nullptr, mg->lev[0].s))
+    if (k_batch_finish(mg, tl, bv->prec, vlev(bv, tl.level), nullptr, GMG_PREC_FP64, nullptr, false, mg->lev[0].s))
       return 1;
   GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
                            mg->stream));
@@ -884,8 +914,8 @@ int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int 
     if (k_set(mg, cvec->prec, vlev(cvec, level), vlen(mg, level), 0.0)) return 1;
     if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
     for (const auto &tl : B.tops)
-      if (k_batch_update_norm(mg, tl, bv->prec, vlev(bv, tl.level), (double *)vlev(xv, tl.level), cvec->prec,
-                              vlev(cvec, tl.level), s))
+      if (k_batch_finish(mg, tl, bv->prec, vlev(bv, tl.level), (double *)vlev(xv, tl.level), cvec->prec,
+                         vlev(cvec, tl.level), false, s))
         return 1;
   } else {
     for (const auto &tl : B.tops)
@@ -893,14 +923,10 @@ int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int 
                            (const double *)vlev(bv, tl.level), vlen(mg, tl.level)))
         return 1;
     if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
-    for (const auto &tl : B.tops) {
-      if (k_matmul_minus_mixed(mg, mg->lev[tl.level], (double *)vlev(bv, tl.level), GMG_PREC_FP32,
-                               vlev(cvec, tl.level)))
+    for (const auto &tl : B.tops)
+      if (k_batch_finish(mg, tl, GMG_PREC_FP64, vlev(bv, tl.level), (double *)vlev(xv, tl.level), GMG_PREC_FP32,
+                         vlev(cvec, tl.level), true, s))
         return 1;
-      if (k_batch_update_norm(mg, tl, GMG_PREC_FP64, vlev(bv, tl.level), (double *)vlev(xv, tl.level), GMG_PREC_FP32,
-                              vlev(cvec, tl.level), s))
-        return 1;
-    }
   }
   GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
                            mg->stream));

@@ -57,6 +57,8 @@ struct NPIter : gmg_np {
   // Iter followed by acc += c (lmgc's dadd after each smoothing step);
   // smoothers fuse the addition into their defect update
   virtual int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result);
+  // `steps` of IterAcc in a row (lmgc's nu1 / nu2 smoothing loops)
+  virtual int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result);
   int Execute(const Args &a) override;  // NPIterExecute, iter.cc:702
   std::string Display() const override;
 };
@@ -75,6 +77,8 @@ struct NPJac : NPSmoother {  // jac, iter.cc:894-942
   int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
   int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) override;
   int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result) override;
+  // each step one fused kernel, the defect alternating between b and a scratch copy
+  int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result) override;
 };
 
 struct NPGs : NPSmoother {  // gs, iter.cc:974-1086
@@ -123,6 +127,10 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   // levels with at most fuse_rows VECTORs run as one fused cluster kernel
   // (gmg_coarse.cu); 0 disables.  cluster = CTAs of that kernel's cluster.
   int fuse_rows = 6000, cluster = 16;
+  // batched hierarchies: the fused cycle runs one block per instance, over
+  // the levels whose largest instance image fits batch_smem bytes ($bsmem; 0 disables)
+  long long batch_smem = BATCH_COARSE_SMEM_BUDGET;
+  bool fuse_here(int level, int prec, int smo);
   int Init(const Args &a) override;
   // smoother code of the fused kernel (0 jac, 1 gs, 2 ilu) or -1 if this
   // configuration cannot be fused

@@ -6,6 +6,9 @@ to --cycles ls iterations, with CUDA graphs off so that every kernel is an
 individual launch in the profiler's launch list.
 
     python -m ug_gb300.profile_case --cycles 2 [--fp64] [--nref 6] [--fuse 40000]
+
+With --batched N: N instances of the batched workload (2D Q1 Poisson,
+levels 3..7, Jacobi V(2,2)) in one batched hierarchy instead.
 """
 import argparse
 
@@ -18,7 +21,23 @@ def main():
     ap.add_argument("--nref", type=int, default=6)
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--fuse", type=int, default=40000)
+    ap.add_argument("--batched", type=int, default=0)
+    ap.add_argument("--order", default="color", choices=["color", "list"])
+    ap.add_argument("--bsmem", type=int, default=None)
     a = ap.parse_args()
+    if a.batched:
+        from ug_gb300.workloads import batch_instances
+        gens, _ = batch_instances(a.batched)
+        order = G.ORDER_COLOR if a.order == "color" else G.ORDER_LIST
+        mg = G.MultiGrid(gens, batched=True, order=order, fp32=True)
+        G.setup_lmgc(mg, "jac", baselevel=0, red=1e-8, maxit=a.cycles, mixed=not a.fp64, graph=False,
+                     bsmem=a.bsmem)
+        mg.launch_count(reset=True)
+        x, lr = mg.solve_host("mgs", mg.pack([g.rhs for g in gens]))
+        print(f"cycles={lr.iters} max defect {lr.first_defect[0]:.3e} -> {lr.last_defect[0]:.3e}, "
+              f"{mg.launch_count()} kernel launches")
+        mg.close()
+        return
     gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
     mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
     G.setup_lmgc(mg, "gs", baselevel=0, red=1e-8, maxit=a.cycles, mixed=not a.fp64, graph=False, fuse=a.fuse)
