@@ -199,6 +199,37 @@ int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_
  * GPU race; order them on one stream.  Enqueued on `stream` (cudaStream_t). */
 int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev, void *stream);
 
+/* ------------------------------------------------ serving pools */
+/* Continuous batching of solves on resident hierarchies (no UG counterpart:
+ * the request loop around UG's ls).  A pool holds `nslots` instances of one
+ * cached topology -- the 3D diffusion workload's unit cube (six Kuhn
+ * tetrahedra) refined `nref` times, the hierarchy gmg_gen_create(1, nref, ...)
+ * builds -- as one batched hierarchy with an ls (FP32 lmgc V(2,2) with
+ * `smoother` "gs" (multicolour) or "jac", base level 0, inside FP64
+ * iterative refinement to `red`, at most `maxit` iterations).  A request is
+ * admitted into a free slot by assembling its coefficient k = exp(g) (seed,
+ * corr, var as gmg_gen_create), its matrices on every level and its
+ * right-hand side on the device; each launch is one ls iteration of all
+ * slots; a poll tests every active slot against its own first defect, so
+ * requests join and leave between iterations.  Pools run on their own
+ * streams and overlap on the GPU.  Admit, fetch and slot_matrix need the
+ * pool idle (the last launch polled). */
+typedef struct gmg_pool gmg_pool;
+int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int maxit, int device, gmg_pool **out);
+int gmg_pool_destroy(gmg_pool *pool);
+gmg_mg *gmg_pool_multigrid(gmg_pool *pool);
+int gmg_pool_set_stream(gmg_pool *pool, void *stream);
+/* slots, VECTORs of one slot's finest level, free slots */
+int gmg_pool_slots(const gmg_pool *pool, int *nslots, int *n_top, int *free_slots);
+int gmg_pool_admit(gmg_pool *pool, int slot, unsigned long long seed, double corr, double var);
+int gmg_pool_launch(gmg_pool *pool);
+/* 0: still running; 1: finished, *ndone slots done (listed in done[]); -1: error */
+int gmg_pool_poll(gmg_pool *pool, int *ndone, int *done);
+/* a done slot's solution (n_top doubles, list order; x may be NULL) and LRESULT; frees the slot */
+int gmg_pool_fetch(gmg_pool *pool, int slot, double *x, gmg_lresult *lr);
+/* slot's matrix values on a level as the device holds them, in gmg_gen_levels' CSR order */
+int gmg_pool_slot_matrix(gmg_pool *pool, int slot, int level, double *val);
+
 /* ------------------------------------------------ one-call solve from host buffers */
 /* Uploads b (finest level, list order; packed on a batched hierarchy), runs ls
  * `solver` ($i $d $r $s $p, with the x/b given to npinit), downloads x. */

@@ -1,0 +1,127 @@
+"""Serving pools and the continuous-batching loop (ug_gb300/serve.py,
+ug_gb300/csrc/gmg_serve.cpp, gmg_assemble.cu).
+
+* On-device assembly reproduces the host generator's matrices: exactly up to
+  rounding (1e-13 relative) for k = 1, and to 2e-5 relative with the
+  log-normal field (the device evaluates the field's phases in 32-bit fixed
+  point and the cosines in FP32, ~1e-6 relative in k); the right-hand side is
+  the same position-keyed load (1e-15).
+* Alone == in the mix: a request's solution and iteration count are bitwise
+  the same whether it runs alone in a pool or joins it between iterations
+  while other requests come and go (same pool shape; every kernel is
+  row-local per slot and the norms reduce each slot's rows in a fixed order).
+* In the mix vs the host-assembled problem solved alone (MultiGrid on the
+  generator's hierarchy, the same mixed-precision solver): 1e-4 relative,
+  the difference of the coefficient fields.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+
+@pytest.fixture(scope="module")
+def G():
+    import ug_gb300
+    ug_gb300.lib()
+    return ug_gb300
+
+
+def test_stream_is_seeded(G):
+    from ug_gb300.serve import poisson_stream, slot_bytes
+    a, b = poisson_stream(50, 200.0), poisson_stream(50, 200.0)
+    assert [(r.arrival, r.nref, r.seed) for r in a] == [(r.arrival, r.nref, r.seed) for r in b]
+    assert all(2 <= r.nref <= 7 for r in a) and all(x.arrival < y.arrival for x, y in zip(a, a[1:]))
+    assert abs(np.mean(np.diff([r.arrival for r in poisson_stream(4000, 200.0)])) - 1 / 200) < 3e-4
+    assert slot_bytes(7) > 7 * slot_bytes(6) > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("var,tol", [(0.0, 1e-13), (1.0, 2e-5)])
+def test_device_assembly_matches_generator(G, var, tol):
+    from ug_gb300.serve import Pool
+    nref, seed = 3, 77
+    pool = Pool(nref, 2)
+    pool.free.remove(1)
+    pool.admit(1, seed, 0.1, var)
+    gen = G.Generator(G.Generator.DIFFUSION3D, nref, seed=seed, corr=0.1, var=var)
+    for l in range(nref + 1):
+        ref = gen.level(l)["val"]
+        got = pool.slot_matrix(1, l, ref.size)
+        assert rel(got, ref) <= tol, l
+    # the slot's right-hand side is the generator's (packed: slot after slot)
+    mg = G.lib().gmg_pool_multigrid(pool._h)
+    b = np.empty(pool.n_top * 2)
+    assert G.lib().gmg_vec_download_packed(G.lib().gmg_vec_by_name(mg, b"rhs"), b.ctypes.data) == 0
+    assert rel(b[pool.n_top:], gen.rhs) <= 1e-15
+    pool.close()
+
+
+def _mixed_solo(G, nref, seed, var):
+    gen = G.Generator(G.Generator.DIFFUSION3D, nref, seed=seed, corr=0.1, var=var)
+    mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
+    G.setup_lmgc(mg, "gs", red=1e-8, abslimit=1e-50, mixed=True)
+    x, lr = mg.solve_host("mgs", gen.rhs)
+    mg.close()
+    return x, lr
+
+
+@pytest.mark.gpu
+def test_alone_equals_in_the_mix(G):
+    from ug_gb300.serve import Pool
+    nref, seed = 4, 4242
+    alone = Pool(nref, 3)
+    xa, lra = alone.solve(seed, slot=0)
+    alone.close()
+    # the same request joins a pool at its third iteration, in another slot,
+    # while two others run and one more arrives later
+    mix = Pool(nref, 3)
+    got = {}
+    others = [11, 12, 13]
+    mix.free = []
+    mix.admit(0, others[0], 0.1, 1.0)
+    mix.active = {0: others[0]}
+    it = 0
+    pending = [(2, 1, seed), (4, 2, others[1])]  # (iteration, slot, seed)
+    while mix.active or pending:
+        while pending and pending[0][0] <= it:
+            _, k, s = pending.pop(0)
+            mix.admit(k, s, 0.1, 1.0)
+            mix.active[k] = s
+        mix.launch()
+        while (done := mix.poll()) is None:
+            pass
+        it += 1
+        for k in done:
+            s = mix.active.pop(k)
+            x, lr = mix.fetch(k)
+            got[s] = (x, lr)
+            if s == others[0] and others[2] not in got and 0 not in mix.active:
+                mix.admit(0, others[2], 0.1, 1.0)  # a new request reuses the freed slot
+                mix.active[0] = others[2]
+    mix.close()
+    xm, lrm = got[seed]
+    assert lrm.converged and lra.converged and lrm.iters == lra.iters
+    assert np.array_equal(xm, xa)
+    assert all(got[s][1].converged for s in others)
+    # the host-assembled problem solved alone: the fields differ by ~1e-6
+    xs, lrs = _mixed_solo(G, nref, seed, 1.0)
+    assert abs(lrs.iters - lrm.iters) <= 1 and rel(xm, xs) <= 1e-4
+
+
+@pytest.mark.gpu
+def test_server_stream(G):
+    """A short Poisson stream through the server: every request converges and
+    equals its alone solution; latencies are measured."""
+    from ug_gb300.serve import Pool, Server, poisson_stream
+    reqs = poisson_stream(18, 3000.0, levels=(1, 3), seed=9)
+    srv = Server(depths=range(1, 4), slots={1: 2, 2: 3, 3: 2})
+    st = srv.run(reqs, keep_x=True)
+    srv.close()
+    assert st.completed == 18 and st.all_converged and st.p99_ms >= st.p50_ms > 0
+    for L, n in ((1, 2), (2, 3), (3, 2)):
+        p = Pool(L, n)
+        for r in [q for q in reqs if q.nref == L][:3]:
+            xa, lra = p.solve(r.seed, slot=0)
+            assert lra.iters == r.iters and np.array_equal(xa, r.x), (L, r.rid)
+        p.close()

@@ -105,6 +105,11 @@ def lib(build_if_missing: bool = True):
         "gmg_mg_create_batched": ([P, P, I, P, P], I), "gmg_mg_num_instances": ([P], I),
         "gmg_mg_instance_info": ([P, I, P, P, P], I), "gmg_vec_upload_packed": ([P, P], I),
         "gmg_vec_download_packed": ([P, P], I), "gmg_ls_instance_result": ([P, I, P], I),
+        "gmg_pool_create": ([I, I, C.c_char_p, D, I, I, P], I), "gmg_pool_destroy": ([P], I),
+        "gmg_pool_multigrid": ([P], P), "gmg_pool_set_stream": ([P, P], I), "gmg_pool_slots": ([P, P, P, P], I),
+        "gmg_pool_admit": ([P, I, C.c_ulonglong, D, D], I), "gmg_pool_launch": ([P], I),
+        "gmg_pool_poll": ([P, P, P], I), "gmg_pool_fetch": ([P, I, P, P], I),
+        "gmg_pool_slot_matrix": ([P, I, I, P], I),
         "gmg_gen_create": ([I, I, C.c_ulonglong, D, D, P], I), "gmg_gen_levels": ([P, P, P], I),
         "gmg_gen_rhs": ([P, P, P], I), "gmg_gen_coords": ([P, I, P], I), "gmg_gen_destroy": ([P], I),
     }

@@ -20,10 +20,16 @@
 #include <cstdint>
 #include <vector>
 
+#ifdef __CUDACC__
+#define UGFX_HD __host__ __device__
+#else
+#define UGFX_HD
+#endif
+
 namespace ugfx {
 
 // splitmix64 (Steele, Lea, Flood 2014): a 64-bit mixing function.
-inline uint64_t mix64(uint64_t z) {
+UGFX_HD inline uint64_t mix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -31,15 +37,15 @@ inline uint64_t mix64(uint64_t z) {
 }
 
 // Uniform double in [0,1) from the top 53 bits.
-inline double u01(uint64_t z) { return double(z >> 11) * (1.0 / 9007199254740992.0); }
+UGFX_HD inline double u01(uint64_t z) { return double(z >> 11) * (1.0 / 9007199254740992.0); }
 
 // Key for an integer lattice point (ix,iy,iz), each < 2^20.
-inline uint64_t lattice_key(int64_t ix, int64_t iy, int64_t iz) {
+UGFX_HD inline uint64_t lattice_key(int64_t ix, int64_t iy, int64_t iz) {
   return (uint64_t(ix) << 42) ^ (uint64_t(iy) << 21) ^ uint64_t(iz);
 }
 
 // i.i.d. uniform[-1,1] value attached to (seed, key).
-inline double rhs_uniform(uint64_t seed, uint64_t key) {
+UGFX_HD inline double rhs_uniform(uint64_t seed, uint64_t key) {
   return 2.0 * u01(mix64(mix64(seed) ^ key)) - 1.0;
 }
 

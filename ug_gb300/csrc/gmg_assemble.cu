@@ -1,0 +1,288 @@
+// On-device value assembly for cached topologies: the 3D P1 diffusion
+// workload (unit cube, six Kuhn tetrahedra red-refined, the Freudenthal
+// triangulation of the cube grid; meshgen.cpp kind 1) assembled straight into
+// one instance ("slot") of a batched hierarchy whose topology was built once.
+//
+// Per level: (1) the coefficient k = exp(g) of every tetrahedron at its
+// centroid, g the random-Fourier-feature field of fields.h; (2) per matrix row
+// the sum over the (up to 24) tetrahedra at the row's node of k_e h K_p, with
+// K_p the stiffness of the unit tetrahedron of type p, written into every
+// device copy of the row (FP64 / FP32 block CSR, sliced ELLPACK, inverse
+// diagonal); boundary rows become unit Dirichlet rows.  The right-hand side is
+// the position-keyed uniform load of fields.h.
+//
+// The field's phases are evaluated exactly in 32-bit fixed point (fractions
+// of a turn): for centroid lattice coordinates c (units of h/4) the phase is
+// phi + sum_d c_d theta_d modulo one turn, with theta_d = w_d h / 4 rounded to
+// 2^-32 turn, so no large argument reaches the cosine; the cosine, the sum
+// over features and exp run in FP32.  k then agrees with the FP64 host
+// generator to ~1e-6 relative.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "fields.h"
+#include "gmg_internal.h"
+#include "gmg_serve.h"
+
+namespace gmg {
+
+namespace {
+
+constexpr int ABLK = 256;
+__constant__ double c_kref[6][16];  // stiffness of the unit Kuhn tetrahedra (h = 1, k = 1)
+__constant__ int c_perm[6][3];      // the axis order of each tetrahedron's path from (0,0,0) to (1,1,1)
+
+// the Kuhn tetrahedra of the unit cube: vertices 0, e_a, e_a + e_b, (1,1,1)
+const int kPerms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+
+// P1 stiffness grad(phi_i).grad(phi_j) * vol of one tetrahedron with vertices V
+void tet_stiffness(const double V[4][3], double *K) {
+  double J[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) J[r][c] = V[c + 1][r] - V[0][r];
+  const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  // rows of J^{-1} are the gradients of the barycentric coordinates 1..3
+  double Ji[3][3];
+  Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+  Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  double G[4][3];
+  for (int d = 0; d < 3; ++d) {
+    G[1][d] = Ji[0][d];
+    G[2][d] = Ji[1][d];
+    G[3][d] = Ji[2][d];
+    G[0][d] = -(Ji[0][d] + Ji[1][d] + Ji[2][d]);
+  }
+  const double vol = std::fabs(det) / 6.0;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) K[i * 4 + j] = vol * (G[i][0] * G[j][0] + G[i][1] * G[j][1] + G[i][2] * G[j][2]);
+}
+
+int upload_constants(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)done.size() > device && done[device]) return 0;
+  double K[6][16];
+  for (int p = 0; p < 6; ++p) {
+    double V[4][3] = {{0, 0, 0}};
+    for (int a = 1; a < 4; ++a) {
+      for (int d = 0; d < 3; ++d) V[a][d] = V[a - 1][d];
+      V[a][kPerms[p][a - 1]] += 1.0;
+    }
+    tet_stiffness(V, K[p]);
+  }
+  GMG_CUDA(cudaMemcpyToSymbol(c_kref, K, sizeof K));
+  GMG_CUDA(cudaMemcpyToSymbol(c_perm, kPerms, sizeof kPerms));
+  if ((int)done.size() <= device) done.resize(device + 1, 0);
+  done[device] = 1;
+  return 0;
+}
+
+// k of every tetrahedron of a level with Nc cells per axis (element
+// ((z Nc + y) Nc + x) 6 + p); prm[m] = (phi, theta_x, theta_y, theta_z) in
+// 2^-32 turns, theta per h/4
+__global__ void __launch_bounds__(ABLK) cube_field_kernel(int Nc, const uint4 *__restrict__ prm, int M, float amp,
+                                                          float *__restrict__ kelem) {
+  __shared__ uint4 sp[GMG_FIELD_MAX_M];
+  for (int m = threadIdx.x; m < M; m += blockDim.x) sp[m] = prm[m];
+  __syncthreads();
+  const long long ne = 6LL * Nc * Nc * Nc;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+    const int p = int(e % 6);
+    const long long cell = e / 6;
+    int c[3] = {int(cell % Nc) * 4, int((cell / Nc) % Nc) * 4, int(cell / ((long long)Nc * Nc)) * 4};
+    c[c_perm[p][0]] += 3;
+    c[c_perm[p][1]] += 2;
+    c[c_perm[p][2]] += 1;
+    float sum = 0.0f;
+    for (int m = 0; m < M; ++m) {
+      const uint32_t ph = sp[m].x + uint32_t(c[0]) * sp[m].y + uint32_t(c[1]) * sp[m].z + uint32_t(c[2]) * sp[m].w;
+      sum += cospif(__uint2float_rn(ph) * 4.656612873077392578125e-10f);  // cos(2 pi ph / 2^32)
+    }
+    kelem[e] = expf(amp * sum);
+  }
+}
+
+__device__ __forceinline__ int lattice_code(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
+
+// one slot's rows of one level
+__global__ void __launch_bounds__(ABLK) cube_assemble_kernel(
+    int nrows, const int *__restrict__ rows, const int *__restrict__ perm, int off, int N,
+    const int *__restrict__ rowptr, const int *__restrict__ col, const float *__restrict__ kelem, double h,
+    double *__restrict__ v64, float *__restrict__ v32, const int *__restrict__ c2s, double *__restrict__ sv64,
+    float *__restrict__ sv32, double *__restrict__ dinv64, float *__restrict__ dinv32) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrows) return;
+  const int i = rows[q], j = perm[i] - off;
+  const int x = j % N, y = (j / N) % N, z = j / (N * N);
+  const bool bnd = x == 0 || y == 0 || z == 0 || x == N - 1 || y == N - 1 || z == N - 1;
+  double acc[27];
+#pragma unroll
+  for (int t = 0; t < 27; ++t) acc[t] = 0.0;
+  if (!bnd) {
+    const int Nc = N - 1;
+    for (int cc = 0; cc < 8; ++cc) {
+      const int a[3] = {cc & 1, (cc >> 1) & 1, (cc >> 2) & 1};  // the node's corner in the cell
+      const long long cell = ((long long)(z - a[2]) * Nc + (y - a[1])) * Nc + (x - a[0]);
+      for (int p = 0; p < 6; ++p) {
+        // vertices relative to the cell origin: 0, e_p0, e_p0 + e_p1, (1,1,1)
+        int V[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {1, 1, 1}};
+        V[1][c_perm[p][0]] = 1;
+        V[2][c_perm[p][0]] = 1;
+        V[2][c_perm[p][1]] = 1;
+        int m = -1;
+        for (int t = 0; t < 4; ++t)
+          if (V[t][0] == a[0] && V[t][1] == a[1] && V[t][2] == a[2]) m = t;
+        if (m < 0) continue;
+        const double ke = kelem ? double(kelem[cell * 6 + p]) : 1.0;
+        for (int t = 0; t < 4; ++t)
+          acc[lattice_code(V[t][0] - a[0], V[t][1] - a[1], V[t][2] - a[2])] += ke * c_kref[p][m * 4 + t];
+      }
+    }
+  }
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    double v;
+    if (bnd) {
+      v = k == rowptr[i] ? 1.0 : 0.0;
+    } else {
+      const int jc = perm[col[k]] - off;
+      v = h * acc[lattice_code(jc % N - x, (jc / N) % N - y, jc / (N * N) - z)];
+    }
+    v64[k] = v;
+    v32[k] = float(v);
+    if (c2s) {
+      sv64[c2s[k]] = v;
+      sv32[c2s[k]] = float(v);
+    }
+    if (k == rowptr[i]) {
+      dinv64[i] = 1.0 / v;
+      dinv32[i] = float(1.0 / v);
+    }
+  }
+}
+
+// the position-keyed load on the slot's finest level; x = 0 there
+__global__ void __launch_bounds__(ABLK) cube_rhs_kernel(int nrows, const int *__restrict__ rows,
+                                                        const int *__restrict__ perm, int off, int N, uint64_t seed,
+                                                        double hd, double *__restrict__ b, double *__restrict__ x) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrows) return;
+  const int i = rows[q], j = perm[i] - off;
+  const int ix = j % N, iy = (j / N) % N, iz = j / (N * N);
+  const bool bnd = ix == 0 || iy == 0 || iz == 0 || ix == N - 1 || iy == N - 1 || iz == N - 1;
+  b[i] = bnd ? 0.0 : ugfx::rhs_uniform(seed, ugfx::lattice_key(ix, iy, iz)) * hd;
+  x[i] = 0.0;
+}
+
+// per-component norms of b over the slot's NEW_DEFECT rows (one block, fixed order)
+template <int S>
+__global__ void __launch_bounds__(ABLK) slot_norm_kernel(int nrows, const int *__restrict__ rows,
+                                                         const uint8_t *__restrict__ flags,
+                                                         const double *__restrict__ b, double *__restrict__ out) {
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int q = threadIdx.x; q < nrows; q += blockDim.x) {
+    const int i = rows[q];
+    if (!(flags[i] & F_NEWDEF)) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc[r] = fma(b[(size_t)i * S + r], b[(size_t)i * S + r], acc[r]);
+  }
+  __shared__ double sh[ABLK / 32][S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < ABLK / 32; ++w) v += sh[w][threadIdx.x];
+    out[threadIdx.x] = sqrt(v);
+  }
+}
+
+unsigned grid_of(long long n) { return unsigned((n + ABLK - 1) / ABLK); }
+
+#define ACHECK(mg)                                                                              \
+  do {                                                                                          \
+    (mg)->launches++;                                                                           \
+    cudaError_t e_ = cudaGetLastError();                                                        \
+    if (e_ != cudaSuccess) {                                                                    \
+      set_error("%s:%d kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_));         \
+      return 1;                                                                                 \
+    }                                                                                           \
+  } while (0)
+
+}  // namespace
+
+void cube_field_params(uint64_t seed, double corr, double var, int level, std::vector<uint32_t> &prm, float *amp,
+                       int *M) {
+  ugfx::LogNormalField f(seed, 3, corr, var, GMG_FIELD_MAX_M);
+  const double h = 1.0 / double(1 << level), two_pi = 6.283185307179586;
+  auto turn = [](double t) -> uint32_t {  // fraction of a turn in [0,1) -> 2^-32 units
+    t -= std::floor(t);
+    double u = std::floor(t * 4294967296.0 + 0.5);
+    return uint32_t(uint64_t(u) & 0xffffffffull);
+  };
+  prm.resize(size_t(f.M) * 4);
+  for (int m = 0; m < f.M; ++m) {
+    prm[m * 4] = turn(f.phi[m] / two_pi);
+    for (int d = 0; d < 3; ++d) prm[m * 4 + 1 + d] = turn(f.w[size_t(m) * 3 + d] * h / 4.0 / two_pi);
+  }
+  *amp = float(f.amp);
+  *M = f.M;
+}
+
+int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem) {
+  GMG_CHECK(M <= GMG_FIELD_MAX_M, "field with %d features (at most %d)", M, GMG_FIELD_MAX_M);
+  if (upload_constants(mg->device)) return 1;
+  const long long ne = 6LL * Nc * Nc * Nc;
+  const unsigned g = unsigned(std::min<long long>((ne + ABLK - 1) / ABLK, 152LL * 16));
+  cube_field_kernel<<<g, ABLK, 0, mg->stream>>>(Nc, reinterpret_cast<const uint4 *>(prm_dev), M, amp, kelem);
+  ACHECK(mg);
+  return 0;
+}
+
+int k_cube_assemble(gmg_mg *mg, const Level &L, const SlotLevel &sl, const float *kelem, double h,
+                    const int *c2s) {
+  GMG_CHECK(L.s == 1 && L.A.v32 && L.dinv32, "cube assembly: scalar level with FP32 copies expected");
+  if (upload_constants(mg->device)) return 1;
+  cube_assemble_kernel<<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(
+      sl.nrows, sl.rows, L.perm_dev, sl.off, sl.N, L.A.rowptr, L.A.col, kelem, h, L.A.v64, L.A.v32, c2s,
+      L.sell_v64, L.sell_v32, L.dinv64, L.dinv32);
+  ACHECK(mg);
+  return 0;
+}
+
+int k_cube_rhs(gmg_mg *mg, const Level &L, const SlotLevel &sl, uint64_t seed, double *b, double *x) {
+  const double h = 1.0 / double(sl.N - 1);
+  cube_rhs_kernel<<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.perm_dev, sl.off, sl.N, seed,
+                                                               h * h * h, b, x);
+  ACHECK(mg);
+  return 0;
+}
+
+int k_slot_norm(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *b, double *out) {
+  switch (L.s) {
+    case 1: slot_norm_kernel<1><<<1, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, out); break;
+    case 2: slot_norm_kernel<2><<<1, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, out); break;
+    case 3: slot_norm_kernel<3><<<1, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, out); break;
+    default: set_error("block size %d not compiled", L.s); return 1;
+  }
+  ACHECK(mg);
+  return 0;
+}
+
+}  // namespace gmg

@@ -257,6 +257,9 @@ constexpr long long BATCH_COARSE_SMEM_BUDGET = 64 * 1024;
 // packed instance vectors of a batched hierarchy <-> one top level's rows
 int k_pack_gather(gmg_mg *mg, int prec, void *dst, const double *packed, const gmg_mg::Batch::TopLevel &tl, int s);
 int k_pack_scatter(gmg_mg *mg, int prec, double *packed, const void *src, const gmg_mg::Batch::TopLevel &tl, int s);
+// the same for the m rows rows[0..m) with packed positions pack[0..m)
+int k_pack_scatter_range(gmg_mg *mg, int prec, double *packed, const void *src, const int *rows, const int *pack, int m,
+                         int s);
 // permutations between UG list order and processing order
 int k_gather(gmg_mg *mg, int prec, void *dst, const double *src_list, const int *perm, int n, int s);
 int k_scatter(gmg_mg *mg, int prec, double *dst_list, const void *src, const int *perm, int n, int s);

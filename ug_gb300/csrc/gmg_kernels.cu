@@ -1473,6 +1473,17 @@ int k_pack_scatter(gmg_mg *mg, int prec, double *packed, const void *src, const 
   return 0;
 }
 
+int k_pack_scatter_range(gmg_mg *mg, int prec, double *packed, const void *src, const int *rows, const int *pack, int m,
+                         int s) {
+  if (m == 0) return 0;
+  if (prec == GMG_PREC_FP64)
+    GMG_LAUNCH((pack_scatter_kernel<double>), grid_for(m), BLK, packed, (const double *)src, rows, pack, m, s);
+  else
+    GMG_LAUNCH((pack_scatter_kernel<float>), grid_for(m), BLK, packed, (const float *)src, rows, pack, m, s);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_gather(gmg_mg *mg, int prec, void *dst, const double *src, const int *perm, int n, int s) {
   if (n == 0) return 0;
   if (prec == GMG_PREC_FP64) GMG_LAUNCH((gather_kernel<double>), grid_for(n), BLK, (double *)dst, src, perm, n, s);

@@ -239,7 +239,9 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
     GMG_CHECK(d.rowptr[i + 1] > d.rowptr[i], "row %d has no diagonal entry", i);
     GMG_CHECK(d.col[d.rowptr[i]] == i, "row %d: first entry is not the diagonal (VSTART)", i);
   }
-  auto adj = sym_adjacency(n, d.rowptr, d.col);
+  // the symmetric adjacency is needed for a colouring or the level sets only
+  std::vector<std::vector<int>> adj;
+  if (!(order == GMG_ORDER_COLOR && colour_in)) adj = sym_adjacency(n, d.rowptr, d.col);
   H.perm.resize(n);
   std::iota(H.perm.begin(), H.perm.end(), 0);
   if (order == GMG_ORDER_COLOR && n > 0) {
@@ -633,6 +635,7 @@ int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *ins
   std::vector<std::vector<int>> off(nl, std::vector<int>(ninst, -1)), colours;
   if (opts.order == GMG_ORDER_COLOR) colours.resize(nl);
   std::vector<gmg_level_desc> desc(nl);
+  std::map<std::tuple<const void *, const void *, int>, std::vector<int>> colour_memo;
   for (int l = 0; l < nl; ++l) {
     U &d = u[l];
     int n = 0;
@@ -670,9 +673,14 @@ int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *ins
         }
       }
       if (!colours.empty()) {
-        int nc = 0;
-        std::vector<int> c = greedy_colour(e.n, sym_adjacency(e.n, e.rowptr, e.col), &nc);
-        colours[l].insert(colours[l].end(), c.begin(), c.end());
+        // instances sharing one level's arrays (a pool of one topology) share its colouring
+        auto key = std::make_tuple((const void *)e.rowptr, (const void *)e.col, e.n);
+        auto it = colour_memo.find(key);
+        if (it == colour_memo.end()) {
+          int nc = 0;
+          it = colour_memo.emplace(key, greedy_colour(e.n, sym_adjacency(e.n, e.rowptr, e.col), &nc)).first;
+        }
+        colours[l].insert(colours[l].end(), it->second.begin(), it->second.end());
       }
       n += e.n;
     }

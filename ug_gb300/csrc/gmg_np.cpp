@@ -972,10 +972,7 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   for (int i = 0; i < GMG_MAX_S; ++i) { reduction[i] = red[i]; abslimit[i] = abs_[i]; }
   GMG_CHECK(!mixed || (xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64 && mg->opts.fp32_copy),
             "ls $mixed needs FP64 x and b and a hierarchy with FP32 copies");
-  const int cprec = mixed ? GMG_PREC_FP32 : bv->prec;
-  if (!cvec || cvec->prec != cprec) cvec = temp_vec(mg, name + "__c" + std::to_string(cprec), cprec);
-  if (mixed && !b32) b32 = temp_vec(mg, name + "__b32", GMG_PREC_FP32);
-  GMG_CHECK(cvec && (!mixed || b32), "ls: temporary vectors");
+  if (prepare_temps(bv)) return 1;
   double reach[GMG_MAX_S];
   for (int i = 0; i < s; ++i) {
     lr->first_defect[i] = lr->last_defect[i];
@@ -1010,6 +1007,20 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
 // creates the numprocs' temporaries), the following ones replay one captured
 // graph of the iteration
 int NPLs::step(int i, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, gmg_lresult *lr) {
+  if (step_async(i, level, xv, bv, Am, lr)) return 1;
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  return 0;
+}
+
+int NPLs::prepare_temps(gmg_vec *bv) {
+  const int cprec = mixed ? GMG_PREC_FP32 : bv->prec;
+  if (!cvec || cvec->prec != cprec) cvec = temp_vec(mg, name + "__c" + std::to_string(cprec), cprec);
+  if (mixed && !b32) b32 = temp_vec(mg, name + "__b32", GMG_PREC_FP32);
+  GMG_CHECK(cvec && (!mixed || b32), "ls: temporary vectors");
+  return 0;
+}
+
+int NPLs::step_async(int i, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, gmg_lresult *lr) {
   int err = 0;
   const bool graph_ok = use_graph && IterNp->capturable();
   if (graph_ok && (graph || i > 0)) {
@@ -1033,7 +1044,6 @@ int NPLs::step(int i, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, gmg_lres
     lr->error_code = err;
     return 1;
   }
-  GMG_CUDA(cudaStreamSynchronize(mg->stream));
   return 0;
 }
 

@@ -186,6 +186,8 @@ struct NPLs : NPLinearSolver {
   bool is_exact_base() const;
   // iteration i of Solver's loop (graph replay after the first), synchronised
   int step(int i, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr);
+  int step_async(int i, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr);  // without the sync
+  int prepare_temps(gmg_vec *b);  // the correction (and FP32 defect) vectors of Solver
   int defect_level(int level, gmg_vec *x, gmg_vec *b);
   // batched hierarchies (gmg_mg_create_batched), solved on their deepest level
   bool batched(int level) const;

@@ -1,0 +1,35 @@
+// Internal interface of the serving pools: on-device assembly into one slot
+// of a batched hierarchy (gmg_assemble.cu), used by gmg_serve.cpp.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "gmg_internal.h"
+
+#define GMG_FIELD_MAX_M 256  // random Fourier features of the coefficient field
+
+namespace gmg {
+
+// one slot's rows on one level of a pool
+struct SlotLevel {
+  int N = 0;              // points per axis of the cube grid on this level
+  int off = 0;            // first union list position of the slot
+  int nrows = 0;          // rows of the slot (N^3)
+  const int *rows = nullptr;  // device: the slot's rows (processing order)
+};
+
+// field features of LogNormalField(seed, 3, corr, var) for a level with h =
+// 2^-level, as (phi, theta_x, theta_y, theta_z) in 2^-32 turns per h/4
+void cube_field_params(uint64_t seed, double corr, double var, int level, std::vector<uint32_t> &prm, float *amp,
+                       int *M);
+// k of every tetrahedron of a level with Nc cells per axis
+int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem);
+// the slot's rows of level L from k (kelem == nullptr: k = 1); c2s maps CSR
+// entries to sliced-ELLPACK entries (nullptr if the level has none)
+int k_cube_assemble(gmg_mg *mg, const Level &L, const SlotLevel &sl, const float *kelem, double h, const int *c2s);
+// right-hand side of the slot (finest level), x = 0 there
+int k_cube_rhs(gmg_mg *mg, const Level &L, const SlotLevel &sl, uint64_t seed, double *b, double *x);
+// per-component norms of b over the slot's NEW_DEFECT rows into out[0..s)
+int k_slot_norm(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *b, double *out);
+
+}  // namespace gmg

@@ -1,0 +1,246 @@
+"""Serving loop: continuous batching of 3D diffusion solves on resident pools.
+
+A request is (arrival time, refinement count L, seed): the unit cube's Kuhn
+tetrahedra refined L times, k = exp(g) from the seed (correlation `corr`,
+variance `var`), the seeded uniform right-hand side -- the problem
+``Generator(DIFFUSION3D, L, seed, corr, var)`` describes.  The server keeps,
+per depth L, pools of slots (gmg_pool_*: one batched hierarchy of the cached
+topology each, sized at start-up from the device's free memory), and runs one
+event loop:
+
+* arrived requests wait in a queue per depth; whenever a pool of that depth
+  is idle between two iterations and has free slots, they are admitted (their
+  matrices and right-hand side are assembled on the device in the free slot);
+* every pool with active slots launches its next ls iteration (a replayed
+  CUDA graph) on its own stream, so pools overlap on the GPU;
+* a finished iteration is polled without blocking; slots whose request met
+  its stopping test are fetched (solution to the host) and freed at once.
+
+Latency = completion time - arrival time (queueing, assembly and all
+iterations included); throughput = completed requests / makespan.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import GmgError, LResult, _err, lib
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float  # seconds after the start of the stream
+    nref: int
+    seed: int
+    start: float = -1.0
+    done: float = -1.0
+    iters: int = 0
+    converged: bool = False
+    x: np.ndarray | None = None
+
+
+def poisson_stream(count: int, rate: float, levels=(2, 7), seed: int = 5) -> list[Request]:
+    """`count` requests with exponential inter-arrival times (mean 1/rate),
+    depths uniform in levels[0]..levels[1], per-request seeds."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    L = rng.integers(levels[0], levels[1] + 1, size=count)
+    return [Request(i, float(t[i]), int(L[i]), 100000 + 7919 * i + seed) for i in range(count)]
+
+
+def cube_unknowns(nref: int) -> int:
+    return ((1 << nref) + 1) ** 3
+
+
+def slot_bytes(nref: int) -> int:
+    """Device bytes one slot of depth nref needs (matrices in FP64/FP32 block
+    CSR and sliced ELLPACK, transfer, vectors), from the cube's pattern: 15
+    entries per row (27 neighbours in the Freudenthal stencil minus 12)."""
+    total = 0
+    for l in range(nref + 1):
+        n = cube_unknowns(l)
+        nnz = 15 * n
+        total += nnz * (4 + 8 + 4) * 2 + n * (8 * 8 + 40)
+    return int(total * 1.15)
+
+
+class Pool:
+    """One gmg_pool: `nslots` slots of depth `nref`."""
+
+    def __init__(self, nref: int, nslots: int, smoother: str = "gs", red: float = 1e-8, maxit: int = 100,
+                 device: int = 0, stream=None):
+        h = C.c_void_p()
+        if lib().gmg_pool_create(nref, nslots, smoother.encode(), red, maxit, device, C.byref(h)):
+            _err("gmg_pool_create")
+        self._h = h
+        self.nref, self.nslots = nref, nslots
+        if stream is not None:
+            lib().gmg_pool_set_stream(h, stream)
+        ns, nt, fr = C.c_int(), C.c_int(), C.c_int()
+        lib().gmg_pool_slots(h, C.byref(ns), C.byref(nt), C.byref(fr))
+        self.n_top = nt.value
+        self.free = list(range(nslots))
+        self.active: dict[int, object] = {}
+        self.busy = False
+        self._done = np.zeros(nslots, np.int32)
+
+    def admit(self, slot: int, seed: int, corr: float, var: float):
+        if lib().gmg_pool_admit(self._h, slot, seed, corr, var):
+            _err("gmg_pool_admit")
+
+    def launch(self):
+        if lib().gmg_pool_launch(self._h):
+            _err("gmg_pool_launch")
+        self.busy = True
+
+    def poll(self):
+        """None while the iteration runs, else the list of finished slots."""
+        nd = C.c_int()
+        r = lib().gmg_pool_poll(self._h, C.byref(nd), self._done.ctypes.data)
+        if r < 0:
+            _err("gmg_pool_poll")
+        if r == 0:
+            return None
+        self.busy = False
+        return [int(k) for k in self._done[:nd.value]]
+
+    def fetch(self, slot: int, want_x: bool = True):
+        lr = LResult()
+        x = np.empty(self.n_top) if want_x else None
+        if lib().gmg_pool_fetch(self._h, slot, None if x is None else x.ctypes.data, C.byref(lr)):
+            _err("gmg_pool_fetch")
+        return x, lr
+
+    def slot_matrix(self, slot: int, level: int, nnz: int) -> np.ndarray:
+        v = np.empty(nnz)
+        if lib().gmg_pool_slot_matrix(self._h, slot, level, v.ctypes.data):
+            _err("gmg_pool_slot_matrix")
+        return v
+
+    def solve(self, seed: int, corr: float = 0.1, var: float = 1.0, slot: int | None = None):
+        """One request alone in this pool (blocking): (x, LResult)."""
+        slot = self.free[0] if slot is None else slot
+        self.free.remove(slot)
+        self.admit(slot, seed, corr, var)
+        while True:
+            self.launch()
+            while (done := self.poll()) is None:
+                pass
+            if slot in done:
+                x, lr = self.fetch(slot)
+                self.free.append(slot)
+                return x, lr
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gmg_pool_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def free_device_memory(device: int = 0) -> int:
+    import torch
+    return int(torch.cuda.mem_get_info(device)[0])
+
+
+@dataclass
+class ServeStats:
+    completed: int
+    makespan_s: float
+    p50_ms: float
+    p99_ms: float
+    mean_ms: float
+    throughput: float
+    iterations_mean: float
+    all_converged: bool
+    per_depth: dict = field(default_factory=dict)
+
+
+class Server:
+    """Pools per depth, sized from free device memory, and the event loop."""
+
+    def __init__(self, depths=range(2, 8), slots=None, hbm_fraction: float = 0.5, smoother: str = "gs",
+                 red: float = 1e-8, maxit: int = 100, corr: float = 0.1, var: float = 1.0, device: int = 0,
+                 max_slots: int = 8):
+        import torch
+        self.corr, self.var = corr, var
+        depths = list(depths)
+        budget = hbm_fraction * free_device_memory(device)
+        if slots is None:
+            # equal request rates per depth: give every depth the same share of
+            # the budget, at least one slot and at most max_slots
+            slots = {L: int(max(1, min(max_slots, (budget / len(depths)) // slot_bytes(L)))) for L in depths}
+        need = sum(slot_bytes(L) * n for L, n in slots.items())
+        if need > budget:
+            raise GmgError(f"pools need {need / 1e9:.1f} GB, {budget / 1e9:.1f} GB available")
+        self.streams = {L: torch.cuda.Stream(device=device) for L in depths}
+        self.pools = {L: Pool(L, slots[L], smoother, red, maxit, device, self.streams[L].cuda_stream)
+                      for L in depths}
+        self.slots = dict(slots)
+
+    def run(self, requests: list[Request], keep_x: bool = False) -> ServeStats:
+        pending = {L: [] for L in self.pools}
+        order = sorted(requests, key=lambda r: r.arrival)
+        nxt = 0
+        done_count = 0
+        t0 = time.perf_counter()
+        while done_count < len(order):
+            now = time.perf_counter() - t0
+            while nxt < len(order) and order[nxt].arrival <= now:
+                pending[order[nxt].nref].append(order[nxt])
+                nxt += 1
+            progressed = False
+            for L, pool in self.pools.items():
+                if pool.busy:
+                    fin = pool.poll()
+                    if fin is None:
+                        continue
+                    progressed = True
+                    tnow = time.perf_counter() - t0
+                    for k in fin:
+                        req = pool.active.pop(k)
+                        x, lr = pool.fetch(k, keep_x)
+                        req.done, req.iters, req.converged = tnow, lr.iters, bool(lr.converged)
+                        req.x = x
+                        pool.free.append(k)
+                        done_count += 1
+                # admissions between two iterations, then the next iteration
+                q = pending[L]
+                while q and pool.free:
+                    req = q.pop(0)
+                    k = pool.free.pop(0)
+                    pool.admit(k, req.seed, self.corr, self.var)
+                    req.start = time.perf_counter() - t0
+                    pool.active[k] = req
+                    progressed = True
+                if pool.active and not pool.busy:
+                    pool.launch()
+            if not progressed:
+                if nxt < len(order) and not any(p.busy for p in self.pools.values()):
+                    wait = order[nxt].arrival - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(min(wait, 0.002))
+        makespan = max(r.done for r in order)
+        lat = np.array([(r.done - r.arrival) * 1e3 for r in order])
+        per = {}
+        for L in self.pools:
+            ls = np.array([(r.done - r.arrival) * 1e3 for r in order if r.nref == L])
+            if ls.size:
+                per[L] = {"count": int(ls.size), "p50_ms": float(np.percentile(ls, 50)),
+                          "p99_ms": float(np.percentile(ls, 99)), "slots": self.slots[L]}
+        return ServeStats(len(order), makespan, float(np.percentile(lat, 50)), float(np.percentile(lat, 99)),
+                          float(lat.mean()), len(order) / makespan, float(np.mean([r.iters for r in order])),
+                          all(r.converged for r in order), per)
+
+    def close(self):
+        for p in self.pools.values():
+            p.close()
