@@ -166,26 +166,45 @@ class ServeStats:
 
 
 class Server:
-    """Pools per depth, sized from free device memory, and the event loop."""
+    """Pools per depth, sized from free device memory, and the event loop.
 
-    def __init__(self, depths=range(2, 8), slots=None, hbm_fraction: float = 0.5, smoother: str = "gs",
+    layout[L] = (pools, slots per pool).  Large depths get one-slot pools
+    (one instance saturates the GPU's bandwidth and a pool iterates all of
+    its slots, busy or not); small depths share few pools of many slots
+    (their cycles are latency-bound, so batching them is what pays).  Two or
+    more pools per depth let a request start while another pool of its depth
+    is mid-iteration."""
+
+    DEFAULT = {1: (2, 8), 2: (2, 8), 3: (2, 8), 4: (2, 8), 5: (2, 4), 6: (3, 1), 7: (4, 1), 8: (2, 1)}
+
+    def __init__(self, depths=range(2, 8), layout=None, hbm_fraction: float = 0.5, smoother: str = "gs",
                  red: float = 1e-8, maxit: int = 100, corr: float = 0.1, var: float = 1.0, device: int = 0,
-                 max_slots: int = 8):
+                 slots=None):
         import torch
         self.corr, self.var = corr, var
         depths = list(depths)
+        if layout is None:
+            layout = {L: ((1, slots[L]) if slots else self.DEFAULT.get(L, (2, 1))) for L in depths}
         budget = hbm_fraction * free_device_memory(device)
-        if slots is None:
-            # equal request rates per depth: give every depth the same share of
-            # the budget, at least one slot and at most max_slots
-            slots = {L: int(max(1, min(max_slots, (budget / len(depths)) // slot_bytes(L)))) for L in depths}
-        need = sum(slot_bytes(L) * n for L, n in slots.items())
+        need = sum(slot_bytes(L) * n * m for L, (n, m) in layout.items())
+        if need > budget:  # shrink the largest depths' pool counts to the budget
+            for L in sorted(layout, reverse=True):
+                while need > budget and layout[L][0] > 1:
+                    need -= slot_bytes(L) * layout[L][1]
+                    layout[L] = (layout[L][0] - 1, layout[L][1])
         if need > budget:
             raise GmgError(f"pools need {need / 1e9:.1f} GB, {budget / 1e9:.1f} GB available")
-        self.streams = {L: torch.cuda.Stream(device=device) for L in depths}
-        self.pools = {L: Pool(L, slots[L], smoother, red, maxit, device, self.streams[L].cuda_stream)
-                      for L in depths}
-        self.slots = dict(slots)
+        self.layout = dict(layout)
+        self.pools = {}
+        self.streams = []
+        for L in depths:
+            npools, nslots = layout[L]
+            self.pools[L] = []
+            for _ in range(npools):
+                st = torch.cuda.Stream(device=device)
+                self.streams.append(st)
+                self.pools[L].append(Pool(L, nslots, smoother, red, maxit, device, st.cuda_stream))
+        self.slots = {L: n * m for L, (n, m) in layout.items()}
 
     def run(self, requests: list[Request], keep_x: bool = False) -> ServeStats:
         pending = {L: [] for L in self.pools}
@@ -199,33 +218,37 @@ class Server:
                 pending[order[nxt].nref].append(order[nxt])
                 nxt += 1
             progressed = False
-            for L, pool in self.pools.items():
-                if pool.busy:
-                    fin = pool.poll()
-                    if fin is None:
-                        continue
-                    progressed = True
-                    tnow = time.perf_counter() - t0
-                    for k in fin:
-                        req = pool.active.pop(k)
-                        x, lr = pool.fetch(k, keep_x)
-                        req.done, req.iters, req.converged = tnow, lr.iters, bool(lr.converged)
-                        req.x = x
-                        pool.free.append(k)
-                        done_count += 1
-                # admissions between two iterations, then the next iteration
+            for L, pools in self.pools.items():
+                for pool in pools:
+                    if pool.busy:
+                        fin = pool.poll()
+                        if fin is None:
+                            continue
+                        progressed = True
+                        tnow = time.perf_counter() - t0
+                        for k in fin:
+                            req = pool.active.pop(k)
+                            x, lr = pool.fetch(k, keep_x)
+                            req.done, req.iters, req.converged = tnow, lr.iters, bool(lr.converged)
+                            req.x = x
+                            pool.free.append(k)
+                            done_count += 1
+                # admissions between two iterations (pools already iterating
+                # first, so requests batch), then the next iterations
                 q = pending[L]
-                while q and pool.free:
-                    req = q.pop(0)
-                    k = pool.free.pop(0)
-                    pool.admit(k, req.seed, self.corr, self.var)
-                    req.start = time.perf_counter() - t0
-                    pool.active[k] = req
-                    progressed = True
-                if pool.active and not pool.busy:
-                    pool.launch()
+                for pool in sorted(pools, key=lambda p: -len(p.active)):
+                    while q and pool.free and not pool.busy:
+                        req = q.pop(0)
+                        k = pool.free.pop(0)
+                        pool.admit(k, req.seed, self.corr, self.var)
+                        req.start = time.perf_counter() - t0
+                        pool.active[k] = req
+                        progressed = True
+                for pool in pools:
+                    if pool.active and not pool.busy:
+                        pool.launch()
             if not progressed:
-                if nxt < len(order) and not any(p.busy for p in self.pools.values()):
+                if nxt < len(order) and not any(p.busy for ps in self.pools.values() for p in ps):
                     wait = order[nxt].arrival - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(min(wait, 0.002))
@@ -236,11 +259,12 @@ class Server:
             ls = np.array([(r.done - r.arrival) * 1e3 for r in order if r.nref == L])
             if ls.size:
                 per[L] = {"count": int(ls.size), "p50_ms": float(np.percentile(ls, 50)),
-                          "p99_ms": float(np.percentile(ls, 99)), "slots": self.slots[L]}
+                          "p99_ms": float(np.percentile(ls, 99)), "pools_x_slots": list(self.layout[L])}
         return ServeStats(len(order), makespan, float(np.percentile(lat, 50)), float(np.percentile(lat, 99)),
                           float(lat.mean()), len(order) / makespan, float(np.mean([r.iters for r in order])),
                           all(r.converged for r in order), per)
 
     def close(self):
-        for p in self.pools.values():
-            p.close()
+        for ps in self.pools.values():
+            for p in ps:
+                p.close()
