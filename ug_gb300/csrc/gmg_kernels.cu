@@ -33,6 +33,51 @@ __device__ __forceinline__ void pdl_prologue() {
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
+// Kernels whose matrix structure is constant for the hierarchy's lifetime
+// load it BEFORE waiting for their predecessor (the loads overlap the
+// predecessor's tail), then wait, then let their successor launch, so only
+// the gathers of data the predecessor wrote remain on the dependent chain.
+// The successor is launched only after this kernel's wait, so at most two
+// kernels of the stream are ever resident at once.
+__device__ __forceinline__ void pdl_wait_then_trigger() { pdl_prologue(); }
+
+// entries of a row prefetched before the wait.  Only launches of at most
+// PREFETCH_MAX_BLOCKS blocks use the prefetching variants (PN > 0): those
+// are latency-bound, while on larger grids the extra registers cost more
+// occupancy than the overlap gains, and the plain streaming loop (PN = 0) is
+// faster.
+template <int S>
+struct PF {
+  static constexpr int N = S == 1 ? 16 : (S == 2 ? 7 : 4);
+};
+constexpr long long PREFETCH_MAX_BLOCKS = 1100;  // ~280k rows (measured: the 65^3 level gains, 320k+ rows lose)
+
+// a sliced-ELLPACK row i: entry k at e0 + 32 k, w entries (padding included);
+// the first PF<S>::N (column, block) pairs are held in registers
+template <class T, int S, int P_ = PF<S>::N>
+struct SellRow {
+  static constexpr int P = P_;
+  int e0, w;
+  int col[P > 0 ? P : 1];
+  T val[P > 0 ? P : 1][S * S];
+  __device__ __forceinline__ void load(int i, const int *__restrict__ sptr, const int *__restrict__ scol,
+                                       const T *__restrict__ sval) {
+    const int base = __ldg(sptr + (i >> 5));
+    w = (__ldg(sptr + (i >> 5) + 1) - base) >> 5;
+    e0 = base + (i & 31);
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      col[k] = 0;
+      if (k < w) {
+        const int e = e0 + 32 * k;
+        col[k] = __ldg(scol + e);
+#pragma unroll
+        for (int q = 0; q < S * S; ++q) val[k][q] = __ldg(sval + (size_t)e * (S * S) + q);
+      }
+    }
+  }
+};
+
 template <typename... KP, typename... A>
 inline void pdl_launch(gmg_mg *mg, void (*kern)(KP...), dim3 grid, dim3 block, A &&...args) {
   cudaLaunchConfig_t cfg = {};
@@ -48,6 +93,28 @@ inline void pdl_launch(gmg_mg *mg, void (*kern)(KP...), dim3 grid, dim3 block, A
   cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 #define GMG_LAUNCH(K, G, B, ...) pdl_launch(mg, K, dim3(G), dim3(B), __VA_ARGS__)
+
+// the CSR entries k0 + lane + TPR q (q < Q) of one row held by one lane,
+// prefetched before the wait
+template <class T, int S, int Q>
+struct CsrLane {
+  int k1, col[Q > 0 ? Q : 1];
+  T val[Q > 0 ? Q : 1][S * S];
+  __device__ __forceinline__ void load(bool valid, int k0, int k1_, int lane, int tpr, const int *__restrict__ cols,
+                                       const T *__restrict__ vals) {
+    k1 = valid ? k1_ : 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int k = k0 + lane + tpr * q;
+      col[q] = 0;
+      if (k < k1) {
+        col[q] = __ldg(cols + k);
+#pragma unroll
+        for (int e = 0; e < S * S; ++e) val[q][e] = __ldg(vals + (size_t)k * (S * S) + e);
+      }
+    }
+  }
+};
 
 template <class T>
 struct Damp {
@@ -125,30 +192,42 @@ __global__ void scale_kernel(T *x, int n, Damp<T> dm) {
 // ugblas.cc:3997: x -= A y, row sums formed before the subtraction.
 // ACC: additionally acc += y (the lmgc `dadd(c, t)` that follows every
 // smoothing step and the coarse-grid correction, iter.cc:7811-7816, 7903).
-template <class T, class TY, int S, int TPR, bool ACC>
+template <class T, class TY, int S, int TPR, bool ACC, int Q>
 __global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__restrict__ rowptr,
                                                          const int *__restrict__ col, const T *__restrict__ val,
                                                          const TY *__restrict__ y, T *__restrict__ x,
                                                          TY *__restrict__ acc) {
-  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int row = gt / TPR, lane = gt & (TPR - 1);
+  const int k0 = row < n ? __ldg(rowptr + row) : 0, k1 = row < n ? __ldg(rowptr + row + 1) : 0;
+  CsrLane<T, S, Q> E;
+  E.load(row < n, k0, k1, lane, TPR, col, val);
+  pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
-  if (row < n) {
-    const int k1 = __ldg(rowptr + row + 1);
-    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
-      const int j = __ldg(col + k);
-      const T *m = val + (size_t)k * (S * S);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    if (k0 + lane + TPR * q < E.k1) {
       T yv[S];
 #pragma unroll
-      for (int c = 0; c < S; ++c) yv[c] = T(__ldg(y + (size_t)j * S + c));
+      for (int c = 0; c < S; ++c) yv[c] = T(y[(size_t)E.col[q] * S + c]);
 #pragma unroll
       for (int r = 0; r < S; ++r)
 #pragma unroll
-        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+        for (int c = 0; c < S; ++c) s[r] = fma(E.val[q][r * S + c], yv[c], s[r]);
     }
+  }
+  for (int k = k0 + lane + TPR * Q; k < E.k1; k += TPR) {
+    const int j = __ldg(col + k);
+    const T *m = val + (size_t)k * (S * S);
+    T yv[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) yv[c] = T(y[(size_t)j * S + c]);
+#pragma unroll
+    for (int r = 0; r < S; ++r)
+#pragma unroll
+      for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
   }
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
@@ -168,27 +247,38 @@ __global__ void __launch_bounds__(BLK) spmv_minus_kernel(int n, const int *__res
 // GB300).  Padding entries are zero blocks at the row itself.  (Loading a
 // row's column indices in one predicated batch before the gathers measured
 // slower on GB300 than this plain loop, which the compiler pipelines.)
-template <class T, class TY, class TA, int S, bool ACC>
+template <class T, class TY, class TA, int S, bool ACC, int PN>
 __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__restrict__ sptr,
                                                         const int *__restrict__ scol, const T *__restrict__ sval,
                                                         const TY *__restrict__ y, T *__restrict__ x,
                                                         TA *__restrict__ acc) {
-  pdl_prologue();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int e0 = __ldg(sptr + (i >> 5));
-  const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+  SellRow<T, S, PN> R;
+  R.load(i, sptr, scol, sval);
+  pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
-  int e = e0 + (i & 31);
+#pragma unroll
+  for (int k = 0; k < PN; ++k) {
+    if (k < R.w) {
+#pragma unroll
+      for (int c = 0; c < S; ++c) {
+        const T yv = T(y[(size_t)R.col[k] * S + c]);
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = fma(R.val[k][r * S + c], yv, s[r]);
+      }
+    }
+  }
+  int e = R.e0 + 32 * PN;
 #pragma unroll 4
-  for (int k = 0; k < w; ++k, e += 32) {
+  for (int k = PN; k < R.w; ++k, e += 32) {
     const int j = __ldg(scol + e);
     const T *m = sval + (size_t)e * (S * S);
 #pragma unroll
     for (int c = 0; c < S; ++c) {
-      const T yv = T(__ldg(y + (size_t)j * S + c));
+      const T yv = T(y[(size_t)j * S + c]);
 #pragma unroll
       for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + c), yv, s[r]);
     }
@@ -203,27 +293,44 @@ __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__rest
 // Sliced-ELLPACK l_lgs wave over the contiguous rows [r0, r1) of one colour:
 // entries to rows j < i (earlier colours) are final, the diagonal (entry 0)
 // and the padding (j == i) are skipped.
-template <class T, int S, bool ALL_ACTIVE>
+template <class T, int S, bool ALL_ACTIVE, int PN>
 __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int *__restrict__ sptr,
                                                       const int *__restrict__ scol, const T *__restrict__ sval,
                                                       const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
                                                       const T *__restrict__ b, T *__restrict__ t) {
-  pdl_prologue();
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1) return;
-  if (!ALL_ACTIVE && !(flags[i] & F_ACTIVE)) {
+  const bool act = ALL_ACTIVE || (__ldg(flags + i) & F_ACTIVE);
+  SellRow<T, S, PN> R;
+  T D[S * S];
+  if (act) {
+    R.load(i, sptr, scol, sval);
+#pragma unroll
+    for (int q = 0; q < S * S; ++q) D[q] = __ldg(dinv + (size_t)i * S * S + q);
+  }
+  pdl_wait_then_trigger();
+  if (!act) {
 #pragma unroll
     for (int r = 0; r < S; ++r) t[(size_t)i * S + r] = T(0);
     return;
   }
-  const int e0 = __ldg(sptr + (i >> 5));
-  const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = b[(size_t)i * S + r];
-  int e = e0 + (i & 31) + 32;
+#pragma unroll
+  for (int k = 1; k < PN; ++k) {
+    if (k < R.w && R.col[k] < i) {
+#pragma unroll
+      for (int c = 0; c < S; ++c) {
+        const T tv = t[(size_t)R.col[k] * S + c];
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = fma(-R.val[k][r * S + c], tv, s[r]);
+      }
+    }
+  }
+  int e = R.e0 + 32 * (PN > 1 ? PN : 1);
 #pragma unroll 4
-  for (int k = 1; k < w; ++k, e += 32) {
+  for (int k = PN > 1 ? PN : 1; k < R.w; ++k, e += 32) {
     const int j = __ldg(scol + e);
     if (j >= i) continue;
     const T *m = sval + (size_t)e * (S * S);
@@ -234,7 +341,6 @@ __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int 
       for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + c), tv, s[r]);
     }
   }
-  const T *D = dinv + (size_t)i * S * S;
 #pragma unroll
   for (int r = 0; r < S; ++r) {
     T v = T(0);
@@ -300,24 +406,35 @@ __device__ __forceinline__ void jac_value(const T *__restrict__ dinv, const uint
   }
 }
 
-template <class T, int S, bool ALL_ACTIVE>
+template <class T, int S, bool ALL_ACTIVE, int PN>
 __global__ void __launch_bounds__(BLK) sell_jac_step_kernel(int n, const int *__restrict__ sptr,
                                                             const int *__restrict__ scol, const T *__restrict__ sval,
                                                             const T *__restrict__ dinv,
                                                             const uint8_t *__restrict__ flags,
                                                             const T *__restrict__ bin, T *__restrict__ bout,
                                                             T *__restrict__ c, Damp<T> dm) {
-  pdl_prologue();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int e0 = __ldg(sptr + (i >> 5));
-  const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+  SellRow<T, S, PN> R;
+  R.load(i, sptr, scol, sval);
+  pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
-  int e = e0 + (i & 31);
+#pragma unroll
+  for (int k = 0; k < PN; ++k) {
+    if (k < R.w) {
+      T tv[S];
+      jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, R.col[k], dm, tv);
+#pragma unroll
+      for (int cc = 0; cc < S; ++cc)
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = fma(R.val[k][r * S + cc], tv[cc], s[r]);
+    }
+  }
+  int e = R.e0 + 32 * PN;
 #pragma unroll 4
-  for (int k = 0; k < w; ++k, e += 32) {
+  for (int k = PN; k < R.w; ++k, e += 32) {
     const int j = __ldg(scol + e);
     const T *m = sval + (size_t)e * (S * S);
     T tv[S];
@@ -378,36 +495,48 @@ __global__ void __launch_bounds__(BLK) jac_step_kernel(int n, const int *__restr
 // ugiter.cc:412: forward solve (D+L) t = b in processing order: row i uses
 // the entries to rows j < i (VINDEX(w) < VINDEX(v)), all of which belong to
 // earlier wavefronts and are final.  Inactive rows get 0.
-template <class T, int S, int TPR, bool ALL_ACTIVE>
+template <class T, int S, int TPR, bool ALL_ACTIVE, int Q>
 __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ rows, int nrows,
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
                                                       const T *__restrict__ val, const T *__restrict__ dinv,
                                                       const uint8_t *__restrict__ flags, const T *__restrict__ b,
                                                       T *__restrict__ t) {
-  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
   const int row = valid ? __ldg(rows + idx) : 0;
-  const bool active = ALL_ACTIVE || (valid && (flags[row] & F_ACTIVE));
+  const bool active = ALL_ACTIVE || (valid && (__ldg(flags + row) & F_ACTIVE));
   const bool work = valid && active;
+  const int k0 = work ? __ldg(rowptr + row) + 1 : 0, k1 = work ? __ldg(rowptr + row + 1) : 0;
+  CsrLane<T, S, Q> E;
+  E.load(work, k0, k1, lane, TPR, col, val);
+  pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
-  if (work) {
-    const int k1 = __ldg(rowptr + row + 1);
-    for (int k = __ldg(rowptr + row) + 1 + lane; k < k1; k += TPR) {
-      const int j = __ldg(col + k);
-      if (j >= row) continue;
-      const T *m = val + (size_t)k * (S * S);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    if (k0 + lane + TPR * q < E.k1 && E.col[q] < row) {
       T yv[S];
 #pragma unroll
-      for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
+      for (int c = 0; c < S; ++c) yv[c] = t[(size_t)E.col[q] * S + c];
 #pragma unroll
       for (int r = 0; r < S; ++r)
 #pragma unroll
-        for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+        for (int c = 0; c < S; ++c) s[r] = fma(E.val[q][r * S + c], yv[c], s[r]);
     }
+  }
+  for (int k = k0 + lane + TPR * Q; k < E.k1; k += TPR) {
+    const int j = __ldg(col + k);
+    if (j >= row) continue;
+    const T *m = val + (size_t)k * (S * S);
+    T yv[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
+#pragma unroll
+    for (int r = 0; r < S; ++r)
+#pragma unroll
+      for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
   }
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
@@ -518,24 +647,42 @@ __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ ro
 // transgrid.cc:117-232 as a gather over R = P^T: coarse rows with VNCLASS >= 2
 // start from 0, the others keep their value; each contribution is
 // weight * (damp * fine defect); components set in the coarse VECSKIP get none.
-template <class T, int S>
+template <class T, int S, int PN>
 __global__ void restrict_kernel(int nc, const int *__restrict__ rrow, const int *__restrict__ rcol,
                                 const T *__restrict__ rw, const uint8_t *__restrict__ cflags,
                                 const uint8_t *__restrict__ cskip, const T *__restrict__ from, T *__restrict__ to,
                                 Damp<T> dm, T *__restrict__ zero) {
-  pdl_prologue();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
+  // the row of R (constant) before the wait
+  constexpr int P = PN > 0 ? PN : 1;
+  const int k0 = __ldg(rrow + c), k1 = __ldg(rrow + c + 1);
+  int fc[P];
+  T fw[P];
+#pragma unroll
+  for (int q = 0; q < PN; ++q) {
+    fc[q] = 0;
+    fw[q] = T(0);
+    if (k0 + q < k1) {
+      fc[q] = __ldg(rcol + k0 + q);
+      fw[q] = __ldg(rw + k0 + q);
+    }
+  }
+  const bool reset = __ldg(cflags + c) & F_RESET;
+  const int sk = __ldg(cskip + c);
+  pdl_wait_then_trigger();
   if (zero)  // lmgc's dset(c_{l-1}, 0), iter.cc:7873, in the same pass
 #pragma unroll
     for (int r = 0; r < S; ++r) zero[(size_t)c * S + r] = T(0);
-  const bool reset = cflags[c] & F_RESET;
-  const int sk = cskip[c];
   T acc[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = reset ? T(0) : to[(size_t)c * S + r];
-  const int k1 = __ldg(rrow + c + 1);
-  for (int k = __ldg(rrow + c); k < k1; ++k) {
+#pragma unroll
+  for (int q = 0; q < PN; ++q)
+    if (k0 + q < k1)
+#pragma unroll
+      for (int r = 0; r < S; ++r) acc[r] = fma(fw[q], dm.d[r] * from[(size_t)fc[q] * S + r], acc[r]);
+  for (int k = k0 + PN; k < k1; ++k) {
     const int f = __ldg(rcol + k);
     const T w = __ldg(rw + k);
 #pragma unroll
@@ -549,20 +696,38 @@ __global__ void restrict_kernel(int nc, const int *__restrict__ rrow, const int 
 // ------------------------------------------------------------ StandardInterpolateCorrection
 // transgrid.cc:235-347: t_f = sum_i (weight_i * damp) * c_i in every component
 // the fine VECSKIP leaves free; rows skipped in all components stay 0.
-template <class T, int S, bool ACC>
+template <class T, int S, bool ACC, int PN>
 __global__ void interp_kernel(int nf, const int *__restrict__ prow, const int *__restrict__ pcol,
                               const T *__restrict__ pw, const uint8_t *__restrict__ fskip,
                               const T *__restrict__ from, T *__restrict__ to, Damp<T> dm, T *__restrict__ acc) {
-  pdl_prologue();
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
-  const int sk = fskip[f];
+  // the row of P (constant) before the wait
+  constexpr int P = PN > 0 ? PN : 1;
+  const int sk = __ldg(fskip + f);
+  const int k0 = __ldg(prow + f), k1 = __ldg(prow + f + 1);
+  int cc[P];
+  T cw[P];
+#pragma unroll
+  for (int q = 0; q < PN; ++q) {
+    cc[q] = 0;
+    cw[q] = T(0);
+    if (k0 + q < k1) {
+      cc[q] = __ldg(pcol + k0 + q);
+      cw[q] = __ldg(pw + k0 + q);
+    }
+  }
+  pdl_wait_then_trigger();
   T v[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) v[r] = T(0);
   if (sk != (1 << S) - 1) {
-    const int k1 = __ldg(prow + f + 1);
-    for (int k = __ldg(prow + f); k < k1; ++k) {
+#pragma unroll
+    for (int q = 0; q < PN; ++q)
+      if (k0 + q < k1)
+#pragma unroll
+        for (int r = 0; r < S; ++r) v[r] = fma(cw[q] * dm.d[r], from[(size_t)cc[q] * S + r], v[r]);
+    for (int k = k0 + PN; k < k1; ++k) {
       const int c = __ldg(pcol + k);
       const T w = __ldg(pw + k);
 #pragma unroll
@@ -1001,8 +1166,12 @@ int spmv_dispatch_tpr(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *
   switch (L.tpr) {
 #define CASE(TP)                                                                                           \
   case TP:                                                                                                 \
-    GMG_LAUNCH((spmv_minus_kernel<T, TY, S, TP, ACC>), grid_for((long long)n * TP), BLK, n, L.A.rowptr, \
-                                                                                           L.A.col, val, y, x, acc); \
+    if (grid_for((long long)n * TP) <= PREFETCH_MAX_BLOCKS)                                                \
+      GMG_LAUNCH((spmv_minus_kernel<T, TY, S, TP, ACC, 4>), grid_for((long long)n * TP), BLK, n, L.A.rowptr, \
+                 L.A.col, val, y, x, acc);                                                                 \
+    else                                                                                                   \
+      GMG_LAUNCH((spmv_minus_kernel<T, TY, S, TP, ACC, 0>), grid_for((long long)n * TP), BLK, n, L.A.rowptr, \
+                 L.A.col, val, y, x, acc);                                                                 \
     break;
     CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32)
 #undef CASE
@@ -1023,12 +1192,21 @@ template <class T, class TY, bool ACC>
 int spmv_dispatch(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, TY *acc) {
   if (L.sell && sell_val<T>(L)) {
     const T *sv = sell_val<T>(L);
+    const bool pre = grid_for(L.n) <= PREFETCH_MAX_BLOCKS;
+#define SK(SS)                                                                                                   \
+  if (pre)                                                                                                       \
+    GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, SS, ACC, PF<SS>::N>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, \
+               sv, y, x, acc);                                                                                   \
+  else                                                                                                           \
+    GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, SS, ACC, 0>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, \
+               x, acc);
     switch (L.s) {
-      case 1: GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, 1, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
-      case 2: GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, 2, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
-      case 3: GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, 3, ACC>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, x, acc); break;
+      case 1: SK(1) break;
+      case 2: SK(2) break;
+      case 3: SK(3) break;
       default: set_error("block size %d not compiled", L.s); return 1;
     }
+#undef SK
     LAUNCH_CHECK(mg);
     return 0;
   }
@@ -1065,12 +1243,20 @@ int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
   for (int w = 0; w < L.lower.nwave(); ++w) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
     if (nr <= 0) continue;
-    if (L.all_active)
-      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, true>), grid_for((long long)nr * TPR), BLK, 
-          L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv, L.flags, b, t);
+    const unsigned g = grid_for((long long)nr * TPR);
+    const bool pre = g <= PREFETCH_MAX_BLOCKS;
+    if (L.all_active && pre)
+      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, true, 4>), g, BLK, L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv,
+                 L.flags, b, t);
+    else if (L.all_active)
+      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, true, 0>), g, BLK, L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv,
+                 L.flags, b, t);
+    else if (pre)
+      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, false, 4>), g, BLK, L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val,
+                 dinv, L.flags, b, t);
     else
-      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, false>), grid_for((long long)nr * TPR), BLK, 
-          L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv, L.flags, b, t);
+      GMG_LAUNCH((gs_wave_kernel<T, S, TPR, false, 0>), g, BLK, L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val,
+                 dinv, L.flags, b, t);
     LAUNCH_CHECK(mg);
   }
   return 0;
@@ -1228,12 +1414,21 @@ int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const floa
     if (k_add_mixed(mg, x, GMG_PREC_FP32, c, (long long)L.n * L.s)) return 1;
     return k_matmul_minus_mixed(mg, L, b, GMG_PREC_FP32, c);
   }
+  const bool pre = grid_for(L.n) <= PREFETCH_MAX_BLOCKS;
+#define RU(SS)                                                                                                   \
+  if (pre)                                                                                                       \
+    GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, PF<SS>::N>), grid_for(L.n), BLK, L.n,          \
+               L.sell_ptr, L.sell_col, L.sell_v64, c, b, x);                                                     \
+  else                                                                                                           \
+    GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, 0>), grid_for(L.n), BLK, L.n, L.sell_ptr,      \
+               L.sell_col, L.sell_v64, c, b, x);
   switch (L.s) {
-    case 1: GMG_LAUNCH((sell_spmv_kernel<double, float, double, 1, true>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, L.sell_v64, c, b, x); break;
-    case 2: GMG_LAUNCH((sell_spmv_kernel<double, float, double, 2, true>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, L.sell_v64, c, b, x); break;
-    case 3: GMG_LAUNCH((sell_spmv_kernel<double, float, double, 3, true>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, L.sell_v64, c, b, x); break;
+    case 1: RU(1) break;
+    case 2: RU(2) break;
+    case 3: RU(3) break;
     default: set_error("block size %d not compiled", L.s); return 1;
   }
+#undef RU
   LAUNCH_CHECK(mg);
   return 0;
 }
@@ -1260,8 +1455,12 @@ template <class T, int S, bool ALL>
 int jac_step_dispatch(gmg_mg *mg, const Level &L, T *bout, const T *bin, T *c, Damp<T> dm) {
   const T *dinv = dinv_of<T>(L);
   if (L.sell && sell_val<T>(L)) {
-    GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sell_val<T>(L),
-               dinv, L.flags, bin, bout, c, dm);
+    if (grid_for(L.n) <= PREFETCH_MAX_BLOCKS)
+      GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, PF<S>::N>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,
+                 sell_val<T>(L), dinv, L.flags, bin, bout, c, dm);
+    else
+      GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, 0>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,
+                 sell_val<T>(L), dinv, L.flags, bin, bout, c, dm);
     LAUNCH_CHECK(mg);
     return 0;
   }
@@ -1308,12 +1507,18 @@ int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
   for (int w = 0; w < L.lower.nwave(); ++w) {
     const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
     if (r1 <= r0) continue;
-    if (L.all_active)
-      GMG_LAUNCH((sell_gs_kernel<T, S, true>), grid_for(r1 - r0), BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv,
-                 L.flags, b, t);
+    const unsigned g = grid_for(r1 - r0);
+    const bool pre = g <= PREFETCH_MAX_BLOCKS;
+    if (L.all_active && pre)
+      GMG_LAUNCH((sell_gs_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags,
+                 b, t);
+    else if (L.all_active)
+      GMG_LAUNCH((sell_gs_kernel<T, S, true, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags, b, t);
+    else if (pre)
+      GMG_LAUNCH((sell_gs_kernel<T, S, false, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags,
+                 b, t);
     else
-      GMG_LAUNCH((sell_gs_kernel<T, S, false>), grid_for(r1 - r0), BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv,
-                 L.flags, b, t);
+      GMG_LAUNCH((sell_gs_kernel<T, S, false, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags, b, t);
     LAUNCH_CHECK(mg);
   }
   return 0;
@@ -1368,10 +1573,16 @@ int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
 int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp,
                void *zero_coarse) {
   if (C.n == 0) return 0;
-#define RK(TT, SS)                                                                                            \
-  GMG_LAUNCH((restrict_kernel<TT, SS>), grid_for(C.n), BLK, C.n, F.R.rowptr, F.R.col, mval<TT>(F.R), C.flags, \
-                                                                 C.skip, (const TT *)from, (TT *)to,            \
-                                                                 make_damp<TT>(damp, SS), (TT *)zero_coarse)
+  const bool pre = grid_for(C.n) <= PREFETCH_MAX_BLOCKS;
+#define RK(TT, SS)                                                                                                 \
+  do {                                                                                                             \
+    if (pre)                                                                                                       \
+      GMG_LAUNCH((restrict_kernel<TT, SS, 16>), grid_for(C.n), BLK, C.n, F.R.rowptr, F.R.col, mval<TT>(F.R),     \
+                 C.flags, C.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS), (TT *)zero_coarse);         \
+    else                                                                                                           \
+      GMG_LAUNCH((restrict_kernel<TT, SS, 0>), grid_for(C.n), BLK, C.n, F.R.rowptr, F.R.col, mval<TT>(F.R),      \
+                 C.flags, C.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS), (TT *)zero_coarse);         \
+  } while (0)
 #define RS(TT)                                  \
   if (F.s == 1) RK(TT, 1);                      \
   else if (F.s == 2) RK(TT, 2);                 \
@@ -1387,10 +1598,16 @@ int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, c
 
 int k_interpolate(gmg_mg *mg, const Level &F, int prec, void *to, const void *from, const double *damp, void *acc) {
   if (F.n == 0) return 0;
+  const bool pre = grid_for(F.n) <= PREFETCH_MAX_BLOCKS;
 #define IK(TT, SS, A)                                                                                              \
-  GMG_LAUNCH((interp_kernel<TT, SS, A>), grid_for(F.n), BLK, F.n, F.P.rowptr, F.P.col, mval<TT>(F.P), F.skip, \
-                                                                  (const TT *)from, (TT *)to,                        \
-                                                                  make_damp<TT>(damp, SS), (TT *)acc)
+  do {                                                                                                             \
+    if (pre)                                                                                                       \
+      GMG_LAUNCH((interp_kernel<TT, SS, A, 4>), grid_for(F.n), BLK, F.n, F.P.rowptr, F.P.col, mval<TT>(F.P),      \
+                 F.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS), (TT *)acc);                          \
+    else                                                                                                           \
+      GMG_LAUNCH((interp_kernel<TT, SS, A, 0>), grid_for(F.n), BLK, F.n, F.P.rowptr, F.P.col, mval<TT>(F.P),      \
+                 F.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS), (TT *)acc);                          \
+  } while (0)
 #define IS(TT)                                                                \
   if (F.s == 1) { if (acc) IK(TT, 1, true); else IK(TT, 1, false); }         \
   else if (F.s == 2) { if (acc) IK(TT, 2, true); else IK(TT, 2, false); }    \
