@@ -9,6 +9,8 @@ individual launch in the profiler's launch list.
 
 With --batched N: N instances of the batched workload (2D Q1 Poisson,
 levels 3..7, Jacobi V(2,2)) in one batched hierarchy instead.
+With --spmv: only the finest level's dmatmul_minus in FP32 (the bench's
+roofline kernel), --cycles times.
 """
 import argparse
 
@@ -24,7 +26,18 @@ def main():
     ap.add_argument("--batched", type=int, default=0)
     ap.add_argument("--order", default="color", choices=["color", "list"])
     ap.add_argument("--bsmem", type=int, default=None)
+    ap.add_argument("--spmv", action="store_true")
     a = ap.parse_args()
+    if a.spmv:
+        gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
+        mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
+        mg.createvector("x32", "y32", prec=G.FP32)
+        for _ in range(a.cycles):
+            mg.dmatmul_minus(mg.top, "x32", "y32")
+        mg.sync()
+        print(f"{a.cycles} launches of dmatmul_minus on {mg.size(mg.top)}")
+        mg.close()
+        return
     if a.batched:
         from ug_gb300.workloads import batch_instances
         gens, _ = batch_instances(a.batched)
