@@ -182,13 +182,18 @@ struct gmg_mg {
       // rows of instance ids[k] (ascending processing order), and pack_dev[q]
       // is row q's position in the packed host layout
       int *ids_dev = nullptr, *ptr_dev = nullptr, *rows_dev = nullptr, *pack_dev = nullptr;
-      // chunks of at most BATCH_CHUNK rows of one instance: chunk h is rows
-      // chunk_q[h]..chunk_q[h+1] of instance chunk_k[h]; instance k owns chunks
-      // inst_cptr[k]..inst_cptr[k+1]; partial sums and per-instance tickets
-      int *chunk_k_dev = nullptr, *chunk_q_dev = nullptr, *inst_cptr_dev = nullptr, *ticket_dev = nullptr;
-      double *partial_dev = nullptr;
+      // chunks of at most BATCH_CHUNK rows of one instance (host): chunk h is
+      // rows chunk_q[h]..chunk_q[h+1] of instance ids[chunk_k[h]]
+      std::vector<int> chunk_k, chunk_q;
     };
     std::vector<TopLevel> tops;
+    // all top levels' chunks in one table (one launch per ls step): chunk h
+    // is rows chunk_q0[h]..chunk_q1[h] of tops[chunk_top[h]]'s lists, of
+    // instance chunk_id[h]; instance k owns chunks inst_c0[k]..inst_c1[k]
+    int nchunks_all = 0;
+    int *chunk_top_dev = nullptr, *chunk_id_dev = nullptr, *chunk_q0_dev = nullptr, *chunk_q1_dev = nullptr;
+    int *inst_c0_dev = nullptr, *inst_c1_dev = nullptr, *ticket_dev = nullptr;
+    double *partial_dev = nullptr;
     uint8_t *conv_dev = nullptr;             // converged flag per instance
     uint8_t *conv_host = nullptr;            // pinned mirror
     double *norms_dev = nullptr, *norms_host = nullptr;  // ninst * GMG_MAX_S
@@ -200,6 +205,7 @@ namespace gmg {
 
 constexpr int REDUCE_BLOCKS = 304;  // 2 x 152 SMs
 constexpr int BATCH_CHUNK = 256;    // rows per block of the batched ls update (one per thread)
+#define GMG_MAX_TOPS 16             // distinct instance depths of a batched hierarchy
 
 // ---------------------------------------------------------------- kernels (gmg_kernels.cu)
 // All launchers enqueue on `st`, count launches in mg->launches, return 0 / 1.
@@ -237,12 +243,15 @@ int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void 
 int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x);
 // base level: if |b| >= abslimit in some component: t = Ainv b; b -= A t; c += t
 int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit);
-// batched ls, the end of an iteration on one top level, over the rows of the
-// instances whose finest level it is: if spmv, b -= A c (FP64 matrix); x += c
-// unless the instance has converged (c != null); per-component norms of b
-// into batch.norms_dev[id*GMG_MAX_S + r]
-int k_batch_finish(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, void *b, double *x, int cprec,
-                   const void *c, bool spmv, int s);
+// batched ls, the end of an iteration over every instance's rows on its own
+// finest level (all top levels, one launch): if spmv, b -= A c (FP64
+// matrix); x += c unless the instance has converged (c != null); the
+// per-component norms of b into batch.norms_dev[id*GMG_MAX_S + r]
+int k_batch_finish(gmg_mg *mg, int bprec, gmg_vec *b, gmg_vec *x, int cprec, gmg_vec *c, bool spmv, int s);
+// on every top level: b32 = b64 and c32 = 0 (one launch)
+int k_batch_refine_prepare(gmg_mg *mg, gmg_vec *b32, gmg_vec *c32, gmg_vec *b64);
+// on every top level: c64 = c32 (one launch)
+int k_batch_widen(gmg_mg *mg, gmg_vec *c64, gmg_vec *c32);
 // the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
 struct CoarseCfg {
   int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;

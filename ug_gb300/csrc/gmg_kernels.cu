@@ -853,8 +853,8 @@ __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, doub
 }
 
 // ------------------------------------------------------------ batched ls
-// The end of one ls iteration on one top level of a batched hierarchy, over
-// the rows of the instances whose finest level it is (no other rows):
+// The end of one ls iteration of a batched hierarchy, over the rows of every
+// instance on its own finest level (all top levels in one launch):
 //   SPMV (mixed precision):  b -= A c with the FP64 matrix (refinement defect);
 //   LSUpdate:                x += c, unless the instance has converged (its x
 //                            then stays that of its converged iteration);
@@ -863,23 +863,39 @@ __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, doub
 // sums go to partial[], and the instance's last block to finish (a ticket
 // per instance, reset by that block) adds them in chunk order, so the norms
 // are deterministic.  c == nullptr: norms only.
+struct FinishTop {
+  const int *rows;
+  const uint8_t *flags;
+  const int *sptr, *scol;  // sliced ELLPACK (sptr == nullptr: block CSR below)
+  const double *sval;
+  const int *rowptr, *col;
+  const double *val;
+  void *b;
+  double *x;
+  const void *c;
+};
+struct FinishArgs {
+  FinishTop t[GMG_MAX_TOPS];
+};
+
 template <class TB, class TC, int S, bool SPMV>
 __global__ void __launch_bounds__(BLK) batch_finish_kernel(
-    const int *__restrict__ chunk_k, const int *__restrict__ chunk_q, const int *__restrict__ inst_cptr,
-    const int *__restrict__ ids, const int *__restrict__ rows, const uint8_t *__restrict__ flags,
-    const uint8_t *__restrict__ conv, const int *__restrict__ sptr, const int *__restrict__ scol,
-    const double *__restrict__ sval, const int *__restrict__ rowptr, const int *__restrict__ col,
-    const double *__restrict__ val, TB *__restrict__ b, double *__restrict__ x, const TC *__restrict__ c,
-    double *__restrict__ partial, int *__restrict__ ticket, double *__restrict__ norms) {
+    const __grid_constant__ FinishArgs A, const int *__restrict__ chunk_top, const int *__restrict__ chunk_id,
+    const int *__restrict__ chunk_q0, const int *__restrict__ chunk_q1, const int *__restrict__ inst_c0,
+    const int *__restrict__ inst_c1, const uint8_t *__restrict__ conv, double *__restrict__ partial,
+    int *__restrict__ ticket, double *__restrict__ norms) {
   pdl_prologue();
-  const int ch = blockIdx.x, k = chunk_k[ch], q0 = chunk_q[ch], q1 = chunk_q[ch + 1];
-  const int id = ids[k];
+  const int ch = blockIdx.x, id = chunk_id[ch], q0 = chunk_q0[ch], q1 = chunk_q1[ch];
+  const FinishTop &T = A.t[chunk_top[ch]];
+  TB *__restrict__ b = (TB *)T.b;
+  const TC *__restrict__ c = (const TC *)T.c;
+  double *__restrict__ x = T.x;
   const bool upd = c != nullptr && !conv[id];
   double acc[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = 0.0;
   for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-    const int i = rows[q];
+    const int i = T.rows[q];
     TB bi[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) bi[r] = b[(size_t)i * S + r];
@@ -887,28 +903,28 @@ __global__ void __launch_bounds__(BLK) batch_finish_kernel(
       double s[S];
 #pragma unroll
       for (int r = 0; r < S; ++r) s[r] = 0.0;
-      if (sptr) {  // sliced ELLPACK row i: entries sptr[i/32] + 32 k + i%32
-        const int e0 = __ldg(sptr + (i >> 5));
-        const int w = (__ldg(sptr + (i >> 5) + 1) - e0) >> 5;
+      if (T.sptr) {  // sliced ELLPACK row i: entries sptr[i/32] + 32 k + i%32
+        const int e0 = __ldg(T.sptr + (i >> 5));
+        const int w = (__ldg(T.sptr + (i >> 5) + 1) - e0) >> 5;
         int e = e0 + (i & 31);
 #pragma unroll 4
         for (int kk = 0; kk < w; ++kk, e += 32) {
-          const int j = __ldg(scol + e);
-          const double *m = sval + (size_t)e * (S * S);
+          const int j = __ldg(T.scol + e);
+          const double *m = T.sval + (size_t)e * (S * S);
 #pragma unroll
           for (int cc = 0; cc < S; ++cc) {
-            const double yv = double(__ldg(c + (size_t)j * S + cc));
+            const double yv = double(c[(size_t)j * S + cc]);
 #pragma unroll
             for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + cc), yv, s[r]);
           }
         }
       } else {
-        for (int kk = __ldg(rowptr + i); kk < __ldg(rowptr + i + 1); ++kk) {
-          const int j = __ldg(col + kk);
-          const double *m = val + (size_t)kk * (S * S);
+        for (int kk = __ldg(T.rowptr + i); kk < __ldg(T.rowptr + i + 1); ++kk) {
+          const int j = __ldg(T.col + kk);
+          const double *m = T.val + (size_t)kk * (S * S);
 #pragma unroll
           for (int cc = 0; cc < S; ++cc) {
-            const double yv = double(__ldg(c + (size_t)j * S + cc));
+            const double yv = double(c[(size_t)j * S + cc]);
 #pragma unroll
             for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + cc), yv, s[r]);
           }
@@ -923,7 +939,7 @@ __global__ void __launch_bounds__(BLK) batch_finish_kernel(
     if (upd)
 #pragma unroll
       for (int r = 0; r < S; ++r) x[(size_t)i * S + r] += double(c[(size_t)i * S + r]);
-    if (flags[i] & F_NEWDEF)
+    if (T.flags[i] & F_NEWDEF)
 #pragma unroll
       for (int r = 0; r < S; ++r) {
         const double v = double(bi[r]);
@@ -946,10 +962,7 @@ __global__ void __launch_bounds__(BLK) batch_finish_kernel(
     __threadfence();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const int n = inst_cptr[k + 1] - inst_cptr[k];
-    last = atomicAdd(ticket + k, 1) == n - 1;
-  }
+  if (threadIdx.x == 0) last = atomicAdd(ticket + id, 1) == inst_c1[id] - inst_c0[id] - 1;
   __syncthreads();
   if (!last) return;
   __threadfence();
@@ -957,7 +970,7 @@ __global__ void __launch_bounds__(BLK) batch_finish_kernel(
   // then a fixed-shape block reduction (deterministic for a given chunking)
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = 0.0;
-  for (int q = inst_cptr[k] + threadIdx.x; q < inst_cptr[k + 1]; q += blockDim.x)
+  for (int q = inst_c0[id] + threadIdx.x; q < inst_c1[id]; q += blockDim.x)
 #pragma unroll
     for (int r = 0; r < S; ++r) acc[r] += __ldcg(partial + (size_t)q * S + r);
   __syncthreads();  // sh is reused
@@ -973,7 +986,45 @@ __global__ void __launch_bounds__(BLK) batch_finish_kernel(
     for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
     norms[(size_t)id * GMG_MAX_S + threadIdx.x] = sqrt(v);
   }
-  if (threadIdx.x == 0) ticket[k] = 0;
+  if (threadIdx.x == 0) ticket[id] = 0;
+}
+
+// element-wise passes over the top levels of a batched hierarchy in one launch
+struct Segs {
+  void *dst[GMG_MAX_TOPS];
+  const void *src[GMG_MAX_TOPS];
+  void *aux[GMG_MAX_TOPS];
+  long long off[GMG_MAX_TOPS + 1];
+  int n;
+};
+
+__device__ __forceinline__ int seg_of(const Segs &sg, long long g) {
+  int t = 0;
+  while (t + 1 < sg.n && g >= sg.off[t + 1]) ++t;
+  return t;
+}
+
+// mixed-precision iteration start: b32 = b64 (dst <- src), c32 = 0 (aux)
+__global__ void refine_prepare_multi_kernel(const __grid_constant__ Segs sg) {
+  pdl_prologue();
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < sg.off[sg.n];
+       g += (long long)gridDim.x * blockDim.x) {
+    const int t = seg_of(sg, g);
+    const long long i = g - sg.off[t];
+    ((float *)sg.dst[t])[i] = float(((const double *)sg.src[t])[i]);
+    ((float *)sg.aux[t])[i] = 0.0f;
+  }
+}
+
+// c64 = c32
+__global__ void widen_multi_kernel(const __grid_constant__ Segs sg) {
+  pdl_prologue();
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < sg.off[sg.n];
+       g += (long long)gridDim.x * blockDim.x) {
+    const int t = seg_of(sg, g);
+    const long long i = g - sg.off[t];
+    ((double *)sg.dst[t])[i] = double(((const float *)sg.src[t])[i]);
+  }
 }
 
 // ------------------------------------------------------------ base solver
@@ -1348,17 +1399,33 @@ int k_convert(gmg_mg *mg, int dp, void *dst, int sp, const void *src, long long 
   return 0;
 }
 
-int k_batch_finish(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, void *b, double *x, int cprec,
-                   const void *c, bool spmv, int s) {
-  if (tl.nchunks == 0) return 0;
+int k_batch_finish(gmg_mg *mg, int bprec, gmg_vec *b, gmg_vec *x, int cprec, gmg_vec *c, bool spmv, int s) {
   const auto &B = mg->batch;
-  const Level &L = mg->lev[tl.level];
+  if (B.nchunks_all == 0) return 0;
   GMG_CHECK(!spmv || (bprec == GMG_PREC_FP64 && c), "batched refinement update needs an FP64 defect and c");
+  GMG_CHECK((int)B.tops.size() <= GMG_MAX_TOPS, "batched hierarchy with %zu top levels (at most %d)", B.tops.size(),
+            GMG_MAX_TOPS);
+  FinishArgs A{};
+  for (size_t t = 0; t < B.tops.size(); ++t) {
+    const int l = B.tops[t].level;
+    const Level &L = mg->lev[l];
+    FinishTop &T = A.t[t];
+    T.rows = B.tops[t].rows_dev;
+    T.flags = L.flags;
+    T.sptr = L.sell ? L.sell_ptr : nullptr;
+    T.scol = L.sell_col;
+    T.sval = L.sell_v64;
+    T.rowptr = L.A.rowptr;
+    T.col = L.A.col;
+    T.val = L.A.v64;
+    T.b = b->lev[l];
+    T.x = x ? (double *)x->lev[l] : nullptr;
+    T.c = c ? c->lev[l] : nullptr;
+  }
 #define BF(TB, TC, SS, SP)                                                                                        \
-  GMG_LAUNCH((batch_finish_kernel<TB, TC, SS, SP>), tl.nchunks, BLK, tl.chunk_k_dev, tl.chunk_q_dev,              \
-             tl.inst_cptr_dev, tl.ids_dev, tl.rows_dev, L.flags, B.conv_dev, L.sell ? L.sell_ptr : nullptr,       \
-             L.sell_col, L.sell_v64, L.A.rowptr, L.A.col, L.A.v64, (TB *)b, x, (const TC *)c, tl.partial_dev,     \
-             tl.ticket_dev, B.norms_dev)
+  GMG_LAUNCH((batch_finish_kernel<TB, TC, SS, SP>), B.nchunks_all, BLK, A, B.chunk_top_dev, B.chunk_id_dev,       \
+             B.chunk_q0_dev, B.chunk_q1_dev, B.inst_c0_dev, B.inst_c1_dev, B.conv_dev, B.partial_dev,             \
+             B.ticket_dev, B.norms_dev)
 #define BS(TB, TC, SP)                         \
   if (s == 1) BF(TB, TC, 1, SP);               \
   else if (s == 2) BF(TB, TC, 2, SP);          \
@@ -1373,6 +1440,48 @@ int k_batch_finish(gmg_mg *mg, const gmg_mg::Batch::TopLevel &tl, int bprec, voi
   }
 #undef BS
 #undef BF
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+static int top_segs(gmg_mg *mg, Segs &sg) {
+  const auto &B = mg->batch;
+  GMG_CHECK((int)B.tops.size() <= GMG_MAX_TOPS, "batched hierarchy with %zu top levels (at most %d)", B.tops.size(),
+            GMG_MAX_TOPS);
+  sg.n = int(B.tops.size());
+  sg.off[0] = 0;
+  for (int t = 0; t < sg.n; ++t) {
+    const Level &L = mg->lev[B.tops[t].level];
+    sg.off[t + 1] = sg.off[t] + (long long)L.n * L.s;
+  }
+  return 0;
+}
+
+int k_batch_refine_prepare(gmg_mg *mg, gmg_vec *b32, gmg_vec *c32, gmg_vec *b64) {
+  Segs sg{};
+  if (top_segs(mg, sg)) return 1;
+  for (int t = 0; t < sg.n; ++t) {
+    const int l = mg->batch.tops[t].level;
+    sg.dst[t] = b32->lev[l];
+    sg.src[t] = b64->lev[l];
+    sg.aux[t] = c32->lev[l];
+  }
+  if (sg.off[sg.n] == 0) return 0;
+  GMG_LAUNCH(refine_prepare_multi_kernel, vec_grid(sg.off[sg.n]), BLK, sg);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_batch_widen(gmg_mg *mg, gmg_vec *c64, gmg_vec *c32) {
+  Segs sg{};
+  if (top_segs(mg, sg)) return 1;
+  for (int t = 0; t < sg.n; ++t) {
+    const int l = mg->batch.tops[t].level;
+    sg.dst[t] = c64->lev[l];
+    sg.src[t] = c32->lev[l];
+  }
+  if (sg.off[sg.n] == 0) return 0;
+  GMG_LAUNCH(widen_multi_kernel, vec_grid(sg.off[sg.n]), BLK, sg);
   LAUNCH_CHECK(mg);
   return 0;
 }

@@ -745,13 +745,37 @@ int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *ins
     tl.ninst = int(tl.ids.size());
     tl.nrows = int(rows.size());
     tl.nchunks = int(chunk_k.size());
+    tl.chunk_k = chunk_k;
+    tl.chunk_q = chunk_q;
     if (upload_owned(L, &tl.ids_dev, tl.ids) || upload_owned(L, &tl.ptr_dev, ptr) || upload_owned(L, &tl.rows_dev, rows) ||
-        upload_owned(L, &tl.pack_dev, pack) || upload_owned(L, &tl.chunk_k_dev, chunk_k) ||
-        upload_owned(L, &tl.chunk_q_dev, chunk_q) || upload_owned(L, &tl.inst_cptr_dev, inst_cptr) ||
-        upload_owned(L, &tl.ticket_dev, std::vector<int>(tl.ninst, 0)) ||
-        upload_owned(L, &tl.partial_dev, std::vector<double>(size_t(tl.nchunks) * s, 0.0)))
+        upload_owned(L, &tl.pack_dev, pack))
       return 1;
     B.tops.push_back(std::move(tl));
+  }
+  GMG_CHECK((int)B.tops.size() <= GMG_MAX_TOPS, "batched hierarchy: %zu distinct instance depths (at most %d)",
+            B.tops.size(), GMG_MAX_TOPS);
+  {  // all top levels' chunks in one table, each instance's chunks contiguous
+    std::vector<int> ctop, cid, cq0, cq1, ic0(ninst, 0), ic1(ninst, 0);
+    for (size_t t = 0; t < B.tops.size(); ++t) {
+      const auto &tl = B.tops[t];
+      for (int h = 0; h < tl.nchunks; ++h) {
+        const int id = tl.ids[tl.chunk_k[h]];
+        if (h == 0 || tl.chunk_k[h] != tl.chunk_k[h - 1]) ic0[id] = int(ctop.size());
+        ctop.push_back(int(t));
+        cid.push_back(id);
+        cq0.push_back(tl.chunk_q[h]);
+        cq1.push_back(tl.chunk_q[h + 1]);
+        ic1[id] = int(ctop.size());
+      }
+    }
+    B.nchunks_all = int(ctop.size());
+    Level &T0 = mg->lev.back();
+    if (upload_owned(T0, &B.chunk_top_dev, ctop) || upload_owned(T0, &B.chunk_id_dev, cid) ||
+        upload_owned(T0, &B.chunk_q0_dev, cq0) || upload_owned(T0, &B.chunk_q1_dev, cq1) ||
+        upload_owned(T0, &B.inst_c0_dev, ic0) || upload_owned(T0, &B.inst_c1_dev, ic1) ||
+        upload_owned(T0, &B.ticket_dev, std::vector<int>(ninst, 0)) ||
+        upload_owned(T0, &B.partial_dev, std::vector<double>(size_t(B.nchunks_all) * s, 0.0)))
+      return 1;
   }
   GMG_CHECK(pack_off[ninst] < (1LL << 31), "batched hierarchy: more than 2^31 top-level rows");
   Level &T = mg->lev.back();

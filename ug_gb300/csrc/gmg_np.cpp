@@ -893,9 +893,7 @@ int NPLs::Residuum(int, int tl, gmg_vec *, gmg_vec *bv, gmg_mat *, gmg_lresult *
 // is updated as b -= A c with the FP64 matrix (iterative refinement).
 int NPLs::batch_norms(gmg_vec *bv) {
   const auto &B = mg->batch;
-  for (const auto &tl : B.tops)
-    if (k_batch_finish(mg, tl, bv->prec, vlev(bv, tl.level), nullptr, GMG_PREC_FP64, nullptr, false, mg->lev[0].s))
-      return 1;
+  if (k_batch_finish(mg, bv->prec, bv, nullptr, GMG_PREC_FP64, nullptr, false, mg->lev[0].s)) return 1;
   GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
                            mg->stream));
   return 0;
@@ -913,20 +911,14 @@ int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int 
     // c below the deepest level is reset by every restriction of the cycle
     if (k_set(mg, cvec->prec, vlev(cvec, level), vlen(mg, level), 0.0)) return 1;
     if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
-    for (const auto &tl : B.tops)
-      if (k_batch_finish(mg, tl, bv->prec, vlev(bv, tl.level), (double *)vlev(xv, tl.level), cvec->prec,
-                         vlev(cvec, tl.level), false, s))
-        return 1;
+    if (k_batch_finish(mg, bv->prec, bv, xv, cvec->prec, cvec, false, s)) return 1;
   } else {
-    for (const auto &tl : B.tops)
-      if (k_refine_prepare(mg, (float *)vlev(b32, tl.level), (float *)vlev(cvec, tl.level),
-                           (const double *)vlev(bv, tl.level), vlen(mg, tl.level)))
-        return 1;
+    if (k_batch_refine_prepare(mg, b32, cvec, bv)) return 1;
     if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
-    for (const auto &tl : B.tops)
-      if (k_batch_finish(mg, tl, GMG_PREC_FP64, vlev(bv, tl.level), (double *)vlev(xv, tl.level), GMG_PREC_FP32,
-                         vlev(cvec, tl.level), true, s))
-        return 1;
+    // the FP64 refinement defect reads c in FP64: one conversion per row
+    // instead of one per stored entry (conversions run on GB300's FP64 pipe)
+    if (k_batch_widen(mg, c64, cvec) || k_batch_finish(mg, GMG_PREC_FP64, bv, xv, GMG_PREC_FP64, c64, true, s))
+      return 1;
   }
   GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
                            mg->stream));
@@ -1016,7 +1008,8 @@ int NPLs::prepare_temps(gmg_vec *bv) {
   const int cprec = mixed ? GMG_PREC_FP32 : bv->prec;
   if (!cvec || cvec->prec != cprec) cvec = temp_vec(mg, name + "__c" + std::to_string(cprec), cprec);
   if (mixed && !b32) b32 = temp_vec(mg, name + "__b32", GMG_PREC_FP32);
-  GMG_CHECK(cvec && (!mixed || b32), "ls: temporary vectors");
+  if (mixed && mg->batch.ninst > 0 && !c64) c64 = temp_vec(mg, name + "__c64", GMG_PREC_FP64);
+  GMG_CHECK(cvec && (!mixed || b32) && (!mixed || mg->batch.ninst == 0 || c64), "ls: temporary vectors");
   return 0;
 }
 

@@ -164,6 +164,7 @@ struct NPLs : NPLinearSolver {
   NPIter *IterNp = nullptr;
   gmg_vec *cvec = nullptr;                   // correction c (precision of x, or FP32 in mixed mode)
   gmg_vec *b32 = nullptr;                    // FP32 defect in mixed mode
+  gmg_vec *c64 = nullptr;                    // FP64 copy of the correction (batched mixed mode)
   bool preprocessed = false;
   // CUDA graph of one iteration (dset c; Iter; update; norm)
   cudaGraphExec_t graph = nullptr;
