@@ -50,6 +50,26 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def reduce_over_ranks(x: float, op: str = "max") -> float:
+    """max (times, latencies) or sum (throughputs) of a per-rank number over
+    all ranks; identity without a process group.  Replicas never exchange
+    data: this is the only collective of the benchmark."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, ms_per_step_max: float, world: int) -> float:
+    """Units per second of the whole job: every rank processes units_per_rank
+    per step, the job takes the slowest rank's time."""
+    return world * units_per_rank / (ms_per_step_max * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -220,6 +240,7 @@ def run_batched(args, stream, flush_l2, world, rank):
 
     ms32, it32, l32, clk32 = timed("bat32")
     ms64, it64, l64, _ = timed("bat64")
+    ms32, ms64 = reduce_over_ranks(ms32), reduce_over_ranks(ms64)
     # device-only: one solve from resident data (b already on the device)
     top = mg.top
     mg.createvector("b0")
@@ -241,6 +262,7 @@ def run_batched(args, stream, flush_l2, world, rank):
         if k >= args.warmup:
             dev_ms.append(a.elapsed_time(e))
     mg.close()
+    dev_ms_max = reduce_over_ranks(float(np.mean(dev_ms)))
     # plain FP64 GPU path: one instance at a time, on a sample
     rng = np.random.default_rng(1)
     sample = sorted(rng.choice(args.batch, size=min(32, args.batch), replace=False).tolist())
@@ -263,11 +285,11 @@ def run_batched(args, stream, flush_l2, world, rank):
     solo_per_s = len(sample) / solo_s
     solo_batch_s = solo_s / frac  # time to solve all instances one at a time
     out.update({
-        "mixed": {"value": world * args.batch / (ms32 * 1e-3), "unit": "solves/s (e2e, host b -> host x)",
+        "mixed": {"value": whole_job_rate(args.batch, ms32, world), "unit": "solves/s (e2e, host b -> host x)",
                   "ms_per_batch": ms32, "iterations_max": it32, "launches_per_batch": l32, "clocks": clk32,
-                  "device_ms_per_batch": float(np.mean(dev_ms)),
-                  "device_value": world * args.batch / (float(np.mean(dev_ms)) * 1e-3)},
-        "fp64_batched": {"value": world * args.batch / (ms64 * 1e-3), "ms_per_batch": ms64, "iterations_max": it64,
+                  "device_ms_per_batch": dev_ms_max,
+                  "device_value": whole_job_rate(args.batch, dev_ms_max, world)},
+        "fp64_batched": {"value": whole_job_rate(args.batch, ms64, world), "ms_per_batch": ms64, "iterations_max": it64,
                          "launches_per_batch": l64},
         "fp64_one_at_a_time": {"value": world * args.batch / solo_batch_s, "unit": "solves/s",
                                "sample": f"{len(sample)} instances solved one after another "
@@ -315,6 +337,9 @@ def run_serving(args, rank):
     with ClockSampler(torch.cuda.current_device()) as clk:
         st = srv.run(reqs)
     srv.close()
+    # replicas: latencies of the slowest rank, throughput of all ranks
+    st.p50_ms, st.p99_ms, st.mean_ms = (reduce_over_ranks(v) for v in (st.p50_ms, st.p99_ms, st.mean_ms))
+    st.throughput = reduce_over_ranks(st.throughput, "sum")
     out = {"workload": f"{args.serve_requests} requests, Poisson arrivals mean {SERVE_RATE:.0f}/s, 3D P1 cube "
                        f"levels U{{{SERVE_LEVELS[0]}..{SERVE_LEVELS[1]}}} (125..2146689 unknowns), k=exp(g) corr 0.1 "
                        f"var 1, FP32 GS V(2,2) in FP64 refinement to 1e-8",
@@ -416,11 +441,7 @@ def run_ours(args):
             torch.cuda.synchronize(); barrier()
             wall = time.perf_counter() - t0
         ms = [a.elapsed_time(b) for a, b in ev]
-        ms_step = float(np.mean(ms))
-        if world > 1:
-            t = torch.tensor([ms_step], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_step = float(t.item())
+        ms_step = reduce_over_ranks(float(np.mean(ms)), "max")
         results[solver] = {"ms_per_step": ms_step, "iters": iters[-1], "launches_per_step": launches / args.steps,
                            "clocks": clk.summary(), "wall_s": wall}
 
@@ -436,7 +457,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         mg.solve_host("mgs32", b_host, x_host)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_ms = float(np.mean(e2e_t)) * 1e3
+    e2e_ms = reduce_over_ranks(float(np.mean(e2e_t)) * 1e3)
 
     # roofline: finest-level dmatmul_minus (the defect / smoother-update pass), HBM-cold
     n, s, nnz = mg.size(top)
@@ -483,7 +504,7 @@ def run_ours(args):
 
     if rank == 0:
         r32, r64 = results["mgs32"], results["mgs64"]
-        value = world * 1e3 / r32["ms_per_step"]
+        value = whole_job_rate(1, r32["ms_per_step"], world)
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
@@ -493,10 +514,11 @@ def run_ours(args):
                                        "parallelism": "replicas" if world > 1 else "1 GPU",
                                        "gs_waves_per_level": waves,
                                        "launches_per_solve": r32["launches_per_step"]}),
-            "fp64": {"value": world * 1e3 / r64["ms_per_step"], "unit": "solves/s", "ms_per_step": r64["ms_per_step"],
+            "fp64": {"value": whole_job_rate(1, r64["ms_per_step"], world), "unit": "solves/s",
+                     "ms_per_step": r64["ms_per_step"],
                      "iterations": r64["iters"]},
             "mixed_over_fp64": r64["ms_per_step"] / r32["ms_per_step"],
-            "e2e": {"value": world * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": int(n * s * 8),
+            "e2e": {"value": whole_job_rate(1, e2e_ms, world), "unit": "solves/s", "h2d_bytes_per_step": int(n * s * 8),
                     "d2h_bytes_per_step": int(n * s * 8), "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "kernel": "spmv_minus_kernel<float> (finest level, HBM-cold)",
                          "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,

@@ -41,6 +41,9 @@ enum : uint8_t {
   F_RESET = 4,   // VNCLASS >= NEWDEF_CLASS (2): reset before restriction
 };
 
+// memcpy for large host buffers (several threads)
+void par_copy(void *dst, const void *src, size_t bytes);
+
 // ---------------------------------------------------------------- device memory
 // All arrays of one hierarchy live in one allocation; sub-arrays are 256-byte
 // aligned so every row / block access can use 128-bit loads.

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <numeric>
 #include <queue>
+#include <thread>
 #include <tuple>
 
 #include "gmg_internal.h"
@@ -28,6 +29,26 @@ void set_error(const char *fmt, ...) {
   va_end(ap);
 }
 const char *last_error() { return g_err; }
+
+// host copies into / out of the pinned staging buffers: one thread per 4 MB,
+// at most 8 (a single thread moves ~10 GB/s, short of the host link)
+void par_copy(void *dst, const void *src, size_t bytes) {
+  const size_t per = size_t(4) << 20;
+  const int nt = int(std::min<size_t>(8, (bytes + per - 1) / per));
+  if (nt <= 1) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  const size_t chunk = ((bytes + nt - 1) / nt + 63) & ~size_t(63);
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) {
+    const size_t o = chunk * t;
+    if (o >= bytes) break;
+    th.emplace_back([=] { std::memcpy((char *)dst + o, (const char *)src + o, std::min(chunk, bytes - o)); });
+  }
+  std::memcpy(dst, src, std::min(chunk, bytes));
+  for (auto &x : th) x.join();
+}
 
 int Arena::alloc(size_t bytes) {
   size = bytes;

@@ -1157,7 +1157,7 @@ int gmg_vec_upload(gmg_vec *v, int level, const double *host) {
   if (check_level(mg, level)) return 1;
   const Level &L = mg->lev[level];
   const size_t len = size_t(L.n) * L.s;
-  std::memcpy(mg->stage_host, host, len * sizeof(double));
+  par_copy(mg->stage_host, host, len * sizeof(double));
   GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
   if (k_gather(mg, v->prec, vlev(v, level), (const double *)mg->stage_dev, L.perm_dev, L.n, L.s)) return 1;
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
@@ -1173,7 +1173,7 @@ int gmg_vec_download(gmg_vec *v, int level, double *host) {
   if (k_scatter(mg, v->prec, (double *)mg->stage_dev, vlev(v, level), L.perm_dev, L.n, L.s)) return 1;
   GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, len * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
-  std::memcpy(host, mg->stage_host, len * sizeof(double));
+  par_copy(host, mg->stage_host, len * sizeof(double));
   return 0;
 }
 
@@ -1396,7 +1396,7 @@ int gmg_vec_upload_packed(gmg_vec *v, const double *host) {
   gmg_mg *mg = v->mg;
   GMG_CHECK(mg->batch.ninst > 0, "gmg_vec_upload_packed: not a batched hierarchy");
   const size_t len = size_t(packed_len(mg));
-  std::memcpy(mg->stage_host, host, len * sizeof(double));
+  par_copy(mg->stage_host, host, len * sizeof(double));
   GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
   for (const auto &tl : mg->batch.tops)
     if (k_pack_gather(mg, v->prec, vlev(v, tl.level), (const double *)mg->stage_dev, tl, mg->lev[0].s)) return 1;
@@ -1413,7 +1413,7 @@ int gmg_vec_download_packed(gmg_vec *v, double *host) {
     if (k_pack_scatter(mg, v->prec, (double *)mg->stage_dev, vlev(v, tl.level), tl, mg->lev[0].s)) return 1;
   GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, len * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
-  std::memcpy(host, mg->stage_host, len * sizeof(double));
+  par_copy(host, mg->stage_host, len * sizeof(double));
   return 0;
 }
 

@@ -298,7 +298,7 @@ int gmg_pool_fetch(gmg_pool *p, int k, double *x_host, gmg_lresult *lr) {
     GMG_CUDA(cudaMemcpyAsync(mg->stage_host + o, (double *)mg->stage_dev + o, sizeof(double) * n * s,
                              cudaMemcpyDeviceToHost, mg->stream));
     GMG_CUDA(cudaStreamSynchronize(mg->stream));
-    std::memcpy(x_host, mg->stage_host + o, sizeof(double) * n * s);
+    par_copy(x_host, mg->stage_host + o, sizeof(double) * n * s);
   }
   if (lr) {
     *lr = gmg_lresult{};
