@@ -478,32 +478,130 @@ static int sc_cmp(const double *x, const double *y, int s) {
 
 /* LinearSolver, np/procs/ls.cc:637-749, preceded by LinearDefect (562) and
  * LinearResiduum (577); LSUpdate (869) adds c on levels baselevel..top. */
+/* the lmgc workspace of levels bl..top; b of the top level is the caller's */
+static int ws_init(orc_ws *w, const orc_mg *mg, double *b) {
+  const int top = mg->nlevels - 1;
+  const int s = mg->lev[top].s;
+  const int bl = mg->baselevel < top ? mg->baselevel : top;
+  memset(w, 0, sizeof *w);
+  w->mg = mg;
+  w->c = (double **)calloc(mg->nlevels, sizeof(double *));
+  w->t = (double **)calloc(mg->nlevels, sizeof(double *));
+  w->b = (double **)calloc(mg->nlevels, sizeof(double *));
+  w->lu = (double **)calloc(mg->nlevels, sizeof(double *));
+  for (int l = bl; l <= top; ++l) {
+    size_t len = (size_t)mg->lev[l].n * s;
+    w->c[l] = (double *)calloc(len, sizeof(double));
+    w->t[l] = (double *)calloc(len, sizeof(double));
+    w->b[l] = (l == top) ? b : (double *)calloc(len, sizeof(double));
+    if (mg->smoother == ORC_ILU && l > bl) {
+      const orc_level *L = &mg->lev[l];
+      int rc;
+      w->lu[l] = (double *)malloc(sizeof(double) * (size_t)L->rowptr[L->n] * s * s);
+      if ((rc = orc_ilu_decomp(L, w->lu[l], mg->beta))) return rc;
+    }
+  }
+  if (base_factor(w, &mg->lev[bl])) return -1000000;
+  return 0;
+}
+
+static void ws_free(orc_ws *w) {
+  const orc_mg *mg = w->mg;
+  const int top = mg->nlevels - 1;
+  const int bl = mg->baselevel < top ? mg->baselevel : top;
+  for (int l = bl; l <= top; ++l) {
+    free(w->c[l]); free(w->t[l]); free(w->lu[l]);
+    if (l != top) free(w->b[l]);
+  }
+  free(w->c); free(w->t); free(w->b); free(w->lu); free(w->base_lu);
+}
+
+/* dmatmul, ugblas.cc:3782: x = A y, per row the products summed, then assigned */
+static void matmul(const orc_level *L, double *x, const double *y) {
+  const int s = L->s, ss = s * s;
+  for (int i = 0; i < L->n; ++i) {
+    double acc[ORC_MAX_S] = {0};
+    for (int k = L->rowptr[i]; k < L->rowptr[i + 1]; ++k) {
+      const double *m = L->val + (size_t)k * ss;
+      const double *w = y + (size_t)L->col[k] * s;
+      for (int r = 0; r < s; ++r) {
+        double t = 0.0;
+        for (int c = 0; c < s; ++c) t += m[r * s + c] * w[c];
+        acc[r] += t;
+      }
+    }
+    for (int r = 0; r < s; ++r) x[(size_t)i * s + r] = acc[r];
+  }
+}
+
+/* ddot ON_SURFACE, ugblas.cc:3104: one sum over the NEW_DEFECT vectors of the
+ * top level, components in order, vectors in list order */
+static double ddot(const orc_level *L, const double *x, const double *y) {
+  const int s = L->s;
+  double sum = 0.0;
+  for (int i = 0; i < L->n; ++i) {
+    if (L->vclass[i] < NEWDEF_CLASS) continue;
+    for (int r = 0; r < s; ++r) sum += x[(size_t)i * s + r] * y[(size_t)i * s + r];
+  }
+  return sum;
+}
+
+int orc_cg_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
+                 double *hist, int *converged) {
+  const int top = mg->nlevels - 1;
+  const int s = mg->lev[top].s;
+  const orc_level *T = &mg->lev[top];
+  const size_t len = (size_t)T->n * s;
+  orc_ws w;
+  int rc = ws_init(&w, mg, b), it = 0;
+  double *p = (double *)calloc(len, sizeof(double)), *t = (double *)calloc(len, sizeof(double));
+  *converged = 0;
+  if (rc) goto done;
+  {
+    double first[ORC_MAX_S], last[ORC_MAX_S], reach[ORC_MAX_S], rho = 1.0; /* CGPrepare, ls.cc:976 */
+    orc_matmul_minus(T, b, x);
+    orc_nrm2x(T, b, first);
+    if (hist) for (int r = 0; r < s; ++r) hist[r] = first[r];
+    for (int r = 0; r < s; ++r) { reach[r] = first[r] * red[r]; if (reach[r] == 0.0) reach[r] = red[r]; }
+    *converged = sc_cmp(first, abslimit, s);
+    for (it = 0; it < maxit; ++it) {
+      if (*converged) break;
+      double *c = w.c[top];
+      memset(c, 0, sizeof(double) * len);
+      if ((rc = lmgc(&w, top))) goto done;
+      /* CGUpdate, ls.cc:989-1064 */
+      matmul(T, t, c);
+      vadd(b, t, len);
+      double lambda = ddot(T, c, b);
+      const double f = lambda / rho;
+      for (size_t i = 0; i < len; ++i) p[i] *= f;
+      rho = lambda;
+      vadd(p, c, len);
+      matmul(T, t, p);
+      lambda = ddot(T, t, p);
+      if (lambda == 0.0) { rc = -2000000; goto done; }
+      const double a = rho / lambda, na = -rho / lambda;
+      for (size_t i = 0; i < len; ++i) x[i] += a * p[i];
+      for (size_t i = 0; i < len; ++i) b[i] += na * t[i];
+      orc_nrm2x(T, b, last);
+      if (hist) for (int r = 0; r < s; ++r) hist[(size_t)(it + 1) * s + r] = last[r];
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) { *converged = 1; ++it; break; }
+    }
+  }
+done:
+  free(p); free(t);
+  ws_free(&w);
+  return rc ? rc : it;
+}
+
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
                  double *hist, int *converged) {
   const int top = mg->nlevels - 1;
   const int s = mg->lev[top].s;
-  const int bl = mg->baselevel < top ? mg->baselevel : top;
   orc_ws w;
-  memset(&w, 0, sizeof w);
-  w.mg = mg;
-  w.c = (double **)calloc(mg->nlevels, sizeof(double *));
-  w.t = (double **)calloc(mg->nlevels, sizeof(double *));
-  w.b = (double **)calloc(mg->nlevels, sizeof(double *));
-  w.lu = (double **)calloc(mg->nlevels, sizeof(double *));
-  int rc = 0, it = 0;
+  int rc = ws_init(&w, mg, b), it = 0;
   *converged = 0;
-  for (int l = bl; l <= top; ++l) {
-    size_t len = (size_t)mg->lev[l].n * s;
-    w.c[l] = (double *)calloc(len, sizeof(double));
-    w.t[l] = (double *)calloc(len, sizeof(double));
-    w.b[l] = (l == top) ? b : (double *)calloc(len, sizeof(double));
-    if (mg->smoother == ORC_ILU && l > bl) {
-      const orc_level *L = &mg->lev[l];
-      w.lu[l] = (double *)malloc(sizeof(double) * (size_t)L->rowptr[L->n] * s * s);
-      if ((rc = orc_ilu_decomp(L, w.lu[l], mg->beta))) goto done;
-    }
-  }
-  if (base_factor(&w, &mg->lev[bl])) { rc = -1000000; goto done; }
+  if (rc) goto done;
   {
     const orc_level *T = &mg->lev[top];
     const size_t len = (size_t)T->n * s;
@@ -524,10 +622,6 @@ int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, cons
     }
   }
 done:
-  for (int l = bl; l <= top; ++l) {
-    free(w.c[l]); free(w.t[l]); free(w.lu[l]);
-    if (l != top) free(w.b[l]);
-  }
-  free(w.c); free(w.t); free(w.b); free(w.lu); free(w.base_lu);
+  ws_free(&w);
   return rc ? rc : it;
 }

@@ -71,6 +71,10 @@ void orc_interpolate(const orc_level *fine, double *to_fine, const double *from_
  * is the start value and receives the solution; b is overwritten by the
  * final defect.  hist (may be NULL) receives s*(maxit+1) defect norms.
  * Returns the number of iterations, or a negative error code. */
+/* The same problem with UG's cg (np/procs/ls.cc:901-1064, CGPrepare /
+ * CGUpdate in LinearSolver's loop) preconditioned by lmgc. */
+int orc_cg_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
+                 double *hist, int *converged);
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit,
                  int maxit, double *hist, int *converged);
 

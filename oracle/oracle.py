@@ -89,7 +89,8 @@ def lib():
         L.orc_restrict.argtypes = [P, P, P, P, P]
         L.orc_interpolate.argtypes = [P, P, P, P]
         L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
-        for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve"):
+        L.orc_cg_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve", "orc_cg_solve"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -179,9 +180,14 @@ class Hierarchy:
         lib().orc_interpolate(self.lev(l), _p(to), _p(fr), _p(dm)); return to
 
     # ---- solver
+    def cg_solve(self, rhs, **kw):
+        """cg (ls.cc:901-1064) preconditioned by lmgc, configured as ls_solve.
+        Returns (x, iterations, converged, history)."""
+        return self.ls_solve(rhs, _solver="cg", **kw)
+
     def ls_solve(self, rhs, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None,
                  beta=None, cdamp=None, red=1e-10, abslimit=1e-50, maxit=100, x0=None,
-                 base_abslimit=1e-10):
+                 base_abslimit=1e-10, _solver="ls"):
         """ls + lmgc as configured by `npinit lmgc $n1 $n2 $g $b` and `npinit ls
         $red $abslimit $m`.  Returns (x, iterations, converged, history)."""
         top = len(self.levels) - 1
@@ -201,7 +207,8 @@ class Hierarchy:
         absv = np.resize(np.asarray(abslimit, np.float64), MAX_S)
         hist = np.zeros((maxit + 1) * s)
         conv = C.c_int(0)
-        it = lib().orc_ls_solve(C.byref(mg), _p(x), _p(b), _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
+        f = lib().orc_cg_solve if _solver == "cg" else lib().orc_ls_solve
+        it = f(C.byref(mg), _p(x), _p(b), _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
         if it < 0:
-            raise RuntimeError(f"oracle ls failed: {it}")
+            raise RuntimeError(f"oracle {_solver} failed: {it}")
         return x, it, bool(conv.value), hist[: (it + 1) * s].reshape(it + 1, s)

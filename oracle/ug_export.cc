@@ -438,6 +438,34 @@ int main(int argc, char **argv) {
     putd("ls_hist", hist);
     putd("ls_x_replay", grab(sol, top));
   }
+
+  // ---- UG's cg (ls.cc:901-1165) preconditioned by the same lmgc, from x = 0
+  {
+    for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
+    for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
+    int i = 0;
+    for (VECTOR *v : g_lev[top].vecs) for (int c = 0; c < s; ++c) VVALUE(v, vcmp(rhs)[c]) = rhs_top[i++];
+    snprintf(cmd, sizeof cmd, "npcreate cgs $c cg; npinit cgs $A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m %d $I lmgc;",
+             maxit);
+    run(cmd);
+    NP_LINEAR_SOLVER *cg = (NP_LINEAR_SOLVER *)GetNumProcByName(mg, "cgs", LINEAR_SOLVER_CLASS_NAME);
+    if (!cg) { fprintf(stderr, "cg lookup failed\n"); return 1; }
+    LRESULT lc;
+    memset(&lc, 0, sizeof lc);
+    if ((*cg->PreProcess)(cg, top, sol, rhs, A, &bl, &res)) { fprintf(stderr, "cg PreProcess failed\n"); return 1; }
+    (*cg->Defect)(cg, top, sol, rhs, A, &res);
+    (*cg->Residuum)(cg, bl, top, sol, rhs, A, &lc);
+    if ((*cg->Solver)(cg, top, sol, rhs, A, cg->abslimit, cg->reduction, &lc)) {
+      fprintf(stderr, "cg Solver failed\n");
+      return 1;
+    }
+    put1i("cg_iters", lc.number_of_linear_iterations); put1i("cg_converged", lc.converged);
+    putd("cg_first", std::vector<double>(lc.first_defect, lc.first_defect + s));
+    putd("cg_last", std::vector<double>(lc.last_defect, lc.last_defect + s));
+    putd("cg_x", grab(sol, top));
+    fprintf(stderr, "UG cg: iters=%d converged=%d last=%.6e\n", (int)lc.number_of_linear_iterations, (int)lc.converged,
+            lc.last_defect[0]);
+  }
   (*ls->PostProcess)(ls, top, sol, rhs, A, &res);
   fclose(g_out);
   return 0;

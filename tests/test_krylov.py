@@ -1,0 +1,69 @@
+"""cg preconditioned by lmgc (np/procs/ls.cc:901-1064) on the device: the
+`gcg` numproc against UG's own cg solves (tests/golden: cg_iters, cg_x) in
+UG's vector order, against the oracle's cg on the reordered hierarchy in
+multicolour order, and its FP32-preconditioner variant against the FP64
+stopping test.  Tolerances: iterations equal (+-1 allowed by the contract),
+solution 1e-10 relative (jac) / 1e-8 (gs, ilu; order-dependent smoothers)."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, permuted_levels, rel
+
+pytestmark = pytest.mark.gpu
+NAMES = golden_names()
+
+
+@pytest.fixture(scope="module")
+def G():
+    import ug_gb300
+    ug_gb300.lib()
+    return ug_gb300
+
+
+def _setup_cg(G, mg, sm, bl, red=1e-10, mixed=False, name="cgs"):
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=0.8 if sm == "jac" else 1.0, red=red, abslimit=1e-50)
+    mg.npcreate(name, "linear_solver.gcg")
+    st = mg.npinit(name, f"$A MAT $x sol $b rhs $red {red} $abslimit 1e-50 $m 100 $I lmgc $mixed {int(mixed)}")
+    assert st == G.NP_EXECUTABLE
+    return name
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_cg_matches_ug(G, name):
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    mg = G.MultiGrid(levels, order=G.ORDER_LIST, fp32=True)
+    sm, bl = fx["smoother"], int(fx["baselevel"][0])
+    _setup_cg(G, mg, sm, bl)
+    x, lr = mg.solve_host("cgs", fx["rhs"])
+    assert lr.converged and abs(lr.iters - int(fx["cg_iters"][0])) <= 1
+    assert rel(x, fx["cg_x"]) <= (1e-10 if sm == "jac" else 1e-8)
+    # the FP32 preconditioner inside the FP64 cg meets the same stopping test
+    mg.npcreate("cgs32", "linear_solver.gcg")
+    mg.npinit("cgs32", "$A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    x32, lr32 = mg.solve_host("cgs32", fx["rhs"])
+    assert lr32.converged and lr32.iters <= int(fx["cg_iters"][0]) + 3
+    assert rel(x32, fx["cg_x"]) <= 1e-6
+    mg.close()
+
+
+@pytest.mark.parametrize("sm", ["jac", "ilu"])
+@pytest.mark.parametrize("order", [0, 1])
+def test_cg_vs_oracle_midsize(G, oracle_mod, order, sm):
+    """3D P1 diffusion 17^3, k = exp(g): device cg vs the oracle's cg on the
+    same (possibly reordered) hierarchy.  (With forward Gauss-Seidel as pre-
+    and post-smoother the V-cycle is not symmetric and UG's cg stagnates near
+    1e-8 on this problem; the oracle reproduces that, so gs is not used here.)"""
+    gen = G.Generator(1, 4, seed=5, corr=0.1, var=1.0)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=order, fp32=True)
+    _setup_cg(G, mg, sm, 0)
+    x, lr = mg.solve_host("cgs", gen.rhs)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    perm = mg.order(mg.top)
+    xo, ito, conv, _ = H.cg_solve(gen.rhs[perm], smoother=sm, baselevel=0, damp=0.8 if sm == "jac" else 1.0,
+                                  red=1e-10, abslimit=1e-50)
+    xr = np.empty_like(xo); xr[perm] = xo
+    assert conv and lr.converged and abs(lr.iters - ito) <= 1
+    assert rel(x, xr) <= (1e-10 if sm == "jac" else 1e-8)
+    mg.close()

@@ -42,3 +42,17 @@ def test_solve_matches_ug(name, oracle_mod):
     assert rel(hist.ravel(), fx["ls_hist"]) <= 1e-12
     # UG's own replay of the ls loop reproduces its solve exactly
     assert rel(fx["ls_x_replay"], fx["ls_x"]) == 0.0
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_cg_matches_ug(name, oracle_mod):
+    """UG's cg (np/procs/ls.cc:901-1064) preconditioned by the same lmgc:
+    the oracle takes UG's iteration count and reaches UG's solution."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    sm = fx["smoother"]
+    x, it, conv, hist = H.cg_solve(fx["rhs"], smoother=sm, baselevel=int(fx["baselevel"][0]),
+                                   damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50)
+    assert conv == bool(fx["cg_converged"][0]) and it == int(fx["cg_iters"][0])
+    assert rel(x, fx["cg_x"]) <= 1e-12
+    assert rel(hist[-1], fx["cg_last"]) <= 1e-10

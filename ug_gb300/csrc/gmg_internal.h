@@ -255,6 +255,14 @@ int k_batch_finish(gmg_mg *mg, int bprec, gmg_vec *b, gmg_vec *x, int cprec, gmg
 int k_batch_refine_prepare(gmg_mg *mg, gmg_vec *b32, gmg_vec *c32, gmg_vec *b64);
 // on every top level: c64 = c32 (one launch)
 int k_batch_widen(gmg_mg *mg, gmg_vec *c64, gmg_vec *c32);
+// cg (FP64 vectors): surface dot of x and y with CGUpdate's scalar step on
+// sc[] (mode 1: f = lambda/rho, rho = lambda; mode 2: alpha = rho/(sign*dot),
+// sc[3] = 1 if that dot is 0); p = f p + c; x += alpha p and b += alpha tn;
+// b -= t
+int k_cg_dot(gmg_mg *mg, const Level &L, const double *x, const double *y, double *sc, int mode, double sign);
+int k_cg_p(gmg_mg *mg, long long len, double *p, const double *c, const double *sc);
+int k_cg_xb(gmg_mg *mg, long long len, double *x, const double *p, double *b, const double *tn, const double *sc);
+int k_sub(gmg_mg *mg, long long len, double *b, const double *t);
 // the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
 struct CoarseCfg {
   int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;

@@ -852,6 +852,94 @@ __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, doub
   }
 }
 
+// ------------------------------------------------------------ cg (ls.cc:989-1064)
+// ddot over the NEW_DEFECT rows (the surface of the top level), FP64, with the
+// deterministic last-block reduction of nrm_kernel; the last block also does
+// CGUpdate's scalar work on device scalars sc[], so a cg iteration needs no
+// host round trip:
+//   MODE 1: lambda = sum; f = lambda / rho; rho = lambda   (sc[CG_F], sc[CG_RHO])
+//   MODE 2: lambda = sign * sum; alpha = rho / lambda, or a flag if lambda = 0
+enum { CG_F = 0, CG_RHO = 1, CG_ALPHA = 2, CG_FLAG = 3 };
+template <int S, bool ALL, int MODE>
+__global__ void __launch_bounds__(BLK) cg_dot_kernel(int n, const double *__restrict__ x, const double *__restrict__ y,
+                                                     const uint8_t *__restrict__ flags, double *__restrict__ partial,
+                                                     unsigned *__restrict__ ticket, double *__restrict__ sc,
+                                                     double sign) {
+  pdl_prologue();
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!ALL && !(flags[i] & F_NEWDEF)) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc = fma(x[(size_t)i * S + r], y[(size_t)i * S + r], acc);
+  }
+  __shared__ double sh[BLK / 32];
+  __shared__ bool last;
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w];
+    partial[blockIdx.x] = v;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[BLK];
+  double v = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(partial + b);
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double lam = sign * red[0];
+    if (MODE == 1) {
+      sc[CG_F] = lam / sc[CG_RHO];
+      sc[CG_RHO] = lam;
+    } else {
+      if (lam == 0.0) {
+        sc[CG_ALPHA] = 0.0;
+        sc[CG_FLAG] = 1.0;
+      } else {
+        sc[CG_ALPHA] = sc[CG_RHO] / lam;
+      }
+    }
+    *ticket = 0u;
+  }
+}
+
+// p = f p + c (dscal, then dadd: two roundings, as UG)
+__global__ void cg_p_kernel(long long len, double *__restrict__ p, const double *__restrict__ c,
+                            const double *__restrict__ sc) {
+  pdl_prologue();
+  const double f = sc[CG_F];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    p[i] = __dadd_rn(__dmul_rn(p[i], f), c[i]);
+}
+
+// x += alpha p; b -= alpha (A p), with tn = -(A p) (two daxpy, as UG)
+__global__ void cg_xb_kernel(long long len, double *__restrict__ x, const double *__restrict__ p,
+                             double *__restrict__ b, const double *__restrict__ tn, const double *__restrict__ sc) {
+  pdl_prologue();
+  const double a = sc[CG_ALPHA];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    x[i] = __dadd_rn(x[i], __dmul_rn(a, p[i]));
+    b[i] = __dadd_rn(b[i], __dmul_rn(a, tn[i]));
+  }
+}
+
+// b -= t (b += A c with t = -(A c))
+__global__ void sub_kernel(long long len, double *__restrict__ b, const double *__restrict__ t) {
+  pdl_prologue();
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    b[i] = __dsub_rn(b[i], t[i]);
+}
+
 // ------------------------------------------------------------ batched ls
 // The end of one ls iteration of a batched hierarchy, over the rows of every
 // instance on its own finest level (all top levels in one launch):
@@ -1748,6 +1836,39 @@ int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x) {
 #undef N1
   set_error("block size %d not compiled", L.s);
   return 1;
+}
+
+int k_cg_dot(gmg_mg *mg, const Level &L, const double *x, const double *y, double *sc, int mode, double sign) {
+  unsigned *ticket = reinterpret_cast<unsigned *>(mg->norms_dev + GMG_MAX_S);
+  const bool all = L.all_active;
+#define CD(SS, A, M) GMG_LAUNCH((cg_dot_kernel<SS, A, M>), REDUCE_BLOCKS, BLK, L.n, x, y, L.flags, mg->partial, ticket, sc, sign)
+#define CM(SS)                                                   \
+  if (mode == 1) { if (all) CD(SS, true, 1); else CD(SS, false, 1); } \
+  else { if (all) CD(SS, true, 2); else CD(SS, false, 2); }
+  if (L.s == 1) { CM(1) } else if (L.s == 2) { CM(2) } else if (L.s == 3) { CM(3) }
+  else { set_error("block size %d not compiled", L.s); return 1; }
+#undef CM
+#undef CD
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_cg_p(gmg_mg *mg, long long len, double *p, const double *c, const double *sc) {
+  GMG_LAUNCH(cg_p_kernel, vec_grid(len), BLK, len, p, c, sc);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_cg_xb(gmg_mg *mg, long long len, double *x, const double *p, double *b, const double *tn, const double *sc) {
+  GMG_LAUNCH(cg_xb_kernel, vec_grid(len), BLK, len, x, p, b, tn, sc);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_sub(gmg_mg *mg, long long len, double *b, const double *t) {
+  GMG_LAUNCH(sub_kernel, vec_grid(len), BLK, len, b, t);
+  LAUNCH_CHECK(mg);
+  return 0;
 }
 
 int k_base_solve(gmg_mg *mg, const Level &L, int prec, void *c, void *b, void *t, const double *abslimit) {

@@ -981,7 +981,7 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   int i;
   for (i = 0; i < maxiter; ++i) {
     if (lr->converged) break;
-    if (step(i, level, xv, bv, Am, lr)) return 1;
+    if (step(i, level, xv, bv, Am, lr) || check_iteration(i)) return 1;
     for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
     for (int r = 0; r < s; ++r)
       GMG_CHECK(std::isfinite(lr->last_defect[r]), "ls: defect is not finite in iteration %d", i + 1);
@@ -1108,6 +1108,83 @@ int NPLs::PostProcess(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *res
   return 0;
 }
 
+// ------------------------------------------------------------ cg
+NPCg::~NPCg() {
+  if (sc) cudaFree(sc);
+  if (flag_host) cudaFreeHost(flag_host);
+}
+
+int NPCg::Init(const Args &a) {  // CGInit: $r restart index (>= 0), then LinearSolverInit
+  if (!a.get_int("r", &restart)) restart = 0;
+  if (restart < 0) return NP_NOT_ACTIVE;
+  return NPLs::Init(a);
+}
+
+std::string NPCg::Display() const {
+  std::ostringstream o;
+  o << NPLs::Display() << "r = " << restart << "\n";
+  return o.str();
+}
+
+// CGPrepare (ls.cc:976): p = 0, rho = 1; then LinearSolver's loop
+int NPCg::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double *abs_, const double *red,
+                 gmg_lresult *lr) {
+  if (check_level(mg, level)) return 1;
+  GMG_CHECK(mg->batch.ninst == 0, "cg on a batched hierarchy is not supported (use ls)");
+  GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64, "cg: x and b must be FP64");
+  if (!p) p = temp_vec(mg, name + "__p", GMG_PREC_FP64);
+  if (!t) t = temp_vec(mg, name + "__t", GMG_PREC_FP64);
+  if (!c64) c64 = temp_vec(mg, name + "__c64", GMG_PREC_FP64);
+  GMG_CHECK(p && t && c64, "cg: temporary vectors");
+  if (!sc) {
+    GMG_CUDA(cudaMalloc(&sc, 4 * sizeof(double)));
+    GMG_CUDA(cudaMallocHost(&flag_host, sizeof(double)));
+  }
+  const double init[4] = {0.0, 1.0, 0.0, 0.0};
+  GMG_CUDA(cudaMemcpyAsync(sc, init, sizeof init, cudaMemcpyHostToDevice, mg->stream));
+  if (k_set(mg, GMG_PREC_FP64, vlev(p, level), vlen(mg, level), 0.0)) return 1;
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  *flag_host = 0.0;
+  return NPLs::Solver(level, xv, bv, Am, abs_, red, lr);
+}
+
+// one pass of LinearSolver's loop body with CGUpdate (ls.cc:694-701, 989-1064)
+int NPCg::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const Level &L = mg->lev[level];
+  const long long len = vlen(mg, level);
+  double *b = (double *)vlev(bv, level), *x = (double *)vlev(xv, level), *pp = (double *)vlev(p, level),
+         *tt = (double *)vlev(t, level), *c;
+  if (!mixed) {
+    c = (double *)vlev(cvec, level);
+    if (k_set(mg, GMG_PREC_FP64, c, len, 0.0)) return 1;
+    if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
+    // t = A c; b += t: the defect before Iter
+    if (k_set(mg, GMG_PREC_FP64, tt, len, 0.0) || k_matmul_minus(mg, L, GMG_PREC_FP64, tt, c, nullptr) ||
+        k_sub(mg, len, b, tt))
+      return 1;
+  } else {
+    // the FP32 preconditioner works on a copy of the defect
+    if (k_refine_prepare(mg, (float *)vlev(b32, level), (float *)vlev(cvec, level), b, len)) return 1;
+    if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    c = (double *)vlev(c64, level);
+    if (k_convert(mg, GMG_PREC_FP64, c, GMG_PREC_FP32, vlev(cvec, level), len)) return 1;
+  }
+  // lambda = (c, b); p = (lambda / rho) p + c; rho = lambda; t = A p;
+  // lambda = (t, p); x += (rho / lambda) p; b -= (rho / lambda) t
+  if (k_cg_dot(mg, L, c, b, sc, 1, 1.0) || k_cg_p(mg, len, pp, c, sc)) return 1;
+  if (k_set(mg, GMG_PREC_FP64, tt, len, 0.0) || k_matmul_minus(mg, L, GMG_PREC_FP64, tt, pp, nullptr)) return 1;
+  if (k_cg_dot(mg, L, tt, pp, sc, 2, -1.0) || k_cg_xb(mg, len, x, pp, b, tt, sc)) return 1;
+  if (k_nrm2x(mg, L, GMG_PREC_FP64, b)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  return 0;
+}
+
+int NPCg::check_iteration(int i) {
+  GMG_CHECK(*flag_host == 0.0, "cg: (A p, p) = 0 in iteration %d", i + 1);  // CGUpdate's lambda == 0 error
+  return 0;
+}
+
 // ------------------------------------------------------------ class registry (CreateClass)
 static gmg_np *construct(const std::string &cls) {
   // the class name's last component selects the constructor (GetConstructor, numproc.cc:145)
@@ -1119,6 +1196,7 @@ static gmg_np *construct(const std::string &cls) {
   if (c == "glmgc") return new NPLmgc;
   if (c == "gtransfer") return new NPTransfer;
   if (c == "gls") return new NPLs;
+  if (c == "gcg") return new NPCg;
   return nullptr;
 }
 

@@ -182,7 +182,9 @@ struct NPLs : NPLinearSolver {
   bool capturable() const override { return false; }
   std::string Display() const override;
   // one iteration without the host-side test: dset c, Iter, update x, norm into mg->norms_dev
-  int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
+  virtual int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
+  // after every synchronised iteration: nonzero stops the solver with an error
+  virtual int check_iteration(int i) { return 0; }
   // the base-solver shortcut of lmgc: `ls $m 1 $I ex` as one kernel
   bool is_exact_base() const;
   // iteration i of Solver's loop (graph replay after the first), synchronised
@@ -198,6 +200,25 @@ struct NPLs : NPLinearSolver {
   int batch_iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
   int batch_solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit, const double *reduction,
                    gmg_lresult *lr);
+};
+
+// cg, np/procs/ls.cc:901-1064: LinearSolver's loop with CGPrepare / CGUpdate
+// (preconditioner `$I`, e.g. lmgc).  The scalars live on the device, so an
+// iteration is one captured graph like ls's.  `$mixed 1` applies the
+// preconditioner in FP32 (its FP64 defect is then never modified, so the
+// CGUpdate step that restores it is skipped).
+struct NPCg : NPLs {
+  int restart = 0;
+  gmg_vec *p = nullptr, *t = nullptr;
+  double *sc = nullptr;       // device: f, rho, alpha, flag
+  double *flag_host = nullptr;  // pinned copy of the flag
+  ~NPCg() override;
+  int Init(const Args &a) override;  // CGInit, ls.cc:939
+  int Solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit, const double *reduction,
+             gmg_lresult *lr) override;
+  int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err) override;
+  int check_iteration(int i) override;
+  std::string Display() const override;
 };
 
 // helpers shared by the numprocs and the C ABI

@@ -27,7 +27,20 @@ def main():
     ap.add_argument("--order", default="color", choices=["color", "list"])
     ap.add_argument("--bsmem", type=int, default=None)
     ap.add_argument("--spmv", action="store_true")
+    ap.add_argument("--pool", type=int, default=0, help="one request in a one-slot serving pool of this depth")
     a = ap.parse_args()
+    if a.pool:
+        from ug_gb300.serve import Pool
+        p = Pool(a.pool, 1)
+        p.free.remove(0)
+        p.admit(0, 2026, 0.1, 1.0)
+        for _ in range(a.cycles):
+            p.launch()
+            while p.poll() is None:
+                pass
+        print(f"{a.cycles} pool iterations, depth {a.pool}")
+        p.close()
+        return
     if a.spmv:
         gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
         mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
