@@ -195,6 +195,52 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- config 1
+def run_c1(args, stream, flush_l2, world, rank):
+    """The reference's CPU-runnable case: 2D Q1 Poisson on the unit square,
+    257x257 nodes (66,049 unknowns; the 4x4 grid refined 6 times, i.e. one quad
+    refined 8 times with base level 2), uniform[-1,1] right-hand side, plain
+    FP64 lmgc V(2,2) with damped Jacobi (omega 0.8) to 1e-10 relative defect."""
+    import torch
+    import ug_gb300 as G
+    gen = G.Generator(G.Generator.POISSON2D, 8, seed=SEED)
+    mg = G.MultiGrid(gen, order=G.ORDER_COLOR, device=torch.cuda.current_device())
+    G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
+    G.setup_lmgc(mg, "jac", baselevel=2, damp=0.8, red=1e-10, abslimit=1e-50)
+    b = np.ascontiguousarray(gen.rhs)
+    x = np.empty_like(b)
+    for _ in range(args.warmup):
+        mg.solve_host("mgs", b, x)
+    ts = []
+    for _ in range(args.steps):
+        flush_l2(); torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, lr = mg.solve_host("mgs", b, x)
+        ts.append((time.perf_counter() - t0) * 1e3)
+        assert lr.converged
+    ms = reduce_over_ranks(float(np.mean(ts)))
+    iters = lr.iters
+    mg.close()
+    out = {"workload": "2D Q1 Poisson 257x257 (66,049 unknowns), lmgc V(2,2) Jacobi omega 0.8, base 4x4 grid, "
+                       "plain FP64, ls to 1e-10 rel defect",
+           "value": whole_job_rate(1, ms, world), "unit": "solves/s (e2e, host b -> host x)", "ms_per_solve": ms,
+           "iterations": iters}
+    if rank == 0:
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build()
+            H = oracle.Hierarchy(gen.levels())
+            t0 = time.perf_counter()
+            _, it, conv, _ = H.ls_solve(gen.rhs, smoother="jac", baselevel=2, damp=0.8, red=1e-10)
+            dt = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                                   "sample": f"one FP64 solve, UG list order ({it} iterations, {dt:.2f} s)"}
+        except Exception as e:  # reported, not fatal
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    return out
+
+
 # ---------------------------------------------------------------- batched workload
 BATCH_N = 512
 
@@ -499,6 +545,7 @@ def run_ours(args):
 
     waves = [mg.num_waves(l) for l in range(mg.nlevels)]
     mg.close()
+    c1 = run_c1(args, stream, flush_l2, world, rank)
     batched = run_batched(args, stream, flush_l2, world, rank) if not args.no_batched else None
     serving = run_serving(args, rank) if not args.no_serving else None
 
@@ -529,6 +576,7 @@ def run_ours(args):
             "gpu_launches": int(r32["launches_per_step"] * args.steps),
             "clocks": r32["clocks"],
             "cpu_baseline": cpu,
+            "config1": c1,
             "batched": batched,
             "serving": serving,
         }

@@ -14,11 +14,12 @@
 // The field's phases are evaluated exactly in 32-bit fixed point (fractions
 // of a turn): for centroid lattice coordinates c (units of h/4) the phase is
 // phi + sum_d c_d theta_d modulo one turn, with theta_d = w_d h / 4 rounded to
-// 2^-32 turn, so no large argument reaches the cosine; the cosine, the sum
-// over features and exp run in FP32.  k then agrees with the FP64 host
-// generator to ~1e-6 relative.
+// 2^-32 turn, so no large argument reaches the sine and cosine; those, the
+// angle additions, the sum over features and exp run in FP32.  k then agrees
+// with the FP64 host generator to ~1e-6 relative.
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -90,30 +91,81 @@ int upload_constants(int device) {
 
 // k of every tetrahedron of a level with Nc cells per axis (element
 // ((z Nc + y) Nc + x) 6 + p); prm[m] = (phi, theta_x, theta_y, theta_z) in
-// 2^-32 turns, theta per h/4
+// 2^-32 turns, theta per h/4.  One thread per cell: the phase of feature m at
+// the centroid of tetrahedron p is the cell's phase (origin, 4 theta per cell
+// step) plus a fixed offset delta_{m,p} = (3 e_p0 + 2 e_p1 + e_p2).theta_m,
+// so each cell takes one sincos per feature and the six cosines follow by
+// angle addition with the offsets' cos / sin tabulated in shared memory.
 __global__ void __launch_bounds__(ABLK) cube_field_kernel(int Nc, const uint4 *__restrict__ prm, int M, float amp,
                                                           float *__restrict__ kelem) {
   __shared__ uint4 sp[GMG_FIELD_MAX_M];
-  for (int m = threadIdx.x; m < M; m += blockDim.x) sp[m] = prm[m];
-  __syncthreads();
-  const long long ne = 6LL * Nc * Nc * Nc;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
-    const int p = int(e % 6);
-    const long long cell = e / 6;
-    int c[3] = {int(cell % Nc) * 4, int((cell / Nc) % Nc) * 4, int(cell / ((long long)Nc * Nc)) * 4};
-    c[c_perm[p][0]] += 3;
-    c[c_perm[p][1]] += 2;
-    c[c_perm[p][2]] += 1;
-    float sum = 0.0f;
-    for (int m = 0; m < M; ++m) {
-      const uint32_t ph = sp[m].x + uint32_t(c[0]) * sp[m].y + uint32_t(c[1]) * sp[m].z + uint32_t(c[2]) * sp[m].w;
-      sum += cospif(__uint2float_rn(ph) * 4.656612873077392578125e-10f);  // cos(2 pi ph / 2^32)
+  __shared__ float2 sd[GMG_FIELD_MAX_M][6];  // (cos, sin) of delta_{m,p}
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const uint4 q = prm[m];
+    sp[m] = q;
+    const uint32_t th[3] = {q.y, q.z, q.w};
+    for (int p = 0; p < 6; ++p) {
+      const uint32_t d = 3u * th[c_perm[p][0]] + 2u * th[c_perm[p][1]] + th[c_perm[p][2]];
+      float sn, cs;
+      sincospif(__uint2float_rn(d) * 4.656612873077392578125e-10f, &sn, &cs);
+      sd[m][p] = make_float2(cs, sn);
     }
-    kelem[e] = expf(amp * sum);
+  }
+  __syncthreads();
+  const long long nc = (long long)Nc * Nc * Nc;
+  for (long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x; cell < nc;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const uint32_t cx = uint32_t(cell % Nc) * 4u, cy = uint32_t((cell / Nc) % Nc) * 4u,
+                   cz = uint32_t(cell / ((long long)Nc * Nc)) * 4u;
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int m = 0; m < M; ++m) {
+      const uint32_t ph = sp[m].x + cx * sp[m].y + cy * sp[m].z + cz * sp[m].w;
+      float s0, c0;
+      sincospif(__uint2float_rn(ph) * 4.656612873077392578125e-10f, &s0, &c0);  // angle 2 pi ph / 2^32
+#pragma unroll
+      for (int p = 0; p < 6; ++p) g[p] += c0 * sd[m][p].x - s0 * sd[m][p].y;  // cos(ph + delta)
+    }
+#pragma unroll
+    for (int p = 0; p < 6; ++p) kelem[cell * 6 + p] = expf(amp * g[p]);
   }
 }
 
 __device__ __forceinline__ int lattice_code(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
+
+// the Kuhn tetrahedra as compile-time functions (kPerms above), so that the
+// unrolled assembly loops index the row accumulators with constants
+__host__ __device__ constexpr int kperm(int p, int k) {
+  return p == 0 ? k
+       : p == 1 ? (k == 0 ? 0 : k == 1 ? 2 : 1)
+       : p == 2 ? (k == 0 ? 1 : k == 1 ? 0 : 2)
+       : p == 3 ? (k == 0 ? 1 : k == 1 ? 2 : 0)
+       : p == 4 ? (k == 0 ? 2 : k == 1 ? 0 : 1)
+                : (k == 0 ? 2 : k == 1 ? 1 : 0);
+}
+// coordinate d of vertex t of tetrahedron p, relative to its cell's origin
+__host__ __device__ constexpr int tvert(int p, int t, int d) {
+  return t == 0 ? 0 : t == 3 ? 1 : t == 1 ? int(d == kperm(p, 0)) : int(d == kperm(p, 0) || d == kperm(p, 1));
+}
+// vertex of tetrahedron p at cell corner cc (bit d = coordinate d), or -1
+__host__ __device__ constexpr int tmatch(int p, int cc) {
+  return (tvert(p, 0, 0) == (cc & 1) && tvert(p, 0, 1) == ((cc >> 1) & 1) && tvert(p, 0, 2) == ((cc >> 2) & 1)) ? 0
+       : (tvert(p, 1, 0) == (cc & 1) && tvert(p, 1, 1) == ((cc >> 1) & 1) && tvert(p, 1, 2) == ((cc >> 2) & 1)) ? 1
+       : (tvert(p, 2, 0) == (cc & 1) && tvert(p, 2, 1) == ((cc >> 1) & 1) && tvert(p, 2, 2) == ((cc >> 2) & 1)) ? 2
+       : (tvert(p, 3, 0) == (cc & 1) && tvert(p, 3, 1) == ((cc >> 1) & 1) && tvert(p, 3, 2) == ((cc >> 2) & 1)) ? 3
+                                                                                                              : -1;
+}
+// lattice code of vertex t of tetrahedron p seen from the node at corner cc
+__host__ __device__ constexpr int tcode(int p, int t, int cc) {
+  return (tvert(p, t, 0) - (cc & 1) + 1) + 3 * (tvert(p, t, 1) - ((cc >> 1) & 1) + 1) +
+         9 * (tvert(p, t, 2) - ((cc >> 2) & 1) + 1);
+}
+
+__device__ __forceinline__ double pick27(const double (&acc)[27], int code) {
+  double v = 0.0;
+#pragma unroll
+  for (int t = 0; t < 27; ++t) v = code == t ? acc[t] : v;
+  return v;
+}
 
 // one slot's rows of one level
 __global__ void __launch_bounds__(ABLK) cube_assemble_kernel(
@@ -131,22 +183,16 @@ __global__ void __launch_bounds__(ABLK) cube_assemble_kernel(
   for (int t = 0; t < 27; ++t) acc[t] = 0.0;
   if (!bnd) {
     const int Nc = N - 1;
-    for (int cc = 0; cc < 8; ++cc) {
-      const int a[3] = {cc & 1, (cc >> 1) & 1, (cc >> 2) & 1};  // the node's corner in the cell
-      const long long cell = ((long long)(z - a[2]) * Nc + (y - a[1])) * Nc + (x - a[0]);
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) {  // the cells around the node; the node is their corner cc
+      const long long cell = ((long long)(z - ((cc >> 2) & 1)) * Nc + (y - ((cc >> 1) & 1))) * Nc + (x - (cc & 1));
+#pragma unroll
       for (int p = 0; p < 6; ++p) {
-        // vertices relative to the cell origin: 0, e_p0, e_p0 + e_p1, (1,1,1)
-        int V[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {1, 1, 1}};
-        V[1][c_perm[p][0]] = 1;
-        V[2][c_perm[p][0]] = 1;
-        V[2][c_perm[p][1]] = 1;
-        int m = -1;
-        for (int t = 0; t < 4; ++t)
-          if (V[t][0] == a[0] && V[t][1] == a[1] && V[t][2] == a[2]) m = t;
+        const int m = tmatch(p, cc);
         if (m < 0) continue;
         const double ke = kelem ? double(kelem[cell * 6 + p]) : 1.0;
-        for (int t = 0; t < 4; ++t)
-          acc[lattice_code(V[t][0] - a[0], V[t][1] - a[1], V[t][2] - a[2])] += ke * c_kref[p][m * 4 + t];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) acc[tcode(p, t, cc)] += ke * c_kref[p][m * 4 + t];
       }
     }
   }
@@ -156,7 +202,7 @@ __global__ void __launch_bounds__(ABLK) cube_assemble_kernel(
       v = k == rowptr[i] ? 1.0 : 0.0;
     } else {
       const int jc = perm[col[k]] - off;
-      v = h * acc[lattice_code(jc % N - x, (jc / N) % N - y, jc / (N * N) - z)];
+      v = h * pick27(acc, lattice_code(jc % N - x, (jc / N) % N - y, jc / (N * N) - z));
     }
     v64[k] = v;
     v32[k] = float(v);
@@ -184,21 +230,25 @@ __global__ void __launch_bounds__(ABLK) cube_rhs_kernel(int nrows, const int *__
   x[i] = 0.0;
 }
 
-// per-component norms of b over the slot's NEW_DEFECT rows (one block, fixed order)
+// per-component norms of b over the slot's NEW_DEFECT rows: a fixed grid of
+// blocks writes partial sums, the block that draws the last ticket adds them
+// in block order (deterministic), writes the norms and resets the ticket
 template <int S>
 __global__ void __launch_bounds__(ABLK) slot_norm_kernel(int nrows, const int *__restrict__ rows,
                                                          const uint8_t *__restrict__ flags,
-                                                         const double *__restrict__ b, double *__restrict__ out) {
+                                                         const double *__restrict__ b, double *__restrict__ partial,
+                                                         unsigned *__restrict__ ticket, double *__restrict__ out) {
   double acc[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = 0.0;
-  for (int q = threadIdx.x; q < nrows; q += blockDim.x) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nrows; q += gridDim.x * blockDim.x) {
     const int i = rows[q];
     if (!(flags[i] & F_NEWDEF)) continue;
 #pragma unroll
     for (int r = 0; r < S; ++r) acc[r] = fma(b[(size_t)i * S + r], b[(size_t)i * S + r], acc[r]);
   }
   __shared__ double sh[ABLK / 32][S];
+  __shared__ bool last;
 #pragma unroll
   for (int r = 0; r < S; ++r) {
     double v = acc[r];
@@ -209,8 +259,20 @@ __global__ void __launch_bounds__(ABLK) slot_norm_kernel(int nrows, const int *_
   if (threadIdx.x < S) {
     double v = 0.0;
     for (int w = 0; w < ABLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * S + threadIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (unsigned k = 0; k < gridDim.x; ++k) v += __ldcg(partial + (size_t)k * S + threadIdx.x);
     out[threadIdx.x] = sqrt(v);
   }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
 unsigned grid_of(long long n) { return unsigned((n + ABLK - 1) / ABLK); }
@@ -248,8 +310,8 @@ void cube_field_params(uint64_t seed, double corr, double var, int level, std::v
 int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem) {
   GMG_CHECK(M <= GMG_FIELD_MAX_M, "field with %d features (at most %d)", M, GMG_FIELD_MAX_M);
   if (upload_constants(mg->device)) return 1;
-  const long long ne = 6LL * Nc * Nc * Nc;
-  const unsigned g = unsigned(std::min<long long>((ne + ABLK - 1) / ABLK, 152LL * 16));
+  const long long nc = (long long)Nc * Nc * Nc;
+  const unsigned g = unsigned(std::min<long long>((nc + ABLK - 1) / ABLK, 152LL * 8));
   cube_field_kernel<<<g, ABLK, 0, mg->stream>>>(Nc, reinterpret_cast<const uint4 *>(prm_dev), M, amp, kelem);
   ACHECK(mg);
   return 0;
@@ -274,11 +336,14 @@ int k_cube_rhs(gmg_mg *mg, const Level &L, const SlotLevel &sl, uint64_t seed, d
   return 0;
 }
 
-int k_slot_norm(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *b, double *out) {
+int k_slot_norm(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *b, double *scratch, double *out) {
+  // scratch: SLOT_NORM_BLOCKS * GMG_MAX_S partial sums, then the ticket
+  const int nb = int(std::min<long long>(SLOT_NORM_BLOCKS, std::max(1, (sl.nrows + ABLK - 1) / ABLK)));
+  unsigned *ticket = reinterpret_cast<unsigned *>(scratch + SLOT_NORM_BLOCKS * GMG_MAX_S);
   switch (L.s) {
-    case 1: slot_norm_kernel<1><<<1, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, out); break;
-    case 2: slot_norm_kernel<2><<<1, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, out); break;
-    case 3: slot_norm_kernel<3><<<1, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, out); break;
+    case 1: slot_norm_kernel<1><<<nb, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, scratch, ticket, out); break;
+    case 2: slot_norm_kernel<2><<<nb, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, scratch, ticket, out); break;
+    case 3: slot_norm_kernel<3><<<nb, ABLK, 0, mg->stream>>>(sl.nrows, sl.rows, L.flags, b, scratch, ticket, out); break;
     default: set_error("block size %d not compiled", L.s); return 1;
   }
   ACHECK(mg);

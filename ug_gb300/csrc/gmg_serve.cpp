@@ -39,6 +39,7 @@ struct gmg_pool {
   uint32_t *prm_dev = nullptr, *prm_host = nullptr;  // field features, per slot and level
   size_t prm_stride = 0;                     // uint32 per slot
   double *first_dev = nullptr, *first_host = nullptr;
+  double *norm_scratch = nullptr;            // partial sums + ticket of the admission norm
   std::vector<int> state, iters, conv, need_first;
   std::vector<double> first, last;
   cudaEvent_t ev = nullptr;
@@ -52,6 +53,7 @@ struct gmg_pool {
     if (prm_dev) cudaFree(prm_dev);
     if (prm_host) cudaFreeHost(prm_host);
     if (first_dev) cudaFree(first_dev);
+    if (norm_scratch) cudaFree(norm_scratch);
     if (first_host) cudaFreeHost(first_host);
     if (mg) gmg_mg_destroy(mg);
     if (tmpl) gmg_gen_destroy(tmpl);
@@ -146,6 +148,8 @@ int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int 
   GMG_CUDA(cudaMallocHost(&P->prm_host, sizeof(uint32_t) * P->prm_stride * nslots));
   GMG_CUDA(cudaMalloc(&P->first_dev, sizeof(double) * GMG_MAX_S * nslots));
   GMG_CUDA(cudaMallocHost(&P->first_host, sizeof(double) * GMG_MAX_S * nslots));
+  GMG_CUDA(cudaMalloc(&P->norm_scratch, sizeof(double) * (SLOT_NORM_BLOCKS * GMG_MAX_S + 1)));
+  GMG_CUDA(cudaMemset(P->norm_scratch, 0, sizeof(double) * (SLOT_NORM_BLOCKS * GMG_MAX_S + 1)));
   GMG_CUDA(cudaEventCreateWithFlags(&P->ev, cudaEventDisableTiming));
   P->state.assign(nslots, SLOT_FREE);
   P->iters.assign(nslots, 0);
@@ -208,7 +212,8 @@ int gmg_pool_admit(gmg_pool *p, int k, unsigned long long seed, double corr, dou
   }
   const Level &T = mg->lev[top];
   if (k_cube_rhs(mg, T, p->sl[k][top], seed, (double *)p->b->lev[top], (double *)p->x->lev[top])) return 1;
-  if (k_slot_norm(mg, T, p->sl[k][top], (const double *)p->b->lev[top], p->first_dev + size_t(k) * GMG_MAX_S))
+  if (k_slot_norm(mg, T, p->sl[k][top], (const double *)p->b->lev[top], p->norm_scratch,
+                  p->first_dev + size_t(k) * GMG_MAX_S))
     return 1;
   GMG_CUDA(cudaMemcpyAsync(p->first_host + size_t(k) * GMG_MAX_S, p->first_dev + size_t(k) * GMG_MAX_S,
                            sizeof(double) * GMG_MAX_S, cudaMemcpyDeviceToHost, mg->stream));

@@ -29,7 +29,9 @@ int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, 
 int k_cube_assemble(gmg_mg *mg, const Level &L, const SlotLevel &sl, const float *kelem, double h, const int *c2s);
 // right-hand side of the slot (finest level), x = 0 there
 int k_cube_rhs(gmg_mg *mg, const Level &L, const SlotLevel &sl, uint64_t seed, double *b, double *x);
-// per-component norms of b over the slot's NEW_DEFECT rows into out[0..s)
-int k_slot_norm(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *b, double *out);
+// per-component norms of b over the slot's NEW_DEFECT rows into out[0..s);
+// scratch holds SLOT_NORM_BLOCKS * GMG_MAX_S doubles and a zeroed ticket
+constexpr int SLOT_NORM_BLOCKS = 304;
+int k_slot_norm(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *b, double *scratch, double *out);
 
 }  // namespace gmg
