@@ -307,6 +307,28 @@ def run_batched(args, stream, flush_l2, world, rank):
         torch.cuda.synchronize()
         if k >= args.warmup:
             dev_ms.append(a.elapsed_time(e))
+    # bandwidth of a large launch: FP32 dmatmul_minus on the deepest union
+    # level (1.7M rows), HBM-cold, CUDA events on the launching stream
+    nl, sl, nnzl = mg.size(top)
+    mg.createvector("rx32", "ry32", prec=G.FP32)
+    algo = nnzl * (4 + 4) + (nl + 1) * 4 + 3 * nl * 4
+    kts = []
+    for k in range(args.warmup + 10):
+        flush_l2()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        mg.dmatmul_minus(top, "rx32", "ry32")
+        e.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            kts.append(a.elapsed_time(e))
+    peak, peak_kind = measured_peak()
+    kms = float(np.mean(kts))
+    roof_large = {"bound": "hbm", "kernel": f"sell_spmv_kernel<float> on the deepest union level ({nl} rows, "
+                                            f"{nnzl} stored entries), HBM-cold",
+                  "achieved": algo / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                  "frac": algo / (kms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind, "algorithmic_bytes": int(algo),
+                  "launch_ms": kms}
     mg.close()
     dev_ms_max = reduce_over_ranks(float(np.mean(dev_ms)))
     # plain FP64 GPU path: one instance at a time, on a sample
@@ -341,6 +363,7 @@ def run_batched(args, stream, flush_l2, world, rank):
                                "sample": f"{len(sample)} instances solved one after another "
                                          f"({solo_per_s:.0f} instance solves/s), scaled to the batch by unknowns"},
         "mixed_batched_over_fp64_one_at_a_time": solo_batch_s / (ms32 * 1e-3),
+        "roofline_large_launch": roof_large,
         "h2d_bytes_per_batch": int(unknowns * 8), "d2h_bytes_per_batch": int(unknowns * 8),
     })
     if rank == 0:
