@@ -9,8 +9,8 @@ individual launch in the profiler's launch list.
 
 With --batched N: N instances of the batched workload (2D Q1 Poisson,
 levels 3..7, Jacobi V(2,2)) in one batched hierarchy instead.
-With --spmv: only the finest level's dmatmul_minus in FP32 (the bench's
-roofline kernel), --cycles times.
+With --spmv / --lgs: only the finest level's dmatmul_minus / Gauss-Seidel
+sweep (l_lgs, one launch per colour) in FP32, --cycles times.
 """
 import argparse
 
@@ -27,6 +27,7 @@ def main():
     ap.add_argument("--order", default="color", choices=["color", "list"])
     ap.add_argument("--bsmem", type=int, default=None)
     ap.add_argument("--spmv", action="store_true")
+    ap.add_argument("--lgs", action="store_true", help="only the finest level's FP32 Gauss-Seidel sweep (l_lgs)")
     ap.add_argument("--pool", type=int, default=0, help="one request in a one-slot serving pool of this depth")
     a = ap.parse_args()
     if a.pool:
@@ -41,14 +42,17 @@ def main():
         print(f"{a.cycles} pool iterations, depth {a.pool}")
         p.close()
         return
-    if a.spmv:
+    if a.spmv or a.lgs:
         gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
         mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
         mg.createvector("x32", "y32", prec=G.FP32)
         for _ in range(a.cycles):
-            mg.dmatmul_minus(mg.top, "x32", "y32")
+            if a.lgs:
+                mg.l_lgs(mg.top, "x32", "y32")
+            else:
+                mg.dmatmul_minus(mg.top, "x32", "y32")
         mg.sync()
-        print(f"{a.cycles} launches of dmatmul_minus on {mg.size(mg.top)}")
+        print(f"{a.cycles} {'l_lgs sweeps' if a.lgs else 'dmatmul_minus launches'} on {mg.size(mg.top)}")
         mg.close()
         return
     if a.batched:

@@ -206,6 +206,14 @@ class Server:
                 self.pools[L].append(Pool(L, nslots, smoother, red, maxit, device, st.cuda_stream))
         self.slots = {L: n * m for L, (n, m) in layout.items()}
 
+    def warm(self, seed: int = 1):
+        """One request through every pool: its first iteration allocates the
+        solver's temporaries and its second captures the iteration's CUDA
+        graph -- work that must not stall the event loop later."""
+        for pools in self.pools.values():
+            for p in pools:
+                p.solve(seed, self.corr, self.var)
+
     def run(self, requests: list[Request], keep_x: bool = False) -> ServeStats:
         pending = {L: [] for L in self.pools}
         order = sorted(requests, key=lambda r: r.arrival)
