@@ -231,6 +231,12 @@ int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const do
 int k_jac_step(gmg_mg *mg, const Level &L, int prec, void *bout, const void *bin, void *c, const double *damp);
 // forward Gauss-Seidel in processing order over the wavefronts; t is overwritten
 int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
+// `steps` multicolour Gauss-Seidel smoothing steps of lmgc (each: t = GS(b),
+// c += t, b -= A t) with the defect implicit between steps; b is the final
+// defect on return, t the last step's correction.  gs_chain_ok: the level
+// qualifies (sliced ELLPACK, colour-contiguous waves, every row ACTIVE)
+bool gs_chain_ok(const Level &L, int prec);
+int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps);
 // ILU forward / backward solve with the factors of L
 int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // coarse = (reset ? 0 : coarse) + R (damp*fine), honouring coarse VECSKIP

@@ -350,6 +350,108 @@ __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int 
   }
 }
 
+// ------------------------------------------------------------ chained Gauss-Seidel steps
+// nu multicolour Gauss-Seidel smoothing steps of lmgc (Step, dadd(c, t),
+// b -= A t each) with the defect kept implicit between steps: after a step
+// (D+L) t = b, so the new defect is b - A t = -U t.  Step 1 of a wave row i:
+// t_i = D_i^{-1}(b_i - sum_{j<i} a_ij t_j); later steps: t_i = D_i^{-1}(
+// -sum_{j != i} a_ij t_j), t updated in place (rows of earlier colours hold
+// the new t, later colours still the previous one); each step adds t to c.
+// After the last step sell_upper_defect_kernel writes b = -U t.  Exact in
+// real arithmetic; rounding differs from the step-by-step form.  Only for
+// all-ACTIVE levels, unit damping and colour-contiguous waves.
+template <class T, int S, bool FIRST, int PN>
+__global__ void __launch_bounds__(BLK) sell_gs_chain_kernel(int r0, int r1, const int *__restrict__ sptr,
+                                                            const int *__restrict__ scol, const T *__restrict__ sval,
+                                                            const T *__restrict__ dinv, const T *__restrict__ b,
+                                                            T *__restrict__ t, T *__restrict__ c) {
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  SellRow<T, S, PN> R;
+  T D[S * S];
+  R.load(i, sptr, scol, sval);
+#pragma unroll
+  for (int q = 0; q < S * S; ++q) D[q] = __ldg(dinv + (size_t)i * S * S + q);
+  pdl_wait_then_trigger();
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = FIRST ? b[(size_t)i * S + r] : T(0);
+#pragma unroll
+  for (int k = 1; k < PN; ++k) {
+    if (k < R.w && (FIRST ? R.col[k] < i : R.col[k] != i)) {
+#pragma unroll
+      for (int cc = 0; cc < S; ++cc) {
+        const T tv = t[(size_t)R.col[k] * S + cc];
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = fma(-R.val[k][r * S + cc], tv, s[r]);
+      }
+    }
+  }
+  int e = R.e0 + 32 * (PN > 1 ? PN : 1);
+#pragma unroll 4
+  for (int k = PN > 1 ? PN : 1; k < R.w; ++k, e += 32) {
+    const int j = __ldg(scol + e);
+    if (FIRST ? j >= i : j == i) continue;
+    const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+    for (int cc = 0; cc < S; ++cc) {
+      const T tv = t[(size_t)j * S + cc];
+#pragma unroll
+      for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + cc), tv, s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    T v = T(0);
+#pragma unroll
+    for (int cc = 0; cc < S; ++cc) v = fma(D[r * S + cc], s[cc], v);
+    t[(size_t)i * S + r] = v;
+    c[(size_t)i * S + r] += v;
+  }
+}
+
+// b = -U t: the defect after the last chained step (entries j > i)
+template <class T, int S, int PN>
+__global__ void __launch_bounds__(BLK) sell_upper_defect_kernel(int n, const int *__restrict__ sptr,
+                                                                const int *__restrict__ scol,
+                                                                const T *__restrict__ sval, const T *__restrict__ t,
+                                                                T *__restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  SellRow<T, S, PN> R;
+  R.load(i, sptr, scol, sval);
+  pdl_wait_then_trigger();
+  T s[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) s[r] = T(0);
+#pragma unroll
+  for (int k = 1; k < PN; ++k) {
+    if (k < R.w && R.col[k] > i) {
+#pragma unroll
+      for (int cc = 0; cc < S; ++cc) {
+        const T tv = t[(size_t)R.col[k] * S + cc];
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = fma(-R.val[k][r * S + cc], tv, s[r]);
+      }
+    }
+  }
+  int e = R.e0 + 32 * (PN > 1 ? PN : 1);
+#pragma unroll 4
+  for (int k = PN > 1 ? PN : 1; k < R.w; ++k, e += 32) {
+    const int j = __ldg(scol + e);
+    if (j <= i) continue;
+    const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+    for (int cc = 0; cc < S; ++cc) {
+      const T tv = t[(size_t)j * S + cc];
+#pragma unroll
+      for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + cc), tv, s[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < S; ++r) b[(size_t)i * S + r] = s[r];
+}
+
 // ------------------------------------------------------------ l_jac
 // ugiter.cc:271: t = D^{-1} b on ACTIVE rows (0 elsewhere), then the
 // smoother's dscalx by damp (iter.cc:836).  D^{-1} is stored per row.
@@ -1719,6 +1821,57 @@ int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     LAUNCH_CHECK(mg);
   }
   return 0;
+}
+
+template <class T, int S>
+int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
+  const T *sv = sell_val<T>(L), *dinv = dinv_of<T>(L);
+  for (int st = 0; st < steps; ++st) {
+    for (int w = 0; w < L.lower.nwave(); ++w) {
+      const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
+      if (r1 <= r0) continue;
+      const unsigned g = grid_for(r1 - r0);
+      const bool pre = g <= PREFETCH_MAX_BLOCKS;
+      if (st == 0 && pre)
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b,
+                   t, c);
+      else if (st == 0)
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b, t, c);
+      else if (pre)
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, false, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b,
+                   t, c);
+      else
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, false, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b, t,
+                   c);
+      LAUNCH_CHECK(mg);
+    }
+  }
+  const unsigned g = grid_for(L.n);
+  if (g <= PREFETCH_MAX_BLOCKS)
+    GMG_LAUNCH((sell_upper_defect_kernel<T, S, PF<S>::N>), g, BLK, L.n, L.sell_ptr, L.sell_col, sv, t, b);
+  else
+    GMG_LAUNCH((sell_upper_defect_kernel<T, S, 0>), g, BLK, L.n, L.sell_ptr, L.sell_col, sv, t, b);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+bool gs_chain_ok(const Level &L, int prec) {
+  return L.sell && L.waves_contiguous && L.all_active && (prec == GMG_PREC_FP64 || (L.sell_v32 && L.dinv32));
+}
+
+int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps) {
+  GMG_CHECK(gs_chain_ok(L, prec) && steps >= 1, "chained Gauss-Seidel steps need a colour-ordered SELL level");
+  if (prec == GMG_PREC_FP64) {
+    if (L.s == 1) return gs_chain<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+    if (L.s == 2) return gs_chain<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+    if (L.s == 3) return gs_chain<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+  } else {
+    if (L.s == 1) return gs_chain<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+    if (L.s == 2) return gs_chain<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+    if (L.s == 3) return gs_chain<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+  }
+  set_error("block size %d not compiled", L.s);
+  return 1;
 }
 
 int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {

@@ -270,6 +270,16 @@ int NPGs::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
   return k_gs(mg, mg->lev[level], x->prec, vlev(x, level), vlev(bv, level));
 }
 
+int NPGs::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result) {
+  if (check_level(mg, level)) return 1;
+  const Level &L = mg->lev[level];
+  bool unit = true;
+  for (int r = 0; r < L.s; ++r) unit = unit && damp[r] == 1.0;
+  if (!unit || steps < 2 || acc->prec != x->prec || bv->prec != x->prec || !gs_chain_ok(L, x->prec))
+    return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
+  return k_gs_chain(mg, L, x->prec, vlev(x, level), vlev(bv, level), vlev(acc, level), steps);
+}
+
 // ilu: ILUInit (iter.cc:5415) reads $beta (and $mindiag, unused by the decomposition)
 int NPIlu::Init(const Args &a) {
   for (double &d : beta) d = 0.0;

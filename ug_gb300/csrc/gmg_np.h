@@ -83,6 +83,9 @@ struct NPJac : NPSmoother {  // jac, iter.cc:894-942
 
 struct NPGs : NPSmoother {  // gs, iter.cc:974-1086
   int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
+  // on colour-ordered sliced-ELLPACK levels with unit damping: the steps
+  // chained, one launch per colour and step plus one for the final defect
+  int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result) override;
 };
 
 struct NPIlu : NPSmoother {  // ilu, iter.cc:5383-5524
