@@ -594,6 +594,119 @@ done:
   return rc ? rc : it;
 }
 
+/* ddotw ON_SURFACE, ugblas.cc:3023 (weights 1): per-component sums over the
+ * NEW_DEFECT vectors of the top level, then added component by component */
+static double ddotw(const orc_level *L, const double *x, const double *y) {
+  const int s = L->s;
+  double a[ORC_MAX_S] = {0};
+  for (int i = 0; i < L->n; ++i) {
+    if (L->vclass[i] < NEWDEF_CLASS) continue;
+    for (int r = 0; r < s; ++r) a[r] += x[(size_t)i * s + r] * y[(size_t)i * s + r];
+  }
+  double sum = 0.0;
+  for (int r = 0; r < s; ++r) sum += 1.0 * a[r];
+  return sum;
+}
+
+/* sc_eq, npscan.cc:1095 */
+static int sc_eq(const double *x, const double *y, double ac, int s) {
+  for (int i = 0; i < s; ++i)
+    if (x[i] < 0.0 || y[i] < 0.0 || fabs(x[i] - y[i]) > ac * sqrt(x[i] * y[i])) return 0;
+  return 1;
+}
+
+/* the preconditioner q = lmgc(d) on a scratch copy of d (Iter updates its defect) */
+static int precond(orc_ws *w, int top, double *q, const double *d, size_t len) {
+  double *bt = w->b[top];
+  memcpy(bt, d, sizeof(double) * len);
+  memset(w->c[top], 0, sizeof(double) * len);
+  int rc = lmgc(w, top);
+  memcpy(q, w->c[top], sizeof(double) * len);
+  return rc;
+}
+
+int orc_bcgs_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
+                   double *hist, int *converged) {
+  const int top = mg->nlevels - 1;
+  const int s = mg->lev[top].s;
+  const orc_level *T = &mg->lev[top];
+  const size_t len = (size_t)T->n * s;
+  orc_ws w;
+  double *scratch = (double *)calloc(len, sizeof(double));
+  int rc = ws_init(&w, mg, scratch), iters = 0;
+  double *r = (double *)calloc(len, sizeof(double)), *p = (double *)calloc(len, sizeof(double)),
+         *v = (double *)calloc(len, sizeof(double)), *sv = (double *)calloc(len, sizeof(double)),
+         *t = (double *)calloc(len, sizeof(double)), *q = (double *)calloc(len, sizeof(double));
+  *converged = 0;
+  if (rc) goto done;
+  {
+    double first[ORC_MAX_S], last[ORC_MAX_S], reach[ORC_MAX_S], old[ORC_MAX_S];
+    double alpha = 0.0, rho_new = 0.0, beta = 0.0, tt = 0.0, rho = 0.0, omega = 0.0;
+    int restart = 1, eq_count = 0, nh = 0;
+    for (int k = 0; k < s; ++k) old[k] = -1.0; /* BCGSPreProcess, ls.cc:1831 */
+    orc_matmul_minus(T, b, x);
+    orc_nrm2x(T, b, first);
+    if (hist) for (int k = 0; k < s; ++k) hist[k] = first[k];
+    for (int k = 0; k < s; ++k) { reach[k] = first[k] * red[k]; if (reach[k] == 0.0) reach[k] = red[k]; }
+    *converged = sc_cmp(first, abslimit, s);
+    /* BCGSSolver, ls.cc:1864-2062 (no restart index, weights 1) */
+    for (int i = 0; i < maxit; ++i) {
+      if (*converged) break;
+      if (restart) {
+        memset(p, 0, sizeof(double) * len);
+        memset(v, 0, sizeof(double) * len);
+        memcpy(r, b, sizeof(double) * len);
+        alpha = rho = omega = 1.0;
+        restart = 0;
+      }
+      rho_new = ddotw(T, b, r);
+      if (rho != 0.0 && omega != 0.0) beta = rho_new * alpha / rho / omega;
+      for (size_t k = 0; k < len; ++k) p[k] *= beta;
+      vadd(p, b, len);
+      { const double a = -beta * omega; for (size_t k = 0; k < len; ++k) p[k] += a * v[k]; }
+      if ((rc = precond(&w, top, q, p, len))) goto done;
+      matmul(T, v, q);
+      alpha = ddotw(T, v, r);
+      if (alpha != 0.0) alpha = rho_new / alpha;
+      for (size_t k = 0; k < len; ++k) x[k] += alpha * q[k];
+      ++iters;
+      memcpy(sv, b, sizeof(double) * len);
+      { const double a = -alpha; for (size_t k = 0; k < len; ++k) sv[k] += a * v[k]; }
+      orc_nrm2x(T, sv, last);
+      ++nh;
+      if (hist) for (int k = 0; k < s; ++k) hist[(size_t)nh * s + k] = last[k];
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) {
+        memcpy(b, sv, sizeof(double) * len);
+        *converged = 1;
+        break;
+      }
+      if ((rc = precond(&w, top, q, sv, len))) goto done;
+      matmul(T, t, q);
+      tt = ddotw(T, t, t);
+      omega = ddotw(T, sv, t);
+      if (tt != 0.0) omega /= tt;
+      for (size_t k = 0; k < len; ++k) x[k] += omega * q[k];
+      memcpy(b, sv, sizeof(double) * len);
+      { const double a = -omega; for (size_t k = 0; k < len; ++k) b[k] += a * t[k]; }
+      rho = rho_new;
+      orc_nrm2x(T, b, last);
+      ++nh;
+      if (hist) for (int k = 0; k < s; ++k) hist[(size_t)nh * s + k] = last[k];
+      ++iters;
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) { *converged = 1; break; }
+      if (sc_eq(last, old, 1e-4, s)) eq_count++;
+      else eq_count = 0;
+      for (int k = 0; k < s; ++k) old[k] = last[k];
+      if (eq_count > 4) { *converged = 0; break; }
+    }
+  }
+done:
+  free(r); free(p); free(v); free(sv); free(t); free(q);
+  ws_free(&w);
+  free(scratch);
+  return rc ? rc : iters;
+}
+
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
                  double *hist, int *converged) {
   const int top = mg->nlevels - 1;

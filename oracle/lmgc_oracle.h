@@ -75,6 +75,10 @@ void orc_interpolate(const orc_level *fine, double *to_fine, const double *from_
  * CGUpdate in LinearSolver's loop) preconditioned by lmgc. */
 int orc_cg_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
                  double *hist, int *converged);
+/* ... and with UG's bcgs (ls.cc:1711-2062, BiCGStab with the lmgc preconditioner,
+ * two half steps per iteration, each counted; hist holds one entry per half step). */
+int orc_bcgs_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
+                   double *hist, int *converged);
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit,
                  int maxit, double *hist, int *converged);
 

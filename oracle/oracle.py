@@ -90,7 +90,9 @@ def lib():
         L.orc_interpolate.argtypes = [P, P, P, P]
         L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_cg_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
-        for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve", "orc_cg_solve"):
+        L.orc_bcgs_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve", "orc_cg_solve",
+                  "orc_bcgs_solve"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -180,6 +182,12 @@ class Hierarchy:
         lib().orc_interpolate(self.lev(l), _p(to), _p(fr), _p(dm)); return to
 
     # ---- solver
+    def bcgs_solve(self, rhs, **kw):
+        """bcgs (ls.cc:1711-2062) preconditioned by lmgc, configured as ls_solve;
+        iterations count half steps, as UG's.  Returns (x, iterations, converged,
+        history)."""
+        return self.ls_solve(rhs, _solver="bcgs", **kw)
+
     def cg_solve(self, rhs, **kw):
         """cg (ls.cc:901-1064) preconditioned by lmgc, configured as ls_solve.
         Returns (x, iterations, converged, history)."""
@@ -205,9 +213,9 @@ class Hierarchy:
         b = np.array(rhs, np.float64)
         redv = np.resize(np.asarray(red, np.float64), MAX_S)
         absv = np.resize(np.asarray(abslimit, np.float64), MAX_S)
-        hist = np.zeros((maxit + 1) * s)
+        hist = np.zeros((2 * maxit + 1) * s)
         conv = C.c_int(0)
-        f = lib().orc_cg_solve if _solver == "cg" else lib().orc_ls_solve
+        f = {"cg": lib().orc_cg_solve, "bcgs": lib().orc_bcgs_solve}.get(_solver, lib().orc_ls_solve)
         it = f(C.byref(mg), _p(x), _p(b), _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
         if it < 0:
             raise RuntimeError(f"oracle {_solver} failed: {it}")

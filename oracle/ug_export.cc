@@ -19,7 +19,9 @@
 //     (NP_LINEAR_SOLVER, ls.cc:637): iteration count, first/last defect and
 //     the final solution, plus the per-iteration defect history obtained by
 //     replaying the ls loop (dset, Lmgc, dadd, dnrm2x) through the same
-//     numprocs.
+//     numprocs;
+//   * the same problem solved with UG's cg and bcgs (ls.cc:901, 1711)
+//     preconditioned by the same lmgc: iterations, defects, solution.
 //
 // usage: ug_export{2d,3d} <problem> <nref> <baselevel> <smoother> <seed> <out>
 //        [maxit] [local_levels]
@@ -437,6 +439,8 @@ int main(int argc, char **argv) {
     }
     putd("ls_hist", hist);
     putd("ls_x_replay", grab(sol, top));
+    // releases what the smoothers allocated (the ILU factor matrix)
+    (*ls->PostProcess)(ls, top, sol, rhs, A, &res);
   }
 
   // ---- UG's cg (ls.cc:901-1165) preconditioned by the same lmgc, from x = 0
@@ -465,6 +469,35 @@ int main(int argc, char **argv) {
     putd("cg_x", grab(sol, top));
     fprintf(stderr, "UG cg: iters=%d converged=%d last=%.6e\n", (int)lc.number_of_linear_iterations, (int)lc.converged,
             lc.last_defect[0]);
+    (*cg->PostProcess)(cg, top, sol, rhs, A, &res);
+  }
+
+  // ---- UG's bcgs (ls.cc:1711-2062) preconditioned by the same lmgc, from x = 0
+  {
+    for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
+    for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
+    int i = 0;
+    for (VECTOR *v : g_lev[top].vecs) for (int c = 0; c < s; ++c) VVALUE(v, vcmp(rhs)[c]) = rhs_top[i++];
+    snprintf(cmd, sizeof cmd,
+             "npcreate bcgs $c bcgs; npinit bcgs $A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m %d $I lmgc;", maxit);
+    run(cmd);
+    NP_LINEAR_SOLVER *bs = (NP_LINEAR_SOLVER *)GetNumProcByName(mg, "bcgs", LINEAR_SOLVER_CLASS_NAME);
+    if (!bs) { fprintf(stderr, "bcgs lookup failed\n"); return 1; }
+    LRESULT lb;
+    memset(&lb, 0, sizeof lb);
+    if ((*bs->PreProcess)(bs, top, sol, rhs, A, &bl, &res)) { fprintf(stderr, "bcgs PreProcess failed\n"); return 1; }
+    (*bs->Defect)(bs, top, sol, rhs, A, &res);
+    (*bs->Residuum)(bs, bl, top, sol, rhs, A, &lb);
+    if ((*bs->Solver)(bs, top, sol, rhs, A, bs->abslimit, bs->reduction, &lb)) {
+      fprintf(stderr, "bcgs Solver failed\n");
+      return 1;
+    }
+    put1i("bcgs_iters", lb.number_of_linear_iterations); put1i("bcgs_converged", lb.converged);
+    putd("bcgs_first", std::vector<double>(lb.first_defect, lb.first_defect + s));
+    putd("bcgs_last", std::vector<double>(lb.last_defect, lb.last_defect + s));
+    putd("bcgs_x", grab(sol, top));
+    fprintf(stderr, "UG bcgs: iters=%d converged=%d last=%.6e\n", (int)lb.number_of_linear_iterations,
+            (int)lb.converged, lb.last_defect[0]);
   }
   (*ls->PostProcess)(ls, top, sol, rhs, A, &res);
   fclose(g_out);

@@ -5,8 +5,8 @@ $REF, default /root/reference), runs oracle/_ref/ug_export{2d,3d} for each
 case below and stores every record as a compressed .npz.  Each fixture holds
 the hierarchy exactly as UG's grid manager and assembly produced it, the
 known-answer vectors of UG's kernels on the finest level, and UG's own ls +
-lmgc solve (iteration count, defect history, solution) and cg + lmgc solve
-(iteration count, defects, solution).
+lmgc solve (iteration count, defect history, solution) and its cg + lmgc and
+bcgs + lmgc solves (iteration count, defects, solution).
 
     python tests/golden/make_golden.py
 """

@@ -56,3 +56,18 @@ def test_cg_matches_ug(name, oracle_mod):
     assert conv == bool(fx["cg_converged"][0]) and it == int(fx["cg_iters"][0])
     assert rel(x, fx["cg_x"]) <= 1e-12
     assert rel(hist[-1], fx["cg_last"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_bcgs_matches_ug(name, oracle_mod):
+    """UG's bcgs (np/procs/ls.cc:1711-2062) preconditioned by the same lmgc:
+    the oracle takes UG's (half-step) iteration count and reaches UG's
+    solution."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    sm = fx["smoother"]
+    x, it, conv, hist = H.bcgs_solve(fx["rhs"], smoother=sm, baselevel=int(fx["baselevel"][0]),
+                                     damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50)
+    assert conv == bool(fx["bcgs_converged"][0]) and it == int(fx["bcgs_iters"][0])
+    assert rel(x, fx["bcgs_x"]) <= 1e-12
+    assert rel(hist[-1], fx["bcgs_last"]) <= 1e-10
