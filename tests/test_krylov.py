@@ -1,8 +1,8 @@
-"""cg preconditioned by lmgc (np/procs/ls.cc:901-1064) on the device: the
-`gcg` numproc against UG's own cg solves (tests/golden: cg_iters, cg_x) in
-UG's vector order, against the oracle's cg on the reordered hierarchy in
-multicolour order, and its FP32-preconditioner variant against the FP64
-stopping test.  Tolerances: iterations equal (+-1 allowed by the contract),
+"""Krylov solvers preconditioned by lmgc on the device: `gcg` (UG's cg,
+np/procs/ls.cc:901-1064) and `gbcgs` (UG's bcgs, ls.cc:1711-2062) against
+UG's own solves (tests/golden: cg_* / bcgs_*) in UG's vector order, against
+the oracle's cg / bcgs on the reordered hierarchy in multicolour order, and
+their FP32-preconditioner variants against the FP64 stopping test.  Tolerances: iterations equal (+-1 allowed by the contract),
 solution 1e-10 relative (jac) / 1e-8 (gs, ilu; order-dependent smoothers)."""
 import numpy as np
 import pytest
@@ -66,4 +66,51 @@ def test_cg_vs_oracle_midsize(G, oracle_mod, order, sm):
     xr = np.empty_like(xo); xr[perm] = xo
     assert conv and lr.converged and abs(lr.iters - ito) <= 1
     assert rel(x, xr) <= (1e-10 if sm == "jac" else 1e-8)
+    mg.close()
+
+
+def _setup_bcgs(G, mg, sm, bl, red=1e-10, mixed=False, name="bcgs"):
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=0.8 if sm == "jac" else 1.0, red=red, abslimit=1e-50)
+    mg.npcreate(name, "linear_solver.gbcgs")
+    st = mg.npinit(name, f"$A MAT $x sol $b rhs $red {red} $abslimit 1e-50 $m 100 $I lmgc $mixed {int(mixed)}")
+    assert st == G.NP_EXECUTABLE
+    return name
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_bcgs_matches_ug(G, name):
+    """bcgs (ls.cc:1711-2062) with the lmgc preconditioner against UG's own
+    bcgs solves: half-step iteration counts +-1, UG's solution."""
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    mg = G.MultiGrid(levels, order=G.ORDER_LIST, fp32=True)
+    sm, bl = fx["smoother"], int(fx["baselevel"][0])
+    _setup_bcgs(G, mg, sm, bl)
+    x, lr = mg.solve_host("bcgs", fx["rhs"])
+    assert lr.converged and abs(lr.iters - int(fx["bcgs_iters"][0])) <= 1
+    assert rel(x, fx["bcgs_x"]) <= (1e-10 if sm == "jac" else 1e-8)
+    mg.npcreate("bcgs32", "linear_solver.gbcgs")
+    mg.npinit("bcgs32", "$A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    x32, lr32 = mg.solve_host("bcgs32", fx["rhs"])
+    assert lr32.converged and lr32.iters <= int(fx["bcgs_iters"][0]) + 4
+    assert rel(x32, fx["bcgs_x"]) <= 1e-6
+    mg.close()
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_bcgs_gs_vs_oracle_midsize(G, oracle_mod, order):
+    """3D P1 diffusion 17^3, k = exp(g), with the (nonsymmetric) Gauss-Seidel
+    V-cycle, where cg stagnates: device bcgs vs the oracle's bcgs on the same
+    (possibly reordered) hierarchy."""
+    gen = G.Generator(1, 4, seed=5, corr=0.1, var=1.0)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=order, fp32=True)
+    _setup_bcgs(G, mg, "gs", 0)
+    x, lr = mg.solve_host("bcgs", gen.rhs)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    perm = mg.order(mg.top)
+    xo, ito, conv, _ = H.bcgs_solve(gen.rhs[perm], smoother="gs", baselevel=0, red=1e-10, abslimit=1e-50)
+    xr = np.empty_like(xo); xr[perm] = xo
+    assert conv and lr.converged and abs(lr.iters - ito) <= 1
+    assert rel(x, xr) <= 1e-8
     mg.close()

@@ -269,6 +269,17 @@ int k_cg_dot(gmg_mg *mg, const Level &L, const double *x, const double *y, doubl
 int k_cg_p(gmg_mg *mg, long long len, double *p, const double *c, const double *sc);
 int k_cg_xb(gmg_mg *mg, long long len, double *x, const double *p, double *b, const double *tn, const double *sc);
 int k_sub(gmg_mg *mg, long long len, double *b, const double *t);
+// bcgs (FP64 vectors, scalars on the device in sc[]; see gmg_kernels.cu):
+// ddotw with the step's scalar update (mode 0 rho, 1 alpha, 2 tt, 3 omega),
+// p = beta p + b + beta omega vn, x += alpha q with s = b + alpha vn, the
+// half-step test of mg->norms_dev against th, x += omega q with b = s + omega tn
+int k_bcgs_dot(gmg_mg *mg, const Level &L, const double *x, const double *y, double *sc, int mode, double sign);
+int k_bcgs_p(gmg_mg *mg, long long len, double *p, const double *b, const double *vn, const double *sc);
+int k_bcgs_xs(gmg_mg *mg, long long len, double *x, const double *q, const double *b, double *sv, const double *vn,
+              const double *sc);
+int k_bcgs_half_test(gmg_mg *mg, int s, const double *th, double *sc);
+int k_bcgs_xb(gmg_mg *mg, long long len, double *x, const double *q, double *b, const double *sv, const double *tn,
+              const double *sc);
 // the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
 struct CoarseCfg {
   int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;

@@ -1042,6 +1042,137 @@ __global__ void sub_kernel(long long len, double *__restrict__ b, const double *
     b[i] = __dsub_rn(b[i], t[i]);
 }
 
+// ------------------------------------------------------------ bcgs (ls.cc:1864-2062)
+// ddotw (ugblas.cc:3023, weights 1): per-component FP64 sums over the NEW_DEFECT
+// rows, deterministic last-block reduction, then the components added in
+// order; the last block also does the step's scalar work on sc[]:
+//   RHO:   rho_new = d; beta = rho_new alpha / rho / omega if rho, omega != 0
+//   ALPHA: a = sign d; alpha = a != 0 ? rho_new / a : a
+//   TT:    tt = d
+//   OMEGA: o = sign d; omega = tt != 0 ? o / tt : o; rho = rho_new
+enum { BC_RHO = 0, BC_RHONEW = 1, BC_ALPHA = 2, BC_BETA = 3, BC_OMEGA = 4, BC_TT = 5, BC_HALF = 6 };
+enum { BM_RHO = 0, BM_ALPHA = 1, BM_TT = 2, BM_OMEGA = 3 };
+template <int S, bool ALL, int MODE>
+__global__ void __launch_bounds__(BLK) bcgs_dot_kernel(int n, const double *__restrict__ x, const double *__restrict__ y,
+                                                       const uint8_t *__restrict__ flags, double *__restrict__ partial,
+                                                       unsigned *__restrict__ ticket, double *__restrict__ sc,
+                                                       double sign) {
+  pdl_prologue();
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!ALL && !(flags[i] & F_NEWDEF)) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc[r] = fma(x[(size_t)i * S + r], y[(size_t)i * S + r], acc[r]);
+  }
+  __shared__ double sh[BLK / 32][S];
+  __shared__ bool last;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * S + threadIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[S][BLK];
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(partial + (size_t)b * S + r);
+    red[r][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int r = 0; r < S; ++r) red[r][threadIdx.x] += red[r][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double d = 0.0;
+    for (int r = 0; r < S; ++r) d += 1.0 * red[r][0];
+    if (MODE == BM_RHO) {
+      sc[BC_RHONEW] = d;
+      if (sc[BC_RHO] != 0.0 && sc[BC_OMEGA] != 0.0) sc[BC_BETA] = d * sc[BC_ALPHA] / sc[BC_RHO] / sc[BC_OMEGA];
+    } else if (MODE == BM_ALPHA) {
+      const double a = sign * d;
+      sc[BC_ALPHA] = a != 0.0 ? sc[BC_RHONEW] / a : a;
+    } else if (MODE == BM_TT) {
+      sc[BC_TT] = d;
+    } else {
+      const double o = sign * d;
+      sc[BC_OMEGA] = sc[BC_TT] != 0.0 ? o / sc[BC_TT] : o;
+      sc[BC_RHO] = sc[BC_RHONEW];
+    }
+    *ticket = 0u;
+  }
+}
+
+// p = beta p; p += b; p += (-beta omega) v, with vn = -v (three UG passes)
+__global__ void bcgs_p_kernel(long long len, double *__restrict__ p, const double *__restrict__ b,
+                              const double *__restrict__ vn, const double *__restrict__ sc) {
+  pdl_prologue();
+  const double beta = sc[BC_BETA], a = beta * sc[BC_OMEGA];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    p[i] = __dadd_rn(__dadd_rn(__dmul_rn(beta, p[i]), b[i]), __dmul_rn(a, vn[i]));
+}
+
+// x += alpha q; s = b; s += (-alpha) v, with vn = -v
+__global__ void bcgs_xs_kernel(long long len, double *__restrict__ x, const double *__restrict__ q,
+                               const double *__restrict__ b, double *__restrict__ sv, const double *__restrict__ vn,
+                               const double *__restrict__ sc) {
+  pdl_prologue();
+  const double a = sc[BC_ALPHA];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    x[i] = __dadd_rn(x[i], __dmul_rn(a, q[i]));
+    sv[i] = __dadd_rn(b[i], __dmul_rn(a, vn[i]));
+  }
+}
+
+// the convergence test after the first half step, on the device: sc_cmp of
+// the norms of s against abslimit or the reduction target (th[0..s), th[8..8+s))
+__global__ void bcgs_half_test_kernel(int s, const double *__restrict__ norms, const double *__restrict__ th,
+                                      double *__restrict__ sc) {
+  pdl_prologue();
+  if (threadIdx.x != 0) return;
+  bool a = true, r = true;
+  for (int k = 0; k < s; ++k) {
+    if (fabs(norms[k]) >= fabs(th[k])) a = false;
+    if (fabs(norms[k]) >= fabs(th[GMG_MAX_S + k])) r = false;
+  }
+  sc[BC_HALF] = (a || r) ? 1.0 : 0.0;
+}
+
+// second half: x += omega q; b = s; b += (-omega) t, with tn = -t -- or, when
+// the first half already met the test, b = s (UG's break after dcopy(b, s))
+__global__ void bcgs_xb_kernel(long long len, double *__restrict__ x, const double *__restrict__ q,
+                               double *__restrict__ b, const double *__restrict__ sv, const double *__restrict__ tn,
+                               const double *__restrict__ sc) {
+  pdl_prologue();
+  const bool half = sc[BC_HALF] != 0.0;
+  const double o = sc[BC_OMEGA];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    if (half) {
+      b[i] = sv[i];
+    } else {
+      x[i] = __dadd_rn(x[i], __dmul_rn(o, q[i]));
+      b[i] = __dadd_rn(sv[i], __dmul_rn(o, tn[i]));
+    }
+  }
+}
+
 // ------------------------------------------------------------ batched ls
 // The end of one ls iteration of a batched hierarchy, over the rows of every
 // instance on its own finest level (all top levels in one launch):
@@ -2020,6 +2151,53 @@ int k_cg_xb(gmg_mg *mg, long long len, double *x, const double *p, double *b, co
 
 int k_sub(gmg_mg *mg, long long len, double *b, const double *t) {
   GMG_LAUNCH(sub_kernel, vec_grid(len), BLK, len, b, t);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_bcgs_dot(gmg_mg *mg, const Level &L, const double *x, const double *y, double *sc, int mode, double sign) {
+  unsigned *ticket = reinterpret_cast<unsigned *>(mg->norms_dev + GMG_MAX_S);
+  const bool all = L.all_active;
+#define BD(SS, A, M) GMG_LAUNCH((bcgs_dot_kernel<SS, A, M>), REDUCE_BLOCKS, BLK, L.n, x, y, L.flags, mg->partial, ticket, sc, sign)
+#define BM(SS, A)                                                                        \
+  switch (mode) {                                                                        \
+    case 0: BD(SS, A, 0); break;                                                         \
+    case 1: BD(SS, A, 1); break;                                                         \
+    case 2: BD(SS, A, 2); break;                                                         \
+    default: BD(SS, A, 3); break;                                                        \
+  }
+#define BA(SS) if (all) { BM(SS, true) } else { BM(SS, false) }
+  if (L.s == 1) { BA(1) } else if (L.s == 2) { BA(2) } else if (L.s == 3) { BA(3) }
+  else { set_error("block size %d not compiled", L.s); return 1; }
+#undef BA
+#undef BM
+#undef BD
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_bcgs_p(gmg_mg *mg, long long len, double *p, const double *b, const double *vn, const double *sc) {
+  GMG_LAUNCH(bcgs_p_kernel, vec_grid(len), BLK, len, p, b, vn, sc);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_bcgs_xs(gmg_mg *mg, long long len, double *x, const double *q, const double *b, double *sv, const double *vn,
+              const double *sc) {
+  GMG_LAUNCH(bcgs_xs_kernel, vec_grid(len), BLK, len, x, q, b, sv, vn, sc);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_bcgs_half_test(gmg_mg *mg, int s, const double *th, double *sc) {
+  GMG_LAUNCH(bcgs_half_test_kernel, 1, 32, s, mg->norms_dev, th, sc);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_bcgs_xb(gmg_mg *mg, long long len, double *x, const double *q, double *b, const double *sv, const double *tn,
+              const double *sc) {
+  GMG_LAUNCH(bcgs_xb_kernel, vec_grid(len), BLK, len, x, q, b, sv, tn, sc);
   LAUNCH_CHECK(mg);
   return 0;
 }

@@ -1195,6 +1195,159 @@ int NPCg::check_iteration(int i) {
   return 0;
 }
 
+// ------------------------------------------------------------ bcgs
+enum { BC_RHO = 0, BC_RHONEW = 1, BC_ALPHA = 2, BC_BETA = 3, BC_OMEGA = 4, BC_TT = 5, BC_HALF = 6 };
+
+NPBcgs::~NPBcgs() {
+  if (sc) cudaFree(sc);
+  if (th) cudaFree(th);
+  if (half_host) cudaFreeHost(half_host);
+}
+
+int NPBcgs::Init(const Args &a) {  // BCGSInit: $R restart index (>= 0)
+  if (!a.get_int("R", &restart)) restart = 0;
+  if (restart < 0) return NP_NOT_ACTIVE;
+  return NPLs::Init(a);
+}
+
+std::string NPBcgs::Display() const {
+  std::ostringstream o;
+  o << NPLs::Display() << "R = " << restart << "\n";
+  return o.str();
+}
+
+// q = M^{-1} d with the preconditioner `$I`, which updates the defect it is
+// given: it works on a copy (BCGSSolver saves and restores d around Iter)
+int NPBcgs::precond(int level, gmg_vec *qv, gmg_vec *dv, gmg_mat *Am, int *err) {
+  const long long len = vlen(mg, level);
+  if (!mixed) {
+    if (k_copy(mg, GMG_PREC_FP64, vlev(pc, level), vlev(dv, level), len) ||
+        k_set(mg, GMG_PREC_FP64, vlev(qv, level), len, 0.0))
+      return 1;
+    return IterNp->Iter(level, qv, pc, Am, err);
+  }
+  if (k_refine_prepare(mg, (float *)vlev(b32, level), (float *)vlev(cvec, level), (const double *)vlev(dv, level), len))
+    return 1;
+  if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+  return k_convert(mg, GMG_PREC_FP64, vlev(qv, level), GMG_PREC_FP32, vlev(cvec, level), len);
+}
+
+// BCGSSolver's loop body (ls.cc:1904-2020) from the restart check on
+int NPBcgs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const Level &L = mg->lev[level];
+  const long long len = vlen(mg, level);
+  double *b = (double *)vlev(bv, level), *x = (double *)vlev(xv, level);
+  double *P = (double *)vlev(p, level), *R = (double *)vlev(r, level), *V = (double *)vlev(vn, level),
+         *S = (double *)vlev(sv, level), *Tn = (double *)vlev(tn, level), *Q = (double *)vlev(q, level);
+  // rho_new = (b, r); beta; p = beta p + b - beta omega v
+  if (k_bcgs_dot(mg, L, b, R, sc, 0, 1.0) || k_bcgs_p(mg, len, P, b, V, sc)) return 1;
+  // q = M^{-1} p; v = A q (kept as -A q); alpha = rho_new / (v, r); x += alpha q; s = b - alpha v
+  if (precond(level, q, p, Am, err)) return 1;
+  if (k_set(mg, GMG_PREC_FP64, V, len, 0.0) || k_matmul_minus(mg, L, GMG_PREC_FP64, V, Q, nullptr)) return 1;
+  if (k_bcgs_dot(mg, L, V, R, sc, 1, -1.0) || k_bcgs_xs(mg, len, x, Q, b, S, V, sc)) return 1;
+  // |s| and the test after the first half step
+  if (k_nrm2x(mg, L, GMG_PREC_FP64, S) || k_bcgs_half_test(mg, L.s, th, sc)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(half_host, mg->norms_dev, sizeof(double) * GMG_MAX_S, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(half_host + GMG_MAX_S, sc + BC_HALF, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  // q = M^{-1} s; t = A q (kept as -A q); omega = (s, t) / (t, t); x += omega q; b = s - omega t
+  if (precond(level, q, sv, Am, err)) return 1;
+  if (k_set(mg, GMG_PREC_FP64, Tn, len, 0.0) || k_matmul_minus(mg, L, GMG_PREC_FP64, Tn, Q, nullptr)) return 1;
+  if (k_bcgs_dot(mg, L, Tn, Tn, sc, 2, 1.0) || k_bcgs_dot(mg, L, S, Tn, sc, 3, -1.0) ||
+      k_bcgs_xb(mg, len, x, Q, b, S, Tn, sc))
+    return 1;
+  if (k_nrm2x(mg, L, GMG_PREC_FP64, b)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
+  return 0;
+}
+
+static int sc_eq(const double *x, const double *y, double ac, int s) {  // npscan.cc:1095
+  for (int i = 0; i < s; ++i)
+    if (x[i] < 0.0 || y[i] < 0.0 || std::fabs(x[i] - y[i]) > ac * std::sqrt(x[i] * y[i])) return 0;
+  return 1;
+}
+
+// BCGSSolver, ls.cc:1864-2062 (weights 1)
+int NPBcgs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double *abs_, const double *red,
+                   gmg_lresult *lr) {
+  if (check_level(mg, level)) return 1;
+  GMG_CHECK(mg->batch.ninst == 0, "bcgs on a batched hierarchy is not supported (use ls)");
+  GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64, "bcgs: x and b must be FP64");
+  GMG_CHECK(!mixed || mg->opts.fp32_copy, "bcgs $mixed needs a hierarchy with FP32 copies");
+  const int s = mg->lev[level].s;
+  const long long len = vlen(mg, level);
+  for (int i = 0; i < GMG_MAX_S; ++i) { reduction[i] = red[i]; abslimit[i] = abs_[i]; }
+  if (prepare_temps(bv)) return 1;
+  gmg_vec **vs[7] = {&r, &p, &vn, &sv, &tn, &q, &pc};
+  const char *nm[7] = {"__r", "__p", "__v", "__s", "__t", "__q", "__pc"};
+  for (int k = 0; k < 7; ++k)
+    if (!*vs[k]) {
+      *vs[k] = temp_vec(mg, name + nm[k], GMG_PREC_FP64);
+      GMG_CHECK(*vs[k], "bcgs: temporary vectors");
+    }
+  if (!sc) {
+    GMG_CUDA(cudaMalloc(&sc, 8 * sizeof(double)));
+    GMG_CUDA(cudaMalloc(&th, 2 * GMG_MAX_S * sizeof(double)));
+    GMG_CUDA(cudaMallocHost(&half_host, (GMG_MAX_S + 1) * sizeof(double)));
+  }
+  double thr[2 * GMG_MAX_S] = {0}, old[GMG_MAX_S];
+  for (int i = 0; i < s; ++i) {
+    lr->first_defect[i] = lr->last_defect[i];
+    thr[i] = abs_[i];
+    thr[GMG_MAX_S + i] = lr->first_defect[i] * red[i];  // sc_mul_check, npscan.cc:1151
+    if (thr[GMG_MAX_S + i] == 0.0) thr[GMG_MAX_S + i] = red[i];
+    old[i] = -1.0;  // BCGSPreProcess: old_defect = -1
+  }
+  const double init[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // alpha = rho_new = beta = tt = 0
+  GMG_CUDA(cudaMemcpyAsync(sc, init, sizeof init, cudaMemcpyHostToDevice, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(th, thr, sizeof thr, cudaMemcpyHostToDevice, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  lr->converged = sc_cmp(lr->first_defect, abs_, s);
+  lr->number_of_linear_iterations = 0;
+  if (graph && (graph_level != level || graph_x != xv || graph_b != bv)) {
+    cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
+  int eq_count = 0, its = 0;
+  for (int i = 0; i < maxiter; ++i) {
+    if (lr->converged) break;
+    if ((restart > 0 && i % restart == 0) || i == 0) {  // p = v = 0, r = b, alpha = rho = omega = 1
+      if (k_set(mg, GMG_PREC_FP64, vlev(p, level), len, 0.0) || k_set(mg, GMG_PREC_FP64, vlev(vn, level), len, 0.0) ||
+          k_copy(mg, GMG_PREC_FP64, vlev(r, level), vlev(bv, level), len))
+        return 1;
+      GMG_CUDA(cudaMemcpyAsync(sc + BC_ALPHA, &scal_host[0], sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+      GMG_CUDA(cudaMemcpyAsync(sc + BC_RHO, &scal_host[1], sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+      GMG_CUDA(cudaMemcpyAsync(sc + BC_OMEGA, &scal_host[2], sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+    }
+    if (step(i, level, xv, bv, Am, lr)) return 1;
+    const double *h = half_host;
+    for (int k = 0; k < s; ++k)
+      GMG_CHECK(std::isfinite(h[k]), "bcgs: defect is not finite in iteration %d", i + 1);
+    ++its;
+    if (h[GMG_MAX_S] != 0.0) {  // the first half step met the test: b = s
+      for (int k = 0; k < s; ++k) lr->last_defect[k] = h[k];
+      lr->converged = 1;
+      break;
+    }
+    for (int k = 0; k < s; ++k) {
+      lr->last_defect[k] = mg->norms_host[k];
+      GMG_CHECK(std::isfinite(lr->last_defect[k]), "bcgs: defect is not finite in iteration %d", i + 1);
+    }
+    ++its;
+    if (sc_cmp(lr->last_defect, abs_, s) || sc_cmp(lr->last_defect, thr + GMG_MAX_S, s)) {
+      lr->converged = 1;
+      break;
+    }
+    eq_count = sc_eq(lr->last_defect, old, 1e-4, s) ? eq_count + 1 : 0;
+    for (int k = 0; k < s; ++k) old[k] = lr->last_defect[k];
+    if (eq_count > 4) {
+      lr->converged = 0;
+      break;
+    }
+  }
+  lr->number_of_linear_iterations = its;
+  return 0;
+}
+
 // ------------------------------------------------------------ class registry (CreateClass)
 static gmg_np *construct(const std::string &cls) {
   // the class name's last component selects the constructor (GetConstructor, numproc.cc:145)
@@ -1207,6 +1360,7 @@ static gmg_np *construct(const std::string &cls) {
   if (c == "gtransfer") return new NPTransfer;
   if (c == "gls") return new NPLs;
   if (c == "gcg") return new NPCg;
+  if (c == "gbcgs") return new NPBcgs;
   return nullptr;
 }
 

@@ -224,6 +224,26 @@ struct NPCg : NPLs {
   std::string Display() const override;
 };
 
+// bcgs, np/procs/ls.cc:1711-2062: BiCGStab preconditioned by `$I` (e.g.
+// lmgc, whose multicolour Gauss-Seidel V-cycle is not symmetric), two half
+// steps per iteration, each counted, with UG's stagnation test.  All scalars
+// and the half-step convergence test live on the device, so an iteration is
+// one captured graph; `$mixed 1` applies the preconditioner in FP32.
+struct NPBcgs : NPLs {
+  int restart = 0;
+  gmg_vec *r = nullptr, *p = nullptr, *vn = nullptr, *sv = nullptr, *tn = nullptr, *q = nullptr, *pc = nullptr;
+  double *sc = nullptr, *th = nullptr;  // device: scalars; abslimit and reduction target
+  double *half_host = nullptr;          // pinned: norms of s after the first half step, then the flag
+  double scal_host[3] = {1.0, 1.0, 1.0};  // restart values of alpha, rho, omega
+  ~NPBcgs() override;
+  int Init(const Args &a) override;  // BCGSInit, ls.cc:1750
+  int Solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit, const double *reduction,
+             gmg_lresult *lr) override;
+  int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err) override;
+  int precond(int level, gmg_vec *qv, gmg_vec *dv, gmg_mat *A, int *err);
+  std::string Display() const override;
+};
+
 // helpers shared by the numprocs and the C ABI
 gmg_vec *temp_vec(gmg_mg *mg, const std::string &name, int prec);
 void *vlev(gmg_vec *v, int level);
