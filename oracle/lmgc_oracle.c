@@ -368,6 +368,7 @@ void orc_interpolate(const orc_level *fine, double *to, const double *from, cons
 typedef struct {
   const orc_mg *mg;
   double **c, **t, **b, **lu; /* per level */
+  int *own_b;                 /* b of the level allocated here (not the caller's) */
   double *base_lu;            /* dense LU of the base level (no pivoting) */
   int base_n;
 } orc_ws;
@@ -478,8 +479,9 @@ static int sc_cmp(const double *x, const double *y, int s) {
 
 /* LinearSolver, np/procs/ls.cc:637-749, preceded by LinearDefect (562) and
  * LinearResiduum (577); LSUpdate (869) adds c on levels baselevel..top. */
-/* the lmgc workspace of levels bl..top; b of the top level is the caller's */
-static int ws_init(orc_ws *w, const orc_mg *mg, double *b) {
+/* the lmgc workspace of levels bl..top; b of a level is the caller's where
+ * bl_caller[l] is given (always for the top level), else allocated here */
+static int ws_init_levels(orc_ws *w, const orc_mg *mg, double *const *b_caller) {
   const int top = mg->nlevels - 1;
   const int s = mg->lev[top].s;
   const int bl = mg->baselevel < top ? mg->baselevel : top;
@@ -489,11 +491,13 @@ static int ws_init(orc_ws *w, const orc_mg *mg, double *b) {
   w->t = (double **)calloc(mg->nlevels, sizeof(double *));
   w->b = (double **)calloc(mg->nlevels, sizeof(double *));
   w->lu = (double **)calloc(mg->nlevels, sizeof(double *));
+  w->own_b = (int *)calloc(mg->nlevels, sizeof(int));
   for (int l = bl; l <= top; ++l) {
     size_t len = (size_t)mg->lev[l].n * s;
     w->c[l] = (double *)calloc(len, sizeof(double));
     w->t[l] = (double *)calloc(len, sizeof(double));
-    w->b[l] = (l == top) ? b : (double *)calloc(len, sizeof(double));
+    w->own_b[l] = b_caller[l] == NULL;
+    w->b[l] = w->own_b[l] ? (double *)calloc(len, sizeof(double)) : b_caller[l];
     if (mg->smoother == ORC_ILU && l > bl) {
       const orc_level *L = &mg->lev[l];
       int rc;
@@ -505,15 +509,23 @@ static int ws_init(orc_ws *w, const orc_mg *mg, double *b) {
   return 0;
 }
 
+/* the workspace of a solve whose defect lives on the top level only */
+static int ws_init(orc_ws *w, const orc_mg *mg, double *b) {
+  double *bc[64] = {0};
+  if (mg->nlevels > 64) return -1;
+  bc[mg->nlevels - 1] = b;
+  return ws_init_levels(w, mg, bc);
+}
+
 static void ws_free(orc_ws *w) {
   const orc_mg *mg = w->mg;
   const int top = mg->nlevels - 1;
   const int bl = mg->baselevel < top ? mg->baselevel : top;
   for (int l = bl; l <= top; ++l) {
     free(w->c[l]); free(w->t[l]); free(w->lu[l]);
-    if (l != top) free(w->b[l]);
+    if (w->own_b && w->own_b[l]) free(w->b[l]);
   }
-  free(w->c); free(w->t); free(w->b); free(w->lu); free(w->base_lu);
+  free(w->c); free(w->t); free(w->b); free(w->lu); free(w->base_lu); free(w->own_b);
 }
 
 /* dmatmul, ugblas.cc:3782: x = A y, per row the products summed, then assigned */
@@ -705,6 +717,93 @@ done:
   ws_free(&w);
   free(scratch);
   return rc ? rc : iters;
+}
+
+/* SetSurfaceClasses, gm/algebra.cc:2838-2925: FINE_GRID_DOF = VCLASS >= 2 and
+ * VNCLASS <= 1; FULLREFINELEVEL = the lowest level holding such a vector
+ * (the top level if none does). */
+static int fine_grid_dof(const orc_level *L, int i) { return L->vclass[i] >= NEWDEF_CLASS && L->vnclass[i] <= 1; }
+int orc_fullrefinelevel(const orc_mg *mg) {
+  const int top = mg->nlevels - 1;
+  int frl = top;
+  for (int l = top; l >= 0; --l)
+    for (int i = 0; i < mg->lev[l].n; ++i)
+      if (fine_grid_dof(&mg->lev[l], i)) { frl = l; break; }
+  return frl;
+}
+
+/* ON_SURFACE row set (np/algebra/vecloop.ct, matloop.ct): FINE_GRID_DOF rows of
+ * the levels FULLREFINELEVEL..top-1, then NEW_DEFECT rows of the top level */
+static int surface_row(const orc_level *L, int i, int is_top) {
+  return is_top ? L->vclass[i] >= NEWDEF_CLASS : fine_grid_dof(L, i);
+}
+
+/* dmatmul_minus ON_SURFACE, ugblas.cc:3997: b -= A x on the surface rows,
+ * each with its own level's matrix and x */
+static void surface_defect(const orc_mg *mg, int frl, double *const *b, double *const *x) {
+  const int top = mg->nlevels - 1;
+  for (int l = frl; l <= top; ++l) {
+    const orc_level *L = &mg->lev[l];
+    const int s = L->s;
+    for (int i = 0; i < L->n; ++i) {
+      if (!surface_row(L, i, l == top)) continue;
+      for (int k = L->rowptr[i]; k < L->rowptr[i + 1]; ++k) {
+        const double *m = L->val + (size_t)k * s * s, *yj = x[l] + (size_t)L->col[k] * s;
+        for (int r = 0; r < s; ++r) {
+          double acc = 0.0;
+          for (int c = 0; c < s; ++c) acc += m[r * s + c] * yj[c];
+          b[l][(size_t)i * s + r] -= acc;
+        }
+      }
+    }
+  }
+}
+
+/* dnrm2x ON_SURFACE, ugblas.cc:3156: sums of squares in the loop order above */
+static void surface_norm(const orc_mg *mg, int frl, double *const *b, double *out) {
+  const int top = mg->nlevels - 1;
+  const int s = mg->lev[top].s;
+  for (int r = 0; r < s; ++r) out[r] = 0.0;
+  for (int l = frl; l <= top; ++l) {
+    const orc_level *L = &mg->lev[l];
+    for (int i = 0; i < L->n; ++i) {
+      if (!surface_row(L, i, l == top)) continue;
+      for (int r = 0; r < s; ++r) { double v = b[l][(size_t)i * s + r]; out[r] += v * v; }
+    }
+  }
+  for (int r = 0; r < s; ++r) out[r] = sqrt(out[r]);
+}
+
+int orc_ls_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
+                        const double *abslimit, int maxit, double *hist, int *converged) {
+  const int top = mg->nlevels - 1;
+  const int s = mg->lev[top].s;
+  const int bl = mg->baselevel < top ? mg->baselevel : top;
+  const int frl = orc_fullrefinelevel(mg);
+  orc_ws w;
+  int rc = ws_init_levels(&w, mg, b), it = 0;
+  *converged = 0;
+  if (rc) goto done;
+  {
+    double first[ORC_MAX_S], last[ORC_MAX_S], reach[ORC_MAX_S];
+    surface_defect(mg, frl, b, x);
+    surface_norm(mg, frl, b, first);
+    if (hist) for (int r = 0; r < s; ++r) hist[r] = first[r];
+    for (int r = 0; r < s; ++r) { reach[r] = first[r] * red[r]; if (reach[r] == 0.0) reach[r] = red[r]; }
+    *converged = sc_cmp(first, abslimit, s);
+    for (it = 0; it < maxit; ++it) {
+      if (*converged) break;
+      memset(w.c[top], 0, sizeof(double) * (size_t)mg->lev[top].n * s);
+      if ((rc = lmgc(&w, top))) goto done;
+      for (int l = bl; l <= top; ++l) vadd(x[l], w.c[l], (size_t)mg->lev[l].n * s); /* LSUpdate, ls.cc:869 */
+      surface_norm(mg, frl, b, last);
+      if (hist) for (int r = 0; r < s; ++r) hist[(size_t)(it + 1) * s + r] = last[r];
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) { *converged = 1; ++it; break; }
+    }
+  }
+done:
+  ws_free(&w);
+  return rc ? rc : it;
 }
 
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,

@@ -81,6 +81,15 @@ int orc_bcgs_solve(const orc_mg *mg, double *x, double *b, const double *red, co
                    double *hist, int *converged);
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit,
                  int maxit, double *hist, int *converged);
+/* ls + lmgc on a locally refined hierarchy: x[l] and b[l] for every level
+ * l = 0..top.  The defect and its norm run over UG's surface (ON_SURFACE:
+ * FINE_GRID_DOF vectors of the levels FULLREFINELEVEL..top-1 and NEW_DEFECT
+ * vectors of the top level, each row with its own level's matrix), and
+ * LSUpdate adds the correction on every level baselevel..top (ls.cc:562,
+ * 577, 869).  On a uniformly refined hierarchy it equals orc_ls_solve. */
+int orc_ls_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
+                        const double *abslimit, int maxit, double *hist, int *converged);
+int orc_fullrefinelevel(const orc_mg *mg); /* SetSurfaceClasses, gm/algebra.cc:2838 */
 
 #ifdef __cplusplus
 }

@@ -89,10 +89,13 @@ def lib():
         L.orc_restrict.argtypes = [P, P, P, P, P]
         L.orc_interpolate.argtypes = [P, P, P, P]
         L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        L.orc_ls_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        L.orc_fullrefinelevel.argtypes = [P]
+        L.orc_fullrefinelevel.restype = C.c_int
         L.orc_cg_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_bcgs_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve", "orc_cg_solve",
-                  "orc_bcgs_solve"):
+                  "orc_bcgs_solve", "orc_ls_solve_levels"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -192,6 +195,51 @@ class Hierarchy:
         """cg (ls.cc:901-1064) preconditioned by lmgc, configured as ls_solve.
         Returns (x, iterations, converged, history)."""
         return self.ls_solve(rhs, _solver="cg", **kw)
+
+    def level_lengths(self):
+        return [L["n"] * L["s"] for L in self.levels]
+
+    def fullrefinelevel(self):
+        """FULLREFINELEVEL (gm/algebra.cc:2838): the lowest level with a
+        FINE_GRID_DOF vector; the top level on a uniformly refined hierarchy."""
+        mg = self._mg()
+        return lib().orc_fullrefinelevel(C.byref(mg))
+
+    def ls_solve_surface(self, rhs_all, *, x0_all=None, red=1e-10, abslimit=1e-50, maxit=100, **kw):
+        """ls + lmgc on a locally refined hierarchy: rhs_all and the returned x
+        hold every level 0..top, concatenated.  The defect and its norms run over
+        UG's surface and the correction is added on every level baselevel..top.
+        Returns (x_all, iterations, converged, history)."""
+        lens = self.level_lengths()
+        offs = np.concatenate([[0], np.cumsum(lens)])
+        b = np.array(rhs_all, np.float64)
+        x = np.zeros(offs[-1]) if x0_all is None else np.array(x0_all, np.float64)
+        assert b.size == offs[-1] and x.size == offs[-1], "arrays must hold every level"
+        bp = (C.c_void_p * len(lens))(*[b.ctypes.data + 8 * int(o) for o in offs[:-1]])
+        xp = (C.c_void_p * len(lens))(*[x.ctypes.data + 8 * int(o) for o in offs[:-1]])
+        mg = self._mg(**kw)
+        s = self.levels[-1]["s"]
+        redv = np.resize(np.asarray(red, np.float64), MAX_S)
+        absv = np.resize(np.asarray(abslimit, np.float64), MAX_S)
+        hist = np.zeros((maxit + 1) * s)
+        conv = C.c_int(0)
+        it = lib().orc_ls_solve_levels(C.byref(mg), xp, bp, _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
+        if it < 0:
+            raise RuntimeError(f"oracle ls failed: {it}")
+        return x, it, bool(conv.value), hist[: (it + 1) * s].reshape(it + 1, s)
+
+    def _mg(self, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None, beta=None, cdamp=None,
+            base_abslimit=1e-10):
+        mg = _MG()
+        mg.nlevels = len(self.levels); mg.lev = C.addressof(self._c)
+        mg.baselevel, mg.nu1, mg.nu2, mg.gamma = baselevel, nu1, nu2, gamma
+        mg.smoother = SMOOTHERS[smoother] if isinstance(smoother, str) else smoother
+        for i in range(MAX_S):
+            mg.damp[i] = 1.0 if damp is None else float(np.resize(damp, MAX_S)[i])
+            mg.beta[i] = 0.0 if beta is None else float(np.resize(beta, MAX_S)[i])
+            mg.cdamp[i] = 1.0 if cdamp is None else float(np.resize(cdamp, MAX_S)[i])
+            mg.base_abslimit[i] = float(np.resize(base_abslimit, MAX_S)[i])
+        return mg
 
     def ls_solve(self, rhs, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None,
                  beta=None, cdamp=None, red=1e-10, abslimit=1e-50, maxit=100, x0=None,

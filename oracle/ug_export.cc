@@ -28,6 +28,13 @@
 //   problem  : poisson  (2D: one Q1 quad; 3D: six Kuhn tets of the unit cube)
 //              diffusion (3D only: P1 with k = exp(g) per element, corr 0.1, var 1)
 //              elasticity (2D only: P1 triangles, plane strain E=1 nu=0.3, 2x2 blocks)
+//              lshape (2D only: the same elasticity on the L-shaped domain
+//                (-1,1)^2 minus [0,1)x(-1,0], six coarse triangles; <nref>
+//                uniform refinements, then <local_levels> local ones: step k
+//                marks every leaf element with a corner within 0.5^k of the
+//                re-entrant corner for red refinement, UG closes the grid
+//                (green closure, yellow copies); the right-hand side lives on
+//                the surface vectors of every level)
 //   smoother : jac (damp 0.8) | gs | ilu
 #include <config.h>
 #include <cmath>
@@ -81,6 +88,31 @@ static void put1(const std::string &n, double x) { put(n, 'd', &x, 1); }
 static void put1i(const std::string &n, int x) { put(n, 'i', &x, 1); }
 
 static INT BndCond(void *, void *, DOUBLE *, DOUBLE *value, INT *type) { value[0] = 0.0; type[0] = 0; return 0; }
+
+// the L-shaped domain: eight corners counter-clockwise (the long edges split
+// so that the six coarse triangles use corners only), straight segments
+static double g_lcorner[8][2] = {{-1, -1}, {0, -1}, {0, 0}, {1, 0}, {1, 1}, {0, 1}, {-1, 1}, {-1, 0}};
+static double g_lseg[8][4];
+static INT lshape_segment(void *data, DOUBLE *param, DOUBLE *result) {
+  const double *e = (const double *)data, t = param[0];
+  if (t < 0.0 || t > 1.0) return 1;
+  result[0] = (1.0 - t) * e[0] + t * e[2];
+  result[1] = (1.0 - t) * e[1] + t * e[3];
+  return 0;
+}
+static int create_lshape_domain() {
+  DOUBLE mid[2] = {0.0, 0.0};
+  if (!CreateDomain("LShape", mid, 1.5, 8, 8, NO)) return 1;
+  for (int i = 0; i < 8; ++i) {
+    const int j = (i + 1) % 8;
+    g_lseg[i][0] = g_lcorner[i][0]; g_lseg[i][1] = g_lcorner[i][1];
+    g_lseg[i][2] = g_lcorner[j][0]; g_lseg[i][3] = g_lcorner[j][1];
+    char name[16];
+    snprintf(name, sizeof name, "side%d", i);
+    if (!CreateBoundarySegment2D(name, 1, 0, i, i, j, 1, 0.0, 1.0, lshape_segment, g_lseg[i])) return 1;
+  }
+  return 0;
+}
 static void run(const char *c) {
   char b[4096];
   snprintf(b, sizeof b, "%s", c);
@@ -156,25 +188,50 @@ int main(int argc, char **argv) {
   uint64_t seed = strtoull(argv[5], nullptr, 10);
   const char *outfile = argv[6];
   int maxit = argc > 7 ? atoi(argv[7]) : 100;
+  int nloc = argc > 8 ? atoi(argv[8]) : 0;
   int ug_argc = 1;
   char *ug_argv0 = argv[0];
   char **ug_argv = &ug_argv0;
   if (InitUg(&ug_argc, &ug_argv)) return 1;
 
-  const bool elast = problem == "elasticity";
+  const bool lshape = problem == "lshape";
+  const bool elast = problem == "elasticity" || lshape;
   const bool diffusion = problem == "diffusion";
   if ((elast && DIMX != 2) || (diffusion && DIMX != 3)) { fprintf(stderr, "problem/dimension mismatch\n"); return 2; }
+  if (nloc > 0 && !lshape) { fprintf(stderr, "local refinement is defined for lshape only\n"); return 2; }
   const int s = elast ? 2 : 1;
 
   CreateBoundaryValueProblem("bvp", BndCond, 0, NULL, 0, NULL);
-  run(DIMX == 2 ? "configure bvp $d Quadrilateral;" : "configure bvp $d Hexahedron;");
+  if (lshape && create_lshape_domain()) { fprintf(stderr, "L-shaped domain\n"); return 1; }
+  run(lshape ? "configure bvp $d LShape;" : DIMX == 2 ? "configure bvp $d Quadrilateral;" : "configure bvp $d Hexahedron;");
   run(s == 1 ? "newformat fmt $V n1: vt 20 $M implicit(vt): mt 4;" : "newformat fmt $V n2: vt 20 $M implicit(vt): mt 4;");
   run("new mg $b bvp $f fmt $h 4000M;");
-  if (DIMX == 2 && !elast) run("ie 0 1 2 3;");
+  if (lshape) {
+    // three unit squares, each split by its diagonal through the re-entrant corner (node 2)
+    run("ie 0 1 2;"); run("ie 0 2 7;"); run("ie 7 2 6;"); run("ie 2 5 6;"); run("ie 2 3 4;"); run("ie 2 4 5;");
+  } else if (DIMX == 2 && !elast) run("ie 0 1 2 3;");
   else if (DIMX == 2) { run("ie 0 1 2;"); run("ie 0 2 3;"); }
   else { run("ie 0 1 2 6;"); run("ie 0 2 3 6;"); run("ie 0 3 7 6;"); run("ie 0 7 4 6;"); run("ie 0 4 5 6;"); run("ie 0 5 1 6;"); }
   run("fixcoarsegrid;");
   for (int l = 0; l < nref; ++l) { run("mark $a;"); run("refine;"); }
+  for (int k = 1; k <= nloc; ++k) {
+    // mark the leaf elements near the re-entrant corner (0, 0); refine closes the grid
+    MULTIGRID *m0 = GetCurrentMultigrid();
+    const double r = std::ldexp(1.0, -k);
+    int nmarked = 0;
+    for (int l = 0; l <= TOPLEVEL(m0); ++l)
+      for (ELEMENT *e = FIRSTELEMENT(GRID_ON_LEVEL(m0, l)); e; e = SUCCE(e)) {
+        if (!EstimateHere(e)) continue;
+        bool near = false;
+        for (int i = 0; i < CORNERS_OF_ELEM(e); ++i) {
+          const double *x = node_xyz(CORNER(e, i));
+          if (x[0] * x[0] + x[1] * x[1] <= r * r) near = true;
+        }
+        if (near) { if (MarkForRefinement(e, RED, 0)) { fprintf(stderr, "mark failed\n"); return 1; } ++nmarked; }
+      }
+    fprintf(stderr, "local step %d: %d elements marked\n", k, nmarked);
+    run("refine;");
+  }
   run("createvector sol rhs kx ky kd kv kc kt;");
   run("creatematrix MAT LU;");
 
@@ -252,8 +309,25 @@ int main(int argc, char **argv) {
         for (m = MNEXT(m); m; m = MNEXT(m)) for (int k = 0; k < s * s; ++k) MVALUE(m, mcmp[k]) = 0.0;
       }
   }
-  // ---- seeded right-hand side on the finest level, keyed by lattice position
-  {
+  // ---- seeded right-hand side, keyed by lattice position
+  if (lshape) {
+    // on the surface: FINE_GRID_DOF vectors below the top level, NEW_DEFECT
+    // vectors on it (the rows UG's ON_SURFACE loops visit, np/algebra/vecloop.ct);
+    // a surface vector on level l carries f * h_l^2 with h_l = 2^-l
+    const double scale = std::ldexp(1.0, top);
+    for (int l = 0; l <= top; ++l) {
+      const double hd = std::ldexp(1.0, -2 * l);
+      for (NODE *n = FIRSTNODE(GRID_ON_LEVEL(mg, l)); n; n = SUCCN(n)) {
+        VECTOR *v = NVECTOR(n);
+        if (!(l == top ? NEW_DEFECT(v) : FINE_GRID_DOF(v))) continue;
+        const double *x = node_xyz(n);
+        int64_t ix = llround((x[0] + 1.0) * scale), iy = llround((x[1] + 1.0) * scale);
+        uint64_t key = ugfx::lattice_key(ix, iy, 0);
+        for (int c = 0; c < s; ++c)
+          VVALUE(v, vcmp(rhs)[c]) = (VECSKIP(v) & (1 << c)) ? 0.0 : ugfx::rhs_uniform(seed + 0x9E37ull * c, key) * hd;
+      }
+    }
+  } else {
     const double scale = double(1 << nref);
     const double hd = std::pow(1.0 / scale, DIMX);
     for (NODE *n = FIRSTNODE(GRID_ON_LEVEL(mg, top)); n; n = SUCCN(n)) {
@@ -271,7 +345,8 @@ int main(int argc, char **argv) {
   if (!g_out) { perror(outfile); return 1; }
   fwrite("UGFX1\n", 1, 6, g_out);
   put1i("dim", DIMX); put1i("nlevels", top + 1); put1i("baselevel", baselevel); put1i("blocksize", s);
-  put1i("nref", nref); put1i("seed", (int)seed);
+  put1i("nref", nref); put1i("seed", (int)seed); put1i("nloc", nloc);
+  put1i("fullrefinelevel", FULLREFINELEVEL(mg));
   put("problem", 's', problem.c_str(), (int64_t)problem.size());
   put("smoother", 's', smoother.c_str(), (int64_t)smoother.size());
 
@@ -295,6 +370,11 @@ int main(int argc, char **argv) {
     std::string p = "L" + std::to_string(l) + "_";
     put1i(p + "n", n); puti(p + "rowptr", rowptr); puti(p + "col", col); putd(p + "val", val);
     puti(p + "vclass", vclass); puti(p + "vnclass", vnclass); puti(p + "skip", skip); putd(p + "xyz", xyz);
+    {
+      std::vector<int> fg(n), nd(n);
+      for (int i = 0; i < n; ++i) { fg[i] = FINE_GRID_DOF(L.vecs[i]) ? 1 : 0; nd[i] = NEW_DEFECT(L.vecs[i]) ? 1 : 0; }
+      puti(p + "fine_grid_dof", fg); puti(p + "new_defect", nd);
+    }
     if (l == 0) continue;
     // standard transfer weights, one row per fine vector
     std::vector<std::vector<std::pair<int, double>>> prow(n);
@@ -322,9 +402,12 @@ int main(int argc, char **argv) {
     puti(q + "rowptr", pptr); puti(q + "col", pcol); putd(q + "w", pw);
   }
   {
-    std::vector<double> b;
+    std::vector<double> b, ball;
     for (VECTOR *v : g_lev[top].vecs) for (int c = 0; c < s; ++c) b.push_back(VVALUE(v, vcmp(rhs)[c]));
     putd("rhs", b);
+    for (int l = 0; l <= top; ++l)
+      for (VECTOR *v : g_lev[l].vecs) for (int c = 0; c < s; ++c) ball.push_back(VVALUE(v, vcmp(rhs)[c]));
+    putd("rhs_all", ball);  // every level, levels concatenated
   }
 
   // ---- kernel known-answer vectors on the finest level
@@ -399,6 +482,15 @@ int main(int argc, char **argv) {
   if (!ls || !lmgc) { fprintf(stderr, "numproc lookup failed\n"); return 1; }
   // keep the rhs to replay the loop afterwards
   std::vector<double> rhs_top = grab(rhs, top);
+  std::vector<std::vector<double>> rhs_lev;
+  for (int l = 0; l <= top; ++l) rhs_lev.push_back(grab(rhs, l));
+  auto restart = [&]() {  // x = 0 and the assembled right-hand side on every level
+    for (int l = 0; l <= top; ++l) {
+      dset(mg, l, l, ALL_VECTORS, sol, 0.0);
+      size_t i = 0;
+      for (VECTOR *v : g_lev[l].vecs) for (int c = 0; c < s; ++c) VVALUE(v, vcmp(rhs)[c]) = rhs_lev[l][i++];
+    }
+  };
   INT bl = 0, res = 0;
   LRESULT lr;
   memset(&lr, 0, sizeof lr);
@@ -414,16 +506,18 @@ int main(int argc, char **argv) {
   putd("ls_first", std::vector<double>(lr.first_defect, lr.first_defect + s));
   putd("ls_last", std::vector<double>(lr.last_defect, lr.last_defect + s));
   putd("ls_x", grab(sol, top));
+  {
+    std::vector<double> xa;
+    for (int l = 0; l <= top; ++l) { auto xl = grab(sol, l); xa.insert(xa.end(), xl.begin(), xl.end()); }
+    putd("ls_x_all", xa);  // every level, levels concatenated (the surface solution spans levels)
+  }
   put1("ls_wall_s", wall_s); put1("ls_cpu_s", cpu_s);
   fprintf(stderr, "UG ls: iters=%d converged=%d first=%.6e last=%.6e wall=%.3fs\n", (int)lr.number_of_linear_iterations,
           (int)lr.converged, lr.first_defect[0], lr.last_defect[0], wall_s);
 
   // replay: x = 0, b = rhs, then per iteration dset(c,0); Lmgc; x += c; |b|
   {
-    for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
-    for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
-    int i = 0;
-    for (VECTOR *v : g_lev[top].vecs) for (int c = 0; c < s; ++c) VVALUE(v, vcmp(rhs)[c]) = rhs_top[i++];
+    restart();
     (*ls->Defect)(ls, top, sol, rhs, A, &res);
     std::vector<double> hist;
     VEC_SCALAR a;
@@ -444,7 +538,7 @@ int main(int argc, char **argv) {
   }
 
   // ---- UG's cg (ls.cc:901-1165) preconditioned by the same lmgc, from x = 0
-  {
+  if (!lshape) {
     for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
     for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
     int i = 0;
@@ -473,7 +567,7 @@ int main(int argc, char **argv) {
   }
 
   // ---- UG's bcgs (ls.cc:1711-2062) preconditioned by the same lmgc, from x = 0
-  {
+  if (!lshape) {
     for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
     for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
     int i = 0;

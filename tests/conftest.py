@@ -16,8 +16,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
-def golden_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+def golden_names(kind="uniform"):
+    """Fixture names: "uniform" (uniformly refined hierarchies, the surface is
+    the top level), "local" (the ls_* cases, locally refined) or "all"."""
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    if kind == "all":
+        return names
+    return [n for n in names if n.startswith("ls_") == (kind == "local")]
 
 
 def load_golden(name):

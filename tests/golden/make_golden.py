@@ -6,7 +6,11 @@ case below and stores every record as a compressed .npz.  Each fixture holds
 the hierarchy exactly as UG's grid manager and assembly produced it, the
 known-answer vectors of UG's kernels on the finest level, and UG's own ls +
 lmgc solve (iteration count, defect history, solution) and its cg + lmgc and
-bcgs + lmgc solves (iteration count, defects, solution).
+bcgs + lmgc solves (iteration count, defects, solution).  The ``ls_*`` cases
+are locally refined: the L-shaped elasticity problem, uniformly refined
+``nref`` times and then ``nloc`` times toward the re-entrant corner, with the
+surface flags (FINE_GRID_DOF, NEW_DEFECT, FULLREFINELEVEL) and the solution on
+every level.
 
     python tests/golden/make_golden.py
 """
@@ -22,7 +26,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 
-# name: (dimension, problem, nref, baselevel, smoother, seed)
+# name: (dimension, problem, nref, baselevel, smoother, seed[, nloc])
 CASES = {
     "q1_jac": (2, "poisson", 5, 2, "jac", 11),
     "q1_gs": (2, "poisson", 5, 2, "gs", 11),
@@ -34,6 +38,9 @@ CASES = {
     "el_jac": (2, "elasticity", 4, 1, "jac", 14),
     "el_gs": (2, "elasticity", 4, 1, "gs", 14),
     "el_ilu": (2, "elasticity", 4, 1, "ilu", 14),
+    "ls_jac": (2, "lshape", 2, 0, "jac", 22, 6),
+    "ls_gs": (2, "lshape", 2, 0, "gs", 22, 6),
+    "ls_ilu": (2, "lshape", 2, 0, "ilu", 22, 6),
 }
 
 
@@ -41,10 +48,11 @@ def main():
     env = dict(os.environ)
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"], check=True, env=env)
     with tempfile.TemporaryDirectory() as tmp:
-        for name, (dim, problem, nref, base, sm, seed) in CASES.items():
+        for name, (dim, problem, nref, base, sm, seed, *rest) in CASES.items():
             exe = os.path.join(ROOT, "oracle", "_ref", f"ug_export{dim}d")
             raw = os.path.join(tmp, name + ".bin")
-            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw], check=True,
+            nloc = rest[0] if rest else 0
+            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw, "100", str(nloc)], check=True,
                            stdout=subprocess.DEVNULL)
             fx = oracle.read_ugfx(raw)
             arrays = {k: (np.array(v) if not isinstance(v, str) else np.array(v)) for k, v in fx.items()}

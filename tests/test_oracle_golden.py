@@ -7,6 +7,7 @@ import pytest
 from conftest import golden_names, load_golden
 
 NAMES = golden_names()
+LOCAL = golden_names("local")
 
 
 def rel(a, b):
@@ -14,7 +15,7 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", NAMES + LOCAL)
 def test_kernels_match_ug(name, oracle_mod):
     fx = load_golden(name)
     H = oracle_mod.Hierarchy.from_ugfx(fx)
@@ -25,7 +26,15 @@ def test_kernels_match_ug(name, oracle_mod):
     lu = H.ilu_decomp(top)
     assert rel(lu, fx["kat_ilu_factors"]) <= 1e-14
     assert rel(H.luiter(top, lu, fx["kat_d"]), fx["kat_ilu"]) <= 1e-14
-    assert rel(H.nrm2x(top, fx["kat_d"]), fx["kat_nrm"]) <= 1e-14
+    if name in LOCAL:
+        # dnrm2x over ALL_VECTORS; the top level of a local hierarchy also holds
+        # copies outside the NEW_DEFECT set, which orc_nrm2x leaves out
+        d = np.asarray(fx["kat_d"]).reshape(int(fx[f"L{top}_n"][0]), -1)
+        assert rel(np.sqrt((d * d).sum(axis=0)), fx["kat_nrm"]) <= 1e-14
+        nd = fx[f"L{top}_new_defect"].astype(bool)
+        assert rel(H.nrm2x(top, fx["kat_d"]), np.sqrt((d[nd] * d[nd]).sum(axis=0))) <= 1e-14
+    else:
+        assert rel(H.nrm2x(top, fx["kat_d"]), fx["kat_nrm"]) <= 1e-14
     assert rel(H.restrict(top, fx["kat_restrict_pre"], fx["kat_d"]), fx["kat_restrict"]) <= 1e-14
     assert rel(H.interpolate(top, fx["kat_interp_coarse"]), fx["kat_interp"]) <= 1e-14
 
@@ -71,3 +80,63 @@ def test_bcgs_matches_ug(name, oracle_mod):
     assert conv == bool(fx["bcgs_converged"][0]) and it == int(fx["bcgs_iters"][0])
     assert rel(x, fx["bcgs_x"]) <= 1e-12
     assert rel(hist[-1], fx["bcgs_last"]) <= 1e-10
+
+
+def _split(fx, flat):
+    n = int(fx["nlevels"][0]); s = int(fx["blocksize"][0])
+    offs = np.cumsum([0] + [int(fx[f"L{l}_n"][0]) * s for l in range(n)])
+    return [np.asarray(flat)[offs[l]:offs[l + 1]] for l in range(n)]
+
+
+@pytest.mark.parametrize("name", LOCAL)
+def test_surface_flags_match_ug(name, oracle_mod):
+    """UG's surface of a locally refined hierarchy follows from the vector
+    classes alone (gm/algebra.cc:2917-2921): FINE_GRID_DOF = VCLASS >= 2 and
+    VNCLASS <= 1, NEW_DEFECT = VCLASS >= 2, FULLREFINELEVEL = the lowest level
+    with a FINE_GRID_DOF vector; the rhs lives on exactly those rows."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    n = int(fx["nlevels"][0]); s = int(fx["blocksize"][0])
+    assert H.fullrefinelevel() == int(fx["fullrefinelevel"][0]) < n - 1
+    rhs = _split(fx, fx["rhs_all"])
+    nsurf = 0
+    for l in range(n):
+        vc, vn = fx[f"L{l}_vclass"], fx[f"L{l}_vnclass"]
+        assert np.array_equal(fx[f"L{l}_fine_grid_dof"], ((vc >= 2) & (vn <= 1)).astype(np.int32))
+        assert np.array_equal(fx[f"L{l}_new_defect"], (vc >= 2).astype(np.int32))
+        surf = (vc >= 2) if l == n - 1 else ((vc >= 2) & (vn <= 1))
+        if l < int(fx["fullrefinelevel"][0]):
+            surf = np.zeros_like(surf)
+        assert not np.any(rhs[l].reshape(-1, s)[~surf]), l
+        nsurf += int(surf.sum())
+    assert nsurf > int(fx[f"L{n - 1}_n"][0])  # the surface spans several levels
+
+
+@pytest.mark.parametrize("name", LOCAL)
+def test_surface_solve_matches_ug(name, oracle_mod):
+    """ls + lmgc on the locally refined L-shaped elasticity problem: the
+    oracle repeats UG's defect history and solution on every level."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    sm = fx["smoother"]
+    x, it, conv, hist = H.ls_solve_surface(fx["rhs_all"], smoother=sm, baselevel=int(fx["baselevel"][0]),
+                                           damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50)
+    assert conv and it == int(fx["ls_iters"][0])
+    assert rel(hist.ravel(), fx["ls_hist"]) <= 1e-12
+    assert rel(x, fx["ls_x_all"]) <= 1e-12
+    assert rel(_split(fx, x)[-1], fx["ls_x"]) <= 1e-12
+    assert rel(fx["ls_x_replay"], fx["ls_x"]) == 0.0
+
+
+@pytest.mark.parametrize("name", ["q1_gs", "el_ilu", "p1k_jac"])
+def test_surface_solve_is_ls_on_uniform(name, oracle_mod):
+    """On a uniformly refined hierarchy the surface is the top level, so the
+    all-level solve gives the top-level solve exactly."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    sm = fx["smoother"]
+    kw = dict(smoother=sm, baselevel=int(fx["baselevel"][0]), damp=0.8 if sm == "jac" else 1.0)
+    x1, it1, _, h1 = H.ls_solve(fx["rhs"], **kw)
+    x2, it2, _, h2 = H.ls_solve_surface(fx["rhs_all"], **kw)
+    assert it1 == it2 and np.array_equal(h1, h2)
+    assert np.array_equal(_split(fx, x2)[-1], x1)
