@@ -242,6 +242,115 @@ def run_c1(args, stream, flush_l2, world, rank):
     return out
 
 
+# ---------------------------------------------------------------- locally refined workload
+LOCAL_NUNI, LOCAL_NLOC = 7, 9
+
+
+def run_local(args, stream, flush_l2, world, rank):
+    """Plane-strain P1 elasticity (E=1, nu=0.3, 2x2 blocks) on the L-shaped
+    domain: six coarse triangles refined 7 times uniformly, then 9 times toward
+    the re-entrant corner (step k: leaf elements with a corner within 0.5^k,
+    green closure, yellow copies; the hierarchy UG's grid manager builds,
+    generated on the host), body force uniform[-1,1] per component.  Block
+    ILU(0) V(2,2), level-scheduled triangular solves in subdomain order
+    (a multicolour order stalls ILU(0) on this system), ls over UG's surface (FINE_GRID_DOF
+    rows of every level) to 1e-8 relative defect, plain FP64 and FP32
+    V-cycle in FP64 refinement."""
+    import torch
+    import ug_gb300 as G
+    t0 = time.perf_counter()
+    gen = G.LocalGenerator(LOCAL_NUNI, LOCAL_NLOC, seed=SEED)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mg = G.MultiGrid(gen, order=G.ORDER_DOMAIN, fp32=True, device=torch.cuda.current_device())
+    G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
+    G.setup_lmgc(mg, "ilu", baselevel=0, red=RED, abslimit=1e-50, name="loc64")
+    mg.npcreate("loc32", "linear_solver.gls")
+    mg.npinit("loc32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    top = mg.top
+    mg.createvector("b0")
+    mg.upload_levels("b0", gen.rhs)
+    mg.ls_preprocess("loc64", top, "sol", "rhs")  # ILU factors of every level (setup, not timed)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    surf = 0
+    for l in range(mg.nlevels):
+        d = gen.level(l)
+        m = (d["vclass"] >= 2) if l == top else ((d["vclass"] >= 2) & (d["vnclass"] <= 1))
+        surf += int(m.sum()) * (0 if l < mg.frl else 1)
+    out = {"workload": f"2D plane-strain P1 elasticity on the L-shaped domain, 2x2 blocks, 6 coarse triangles "
+                       f"refined {LOCAL_NUNI}x uniformly + {LOCAL_NLOC}x toward the re-entrant corner "
+                       f"(UG's local refinement: green closure, yellow copies), block ILU(0) V(2,2) level-scheduled "
+                       f"in subdomain order, ls over the surface to 1e-8 rel defect",
+           "levels": mg.nlevels, "fullrefinelevel": mg.frl, "surface_dofs": 2 * surf,
+           "vectors_all_levels": int(sum(mg.size(l)[0] for l in range(mg.nlevels))),
+           "nnzb_all_levels": int(sum(mg.size(l)[2] for l in range(mg.nlevels))),
+           "generate_s": gen_s, "setup_s": setup_s}
+
+    def step(solver):
+        lr = G.LResult()
+        for l in range(mg.nlevels):
+            mg.dcopy(l, "rhs", "b0")
+            mg.dset(l, "sol", 0.0)
+        mg.ls_defect(solver, top, "sol", "rhs")
+        mg.ls_residuum(solver, 0, top, "sol", "rhs", lr)
+        mg.ls_solver(solver, top, "sol", "rhs", lr)
+        return lr
+
+    res = {}
+    for solver in ("loc64", "loc32"):
+        for _ in range(args.warmup):
+            step(solver)
+        ms, launches = [], 0
+        for _ in range(args.steps):
+            flush_l2()
+            mg.launch_count(reset=True)
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            lr = step(solver)
+            e.record(stream)
+            torch.cuda.synchronize()
+            launches += mg.launch_count()
+            assert lr.converged, f"{solver} did not converge"
+            ms.append(a.elapsed_time(e))
+        res[solver] = (reduce_over_ranks(float(np.mean(ms))), lr.iters, launches / args.steps)
+    b_host = np.ascontiguousarray(gen.rhs)
+    x_host = np.empty_like(b_host)
+    mg.solve_host("loc32", b_host, x_host)
+    e2e = []
+    for _ in range(args.steps):
+        flush_l2(); torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, lr = mg.solve_host("loc32", b_host, x_host)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+        assert lr.converged
+    e2e_ms = reduce_over_ranks(float(np.mean(e2e)))
+    mg.close()
+    (ms64, it64, l64), (ms32, it32, l32) = res["loc64"], res["loc32"]
+    out.update({"mixed": {"value": whole_job_rate(1, ms32, world), "unit": "solves/s", "ms_per_solve": ms32,
+                          "iterations": it32, "launches_per_solve": l32},
+                "fp64": {"value": whole_job_rate(1, ms64, world), "unit": "solves/s", "ms_per_solve": ms64,
+                         "iterations": it64, "launches_per_solve": l64},
+                "mixed_over_fp64": ms64 / ms32,
+                "e2e": {"value": whole_job_rate(1, e2e_ms, world), "unit": "solves/s (mixed, host b -> host x)",
+                        "h2d_bytes_per_step": int(b_host.size * 8), "d2h_bytes_per_step": int(b_host.size * 8),
+                        "ms_per_step": e2e_ms}})
+    if rank == 0:
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build()
+            H = oracle.Hierarchy(gen.levels())
+            t0 = time.perf_counter()
+            _, it, conv, _ = H.ls_solve_surface(gen.rhs, smoother="ilu", baselevel=0, red=RED)
+            dt = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                                   "sample": f"one full FP64 solve, list order ({it} iterations, {dt:.1f} s)"}
+        except Exception as e:  # reported, not fatal
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    return out
+
+
 # ---------------------------------------------------------------- batched workload
 BATCH_N = 512
 
@@ -584,6 +693,7 @@ def run_ours(args):
     waves = [mg.num_waves(l) for l in range(mg.nlevels)]
     mg.close()
     c1 = run_c1(args, stream, flush_l2, world, rank)
+    local_c3 = run_local(args, stream, flush_l2, world, rank) if not args.no_local else None
     batched = run_batched(args, stream, flush_l2, world, rank) if not args.no_batched else None
     serving = run_serving(args, rank) if not args.no_serving else None
 
@@ -620,6 +730,7 @@ def run_ours(args):
             "clocks": r32["clocks"],
             "cpu_baseline": cpu,
             "config1": c1,
+            "local_refinement": local_c3,
             "batched": batched,
             "serving": serving,
         }
@@ -635,6 +746,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances workload")
+    ap.add_argument("--no-local", action="store_true", help="skip the locally refined workload")
     ap.add_argument("--batch", type=int, default=BATCH_N, help="instances of the batched workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests of the serving stream")

@@ -65,6 +65,8 @@ typedef struct {
 /* processing order of every level (the `order` numproc, np/procs/order.cc) */
 #define GMG_ORDER_LIST 0  /* UG's VECTOR-list order: gs / ilu reproduce l_lgs / l_luiter */
 #define GMG_ORDER_COLOR 1 /* multicolour order (greedy colouring of the matrix graph) */
+#define GMG_ORDER_DOMAIN 2 /* subdomain order: interiors of small breadth-first subdomains, then the
+                              coloured interface rows (level-scheduled ILU / GS with few wavefronts) */
 
 #define GMG_PREC_FP64 0
 #define GMG_PREC_FP32 1
@@ -230,9 +232,21 @@ int gmg_pool_fetch(gmg_pool *pool, int slot, double *x, gmg_lresult *lr);
 /* slot's matrix values on a level as the device holds them, in gmg_gen_levels' CSR order */
 int gmg_pool_slot_matrix(gmg_pool *pool, int slot, int level, double *val);
 
+/* ------------------------------------------------ locally refined hierarchies */
+/* A hierarchy whose FINE_GRID_DOF rows (VCLASS >= 2 and VNCLASS <= 1,
+ * gm/algebra.cc:2917-2921) reach below the top level is locally refined:
+ * its surface spans the levels FULLREFINELEVEL..top, and ls's defect, norms
+ * and update follow UG's ON_SURFACE loops (np/procs/ls.cc:562, 577, 869).
+ * Host vectors of such a hierarchy hold every level, levels 0..top
+ * concatenated, each in list order (as UG's VECDATA on all levels). */
+int gmg_mg_full_refine_level(const gmg_mg *mg);  /* FULLREFINELEVEL (top if uniform) */
+int gmg_vec_upload_levels(gmg_vec *v, const double *host);
+int gmg_vec_download_levels(gmg_vec *v, double *host);
+
 /* ------------------------------------------------ one-call solve from host buffers */
-/* Uploads b (finest level, list order; packed on a batched hierarchy), runs ls
- * `solver` ($i $d $r $s $p, with the x/b given to npinit), downloads x. */
+/* Uploads b (finest level, list order; packed on a batched hierarchy; every
+ * level on a locally refined one), runs ls `solver` ($i $d $r $s $p, with the
+ * x/b given to npinit), downloads x (same layout as b). */
 int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double *x_host, gmg_lresult *lr);
 
 /* ------------------------------------------------ structured hierarchies */
@@ -251,6 +265,20 @@ int gmg_gen_levels(gmg_gen *g, const gmg_level_desc **levels, int *nlevels);
 int gmg_gen_rhs(gmg_gen *g, const double **rhs, int *len);
 int gmg_gen_coords(gmg_gen *g, int level, const double **xyz);
 int gmg_gen_destroy(gmg_gen *g);
+
+/* Locally refined workload: plane-strain P1 elasticity (E=1, nu=0.3, 2x2
+ * blocks) on the L-shaped domain (-1,1)^2 minus [0,1)x(-1,0], six coarse
+ * triangles refined nuni times uniformly, then nloc times toward the
+ * re-entrant corner (step k marks the leaf elements with a corner within
+ * 0.5^k; closure, yellow copies and vector classes by UG's rules).  The
+ * right-hand side holds every level, concatenated (the surface rows carry
+ * the load, the others 0). */
+typedef struct gmg_lgen gmg_lgen;
+int gmg_lgen_create(int nuni, int nloc, unsigned long long seed, gmg_lgen **out);
+int gmg_lgen_levels(gmg_lgen *g, const gmg_level_desc **levels, int *nlevels);
+int gmg_lgen_rhs(gmg_lgen *g, const double **rhs, long long *len);
+int gmg_lgen_coords(gmg_lgen *g, int level, const double **xyz);
+int gmg_lgen_destroy(gmg_lgen *g);
 
 #ifdef __cplusplus
 }

@@ -341,6 +341,12 @@ int main(int argc, char **argv) {
   }
 
   index_levels(mg);
+  for (int l = 0; l <= top; ++l) {  // element census per level: corners, refinement class
+    int cnt[5][4] = {{0}};
+    for (ELEMENT *e = FIRSTELEMENT(GRID_ON_LEVEL(mg, l)); e; e = SUCCE(e)) cnt[CORNERS_OF_ELEM(e)][ECLASS(e)]++;
+    fprintf(stderr, "level %d elements: tri yellow/green/red %d/%d/%d quad %d\n", l, cnt[3][YELLOW_CLASS],
+            cnt[3][GREEN_CLASS], cnt[3][RED_CLASS], cnt[4][0] + cnt[4][1] + cnt[4][2] + cnt[4][3]);
+  }
   g_out = fopen(outfile, "wb");
   if (!g_out) { perror(outfile); return 1; }
   fwrite("UGFX1\n", 1, 6, g_out);

@@ -80,3 +80,50 @@ def test_generator_matches_ug(name, kind, nref, seed, corr, var):
         maps[top] = np.array([gk[k] for k in _keys(fx[f"L{top}_xyz"], scale)])
     rhs_g = gen.rhs.reshape(-1, s)[maps[top]].ravel()
     assert np.allclose(rhs_g, fx["rhs"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("name,nuni,nloc,seed", [("ls_gs", 2, 6, 22)])
+def test_local_generator_matches_ug(name, nuni, nloc, seed):
+    """The locally refined L-shape hierarchy (meshgen_local.cpp) is UG's:
+    after matching vectors by coordinates, every level has UG's vectors,
+    matrix (pattern and values), VCLASS / VNCLASS / VECSKIP, transfer weights
+    and right-hand side."""
+    import ug_gb300 as G
+    fx = load_golden(name)
+    gen = G.LocalGenerator(nuni, nloc, seed=seed)
+    assert gen.nlevels == int(fx["nlevels"][0])
+    s = int(fx["blocksize"][0])
+    scale = 1 << (gen.nlevels - 1)
+    offs_g = np.cumsum([0] + [gen.level(l)["n"] * s for l in range(gen.nlevels)])
+    offs_u = np.cumsum([0] + [int(fx[f"L{l}_n"][0]) * s for l in range(gen.nlevels)])
+    maps = []
+    for l in range(gen.nlevels):
+        g = gen.level(l)
+        n = int(fx[f"L{l}_n"][0])
+        assert g["n"] == n and g["rowptr"][-1] == fx[f"L{l}_rowptr"][-1]
+        gk = {k: i for i, k in enumerate(_keys(g["xyz"], scale))}
+        m = np.array([gk[k] for k in _keys(fx[f"L{l}_xyz"], scale)])
+        maps.append(m)
+        for f in ("skip", "vclass", "vnclass"):
+            assert np.array_equal(g[f][m], fx[f"L{l}_{f}"]), (l, f)
+        rp, col, val = fx[f"L{l}_rowptr"], fx[f"L{l}_col"], fx[f"L{l}_val"].reshape(-1, s * s)
+        gval = g["val"].reshape(-1, s * s)
+        vmax = np.abs(val).max()
+        for i in range(n):
+            gi = m[i]
+            gents = {int(g["col"][k]): gval[k] for k in range(g["rowptr"][gi], g["rowptr"][gi + 1])}
+            uents = {int(m[col[k]]): val[k] for k in range(rp[i], rp[i + 1])}
+            assert set(gents) == set(uents), f"level {l} row {i}: pattern differs"
+            for c, v in uents.items():
+                assert np.allclose(gents[c], v, rtol=0, atol=1e-13 * vmax), f"level {l} row {i}"
+        rg = gen.rhs[offs_g[l]:offs_g[l + 1]].reshape(-1, s)[m].ravel()
+        assert np.allclose(rg, fx["rhs_all"][offs_u[l]:offs_u[l + 1]], rtol=0, atol=1e-15), l
+        if l == 0:
+            continue
+        prp, pcol, pw = fx[f"P{l}_rowptr"], fx[f"P{l}_col"], fx[f"P{l}_w"]
+        mc = maps[l - 1]
+        for i in range(n):
+            gi = m[i]
+            ge = {int(g["pcol"][k]): g["pw"][k] for k in range(g["prowptr"][gi], g["prowptr"][gi + 1])}
+            ue = {int(mc[pcol[k]]): pw[k] for k in range(prp[i], prp[i + 1])}
+            assert ge.keys() == ue.keys() and all(abs(ge[k] - ue[k]) < 1e-15 for k in ue)

@@ -1,0 +1,154 @@
+"""Locally refined hierarchies on the GPU: the L-shaped plane-strain problem
+refined toward its re-entrant corner by UG itself (tests/golden/ls_*.npz).
+The surface spans several levels (FINE_GRID_DOF rows below the top level),
+so ls's defect and norms run over UG's ON_SURFACE rows of every level and
+LSUpdate adds the correction on every level (np/procs/ls.cc:562, 577, 869).
+
+* list order: UG's iteration count and UG's solution on EVERY level (jac
+  1e-10 relative, gs / ilu 1e-8 and iterations +-1, the contract's bounds);
+* multicolour order: the oracle's surface solve on the reordered hierarchy;
+* mixed precision (FP32 V-cycle in FP64 refinement of the surface defect):
+  converges to the FP64 stopping test, error against a tightly converged
+  FP64 oracle solution at most 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, permuted_levels, rel
+
+pytestmark = pytest.mark.gpu
+LOCAL = golden_names("local")
+
+
+@pytest.fixture(scope="module")
+def G():
+    import ug_gb300
+    ug_gb300.lib()
+    return ug_gb300
+
+
+def _damp(sm):
+    return 0.8 if sm == "jac" else 1.0
+
+
+def _split(mg, flat):
+    return mg.split_levels(np.asarray(flat))
+
+
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("fuse", [0, None])
+@pytest.mark.parametrize("name", LOCAL)
+def test_local_solve_matches_ug(G, name, fuse, graph):
+    fx = load_golden(name)
+    mg = G.MultiGrid(G.levels_from_ugfx(fx), order=0)
+    assert mg.local and mg.frl == int(fx["fullrefinelevel"][0])
+    sm = fx["smoother"]
+    G.setup_lmgc(mg, sm, baselevel=int(fx["baselevel"][0]), damp=_damp(sm), red=1e-10, abslimit=1e-50, fuse=fuse,
+                 graph=graph)
+    x, lr = mg.solve_host("mgs", fx["rhs_all"])
+    it_ug = int(fx["ls_iters"][0])
+    assert lr.converged
+    assert abs(lr.first_defect[0] - fx["ls_hist"][0]) <= 1e-12 * fx["ls_hist"][0]
+    if sm == "jac":
+        assert lr.iters == it_ug
+        assert rel(x, fx["ls_x_all"]) <= 1e-10
+    else:
+        assert abs(lr.iters - it_ug) <= 1
+        assert rel(x, fx["ls_x_all"]) <= 1e-8
+    x2, lr2 = mg.solve_host("mgs", fx["rhs_all"])
+    assert lr2.iters == lr.iters and np.array_equal(x, x2)
+    mg.close()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("name", LOCAL + ["el_ilu", "q1_gs", "p1k_ilu"])
+def test_local_multicolour_matches_oracle(G, oracle_mod, name, order):
+    """Multicolour (1) and subdomain (2) processing orders: the device solve
+    is the oracle's on the reordered hierarchy (uniform fixtures included:
+    their surface is the top level)."""
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    mg = G.MultiGrid(levels, order=order)
+    if "rhs_all" not in fx:
+        fx = dict(fx)
+        fx["rhs_all"] = np.concatenate([np.zeros(d["n"] * d["s"]) for d in levels[:-1]] + [fx["rhs"]])
+    sm = fx["smoother"]
+    bl = int(fx["baselevel"][0])
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    b_in = fx["rhs_all"] if mg.local else fx["rhs"]
+    x, lr = mg.solve_host("mgs", b_in)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    s = levels[0]["s"]
+    perms = [mg.order(l) for l in range(mg.nlevels)]
+    lens = [d["n"] * s for d in levels]
+    offs = np.cumsum([0] + lens)
+    b_all = np.asarray(fx["rhs_all"])
+    b_p = np.concatenate([b_all[offs[l]:offs[l + 1]].reshape(-1, s)[p].ravel() for l, p in enumerate(perms)])
+    xo, ito, conv, _ = H.ls_solve_surface(b_p, smoother=sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    xr = []
+    for l, p in enumerate(perms):
+        o = np.empty((len(p), s)); o[p] = xo[offs[l]:offs[l + 1]].reshape(-1, s); xr.append(o.ravel())
+    xr = np.concatenate(xr) if mg.local else xr[-1]
+    assert conv and lr.converged and lr.iters == ito
+    assert rel(x, xr) <= 1e-10
+    mg.close()
+
+
+@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("name", LOCAL)
+def test_local_mixed_precision(G, oracle_mod, name, order):
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    mg = G.MultiGrid(levels, order=order, fp32=True)
+    sm = fx["smoother"]
+    bl = int(fx["baselevel"][0])
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-8, abslimit=1e-50, mixed=True)
+    x, lr = mg.solve_host("mgs", fx["rhs_all"])
+    assert lr.converged and lr.last_defect[0] <= 1e-8 * lr.first_defect[0]
+    # the FP64 iteration in the same order (multicolour ILU / GS is another
+    # preconditioner than UG's list order) to the same reduction
+    m64 = G.MultiGrid(levels, order=order)
+    G.setup_lmgc(m64, sm, baselevel=bl, damp=_damp(sm), red=1e-8, abslimit=1e-50)
+    _, lr64 = m64.solve_host("mgs", fx["rhs_all"])
+    m64.close()
+    assert lr64.converged and lr.iters <= lr64.iters + 2
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    xo, _, conv, _ = H.ls_solve_surface(fx["rhs_all"], smoother=sm, baselevel=bl, damp=_damp(sm), red=1e-14,
+                                        abslimit=1e-50)
+    assert conv
+    # the surface solution: FINE_GRID_DOF rows below the top, NEW_DEFECT rows on it
+    frl, top = mg.frl, mg.top
+    s = levels[0]["s"]
+    xs, xos = [], []
+    for l, (a, b) in enumerate(zip(_split(mg, x), _split(mg, xo))):
+        if l < frl:
+            continue
+        vc, vn = fx[f"L{l}_vclass"], fx[f"L{l}_vnclass"]
+        m = (vc >= 2) if l == top else ((vc >= 2) & (vn <= 1))
+        xs.append(a.reshape(-1, s)[m].ravel()); xos.append(b.reshape(-1, s)[m].ravel())
+    assert rel(np.concatenate(xs), np.concatenate(xos)) <= 1e-6
+    mg.close()
+
+
+@pytest.mark.parametrize("sm,order", [("ilu", 2), ("gs", 2), ("gs", 0), ("jac", 1)])
+def test_generated_local_vs_oracle(G, oracle_mod, sm, order):
+    """The generated L-shape hierarchy (UG's local refinement rebuilt on the
+    host, 5 uniform + 9 local steps, 43k surface unknowns): the device solve
+    and the oracle's surface solve on the same (reordered) hierarchy agree."""
+    gen = G.LocalGenerator(5, 9, seed=2026)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=order)
+    assert mg.local and mg.nlevels == 15
+    G.setup_lmgc(mg, sm, baselevel=0, damp=_damp(sm), red=1e-8, abslimit=1e-50)
+    x, lr = mg.solve_host("mgs", gen.rhs)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    s = 2
+    perms = [mg.order(l) for l in range(mg.nlevels)]
+    b_p = np.concatenate([b.reshape(-1, s)[p].ravel() for b, p in zip(_split(mg, gen.rhs), perms)])
+    xo, ito, conv, _ = H.ls_solve_surface(b_p, smoother=sm, baselevel=0, damp=_damp(sm), red=1e-8, abslimit=1e-50)
+    xr = []
+    for xl, p in zip(_split(mg, xo), perms):
+        o = np.empty((len(p), s)); o[p] = xl.reshape(-1, s); xr.append(o.ravel())
+    assert conv and lr.converged and abs(lr.iters - ito) <= 1
+    assert rel(x, np.concatenate(xr)) <= 1e-8
+    mg.close()

@@ -25,12 +25,12 @@ import os
 import numpy as np
 
 __all__ = ["GmgError", "Generator", "MultiGrid", "LResult", "lib", "LIB_PATH",
-           "ORDER_LIST", "ORDER_COLOR", "FP64", "FP32"]
+           "ORDER_LIST", "ORDER_COLOR", "ORDER_DOMAIN", "FP64", "FP32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libug_gb300.so")
 MAX_S = 8
-ORDER_LIST, ORDER_COLOR = 0, 1
+ORDER_LIST, ORDER_COLOR, ORDER_DOMAIN = 0, 1, 2
 FP64, FP32 = 0, 1
 NP_NOT_INIT, NP_NOT_ACTIVE, NP_ACTIVE, NP_EXECUTABLE = 0, 1, 2, 3
 
@@ -110,6 +110,10 @@ def lib(build_if_missing: bool = True):
         "gmg_pool_admit": ([P, I, C.c_ulonglong, D, D], I), "gmg_pool_launch": ([P], I),
         "gmg_pool_poll": ([P, P, P], I), "gmg_pool_fetch": ([P, I, P, P], I),
         "gmg_pool_slot_matrix": ([P, I, I, P], I),
+        "gmg_mg_full_refine_level": ([P], I), "gmg_vec_upload_levels": ([P, P], I),
+        "gmg_vec_download_levels": ([P, P], I),
+        "gmg_lgen_create": ([I, I, C.c_ulonglong, P], I), "gmg_lgen_levels": ([P, P, P], I),
+        "gmg_lgen_rhs": ([P, P, P], I), "gmg_lgen_coords": ([P, I, P], I), "gmg_lgen_destroy": ([P], I),
         "gmg_gen_create": ([I, I, C.c_ulonglong, D, D, P], I), "gmg_gen_levels": ([P, P, P], I),
         "gmg_gen_rhs": ([P, P, P], I), "gmg_gen_coords": ([P, I, P], I), "gmg_gen_destroy": ([P], I),
     }
@@ -181,17 +185,56 @@ class Generator:
         if l > 0:
             prow = arr(d.prowptr, n + 1, C.c_int)
             out.update(prowptr=prow, pcol=arr(d.pcol, int(prow[-1]), C.c_int), pw=arr(d.pw, int(prow[-1]), C.c_double))
-        xp = C.POINTER(C.c_double)()
-        lib().gmg_gen_coords(self._h, l, C.byref(xp))
-        out["xyz"] = np.ctypeslib.as_array(xp, (n * 3,)).copy().reshape(n, 3)
+        out["xyz"] = np.ctypeslib.as_array(self._coords(l), (n * 3,)).copy().reshape(n, 3)
         return out
 
     def levels(self):
         return [self.level(l) for l in range(self.nlevels)]
 
+    def _coords(self, l):
+        xp = C.POINTER(C.c_double)()
+        lib().gmg_gen_coords(self._h, l, C.byref(xp))
+        return xp
+
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.gmg_gen_destroy(self._h)
+            self._h = None
+
+
+class LocalGenerator(Generator):
+    """Locally refined hierarchy (gmg_lgen_create): plane-strain P1 elasticity
+    on the L-shaped domain, ``nuni`` uniform refinements of the six coarse
+    triangles, then ``nloc`` steps toward the re-entrant corner (step k
+    refines the leaf elements with a corner within 0.5^k), closed and
+    classified by UG's rules.  ``rhs`` holds every level, concatenated."""
+
+    def __init__(self, nuni: int, nloc: int, seed: int = 1):
+        L = lib()
+        h = C.c_void_p()
+        if L.gmg_lgen_create(nuni, nloc, seed, C.byref(h)):
+            _err("gmg_lgen_create")
+        self._h = h
+        self.kind, self.nuni, self.nloc = "lshape", nuni, nloc
+        lev = C.POINTER(LevelDesc)()
+        nl = C.c_int()
+        L.gmg_lgen_levels(h, C.byref(lev), C.byref(nl))
+        self._desc = lev
+        self.nlevels = nl.value
+        self.nref = self.nlevels - 1
+        rp = C.POINTER(C.c_double)()
+        ln = C.c_longlong()
+        L.gmg_lgen_rhs(h, C.byref(rp), C.byref(ln))
+        self.rhs = np.ctypeslib.as_array(rp, (ln.value,)).copy()
+
+    def _coords(self, l):
+        xp = C.POINTER(C.c_double)()
+        lib().gmg_lgen_coords(self._h, l, C.byref(xp))
+        return xp
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.gmg_lgen_destroy(self._h)
             self._h = None
 
 
@@ -271,7 +314,30 @@ class MultiGrid:
                 self.pack_off.append(po.value)
             self.block = self.size(0)[1]
             self.packed_len = (self.pack_off[-1] + self.inst_n[-1]) * self.block
+        # locally refined: the surface spans levels frl..top, host vectors hold every level
+        self.frl = L.gmg_mg_full_refine_level(h)
+        self.local = self.frl < self.top
+        self.level_len = [self.size(l)[0] * self.size(l)[1] for l in range(nl)]
         del keep  # the device holds its own copies
+
+    # ---- locally refined hierarchies
+    def split_levels(self, flat) -> list:
+        """Per-level views of an every-level vector (levels concatenated)."""
+        offs = np.concatenate([[0], np.cumsum(self.level_len)])
+        return [flat[offs[l]:offs[l + 1]] for l in range(self.nlevels)]
+
+    def upload_levels(self, name: str, data):
+        a = np.ascontiguousarray(data, np.float64).ravel()
+        if a.size != sum(self.level_len):
+            raise GmgError(f"upload_levels {name}: {a.size} values for {sum(self.level_len)}")
+        if lib().gmg_vec_upload_levels(self.vec(name), _ptr(a)):
+            _err(f"upload_levels {name}")
+
+    def download_levels(self, name: str) -> np.ndarray:
+        a = np.empty(sum(self.level_len))
+        if lib().gmg_vec_download_levels(self.vec(name), _ptr(a)):
+            _err(f"download_levels {name}")
+        return a
 
     # ---- batched hierarchies
     def split(self, packed) -> list:
@@ -513,9 +579,10 @@ class MultiGrid:
 
     def solve_host(self, solver: str, b, x=None):
         """gmg_solve_host: b (finest level, list order; packed on a batched
-        hierarchy) -> (x, LResult)."""
+        hierarchy; every level, concatenated, on a locally refined one) ->
+        (x, LResult), x in the layout of b."""
         n, s, _ = self.size(self.top)
-        length = self.packed_len if self.ninst else n * s
+        length = self.packed_len if self.ninst else (sum(self.level_len) if self.local else n * s)
         bb = np.ascontiguousarray(b, np.float64).ravel()
         if bb.size != length:
             raise GmgError(f"solve {solver}: {bb.size} values for {length}")

@@ -39,6 +39,7 @@ enum : uint8_t {
   F_ACTIVE = 1,  // VCLASS >= ACTIVE_CLASS (3): updated by the smoothers
   F_NEWDEF = 2,  // VCLASS >= NEWDEF_CLASS (2): restricted into the coarse grid
   F_RESET = 4,   // VNCLASS >= NEWDEF_CLASS (2): reset before restriction
+  F_FINE = 8,    // FINE_GRID_DOF: VCLASS >= 2 and VNCLASS <= 1 (a surface row below the top level)
 };
 
 // memcpy for large host buffers (several threads)
@@ -156,6 +157,11 @@ struct gmg_mg {
   gmg_mg_opts opts{};
   gmg::Arena arena;
   std::vector<gmg::Level> lev;
+  // FULLREFINELEVEL (gm/algebra.cc:2838): the lowest level holding a
+  // FINE_GRID_DOF row; below the top level only on a locally refined
+  // hierarchy, whose surface then spans levels frl..top
+  int frl = 0;
+  bool local() const { return frl < int(lev.size()) - 1; }
   std::map<std::string, std::unique_ptr<gmg_vec>> vecs;
   std::map<std::string, std::unique_ptr<gmg_mat>> mats;
   std::map<std::string, std::unique_ptr<gmg_np>> nps;
@@ -207,6 +213,33 @@ struct gmg_mg {
 namespace gmg {
 
 constexpr int REDUCE_BLOCKS = 304;  // 2 x 152 SMs
+
+// the levels of one surface operation on a locally refined hierarchy, passed
+// by value to one kernel: rows row0[l]..row0[l+1] of the launch are the rows
+// of table entry l; mask selects its surface rows (0: none), addx adds y to x
+// on every row, b32/c32 are the FP32 copies of the mixed iteration
+constexpr int SURF_MAX_LEVELS = 24;
+struct SurfLevels {
+  int nlev = 0;
+  int row0[SURF_MAX_LEVELS + 1] = {0};
+  const int *rowptr[SURF_MAX_LEVELS] = {};
+  const int *col[SURF_MAX_LEVELS] = {};
+  const double *val[SURF_MAX_LEVELS] = {};
+  const uint8_t *flags[SURF_MAX_LEVELS] = {};
+  uint8_t mask[SURF_MAX_LEVELS] = {};
+  uint8_t addx[SURF_MAX_LEVELS] = {};
+  double *b[SURF_MAX_LEVELS] = {};
+  double *x[SURF_MAX_LEVELS] = {};
+  const void *y[SURF_MAX_LEVELS] = {};
+  float *b32[SURF_MAX_LEVELS] = {};
+  float *c32[SURF_MAX_LEVELS] = {};
+};
+// masked rows: b -= A y (FP64 matrix, y of precision yprec); addx rows: x += y
+int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s);
+// b32 = b on every row; c32 = 0 where given
+int k_surf_prepare(gmg_mg *mg, const SurfLevels &t, int s);
+// per-component norms of b over the masked rows into mg->norms_dev
+int k_surf_nrm2x(gmg_mg *mg, const SurfLevels &t, int s);
 constexpr int BATCH_CHUNK = 256;    // rows per block of the batched ls update (one per thread)
 #define GMG_MAX_TOPS 16             // distinct instance depths of a batched hierarchy
 

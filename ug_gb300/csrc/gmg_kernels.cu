@@ -2278,4 +2278,152 @@ int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *per
   return 0;
 }
 
+// ------------------------------------------------------------ surface of a locally refined hierarchy
+// UG's ON_SURFACE loops (np/algebra/vecloop.ct, matloop.ct) visit the
+// FINE_GRID_DOF vectors of the levels FULLREFINELEVEL..top-1 and the
+// NEW_DEFECT vectors of the top level, each row with its own level's matrix
+// and vectors.  One launch covers every level of a SurfLevels table: thread g
+// handles row g - row0[l] of the level l with row0[l] <= g < row0[l+1].
+template <int S, class YT>
+__global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
+  pdl_prologue();
+  const int total = t.row0[t.nlev];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int l = 0;
+    while (g >= t.row0[l + 1]) ++l;
+    const int i = g - t.row0[l];
+    const YT *__restrict__ y = static_cast<const YT *>(t.y[l]);
+    if (t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l])) {
+      double acc[S];
+#pragma unroll
+      for (int r = 0; r < S; ++r) acc[r] = 0.0;
+      const int k1 = __ldg(t.rowptr[l] + i + 1);
+      for (int k = __ldg(t.rowptr[l] + i); k < k1; ++k) {
+        const int j = __ldg(t.col[l] + k);
+        const double *m = t.val[l] + (size_t)k * (S * S);
+        double yj[S];
+#pragma unroll
+        for (int c = 0; c < S; ++c) yj[c] = double(y[(size_t)j * S + c]);
+#pragma unroll
+        for (int r = 0; r < S; ++r)
+#pragma unroll
+          for (int c = 0; c < S; ++c) acc[r] = fma(__ldg(m + r * S + c), yj[c], acc[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < S; ++r) t.b[l][(size_t)i * S + r] -= acc[r];
+    }
+    if (t.addx[l]) {
+#pragma unroll
+      for (int r = 0; r < S; ++r) t.x[l][(size_t)i * S + r] += double(y[(size_t)i * S + r]);
+    }
+  }
+}
+
+// b32 = b64 on every row of the table's levels; c32 = 0 where zc is set
+template <int S>
+__global__ void __launch_bounds__(BLK) surf_prepare_kernel(SurfLevels t) {
+  pdl_prologue();
+  const int total = t.row0[t.nlev];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int l = 0;
+    while (g >= t.row0[l + 1]) ++l;
+    const size_t i = size_t(g - t.row0[l]) * S;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      t.b32[l][i + r] = float(t.b[l][i + r]);
+      if (t.c32[l]) t.c32[l][i + r] = 0.0f;
+    }
+  }
+}
+
+// dnrm2x ON_SURFACE: per-component sums of squares over the surface rows of
+// every level, with the deterministic two-stage reduction of nrm_kernel
+template <int S>
+__global__ void __launch_bounds__(BLK) surf_nrm_kernel(SurfLevels t, double *__restrict__ partial,
+                                                       unsigned *__restrict__ ticket, double *__restrict__ out) {
+  pdl_prologue();
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  const int total = t.row0[t.nlev];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int l = 0;
+    while (g >= t.row0[l + 1]) ++l;
+    const int i = g - t.row0[l];
+    if (!(t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l]))) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      const double v = t.b[l][(size_t)i * S + r];
+      acc[r] = fma(v, v, acc[r]);
+    }
+  }
+  __shared__ double sh[BLK / 32][S];
+  __shared__ bool last;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * S + threadIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[BLK];
+  for (int r = 0; r < S; ++r) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(partial + (size_t)b * S + r);
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[r] = sqrt(red[0]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s) {
+  if (t.row0[t.nlev] == 0) return 0;
+  const int g = vec_grid(t.row0[t.nlev]);
+#define SU(SS) { if (yprec == GMG_PREC_FP64) GMG_LAUNCH((surf_update_kernel<SS, double>), g, BLK, t); \
+                 else GMG_LAUNCH((surf_update_kernel<SS, float>), g, BLK, t); }
+  if (s == 1) SU(1) else if (s == 2) SU(2) else if (s == 3) SU(3)
+  else { set_error("block size %d not compiled", s); return 1; }
+#undef SU
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_surf_prepare(gmg_mg *mg, const SurfLevels &t, int s) {
+  if (t.row0[t.nlev] == 0) return 0;
+  const int g = vec_grid(t.row0[t.nlev]);
+  if (s == 1) GMG_LAUNCH((surf_prepare_kernel<1>), g, BLK, t);
+  else if (s == 2) GMG_LAUNCH((surf_prepare_kernel<2>), g, BLK, t);
+  else if (s == 3) GMG_LAUNCH((surf_prepare_kernel<3>), g, BLK, t);
+  else { set_error("block size %d not compiled", s); return 1; }
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_surf_nrm2x(gmg_mg *mg, const SurfLevels &t, int s) {
+  unsigned *ticket = reinterpret_cast<unsigned *>(mg->norms_dev + GMG_MAX_S);
+  if (s == 1) GMG_LAUNCH((surf_nrm_kernel<1>), REDUCE_BLOCKS, BLK, t, mg->partial, ticket, mg->norms_dev);
+  else if (s == 2) GMG_LAUNCH((surf_nrm_kernel<2>), REDUCE_BLOCKS, BLK, t, mg->partial, ticket, mg->norms_dev);
+  else if (s == 3) GMG_LAUNCH((surf_nrm_kernel<3>), REDUCE_BLOCKS, BLK, t, mg->partial, ticket, mg->norms_dev);
+  else { set_error("block size %d not compiled", s); return 1; }
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 }  // namespace gmg

@@ -161,6 +161,69 @@ static std::vector<std::vector<int>> sym_adjacency(int n, const int *rowptr, con
   return adj;
 }
 
+// Subdomain order (GMG_ORDER_DOMAIN) for the level-scheduled triangular
+// sweeps of ILU and Gauss-Seidel: the rows are grown, in breadth-first order
+// of the matrix graph, into compact subdomains of at most DOMAIN_ROWS rows;
+// the interior rows of every subdomain come first (subdomain by subdomain,
+// breadth-first inside), then the interface rows (those with a neighbour in
+// another subdomain), coloured among themselves and taken colour by colour.
+// A sweep then has about (subdomain depth + interface colours) wavefronts
+// whatever the level size, while the ILU(0) factors keep the quality of a
+// breadth-first order inside every subdomain (a multicolour order decouples
+// every row from its neighbours and weakens ILU(0) badly on systems).
+constexpr int DOMAIN_ROWS = 64;
+
+static std::vector<int> domain_order(int n, const std::vector<std::vector<int>> &adj) {
+  std::vector<int> bfs, pos(n, -1);
+  bfs.reserve(n);
+  for (int s0 = 0; s0 < n; ++s0) {
+    if (pos[s0] >= 0) continue;
+    size_t head = bfs.size();
+    pos[s0] = int(bfs.size());
+    bfs.push_back(s0);
+    while (head < bfs.size()) {
+      const int i = bfs[head++];
+      for (int j : adj[i])
+        if (pos[j] < 0) { pos[j] = int(bfs.size()); bfs.push_back(j); }
+    }
+  }
+  std::vector<int> region(n, -1), queue;
+  int nreg = 0;
+  for (int s0 : bfs) {
+    if (region[s0] >= 0) continue;
+    queue.assign(1, s0);
+    region[s0] = nreg;
+    int cnt = 1;
+    for (size_t h = 0; h < queue.size() && cnt < DOMAIN_ROWS; ++h)
+      for (int j : adj[queue[h]])
+        if (region[j] < 0 && cnt < DOMAIN_ROWS) { region[j] = nreg; ++cnt; queue.push_back(j); }
+    ++nreg;
+  }
+  std::vector<int> interior, iface;
+  std::vector<char> is_iface(n, 0);
+  for (int i : bfs) {
+    bool in = true;
+    for (int j : adj[i]) in &= region[j] == region[i];
+    if (in) interior.push_back(i); else { iface.push_back(i); is_iface[i] = 1; }
+  }
+  std::stable_sort(interior.begin(), interior.end(), [&](int a, int b) { return region[a] < region[b]; });
+  // colour the interface rows among themselves
+  std::vector<int> local(n, -1);
+  for (size_t k = 0; k < iface.size(); ++k) local[iface[k]] = int(k);
+  std::vector<std::vector<int>> sub(iface.size());
+  for (size_t k = 0; k < iface.size(); ++k)
+    for (int j : adj[iface[k]])
+      if (is_iface[j]) sub[k].push_back(local[j]);
+  int nc = 0;
+  std::vector<int> colour = greedy_colour(int(iface.size()), sub, &nc);
+  std::vector<int> ord(iface.size());
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return colour[a] < colour[b]; });
+  std::vector<int> perm = std::move(interior);
+  for (int k : ord) perm.push_back(iface[k]);
+  return perm;
+}
+
 // Level sets of the triangular dependency graph in processing order.
 // forward: row i waits for its neighbours j < i; backward: for j > i.
 static void wavefronts(int n, const std::vector<std::vector<int>> &adj, bool forward, std::vector<int> &ptr,
@@ -289,6 +352,8 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
       H.uptr.push_back(int(H.urows.size()));
     }
     H.contiguous = true;
+  } else if (order == GMG_ORDER_DOMAIN && n > 0) {
+    H.perm = domain_order(n, adj);
   }
   H.iperm.resize(n);
   for (int i = 0; i < n; ++i) H.iperm[H.perm[i]] = i;
@@ -314,6 +379,7 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
     if (vc >= 3) f |= F_ACTIVE; else H.all_active = false;
     if (vc >= 2) f |= F_NEWDEF;
     if (vn >= 2) f |= F_RESET;
+    if (vc >= 2 && vn <= 1) f |= F_FINE;
     H.flags[i] = f;
     H.skip[i] = uint8_t(sk & 0xff);
     if (sk) H.any_skip = true;
@@ -577,6 +643,13 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
     L.h_skip = std::move(h.skip);
   }
   GMG_CHECK(mg->arena.used <= mg->arena.size, "arena overflow");
+  // FULLREFINELEVEL (SetSurfaceClasses, gm/algebra.cc:2905-2921)
+  mg->frl = nlevels - 1;
+  for (int l = nlevels - 1; l >= 0; --l)
+    for (uint8_t f : mg->lev[l].h_flags)
+      if (f & F_FINE) { mg->frl = l; break; }
+  GMG_CHECK(!mg->local() || nlevels <= SURF_MAX_LEVELS, "a locally refined hierarchy has at most %d levels",
+            SURF_MAX_LEVELS);
   // scratch
   // reduction scratch: per-block partial sums, the norms, and the norm kernel's ticket counter
   const size_t scratch = sizeof(double) * (REDUCE_BLOCKS * GMG_MAX_S + GMG_MAX_S + 1);
@@ -586,6 +659,11 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
   GMG_CUDA(cudaMallocHost(&mg->norms_host, sizeof(double) * GMG_MAX_S));
   mg->lev.back().own.push_back(mg->partial);
   size_t top_len = std::max(size_t(mg->lev.back().n) * s, stage_min);
+  if (mg->local()) {  // host vectors of a locally refined hierarchy hold every level
+    size_t all = 0;
+    for (const auto &L : mg->lev) all += size_t(L.n) * s;
+    top_len = std::max(top_len, all);
+  }
   GMG_CUDA(cudaMallocHost(&mg->stage_host, sizeof(double) * (top_len ? top_len : 1)));
   GMG_CUDA(cudaMalloc(&mg->stage_dev, sizeof(double) * (top_len ? top_len : 1)));
   mg->lev.back().own.push_back(mg->stage_dev);

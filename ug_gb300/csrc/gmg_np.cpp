@@ -853,12 +853,53 @@ int NPLs::PreProcess(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *bl, 
 
 bool NPLs::batched(int level) const { return mg->batch.ninst > 0 && level == int(mg->lev.size()) - 1; }
 
+// ---- the surface of a locally refined hierarchy
+// ON_SURFACE with tolevel tl (np/algebra/vecloop.ct, matloop.ct): the
+// FINE_GRID_DOF rows of the levels FULLREFINELEVEL..tl-1 and the NEW_DEFECT
+// rows of tl.  Table entries for the levels lo..hi, with that row mask on the
+// levels from FULLREFINELEVEL up (none below).
+static void surf_table(gmg_mg *mg, int lo, int hi, int tl, SurfLevels &t) {
+  t = SurfLevels{};
+  for (int l = lo; l <= hi; ++l) {
+    const Level &L = mg->lev[l];
+    const int e = t.nlev++;
+    t.row0[e + 1] = t.row0[e] + L.n;
+    t.rowptr[e] = L.A.rowptr; t.col[e] = L.A.col; t.val[e] = L.A.v64; t.flags[e] = L.flags;
+    t.mask[e] = l == tl ? F_NEWDEF : (l >= mg->frl && l < tl ? F_FINE : 0);
+  }
+}
+
+static int surf_lo(gmg_mg *mg, int tl) { return std::min(mg->frl, tl); }
+
+// LinearDefect ON_SURFACE: b -= A x on the surface rows, level by level
+static int surface_defect(gmg_mg *mg, int tl, gmg_vec *xv, gmg_vec *bv) {
+  GMG_CHECK(bv->prec == GMG_PREC_FP64, "ls: a locally refined hierarchy needs an FP64 defect");
+  SurfLevels t;
+  surf_table(mg, surf_lo(mg, tl), tl, tl, t);
+  for (int e = 0; e < t.nlev; ++e) {
+    const int l = surf_lo(mg, tl) + e;
+    t.b[e] = (double *)vlev(bv, l);
+    t.y[e] = vlev(xv, l);
+  }
+  return k_surf_update(mg, t, xv->prec, mg->lev[tl].s);
+}
+
+// dnrm2x ON_SURFACE into mg->norms_dev
+static int surface_norm(gmg_mg *mg, int tl, gmg_vec *bv) {
+  GMG_CHECK(bv->prec == GMG_PREC_FP64, "ls: a locally refined hierarchy needs an FP64 defect");
+  SurfLevels t;
+  surf_table(mg, surf_lo(mg, tl), tl, tl, t);
+  for (int e = 0; e < t.nlev; ++e) t.b[e] = (double *)vlev(bv, surf_lo(mg, tl) + e);
+  return k_surf_nrm2x(mg, t, mg->lev[tl].s);
+}
+
 // LinearDefect, ls.cc:562: b -= A x on the surface, which is the top level
 // of a uniformly refined hierarchy (on a batched hierarchy: every instance's
 // own top level; a level that is some instance's top is updated whole, which
 // only touches the other instances' restricted, reset rows there)
 int NPLs::Defect(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *res) {
   if (check_level(mg, level)) return 1;
+  if (mg->local()) return surface_defect(mg, level, xv, bv);
   if (batched(level)) {
     for (const auto &tl : mg->batch.tops)
       if (defect_level(tl.level, xv, bv)) return 1;
@@ -890,10 +931,58 @@ int NPLs::Residuum(int, int tl, gmg_vec *, gmg_vec *bv, gmg_mat *, gmg_lresult *
     }
     return 0;
   }
-  if (k_nrm2x(mg, mg->lev[tl], bv->prec, vlev(bv, tl))) return 1;
+  if (mg->local() ? surface_norm(mg, tl, bv) : k_nrm2x(mg, mg->lev[tl], bv->prec, vlev(bv, tl))) return 1;
   GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
   for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
+  return 0;
+}
+
+// one ls iteration on a locally refined hierarchy.  LSUpdate adds c on every
+// level baselevel..top (ls.cc:869); lmgc has kept the surface defect on the
+// FINE_GRID_DOF rows of the lower levels (restriction resets only VNCLASS >= 2
+// rows).  Mixed: the FP32 cycle starts from the FP64 surface defect of every
+// level, and the FP64 defect of each surface row is updated with its own
+// level's matrix: b_l -= A_l c_l (UG's defect satisfies b_l = f_l - A_l x_l
+// on those rows, because lmgc subtracts A_l of every correction it adds to c_l).
+int NPLs::surface_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const int s = mg->lev[level].s;
+  const int bl = std::min(baselevel, level);
+  GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64,
+            "ls: a locally refined hierarchy needs FP64 x and b");
+  SurfLevels t;
+  if (!mixed) {
+    if (k_set(mg, cvec->prec, vlev(cvec, level), vlen(mg, level), 0.0)) return 1;
+    if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
+    surf_table(mg, bl, level, level, t);
+    for (int e = 0; e < t.nlev; ++e) {
+      t.mask[e] = 0;
+      t.addx[e] = 1;
+      t.x[e] = (double *)vlev(xv, bl + e);
+      t.y[e] = vlev(cvec, bl + e);
+    }
+    if (k_surf_update(mg, t, cvec->prec, s)) return 1;
+  } else {
+    const int lo = surf_lo(mg, level);
+    surf_table(mg, lo, level, level, t);
+    for (int e = 0; e < t.nlev; ++e) {
+      t.b[e] = (double *)vlev(bv, lo + e);
+      t.b32[e] = (float *)vlev(b32, lo + e);
+      t.c32[e] = lo + e == level ? (float *)vlev(cvec, level) : nullptr;
+    }
+    if (k_surf_prepare(mg, t, s)) return 1;
+    if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    surf_table(mg, bl, level, level, t);
+    for (int e = 0; e < t.nlev; ++e) {
+      t.addx[e] = 1;
+      t.b[e] = (double *)vlev(bv, bl + e);
+      t.x[e] = (double *)vlev(xv, bl + e);
+      t.y[e] = vlev(cvec, bl + e);
+    }
+    if (k_surf_update(mg, t, GMG_PREC_FP32, s)) return 1;
+  }
+  if (surface_norm(mg, level, bv)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
   return 0;
 }
 
@@ -937,6 +1026,7 @@ int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int 
 
 int NPLs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
   if (batched(level)) return batch_iteration(level, xv, bv, Am, err);
+  if (mg->local()) return surface_iteration(level, xv, bv, Am, err);
   const Level &L = mg->lev[level];
   const long long len = vlen(mg, level);
   if (!mixed) {
@@ -1141,6 +1231,7 @@ int NPCg::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
                  gmg_lresult *lr) {
   if (check_level(mg, level)) return 1;
   GMG_CHECK(mg->batch.ninst == 0, "cg on a batched hierarchy is not supported (use ls)");
+  GMG_CHECK(!mg->local(), "cg on a locally refined hierarchy is not supported (use ls)");
   GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64, "cg: x and b must be FP64");
   if (!p) p = temp_vec(mg, name + "__p", GMG_PREC_FP64);
   if (!t) t = temp_vec(mg, name + "__t", GMG_PREC_FP64);
@@ -1271,6 +1362,7 @@ int NPBcgs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const doubl
                    gmg_lresult *lr) {
   if (check_level(mg, level)) return 1;
   GMG_CHECK(mg->batch.ninst == 0, "bcgs on a batched hierarchy is not supported (use ls)");
+  GMG_CHECK(!mg->local(), "bcgs on a locally refined hierarchy is not supported (use ls)");
   GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64, "bcgs: x and b must be FP64");
   GMG_CHECK(!mixed || mg->opts.fp32_copy, "bcgs $mixed needs a hierarchy with FP32 copies");
   const int s = mg->lev[level].s;
@@ -1619,6 +1711,11 @@ int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double 
     if (gmg_vec_upload_packed(ls->b, b_host)) return 1;
     for (const auto &tl : mg->batch.tops)
       if (k_set(mg, ls->x->prec, vlev(ls->x, tl.level), vlen(mg, tl.level), 0.0)) return 1;
+  } else if (mg->local()) {
+    // every level: b as given, x = 0
+    if (gmg_vec_upload_levels(ls->b, b_host)) return 1;
+    for (int l = 0; l <= top; ++l)
+      if (k_set(mg, ls->x->prec, vlev(ls->x, l), vlen(mg, l), 0.0)) return 1;
   } else {
     if (gmg_vec_upload(ls->b, top, b_host)) return 1;
     if (k_set(mg, ls->x->prec, vlev(ls->x, top), vlen(mg, top), 0.0)) return 1;
@@ -1626,8 +1723,46 @@ int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double 
   if (ls->Defect(top, ls->x, ls->b, ls->A, &res)) return 1;
   if (ls->Residuum(gls ? gls->baselevel : 0, top, ls->x, ls->b, ls->A, lr)) return 1;
   if (ls->Solver(top, ls->x, ls->b, ls->A, ls->abslimit, ls->reduction, lr)) return 1;
-  return mg->batch.ninst > 0 ? gmg_vec_download_packed(ls->x, x_host) : gmg_vec_download(ls->x, top, x_host);
+  if (mg->batch.ninst > 0) return gmg_vec_download_packed(ls->x, x_host);
+  return mg->local() ? gmg_vec_download_levels(ls->x, x_host) : gmg_vec_download(ls->x, top, x_host);
 }
+
+// every level of v, levels concatenated, each in UG list order (one staged copy)
+int gmg_vec_upload_levels(gmg_vec *v, const double *host) {
+  if (!v || !host) { set_error("gmg_vec_upload_levels: bad arguments"); return 1; }
+  gmg_mg *mg = v->mg;
+  size_t len = 0;
+  for (const auto &L : mg->lev) len += size_t(L.n) * L.s;
+  GMG_CHECK(mg->local(), "gmg_vec_upload_levels: not a locally refined hierarchy");
+  par_copy(mg->stage_host, host, len * sizeof(double));
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+  size_t off = 0;
+  for (int l = 0; l < int(mg->lev.size()); ++l) {
+    const Level &L = mg->lev[l];
+    if (k_gather(mg, v->prec, vlev(v, l), (const double *)mg->stage_dev + off, L.perm_dev, L.n, L.s)) return 1;
+    off += size_t(L.n) * L.s;
+  }
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  return 0;
+}
+
+int gmg_vec_download_levels(gmg_vec *v, double *host) {
+  if (!v || !host) { set_error("gmg_vec_download_levels: bad arguments"); return 1; }
+  gmg_mg *mg = v->mg;
+  GMG_CHECK(mg->local(), "gmg_vec_download_levels: not a locally refined hierarchy");
+  size_t off = 0;
+  for (int l = 0; l < int(mg->lev.size()); ++l) {
+    const Level &L = mg->lev[l];
+    if (k_scatter(mg, v->prec, (double *)mg->stage_dev + off, vlev(v, l), L.perm_dev, L.n, L.s)) return 1;
+    off += size_t(L.n) * L.s;
+  }
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, off * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  par_copy(host, mg->stage_host, off * sizeof(double));
+  return 0;
+}
+
+int gmg_mg_full_refine_level(const gmg_mg *mg) { return mg ? mg->frl : -1; }
 
 static long long packed_len(const gmg_mg *mg) {
   return mg->batch.pack_off.empty() ? 0 : mg->batch.pack_off.back() * mg->lev[0].s;

@@ -195,6 +195,8 @@ struct NPLs : NPLinearSolver {
   int step_async(int i, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr);  // without the sync
   int prepare_temps(gmg_vec *b);  // the correction (and FP32 defect) vectors of Solver
   int defect_level(int level, gmg_vec *x, gmg_vec *b);
+  // locally refined hierarchies: the iteration over the surface of every level
+  int surface_iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
   // batched hierarchies (gmg_mg_create_batched), solved on their deepest level
   bool batched(int level) const;
   std::vector<double> inst_first, inst_last;  // ninst * GMG_MAX_S, per-instance defects

@@ -11,6 +11,8 @@ With --batched N: N instances of the batched workload (2D Q1 Poisson,
 levels 3..7, Jacobi V(2,2)) in one batched hierarchy instead.
 With --spmv / --lgs: only the finest level's dmatmul_minus / Gauss-Seidel
 sweep (l_lgs, one launch per colour) in FP32, --cycles times.
+With --local NUNI: the locally refined L-shaped elasticity workload (NUNI
+uniform + --nloc local refinements, block ILU(0) V(2,2)) instead.
 """
 import argparse
 
@@ -29,7 +31,19 @@ def main():
     ap.add_argument("--spmv", action="store_true")
     ap.add_argument("--lgs", action="store_true", help="only the finest level's FP32 Gauss-Seidel sweep (l_lgs)")
     ap.add_argument("--pool", type=int, default=0, help="one request in a one-slot serving pool of this depth")
+    ap.add_argument("--local", type=int, default=0, help="uniform refinements of the locally refined workload")
+    ap.add_argument("--nloc", type=int, default=9)
     a = ap.parse_args()
+    if a.local:
+        gen = G.LocalGenerator(a.local, a.nloc, seed=2026)
+        mg = G.MultiGrid(gen, order=G.ORDER_DOMAIN, fp32=True)
+        G.setup_lmgc(mg, "ilu", baselevel=0, red=1e-8, maxit=a.cycles, mixed=not a.fp64, graph=False)
+        mg.launch_count(reset=True)
+        x, lr = mg.solve_host("mgs", gen.rhs)
+        print(f"cycles={lr.iters} defect {lr.first_defect[0]:.3e} -> {lr.last_defect[0]:.3e}, "
+              f"{mg.launch_count()} kernel launches")
+        mg.close()
+        return
     if a.pool:
         from ug_gb300.serve import Pool
         p = Pool(a.pool, 1)
