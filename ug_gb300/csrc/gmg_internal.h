@@ -124,6 +124,28 @@ struct Level {
   float *sell_v32 = nullptr;
   // the forward schedule's wavefronts are contiguous row ranges (multicolour order)
   bool waves_contiguous = false;
+  // subdomain order (GMG_ORDER_DOMAIN): rows 0..dom_nint are the interiors of
+  // dom_nreg subdomains (no neighbour outside their own subdomain), the rest
+  // interface rows, colour c at dom_cptr[c]..dom_cptr[c+1].  Per subdomain
+  // its interior wavefronts, forward (dom_f*) and backward (dom_b*):
+  // subdomain r's waves are wptr[wbeg[r]..wbeg[r+1]], wave w is rows
+  // rows[wptr[w]..wptr[w+1]]; dom_iface lists rows dom_nint..n-1
+  int dom_nreg = 0, dom_nint = 0;
+  std::vector<int> dom_cptr;
+  int *dom_fwbeg = nullptr, *dom_fwptr = nullptr, *dom_frows = nullptr;
+  int *dom_bwbeg = nullptr, *dom_bwptr = nullptr, *dom_brows = nullptr;
+  int *dom_iface = nullptr;
+  std::vector<int> h_dom_fwbeg, h_dom_fwptr, h_dom_frows, h_dom_bwbeg, h_dom_bwptr, h_dom_brows;
+  // the ILU factors of every subdomain interior in local numbering (filled by
+  // the ilu PreProcess): interior row at position p of the wave list has
+  // entries ent0[p]..ent0[p+1] with the subdomain-local column col[] and the
+  // factor entry k[]; a subdomain's rows outside its interior that the
+  // backward sweep reads are ext[ext0[r]..ext0[r+1]] (local numbers after
+  // the interior); smem = the shared memory one subdomain block needs
+  struct RegionTab {
+    int *ent0 = nullptr, *col = nullptr, *k = nullptr, *ext0 = nullptr, *ext = nullptr;
+    int max_rows = 0, max_ent = 0, max_waves = 0;
+  } dom_lt, dom_ut;
 };
 
 struct Vec {

@@ -94,6 +94,22 @@ inline void pdl_launch(gmg_mg *mg, void (*kern)(KP...), dim3 grid, dim3 block, A
 }
 #define GMG_LAUNCH(K, G, B, ...) pdl_launch(mg, K, dim3(G), dim3(B), __VA_ARGS__)
 
+// the same with dynamic shared memory (at most the default 48 KB)
+template <typename... KP, typename... A>
+inline void pdl_launch_smem(gmg_mg *mg, void (*kern)(KP...), dim3 grid, dim3 block, size_t smem, A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = mg->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = mg->opts.disable_pdl ? 0 : 1;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
 // the CSR entries k0 + lane + TPR q (q < Q) of one row held by one lane,
 // prefetched before the wait
 template <class T, int S, int Q>
@@ -743,6 +759,186 @@ __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ ro
       t[(size_t)row * S + r] = v;
     }
   }
+}
+
+// ILU sweep over the subdomain interiors of GMG_ORDER_DOMAIN: one block per
+// subdomain walks its own wavefronts, separated by __syncthreads (an interior
+// row has no neighbour outside its subdomain, so no other block's rows are
+// involved; the interface rows run before (backward) or after (forward) as
+// ordinary colour launches).  FWD: t = b - L t (unit lower factor), 0 off
+// ACTIVE rows; backward: t = D^{-1} (t - U t) on ACTIVE rows.
+constexpr int REGION_BLK = 256;
+template <class T, int S, int TPR, bool ALL_ACTIVE, bool FWD>
+__global__ void __launch_bounds__(REGION_BLK) ilu_region_kernel(
+    const int *__restrict__ wbeg, const int *__restrict__ wptr, const int *__restrict__ rows,
+    const int *__restrict__ rowptr, const int *__restrict__ col, const T *__restrict__ val, const T *__restrict__ dinv,
+    const uint8_t *__restrict__ flags, const T *__restrict__ b, T *t) {
+  pdl_prologue();
+  const int w0 = __ldg(wbeg + blockIdx.x), w1 = __ldg(wbeg + blockIdx.x + 1);
+  const int sub = threadIdx.x / TPR, lane = threadIdx.x & (TPR - 1);
+  for (int w = w0; w < w1; ++w) {
+    const int a = __ldg(wptr + w), e = __ldg(wptr + w + 1);
+    for (int base = a; base < e; base += REGION_BLK / TPR) {
+      const int idx = base + sub;
+      const bool valid = idx < e;
+      const int row = valid ? __ldg(rows + idx) : 0;
+      const bool act = valid && (ALL_ACTIVE || (flags[row] & F_ACTIVE));
+      T sm[S];
+#pragma unroll
+      for (int r = 0; r < S; ++r) sm[r] = T(0);
+      if (act) {
+        const int k1 = __ldg(rowptr + row + 1);
+        for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+          const int j = __ldg(col + k);
+          const T *m = val + (size_t)k * (S * S);
+          T yv[S];
+#pragma unroll
+          for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
+#pragma unroll
+          for (int r = 0; r < S; ++r)
+#pragma unroll
+            for (int c = 0; c < S; ++c) sm[r] = fma(__ldg(m + r * S + c), yv[c], sm[r]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < S; ++r) sm[r] = group_sum<TPR>(sm[r]);
+      if (valid && lane == 0) {
+        if (FWD) {
+#pragma unroll
+          for (int r = 0; r < S; ++r) t[(size_t)row * S + r] = act ? b[(size_t)row * S + r] - sm[r] : T(0);
+        } else if (act) {
+          T rhs[S];
+#pragma unroll
+          for (int r = 0; r < S; ++r) rhs[r] = t[(size_t)row * S + r] - sm[r];
+          const T *D = dinv + (size_t)row * S * S;
+#pragma unroll
+          for (int r = 0; r < S; ++r) {
+            T v = T(0);
+#pragma unroll
+            for (int c = 0; c < S; ++c) v = fma(D[r * S + c], rhs[c], v);
+            t[(size_t)row * S + r] = v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The same sweep with the subdomain in shared memory: the block first copies
+// its interior rows' right-hand side (forward) or current values (backward),
+// the rows outside the interior it reads, its factor entries (local columns,
+// values), the interior rows' entry ranges, ACTIVE flags and (backward)
+// inverse diagonal blocks, and its wavefront bounds; the wavefronts then
+// touch shared memory only, and the results are written back at the end.
+// Dynamic shared memory, region_smem_bytes(): values (max_ent * S*S), inverse
+// diagonals (max_rows * S*S, backward), vector entries (max_rows * S), then
+// columns (max_ent), entry offsets (max_rows + 1), wave bounds
+// (max_waves + 1) and flags (max_rows).
+constexpr int REGION_TPR = 4;
+template <class T, int S, bool ALL_ACTIVE, bool FWD>
+__global__ void __launch_bounds__(REGION_BLK) ilu_region_smem_kernel(
+    const int *__restrict__ wbeg, const int *__restrict__ wptr, const int *__restrict__ rows,
+    const int *__restrict__ ent0, const int *__restrict__ lcol, const int *__restrict__ kidx,
+    const int *__restrict__ ext0, const int *__restrict__ ext, const T *__restrict__ val, const T *__restrict__ dinv,
+    const uint8_t *__restrict__ flags, const T *__restrict__ b, T *t, int max_ent, int max_rows) {
+  constexpr int SS = S * S, TPR = REGION_TPR;
+  extern __shared__ __align__(16) unsigned char region_smem[];
+  T *v_s = reinterpret_cast<T *>(region_smem);
+  T *d_s = v_s + (size_t)max_ent * SS;
+  T *t_s = d_s + (FWD ? 0 : (size_t)max_rows * SS);
+  int *c_s = reinterpret_cast<int *>(t_s + (size_t)max_rows * S);
+  int *eo_s = c_s + max_ent;
+  int *w_s = eo_s + max_rows + 1;
+  const int r = blockIdx.x;
+  const int wb = __ldg(wbeg + r), we = __ldg(wbeg + r + 1);
+  uint8_t *a_s = reinterpret_cast<uint8_t *>(w_s + (we - wb) + 1);
+  // structure first (constant for the hierarchy's lifetime), then the wait
+  const int i0 = __ldg(wptr + wb), i1 = __ldg(wptr + we), nloc = i1 - i0;
+  const int x0 = __ldg(ext0 + r), x1 = __ldg(ext0 + r + 1);
+  const int e0 = __ldg(ent0 + i0), e1 = __ldg(ent0 + i1);
+  for (int e = threadIdx.x; e < e1 - e0; e += blockDim.x) {
+    c_s[e] = __ldg(lcol + e0 + e);
+    const T *m = val + (size_t)__ldg(kidx + e0 + e) * SS;
+#pragma unroll
+    for (int q = 0; q < SS; ++q) v_s[e * SS + q] = __ldg(m + q);
+  }
+  for (int q = threadIdx.x; q <= nloc; q += blockDim.x) eo_s[q] = __ldg(ent0 + i0 + q) - e0;
+  for (int w = threadIdx.x; w <= we - wb; w += blockDim.x) w_s[w] = __ldg(wptr + wb + w) - i0;
+  for (int q = threadIdx.x; q < nloc; q += blockDim.x) {
+    const int row = __ldg(rows + i0 + q);
+    a_s[q] = ALL_ACTIVE || (flags[row] & F_ACTIVE);
+    if (!FWD)
+#pragma unroll
+      for (int k = 0; k < SS; ++k) d_s[q * SS + k] = __ldg(dinv + (size_t)row * SS + k);
+  }
+  pdl_prologue();
+  for (int q = threadIdx.x; q < nloc; q += blockDim.x) {
+    const int row = __ldg(rows + i0 + q);
+#pragma unroll
+    for (int c = 0; c < S; ++c) t_s[q * S + c] = FWD ? b[(size_t)row * S + c] : t[(size_t)row * S + c];
+  }
+  for (int q = threadIdx.x; q < x1 - x0; q += blockDim.x) {
+    const int row = __ldg(ext + x0 + q);
+#pragma unroll
+    for (int c = 0; c < S; ++c) t_s[(nloc + q) * S + c] = t[(size_t)row * S + c];
+  }
+  __syncthreads();
+  const int sub = threadIdx.x / TPR, lane = threadIdx.x & (TPR - 1);
+  for (int w = 0; w < we - wb; ++w) {
+    const int a = w_s[w], e = w_s[w + 1];
+    for (int base = a; base < e; base += REGION_BLK / TPR) {
+      const int q = base + sub;
+      const bool valid = q < e;
+      const bool act = valid && a_s[q];
+      T sm[S];
+#pragma unroll
+      for (int rr = 0; rr < S; ++rr) sm[rr] = T(0);
+      if (act) {
+        const int k1 = eo_s[q + 1];
+        for (int k = eo_s[q] + lane; k < k1; k += TPR) {
+          const int j = c_s[k];
+          const T *m = v_s + k * SS;
+#pragma unroll
+          for (int rr = 0; rr < S; ++rr)
+#pragma unroll
+            for (int c = 0; c < S; ++c) sm[rr] = fma(m[rr * S + c], t_s[j * S + c], sm[rr]);
+        }
+      }
+#pragma unroll
+      for (int rr = 0; rr < S; ++rr) sm[rr] = group_sum<TPR>(sm[rr]);
+      if (valid && lane == 0) {
+        if (FWD) {
+#pragma unroll
+          for (int rr = 0; rr < S; ++rr) t_s[q * S + rr] = act ? t_s[q * S + rr] - sm[rr] : T(0);
+        } else if (act) {
+          T rhs[S];
+#pragma unroll
+          for (int rr = 0; rr < S; ++rr) rhs[rr] = t_s[q * S + rr] - sm[rr];
+          const T *D = d_s + q * SS;
+#pragma unroll
+          for (int rr = 0; rr < S; ++rr) {
+            T v = T(0);
+#pragma unroll
+            for (int c = 0; c < S; ++c) v = fma(D[rr * S + c], rhs[c], v);
+            t_s[q * S + rr] = v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < nloc; q += blockDim.x) {
+    const int row = __ldg(rows + i0 + q);
+#pragma unroll
+    for (int c = 0; c < S; ++c) t[(size_t)row * S + c] = t_s[q * S + c];
+  }
+}
+
+template <class T, int S>
+size_t region_smem_bytes(const Level::RegionTab &R, bool fwd) {
+  return (size_t(R.max_ent) * S * S + (fwd ? 0 : size_t(R.max_rows) * S * S) + size_t(R.max_rows) * S) * sizeof(T) +
+         (size_t(R.max_ent) + R.max_rows + 1 + R.max_waves + 1) * sizeof(int) + size_t(R.max_rows);
 }
 
 // ------------------------------------------------------------ StandardRestrict
@@ -1634,8 +1830,51 @@ int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
   return 0;
 }
 
+// the ILU solve in subdomain order: interiors (one block per subdomain), the
+// interface colours forward; the interface colours backward, interiors
+template <class T, int S, int TPR, bool ALL>
+int ilu_domain(gmg_mg *mg, const Level &L, T *t, const T *b) {
+  const T *lv = mval<T>(L.L), *uv = mval<T>(L.U), *ud = udinv_of<T>(L);
+  const int nc = int(L.dom_cptr.size()) - 1;
+  const size_t fsm = region_smem_bytes<T, S>(L.dom_lt, true), bsm = region_smem_bytes<T, S>(L.dom_ut, false);
+  const bool smem = L.dom_lt.ent0 && fsm <= 48 * 1024 && bsm <= 48 * 1024;
+  if (smem)
+    pdl_launch_smem(mg, ilu_region_smem_kernel<T, S, ALL, true>, dim3(L.dom_nreg), dim3(REGION_BLK), fsm,
+                    L.dom_fwbeg, L.dom_fwptr, L.dom_frows, L.dom_lt.ent0, L.dom_lt.col, L.dom_lt.k, L.dom_lt.ext0,
+                    L.dom_lt.ext, lv, (const T *)nullptr, L.flags, b, t, L.dom_lt.max_ent, L.dom_lt.max_rows);
+  else
+    GMG_LAUNCH((ilu_region_kernel<T, S, TPR, ALL, true>), L.dom_nreg, REGION_BLK, L.dom_fwbeg, L.dom_fwptr,
+               L.dom_frows, L.L.rowptr, L.L.col, lv, (const T *)nullptr, L.flags, b, t);
+  LAUNCH_CHECK(mg);
+  for (int c = 0; c < nc; ++c) {
+    const int r0 = L.dom_cptr[c], nr = L.dom_cptr[c + 1] - r0;
+    if (nr <= 0) continue;
+    GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, ALL>), grid_for((long long)nr * TPR), BLK, L.dom_iface + (r0 - L.dom_nint),
+               nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
+    LAUNCH_CHECK(mg);
+  }
+  for (int c = nc - 1; c >= 0; --c) {
+    const int r0 = L.dom_cptr[c], nr = L.dom_cptr[c + 1] - r0;
+    if (nr <= 0) continue;
+    GMG_LAUNCH((ilu_bwd_kernel<T, S, TPR, ALL>), grid_for((long long)nr * TPR), BLK, L.dom_iface + (r0 - L.dom_nint),
+               nr, L.U.rowptr, L.U.col, uv, ud, L.flags, t);
+    LAUNCH_CHECK(mg);
+  }
+  if (smem)
+    pdl_launch_smem(mg, ilu_region_smem_kernel<T, S, ALL, false>, dim3(L.dom_nreg), dim3(REGION_BLK), bsm,
+                    L.dom_bwbeg, L.dom_bwptr, L.dom_brows, L.dom_ut.ent0, L.dom_ut.col, L.dom_ut.k, L.dom_ut.ext0,
+                    L.dom_ut.ext, uv, ud, L.flags, (const T *)nullptr, t, L.dom_ut.max_ent, L.dom_ut.max_rows);
+  else
+    GMG_LAUNCH((ilu_region_kernel<T, S, TPR, ALL, false>), L.dom_nreg, REGION_BLK, L.dom_bwbeg, L.dom_bwptr,
+               L.dom_brows, L.U.rowptr, L.U.col, uv, ud, L.flags, (const T *)nullptr, t);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 template <class T, int S, int TPR>
 int ilu_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
+  if (L.dom_nreg > 0)
+    return L.all_active ? ilu_domain<T, S, TPR, true>(mg, L, t, b) : ilu_domain<T, S, TPR, false>(mg, L, t, b);
   const T *lv = mval<T>(L.L), *uv = mval<T>(L.U), *ud = udinv_of<T>(L);
   for (int w = 0; w < L.lower.nwave(); ++w) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;

@@ -173,7 +173,14 @@ static std::vector<std::vector<int>> sym_adjacency(int n, const int *rowptr, con
 // every row from its neighbours and weakens ILU(0) badly on systems).
 constexpr int DOMAIN_ROWS = 64;
 
-static std::vector<int> domain_order(int n, const std::vector<std::vector<int>> &adj) {
+struct DomainOrder {
+  std::vector<int> perm;    // processing order
+  std::vector<int> region;  // subdomain of every (UG-order) row
+  int nreg = 0, nint = 0;   // subdomains; interior rows (processing rows 0..nint)
+  std::vector<int> cptr;    // interface colour c: processing rows cptr[c]..cptr[c+1]
+};
+
+static DomainOrder domain_order(int n, const std::vector<std::vector<int>> &adj) {
   std::vector<int> bfs, pos(n, -1);
   bfs.reserve(n);
   for (int s0 = 0; s0 < n; ++s0) {
@@ -219,9 +226,43 @@ static std::vector<int> domain_order(int n, const std::vector<std::vector<int>> 
   std::vector<int> ord(iface.size());
   std::iota(ord.begin(), ord.end(), 0);
   std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return colour[a] < colour[b]; });
-  std::vector<int> perm = std::move(interior);
-  for (int k : ord) perm.push_back(iface[k]);
-  return perm;
+  DomainOrder D;
+  D.nint = int(interior.size());
+  D.perm = std::move(interior);
+  for (int k : ord) D.perm.push_back(iface[k]);
+  D.region = std::move(region);
+  D.nreg = nreg;
+  D.cptr.assign(nc + 1, 0);
+  for (int c : colour) D.cptr[c + 1]++;
+  for (int c = 0; c < nc; ++c) D.cptr[c + 1] += D.cptr[c];
+  for (int &v : D.cptr) v += D.nint;
+  return D;
+}
+
+// the interior rows of every subdomain grouped by wavefront: subdomain r's
+// waves are wptr[wbeg[r]..wbeg[r+1]], wave w is rows[wptr[w]..wptr[w+1]]
+static void domain_waves(int nint, const std::vector<int> &reg_of, const std::vector<int> &ptr,
+                         const std::vector<int> &rows, int nreg, std::vector<int> &wbeg, std::vector<int> &wptr,
+                         std::vector<int> &out) {
+  std::vector<int> wave_of(nint, 0);
+  for (int w = 0; w + 1 < int(ptr.size()); ++w)
+    for (int k = ptr[w]; k < ptr[w + 1]; ++k)
+      if (rows[k] < nint) wave_of[rows[k]] = w;
+  out.resize(nint);
+  std::iota(out.begin(), out.end(), 0);
+  std::stable_sort(out.begin(), out.end(), [&](int a, int b) {
+    return reg_of[a] != reg_of[b] ? reg_of[a] < reg_of[b] : wave_of[a] < wave_of[b];
+  });
+  wbeg.assign(1, 0);
+  wptr.assign(1, 0);
+  for (int r = 0, k = 0; r < nreg; ++r) {
+    while (k < nint && reg_of[out[k]] == r) {
+      const int w = wave_of[out[k]];
+      while (k < nint && reg_of[out[k]] == r && wave_of[out[k]] == w) ++k;
+      wptr.push_back(k);
+    }
+    wbeg.push_back(int(wptr.size()) - 1);
+  }
 }
 
 // Level sets of the triangular dependency graph in processing order.
@@ -278,6 +319,9 @@ struct HostLevel {
   std::vector<double> pw, rw;
   bool all_active = true, any_skip = false, contiguous = false;
   int ncolour = 0;
+  // subdomain order: per-subdomain interior waves (forward / backward), interface colours
+  int dom_nreg = 0, dom_nint = 0;
+  std::vector<int> dom_region, dom_cptr, dom_fwbeg, dom_fwptr, dom_frows, dom_bwbeg, dom_bwptr, dom_brows;
   std::vector<int> sptr, scol;  // sliced ELLPACK (32-row slices)
   std::vector<double> sval;
 };
@@ -353,7 +397,12 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
     }
     H.contiguous = true;
   } else if (order == GMG_ORDER_DOMAIN && n > 0) {
-    H.perm = domain_order(n, adj);
+    DomainOrder D = domain_order(n, adj);
+    H.perm = std::move(D.perm);
+    H.dom_region = std::move(D.region);
+    H.dom_nreg = D.nreg;
+    H.dom_nint = D.nint;
+    H.dom_cptr = std::move(D.cptr);
   }
   H.iperm.resize(n);
   for (int i = 0; i < n; ++i) H.iperm[H.perm[i]] = i;
@@ -399,6 +448,12 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
     }
     wavefronts(n, padj, true, H.lptr, H.lrows);
     wavefronts(n, padj, false, H.uptr, H.urows);
+    if (H.dom_nreg > 0) {
+      std::vector<int> reg_of(H.dom_nint);
+      for (int i = 0; i < H.dom_nint; ++i) reg_of[i] = H.dom_region[H.perm[i]];
+      domain_waves(H.dom_nint, reg_of, H.lptr, H.lrows, H.dom_nreg, H.dom_fwbeg, H.dom_fwptr, H.dom_frows);
+      domain_waves(H.dom_nint, reg_of, H.uptr, H.urows, H.dom_nreg, H.dom_bwbeg, H.dom_bwptr, H.dom_brows);
+    }
   }
   if (n >= SELL_MIN_ROWS) build_sell(H);
   return 0;
@@ -643,6 +698,29 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
     L.h_skip = std::move(h.skip);
   }
   GMG_CHECK(mg->arena.used <= mg->arena.size, "arena overflow");
+  // subdomain tables of the triangular sweeps
+  for (int l = 0; l < nlevels; ++l) {
+    HostLevel &h = H[l];
+    Level &L = mg->lev[l];
+    if (h.dom_nreg == 0) continue;
+    L.dom_nreg = h.dom_nreg;
+    L.dom_nint = h.dom_nint;
+    L.dom_cptr = h.dom_cptr;
+    L.h_dom_fwbeg = h.dom_fwbeg; L.h_dom_fwptr = h.dom_fwptr; L.h_dom_frows = h.dom_frows;
+    L.h_dom_bwbeg = h.dom_bwbeg; L.h_dom_bwptr = h.dom_bwptr; L.h_dom_brows = h.dom_brows;
+    std::vector<int> iface(h.n - h.dom_nint);
+    std::iota(iface.begin(), iface.end(), h.dom_nint);
+    auto put = [&](int **dst, const std::vector<int> &src) -> int {
+      GMG_CUDA(cudaMalloc(dst, sizeof(int) * std::max<size_t>(src.size(), 1)));
+      L.own.push_back(*dst);
+      if (!src.empty()) GMG_CUDA(cudaMemcpy(*dst, src.data(), sizeof(int) * src.size(), cudaMemcpyHostToDevice));
+      return 0;
+    };
+    if (put(&L.dom_fwbeg, h.dom_fwbeg) || put(&L.dom_fwptr, h.dom_fwptr) || put(&L.dom_frows, h.dom_frows) ||
+        put(&L.dom_bwbeg, h.dom_bwbeg) || put(&L.dom_bwptr, h.dom_bwptr) || put(&L.dom_brows, h.dom_brows) ||
+        put(&L.dom_iface, iface))
+      return 1;
+  }
   // FULLREFINELEVEL (SetSurfaceClasses, gm/algebra.cc:2905-2921)
   mg->frl = nlevels - 1;
   for (int l = nlevels - 1; l >= 0; --l)

@@ -389,6 +389,44 @@ static int dev_copy(gmg::Level &L, T **dst, const std::vector<T> &src) {
   return 0;
 }
 
+// the factor entries of every subdomain interior in subdomain-local numbering
+// (GMG_ORDER_DOMAIN): the interior rows in wave order, then the rows outside
+// the interior the sweep reads (the subdomain's own interface rows, backward
+// only; the forward sweep of an interior row reads earlier interior rows only)
+static int region_tables(Level &L, const std::vector<int> &wbeg, const std::vector<int> &wptr,
+                         const std::vector<int> &rows, const std::vector<int> &fr, const std::vector<int> &fc, bool fwd,
+                         Level::RegionTab &T) {
+  std::vector<int> local(L.n, -1), ent0{0}, col, kk, ext0{0}, ext;
+  T.max_rows = T.max_ent = T.max_waves = 0;
+  for (int r = 0; r < L.dom_nreg; ++r) {
+    const int i0 = wptr[wbeg[r]], i1 = wptr[wbeg[r + 1]], nloc = i1 - i0;
+    for (int p = i0; p < i1; ++p) local[rows[p]] = p - i0;
+    const size_t x0 = ext.size(), c0 = col.size();
+    for (int p = i0; p < i1; ++p) {
+      const int row = rows[p];
+      for (int k = fr[row]; k < fr[row + 1]; ++k) {
+        const int j = fc[k];
+        if (local[j] < 0) {
+          GMG_CHECK(!fwd, "subdomain %d: forward ILU entry outside the interior", r);
+          local[j] = nloc + int(ext.size() - x0);
+          ext.push_back(j);
+        }
+        col.push_back(local[j]);
+        kk.push_back(k);
+      }
+      ent0.push_back(int(col.size()));
+    }
+    ext0.push_back(int(ext.size()));
+    T.max_rows = std::max(T.max_rows, nloc + int(ext.size() - x0));
+    T.max_ent = std::max(T.max_ent, int(col.size() - c0));
+    T.max_waves = std::max(T.max_waves, wbeg[r + 1] - wbeg[r]);
+    for (int p = i0; p < i1; ++p) local[rows[p]] = -1;
+    for (size_t q = x0; q < ext.size(); ++q) local[ext[q]] = -1;
+  }
+  return dev_copy(L, &T.ent0, ent0) || dev_copy(L, &T.col, col) || dev_copy(L, &T.k, kk) ||
+         dev_copy(L, &T.ext0, ext0) || dev_copy(L, &T.ext, ext);
+}
+
 // ILUPreProcess, iter.cc:5444: factor a copy of A and split it into the unit
 // lower factor, the strict upper factor and the inverted diagonal blocks.
 int NPIlu::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *result) {
@@ -432,6 +470,10 @@ int NPIlu::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel
     std::vector<float> lv32(lv.begin(), lv.end()), uv32(uv.begin(), uv.end()), ud32(ud.begin(), ud.end());
     if (dev_copy(L, &L.L.v32, lv32) || dev_copy(L, &L.U.v32, uv32) || dev_copy(L, &L.udinv32, ud32)) return 1;
   }
+  if (L.dom_nreg > 0 &&
+      (region_tables(L, L.h_dom_fwbeg, L.h_dom_fwptr, L.h_dom_frows, lr, lc, true, L.dom_lt) ||
+       region_tables(L, L.h_dom_bwbeg, L.h_dom_bwptr, L.h_dom_brows, ur, uc, false, L.dom_ut)))
+    return 1;
   L.ilu_ready = true;
   return 0;
 }
