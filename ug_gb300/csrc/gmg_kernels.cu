@@ -680,26 +680,46 @@ __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ ro
 // ------------------------------------------------------------ l_luiter
 // ugiter.cc:4444: forward with the unit lower factor, then backward with the
 // strict upper factor and the stored inverse diagonal (StoreInverse).
+// One wavefront of the ILU solve, TPR threads per row.  Each lane's first
+// entry (column, factor block) and, backward, the inverse diagonal block are
+// loaded before the launch wait (constant structure), so only the gathers of
+// t written by the previous wavefront remain after it.
 template <class T, int S, int TPR, bool ALL_ACTIVE>
 __global__ void __launch_bounds__(BLK) ilu_fwd_kernel(const int *__restrict__ rows, int nrows,
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
                                                       const T *__restrict__ val, const uint8_t *__restrict__ flags,
                                                       const T *__restrict__ b, T *__restrict__ t) {
-  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
   const int row = valid ? __ldg(rows + idx) : 0;
   const bool active = ALL_ACTIVE || (valid && (flags[row] & F_ACTIVE));
+  int k = 0, k1 = 0, j0 = 0;
+  T m0[S * S];
+  if (valid && active) {
+    k = __ldg(rowptr + row) + lane;
+    k1 = __ldg(rowptr + row + 1);
+    if (k < k1) {
+      j0 = __ldg(col + k);
+#pragma unroll
+      for (int e = 0; e < S * S; ++e) m0[e] = __ldg(val + (size_t)k * (S * S) + e);
+    }
+  }
+  pdl_prologue();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
-  if (valid && active) {
-    const int k1 = __ldg(rowptr + row + 1);
-    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+  if (k < k1) {
+    T yv[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j0 * S + c];
+#pragma unroll
+    for (int r = 0; r < S; ++r)
+#pragma unroll
+      for (int c = 0; c < S; ++c) s[r] = fma(m0[r * S + c], yv[c], s[r]);
+    for (k += TPR; k < k1; k += TPR) {
       const int j = __ldg(col + k);
       const T *m = val + (size_t)k * (S * S);
-      T yv[S];
 #pragma unroll
       for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
 #pragma unroll
@@ -721,21 +741,40 @@ __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ ro
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
                                                       const T *__restrict__ val, const T *__restrict__ dinv,
                                                       const uint8_t *__restrict__ flags, T *__restrict__ t) {
-  pdl_prologue();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
   const int row = valid ? __ldg(rows + idx) : 0;
   const bool work = valid && (ALL_ACTIVE || (flags[row] & F_ACTIVE));
+  int k = 0, k1 = 0, j0 = 0;
+  T m0[S * S], D[S * S];
+  if (work) {
+    k = __ldg(rowptr + row) + lane;
+    k1 = __ldg(rowptr + row + 1);
+    if (k < k1) {
+      j0 = __ldg(col + k);
+#pragma unroll
+      for (int e = 0; e < S * S; ++e) m0[e] = __ldg(val + (size_t)k * (S * S) + e);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int e = 0; e < S * S; ++e) D[e] = __ldg(dinv + (size_t)row * S * S + e);
+  }
+  pdl_prologue();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
-  if (work) {
-    const int k1 = __ldg(rowptr + row + 1);
-    for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+  if (k < k1) {
+    T yv[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j0 * S + c];
+#pragma unroll
+    for (int r = 0; r < S; ++r)
+#pragma unroll
+      for (int c = 0; c < S; ++c) s[r] = fma(m0[r * S + c], yv[c], s[r]);
+    for (k += TPR; k < k1; k += TPR) {
       const int j = __ldg(col + k);
       const T *m = val + (size_t)k * (S * S);
-      T yv[S];
 #pragma unroll
       for (int c = 0; c < S; ++c) yv[c] = t[(size_t)j * S + c];
 #pragma unroll
@@ -750,7 +789,6 @@ __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ ro
     T rhs[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) rhs[r] = t[(size_t)row * S + r] - s[r];
-    const T *D = dinv + (size_t)row * S * S;
 #pragma unroll
     for (int r = 0; r < S; ++r) {
       T v = T(0);
