@@ -165,6 +165,19 @@ int gmg_transfer_restrict_defect(gmg_np *np, int level, gmg_vec *to, gmg_vec *fr
 int gmg_transfer_interpolate_correction(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A,
                                         const double *damp, int *result);
 int gmg_transfer_postprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+/* NP_TRANSFER's solution operations (transfer.h:79-166 InterpolateNewVectors /
+ * ProjectSolution / AdaptCorrection; transfer.cc:775, 794, 812): after a
+ * refinement the new vectors (VNEW, set with gmg_mg_set_new_vectors) of levels
+ * fl+1..tl take the interpolated coarse solution (StandardIntNewNodeVector,
+ * transgrid.cc:354); a solution is projected from tl down to fl by copying
+ * each son node's value to its father (StandardProject, transgrid.cc:655);
+ * AdaptCorrection is UG's default no-op ($l is rejected). */
+int gmg_transfer_interpolate_new_vectors(gmg_np *np, int fl, int tl, gmg_vec *x, int *result);
+int gmg_transfer_project_solution(gmg_np *np, int fl, int tl, gmg_vec *x, int *result);
+int gmg_transfer_adapt_correction(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result);
+/* VNEW of a level's vectors (n ints, list order; gm.h VNEW, set for the vectors the
+ * last AdaptMultiGrid created) */
+int gmg_mg_set_new_vectors(gmg_mg *mg, int level, const int *vnew);
 
 /* NP_LINEAR_SOLVER (np/procs/ls.h:79-132); Solver takes (abslimit, reduction)
  * in the order of np/procs/ls.cc:637. */

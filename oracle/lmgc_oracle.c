@@ -364,6 +364,35 @@ void orc_interpolate(const orc_level *fine, double *to, const double *from, cons
   }
 }
 
+/* StandardIntNewNodeVector, np/algebra/transgrid.cc:354-430: every fine
+ * vector with VNEW set takes the coarse values through its transfer row (a
+ * corner copy, or the father element's shape functions GNs), every
+ * component, VECSKIP not consulted; the other fine vectors keep theirs. */
+void orc_interpolate_new(const orc_level *fine, const int *vnew, double *x_fine, const double *x_coarse) {
+  const int s = fine->s;
+  for (int f = 0; f < fine->n; ++f) {
+    if (!vnew[f]) continue;
+    for (int r = 0; r < s; ++r) {
+      double acc = 0.0;
+      for (int k = fine->prowptr[f]; k < fine->prowptr[f + 1]; ++k)
+        acc += fine->pw[k] * x_coarse[(size_t)fine->pcol[k] * s + r];
+      x_fine[(size_t)f * s + r] = acc;
+    }
+  }
+}
+
+/* StandardProject, transgrid.cc:655-700 (node vectors): a coarse vector
+ * whose node has a son node takes the son's values.  The son is the fine
+ * corner copy, the fine vector whose transfer row is the single weight 1. */
+void orc_project(const orc_level *fine, double *x_coarse, const double *x_fine) {
+  const int s = fine->s;
+  for (int f = 0; f < fine->n; ++f) {
+    const int k = fine->prowptr[f];
+    if (fine->prowptr[f + 1] - k != 1 || fine->pw[k] != 1.0) continue;
+    for (int r = 0; r < s; ++r) x_coarse[(size_t)fine->pcol[k] * s + r] = x_fine[(size_t)f * s + r];
+  }
+}
+
 /* ---------------------------------------------------------------- solver */
 typedef struct {
   const orc_mg *mg;

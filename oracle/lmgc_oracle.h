@@ -65,6 +65,9 @@ void orc_restrict(const orc_level *fine, const orc_level *coarse, double *to_coa
                   const double *from_fine, const double *damp);                   /* StandardRestrict */
 void orc_interpolate(const orc_level *fine, double *to_fine, const double *from_coarse,
                      const double *damp);                                         /* StandardInterpolateCorrection */
+void orc_interpolate_new(const orc_level *fine, const int *vnew, double *x_fine,
+                         const double *x_coarse);                                 /* StandardIntNewNodeVector */
+void orc_project(const orc_level *fine, double *x_coarse, const double *x_fine);  /* StandardProject */
 
 /* ---- solver ----
  * Solves A x = b on level top = nlevels-1 with ls + lmgc.  x (finest, n*s)

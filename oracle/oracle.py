@@ -88,6 +88,8 @@ def lib():
         L.orc_nrm2x.argtypes = [P, P, P]
         L.orc_restrict.argtypes = [P, P, P, P, P]
         L.orc_interpolate.argtypes = [P, P, P, P]
+        L.orc_interpolate_new.argtypes = [P, P, P, P]
+        L.orc_project.argtypes = [P, P, P]
         L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_ls_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_fullrefinelevel.argtypes = [P]
@@ -183,6 +185,34 @@ class Hierarchy:
         to = np.zeros(L["n"] * L["s"]); fr = np.ascontiguousarray(from_coarse, np.float64)
         dm = np.ones(MAX_S) if damp is None else np.resize(np.asarray(damp, np.float64), MAX_S)
         lib().orc_interpolate(self.lev(l), _p(to), _p(fr), _p(dm)); return to
+
+    def interpolate_new(self, l, vnew, x_fine, x_coarse):
+        """StandardIntNewNodeVector: fine vectors with VNEW take P x_coarse."""
+        xf = np.array(x_fine, np.float64); xc = np.ascontiguousarray(x_coarse, np.float64)
+        vn = np.ascontiguousarray(vnew, np.int32)
+        lib().orc_interpolate_new(self.lev(l), _p(vn), _p(xf), _p(xc)); return xf
+
+    def project(self, l, x_coarse, x_fine):
+        """StandardProject: coarse vectors with a son node take its values."""
+        xc = np.array(x_coarse, np.float64); xf = np.ascontiguousarray(x_fine, np.float64)
+        lib().orc_project(self.lev(l), _p(xc), _p(xf)); return xc
+
+    def interpolate_new_vectors(self, fl, tl, x_all, vnew):
+        """InterpolateNewVectors (transfer.cc:775): levels fl+1..tl in turn,
+        on an every-level vector (levels concatenated)."""
+        x = np.array(x_all, np.float64)
+        offs = np.cumsum([0] + self.level_lengths())
+        for l in range(fl + 1, tl + 1):
+            x[offs[l]:offs[l + 1]] = self.interpolate_new(l, vnew[l], x[offs[l]:offs[l + 1]], x[offs[l - 1]:offs[l]])
+        return x
+
+    def project_solution(self, fl, tl, x_all):
+        """ProjectSolution (transfer.cc:794): levels tl-1 down to fl."""
+        x = np.array(x_all, np.float64)
+        offs = np.cumsum([0] + self.level_lengths())
+        for l in range(tl - 1, fl - 1, -1):
+            x[offs[l]:offs[l + 1]] = self.project(l + 1, x[offs[l]:offs[l + 1]], x[offs[l + 1]:offs[l + 2]])
+        return x
 
     # ---- solver
     def bcgs_solve(self, rhs, **kw):

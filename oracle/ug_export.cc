@@ -58,6 +58,7 @@
 #include "numproc.h"
 #include "shapes.h"
 #include "std_domain.h"
+#include "transfer.h"
 #include "udm.h"
 #include "ugdevices.h"
 #include "ugm.h"
@@ -473,6 +474,33 @@ int main(int argc, char **argv) {
 
   // ---- full solve through UG's numprocs
   run("npcreate transfer $c transfer; npinit transfer;");
+  // ---- the transfer numproc's solution operations on every level
+  // (transfer.cc:775 InterpolateNewVectors -> StandardIntNewNodeVector,
+  // transfer.cc:794 ProjectSolution -> StandardProject), with VNEW of the
+  // last refinement step
+  {
+    NP_TRANSFER *tr = (NP_TRANSFER *)GetNumProcByName(mg, "transfer", TRANSFER_CLASS_NAME);
+    if (!tr) { fprintf(stderr, "transfer lookup failed\n"); return 1; }
+    auto grab_all = [&](VECDATA_DESC *vd) {
+      std::vector<double> r;
+      for (int l = 0; l <= top; ++l) { auto x = grab(vd, l); r.insert(r.end(), x.begin(), x.end()); }
+      return r;
+    };
+    for (int l = 0; l <= top; ++l) {
+      std::vector<int> vn;
+      for (VECTOR *v : g_lev[l].vecs) vn.push_back(VNEW(v) ? 1 : 0);
+      puti("L" + std::to_string(l) + "_vnew", vn);
+    }
+    for (int l = 0; l <= top; ++l) fill(kx, GRID_ON_LEVEL(mg, l));
+    putd("kat_newvec_pre", grab_all(kx));
+    INT r = 0;
+    if ((*tr->InterpolateNewVectors)(tr, 0, top, kx, &r)) { fprintf(stderr, "InterpolateNewVectors failed\n"); return 1; }
+    putd("kat_newvec", grab_all(kx));
+    for (int l = 0; l <= top; ++l) fill(kx, GRID_ON_LEVEL(mg, l));
+    putd("kat_project_pre", grab_all(kx));
+    if ((*tr->ProjectSolution)(tr, 0, top, kx, &r)) { fprintf(stderr, "ProjectSolution failed\n"); return 1; }
+    putd("kat_project", grab_all(kx));
+  }
   if (smoother == "jac") run("npcreate smooth $c jac; npinit smooth $damp 0.8;");
   else if (smoother == "gs") run("npcreate smooth $c gs; npinit smooth;");
   else run("npcreate smooth $c ilu; npinit smooth;");

@@ -233,3 +233,28 @@ def test_midsize_vs_oracle(G, oracle_mod, kind, nref, sm, bl, var, order):
     d = H.matmul_minus(mg.top, gen.rhs.reshape(-1, s)[perm].ravel(), x32.reshape(-1, s)[perm].ravel())
     assert np.all(H.nrm2x(mg.top, d) <= 1.01e-8 * H.nrm2x(mg.top, gen.rhs.reshape(-1, s)[perm].ravel()))
     mg.close()
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+@pytest.mark.parametrize("name", golden_names("all"))
+def test_solution_transfer_matches_ug(G, name, order):
+    """NP_TRANSFER's InterpolateNewVectors and ProjectSolution (transfer.cc:775,
+    794) on every level of UG's hierarchies: the new vectors of the last
+    refinement take UG's interpolated values, the projection copies son to
+    father as UG's StandardProject does, bit for bit."""
+    fx = load_golden(name)
+    mg = G.MultiGrid(G.levels_from_ugfx(fx), order=order)
+    mg.createvector("x")
+    mg.npcreate("tr", "transfer.gtransfer"); mg.npinit("tr", "")
+    n = mg.nlevels
+    offs = np.cumsum([0] + mg.level_len)
+    for l in range(n):
+        mg.set_new_vectors(l, fx[f"L{l}_vnew"])
+    for pre, post, op in (("kat_newvec_pre", "kat_newvec", mg.transfer_interpolate_new_vectors),
+                          ("kat_project_pre", "kat_project", mg.transfer_project_solution)):
+        for l in range(n):
+            mg.upload("x", l, fx[pre][offs[l]:offs[l + 1]])
+        op("tr", 0, n - 1, "x")
+        got = np.concatenate([mg.download("x", l) for l in range(n)])
+        assert np.array_equal(got, fx[post]), (name, post)
+    mg.close()

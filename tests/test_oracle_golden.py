@@ -140,3 +140,18 @@ def test_surface_solve_is_ls_on_uniform(name, oracle_mod):
     x2, it2, _, h2 = H.ls_solve_surface(fx["rhs_all"], **kw)
     assert it1 == it2 and np.array_equal(h1, h2)
     assert np.array_equal(_split(fx, x2)[-1], x1)
+
+
+@pytest.mark.parametrize("name", NAMES + LOCAL)
+def test_solution_transfer_matches_ug(name, oracle_mod):
+    """StandardIntNewNodeVector / StandardProject (transgrid.cc:354, 655) as
+    UG's transfer numproc runs them over every level (transfer.cc:775, 794):
+    the oracle repeats UG's results bit for bit."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    n = int(fx["nlevels"][0])
+    vnew = [fx[f"L{l}_vnew"] for l in range(n)]
+    x = H.interpolate_new_vectors(0, n - 1, fx["kat_newvec_pre"], vnew)
+    assert np.array_equal(x, fx["kat_newvec"])
+    x = H.project_solution(0, n - 1, fx["kat_project_pre"])
+    assert np.array_equal(x, fx["kat_project"])

@@ -93,6 +93,9 @@ def lib(build_if_missing: bool = True):
         "gmg_transfer_restrict_defect": ([P, I, P, P, P, P, P], I),
         "gmg_transfer_interpolate_correction": ([P, I, P, P, P, P, P], I),
         "gmg_transfer_postprocess": ([P, P, I, P, P, P, P], I),
+        "gmg_transfer_interpolate_new_vectors": ([P, I, I, P, P], I),
+        "gmg_transfer_project_solution": ([P, I, I, P, P], I),
+        "gmg_transfer_adapt_correction": ([P, I, P, P, P, P], I), "gmg_mg_set_new_vectors": ([P, I, P], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -504,6 +507,24 @@ class MultiGrid:
         if lib().gmg_ls_preprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(bl), C.byref(res)):
             _err(f"{obj} PreProcess")
         return bl.value
+
+    def set_new_vectors(self, level: int, vnew):
+        """VNEW flags of a level's vectors (list order)."""
+        a = np.ascontiguousarray(vnew, np.int32)
+        if a.size != self.size(level)[0]:
+            raise GmgError(f"set_new_vectors: {a.size} flags for {self.size(level)[0]} vectors")
+        if lib().gmg_mg_set_new_vectors(self._h, level, _ptr(a)):
+            _err("set_new_vectors")
+
+    def transfer_interpolate_new_vectors(self, obj, fl, tl, x):
+        res = C.c_int()
+        if lib().gmg_transfer_interpolate_new_vectors(self.np(obj), fl, tl, self.vec(x), C.byref(res)):
+            _err(f"{obj} InterpolateNewVectors")
+
+    def transfer_project_solution(self, obj, fl, tl, x):
+        res = C.c_int()
+        if lib().gmg_transfer_project_solution(self.np(obj), fl, tl, self.vec(x), C.byref(res)):
+            _err(f"{obj} ProjectSolution")
 
     def ls_defect(self, obj, level, x, b, A="MAT"):
         res = C.c_int()

@@ -40,6 +40,7 @@ enum : uint8_t {
   F_NEWDEF = 2,  // VCLASS >= NEWDEF_CLASS (2): restricted into the coarse grid
   F_RESET = 4,   // VNCLASS >= NEWDEF_CLASS (2): reset before restriction
   F_FINE = 8,    // FINE_GRID_DOF: VCLASS >= 2 and VNCLASS <= 1 (a surface row below the top level)
+  F_VNEW = 16,   // VNEW: created by the last refinement (gmg_mg_set_new_vectors)
 };
 
 // memcpy for large host buffers (several threads)
@@ -102,6 +103,9 @@ struct Level {
   std::vector<void *> own;      // cudaMalloc'd arrays owned outside the arena
   // transfer from level-1: P (rows = this level), R (rows = level-1 VECTORs)
   DevCSR P, R;
+  // son of every level-1 row: the row of this level that is its corner copy
+  // (a transfer row with the single weight 1), -1 if none (StandardProject)
+  int *son = nullptr;
   // base solve: explicit inverse of the level matrix (filled by ex PreProcess)
   double *ainv = nullptr;
   int base_dim = 0;
@@ -303,6 +307,10 @@ int k_refine_prepare(gmg_mg *mg, float *b32, float *c32, const double *b64, long
 // fine t = P (damp*coarse) honouring fine VECSKIP; acc += t if acc != null
 int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void *from, const double *damp,
                   void *acc);
+// StandardIntNewNodeVector: fine rows with F_VNEW take P x_coarse (every component)
+int k_interpolate_new(gmg_mg *mg, const Level &fine, int prec, void *x_fine, const void *x_coarse);
+// StandardProject: coarse rows with a son take the son's values
+int k_project(gmg_mg *mg, const Level &fine, const Level &coarse, int prec, void *x_coarse, const void *x_fine);
 // per-component 2-norms of the NEW_DEFECT rows into mg->norms_dev (device)
 int k_nrm2x(gmg_mg *mg, const Level &L, int prec, const void *x);
 // base level: if |b| >= abslimit in some component: t = Ainv b; b -= A t; c += t

@@ -2555,6 +2555,66 @@ int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *per
   return 0;
 }
 
+// ------------------------------------------------------------ solution transfer (transgrid.cc:354, 655)
+template <class T, int S>
+__global__ void __launch_bounds__(BLK) interp_new_kernel(int nf, const int *__restrict__ prow,
+                                                         const int *__restrict__ pcol, const double *__restrict__ pw,
+                                                         const uint8_t *__restrict__ flags, T *xf,
+                                                         const T *__restrict__ xc) {
+  pdl_prologue();
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    if (!(flags[f] & F_VNEW)) continue;
+    double acc[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc[r] = 0.0;
+    for (int k = prow[f]; k < prow[f + 1]; ++k) {
+      const int c = pcol[k];
+      const double w = pw[k];
+#pragma unroll
+      for (int r = 0; r < S; ++r) acc[r] = __dadd_rn(acc[r], __dmul_rn(w, double(xc[(size_t)c * S + r])));
+    }
+#pragma unroll
+    for (int r = 0; r < S; ++r) xf[(size_t)f * S + r] = T(acc[r]);
+  }
+}
+
+template <class T, int S>
+__global__ void __launch_bounds__(BLK) project_kernel(int nc, const int *__restrict__ son, T *xc,
+                                                      const T *__restrict__ xf) {
+  pdl_prologue();
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int f = son[c];
+    if (f < 0) continue;
+#pragma unroll
+    for (int r = 0; r < S; ++r) xc[(size_t)c * S + r] = xf[(size_t)f * S + r];
+  }
+}
+
+int k_interpolate_new(gmg_mg *mg, const Level &F, int prec, void *xf, const void *xc) {
+  if (F.n == 0) return 0;
+#define IN(TT, SS) GMG_LAUNCH((interp_new_kernel<TT, SS>), vec_grid(F.n), BLK, F.n, F.P.rowptr, F.P.col, F.P.v64, \
+                              F.flags, (TT *)xf, (const TT *)xc)
+  if (prec == GMG_PREC_FP64) { if (F.s == 1) IN(double, 1); else if (F.s == 2) IN(double, 2); else if (F.s == 3) IN(double, 3);
+                               else { set_error("block size %d not compiled", F.s); return 1; } }
+  else { if (F.s == 1) IN(float, 1); else if (F.s == 2) IN(float, 2); else if (F.s == 3) IN(float, 3);
+         else { set_error("block size %d not compiled", F.s); return 1; } }
+#undef IN
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_project(gmg_mg *mg, const Level &F, const Level &C, int prec, void *xc, const void *xf) {
+  if (C.n == 0) return 0;
+#define PJ(TT, SS) GMG_LAUNCH((project_kernel<TT, SS>), vec_grid(C.n), BLK, C.n, F.son, (TT *)xc, (const TT *)xf)
+  if (prec == GMG_PREC_FP64) { if (F.s == 1) PJ(double, 1); else if (F.s == 2) PJ(double, 2); else if (F.s == 3) PJ(double, 3);
+                               else { set_error("block size %d not compiled", F.s); return 1; } }
+  else { if (F.s == 1) PJ(float, 1); else if (F.s == 2) PJ(float, 2); else if (F.s == 3) PJ(float, 3);
+         else { set_error("block size %d not compiled", F.s); return 1; } }
+#undef PJ
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 // ------------------------------------------------------------ surface of a locally refined hierarchy
 // UG's ON_SURFACE loops (np/algebra/vecloop.ct, matloop.ct) visit the
 // FINE_GRID_DOF vectors of the levels FULLREFINELEVEL..top-1 and the

@@ -698,6 +698,17 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
     L.h_skip = std::move(h.skip);
   }
   GMG_CHECK(mg->arena.used <= mg->arena.size, "arena overflow");
+  // son of every coarse row (the fine corner copy), for StandardProject
+  for (int l = 1; l < nlevels; ++l) {
+    HostLevel &h = H[l];
+    std::vector<int> son(H[l - 1].n, -1);
+    for (int f = 0; f < h.n; ++f)
+      if (h.prow[f + 1] - h.prow[f] == 1 && h.pw[h.prow[f]] == 1.0) son[h.pcol[h.prow[f]]] = f;
+    Level &L = mg->lev[l];
+    GMG_CUDA(cudaMalloc(&L.son, sizeof(int) * std::max<size_t>(son.size(), 1)));
+    L.own.push_back(L.son);
+    if (!son.empty()) GMG_CUDA(cudaMemcpy(L.son, son.data(), sizeof(int) * son.size(), cudaMemcpyHostToDevice));
+  }
   // subdomain tables of the triangular sweeps
   for (int l = 0; l < nlevels; ++l) {
     HostLevel &h = H[l];
@@ -774,6 +785,21 @@ static std::vector<int> instance_rows(const Level &L, int off, int n) {
 }
 
 extern "C" {
+
+// VNEW of a level's vectors (list order), kept as row flag F_VNEW
+int gmg_mg_set_new_vectors(gmg_mg *mg, int level, const int *vnew) {
+  if (!mg || level < 0 || level >= int(mg->lev.size()) || !vnew) {
+    set_error("gmg_mg_set_new_vectors: bad arguments");
+    return 1;
+  }
+  Level &L = mg->lev[level];
+  for (int i = 0; i < L.n; ++i) {
+    uint8_t &f = L.h_flags[i];
+    f = uint8_t(vnew[L.perm[i]] ? (f | F_VNEW) : (f & ~F_VNEW));
+  }
+  if (L.n) GMG_CUDA(cudaMemcpy(L.flags, L.h_flags.data(), L.n, cudaMemcpyHostToDevice));
+  return 0;
+}
 
 int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *opts_in, gmg_mg **out) {
   if (!out || !levels || nlevels < 1) { set_error("gmg_mg_create: bad arguments"); return 1; }

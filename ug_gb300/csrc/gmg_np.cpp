@@ -621,6 +621,7 @@ int NPTransfer::Init(const Args &a) {  // TransferInit / NPTransferInit
   a.get_sc("damp", damp);
   GMG_CHECK(!a.option("M") && !a.option("S") && !a.option("D"),
             "transfer: only the standard (shape-function) mode is implemented");
+  GMG_CHECK(!a.option("l"), "transfer: $l (MinimizeLevel in AdaptCorrection) is not implemented");
   return (!A && !b && !x && !c) ? NP_ACTIVE : NP_EXECUTABLE;
 }
 
@@ -643,6 +644,24 @@ int NPTransfer::InterpolateCorrection(int level, gmg_vec *to, gmg_vec *from, gmg
   GMG_CHECK(to->prec == from->prec, "InterpolateCorrection: precision mismatch");
   return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), dmp, nullptr);
 }
+
+// InterpolateNewVectors, transfer.cc:775: StandardIntNewNodeVector on levels fl+1..tl
+int NPTransfer::InterpolateNewVectors(int fl, int tl, gmg_vec *xv, int *result) {
+  GMG_CHECK(xv && fl >= 0 && tl < int(mg->lev.size()), "InterpolateNewVectors: bad arguments");
+  for (int l = fl + 1; l <= tl; ++l)
+    if (k_interpolate_new(mg, mg->lev[l], xv->prec, vlev(xv, l), vlev(xv, l - 1))) return 1;
+  return 0;
+}
+
+// ProjectSolution, transfer.cc:794: StandardProject on levels tl-1 down to fl
+int NPTransfer::ProjectSolution(int fl, int tl, gmg_vec *xv, int *result) {
+  GMG_CHECK(xv && fl >= 0 && tl < int(mg->lev.size()), "ProjectSolution: bad arguments");
+  for (int l = tl - 1; l >= fl; --l)
+    if (k_project(mg, mg->lev[l + 1], mg->lev[l], xv->prec, vlev(xv, l), vlev(xv, l + 1))) return 1;
+  return 0;
+}
+
+int NPTransfer::AdaptCorrection(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *) { return check_level(mg, level); }
 
 int NPTransfer::Execute(const Args &a) {
   const int level = int(mg->lev.size()) - 1;
@@ -1634,6 +1653,21 @@ int gmg_transfer_interpolate_correction(gmg_np *np, int level, gmg_vec *to, gmg_
   AS(NPTransfer, np, NPK_TRANSFER);
   int dummy;
   return p->InterpolateCorrection(level, to, from, A, damp ? damp : p->damp, result ? result : &dummy);
+}
+int gmg_transfer_interpolate_new_vectors(gmg_np *np, int fl, int tl, gmg_vec *x, int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy = 0;
+  return p->InterpolateNewVectors(fl, tl, x, result ? result : &dummy);
+}
+int gmg_transfer_project_solution(gmg_np *np, int fl, int tl, gmg_vec *x, int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy = 0;
+  return p->ProjectSolution(fl, tl, x, result ? result : &dummy);
+}
+int gmg_transfer_adapt_correction(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) {
+  AS(NPTransfer, np, NPK_TRANSFER);
+  int dummy = 0;
+  return p->AdaptCorrection(level, c, b, A, result ? result : &dummy);
 }
 int gmg_transfer_postprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);

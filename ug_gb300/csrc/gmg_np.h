@@ -114,6 +114,12 @@ struct NPTransfer : gmg_np {
   virtual int InterpolateCorrection(int level, gmg_vec *to, gmg_vec *from, gmg_mat *A, const double *damp,
                                     int *result);
   virtual int PostProcess(int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+  // the solution on new vectors after a refinement (transfer.cc:775) and the
+  // projection of a solution to the coarser levels (transfer.cc:794)
+  virtual int InterpolateNewVectors(int fl, int tl, gmg_vec *x, int *result);
+  virtual int ProjectSolution(int fl, int tl, gmg_vec *x, int *result);
+  // transfer.cc:812: MinimizeLevel only with `$l`, which is not supported: a no-op
+  virtual int AdaptCorrection(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result);
   int Execute(const Args &a) override;
   std::string Display() const override;
 };
