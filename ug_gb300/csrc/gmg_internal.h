@@ -123,6 +123,7 @@ struct Level {
   // row itself): one thread per row, coalesced 32-row loads, no reductions
   bool sell = false;
   int *sell_ptr = nullptr;  // nslices+1 entry offsets
+  long long sell_nent = 0;  // stored entries (padding included)
   int *sell_col = nullptr;
   double *sell_v64 = nullptr;
   float *sell_v32 = nullptr;

@@ -52,6 +52,18 @@ struct PF {
 };
 constexpr long long PREFETCH_MAX_BLOCKS = 1100;  // ~280k rows (measured: the 65^3 level gains, 320k+ rows lose)
 
+// PN < 0 selects the plain loop with evict-first loads of the matrix stream
+// (ld.global.cs): used where a level's sliced-ELLPACK matrix is larger than
+// most of L2, so that its single-use stream does not push out the gathered
+// vector entries; smaller matrices keep the default policy, which lets them
+// stay in L2 from one smoothing step to the next.
+constexpr long long STREAM_MIN_BYTES = 96ll << 20;
+template <bool ST, class T>
+__device__ __forceinline__ T ld_mat(const T *p) {
+  if constexpr (ST) return __ldcs(p);
+  else return __ldg(p);
+}
+
 // a sliced-ELLPACK row i: entry k at e0 + 32 k, w entries (padding included);
 // the first PF<S>::N (column, block) pairs are held in registers
 template <class T, int S, int P_ = PF<S>::N>
@@ -268,16 +280,18 @@ __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__rest
                                                         const int *__restrict__ scol, const T *__restrict__ sval,
                                                         const TY *__restrict__ y, T *__restrict__ x,
                                                         TA *__restrict__ acc) {
+  constexpr int P0 = PN > 0 ? PN : 0;
+  constexpr bool ST = PN < 0;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  SellRow<T, S, PN> R;
+  SellRow<T, S, P0> R;
   R.load(i, sptr, scol, sval);
   pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
 #pragma unroll
-  for (int k = 0; k < PN; ++k) {
+  for (int k = 0; k < P0; ++k) {
     if (k < R.w) {
 #pragma unroll
       for (int c = 0; c < S; ++c) {
@@ -287,16 +301,16 @@ __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__rest
       }
     }
   }
-  int e = R.e0 + 32 * PN;
+  int e = R.e0 + 32 * P0;
 #pragma unroll 4
-  for (int k = PN; k < R.w; ++k, e += 32) {
-    const int j = __ldg(scol + e);
+  for (int k = P0; k < R.w; ++k, e += 32) {
+    const int j = ld_mat<ST>(scol + e);
     const T *m = sval + (size_t)e * (S * S);
 #pragma unroll
     for (int c = 0; c < S; ++c) {
       const T yv = T(y[(size_t)j * S + c]);
 #pragma unroll
-      for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + c), yv, s[r]);
+      for (int r = 0; r < S; ++r) s[r] = fma(ld_mat<ST>(m + r * S + c), yv, s[r]);
     }
   }
 #pragma unroll
@@ -531,16 +545,18 @@ __global__ void __launch_bounds__(BLK) sell_jac_step_kernel(int n, const int *__
                                                             const uint8_t *__restrict__ flags,
                                                             const T *__restrict__ bin, T *__restrict__ bout,
                                                             T *__restrict__ c, Damp<T> dm) {
+  constexpr int P0 = PN > 0 ? PN : 0;
+  constexpr bool ST = PN < 0;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  SellRow<T, S, PN> R;
+  SellRow<T, S, P0> R;
   R.load(i, sptr, scol, sval);
   pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
 #pragma unroll
-  for (int k = 0; k < PN; ++k) {
+  for (int k = 0; k < P0; ++k) {
     if (k < R.w) {
       T tv[S];
       jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, R.col[k], dm, tv);
@@ -550,17 +566,17 @@ __global__ void __launch_bounds__(BLK) sell_jac_step_kernel(int n, const int *__
         for (int r = 0; r < S; ++r) s[r] = fma(R.val[k][r * S + cc], tv[cc], s[r]);
     }
   }
-  int e = R.e0 + 32 * PN;
+  int e = R.e0 + 32 * P0;
 #pragma unroll 4
-  for (int k = PN; k < R.w; ++k, e += 32) {
-    const int j = __ldg(scol + e);
+  for (int k = P0; k < R.w; ++k, e += 32) {
+    const int j = ld_mat<ST>(scol + e);
     const T *m = sval + (size_t)e * (S * S);
     T tv[S];
     jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, j, dm, tv);
 #pragma unroll
     for (int cc = 0; cc < S; ++cc)
 #pragma unroll
-      for (int r = 0; r < S; ++r) s[r] = fma(__ldg(m + r * S + cc), tv[cc], s[r]);
+      for (int r = 0; r < S; ++r) s[r] = fma(ld_mat<ST>(m + r * S + cc), tv[cc], s[r]);
   }
   T ti[S];
   jac_value<T, S, ALL_ACTIVE>(dinv, flags, bin, i, dm, ti);
@@ -1793,16 +1809,23 @@ template <>
 const double *sell_val<double>(const Level &L) { return L.sell_v64; }
 template <>
 const float *sell_val<float>(const Level &L) { return L.sell_v32; }
+// bytes of a level's sliced-ELLPACK matrix stream in precision T
+template <class T>
+long long sell_bytes(const Level &L) { return L.sell_nent * ((long long)L.s * L.s * sizeof(T) + 4); }
 
 template <class T, class TY, bool ACC>
 int spmv_dispatch(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, TY *acc) {
   if (L.sell && sell_val<T>(L)) {
     const T *sv = sell_val<T>(L);
     const bool pre = grid_for(L.n) <= PREFETCH_MAX_BLOCKS;
+    const bool st = sell_bytes<T>(L) > STREAM_MIN_BYTES;
 #define SK(SS)                                                                                                   \
   if (pre)                                                                                                       \
     GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, SS, ACC, PF<SS>::N>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, \
                sv, y, x, acc);                                                                                   \
+  else if (st)                                                                                                   \
+    GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, SS, ACC, -1>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, \
+               x, acc);                                                                                          \
   else                                                                                                           \
     GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, SS, ACC, 0>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, sv, y, \
                x, acc);
@@ -2122,10 +2145,14 @@ int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const floa
     return k_matmul_minus_mixed(mg, L, b, GMG_PREC_FP32, c);
   }
   const bool pre = grid_for(L.n) <= PREFETCH_MAX_BLOCKS;
+  const bool st = sell_bytes<double>(L) > STREAM_MIN_BYTES;
 #define RU(SS)                                                                                                   \
   if (pre)                                                                                                       \
     GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, PF<SS>::N>), grid_for(L.n), BLK, L.n,          \
                L.sell_ptr, L.sell_col, L.sell_v64, c, b, x);                                                     \
+  else if (st)                                                                                                   \
+    GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, -1>), grid_for(L.n), BLK, L.n, L.sell_ptr,     \
+               L.sell_col, L.sell_v64, c, b, x);                                                                 \
   else                                                                                                           \
     GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, 0>), grid_for(L.n), BLK, L.n, L.sell_ptr,      \
                L.sell_col, L.sell_v64, c, b, x);
@@ -2164,6 +2191,9 @@ int jac_step_dispatch(gmg_mg *mg, const Level &L, T *bout, const T *bin, T *c, D
   if (L.sell && sell_val<T>(L)) {
     if (grid_for(L.n) <= PREFETCH_MAX_BLOCKS)
       GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, PF<S>::N>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,
+                 sell_val<T>(L), dinv, L.flags, bin, bout, c, dm);
+    else if (sell_bytes<T>(L) > STREAM_MIN_BYTES)
+      GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, -1>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,
                  sell_val<T>(L), dinv, L.flags, bin, bout, c, dm);
     else
       GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, 0>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,

@@ -674,6 +674,7 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
     L.waves_contiguous = h.contiguous;
     if (!h.sptr.empty()) {
       L.sell = true;
+      L.sell_nent = h.sptr.back();
       L.sell_ptr = mg->arena.take_n<int>(h.sptr.size());
       L.sell_col = mg->arena.take_n<int>(h.scol.size());
       L.sell_v64 = mg->arena.take_n<double>(h.sval.size());
