@@ -178,6 +178,13 @@ int gmg_transfer_adapt_correction(gmg_np *np, int level, gmg_vec *c, gmg_vec *b,
 /* VNEW of a level's vectors (n ints, list order; gm.h VNEW, set for the vectors the
  * last AdaptMultiGrid created) */
 int gmg_mg_set_new_vectors(gmg_mg *mg, int level, const int *vnew);
+/* New matrix values of one level, structure unchanged (the next assembly of a
+ * time or Newton step): val in the level's gmg_level_desc layout (list order,
+ * MATRIX-list order, s*s per block).  Every device copy is rewritten in place,
+ * ILU factors and the base inverse (if built) are recomputed, fused coarse
+ * images and captured iteration graphs are rebuilt on next use.  Not for
+ * batched hierarchies. */
+int gmg_mg_update_values(gmg_mg *mg, int level, const double *val);
 
 /* NP_LINEAR_SOLVER (np/procs/ls.h:79-132); Solver takes (abslimit, reduction)
  * in the order of np/procs/ls.cc:637. */

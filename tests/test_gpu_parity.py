@@ -258,3 +258,36 @@ def test_solution_transfer_matches_ug(G, name, order):
         got = np.concatenate([mg.download("x", l) for l in range(n)])
         assert np.array_equal(got, fx[post]), (name, post)
     mg.close()
+
+
+@pytest.mark.parametrize("fuse", [0, None])
+@pytest.mark.parametrize("sm", ["jac", "gs", "ilu"])
+def test_update_values_matches_ug(G, sm, fuse):
+    """New matrix values on a resident hierarchy (gmg_mg_update_values): the
+    3D Poisson hierarchy, solved once (ILU factors, base inverse, fused coarse
+    images and the captured iteration built), gets the k = exp(g) diffusion
+    values of every level (the same mesh); its next solve is UG's diffusion
+    solve (iterations and solution)."""
+    src, dst = load_golden("p1_gs"), load_golden(f"p1k_{sm}")
+    n = int(src["nlevels"][0])
+    for l in range(n):
+        assert np.array_equal(src[f"L{l}_rowptr"], dst[f"L{l}_rowptr"])
+        assert np.array_equal(src[f"L{l}_col"], dst[f"L{l}_col"])
+    mg = G.MultiGrid(G.levels_from_ugfx(src), order=0)
+    bl = int(dst["baselevel"][0])
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50, fuse=fuse)
+    for _ in range(2):
+        _, lr0 = mg.solve_host("mgs", src["rhs"])
+        assert lr0.converged
+    for l in range(n):
+        mg.update_values(l, dst[f"L{l}_val"])
+    x, lr = mg.solve_host("mgs", dst["rhs"])
+    it_ug = int(dst["ls_iters"][0])
+    assert lr.converged
+    if sm == "jac":
+        assert lr.iters == it_ug and rel(x, dst["ls_x"]) <= 1e-10
+    else:
+        assert abs(lr.iters - it_ug) <= 1 and rel(x, dst["ls_x"]) <= 1e-8
+    x2, lr2 = mg.solve_host("mgs", dst["rhs"])  # replayed graph after the update
+    assert lr2.iters == lr.iters and np.array_equal(x, x2)
+    mg.close()

@@ -96,6 +96,7 @@ def lib(build_if_missing: bool = True):
         "gmg_transfer_interpolate_new_vectors": ([P, I, I, P, P], I),
         "gmg_transfer_project_solution": ([P, I, I, P, P], I),
         "gmg_transfer_adapt_correction": ([P, I, P, P, P, P], I), "gmg_mg_set_new_vectors": ([P, I, P], I),
+        "gmg_mg_update_values": ([P, I, P], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -507,6 +508,15 @@ class MultiGrid:
         if lib().gmg_ls_preprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(bl), C.byref(res)):
             _err(f"{obj} PreProcess")
         return bl.value
+
+    def update_values(self, level: int, val):
+        """New matrix values of a level (gmg_level_desc layout), structure unchanged."""
+        a = np.ascontiguousarray(val, np.float64).ravel()
+        n, s, nnz = self.size(level)
+        if a.size != nnz * s * s:
+            raise GmgError(f"update_values: {a.size} values for {nnz} blocks of {s}x{s}")
+        if lib().gmg_mg_update_values(self._h, level, _ptr(a)):
+            _err("update_values")
 
     def set_new_vectors(self, level: int, vnew):
         """VNEW flags of a level's vectors (list order)."""

@@ -97,6 +97,7 @@ struct Level {
   Sched upper;                  // backward wavefronts (ilu backward)
   // ILU(0) factors in processing order (filled by the ilu numproc's PreProcess)
   bool ilu_ready = false;
+  double ilu_beta[GMG_MAX_S] = {0};
   DevCSR L, U;                  // strict lower (unit diagonal) / strict upper parts
   double *udinv64 = nullptr;    // inverted diagonal blocks of U
   float *udinv32 = nullptr;
@@ -200,6 +201,10 @@ struct gmg_mg {
   void *stage_dev = nullptr;   // n_top*s doubles
   double *stage_host = nullptr;// pinned, n_top*s doubles
   long long launches = 0;
+  // bumped when device copies that captured iterations point into are
+  // replaced (gmg_mg_update_values drops the fused coarse images): a CUDA
+  // graph captured under an older epoch is re-captured
+  long long graph_epoch = 0;
   std::vector<std::unique_ptr<gmg::CoarseImageBase>> coarse_images;
   std::map<std::tuple<int, int, int, int>, long long> coarse_smem_cache;  // (bl, lc, prec, smoother)
   // batched hierarchies (gmg_mg_create_batched): independent instances stored
@@ -308,6 +313,9 @@ int k_refine_prepare(gmg_mg *mg, float *b32, float *c32, const double *b64, long
 // fine t = P (damp*coarse) honouring fine VECSKIP; acc += t if acc != null
 int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void *from, const double *damp,
                   void *acc);
+// after new matrix values (gmg_mg_update_values): the ILU factors and the
+// base level's inverse of `level`, if built, recomputed into their arrays
+int refresh_factors(gmg_mg *mg, int level);
 // StandardIntNewNodeVector: fine rows with F_VNEW take P x_coarse (every component)
 int k_interpolate_new(gmg_mg *mg, const Level &fine, int prec, void *x_fine, const void *x_coarse);
 // StandardProject: coarse rows with a son take the son's values

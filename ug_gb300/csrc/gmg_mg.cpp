@@ -787,6 +787,64 @@ static std::vector<int> instance_rows(const Level &L, int off, int n) {
 
 extern "C" {
 
+// New matrix values of one level with the structure unchanged (e.g. the next
+// assembly of a time step or Newton step): `val` in the level's
+// gmg_level_desc layout.  Every device copy is rewritten in place (block
+// CSR FP64/FP32, sliced ELLPACK, inverse diagonal blocks, and the ILU factors
+// and base-level inverse if built); the fused coarse images are dropped and
+// rebuilt on their next use, and iterations captured as CUDA graphs are
+// re-captured.
+int gmg_mg_update_values(gmg_mg *mg, int level, const double *val) {
+  if (!mg || level < 0 || level >= int(mg->lev.size()) || !val) {
+    set_error("gmg_mg_update_values: bad arguments");
+    return 1;
+  }
+  GMG_CHECK(mg->batch.ninst == 0, "gmg_mg_update_values: not for batched hierarchies (the pools rewrite slots)");
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  Level &L = mg->lev[level];
+  const int n = L.n, s = L.s, ss = s * s;
+  std::vector<int> iperm(n);
+  for (int i = 0; i < n; ++i) iperm[L.perm[i]] = i;
+  std::vector<long long> off(size_t(n) + 1, 0);  // first entry of list row o in `val`
+  for (int o = 0; o < n; ++o) off[o + 1] = off[o] + (L.h_rowptr[iperm[o] + 1] - L.h_rowptr[iperm[o]]);
+  for (int i = 0; i < n; ++i) {
+    const long long src = off[L.perm[i]];
+    for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k)
+      std::memcpy(&L.h_val[size_t(k) * ss], &val[size_t(src + k - L.h_rowptr[i]) * ss], sizeof(double) * ss);
+  }
+  const size_t nnz = L.h_val.size() / ss;
+  GMG_CUDA(cudaMemcpy(L.A.v64, L.h_val.data(), L.h_val.size() * sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<double> dinv(size_t(n) * ss, 0.0);
+  for (int i = 0; i < n; ++i) {
+    if (!(L.h_flags[i] & F_ACTIVE)) continue;
+    GMG_CHECK(!invert_block(s, &L.h_val[size_t(L.h_rowptr[i]) * ss], &dinv[size_t(i) * ss]),
+              "singular diagonal block in row %d", L.perm[i]);
+  }
+  GMG_CUDA(cudaMemcpy(L.dinv64, dinv.data(), dinv.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (L.A.v32) {
+    auto v = to_f32(L.h_val), dv = to_f32(dinv);
+    GMG_CUDA(cudaMemcpy(L.A.v32, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice));
+    GMG_CUDA(cudaMemcpy(L.dinv32, dv.data(), dv.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  if (L.sell) {
+    HostLevel H;
+    H.n = n; H.s = s;
+    H.rowptr = L.h_rowptr; H.col = L.h_col; H.val = L.h_val;
+    build_sell(H);
+    GMG_CHECK((long long)H.sptr.back() == L.sell_nent, "gmg_mg_update_values: sliced ELLPACK layout changed");
+    GMG_CUDA(cudaMemcpy(L.sell_v64, H.sval.data(), H.sval.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (L.sell_v32) {
+      auto sv = to_f32(H.sval);
+      GMG_CUDA(cudaMemcpy(L.sell_v32, sv.data(), sv.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+  }
+  (void)nnz;
+  if (refresh_factors(mg, level)) return 1;
+  mg->coarse_images.clear();
+  ++mg->graph_epoch;
+  return 0;
+}
+
 // VNEW of a level's vectors (list order), kept as row flag F_VNEW
 int gmg_mg_set_new_vectors(gmg_mg *mg, int level, const int *vnew) {
   if (!mg || level < 0 || level >= int(mg->lev.size()) || !vnew) {

@@ -389,6 +389,8 @@ static int dev_copy(gmg::Level &L, T **dst, const std::vector<T> &src) {
   return 0;
 }
 
+static int ilu_build(gmg_mg *mg, Level &L, int level, const double *beta, bool in_place, int *result);
+
 // the factor entries of every subdomain interior in subdomain-local numbering
 // (GMG_ORDER_DOMAIN): the interior rows in wave order, then the rows outside
 // the interior the sweep reads (the subdomain's own interface rows, backward
@@ -434,6 +436,13 @@ int NPIlu::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel
   Level &L = mg->lev[level];
   *baselevel = level;
   if (L.ilu_ready) return 0;
+  return ilu_build(mg, L, level, beta, false, result);
+}
+
+// the ILU(0) factors of level L with the given beta, split into the unit
+// lower factor, the strict upper factor and the inverted diagonal blocks;
+// in_place: the level's factor arrays exist (same structure) and are rewritten
+static int ilu_build(gmg_mg *mg, Level &L, int level, const double *beta, bool in_place, int *result) {
   std::vector<double> lu;
   int rc = ilu_factor_host(L, beta, lu);
   if (rc) {
@@ -458,6 +467,24 @@ int NPIlu::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel
     }
     lr[i + 1] = int(lc.size());
     ur[i + 1] = int(uc.size());
+  }
+  std::copy(beta, beta + GMG_MAX_S, L.ilu_beta);
+  if (in_place) {
+    GMG_CHECK(L.L.nnz == (long long)lc.size() && L.U.nnz == (long long)uc.size(), "ILU refresh: factor pattern changed");
+    auto put = [](void *dst, const void *src, size_t bytes) -> int {
+      if (bytes) GMG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+      return 0;
+    };
+    if (put(L.L.v64, lv.data(), lv.size() * 8) || put(L.U.v64, uv.data(), uv.size() * 8) ||
+        put(L.udinv64, ud.data(), ud.size() * 8))
+      return 1;
+    if (mg->opts.fp32_copy) {
+      std::vector<float> lv32(lv.begin(), lv.end()), uv32(uv.begin(), uv.end()), ud32(ud.begin(), ud.end());
+      if (put(L.L.v32, lv32.data(), lv32.size() * 4) || put(L.U.v32, uv32.data(), uv32.size() * 4) ||
+          put(L.udinv32, ud32.data(), ud32.size() * 4))
+        return 1;
+    }
+    return 0;
   }
   L.L.nrows = L.U.nrows = n;
   L.L.nnz = lc.size();
@@ -530,6 +557,8 @@ static void dense_block(const Level &L, const int *rows, int m, std::vector<doub
   }
 }
 
+static int base_inverse(Level &L, int level, bool in_place, int *result);
+
 int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel, int *result) {
   if (check_level(mg, level)) return 1;
   Level &L = mg->lev[level];
@@ -568,8 +597,15 @@ int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel,
     L.base_dim = 0;  // no single dense inverse (the fused coarse cycle needs one)
     return 0;
   }
-  const int N = L.n * s;
+  return base_inverse(L, level, false, result);
+}
+
+// the explicit inverse of a (not block-diagonal) base level; in_place: into
+// the existing array (same size)
+static int base_inverse(Level &L, int level, bool in_place, int *result) {
+  const int N = L.n * L.s;
   GMG_CHECK(N <= 4096, "ex: level %d has %d unknowns, above the dense base-solver limit 4096", level, N);
+  std::vector<double> a, inv;
   std::vector<int> rows(L.n);
   std::iota(rows.begin(), rows.end(), 0);
   dense_block(L, rows.data(), L.n, a);
@@ -578,9 +614,17 @@ int NPEx::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel,
     set_error("ex: singular base-level matrix");
     return 1;
   }
-  GMG_CUDA(cudaMalloc(&L.ainv, inv.size() * sizeof(double)));
+  if (!in_place) GMG_CUDA(cudaMalloc(&L.ainv, inv.size() * sizeof(double)));
   GMG_CUDA(cudaMemcpy(L.ainv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
   L.base_dim = N;
+  return 0;
+}
+
+int refresh_factors(gmg_mg *mg, int level) {
+  Level &L = mg->lev[level];
+  int result = 0;
+  if (L.ilu_ready && ilu_build(mg, L, level, L.ilu_beta, true, &result)) return 1;
+  if (L.ainv && L.base_dim > 0 && base_inverse(L, level, true, &result)) return 1;
   return 0;
 }
 
@@ -1134,7 +1178,7 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   }
   lr->converged = sc_cmp(lr->first_defect, abs_, s);
   lr->number_of_linear_iterations = 0;
-  if (graph && (graph_level != level || graph_x != xv || graph_b != bv)) {
+  if (graph && (graph_level != level || graph_x != xv || graph_b != bv || graph_epoch != mg->graph_epoch)) {
     cudaGraphExecDestroy(graph);
     graph = nullptr;
   }
@@ -1188,7 +1232,7 @@ int NPLs::step_async(int i, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, gm
       GMG_CUDA(ce);
       GMG_CUDA(cudaGraphInstantiate(&graph, g, 0));
       cudaGraphDestroy(g);
-      graph_level = level; graph_x = xv; graph_b = bv;
+      graph_level = level; graph_x = xv; graph_b = bv; graph_epoch = mg->graph_epoch;
       graph_kernels = mg->launches - before;  // captured, not yet run
       mg->launches = before;
     }
@@ -1456,7 +1500,7 @@ int NPBcgs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const doubl
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
   lr->converged = sc_cmp(lr->first_defect, abs_, s);
   lr->number_of_linear_iterations = 0;
-  if (graph && (graph_level != level || graph_x != xv || graph_b != bv)) {
+  if (graph && (graph_level != level || graph_x != xv || graph_b != bv || graph_epoch != mg->graph_epoch)) {
     cudaGraphExecDestroy(graph);
     graph = nullptr;
   }

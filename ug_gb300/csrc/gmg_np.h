@@ -180,6 +180,7 @@ struct NPLs : NPLinearSolver {
   int graph_level = -1;
   gmg_vec *graph_x = nullptr, *graph_b = nullptr;
   long long graph_kernels = 0;  // kernels per replay (for the launch counter)
+  long long graph_epoch = 0;    // mg->graph_epoch when captured
   ~NPLs() override;
   int Init(const Args &a) override;
   int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) override;
