@@ -152,3 +152,25 @@ def test_generated_local_vs_oracle(G, oracle_mod, sm, order):
     assert conv and lr.converged and abs(lr.iters - ito) <= 1
     assert rel(x, np.concatenate(xr)) <= 1e-8
     mg.close()
+
+
+def test_update_values_scales_local_solution(G):
+    """gmg_mg_update_values on the generated L-shape hierarchy in subdomain
+    order (ILU factors rebuilt in place): doubling every level's matrix
+    halves the converged solution on every level."""
+    gen = G.LocalGenerator(5, 9, seed=2026)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=2)
+    G.setup_lmgc(mg, "ilu", baselevel=0, red=1e-12, abslimit=1e-50)
+    x1, lr1 = mg.solve_host("mgs", gen.rhs)
+    for l, d in enumerate(levels):
+        v = np.array(d["val"], np.float64).reshape(-1, 4)
+        # Dirichlet rows keep their unit diagonal (UG's assembly sets them so)
+        rp = d["rowptr"]
+        for i in np.nonzero(d["skip"])[0]:
+            v[rp[i]:rp[i + 1]] /= 2.0
+        mg.update_values(l, 2.0 * v)
+    x2, lr2 = mg.solve_host("mgs", gen.rhs)
+    assert lr1.converged and lr2.converged and abs(lr1.iters - lr2.iters) <= 1
+    assert rel(2.0 * x2, x1) <= 1e-8
+    mg.close()

@@ -812,7 +812,6 @@ int gmg_mg_update_values(gmg_mg *mg, int level, const double *val) {
     for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k)
       std::memcpy(&L.h_val[size_t(k) * ss], &val[size_t(src + k - L.h_rowptr[i]) * ss], sizeof(double) * ss);
   }
-  const size_t nnz = L.h_val.size() / ss;
   GMG_CUDA(cudaMemcpy(L.A.v64, L.h_val.data(), L.h_val.size() * sizeof(double), cudaMemcpyHostToDevice));
   std::vector<double> dinv(size_t(n) * ss, 0.0);
   for (int i = 0; i < n; ++i) {
@@ -838,7 +837,6 @@ int gmg_mg_update_values(gmg_mg *mg, int level, const double *val) {
       GMG_CUDA(cudaMemcpy(L.sell_v32, sv.data(), sv.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
   }
-  (void)nnz;
   if (refresh_factors(mg, level)) return 1;
   mg->coarse_images.clear();
   ++mg->graph_epoch;
