@@ -835,6 +835,236 @@ done:
   return rc ? rc : it;
 }
 
+/* ---- Krylov solvers over the levels baselevel..top of a locally refined
+ * hierarchy: vector operations ALL_VECTORS on every level, products ON_SURFACE */
+
+/* ddot / ddotw ON_SURFACE (ugblas.cc:3104 / 3023): the surface rows in the
+ * loop order of matloop.ct; ddot sums every component into one sum, ddotw
+ * (weights 1) per component, then adds the components */
+static double surface_ddot(const orc_mg *mg, int frl, double *const *x, double *const *y, int weighted) {
+  const int top = mg->nlevels - 1, s = mg->lev[top].s;
+  double sum = 0.0, a[ORC_MAX_S] = {0};
+  for (int l = frl; l <= top; ++l) {
+    const orc_level *L = &mg->lev[l];
+    for (int i = 0; i < L->n; ++i) {
+      if (!surface_row(L, i, l == top)) continue;
+      for (int r = 0; r < s; ++r) {
+        const double v = x[l][(size_t)i * s + r] * y[l][(size_t)i * s + r];
+        if (weighted) a[r] += v; else sum += v;
+      }
+    }
+  }
+  if (weighted)
+    for (int r = 0; r < s; ++r) sum += 1.0 * a[r];
+  return sum;
+}
+
+/* dmatmul ON_SURFACE (x = A y on the surface rows only, the other rows keep
+ * their values) or ALL_VECTORS on the levels bl..top */
+static void levels_matmul(const orc_mg *mg, int frl, int bl, int surface, double *const *x, double *const *y) {
+  const int top = mg->nlevels - 1;
+  for (int l = surface ? frl : bl; l <= top; ++l) {
+    const orc_level *L = &mg->lev[l];
+    const int s = L->s, ss = s * s;
+    for (int i = 0; i < L->n; ++i) {
+      if (surface && !surface_row(L, i, l == top)) continue;
+      double acc[ORC_MAX_S] = {0};
+      for (int k = L->rowptr[i]; k < L->rowptr[i + 1]; ++k) {
+        const double *m = L->val + (size_t)k * ss, *w = y[l] + (size_t)L->col[k] * s;
+        for (int r = 0; r < s; ++r) {
+          double t = 0.0;
+          for (int c = 0; c < s; ++c) t += m[r * s + c] * w[c];
+          acc[r] += t;
+        }
+      }
+      for (int r = 0; r < s; ++r) x[l][(size_t)i * s + r] = acc[r];
+    }
+  }
+}
+
+typedef struct {
+  int nl;
+  double *v[32];
+} orc_lvec; /* one vector on every level (NULL below bl) */
+
+static int lvec_alloc(const orc_mg *mg, int bl, orc_lvec *v) {
+  memset(v, 0, sizeof *v);
+  v->nl = mg->nlevels;
+  if (mg->nlevels > 32) return -1;
+  for (int l = bl; l < mg->nlevels; ++l)
+    if (!(v->v[l] = (double *)calloc((size_t)mg->lev[l].n * mg->lev[l].s, sizeof(double)))) return -1;
+  return 0;
+}
+static void lvec_free(orc_lvec *v) { for (int l = 0; l < v->nl; ++l) free(v->v[l]); }
+static size_t lvlen(const orc_mg *mg, int l) { return (size_t)mg->lev[l].n * mg->lev[l].s; }
+
+/* the lmgc preconditioner on a copy of d (every level): q = c */
+static int precond_levels(orc_ws *w, int bl, double *const *q, double *const *d) {
+  const orc_mg *mg = w->mg;
+  const int top = mg->nlevels - 1;
+  for (int l = bl; l <= top; ++l) memcpy(w->b[l], d[l], sizeof(double) * lvlen(mg, l));
+  memset(w->c[top], 0, sizeof(double) * lvlen(mg, top));
+  int rc = lmgc(w, top);
+  for (int l = bl; l <= top; ++l) memcpy(q[l], w->c[l], sizeof(double) * lvlen(mg, l));
+  return rc;
+}
+
+int orc_cg_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
+                        const double *abslimit, int maxit, double *hist, int *converged) {
+  const int top = mg->nlevels - 1, s = mg->lev[top].s;
+  const int bl = mg->baselevel < top ? mg->baselevel : top;
+  const int frl = orc_fullrefinelevel(mg);
+  orc_ws w;
+  orc_lvec p, t;
+  if (frl < bl) return -3000000; /* the surface would reach below the allocated levels */
+  int rc = ws_init_levels(&w, mg, b), it = 0;
+  if (!rc) rc = lvec_alloc(mg, bl, &p);
+  if (!rc) rc = lvec_alloc(mg, bl, &t);
+  *converged = 0;
+  if (rc) goto done;
+  {
+    double first[ORC_MAX_S], last[ORC_MAX_S], reach[ORC_MAX_S], rho = 1.0; /* CGPrepare, ls.cc:976 */
+    surface_defect(mg, frl, b, x);
+    surface_norm(mg, frl, b, first);
+    if (hist) for (int r = 0; r < s; ++r) hist[r] = first[r];
+    for (int r = 0; r < s; ++r) { reach[r] = first[r] * red[r]; if (reach[r] == 0.0) reach[r] = red[r]; }
+    *converged = sc_cmp(first, abslimit, s);
+    for (it = 0; it < maxit; ++it) {
+      if (*converged) break;
+      memset(w.c[top], 0, sizeof(double) * lvlen(mg, top));
+      if ((rc = lmgc(&w, top))) goto done;
+      /* CGUpdate, ls.cc:989-1030 on the levels bl..top */
+      double *const *c = w.c;
+      levels_matmul(mg, frl, bl, 0, t.v, c);
+      for (int l = bl; l <= top; ++l) vadd(b[l], t.v[l], lvlen(mg, l));
+      double lambda = surface_ddot(mg, frl, c, b, 0);
+      const double f = lambda / rho;
+      for (int l = bl; l <= top; ++l) for (size_t i = 0; i < lvlen(mg, l); ++i) p.v[l][i] *= f;
+      rho = lambda;
+      for (int l = bl; l <= top; ++l) vadd(p.v[l], c[l], lvlen(mg, l));
+      levels_matmul(mg, frl, bl, 0, t.v, p.v);
+      lambda = surface_ddot(mg, frl, t.v, p.v, 0);
+      if (lambda == 0.0) { rc = -2000000; goto done; }
+      const double a = rho / lambda, na = -rho / lambda;
+      for (int l = bl; l <= top; ++l)
+        for (size_t i = 0; i < lvlen(mg, l); ++i) { x[l][i] += a * p.v[l][i]; }
+      for (int l = bl; l <= top; ++l)
+        for (size_t i = 0; i < lvlen(mg, l); ++i) { b[l][i] += na * t.v[l][i]; }
+      surface_norm(mg, frl, b, last);
+      if (hist) for (int r = 0; r < s; ++r) hist[(size_t)(it + 1) * s + r] = last[r];
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) { *converged = 1; ++it; break; }
+    }
+  }
+done:
+  lvec_free(&p); lvec_free(&t);
+  ws_free(&w);
+  return rc ? rc : it;
+}
+
+int orc_bcgs_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
+                          const double *abslimit, int maxit, double *hist, int *converged) {
+  const int top = mg->nlevels - 1, s = mg->lev[top].s;
+  const int bl = mg->baselevel < top ? mg->baselevel : top;
+  const int frl = orc_fullrefinelevel(mg);
+  orc_ws w;
+  orc_lvec r, p, v, sv, t, q;
+  double *scratch[32] = {0};
+  int rc = 0, iters = 0;
+  *converged = 0;
+  if (mg->nlevels > 32) return -1;
+  if (frl < bl) return -3000000;
+  for (int l = bl; l <= top; ++l) scratch[l] = (double *)calloc(lvlen(mg, l), sizeof(double));
+  rc = ws_init_levels(&w, mg, scratch);
+  if (!rc) rc = lvec_alloc(mg, bl, &r);
+  if (!rc) rc = lvec_alloc(mg, bl, &p);
+  if (!rc) rc = lvec_alloc(mg, bl, &v);
+  if (!rc) rc = lvec_alloc(mg, bl, &sv);
+  if (!rc) rc = lvec_alloc(mg, bl, &t);
+  if (!rc) rc = lvec_alloc(mg, bl, &q);
+  if (rc) goto done;
+  {
+    double first[ORC_MAX_S], last[ORC_MAX_S], reach[ORC_MAX_S], old[ORC_MAX_S];
+    double alpha = 0.0, rho_new = 0.0, beta = 0.0, tt = 0.0, rho = 0.0, omega = 0.0;
+    int restart = 1, eq_count = 0, nh = 0;
+    for (int k = 0; k < s; ++k) old[k] = -1.0; /* BCGSPreProcess, ls.cc:1831 */
+    surface_defect(mg, frl, b, x);
+    surface_norm(mg, frl, b, first);
+    if (hist) for (int k = 0; k < s; ++k) hist[k] = first[k];
+    for (int k = 0; k < s; ++k) { reach[k] = first[k] * red[k]; if (reach[k] == 0.0) reach[k] = red[k]; }
+    *converged = sc_cmp(first, abslimit, s);
+    /* BCGSSolver, ls.cc:1864-2062 on the levels bl..top (no restart index, weights 1) */
+    for (int i = 0; i < maxit; ++i) {
+      if (*converged) break;
+      if (restart) {
+        for (int l = bl; l <= top; ++l) {
+          memset(p.v[l], 0, sizeof(double) * lvlen(mg, l));
+          memset(v.v[l], 0, sizeof(double) * lvlen(mg, l));
+          memcpy(r.v[l], b[l], sizeof(double) * lvlen(mg, l));
+        }
+        alpha = rho = omega = 1.0;
+        restart = 0;
+      }
+      rho_new = surface_ddot(mg, frl, b, r.v, 1);
+      if (rho != 0.0 && omega != 0.0) beta = rho_new * alpha / rho / omega;
+      for (int l = bl; l <= top; ++l) {
+        const size_t n = lvlen(mg, l);
+        for (size_t k = 0; k < n; ++k) p.v[l][k] *= beta;
+        vadd(p.v[l], b[l], n);
+        const double a = -beta * omega;
+        for (size_t k = 0; k < n; ++k) p.v[l][k] += a * v.v[l][k];
+      }
+      if ((rc = precond_levels(&w, bl, q.v, p.v))) goto done;
+      levels_matmul(mg, frl, bl, 1, v.v, q.v);
+      alpha = surface_ddot(mg, frl, v.v, r.v, 1);
+      if (alpha != 0.0) alpha = rho_new / alpha;
+      for (int l = bl; l <= top; ++l)
+        for (size_t k = 0; k < lvlen(mg, l); ++k) x[l][k] += alpha * q.v[l][k];
+      ++iters;
+      for (int l = bl; l <= top; ++l) {
+        const size_t n = lvlen(mg, l);
+        memcpy(sv.v[l], b[l], sizeof(double) * n);
+        const double a = -alpha;
+        for (size_t k = 0; k < n; ++k) sv.v[l][k] += a * v.v[l][k];
+      }
+      surface_norm(mg, frl, sv.v, last);
+      ++nh;
+      if (hist) for (int k = 0; k < s; ++k) hist[(size_t)nh * s + k] = last[k];
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) {
+        for (int l = bl; l <= top; ++l) memcpy(b[l], sv.v[l], sizeof(double) * lvlen(mg, l));
+        *converged = 1;
+        break;
+      }
+      if ((rc = precond_levels(&w, bl, q.v, sv.v))) goto done;
+      levels_matmul(mg, frl, bl, 1, t.v, q.v);
+      tt = surface_ddot(mg, frl, t.v, t.v, 1);
+      omega = surface_ddot(mg, frl, sv.v, t.v, 1);
+      if (tt != 0.0) omega /= tt;
+      for (int l = bl; l <= top; ++l) {
+        const size_t n = lvlen(mg, l);
+        for (size_t k = 0; k < n; ++k) x[l][k] += omega * q.v[l][k];
+        memcpy(b[l], sv.v[l], sizeof(double) * n);
+        const double a = -omega;
+        for (size_t k = 0; k < n; ++k) b[l][k] += a * t.v[l][k];
+      }
+      rho = rho_new;
+      surface_norm(mg, frl, b, last);
+      ++nh;
+      if (hist) for (int k = 0; k < s; ++k) hist[(size_t)nh * s + k] = last[k];
+      ++iters;
+      if (sc_cmp(last, abslimit, s) || sc_cmp(last, reach, s)) { *converged = 1; break; }
+      if (sc_eq(last, old, 1e-4, s)) eq_count++;
+      else eq_count = 0;
+      for (int k = 0; k < s; ++k) old[k] = last[k];
+      if (eq_count > 4) { *converged = 0; break; }
+    }
+  }
+done:
+  lvec_free(&r); lvec_free(&p); lvec_free(&v); lvec_free(&sv); lvec_free(&t); lvec_free(&q);
+  ws_free(&w);
+  for (int l = 0; l < 32; ++l) free(scratch[l]);
+  return rc ? rc : iters;
+}
+
 int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, const double *abslimit, int maxit,
                  double *hist, int *converged) {
   const int top = mg->nlevels - 1;

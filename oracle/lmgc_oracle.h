@@ -93,6 +93,13 @@ int orc_ls_solve(const orc_mg *mg, double *x, double *b, const double *red, cons
 int orc_ls_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
                         const double *abslimit, int maxit, double *hist, int *converged);
 int orc_fullrefinelevel(const orc_mg *mg); /* SetSurfaceClasses, gm/algebra.cc:2838 */
+/* cg and bcgs (ls.cc:989-1030, 1864-2062) on every level baselevel..top:
+ * vector operations ALL_VECTORS on each level, dot products (ddot / ddotw)
+ * and bcgs's dmatmul ON_SURFACE, as UG runs them on a locally refined grid. */
+int orc_cg_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
+                        const double *abslimit, int maxit, double *hist, int *converged);
+int orc_bcgs_solve_levels(const orc_mg *mg, double *const *x, double *const *b, const double *red,
+                          const double *abslimit, int maxit, double *hist, int *converged);
 
 #ifdef __cplusplus
 }

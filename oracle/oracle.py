@@ -92,12 +92,14 @@ def lib():
         L.orc_project.argtypes = [P, P, P]
         L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_ls_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        L.orc_cg_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        L.orc_bcgs_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_fullrefinelevel.argtypes = [P]
         L.orc_fullrefinelevel.restype = C.c_int
         L.orc_cg_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_bcgs_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         for f in ("orc_jac", "orc_lgs", "orc_ilu_decomp", "orc_luiter", "orc_ls_solve", "orc_cg_solve",
-                  "orc_bcgs_solve", "orc_ls_solve_levels"):
+                  "orc_bcgs_solve", "orc_ls_solve_levels", "orc_cg_solve_levels", "orc_bcgs_solve_levels"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -235,7 +237,15 @@ class Hierarchy:
         mg = self._mg()
         return lib().orc_fullrefinelevel(C.byref(mg))
 
-    def ls_solve_surface(self, rhs_all, *, x0_all=None, red=1e-10, abslimit=1e-50, maxit=100, **kw):
+    def cg_solve_surface(self, rhs_all, **kw):
+        """cg preconditioned by lmgc on every level (see ls_solve_surface)."""
+        return self.ls_solve_surface(rhs_all, _solver="cg", **kw)
+
+    def bcgs_solve_surface(self, rhs_all, **kw):
+        """bcgs preconditioned by lmgc on every level; iterations count half steps."""
+        return self.ls_solve_surface(rhs_all, _solver="bcgs", **kw)
+
+    def ls_solve_surface(self, rhs_all, *, x0_all=None, red=1e-10, abslimit=1e-50, maxit=100, _solver="ls", **kw):
         """ls + lmgc on a locally refined hierarchy: rhs_all and the returned x
         hold every level 0..top, concatenated.  The defect and its norms run over
         UG's surface and the correction is added on every level baselevel..top.
@@ -251,11 +261,13 @@ class Hierarchy:
         s = self.levels[-1]["s"]
         redv = np.resize(np.asarray(red, np.float64), MAX_S)
         absv = np.resize(np.asarray(abslimit, np.float64), MAX_S)
-        hist = np.zeros((maxit + 1) * s)
+        hist = np.zeros((2 * maxit + 1) * s)
         conv = C.c_int(0)
-        it = lib().orc_ls_solve_levels(C.byref(mg), xp, bp, _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
+        f = {"cg": lib().orc_cg_solve_levels, "bcgs": lib().orc_bcgs_solve_levels}.get(_solver,
+                                                                                        lib().orc_ls_solve_levels)
+        it = f(C.byref(mg), xp, bp, _p(redv), _p(absv), maxit, _p(hist), C.byref(conv))
         if it < 0:
-            raise RuntimeError(f"oracle ls failed: {it}")
+            raise RuntimeError(f"oracle {_solver} failed: {it}")
         return x, it, bool(conv.value), hist[: (it + 1) * s].reshape(it + 1, s)
 
     def _mg(self, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None, beta=None, cdamp=None,

@@ -515,7 +515,6 @@ int main(int argc, char **argv) {
   NP_ITER *lmgc = (NP_ITER *)GetNumProcByName(mg, "lmgc", ITER_CLASS_NAME);
   if (!ls || !lmgc) { fprintf(stderr, "numproc lookup failed\n"); return 1; }
   // keep the rhs to replay the loop afterwards
-  std::vector<double> rhs_top = grab(rhs, top);
   std::vector<std::vector<double>> rhs_lev;
   for (int l = 0; l <= top; ++l) rhs_lev.push_back(grab(rhs, l));
   auto restart = [&]() {  // x = 0 and the assembled right-hand side on every level
@@ -572,11 +571,8 @@ int main(int argc, char **argv) {
   }
 
   // ---- UG's cg (ls.cc:901-1165) preconditioned by the same lmgc, from x = 0
-  if (!lshape) {
-    for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
-    for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
-    int i = 0;
-    for (VECTOR *v : g_lev[top].vecs) for (int c = 0; c < s; ++c) VVALUE(v, vcmp(rhs)[c]) = rhs_top[i++];
+  {
+    restart();
     snprintf(cmd, sizeof cmd, "npcreate cgs $c cg; npinit cgs $A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m %d $I lmgc;",
              maxit);
     run(cmd);
@@ -595,17 +591,19 @@ int main(int argc, char **argv) {
     putd("cg_first", std::vector<double>(lc.first_defect, lc.first_defect + s));
     putd("cg_last", std::vector<double>(lc.last_defect, lc.last_defect + s));
     putd("cg_x", grab(sol, top));
+    {
+      std::vector<double> xa;
+      for (int l = 0; l <= top; ++l) { auto xl = grab(sol, l); xa.insert(xa.end(), xl.begin(), xl.end()); }
+      putd("cg_x_all", xa);
+    }
     fprintf(stderr, "UG cg: iters=%d converged=%d last=%.6e\n", (int)lc.number_of_linear_iterations, (int)lc.converged,
             lc.last_defect[0]);
     (*cg->PostProcess)(cg, top, sol, rhs, A, &res);
   }
 
   // ---- UG's bcgs (ls.cc:1711-2062) preconditioned by the same lmgc, from x = 0
-  if (!lshape) {
-    for (int l = 0; l <= top; ++l) dset(mg, l, l, ALL_VECTORS, sol, 0.0);
-    for (int l = 0; l < top; ++l) dset(mg, l, l, ALL_VECTORS, rhs, 0.0);
-    int i = 0;
-    for (VECTOR *v : g_lev[top].vecs) for (int c = 0; c < s; ++c) VVALUE(v, vcmp(rhs)[c]) = rhs_top[i++];
+  {
+    restart();
     snprintf(cmd, sizeof cmd,
              "npcreate bcgs $c bcgs; npinit bcgs $A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m %d $I lmgc;", maxit);
     run(cmd);
@@ -624,6 +622,11 @@ int main(int argc, char **argv) {
     putd("bcgs_first", std::vector<double>(lb.first_defect, lb.first_defect + s));
     putd("bcgs_last", std::vector<double>(lb.last_defect, lb.last_defect + s));
     putd("bcgs_x", grab(sol, top));
+    {
+      std::vector<double> xa;
+      for (int l = 0; l <= top; ++l) { auto xl = grab(sol, l); xa.insert(xa.end(), xl.begin(), xl.end()); }
+      putd("bcgs_x_all", xa);
+    }
     fprintf(stderr, "UG bcgs: iters=%d converged=%d last=%.6e\n", (int)lb.number_of_linear_iterations,
             (int)lb.converged, lb.last_defect[0]);
   }

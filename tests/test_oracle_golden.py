@@ -155,3 +155,21 @@ def test_solution_transfer_matches_ug(name, oracle_mod):
     assert np.array_equal(x, fx["kat_newvec"])
     x = H.project_solution(0, n - 1, fx["kat_project_pre"])
     assert np.array_equal(x, fx["kat_project"])
+
+
+@pytest.mark.parametrize("solver", ["cg", "bcgs"])
+@pytest.mark.parametrize("name", LOCAL)
+def test_surface_krylov_matches_ug(name, solver, oracle_mod):
+    """UG's cg and bcgs with the lmgc preconditioner on the locally refined
+    problem: vector operations on every level, dot products (and bcgs's
+    matrix products) ON_SURFACE.  The oracle takes UG's iteration count and
+    reaches UG's solution on every level."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    sm = fx["smoother"]
+    f = H.cg_solve_surface if solver == "cg" else H.bcgs_solve_surface
+    x, it, conv, hist = f(fx["rhs_all"], smoother=sm, baselevel=int(fx["baselevel"][0]),
+                          damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50)
+    assert conv == bool(fx[f"{solver}_converged"][0]) and it == int(fx[f"{solver}_iters"][0])
+    assert rel(x, fx[f"{solver}_x_all"]) <= 1e-12
+    assert rel(hist[-1], fx[f"{solver}_last"]) <= 1e-10
