@@ -174,3 +174,66 @@ def test_update_values_scales_local_solution(G):
     assert lr1.converged and lr2.converged and abs(lr1.iters - lr2.iters) <= 1
     assert rel(2.0 * x2, x1) <= 1e-8
     mg.close()
+
+
+def _setup_krylov(G, mg, cls, sm, name, red=1e-10, mixed=False):
+    mg.npcreate(name, f"linear_solver.{cls}")
+    st = mg.npinit(name, f"$A MAT $x sol $b rhs $red {red} $abslimit 1e-50 $m 100 $I lmgc $mixed {int(mixed)}")
+    assert st == G.NP_EXECUTABLE
+
+
+@pytest.mark.parametrize("solver", ["cg", "bcgs"])
+@pytest.mark.parametrize("name", LOCAL)
+def test_local_krylov_matches_ug(G, name, solver):
+    """UG's cg / bcgs preconditioned by lmgc on the locally refined problem
+    (vector operations on every level, products ON_SURFACE): UG's iteration
+    count and UG's solution on every level; the FP32 preconditioner meets the
+    same stopping test within 1e-6."""
+    fx = load_golden(name)
+    mg = G.MultiGrid(G.levels_from_ugfx(fx), order=0, fp32=True)
+    sm, bl = fx["smoother"], int(fx["baselevel"][0])
+    G.setup_lmgc(mg, sm, baselevel=bl, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+    _setup_krylov(G, mg, "g" + solver, sm, "ks")
+    x, lr = mg.solve_host("ks", fx["rhs_all"])
+    it_ug = int(fx[f"{solver}_iters"][0])
+    assert lr.converged and abs(lr.iters - it_ug) <= 1
+    assert rel(x, fx[f"{solver}_x_all"]) <= (1e-10 if sm == "jac" else 1e-8)
+    _setup_krylov(G, mg, "g" + solver, sm, "ks32", mixed=True)
+    x32, lr32 = mg.solve_host("ks32", fx["rhs_all"])
+    assert lr32.converged and lr32.iters <= it_ug + 3
+    top, frl = mg.top, mg.frl
+    s = 2
+    parts = []
+    for l, (a, b) in enumerate(zip(_split(mg, x32), _split(mg, fx[f"{solver}_x_all"]))):
+        if l < frl:
+            continue
+        vc, vn = fx[f"L{l}_vclass"], fx[f"L{l}_vnclass"]
+        m = (vc >= 2) if l == top else ((vc >= 2) & (vn <= 1))
+        parts.append((a.reshape(-1, s)[m].ravel(), b.reshape(-1, s)[m].ravel()))
+    assert rel(np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts])) <= 1e-6
+    mg.close()
+
+
+@pytest.mark.parametrize("solver", ["cg", "bcgs"])
+def test_generated_local_krylov_vs_oracle(G, oracle_mod, solver):
+    """cg / bcgs with ILU in subdomain order on the generated L-shape
+    hierarchy (5 uniform + 9 local steps): the device matches the oracle on
+    the reordered hierarchy."""
+    gen = G.LocalGenerator(5, 9, seed=2026)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=2)
+    G.setup_lmgc(mg, "ilu", baselevel=0, red=1e-8, abslimit=1e-50)
+    _setup_krylov(G, mg, "g" + solver, "ilu", "ks", red=1e-8)
+    x, lr = mg.solve_host("ks", gen.rhs)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    s = 2
+    perms = [mg.order(l) for l in range(mg.nlevels)]
+    b_p = np.concatenate([b.reshape(-1, s)[p].ravel() for b, p in zip(_split(mg, gen.rhs), perms)])
+    f = H.cg_solve_surface if solver == "cg" else H.bcgs_solve_surface
+    xo, ito, conv, _ = f(b_p, smoother="ilu", baselevel=0, red=1e-8, abslimit=1e-50)
+    xr = []
+    for xl, p in zip(_split(mg, xo), perms):
+        o = np.empty((len(p), s)); o[p] = xl.reshape(-1, s); xr.append(o.ravel())
+    assert conv and lr.converged and abs(lr.iters - ito) <= 1
+    assert rel(x, np.concatenate(xr)) <= 1e-8
+    mg.close()

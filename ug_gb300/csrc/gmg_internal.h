@@ -259,6 +259,7 @@ struct SurfLevels {
   const double *val[SURF_MAX_LEVELS] = {};
   const uint8_t *flags[SURF_MAX_LEVELS] = {};
   uint8_t mask[SURF_MAX_LEVELS] = {};
+  uint8_t all[SURF_MAX_LEVELS] = {};    // every row of the level (instead of mask)
   uint8_t addx[SURF_MAX_LEVELS] = {};
   double *b[SURF_MAX_LEVELS] = {};
   double *x[SURF_MAX_LEVELS] = {};
@@ -266,8 +267,12 @@ struct SurfLevels {
   float *b32[SURF_MAX_LEVELS] = {};
   float *c32[SURF_MAX_LEVELS] = {};
 };
-// masked rows: b -= A y (FP64 matrix, y of precision yprec); addx rows: x += y
-int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s);
+// selected rows (mask, or all): op 0 b -= A y, 1 b += A y, 2 b = -(A y) (FP64
+// matrix, y of precision yprec); addx levels: x += y on every row
+int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s, int op = 0);
+// dot product of x (t.b) and y (t.y) over the surface rows with the cg (kind
+// 0, mode 1/2) or bcgs (kind 1, modes 0-3) scalar step on sc[]
+int k_surf_dot(gmg_mg *mg, const SurfLevels &t, int s, int kind, int mode, double sign, double *sc);
 // b32 = b on every row; c32 = 0 where given
 int k_surf_prepare(gmg_mg *mg, const SurfLevels &t, int s);
 // per-component norms of b over the masked rows into mg->norms_dev

@@ -1212,6 +1212,19 @@ __global__ void nrm_stage2(int nblocks, const double *__restrict__ partial, doub
 //   MODE 1: lambda = sum; f = lambda / rho; rho = lambda   (sc[CG_F], sc[CG_RHO])
 //   MODE 2: lambda = sign * sum; alpha = rho / lambda, or a flag if lambda = 0
 enum { CG_F = 0, CG_RHO = 1, CG_ALPHA = 2, CG_FLAG = 3 };
+template <int MODE>
+__device__ __forceinline__ void cg_scalars(double lam, double *sc) {
+  if (MODE == 1) {
+    sc[CG_F] = lam / sc[CG_RHO];
+    sc[CG_RHO] = lam;
+  } else if (lam == 0.0) {
+    sc[CG_ALPHA] = 0.0;
+    sc[CG_FLAG] = 1.0;
+  } else {
+    sc[CG_ALPHA] = sc[CG_RHO] / lam;
+  }
+}
+
 template <int S, bool ALL, int MODE>
 __global__ void __launch_bounds__(BLK) cg_dot_kernel(int n, const double *__restrict__ x, const double *__restrict__ y,
                                                      const uint8_t *__restrict__ flags, double *__restrict__ partial,
@@ -1249,18 +1262,7 @@ __global__ void __launch_bounds__(BLK) cg_dot_kernel(int n, const double *__rest
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double lam = sign * red[0];
-    if (MODE == 1) {
-      sc[CG_F] = lam / sc[CG_RHO];
-      sc[CG_RHO] = lam;
-    } else {
-      if (lam == 0.0) {
-        sc[CG_ALPHA] = 0.0;
-        sc[CG_FLAG] = 1.0;
-      } else {
-        sc[CG_ALPHA] = sc[CG_RHO] / lam;
-      }
-    }
+    cg_scalars<MODE>(sign * red[0], sc);
     *ticket = 0u;
   }
 }
@@ -1302,6 +1304,22 @@ __global__ void sub_kernel(long long len, double *__restrict__ b, const double *
 //   OMEGA: o = sign d; omega = tt != 0 ? o / tt : o; rho = rho_new
 enum { BC_RHO = 0, BC_RHONEW = 1, BC_ALPHA = 2, BC_BETA = 3, BC_OMEGA = 4, BC_TT = 5, BC_HALF = 6 };
 enum { BM_RHO = 0, BM_ALPHA = 1, BM_TT = 2, BM_OMEGA = 3 };
+template <int MODE>
+__device__ __forceinline__ void bcgs_scalars(double d, double sign, double *sc) {
+  if (MODE == BM_RHO) {
+    sc[BC_RHONEW] = d;
+    if (sc[BC_RHO] != 0.0 && sc[BC_OMEGA] != 0.0) sc[BC_BETA] = d * sc[BC_ALPHA] / sc[BC_RHO] / sc[BC_OMEGA];
+  } else if (MODE == BM_ALPHA) {
+    const double a = sign * d;
+    sc[BC_ALPHA] = a != 0.0 ? sc[BC_RHONEW] / a : a;
+  } else if (MODE == BM_TT) {
+    sc[BC_TT] = d;
+  } else {
+    const double o = sign * d;
+    sc[BC_OMEGA] = sc[BC_TT] != 0.0 ? o / sc[BC_TT] : o;
+    sc[BC_RHO] = sc[BC_RHONEW];
+  }
+}
 template <int S, bool ALL, int MODE>
 __global__ void __launch_bounds__(BLK) bcgs_dot_kernel(int n, const double *__restrict__ x, const double *__restrict__ y,
                                                        const uint8_t *__restrict__ flags, double *__restrict__ partial,
@@ -1353,19 +1371,7 @@ __global__ void __launch_bounds__(BLK) bcgs_dot_kernel(int n, const double *__re
   if (threadIdx.x == 0) {
     double d = 0.0;
     for (int r = 0; r < S; ++r) d += 1.0 * red[r][0];
-    if (MODE == BM_RHO) {
-      sc[BC_RHONEW] = d;
-      if (sc[BC_RHO] != 0.0 && sc[BC_OMEGA] != 0.0) sc[BC_BETA] = d * sc[BC_ALPHA] / sc[BC_RHO] / sc[BC_OMEGA];
-    } else if (MODE == BM_ALPHA) {
-      const double a = sign * d;
-      sc[BC_ALPHA] = a != 0.0 ? sc[BC_RHONEW] / a : a;
-    } else if (MODE == BM_TT) {
-      sc[BC_TT] = d;
-    } else {
-      const double o = sign * d;
-      sc[BC_OMEGA] = sc[BC_TT] != 0.0 ? o / sc[BC_TT] : o;
-      sc[BC_RHO] = sc[BC_RHONEW];
-    }
+    bcgs_scalars<MODE>(d, sign, sc);
     *ticket = 0u;
   }
 }
@@ -2651,7 +2657,9 @@ int k_project(gmg_mg *mg, const Level &F, const Level &C, int prec, void *xc, co
 // NEW_DEFECT vectors of the top level, each row with its own level's matrix
 // and vectors.  One launch covers every level of a SurfLevels table: thread g
 // handles row g - row0[l] of the level l with row0[l] <= g < row0[l+1].
-template <int S, class YT>
+// OP 0: b -= A y, 1: b += A y, 2: b = -(A y) on the selected rows (the
+// surface rows of `mask`, or every row where `all` is set)
+template <int S, class YT, int OP>
 __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
   pdl_prologue();
   const int total = t.row0[t.nlev];
@@ -2660,7 +2668,7 @@ __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
     while (g >= t.row0[l + 1]) ++l;
     const int i = g - t.row0[l];
     const YT *__restrict__ y = static_cast<const YT *>(t.y[l]);
-    if (t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l])) {
+    if (t.all[l] || (t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l]))) {
       double acc[S];
 #pragma unroll
       for (int r = 0; r < S; ++r) acc[r] = 0.0;
@@ -2677,7 +2685,10 @@ __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
           for (int c = 0; c < S; ++c) acc[r] = fma(__ldg(m + r * S + c), yj[c], acc[r]);
       }
 #pragma unroll
-      for (int r = 0; r < S; ++r) t.b[l][(size_t)i * S + r] -= acc[r];
+      for (int r = 0; r < S; ++r) {
+        double &bv = t.b[l][(size_t)i * S + r];
+        bv = OP == 0 ? bv - acc[r] : (OP == 1 ? bv + acc[r] : -acc[r]);
+      }
     }
     if (t.addx[l]) {
 #pragma unroll
@@ -2760,14 +2771,96 @@ __global__ void __launch_bounds__(BLK) surf_nrm_kernel(SurfLevels t, double *__r
   if (threadIdx.x == 0) *ticket = 0u;
 }
 
-int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s) {
+int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s, int op) {
   if (t.row0[t.nlev] == 0) return 0;
   const int g = vec_grid(t.row0[t.nlev]);
-#define SU(SS) { if (yprec == GMG_PREC_FP64) GMG_LAUNCH((surf_update_kernel<SS, double>), g, BLK, t); \
-                 else GMG_LAUNCH((surf_update_kernel<SS, float>), g, BLK, t); }
+#define SO(SS, OP) { if (yprec == GMG_PREC_FP64) GMG_LAUNCH((surf_update_kernel<SS, double, OP>), g, BLK, t); \
+                     else GMG_LAUNCH((surf_update_kernel<SS, float, OP>), g, BLK, t); }
+#define SU(SS) { if (op == 0) SO(SS, 0) else if (op == 1) SO(SS, 1) else SO(SS, 2) }
   if (s == 1) SU(1) else if (s == 2) SU(2) else if (s == 3) SU(3)
   else { set_error("block size %d not compiled", s); return 1; }
 #undef SU
+#undef SO
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+// a Krylov dot product over the surface rows of every level (x in t.b, y in
+// t.y, FP64), per-component partial sums, the deterministic reduction of
+// nrm_kernel, then the solver's scalar step on sc[] (KIND 0: cg's MODE 1 / 2,
+// KIND 1: bcgs's BM_* modes)
+template <int S, int KIND, int MODE>
+__global__ void __launch_bounds__(BLK) surf_dot_kernel(SurfLevels t, double *__restrict__ partial,
+                                                       unsigned *__restrict__ ticket, double *__restrict__ sc,
+                                                       double sign) {
+  pdl_prologue();
+  double acc[S];
+#pragma unroll
+  for (int r = 0; r < S; ++r) acc[r] = 0.0;
+  const int total = t.row0[t.nlev];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int l = 0;
+    while (g >= t.row0[l + 1]) ++l;
+    const int i = g - t.row0[l];
+    if (!(t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l]))) continue;
+    const double *__restrict__ y = static_cast<const double *>(t.y[l]);
+#pragma unroll
+    for (int r = 0; r < S; ++r) acc[r] = fma(t.b[l][(size_t)i * S + r], y[(size_t)i * S + r], acc[r]);
+  }
+  __shared__ double sh[BLK / 32][S];
+  __shared__ bool last;
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S) {
+    double v = 0.0;
+    for (int w = 0; w < BLK / 32; ++w) v += sh[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * S + threadIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[S][BLK];
+#pragma unroll
+  for (int r = 0; r < S; ++r) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(partial + (size_t)b * S + r);
+    red[r][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int r = 0; r < S; ++r) red[r][threadIdx.x] += red[r][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double d = 0.0;
+    for (int r = 0; r < S; ++r) d += red[r][0];
+    if (KIND == 0) cg_scalars<MODE>(sign * d, sc);
+    else bcgs_scalars<MODE>(d, sign, sc);
+    *ticket = 0u;
+  }
+}
+
+int k_surf_dot(gmg_mg *mg, const SurfLevels &t, int s, int kind, int mode, double sign, double *sc) {
+  unsigned *ticket = reinterpret_cast<unsigned *>(mg->norms_dev + GMG_MAX_S);
+#define SD(SS, K, M) GMG_LAUNCH((surf_dot_kernel<SS, K, M>), REDUCE_BLOCKS, BLK, t, mg->partial, ticket, sc, sign)
+#define SM(SS)                                                                   \
+  if (kind == 0) { if (mode == 1) SD(SS, 0, 1); else SD(SS, 0, 2); }             \
+  else if (mode == BM_RHO) SD(SS, 1, BM_RHO); else if (mode == BM_ALPHA) SD(SS, 1, BM_ALPHA); \
+  else if (mode == BM_TT) SD(SS, 1, BM_TT); else SD(SS, 1, BM_OMEGA);
+  if (s == 1) { SM(1) } else if (s == 2) { SM(2) } else if (s == 3) { SM(3) }
+  else { set_error("block size %d not compiled", s); return 1; }
+#undef SM
+#undef SD
   LAUNCH_CHECK(mg);
   return 0;
 }

@@ -1336,7 +1336,6 @@ int NPCg::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
                  gmg_lresult *lr) {
   if (check_level(mg, level)) return 1;
   GMG_CHECK(mg->batch.ninst == 0, "cg on a batched hierarchy is not supported (use ls)");
-  GMG_CHECK(!mg->local(), "cg on a locally refined hierarchy is not supported (use ls)");
   GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64, "cg: x and b must be FP64");
   if (!p) p = temp_vec(mg, name + "__p", GMG_PREC_FP64);
   if (!t) t = temp_vec(mg, name + "__t", GMG_PREC_FP64);
@@ -1348,14 +1347,70 @@ int NPCg::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   }
   const double init[4] = {0.0, 1.0, 0.0, 0.0};
   GMG_CUDA(cudaMemcpyAsync(sc, init, sizeof init, cudaMemcpyHostToDevice, mg->stream));
-  if (k_set(mg, GMG_PREC_FP64, vlev(p, level), vlen(mg, level), 0.0)) return 1;
+  // CGPrepare, ls.cc:976: p = 0 on the levels baselevel..level
+  for (int l = mg->local() ? std::min(baselevel, level) : level; l <= level; ++l)
+    if (k_set(mg, GMG_PREC_FP64, vlev(p, l), vlen(mg, l), 0.0)) return 1;
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
   *flag_host = 0.0;
   return NPLs::Solver(level, xv, bv, Am, abs_, red, lr);
 }
 
+// per-level tables of a Krylov iteration on a locally refined hierarchy
+static SurfLevels krylov_table(gmg_mg *mg, int lo, int hi, int tl, bool all_rows, gmg_vec *bx, gmg_vec *y) {
+  SurfLevels t;
+  surf_table(mg, lo, hi, tl, t);
+  for (int e = 0; e < t.nlev; ++e) {
+    t.all[e] = all_rows;
+    t.b[e] = (double *)vlev(bx, lo + e);
+    t.y[e] = vlev(y, lo + e);
+  }
+  return t;
+}
+
+// CGUpdate (ls.cc:989-1030) on a locally refined hierarchy: every vector
+// operation on the levels bl..top, with each level's matrix on all its rows;
+// the dot products over UG's surface
+int NPCg::surface_cg_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const int s = mg->lev[level].s, bl = std::min(baselevel, level), lo = surf_lo(mg, level);
+  GMG_CHECK(lo >= bl, "cg: the surface reaches below the base level");
+  gmg_vec *cv = cvec;
+  if (!mixed) {
+    if (k_set(mg, GMG_PREC_FP64, vlev(cvec, level), vlen(mg, level), 0.0)) return 1;
+    if (IterNp->Iter(level, cvec, bv, Am, err)) return 1;
+    // b += A c on every row: the defect before Iter
+    if (k_surf_update(mg, krylov_table(mg, bl, level, level, true, bv, cvec), GMG_PREC_FP64, s, 1)) return 1;
+  } else {
+    SurfLevels t;
+    surf_table(mg, lo, level, level, t);
+    for (int e = 0; e < t.nlev; ++e) {
+      t.b[e] = (double *)vlev(bv, lo + e);
+      t.b32[e] = (float *)vlev(b32, lo + e);
+      t.c32[e] = lo + e == level ? (float *)vlev(cvec, level) : nullptr;
+    }
+    if (k_surf_prepare(mg, t, s) || IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    for (int l = bl; l <= level; ++l)
+      if (k_convert(mg, GMG_PREC_FP64, vlev(c64, l), GMG_PREC_FP32, vlev(cvec, l), vlen(mg, l))) return 1;
+    cv = c64;
+  }
+  // lambda = (c, b); p = (lambda / rho) p + c; t = -(A p); lambda = (t, p); x += alpha p; b -= alpha (A p)
+  if (k_surf_dot(mg, krylov_table(mg, lo, level, level, false, cv, bv), s, 0, 1, 1.0, sc)) return 1;
+  for (int l = bl; l <= level; ++l)
+    if (k_cg_p(mg, vlen(mg, l), (double *)vlev(p, l), (const double *)vlev(cv, l), sc)) return 1;
+  if (k_surf_update(mg, krylov_table(mg, bl, level, level, true, t, p), GMG_PREC_FP64, s, 2)) return 1;
+  if (k_surf_dot(mg, krylov_table(mg, lo, level, level, false, t, p), s, 0, 2, -1.0, sc)) return 1;
+  for (int l = bl; l <= level; ++l)
+    if (k_cg_xb(mg, vlen(mg, l), (double *)vlev(xv, l), (const double *)vlev(p, l), (double *)vlev(bv, l),
+                (const double *)vlev(t, l), sc))
+      return 1;
+  if (surface_norm(mg, level, bv)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  return 0;
+}
+
 // one pass of LinearSolver's loop body with CGUpdate (ls.cc:694-701, 989-1064)
 int NPCg::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  if (mg->local()) return surface_cg_iteration(level, xv, bv, Am, err);
   const Level &L = mg->lev[level];
   const long long len = vlen(mg, level);
   double *b = (double *)vlev(bv, level), *x = (double *)vlev(xv, level), *pp = (double *)vlev(p, level),
@@ -1428,8 +1483,67 @@ int NPBcgs::precond(int level, gmg_vec *qv, gmg_vec *dv, gmg_mat *Am, int *err) 
   return k_convert(mg, GMG_PREC_FP64, vlev(qv, level), GMG_PREC_FP32, vlev(cvec, level), len);
 }
 
+// the preconditioner on every level baselevel..top of a locally refined
+// hierarchy: q = lmgc(d) with d kept (Iter works on a copy / FP32 copy)
+int NPBcgs::precond_levels(int level, gmg_vec *qv, gmg_vec *dv, gmg_mat *Am, int *err) {
+  const int s = mg->lev[level].s, bl = std::min(baselevel, level), lo = surf_lo(mg, level);
+  if (!mixed) {
+    for (int l = bl; l <= level; ++l)
+      if (k_copy(mg, GMG_PREC_FP64, vlev(pc, l), vlev(dv, l), vlen(mg, l))) return 1;
+    if (k_set(mg, GMG_PREC_FP64, vlev(qv, level), vlen(mg, level), 0.0)) return 1;
+    return IterNp->Iter(level, qv, pc, Am, err);
+  }
+  SurfLevels t;
+  surf_table(mg, lo, level, level, t);
+  for (int e = 0; e < t.nlev; ++e) {
+    t.b[e] = (double *)vlev(dv, lo + e);
+    t.b32[e] = (float *)vlev(b32, lo + e);
+    t.c32[e] = lo + e == level ? (float *)vlev(cvec, level) : nullptr;
+  }
+  if (k_surf_prepare(mg, t, s) || IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+  for (int l = bl; l <= level; ++l)
+    if (k_convert(mg, GMG_PREC_FP64, vlev(qv, l), GMG_PREC_FP32, vlev(cvec, l), vlen(mg, l))) return 1;
+  return 0;
+}
+
+// BCGSSolver's loop body on a locally refined hierarchy: vector operations on
+// the levels bl..top, dot products and the matrix products v = A q, t = A q
+// over UG's surface (the other rows of v and t keep their values, as UG's
+// dmatmul ON_SURFACE leaves them)
+int NPBcgs::surface_bcgs_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  const int s = mg->lev[level].s, bl = std::min(baselevel, level), lo = surf_lo(mg, level);
+  GMG_CHECK(lo >= bl, "bcgs: the surface reaches below the base level");
+  if (k_surf_dot(mg, krylov_table(mg, lo, level, level, false, bv, r), s, 1, 0, 1.0, sc)) return 1;
+  for (int l = bl; l <= level; ++l)
+    if (k_bcgs_p(mg, vlen(mg, l), (double *)vlev(p, l), (const double *)vlev(bv, l), (const double *)vlev(vn, l), sc))
+      return 1;
+  if (precond_levels(level, q, p, Am, err)) return 1;
+  if (k_surf_update(mg, krylov_table(mg, lo, level, level, false, vn, q), GMG_PREC_FP64, s, 2)) return 1;
+  if (k_surf_dot(mg, krylov_table(mg, lo, level, level, false, vn, r), s, 1, 1, -1.0, sc)) return 1;
+  for (int l = bl; l <= level; ++l)
+    if (k_bcgs_xs(mg, vlen(mg, l), (double *)vlev(xv, l), (const double *)vlev(q, l), (const double *)vlev(bv, l),
+                  (double *)vlev(sv, l), (const double *)vlev(vn, l), sc))
+      return 1;
+  if (surface_norm(mg, level, sv) || k_bcgs_half_test(mg, s, th, sc)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(half_host, mg->norms_dev, sizeof(double) * GMG_MAX_S, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(half_host + GMG_MAX_S, sc + BC_HALF, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  if (precond_levels(level, q, sv, Am, err)) return 1;
+  if (k_surf_update(mg, krylov_table(mg, lo, level, level, false, tn, q), GMG_PREC_FP64, s, 2)) return 1;
+  if (k_surf_dot(mg, krylov_table(mg, lo, level, level, false, tn, tn), s, 1, 2, 1.0, sc) ||
+      k_surf_dot(mg, krylov_table(mg, lo, level, level, false, sv, tn), s, 1, 3, -1.0, sc))
+    return 1;
+  for (int l = bl; l <= level; ++l)
+    if (k_bcgs_xb(mg, vlen(mg, l), (double *)vlev(xv, l), (const double *)vlev(q, l), (double *)vlev(bv, l),
+                  (const double *)vlev(sv, l), (const double *)vlev(tn, l), sc))
+      return 1;
+  if (surface_norm(mg, level, bv)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
+  return 0;
+}
+
 // BCGSSolver's loop body (ls.cc:1904-2020) from the restart check on
 int NPBcgs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
+  if (mg->local()) return surface_bcgs_iteration(level, xv, bv, Am, err);
   const Level &L = mg->lev[level];
   const long long len = vlen(mg, level);
   double *b = (double *)vlev(bv, level), *x = (double *)vlev(xv, level);
@@ -1467,7 +1581,6 @@ int NPBcgs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const doubl
                    gmg_lresult *lr) {
   if (check_level(mg, level)) return 1;
   GMG_CHECK(mg->batch.ninst == 0, "bcgs on a batched hierarchy is not supported (use ls)");
-  GMG_CHECK(!mg->local(), "bcgs on a locally refined hierarchy is not supported (use ls)");
   GMG_CHECK(xv->prec == GMG_PREC_FP64 && bv->prec == GMG_PREC_FP64, "bcgs: x and b must be FP64");
   GMG_CHECK(!mixed || mg->opts.fp32_copy, "bcgs $mixed needs a hierarchy with FP32 copies");
   const int s = mg->lev[level].s;
@@ -1508,9 +1621,12 @@ int NPBcgs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const doubl
   for (int i = 0; i < maxiter; ++i) {
     if (lr->converged) break;
     if ((restart > 0 && i % restart == 0) || i == 0) {  // p = v = 0, r = b, alpha = rho = omega = 1
-      if (k_set(mg, GMG_PREC_FP64, vlev(p, level), len, 0.0) || k_set(mg, GMG_PREC_FP64, vlev(vn, level), len, 0.0) ||
-          k_copy(mg, GMG_PREC_FP64, vlev(r, level), vlev(bv, level), len))
-        return 1;
+      for (int l = mg->local() ? std::min(baselevel, level) : level; l <= level; ++l) {
+        const long long ln = vlen(mg, l);
+        if (k_set(mg, GMG_PREC_FP64, vlev(p, l), ln, 0.0) || k_set(mg, GMG_PREC_FP64, vlev(vn, l), ln, 0.0) ||
+            k_copy(mg, GMG_PREC_FP64, vlev(r, l), vlev(bv, l), ln))
+          return 1;
+      }
       GMG_CUDA(cudaMemcpyAsync(sc + BC_ALPHA, &scal_host[0], sizeof(double), cudaMemcpyHostToDevice, mg->stream));
       GMG_CUDA(cudaMemcpyAsync(sc + BC_RHO, &scal_host[1], sizeof(double), cudaMemcpyHostToDevice, mg->stream));
       GMG_CUDA(cudaMemcpyAsync(sc + BC_OMEGA, &scal_host[2], sizeof(double), cudaMemcpyHostToDevice, mg->stream));

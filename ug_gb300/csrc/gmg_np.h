@@ -229,6 +229,8 @@ struct NPCg : NPLs {
   int Solver(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit, const double *reduction,
              gmg_lresult *lr) override;
   int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err) override;
+  // locally refined hierarchies: CGUpdate on every level, products ON_SURFACE
+  int surface_cg_iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
   int check_iteration(int i) override;
   std::string Display() const override;
 };
@@ -250,6 +252,9 @@ struct NPBcgs : NPLs {
              gmg_lresult *lr) override;
   int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err) override;
   int precond(int level, gmg_vec *qv, gmg_vec *dv, gmg_mat *A, int *err);
+  // locally refined hierarchies: every level baselevel..top, products ON_SURFACE
+  int surface_bcgs_iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
+  int precond_levels(int level, gmg_vec *qv, gmg_vec *dv, gmg_mat *A, int *err);
   std::string Display() const override;
 };
 
