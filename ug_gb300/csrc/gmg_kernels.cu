@@ -700,11 +700,14 @@ __global__ void __launch_bounds__(BLK) gs_wave_kernel(const int *__restrict__ ro
 // entry (column, factor block) and, backward, the inverse diagonal block are
 // loaded before the launch wait (constant structure), so only the gathers of
 // t written by the previous wavefront remain after it.
-template <class T, int S, int TPR, bool ALL_ACTIVE>
+// DIAG: the rows have no upper-factor entries (the last colour of the
+// subdomain order), so their backward step t = D^{-1} t follows at once
+template <class T, int S, int TPR, bool ALL_ACTIVE, bool DIAG = false>
 __global__ void __launch_bounds__(BLK) ilu_fwd_kernel(const int *__restrict__ rows, int nrows,
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
                                                       const T *__restrict__ val, const uint8_t *__restrict__ flags,
-                                                      const T *__restrict__ b, T *__restrict__ t) {
+                                                      const T *__restrict__ b, T *__restrict__ t,
+                                                      const T *__restrict__ dinv) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int idx = gt / TPR, lane = gt & (TPR - 1);
   const bool valid = idx < nrows;
@@ -747,8 +750,21 @@ __global__ void __launch_bounds__(BLK) ilu_fwd_kernel(const int *__restrict__ ro
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
   if (valid && lane == 0) {
+    if (DIAG && active) {
+      T rhs[S];
 #pragma unroll
-    for (int r = 0; r < S; ++r) t[(size_t)row * S + r] = active ? b[(size_t)row * S + r] - s[r] : T(0);
+      for (int r = 0; r < S; ++r) rhs[r] = b[(size_t)row * S + r] - s[r];
+#pragma unroll
+      for (int r = 0; r < S; ++r) {
+        T v = T(0);
+#pragma unroll
+        for (int c = 0; c < S; ++c) v = fma(__ldg(dinv + (size_t)row * S * S + r * S + c), rhs[c], v);
+        t[(size_t)row * S + r] = v;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < S; ++r) t[(size_t)row * S + r] = active ? b[(size_t)row * S + r] - s[r] : T(0);
+    }
   }
 }
 
@@ -1913,14 +1929,20 @@ int ilu_domain(gmg_mg *mg, const Level &L, T *t, const T *b) {
     GMG_LAUNCH((ilu_region_kernel<T, S, TPR, ALL, true>), L.dom_nreg, REGION_BLK, L.dom_fwbeg, L.dom_fwptr,
                L.dom_frows, L.L.rowptr, L.L.col, lv, (const T *)nullptr, L.flags, b, t);
   LAUNCH_CHECK(mg);
+  // the last colour's rows have no upper entries: its forward and backward
+  // steps are one launch
   for (int c = 0; c < nc; ++c) {
     const int r0 = L.dom_cptr[c], nr = L.dom_cptr[c + 1] - r0;
     if (nr <= 0) continue;
-    GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, ALL>), grid_for((long long)nr * TPR), BLK, L.dom_iface + (r0 - L.dom_nint),
-               nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
+    if (c == nc - 1)
+      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, ALL, true>), grid_for((long long)nr * TPR), BLK,
+                 L.dom_iface + (r0 - L.dom_nint), nr, L.L.rowptr, L.L.col, lv, L.flags, b, t, ud);
+    else
+      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, ALL, false>), grid_for((long long)nr * TPR), BLK,
+                 L.dom_iface + (r0 - L.dom_nint), nr, L.L.rowptr, L.L.col, lv, L.flags, b, t, (const T *)nullptr);
     LAUNCH_CHECK(mg);
   }
-  for (int c = nc - 1; c >= 0; --c) {
+  for (int c = nc - 2; c >= 0; --c) {
     const int r0 = L.dom_cptr[c], nr = L.dom_cptr[c + 1] - r0;
     if (nr <= 0) continue;
     GMG_LAUNCH((ilu_bwd_kernel<T, S, TPR, ALL>), grid_for((long long)nr * TPR), BLK, L.dom_iface + (r0 - L.dom_nint),
@@ -1947,11 +1969,11 @@ int ilu_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
     if (nr <= 0) continue;
     if (L.all_active)
-      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, true>), grid_for((long long)nr * TPR), BLK, 
-          L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
+      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, true>), grid_for((long long)nr * TPR), BLK,
+                 L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t, (const T *)nullptr);
     else
-      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, false>), grid_for((long long)nr * TPR), BLK, 
-          L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t);
+      GMG_LAUNCH((ilu_fwd_kernel<T, S, TPR, false>), grid_for((long long)nr * TPR), BLK,
+                 L.lower.rows + r0, nr, L.L.rowptr, L.L.col, lv, L.flags, b, t, (const T *)nullptr);
     LAUNCH_CHECK(mg);
   }
   for (int w = 0; w < L.upper.nwave(); ++w) {
