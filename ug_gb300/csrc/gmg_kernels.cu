@@ -837,7 +837,7 @@ __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ ro
 // involved; the interface rows run before (backward) or after (forward) as
 // ordinary colour launches).  FWD: t = b - L t (unit lower factor), 0 off
 // ACTIVE rows; backward: t = D^{-1} (t - U t) on ACTIVE rows.
-constexpr int REGION_BLK = 256;
+constexpr int REGION_BLK = 128;
 template <class T, int S, int TPR, bool ALL_ACTIVE, bool FWD>
 __global__ void __launch_bounds__(REGION_BLK) ilu_region_kernel(
     const int *__restrict__ wbeg, const int *__restrict__ wptr, const int *__restrict__ rows,
