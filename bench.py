@@ -262,7 +262,7 @@ def run_local(args, stream, flush_l2, world, rank):
     gen = G.LocalGenerator(LOCAL_NUNI, LOCAL_NLOC, seed=SEED)
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    mg = G.MultiGrid(gen, order=G.ORDER_DOMAIN, fp32=True, device=torch.cuda.current_device())
+    mg = G.MultiGrid(gen, order=G.ORDER_DOMAIN, fp32=True, autotune=True, device=torch.cuda.current_device())
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     G.setup_lmgc(mg, "ilu", baselevel=0, red=RED, abslimit=1e-50, name="loc64")
     mg.npcreate("loc32", "linear_solver.gls")
@@ -388,7 +388,8 @@ def run_batched(args, stream, flush_l2, world, rank):
     import ug_gb300 as G
     from ug_gb300.workloads import batch_instances
     gens, nrefs = batch_instances(args.batch)
-    mg = G.MultiGrid(gens, batched=True, order=G.ORDER_COLOR, fp32=True, device=torch.cuda.current_device())
+    mg = G.MultiGrid(gens, batched=True, order=G.ORDER_COLOR, fp32=True, autotune=True,
+                     device=torch.cuda.current_device())
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     G.setup_lmgc(mg, "jac", baselevel=0, red=RED, abslimit=1e-50, name="bat64")
     mg.npcreate("bat32", "linear_solver.gls")
@@ -715,6 +716,7 @@ def run_ours(args):
             cpu = {"value": None, "unit": "solves/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
 
     waves = [mg.num_waves(l) for l in range(mg.nlevels)]
+    variants = [mg.level_variant(l) for l in range(mg.nlevels)]
     mg.close()
     c1 = run_c1(args, stream, flush_l2, world, rank)
     local_c3 = run_local(args, stream, flush_l2, world, rank) if not args.no_local else None
@@ -732,6 +734,7 @@ def run_ours(args):
             "config": workload_config({"iterations_mixed": r32["iters"], "iterations_fp64": r64["iters"],
                                        "parallelism": "replicas" if world > 1 else "1 GPU",
                                        "gs_waves_per_level": waves,
+                                       "kernel_variants_per_level (autotuned)": variants,
                                        "launches_per_solve": r32["launches_per_step"]}),
             "fp64": {"value": whole_job_rate(1, r64["ms_per_step"], world), "unit": "solves/s",
                      "ms_per_step": r64["ms_per_step"],

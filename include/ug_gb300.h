@@ -74,7 +74,7 @@ typedef struct {
 typedef struct {
   int order;        /* GMG_ORDER_* */
   int fp32_copy;    /* also keep FP32 copies of matrices/transfers (mixed precision) */
-  int autotune;     /* time SpMV variants per level at creation and keep the fastest */
+  int autotune;     /* time each level's kernel variants at creation and keep the fastest */
   int device;       /* CUDA device ordinal */
   int disable_pdl;  /* 1: launch without programmatic dependent launch */
 } gmg_mg_opts;
@@ -94,6 +94,11 @@ int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm);
 int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val);
 /* Number of multicolour classes (wavefronts of the gs/ilu schedule) on a level. */
 int gmg_mg_num_waves(const gmg_mg *mg, int level);
+/* The kernel variant a level runs: threads per row (CSR levels, 0 on
+ * sliced-ELLPACK levels), row structure prefetched before the launch wait and
+ * evict-first matrix stream (1 / 0, -1 = chosen by size); set by the
+ * autotuner (gmg_mg_opts.autotune) at creation. */
+int gmg_mg_level_variant(const gmg_mg *mg, int level, int *tpr, int *prefetch, int *stream);
 /* Device bytes held by the hierarchy. */
 long long gmg_mg_device_bytes(const gmg_mg *mg);
 /* Kernel launches issued by mg since creation (or the last reset). */

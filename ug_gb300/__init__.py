@@ -96,7 +96,7 @@ def lib(build_if_missing: bool = True):
         "gmg_transfer_interpolate_new_vectors": ([P, I, I, P, P], I),
         "gmg_transfer_project_solution": ([P, I, I, P, P], I),
         "gmg_transfer_adapt_correction": ([P, I, P, P, P, P], I), "gmg_mg_set_new_vectors": ([P, I, P], I),
-        "gmg_mg_update_values": ([P, I, P], I),
+        "gmg_mg_update_values": ([P, I, P], I), "gmg_mg_level_variant": ([P, I, P, P, P], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -508,6 +508,13 @@ class MultiGrid:
         if lib().gmg_ls_preprocess(self.np(obj), level, self.vec(x), self.vec(b), self.mat(A), C.byref(bl), C.byref(res)):
             _err(f"{obj} PreProcess")
         return bl.value
+
+    def level_variant(self, level: int) -> dict:
+        """The kernel variant of a level (autotuner's choice, -1 = by size)."""
+        t, p, st = C.c_int(), C.c_int(), C.c_int()
+        if lib().gmg_mg_level_variant(self._h, level, C.byref(t), C.byref(p), C.byref(st)):
+            _err("level_variant")
+        return {"tpr": t.value, "prefetch": p.value, "stream": st.value}
 
     def update_values(self, level: int, val):
         """New matrix values of a level (gmg_level_desc layout), structure unchanged."""

@@ -119,6 +119,9 @@ struct Level {
   long long *blk_aoff_dev = nullptr;
   // SpMV variant: threads cooperating on one row
   int tpr = 8;
+  // kernel variants of the level (autotuner; -1: by size): prefetch the
+  // rows' structure before the launch wait; evict-first matrix stream
+  int prefetch = -1, stream = -1;
   // sliced ELLPACK copy of A (slices of 32 consecutive rows stored column by
   // column, padded to the slice's longest row with zero blocks pointing at the
   // row itself): one thread per row, coalesced 32-row loads, no reductions

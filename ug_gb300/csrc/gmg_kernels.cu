@@ -58,6 +58,13 @@ constexpr long long PREFETCH_MAX_BLOCKS = 1100;  // ~280k rows (measured: the 65
 // vector entries; smaller matrices keep the default policy, which lets them
 // stay in L2 from one smoothing step to the next.
 constexpr long long STREAM_MIN_BYTES = 96ll << 20;
+
+// per-level variant choice: the autotuner's (Level::prefetch / Level::stream
+// 0 or 1), else the thresholds above (-1)
+inline bool use_prefetch(const Level &L, long long grid) {
+  return L.prefetch < 0 ? grid <= PREFETCH_MAX_BLOCKS : L.prefetch != 0;
+}
+inline bool use_stream(const Level &L, long long bytes) { return L.stream < 0 ? bytes > STREAM_MIN_BYTES : L.stream != 0; }
 template <bool ST, class T>
 __device__ __forceinline__ T ld_mat(const T *p) {
   if constexpr (ST) return __ldcs(p);
@@ -1810,7 +1817,7 @@ int spmv_dispatch_tpr(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *
   switch (L.tpr) {
 #define CASE(TP)                                                                                           \
   case TP:                                                                                                 \
-    if (grid_for((long long)n * TP) <= PREFETCH_MAX_BLOCKS)                                                \
+    if (use_prefetch(L, grid_for((long long)n * TP)))                                                      \
       GMG_LAUNCH((spmv_minus_kernel<T, TY, S, TP, ACC, 4>), grid_for((long long)n * TP), BLK, n, L.A.rowptr, \
                  L.A.col, val, y, x, acc);                                                                 \
     else                                                                                                   \
@@ -1839,8 +1846,8 @@ template <class T, class TY, bool ACC>
 int spmv_dispatch(gmg_mg *mg, const Level &L, const T *val, T *x, const TY *y, TY *acc) {
   if (L.sell && sell_val<T>(L)) {
     const T *sv = sell_val<T>(L);
-    const bool pre = grid_for(L.n) <= PREFETCH_MAX_BLOCKS;
-    const bool st = sell_bytes<T>(L) > STREAM_MIN_BYTES;
+    const bool pre = use_prefetch(L, grid_for(L.n));
+    const bool st = use_stream(L, sell_bytes<T>(L));
 #define SK(SS)                                                                                                   \
   if (pre)                                                                                                       \
     GMG_LAUNCH((sell_spmv_kernel<T, TY, TY, SS, ACC, PF<SS>::N>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col, \
@@ -1895,7 +1902,7 @@ int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
     if (nr <= 0) continue;
     const unsigned g = grid_for((long long)nr * TPR);
-    const bool pre = g <= PREFETCH_MAX_BLOCKS;
+    const bool pre = use_prefetch(L, g);
     if (L.all_active && pre)
       GMG_LAUNCH((gs_wave_kernel<T, S, TPR, true, 4>), g, BLK, L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv,
                  L.flags, b, t);
@@ -2172,8 +2179,8 @@ int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const floa
     if (k_add_mixed(mg, x, GMG_PREC_FP32, c, (long long)L.n * L.s)) return 1;
     return k_matmul_minus_mixed(mg, L, b, GMG_PREC_FP32, c);
   }
-  const bool pre = grid_for(L.n) <= PREFETCH_MAX_BLOCKS;
-  const bool st = sell_bytes<double>(L) > STREAM_MIN_BYTES;
+  const bool pre = use_prefetch(L, grid_for(L.n));
+  const bool st = use_stream(L, sell_bytes<double>(L));
 #define RU(SS)                                                                                                   \
   if (pre)                                                                                                       \
     GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, PF<SS>::N>), grid_for(L.n), BLK, L.n,          \
@@ -2217,10 +2224,10 @@ template <class T, int S, bool ALL>
 int jac_step_dispatch(gmg_mg *mg, const Level &L, T *bout, const T *bin, T *c, Damp<T> dm) {
   const T *dinv = dinv_of<T>(L);
   if (L.sell && sell_val<T>(L)) {
-    if (grid_for(L.n) <= PREFETCH_MAX_BLOCKS)
+    if (use_prefetch(L, grid_for(L.n)))
       GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, PF<S>::N>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,
                  sell_val<T>(L), dinv, L.flags, bin, bout, c, dm);
-    else if (sell_bytes<T>(L) > STREAM_MIN_BYTES)
+    else if (use_stream(L, sell_bytes<T>(L)))
       GMG_LAUNCH((sell_jac_step_kernel<T, S, ALL, -1>), grid_for(L.n), BLK, L.n, L.sell_ptr, L.sell_col,
                  sell_val<T>(L), dinv, L.flags, bin, bout, c, dm);
     else
@@ -2273,7 +2280,7 @@ int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
     if (r1 <= r0) continue;
     const unsigned g = grid_for(r1 - r0);
-    const bool pre = g <= PREFETCH_MAX_BLOCKS;
+    const bool pre = use_prefetch(L, g);
     if (L.all_active && pre)
       GMG_LAUNCH((sell_gs_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags,
                  b, t);
@@ -2297,7 +2304,7 @@ int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
       const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
       if (r1 <= r0) continue;
       const unsigned g = grid_for(r1 - r0);
-      const bool pre = g <= PREFETCH_MAX_BLOCKS;
+      const bool pre = use_prefetch(L, g);
       if (st == 0 && pre)
         GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b,
                    t, c);
@@ -2313,7 +2320,7 @@ int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
     }
   }
   const unsigned g = grid_for(L.n);
-  if (g <= PREFETCH_MAX_BLOCKS)
+  if (use_prefetch(L, g))
     GMG_LAUNCH((sell_upper_defect_kernel<T, S, PF<S>::N>), g, BLK, L.n, L.sell_ptr, L.sell_col, sv, t, b);
   else
     GMG_LAUNCH((sell_upper_defect_kernel<T, S, 0>), g, BLK, L.n, L.sell_ptr, L.sell_col, sv, t, b);
@@ -2389,7 +2396,7 @@ int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
 int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp,
                void *zero_coarse) {
   if (C.n == 0) return 0;
-  const bool pre = grid_for(C.n) <= PREFETCH_MAX_BLOCKS;
+  const bool pre = use_prefetch(C, grid_for(C.n));
 #define RK(TT, SS)                                                                                                 \
   do {                                                                                                             \
     if (pre)                                                                                                       \
@@ -2414,7 +2421,7 @@ int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, c
 
 int k_interpolate(gmg_mg *mg, const Level &F, int prec, void *to, const void *from, const double *damp, void *acc) {
   if (F.n == 0) return 0;
-  const bool pre = grid_for(F.n) <= PREFETCH_MAX_BLOCKS;
+  const bool pre = use_prefetch(F, grid_for(F.n));
 #define IK(TT, SS, A)                                                                                              \
   do {                                                                                                             \
     if (pre)                                                                                                       \

@@ -506,10 +506,17 @@ static int pick_tpr(const HostLevel &H) {
 }
 
 // ------------------------------------------------------------ autotuner
-// Times dmatmul_minus with 4, 8 and 16 threads per row on the level's own
-// matrix (CUDA events, median of 5) and keeps the fastest.
+// Picks each level's kernel variant by timing the level's dmatmul_minus (the
+// stream every smoother and transfer kernel of the level shares) back to
+// back: on sliced-ELLPACK levels the size-based choice, the row structure
+// prefetched before the launch wait, or the plain streaming loop (with an
+// evict-first matrix stream where the matrix exceeds half of L2); on CSR
+// levels the threads per row.
+// Median of 5 timed launches after one warm-up, in the precision the
+// V-cycle uses (FP32 when the hierarchy has FP32 copies).
 static int autotune_level(gmg_mg *mg, Level &L) {
-  if (L.n < 4096) return 0;
+  if (L.n < 256) return 0;
+  const int prec = mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64;
   void *x = nullptr, *y = nullptr;
   size_t len = size_t(L.n) * L.s;
   GMG_CUDA(cudaMalloc(&x, len * sizeof(double)));
@@ -519,27 +526,50 @@ static int autotune_level(gmg_mg *mg, Level &L) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  int best = L.tpr;
-  float best_ms = 1e30f;
-  const int cands[3] = {4, 8, 16};
-  for (int c : cands) {
-    if (L.s > 1 && c > 8) continue;
-    L.tpr = c;
+  auto time_it = [&]() -> float {
     std::vector<float> ts;
     for (int rep = 0; rep < 6; ++rep) {
       cudaEventRecord(e0, mg->stream);
-      if (k_matmul_minus(mg, L, GMG_PREC_FP64, x, y, nullptr)) break;
+      if (k_matmul_minus(mg, L, prec, x, y, nullptr)) return 1e30f;
       cudaEventRecord(e1, mg->stream);
       cudaEventSynchronize(e1);
       float ms = 0;
       cudaEventElapsedTime(&ms, e0, e1);
       if (rep) ts.push_back(ms);
     }
-    if (ts.empty()) continue;
     std::sort(ts.begin(), ts.end());
-    if (ts[ts.size() / 2] < best_ms) { best_ms = ts[ts.size() / 2]; best = c; }
+    return ts[ts.size() / 2];
+  };
+  float best_ms = 1e30f;
+  if (L.sell) {
+    // the size-based default first; another variant must be 5 % faster to
+    // replace it (a back-to-back launch sees a warmer L2 than the cycle,
+    // where the smoothers re-read the matrix between two products); the
+    // evict-first stream only where the matrix cannot stay in L2 anyway
+    const long long mbytes = L.sell_nent * ((long long)L.s * L.s * (prec == GMG_PREC_FP32 ? 4 : 8) + 4);
+    const bool big = mbytes > (64ll << 20);
+    int cands[3][2] = {{-1, -1}, {1, 0}, {0, big ? 1 : 0}};  // (prefetch, stream)
+    int bp = -1, bs = -1;
+    for (int k = 0; k < 3; ++k) {
+      L.prefetch = cands[k][0];
+      L.stream = cands[k][1];
+      const float ms = time_it();
+      if (k == 0) { best_ms = ms; continue; }
+      if (ms < 0.95f * best_ms) { best_ms = ms; bp = cands[k][0]; bs = cands[k][1]; }
+    }
+    L.prefetch = bp;
+    L.stream = bs;
+  } else {
+    int best = L.tpr;
+    const int cands[3] = {4, 8, 16};
+    for (int c : cands) {
+      if (L.s > 1 && c > 8) continue;
+      L.tpr = c;
+      const float ms = time_it();
+      if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    L.tpr = best;
   }
-  L.tpr = best;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(x);
@@ -840,6 +870,18 @@ int gmg_mg_update_values(gmg_mg *mg, int level, const double *val) {
   if (refresh_factors(mg, level)) return 1;
   mg->coarse_images.clear();
   ++mg->graph_epoch;
+  return 0;
+}
+
+// the kernel variant of a level: threads per row (CSR levels), prefetch
+// before the launch wait and evict-first stream (sliced-ELLPACK levels; -1 =
+// chosen by size)
+int gmg_mg_level_variant(const gmg_mg *mg, int level, int *tpr, int *prefetch, int *stream) {
+  if (!mg || level < 0 || level >= int(mg->lev.size())) { set_error("gmg_mg_level_variant: bad arguments"); return 1; }
+  const Level &L = mg->lev[level];
+  if (tpr) *tpr = L.sell ? 0 : L.tpr;
+  if (prefetch) *prefetch = L.prefetch;
+  if (stream) *stream = L.stream;
   return 0;
 }
 
