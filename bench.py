@@ -388,7 +388,7 @@ def run_batched(args, stream, flush_l2, world, rank):
     import ug_gb300 as G
     from ug_gb300.workloads import batch_instances
     gens, nrefs = batch_instances(args.batch)
-    mg = G.MultiGrid(gens, batched=True, order=G.ORDER_COLOR, fp32=True, autotune=True,
+    mg = G.MultiGrid(gens, batched=True, order=G.ORDER_LIST, fp32=True, autotune=True,
                      device=torch.cuda.current_device())
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     G.setup_lmgc(mg, "jac", baselevel=0, red=RED, abslimit=1e-50, name="bat64")
