@@ -1902,7 +1902,7 @@ int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], nr = L.lower.ptr[w + 1] - r0;
     if (nr <= 0) continue;
     const unsigned g = grid_for((long long)nr * TPR);
-    const bool pre = use_prefetch(L, g);
+    const bool pre = g <= PREFETCH_MAX_BLOCKS;  // per wave (the autotuner times whole-level launches)
     if (L.all_active && pre)
       GMG_LAUNCH((gs_wave_kernel<T, S, TPR, true, 4>), g, BLK, L.lower.rows + r0, nr, L.A.rowptr, L.A.col, val, dinv,
                  L.flags, b, t);
@@ -2280,7 +2280,7 @@ int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
     const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
     if (r1 <= r0) continue;
     const unsigned g = grid_for(r1 - r0);
-    const bool pre = use_prefetch(L, g);
+    const bool pre = g <= PREFETCH_MAX_BLOCKS;  // per wave (the autotuner times whole-level launches)
     if (L.all_active && pre)
       GMG_LAUNCH((sell_gs_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags,
                  b, t);
@@ -2304,7 +2304,7 @@ int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
       const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
       if (r1 <= r0) continue;
       const unsigned g = grid_for(r1 - r0);
-      const bool pre = use_prefetch(L, g);
+      const bool pre = g <= PREFETCH_MAX_BLOCKS;  // per wave (the autotuner times whole-level launches)
       if (st == 0 && pre)
         GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b,
                    t, c);

@@ -12,6 +12,8 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <condition_variable>
+#include <mutex>
 #include <queue>
 #include <thread>
 #include <tuple>
@@ -30,24 +32,83 @@ void set_error(const char *fmt, ...) {
 }
 const char *last_error() { return g_err; }
 
-// host copies into / out of the pinned staging buffers: one thread per 4 MB,
-// at most 8 (a single thread moves ~10 GB/s, short of the host link)
+// host copies into / out of the pinned staging buffers, split over a pool of
+// worker threads kept for the process (a single thread moves ~10-20 GB/s,
+// short of the host link; creating threads per call costs tens of us):
+// one part per 512 KB, at most 8 parts, the caller copies part 0
+namespace {
+class CopyPool {
+ public:
+  static CopyPool &get() {
+    static CopyPool pool;
+    return pool;
+  }
+  void run(char *dst, const char *src, size_t bytes, int parts) {
+    std::unique_lock<std::mutex> lk(m_);
+    busy_.wait(lk, [&] { return pending_ == 0; });  // one copy at a time
+    dst_ = dst; src_ = src; bytes_ = bytes; parts_ = parts;
+    chunk_ = ((bytes + parts - 1) / parts + 63) & ~size_t(63);
+    next_ = 1;
+    pending_ = parts - 1;
+    ++gen_;
+    lk.unlock();
+    work_.notify_all();
+    std::memcpy(dst, src, std::min(chunk_, bytes));
+    lk.lock();
+    done_.wait(lk, [&] { return pending_ == 0; });
+    busy_.notify_one();
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    work_.notify_all();
+    for (auto &t : th_) t.join();
+  }
+
+ private:
+  CopyPool() {
+    for (int t = 0; t < 7; ++t) th_.emplace_back([this] { loop(); });
+  }
+  void loop() {
+    unsigned long long seen = 0;
+    std::unique_lock<std::mutex> lk(m_);
+    for (;;) {
+      work_.wait(lk, [&] { return stop_ || (gen_ != seen && next_ < parts_); });
+      if (stop_) return;
+      const int part = next_++;
+      if (next_ >= parts_) seen = gen_;
+      const size_t o = chunk_ * size_t(part);
+      char *d = dst_;
+      const char *s = src_;
+      const size_t n = o < bytes_ ? std::min(chunk_, bytes_ - o) : 0;
+      lk.unlock();
+      if (n) std::memcpy(d + o, s + o, n);
+      lk.lock();
+      if (--pending_ == 0) done_.notify_all();
+    }
+  }
+  std::mutex m_;
+  std::condition_variable work_, done_, busy_;
+  std::vector<std::thread> th_;
+  char *dst_ = nullptr;
+  const char *src_ = nullptr;
+  size_t bytes_ = 0, chunk_ = 0;
+  int parts_ = 0, next_ = 0, pending_ = 0;
+  unsigned long long gen_ = 0;
+  bool stop_ = false;
+};
+}  // namespace
+
 void par_copy(void *dst, const void *src, size_t bytes) {
-  const size_t per = size_t(4) << 20;
-  const int nt = int(std::min<size_t>(8, (bytes + per - 1) / per));
-  if (nt <= 1) {
+  const size_t per = size_t(512) << 10;
+  const int parts = int(std::min<size_t>(8, (bytes + per - 1) / per));
+  if (parts <= 1) {
     std::memcpy(dst, src, bytes);
     return;
   }
-  const size_t chunk = ((bytes + nt - 1) / nt + 63) & ~size_t(63);
-  std::vector<std::thread> th;
-  for (int t = 1; t < nt; ++t) {
-    const size_t o = chunk * t;
-    if (o >= bytes) break;
-    th.emplace_back([=] { std::memcpy((char *)dst + o, (const char *)src + o, std::min(chunk, bytes - o)); });
-  }
-  std::memcpy(dst, src, std::min(chunk, bytes));
-  for (auto &x : th) x.join();
+  CopyPool::get().run(static_cast<char *>(dst), static_cast<const char *>(src), bytes, parts);
 }
 
 int Arena::alloc(size_t bytes) {
@@ -507,13 +568,13 @@ static int pick_tpr(const HostLevel &H) {
 
 // ------------------------------------------------------------ autotuner
 // Picks each level's kernel variant by timing the level's dmatmul_minus (the
-// stream every smoother and transfer kernel of the level shares) back to
-// back: on sliced-ELLPACK levels the size-based choice, the row structure
+// stream every smoother and transfer kernel of the level shares) in chains
+// of 8 launches: on sliced-ELLPACK levels the size-based choice, the row structure
 // prefetched before the launch wait, or the plain streaming loop (with an
 // evict-first matrix stream where the matrix exceeds half of L2); on CSR
 // levels the threads per row.
-// Median of 5 timed launches after one warm-up, in the precision the
-// V-cycle uses (FP32 when the hierarchy has FP32 copies).
+// Median of 3 timed chains after one warm-up, in the precision the V-cycle
+// uses (FP32 when the hierarchy has FP32 copies).
 static int autotune_level(gmg_mg *mg, Level &L) {
   if (L.n < 256) return 0;
   const int prec = mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64;
@@ -526,16 +587,21 @@ static int autotune_level(gmg_mg *mg, Level &L) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  // a chain of launches, as in the cycle: programmatic dependent launch lets
+  // each kernel's pre-wait part overlap its predecessor, which an isolated
+  // launch would not show
+  constexpr int CHAIN = 8;
   auto time_it = [&]() -> float {
     std::vector<float> ts;
-    for (int rep = 0; rep < 6; ++rep) {
+    for (int rep = 0; rep < 4; ++rep) {
       cudaEventRecord(e0, mg->stream);
-      if (k_matmul_minus(mg, L, prec, x, y, nullptr)) return 1e30f;
+      for (int k = 0; k < CHAIN; ++k)
+        if (k_matmul_minus(mg, L, prec, x, y, nullptr)) return 1e30f;
       cudaEventRecord(e1, mg->stream);
       cudaEventSynchronize(e1);
       float ms = 0;
       cudaEventElapsedTime(&ms, e0, e1);
-      if (rep) ts.push_back(ms);
+      if (rep) ts.push_back(ms / CHAIN);
     }
     std::sort(ts.begin(), ts.end());
     return ts[ts.size() / 2];
