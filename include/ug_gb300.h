@@ -206,6 +206,11 @@ int gmg_dcopy(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y);                   
 int gmg_dadd(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y);                             /* dadd 2586: x += y */
 int gmg_dmatmul_minus(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *A, gmg_vec *y);        /* 3997: x -= A y */
 int gmg_dnrm2x(gmg_mg *mg, int level, gmg_vec *x, double *norms);                        /* 3156 */
+int gmg_dmatmul(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *A, gmg_vec *y);              /* 3782: x = A y (FP64 x) */
+int gmg_dmatmul_add(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *A, gmg_vec *y);          /* 3889: x += A y */
+int gmg_dscalx(gmg_mg *mg, int level, gmg_vec *x, const double *a);                       /* 2510: x *= a */
+int gmg_daxpy(gmg_mg *mg, int level, gmg_vec *x, const double *a, gmg_vec *y);            /* 2875: x += a y */
+int gmg_ddot(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, double *result);              /* 3104 (FP64) */
 int gmg_l_jac(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);                /* ugiter.cc:271 */
 int gmg_l_lgs(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);                /* ugiter.cc:412 */
 int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *M, const double *beta);            /* ugiter.cc:2252 */

@@ -291,3 +291,43 @@ def test_update_values_matches_ug(G, sm, fuse):
     x2, lr2 = mg.solve_host("mgs", dst["rhs"])  # replayed graph after the update
     assert lr2.iters == lr.iters and np.array_equal(x, x2)
     mg.close()
+
+
+def _bsr_apply(d, y):
+    s = int(d["s"]); rp, col = np.asarray(d["rowptr"]), np.asarray(d["col"])
+    val = np.asarray(d["val"]).reshape(-1, s, s)
+    yb = np.asarray(y).reshape(-1, s)
+    out = np.zeros_like(yb)
+    for i in range(int(d["n"])):
+        for k in range(rp[i], rp[i + 1]):
+            out[i] += val[k] @ yb[col[k]]
+    return out.ravel()
+
+
+@pytest.mark.parametrize("name", ["q1_jac", "el_ilu", "p1k_gs"])
+def test_blas_level_operations(G, name):
+    """dmatmul, dmatmul_add, dscalx, daxpy, ddot (ugblas.cc:3782, 3889, 2510,
+    2875, 3104) on one level against numpy, 1e-12 relative."""
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    mg = G.MultiGrid(levels, order=1)
+    top = mg.top
+    d = levels[top]
+    s = int(d["s"])
+    rng = np.random.default_rng(3)
+    x0, y = rng.uniform(-1, 1, d["n"] * s), rng.uniform(-1, 1, d["n"] * s)
+    mg.createvector("x", "y")
+    mg.upload("y", top, y)
+    ay = _bsr_apply(d, y)
+    mg.upload("x", top, x0); mg.dmatmul(top, "x", "y")
+    assert rel(mg.download("x", top), ay) <= 1e-12
+    mg.upload("x", top, x0); mg.dmatmul_add(top, "x", "y")
+    assert rel(mg.download("x", top), x0 + ay) <= 1e-12
+    a = np.array([0.5, -2.0, 3.0])[:s]
+    mg.upload("x", top, x0); mg.dscalx(top, "x", a)
+    assert rel(mg.download("x", top), (x0.reshape(-1, s) * a).ravel()) <= 1e-15
+    mg.upload("x", top, x0); mg.daxpy(top, "x", a, "y")
+    assert rel(mg.download("x", top), (x0.reshape(-1, s) + a * y.reshape(-1, s)).ravel()) <= 1e-15
+    mg.upload("x", top, x0)
+    assert abs(mg.ddot(top, "x", "y") - float(x0 @ y)) <= 1e-12 * np.sum(np.abs(x0 * y))
+    mg.close()

@@ -102,6 +102,8 @@ def lib(build_if_missing: bool = True):
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
         "gmg_dset": ([P, I, P, D], I), "gmg_dcopy": ([P, I, P, P], I), "gmg_dadd": ([P, I, P, P], I),
         "gmg_dmatmul_minus": ([P, I, P, P, P], I), "gmg_dnrm2x": ([P, I, P, P], I),
+        "gmg_dmatmul": ([P, I, P, P, P], I), "gmg_dmatmul_add": ([P, I, P, P, P], I),
+        "gmg_dscalx": ([P, I, P, P], I), "gmg_daxpy": ([P, I, P, P, P], I), "gmg_ddot": ([P, I, P, P, P], I),
         "gmg_l_jac": ([P, I, P, P, P], I), "gmg_l_lgs": ([P, I, P, P, P], I),
         "gmg_l_ilu_decomp": ([P, I, P, P], I), "gmg_l_luiter": ([P, I, P, P, P], I),
         "gmg_standard_restrict": ([P, I, P, P, P], I), "gmg_standard_interpolate_correction": ([P, I, P, P, P], I),
@@ -581,6 +583,30 @@ class MultiGrid:
     def dmatmul_minus(self, level, x, y, A="MAT"):
         if lib().gmg_dmatmul_minus(self._h, level, self.vec(x), self.mat(A), self.vec(y)):
             _err("dmatmul_minus")
+
+    def dmatmul(self, level, x, y, A="MAT"):
+        if lib().gmg_dmatmul(self._h, level, self.vec(x), self.mat(A), self.vec(y)):
+            _err("dmatmul")
+
+    def dmatmul_add(self, level, x, y, A="MAT"):
+        if lib().gmg_dmatmul_add(self._h, level, self.vec(x), self.mat(A), self.vec(y)):
+            _err("dmatmul_add")
+
+    def dscalx(self, level, x, a):
+        f = _sc(a)
+        if lib().gmg_dscalx(self._h, level, self.vec(x), _ptr(f)):
+            _err("dscalx")
+
+    def daxpy(self, level, x, a, y):
+        f = _sc(a)
+        if lib().gmg_daxpy(self._h, level, self.vec(x), _ptr(f), self.vec(y)):
+            _err("daxpy")
+
+    def ddot(self, level, x, y) -> float:
+        r = C.c_double()
+        if lib().gmg_ddot(self._h, level, self.vec(x), self.vec(y), C.byref(r)):
+            _err("ddot")
+        return r.value
 
     def dnrm2x(self, level, x):
         out = np.zeros(MAX_S)

@@ -270,11 +270,12 @@ struct SurfLevels {
   float *b32[SURF_MAX_LEVELS] = {};
   float *c32[SURF_MAX_LEVELS] = {};
 };
-// selected rows (mask, or all): op 0 b -= A y, 1 b += A y, 2 b = -(A y) (FP64
+// selected rows (mask, or all): op 0 b -= A y, 1 b += A y, 2 b = -(A y), 3 b = A y (FP64
 // matrix, y of precision yprec); addx levels: x += y on every row
 int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s, int op = 0);
-// dot product of x (t.b) and y (t.y) over the surface rows with the cg (kind
-// 0, mode 1/2) or bcgs (kind 1, modes 0-3) scalar step on sc[]
+// dot product of x (t.b) and y (t.y) over the selected rows with the cg (kind
+// 0, mode 1/2) or bcgs (kind 1, modes 0-3) scalar step on sc[], or (kind 2)
+// the plain sum times sign into sc[0]
 int k_surf_dot(gmg_mg *mg, const SurfLevels &t, int s, int kind, int mode, double sign, double *sc);
 // b32 = b on every row; c32 = 0 where given
 int k_surf_prepare(gmg_mg *mg, const SurfLevels &t, int s);
@@ -289,6 +290,8 @@ int k_set(gmg_mg *mg, int prec, void *x, long long len, double a);
 int k_copy(gmg_mg *mg, int prec, void *x, const void *y, long long len);
 int k_add(gmg_mg *mg, int prec, void *x, const void *y, long long len);
 int k_scale(gmg_mg *mg, int prec, void *x, int n, int s, const double *damp);
+// x += a y, a per component
+int k_axpy(gmg_mg *mg, int prec, void *x, const void *y, int n, int s, const double *a);
 int k_convert(gmg_mg *mg, int dst_prec, void *dst, int src_prec, const void *src, long long len);
 int k_add_mixed(gmg_mg *mg, double *x64, int src_prec, const void *c, long long len);  // x64 += c
 // x -= A y (A in the precision of x/y); if acc != null also acc += y

@@ -2620,6 +2620,29 @@ int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *per
   return 0;
 }
 
+// daxpy, ugblas.cc:2875: x += a y (per component a), one rounding each
+template <class T, int S>
+__global__ void __launch_bounds__(BLK) axpy_kernel(long long n, T *__restrict__ x, const T *__restrict__ y,
+                                                   Damp<T> a) {
+  pdl_prologue();
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int r = 0; r < S; ++r) x[i * S + r] = x[i * S + r] + a.d[r] * y[i * S + r];
+}
+
+int k_axpy(gmg_mg *mg, int prec, void *x, const void *y, int n, int s, const double *a) {
+  if (n <= 0) return 0;
+#define AX(TT, SS) GMG_LAUNCH((axpy_kernel<TT, SS>), grid_for(n), BLK, (long long)n, (TT *)x, (const TT *)y, \
+                              make_damp<TT>(a, SS))
+  if (prec == GMG_PREC_FP64) { if (s == 1) AX(double, 1); else if (s == 2) AX(double, 2); else if (s == 3) AX(double, 3);
+                               else { set_error("block size %d not compiled", s); return 1; } }
+  else { if (s == 1) AX(float, 1); else if (s == 2) AX(float, 2); else if (s == 3) AX(float, 3);
+         else { set_error("block size %d not compiled", s); return 1; } }
+#undef AX
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 // ------------------------------------------------------------ solution transfer (transgrid.cc:354, 655)
 template <class T, int S>
 __global__ void __launch_bounds__(BLK) interp_new_kernel(int nf, const int *__restrict__ prow,
@@ -2686,7 +2709,7 @@ int k_project(gmg_mg *mg, const Level &F, const Level &C, int prec, void *xc, co
 // NEW_DEFECT vectors of the top level, each row with its own level's matrix
 // and vectors.  One launch covers every level of a SurfLevels table: thread g
 // handles row g - row0[l] of the level l with row0[l] <= g < row0[l+1].
-// OP 0: b -= A y, 1: b += A y, 2: b = -(A y) on the selected rows (the
+// OP 0: b -= A y, 1: b += A y, 2: b = -(A y), 3: b = A y on the selected rows (the
 // surface rows of `mask`, or every row where `all` is set)
 template <int S, class YT, int OP>
 __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
@@ -2716,7 +2739,7 @@ __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
 #pragma unroll
       for (int r = 0; r < S; ++r) {
         double &bv = t.b[l][(size_t)i * S + r];
-        bv = OP == 0 ? bv - acc[r] : (OP == 1 ? bv + acc[r] : -acc[r]);
+        bv = OP == 0 ? bv - acc[r] : (OP == 1 ? bv + acc[r] : (OP == 2 ? -acc[r] : acc[r]));
       }
     }
     if (t.addx[l]) {
@@ -2805,7 +2828,7 @@ int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s, int op) {
   const int g = vec_grid(t.row0[t.nlev]);
 #define SO(SS, OP) { if (yprec == GMG_PREC_FP64) GMG_LAUNCH((surf_update_kernel<SS, double, OP>), g, BLK, t); \
                      else GMG_LAUNCH((surf_update_kernel<SS, float, OP>), g, BLK, t); }
-#define SU(SS) { if (op == 0) SO(SS, 0) else if (op == 1) SO(SS, 1) else SO(SS, 2) }
+#define SU(SS) { if (op == 0) SO(SS, 0) else if (op == 1) SO(SS, 1) else if (op == 2) SO(SS, 2) else SO(SS, 3) }
   if (s == 1) SU(1) else if (s == 2) SU(2) else if (s == 3) SU(3)
   else { set_error("block size %d not compiled", s); return 1; }
 #undef SU
@@ -2831,7 +2854,7 @@ __global__ void __launch_bounds__(BLK) surf_dot_kernel(SurfLevels t, double *__r
     int l = 0;
     while (g >= t.row0[l + 1]) ++l;
     const int i = g - t.row0[l];
-    if (!(t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l]))) continue;
+    if (!(t.all[l] || (t.mask[l] && (__ldg(t.flags[l] + i) & t.mask[l])))) continue;
     const double *__restrict__ y = static_cast<const double *>(t.y[l]);
 #pragma unroll
     for (int r = 0; r < S; ++r) acc[r] = fma(t.b[l][(size_t)i * S + r], y[(size_t)i * S + r], acc[r]);
@@ -2874,7 +2897,8 @@ __global__ void __launch_bounds__(BLK) surf_dot_kernel(SurfLevels t, double *__r
     double d = 0.0;
     for (int r = 0; r < S; ++r) d += red[r][0];
     if (KIND == 0) cg_scalars<MODE>(sign * d, sc);
-    else bcgs_scalars<MODE>(d, sign, sc);
+    else if (KIND == 1) bcgs_scalars<MODE>(d, sign, sc);
+    else sc[0] = sign * d;
     *ticket = 0u;
   }
 }
@@ -2883,7 +2907,8 @@ int k_surf_dot(gmg_mg *mg, const SurfLevels &t, int s, int kind, int mode, doubl
   unsigned *ticket = reinterpret_cast<unsigned *>(mg->norms_dev + GMG_MAX_S);
 #define SD(SS, K, M) GMG_LAUNCH((surf_dot_kernel<SS, K, M>), REDUCE_BLOCKS, BLK, t, mg->partial, ticket, sc, sign)
 #define SM(SS)                                                                   \
-  if (kind == 0) { if (mode == 1) SD(SS, 0, 1); else SD(SS, 0, 2); }             \
+  if (kind == 2) SD(SS, 2, 0);                                                    \
+  else if (kind == 0) { if (mode == 1) SD(SS, 0, 1); else SD(SS, 0, 2); }        \
   else if (mode == BM_RHO) SD(SS, 1, BM_RHO); else if (mode == BM_ALPHA) SD(SS, 1, BM_ALPHA); \
   else if (mode == BM_TT) SD(SS, 1, BM_TT); else SD(SS, 1, BM_OMEGA);
   if (s == 1) { SM(1) } else if (s == 2) { SM(2) } else if (s == 3) { SM(3) }

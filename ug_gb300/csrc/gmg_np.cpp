@@ -1886,6 +1886,54 @@ int gmg_dmatmul_minus(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) 
   GMG_CHECK(y->prec == x->prec, "dmatmul_minus: precision mismatch");
   return k_matmul_minus(mg, mg->lev[level], x->prec, vlev(x, level), vlev(y, level), nullptr);
 }
+// dmatmul / dmatmul_add, ugblas.cc:3782 / 3889: x = A y, x += A y (FP64, every row)
+static int matmul_op(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, int op) {
+  GMG_CHECK(x->prec == GMG_PREC_FP64, "dmatmul: x must be FP64");
+  SurfLevels t;
+  surf_table(mg, level, level, level, t);
+  t.all[0] = 1;
+  t.b[0] = (double *)vlev(x, level);
+  t.y[0] = vlev(y, level);
+  return k_surf_update(mg, t, y->prec, mg->lev[level].s, op);
+}
+int gmg_dmatmul(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) {
+  MGV(mg, level);
+  return matmul_op(mg, level, x, y, 3);
+}
+int gmg_dmatmul_add(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) {
+  MGV(mg, level);
+  return matmul_op(mg, level, x, y, 1);
+}
+// dscalx, ugblas.cc:2510: x *= a per component
+int gmg_dscalx(gmg_mg *mg, int level, gmg_vec *x, const double *a) {
+  MGV(mg, level);
+  GMG_CHECK(a, "dscalx: no factors");
+  double f[GMG_MAX_S];
+  for (int r = 0; r < GMG_MAX_S; ++r) f[r] = r < mg->lev[level].s ? a[r] : 1.0;
+  return k_scale(mg, x->prec, vlev(x, level), mg->lev[level].n, mg->lev[level].s, f);
+}
+// daxpyx, ugblas.cc:2875: x += a y per component
+int gmg_daxpy(gmg_mg *mg, int level, gmg_vec *x, const double *a, gmg_vec *y) {
+  MGV(mg, level);
+  GMG_CHECK(a && x->prec == y->prec, "daxpy: no factors or precision mismatch");
+  return k_axpy(mg, x->prec, vlev(x, level), vlev(y, level), mg->lev[level].n, mg->lev[level].s, a);
+}
+// ddot, ugblas.cc:3104: the sum over every row and component (FP64)
+int gmg_ddot(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, double *result) {
+  MGV(mg, level);
+  GMG_CHECK(result && x->prec == GMG_PREC_FP64 && y->prec == GMG_PREC_FP64, "ddot: FP64 vectors and a result");
+  SurfLevels t;
+  surf_table(mg, level, level, level, t);
+  t.all[0] = 1;
+  t.b[0] = (double *)vlev(x, level);
+  t.y[0] = vlev(y, level);
+  double *sc = mg->norms_dev;  // scratch: the norms' slot 0
+  if (k_surf_dot(mg, t, mg->lev[level].s, 2, 0, 1.0, sc)) return 1;
+  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, sc, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  *result = mg->norms_host[0];
+  return 0;
+}
 int gmg_dnrm2x(gmg_mg *mg, int level, gmg_vec *x, double *norms) {
   MGV(mg, level);
   if (k_nrm2x(mg, mg->lev[level], x->prec, vlev(x, level))) return 1;
