@@ -293,6 +293,39 @@ def test_update_values_matches_ug(G, sm, fuse):
     mg.close()
 
 
+@pytest.mark.parametrize("maxit", [100, 3])
+@pytest.mark.parametrize("name,order,mixed", [("p1_gs", 0, False), ("q1_jac", 1, False), ("el_ilu", 0, False),
+                                              ("q1_gs", 1, True), ("ls_ilu", 0, False), ("ls_gs", 0, True)])
+def test_device_loop_matches_host_loop(G, name, order, mixed, maxit):
+    """ls's loop after the first iteration runs on the device as one
+    conditional graph (a WHILE node over the iteration and the stopping test,
+    ls.cc:680-730); the host loop ($dloop 0) is the same loop tested on the
+    host.  Both stop at the same iteration (converged, or at $m unconverged)
+    with the same last defect and the same x, bit for bit; the second solve
+    replays the built loop graph."""
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    sm = fx["smoother"]
+    out = {}
+    for dloop in (True, False):
+        mg = G.MultiGrid(levels, order=order, fp32=mixed)
+        G.setup_lmgc(mg, sm, baselevel=int(fx["baselevel"][0]), damp=_damp(sm), red=1e-10, abslimit=1e-50,
+                     maxit=maxit, mixed=mixed, dloop=dloop)
+        rhs = fx["rhs_all"] if mg.local else fx["rhs"]
+        runs = [mg.solve_host("mgs", rhs) for _ in range(2)]
+        out[dloop] = (runs, mg.npdisplay("mgs"))
+        mg.close()
+    (dev, dev_disp), (host, host_disp) = out[True], out[False]
+    assert "loop = device (built)" in dev_disp, dev_disp
+    assert "loop = host" in host_disp
+    for (xd, ld), (xh, lh) in zip(dev, host):
+        assert ld.iters == lh.iters and ld.converged == lh.converged
+        assert ld.converged == (maxit == 100)
+        assert ld.iters == (lh.iters if maxit == 100 else 3)
+        assert list(ld.last_defect) == list(lh.last_defect)
+        assert np.array_equal(xd, xh)
+
+
 def _bsr_apply(d, y):
     s = int(d["s"]); rp, col = np.asarray(d["rowptr"]), np.asarray(d["col"])
     val = np.asarray(d["val"]).reshape(-1, s, s)

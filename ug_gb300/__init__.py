@@ -671,7 +671,8 @@ class MultiGrid:
 def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: int = 2, nu2: int = 2,
                damp: float | None = None, red: float = 1e-10, abslimit: float = 1e-50, maxit: int = 100,
                mixed: bool = False, x: str = "sol", b: str = "rhs", name: str = "mgs",
-               fuse: int | None = None, graph: bool = True, bsmem: int | None = None) -> str:
+               fuse: int | None = None, graph: bool = True, bsmem: int | None = None,
+               dloop: bool = True) -> str:
     """The standard script of the workloads, as UG numproc commands:
 
         npcreate transfer $c gtransfer; npcreate smooth $c g<smoother>;
@@ -695,7 +696,7 @@ def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: in
     mg.npinit("lmgc", f"$S smooth smooth basesolver $T transfer $n1 {nu1} $n2 {nu2} $b {baselevel}{fz}")
     mg.npcreate(name, "linear_solver.gls")
     st = mg.npinit(name, f"$A MAT $x {x} $b {b} $red {red} $abslimit {abslimit} $m {maxit} $I lmgc"
-                         f" $mixed {int(mixed)} $graph {int(graph)}")
+                         f" $mixed {int(mixed)} $graph {int(graph)} $dloop {int(dloop)}")
     if st != NP_EXECUTABLE:
         raise GmgError(f"{name} not executable (status {st})")
     return name

@@ -2620,6 +2620,35 @@ int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *per
   return 0;
 }
 
+// the test of ls's loop after one device-side iteration: the same
+// comparisons as the host loop (sc_cmp, npscan.cc:1027: every |d_r| < |lim_r|)
+__global__ void ls_loop_test_kernel(LsLoopState *st, const double *__restrict__ norms, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0) return;
+  const int it = st->it + 1, s = st->s;
+  st->it = it;
+  bool finite = true, below_abs = true, below_reach = true;
+  for (int r = 0; r < s; ++r) {
+    const double d = norms[r];
+    st->last[r] = d;
+    finite = finite && isfinite(d);
+    below_abs = below_abs && fabs(d) < fabs(st->abs[r]);
+    below_reach = below_reach && fabs(d) < fabs(st->reach[r]);
+  }
+  if (!finite) {
+    st->bad = it;
+    cudaGraphSetConditional(h, 0);
+    return;
+  }
+  if (below_abs || below_reach) st->conv = 1;
+  cudaGraphSetConditional(h, (!st->conv && it < st->maxit) ? 1u : 0u);
+}
+
+int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, cudaGraphConditionalHandle h) {
+  ls_loop_test_kernel<<<1, 32, 0, mg->stream>>>(st, mg->norms_dev, h);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 // daxpy, ugblas.cc:2875: x += a y (per component a), one rounding each
 template <class T, int S>
 __global__ void __launch_bounds__(BLK) axpy_kernel(long long n, T *__restrict__ x, const T *__restrict__ y,

@@ -914,6 +914,9 @@ int NPLinearSolver::Execute(const Args &a) {
 
 NPLs::~NPLs() {
   if (graph) cudaGraphExecDestroy(graph);
+  if (loop_graph) cudaGraphExecDestroy(loop_graph);
+  if (loop_dev) cudaFree(loop_dev);
+  if (loop_host) cudaFreeHost(loop_host);
 }
 
 int NPLs::Init(const Args &a) {  // LinearSolverInit, ls.cc:788
@@ -927,14 +930,19 @@ int NPLs::Init(const Args &a) {  // LinearSolverInit, ls.cc:788
   display = a.get_word("d", &d) ? (d == "full" ? 2 : d == "red" ? 1 : 0) : 0;
   if (!a.get_int("mixed", &mixed)) mixed = 0;
   if (!a.get_int("graph", &use_graph)) use_graph = 1;
+  if (!a.get_int("dloop", &use_device_loop)) use_device_loop = 1;
   if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+  if (loop_graph) { cudaGraphExecDestroy(loop_graph); loop_graph = nullptr; }
   return InitLS(a);
 }
 
 std::string NPLs::Display() const {
   std::ostringstream o;
   o << "class " << cls << "\nm = " << maxiter << "\nbaselevel = " << baselevel
-    << "\nIter = " << (IterNp ? IterNp->name : "---") << "\nmixed = " << mixed << "\nred = "
+    << "\nIter = " << (IterNp ? IterNp->name : "---") << "\nmixed = " << mixed << "\nloop = "
+    << (!use_device_loop || !use_graph ? "host" : loop_unavailable ? "host (conditional graph unavailable)"
+                                                                   : loop_graph ? "device (built)" : "device")
+    << "\nred = "
     << fmt_sc(reduction, 1) << "\nabslimit = " << fmt_sc(abslimit, 1) << "\n";
   return o.str();
 }
@@ -1087,7 +1095,8 @@ int NPLs::surface_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, in
     if (k_surf_update(mg, t, GMG_PREC_FP32, s)) return 1;
   }
   if (surface_norm(mg, level, bv)) return 1;
-  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
+  if (norm_to_host)
+    GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
   return 0;
 }
 
@@ -1151,7 +1160,8 @@ int NPLs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) 
       return 1;
   }
   if (k_nrm2x(mg, L, bv->prec, vlev(bv, level))) return 1;
-  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
+  if (norm_to_host)
+    GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
   return 0;
 }
 
@@ -1178,14 +1188,22 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   }
   lr->converged = sc_cmp(lr->first_defect, abs_, s);
   lr->number_of_linear_iterations = 0;
-  if (graph && (graph_level != level || graph_x != xv || graph_b != bv || graph_epoch != mg->graph_epoch)) {
-    cudaGraphExecDestroy(graph);
+  if ((graph || loop_graph) &&
+      (graph_level != level || graph_x != xv || graph_b != bv || graph_epoch != mg->graph_epoch)) {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (loop_graph) cudaGraphExecDestroy(loop_graph);
     graph = nullptr;
+    loop_graph = nullptr;
   }
   if (batched(level)) return batch_solver(level, xv, bv, Am, abs_, red, lr);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GMG_CUDA(cudaStreamIsCapturing(mg->stream, &cap));
+  const bool on_device = use_device_loop && use_graph && !loop_unavailable && IterNp->capturable() &&
+                         cap == cudaStreamCaptureStatusNone;
   int i;
   for (i = 0; i < maxiter; ++i) {
     if (lr->converged) break;
+    if (i > 0 && on_device) return device_loop(i, level, xv, bv, Am, abs_, reach, lr);
     if (step(i, level, xv, bv, Am, lr) || check_iteration(i)) return 1;
     for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
     for (int r = 0; r < s; ++r)
@@ -1197,6 +1215,106 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
     }
   }
   if (!lr->converged) lr->number_of_linear_iterations = i;
+  return 0;
+}
+
+// the conditional graph of ls's loop: a WHILE node (its condition 1 at every
+// launch, for the host launches it only while an iteration is due) whose body
+// is one iteration, captured without the norms' copy to the host, and the
+// test that counts it and sets the condition for the next pass.  Any error in
+// building it leaves the host loop in charge.
+int NPLs::build_loop(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am) {
+  if (!loop_dev) {
+    GMG_CUDA(cudaMalloc(&loop_dev, sizeof(LsLoopState)));
+    GMG_CUDA(cudaMallocHost(&loop_host, sizeof(LsLoopState)));
+  }
+  cudaGraph_t g = nullptr;
+  GMG_CUDA(cudaGraphCreate(&g, 0));
+  auto unavailable = [&](const char *what, cudaError_t e) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    loop_unavailable = true;
+    if (getenv("GMG_VERBOSE")) fprintf(stderr, "ls: device loop unavailable (%s: %s)\n", what, cudaGetErrorString(e));
+    return 0;
+  };
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return unavailable("handle", e);
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p);
+  if (e != cudaSuccess) return unavailable("conditional node", e);
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(mg->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return unavailable("capture", e);
+  const long long before = mg->launches;
+  int err = 0;
+  norm_to_host = false;
+  int rc = iteration(level, xv, bv, Am, &err);
+  norm_to_host = true;
+  if (!rc) rc = k_ls_loop_test(mg, loop_dev, h);
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(mg->stream, &captured);
+  loop_kernels = mg->launches - before;
+  mg->launches = before;
+  // the same iteration ran eagerly before: a failure here is the capture's
+  if (rc) return unavailable("capture of the iteration", cudaErrorStreamCaptureUnsupported);
+  if (e != cudaSuccess) return unavailable("end capture", e);
+  e = cudaGraphInstantiate(&loop_graph, g, 0);
+  if (e != cudaSuccess) {
+    loop_graph = nullptr;
+    return unavailable("instantiate", e);
+  }
+  cudaGraphDestroy(g);
+  graph_level = level; graph_x = xv; graph_b = bv; graph_epoch = mg->graph_epoch;
+  return 0;
+}
+
+int NPLs::device_loop(int i0, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double *abs_,
+                      const double *reach, gmg_lresult *lr) {
+  const int s = mg->lev[level].s;
+  if (!loop_graph) {
+    if (build_loop(level, xv, bv, Am)) return 1;
+    if (!loop_graph) {  // not available on this system: the host loop from iteration i0
+      int i;
+      for (i = i0; i < maxiter; ++i) {
+        if (step(i, level, xv, bv, Am, lr) || check_iteration(i)) return 1;
+        for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
+        for (int r = 0; r < s; ++r)
+          GMG_CHECK(std::isfinite(lr->last_defect[r]), "ls: defect is not finite in iteration %d", i + 1);
+        if (sc_cmp(lr->last_defect, abs_, s) || sc_cmp(lr->last_defect, reach, s)) {
+          lr->converged = 1;
+          lr->number_of_linear_iterations = i + 1;
+          return 0;
+        }
+      }
+      lr->number_of_linear_iterations = i;
+      return 0;
+    }
+  }
+  LsLoopState &st = *loop_host;
+  st = LsLoopState();
+  st.it = i0;
+  st.maxit = maxiter;
+  st.s = s;
+  for (int r = 0; r < s; ++r) {
+    st.abs[r] = abs_[r];
+    st.reach[r] = reach[r];
+    st.last[r] = lr->last_defect[r];
+  }
+  GMG_CUDA(cudaMemcpyAsync(loop_dev, loop_host, sizeof(LsLoopState), cudaMemcpyHostToDevice, mg->stream));
+  GMG_CUDA(cudaGraphLaunch(loop_graph, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(loop_host, loop_dev, sizeof(LsLoopState), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  mg->launches += (st.it - i0) * loop_kernels;
+  for (int r = 0; r < s; ++r) lr->last_defect[r] = st.last[r];
+  GMG_CHECK(st.bad == 0, "ls: defect is not finite in iteration %d", st.bad);
+  lr->converged = st.conv;
+  lr->number_of_linear_iterations = st.it;
   return 0;
 }
 

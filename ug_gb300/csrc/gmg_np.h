@@ -181,6 +181,19 @@ struct NPLs : NPLinearSolver {
   gmg_vec *graph_x = nullptr, *graph_b = nullptr;
   long long graph_kernels = 0;  // kernels per replay (for the launch counter)
   long long graph_epoch = 0;    // mg->graph_epoch when captured
+  // the loop after the first iteration as one graph: a conditional WHILE node
+  // whose body is the iteration plus the device-side test (k_ls_loop_test);
+  // $dloop 0 keeps the host loop
+  int use_device_loop = 1;
+  bool loop_unavailable = false;  // the conditional graph failed to build: host loop
+  bool norm_to_host = true;       // iteration() copies the norms to norms_host
+  cudaGraphExec_t loop_graph = nullptr;
+  long long loop_kernels = 0;     // kernels per pass of the body, the test included
+  LsLoopState *loop_dev = nullptr, *loop_host = nullptr;
+  int build_loop(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A);
+  // iterations i0+1.. of Solver on the device; fills lr like the host loop
+  int device_loop(int i0, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
+                  const double *reach, gmg_lresult *lr);
   ~NPLs() override;
   int Init(const Args &a) override;
   int PreProcess(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result) override;
