@@ -310,6 +310,30 @@ int gmg_lgen_rhs(gmg_lgen *g, const double **rhs, long long *len);
 int gmg_lgen_coords(gmg_lgen *g, int level, const double **xyz);
 int gmg_lgen_destroy(gmg_lgen *g);
 
+/* ---- orderings: UG's order numprocs on a flattened level ----------------
+ * UG orders a level's VECTOR list with its order numprocs (np/procs/order.cc:
+ * order.lex, order.bw) before solving; Gauss-Seidel and ILU then visit the
+ * rows in list order.  A hierarchy flattened from UG after that ordering is
+ * already in the new order (GMG_ORDER_LIST follows it).  These functions
+ * compute the same orders on a gmg_level_desc on the host, before
+ * gmg_mg_create: perm[i] = the current index of the vector that goes to
+ * position i.  The caller renumbers the level's rows and columns, P's rows on
+ * this level and P's columns on the next finer level (ug_gb300.permute_levels).
+ * Host work only; no device is touched. */
+
+/* order.bw (OrderBW, order.cc:343): two breadth-first sweeps over the
+ * matrix graph, the second from the vector the first reached last; entries
+ * of a row in stored order.  Fails if the graph is not connected (UG
+ * asserts).  bandwidth (may be NULL) = max |i - j| in the new numbering. */
+int gmg_order_bw(const gmg_level_desc *level, int *perm, int *bandwidth);
+/* order.lex $config <config> (OrderLex, order.cc:287 -> LexOrderVectorsInGrid,
+ * gm/algebra.cc:4699): sort by position, config one letter per dimension
+ * (r/l x, u/d y, f/b z; + / - direction; the last letter most significant),
+ * coordinates xyz[i * xyz_stride + d], differences scaled by inv_mesh_size
+ * (UG: 2^level * NN(level 0)^(1/dim) / domain radius) and equal within 1e-3. */
+int gmg_order_lex(const gmg_level_desc *level, int dim, const double *xyz, int xyz_stride, const char *config,
+                  double inv_mesh_size, int *perm);
+
 #ifdef __cplusplus
 }
 #endif

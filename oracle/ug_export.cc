@@ -56,6 +56,7 @@
 #include "ls.h"
 #include "np.h"
 #include "numproc.h"
+#include "order.h"
 #include "shapes.h"
 #include "std_domain.h"
 #include "transfer.h"
@@ -180,7 +181,7 @@ static MATRIX *mat_of(VECTOR *a, VECTOR *b) {
 
 int main(int argc, char **argv) {
   if (argc < 7) {
-    fprintf(stderr, "usage: %s problem nref baselevel smoother seed out [maxit]\n", argv[0]);
+    fprintf(stderr, "usage: %s problem nref baselevel smoother seed out [maxit] [nloc] [order]\n", argv[0]);
     return 2;
   }
   std::string problem = argv[1];
@@ -190,6 +191,10 @@ int main(int argc, char **argv) {
   const char *outfile = argv[6];
   int maxit = argc > 7 ? atoi(argv[7]) : 100;
   int nloc = argc > 8 ? atoi(argv[8]) : 0;
+  // UG's ordering numprocs (order.cc:931) applied to every level after the
+  // assembly: "bw" (order.bw) or "lex:<config>" (order.lex $config <config>)
+  std::string order = argc > 9 ? argv[9] : "none";
+  char cmd[512];
   int ug_argc = 1;
   char *ug_argv0 = argv[0];
   char **ug_argv = &ug_argv0;
@@ -341,6 +346,23 @@ int main(int argc, char **argv) {
     }
   }
 
+  if (order != "none") {
+    if (order == "bw") {
+      run("npcreate ord $c bw; npinit ord;");
+    } else if (order.compare(0, 4, "lex:") == 0) {
+      snprintf(cmd, sizeof cmd, "npcreate ord $c lex; npinit ord $config %s;", order.c_str() + 4);
+      run(cmd);
+    } else {
+      fprintf(stderr, "unknown order %s\n", order.c_str());
+      return 2;
+    }
+    NP_ORDER *ord = (NP_ORDER *)GetNumProcByName(mg, "ord", ORDER_CLASS_NAME);
+    if (!ord) { fprintf(stderr, "no order numproc\n"); return 1; }
+    for (int l = 0; l <= top; ++l) {
+      INT res = 0;
+      if ((*ord->Order)(ord, l, NULL, &res)) { fprintf(stderr, "order failed on level %d\n", l); return 1; }
+    }
+  }
   index_levels(mg);
   for (int l = 0; l <= top; ++l) {  // element census per level: corners, refinement class
     int cnt[5][4] = {{0}};
@@ -356,6 +378,7 @@ int main(int argc, char **argv) {
   put1i("fullrefinelevel", FULLREFINELEVEL(mg));
   put("problem", 's', problem.c_str(), (int64_t)problem.size());
   put("smoother", 's', smoother.c_str(), (int64_t)smoother.size());
+  put("order", 's', order.c_str(), (int64_t)order.size());
 
   // ---- hierarchy
   for (int l = 0; l <= top; ++l) {
@@ -506,7 +529,6 @@ int main(int argc, char **argv) {
   else run("npcreate smooth $c ilu; npinit smooth;");
   run("npcreate base $c ex; npinit base;");
   run("npcreate basesolver $c ls; npinit basesolver $red 1e-14 $m 1 $I base;");
-  char cmd[512];
   snprintf(cmd, sizeof cmd, "npcreate lmgc $c lmgc; npinit lmgc $S smooth smooth basesolver $T transfer $n1 2 $n2 2 $b %d;", baselevel);
   run(cmd);
   snprintf(cmd, sizeof cmd, "npcreate mgs $c ls; npinit mgs $A MAT $x sol $b rhs $red 1e-10 $abslimit 1e-50 $m %d $I lmgc;", maxit);

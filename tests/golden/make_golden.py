@@ -12,7 +12,10 @@ are locally refined: the L-shaped elasticity problem, uniformly refined
 surface flags (FINE_GRID_DOF, NEW_DEFECT, FULLREFINELEVEL) and the solution on
 every level.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]
+
+The ``*bw*`` / ``*lex*`` cases repeat a case above after one of UG's order
+numprocs renumbered every level (its GS / ILU then sweep in the new order).
 """
 import os
 import subprocess
@@ -26,7 +29,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 
-# name: (dimension, problem, nref, baselevel, smoother, seed[, nloc])
+# name: (dimension, problem, nref, baselevel, smoother, seed[, nloc[, order]]);
+# order = one of UG's order numprocs run on every level after the assembly
+# ("bw" = order.bw, "lex:<config>" = order.lex $config <config>)
 CASES = {
     "q1_jac": (2, "poisson", 5, 2, "jac", 11),
     "q1_gs": (2, "poisson", 5, 2, "gs", 11),
@@ -41,19 +46,28 @@ CASES = {
     "ls_jac": (2, "lshape", 2, 0, "jac", 22, 6),
     "ls_gs": (2, "lshape", 2, 0, "gs", 22, 6),
     "ls_ilu": (2, "lshape", 2, 0, "ilu", 22, 6),
+    "q1bw_gs": (2, "poisson", 5, 2, "gs", 11, 0, "bw"),
+    "q1lex_ilu": (2, "poisson", 5, 2, "ilu", 11, 0, "lex:ur"),
+    "p1lex_gs": (3, "poisson", 3, 0, "gs", 12, 0, "lex:dfl"),
+    "elbw_ilu": (2, "elasticity", 4, 1, "ilu", 14, 0, "bw"),
+    "ls_bw_gs": (2, "lshape", 2, 0, "gs", 22, 6, "bw"),
 }
 
 
 def main():
     env = dict(os.environ)
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"], check=True, env=env)
+    only = set(sys.argv[1:])  # optional: the names to regenerate
     with tempfile.TemporaryDirectory() as tmp:
         for name, (dim, problem, nref, base, sm, seed, *rest) in CASES.items():
+            if only and name not in only:
+                continue
             exe = os.path.join(ROOT, "oracle", "_ref", f"ug_export{dim}d")
             raw = os.path.join(tmp, name + ".bin")
             nloc = rest[0] if rest else 0
-            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw, "100", str(nloc)], check=True,
-                           stdout=subprocess.DEVNULL)
+            order = rest[1] if len(rest) > 1 else "none"
+            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw, "100", str(nloc), order],
+                           check=True, stdout=subprocess.DEVNULL)
             fx = oracle.read_ugfx(raw)
             arrays = {k: (np.array(v) if not isinstance(v, str) else np.array(v)) for k, v in fx.items()}
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)

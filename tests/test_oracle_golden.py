@@ -64,7 +64,9 @@ def test_cg_matches_ug(name, oracle_mod):
                                    damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50)
     assert conv == bool(fx["cg_converged"][0]) and it == int(fx["cg_iters"][0])
     assert rel(x, fx["cg_x"]) <= 1e-12
-    assert rel(hist[-1], fx["cg_last"]) <= 1e-10
+    # the last defect sits near the rounding level of the first one (~1e-12 of
+    # it); its summation order differs, so it is compared on that scale
+    assert np.all(np.abs(np.asarray(hist[-1]) - fx["cg_last"]) <= 1e-12 * fx["cg_first"])
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -79,7 +81,9 @@ def test_bcgs_matches_ug(name, oracle_mod):
                                      damp=0.8 if sm == "jac" else 1.0, red=1e-10, abslimit=1e-50)
     assert conv == bool(fx["bcgs_converged"][0]) and it == int(fx["bcgs_iters"][0])
     assert rel(x, fx["bcgs_x"]) <= 1e-12
-    assert rel(hist[-1], fx["bcgs_last"]) <= 1e-10
+    # the last defect sits near the rounding level of the first one (~1e-12 of
+    # it); its summation order differs, so it is compared on that scale
+    assert np.all(np.abs(np.asarray(hist[-1]) - fx["bcgs_last"]) <= 1e-12 * fx["bcgs_first"])
 
 
 def _split(fx, flat):

@@ -1,0 +1,101 @@
+"""UG's ordering numprocs (np/procs/order.cc: order.bw, order.lex) on a
+flattened hierarchy, host side.
+
+The ``*bw*`` / ``*lex*`` fixtures are UG's own hierarchies after UG ran the
+order numproc on every level (tests/golden/make_golden.py).  gmg_order_bw /
+gmg_order_lex on the unordered fixture of the same case, applied with
+permute_levels, give exactly UG's reordered hierarchy: rows, columns and
+values of every level's matrix, the transfer weights, the vector classes,
+the positions and the right-hand side.  The solves on the reordered fixtures
+(UG's iteration counts in the new Gauss-Seidel / ILU order) are covered by
+the generic oracle and device parity tests over every fixture.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+# ordered fixture: (unordered fixture of the same case, domain radius of the
+# UG domain: unit square / cube 0.5, L-shape 1.0)
+ORDERED = {"q1bw_gs": ("q1_gs", 0.5), "q1lex_ilu": ("q1_ilu", 0.5), "p1lex_gs": ("p1_gs", 0.5),
+           "elbw_ilu": ("el_ilu", 0.5), "ls_bw_gs": ("ls_gs", 1.0)}
+KEYS = ("rowptr", "col", "val", "vclass", "vnclass", "skip", "prowptr", "pcol", "pw")
+
+
+@pytest.fixture(scope="module")
+def G():
+    import ug_gb300
+    ug_gb300.lib()
+    return ug_gb300
+
+
+def _xyz(fx, l):
+    return np.asarray(fx[f"L{l}_xyz"]).reshape(-1, 3)
+
+
+def _perms(G, fx, order, radius):
+    levels = G.levels_from_ugfx(fx)
+    dim = int(fx["dim"][0])
+    perms = []
+    for l, lev in enumerate(levels):
+        if order == "bw":
+            p, bw = G.order_bw(lev)
+            assert bw >= 0
+        else:
+            p = G.order_lex(lev, _xyz(fx, l)[:, :dim], order[4:], G.lex_inv_mesh_size(l, levels[0]["n"], dim, radius))
+        assert np.array_equal(np.sort(p), np.arange(lev["n"]))
+        perms.append(p)
+    return levels, perms
+
+
+@pytest.mark.parametrize("name", sorted(ORDERED))
+def test_order_reproduces_ug(G, name):
+    base_name, radius = ORDERED[name]
+    fx, base = load_golden(name), load_golden(base_name)
+    order = str(fx["order"])
+    assert order != "none" and str(base.get("order", "none")) == "none"
+    levels, perms = _perms(G, base, order, radius)
+    got = G.permute_levels(levels, perms)
+    want = G.levels_from_ugfx(fx)
+    s = int(fx["blocksize"][0])
+    for l, (a, b) in enumerate(zip(got, want)):
+        for k in KEYS:
+            if b.get(k) is not None:
+                assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), (name, l, k)
+        assert np.array_equal(_xyz(base, l)[perms[l]], _xyz(fx, l)), (name, l)
+        for k in ("fine_grid_dof", "new_defect"):
+            assert np.array_equal(np.asarray(base[f"L{l}_{k}"])[perms[l]], fx[f"L{l}_{k}"])
+    assert np.array_equal(G.permute_vector(base["rhs"], perms[-1], s), fx["rhs"])
+    offs = np.cumsum([0] + [lev["n"] * s for lev in levels])
+    rhs_all = np.concatenate([G.permute_vector(base["rhs_all"][offs[l]:offs[l + 1]], perms[l], s)
+                              for l in range(len(levels))])
+    assert np.array_equal(rhs_all, fx["rhs_all"])
+
+
+def test_order_bw_bandwidth(G):
+    """The bandwidth order.bw reports (order.cc:400-411) on UG's reordered
+    finest level: max |i - j| over its entries."""
+    fx = load_golden("q1bw_gs")
+    top = G.levels_from_ugfx(fx)[-1]
+    rp, col = np.asarray(top["rowptr"]), np.asarray(top["col"])
+    rows = np.repeat(np.arange(top["n"]), np.diff(rp))
+    levels, perms = _perms(G, load_golden("q1_gs"), "bw", 0.5)
+    _, bw = G.order_bw(levels[-1])
+    assert bw == int(np.max(np.abs(rows - col)))
+
+
+def test_order_errors(G):
+    """order.bw on a matrix graph that is not connected fails (UG asserts);
+    order.lex rejects configs that OrderLexInit rejects."""
+    lev = {"n": 4, "s": 1, "rowptr": np.array([0, 2, 4, 6, 8]), "col": np.array([0, 1, 1, 0, 2, 3, 3, 2]),
+           "val": np.ones(8), "vclass": np.full(4, 3), "vnclass": np.full(4, 3), "skip": np.zeros(4)}
+    with pytest.raises(G.GmgError, match="not connected"):
+        G.order_bw(lev)
+    xyz = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0]])
+    for bad in ("rx", "r", "ruf"):
+        with pytest.raises(G.GmgError):
+            G.order_lex(lev, xyz, bad, 1.0, dim=2)
+    # 'ru': x ascending within rows of equal y (the last letter is the major key)
+    assert G.order_lex(lev, xyz, "ru", 1.0).tolist() == [0, 1, 2, 3]
+    assert G.order_lex(lev, xyz, "ur", 1.0).tolist() == [0, 2, 1, 3]
+    assert G.order_lex(lev, xyz, "ld", 1.0).tolist() == [3, 2, 1, 0]

@@ -122,6 +122,7 @@ def lib(build_if_missing: bool = True):
         "gmg_lgen_rhs": ([P, P, P], I), "gmg_lgen_coords": ([P, I, P], I), "gmg_lgen_destroy": ([P], I),
         "gmg_gen_create": ([I, I, C.c_ulonglong, D, D, P], I), "gmg_gen_levels": ([P, P, P], I),
         "gmg_gen_rhs": ([P, P, P], I), "gmg_gen_coords": ([P, I, P], I), "gmg_gen_destroy": ([P], I),
+        "gmg_order_bw": ([P, P, P], I), "gmg_order_lex": ([P, I, P, I, C.c_char_p, D, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -278,6 +279,93 @@ def _desc_array(levels, keep: list):
                                 _ptr(dbl["pw"]))
     keep.append(desc_arr)
     return desc_arr, nl
+
+
+def order_bw(level: dict) -> tuple[np.ndarray, int]:
+    """UG's order.bw (np/procs/order.cc:343) on one level: (perm, bandwidth),
+    perm[i] = the current index of the vector placed at i (gmg_order_bw)."""
+    keep = []
+    desc, _ = _desc_array([level], keep)
+    perm = np.empty(int(level["n"]), np.int32)
+    bw = C.c_int(0)
+    if lib().gmg_order_bw(C.byref(desc[0]), _ptr(perm), C.byref(bw)):
+        _err("order bw")
+    return perm, bw.value
+
+
+def order_lex(level: dict, xyz, config: str, inv_mesh_size: float, dim: int | None = None) -> np.ndarray:
+    """UG's order.lex $config <config> (order.cc:287, LexOrderVectorsInGrid
+    gm/algebra.cc:4699) on one level; xyz one row of coordinates per vector
+    (gmg_order_lex)."""
+    keep = []
+    desc, _ = _desc_array([level], keep)
+    xyz = np.ascontiguousarray(np.asarray(xyz, np.float64).reshape(int(level["n"]), -1))
+    dim = len(config) if dim is None else dim
+    perm = np.empty(int(level["n"]), np.int32)
+    if lib().gmg_order_lex(C.byref(desc[0]), dim, _ptr(xyz), xyz.shape[1], config.encode(), float(inv_mesh_size),
+                           _ptr(perm)):
+        _err(f"order lex {config}")
+    return perm
+
+
+def lex_inv_mesh_size(level: int, n_level0: int, dim: int, radius: float) -> float:
+    """UG's scaling of position differences in LexOrderVectorsInGrid
+    (gm/algebra.cc:4721): 2^level * NN(level 0)^(1/dim) / radius."""
+    return float(2 ** level) * float(n_level0) ** (1.0 / dim) / radius
+
+
+def permute_vector(v, perm, s: int = 1) -> np.ndarray:
+    """A level vector (s components per row) in the order perm."""
+    return np.asarray(v).reshape(-1, s)[np.asarray(perm)].ravel()
+
+
+def permute_levels(levels: list[dict], perms: list) -> list[dict]:
+    """Level dicts renumbered by one permutation per level (None = keep):
+    rows and columns of A, the per-row classes, P's rows on the level and P's
+    columns on the next finer level.  Each row keeps its entries in stored
+    order (UG's order numprocs leave the matrix lists alone)."""
+    inv = []
+    for d, p in zip(levels, perms):
+        if p is None:
+            inv.append(None)
+            continue
+        p = np.asarray(p, np.int64)
+        q = np.empty_like(p)
+        q[p] = np.arange(p.size)
+        inv.append(q)
+
+    def rows(rowptr, col, vals, p, cmap, width):
+        rowptr = np.asarray(rowptr, np.int64)
+        col = np.asarray(col)
+        lens = np.diff(rowptr)
+        if p is not None:
+            lens = lens[p]
+        newptr = np.zeros(lens.size + 1, np.int64)
+        np.cumsum(lens, out=newptr[1:])
+        if p is None:
+            idx = np.arange(col.size)
+        else:
+            starts = rowptr[:-1][p]
+            idx = np.repeat(starts - newptr[:-1], lens) + np.arange(int(newptr[-1]))
+        newcol = col[idx]
+        if cmap is not None:
+            newcol = cmap[newcol]
+        newval = np.asarray(vals).reshape(col.size, width)[idx].ravel()
+        return newptr.astype(np.int32), newcol.astype(np.int32), newval
+
+    out = []
+    for l, d in enumerate(levels):
+        p, q = perms[l], inv[l]
+        s = int(d["s"])
+        e = dict(d)
+        e["rowptr"], e["col"], e["val"] = rows(d["rowptr"], d["col"], d["val"], p, q, s * s)
+        for k in ("vclass", "vnclass", "skip"):
+            if d.get(k) is not None and p is not None:
+                e[k] = np.asarray(d[k])[np.asarray(p)]
+        if d.get("prowptr") is not None:
+            e["prowptr"], e["pcol"], e["pw"] = rows(d["prowptr"], d["pcol"], d["pw"], p, inv[l - 1], 1)
+        out.append(e)
+    return out
 
 
 class MultiGrid:
