@@ -326,6 +326,29 @@ def test_device_loop_matches_host_loop(G, name, order, mixed, maxit):
         assert np.array_equal(xd, xh)
 
 
+@pytest.mark.parametrize("name,order", [("p1k_gs", 1), ("p1k_ilu", 0), ("q1_jac", 0), ("el_ilu", 0), ("el_gs", 1),
+                                        ("ls_gs", 0)])
+def test_coarse_narrow_team_is_bit_identical(G, name, order):
+    """The fused coarse cycle runs its smallest levels (at most ~4 rows per
+    lane group) with a team of 128 threads on a named barrier while the other
+    warps wait once ($narrow 1, the default).  Rows, lanes per row and the
+    summation order are those of the whole block, so the solve is identical
+    bit for bit to $narrow 0."""
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    sm = fx["smoother"]
+    out = []
+    for narrow in (True, False):
+        mg = G.MultiGrid(levels, order=order)
+        G.setup_lmgc(mg, sm, baselevel=int(fx["baselevel"][0]), damp=_damp(sm), red=1e-10, abslimit=1e-50,
+                     narrow=narrow)
+        out.append(mg.solve_host("mgs", fx["rhs_all"] if mg.local else fx["rhs"]))
+        mg.close()
+    (x1, l1), (x0, l0) = out
+    assert l1.converged and l1.iters == l0.iters
+    assert np.array_equal(x1, x0)
+
+
 def _bsr_apply(d, y):
     s = int(d["s"]); rp, col = np.asarray(d["rowptr"]), np.asarray(d["col"])
     val = np.asarray(d["val"]).reshape(-1, s, s)

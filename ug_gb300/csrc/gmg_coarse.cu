@@ -38,6 +38,7 @@ namespace {
 constexpr int MAXCL = 12;
 constexpr int CBLK = 1024;  // threads of the single-hierarchy cycle
 constexpr int BBLK = 256;   // threads per instance of the batched cycle
+constexpr int NARROW = 128; // threads of the team that runs the smallest levels
 
 // level description: byte offsets into the shared-memory image
 struct SLev {
@@ -54,6 +55,7 @@ struct SLev {
 struct SArgs {
   int nl, nu1, nu2, unit_damp, smem_bytes, image_bytes;
   int zero_top_c;     // batched: zero c on the top fused level first
+  int narrow;         // levels 0..narrow-1 run by the first NARROW threads (0: none)
   const int4 *image;  // static part, image_bytes (multiple of 16)
   double damp[GMG_MAX_S], cdamp[GMG_MAX_S], abslimit[GMG_MAX_S];
   int o_ainv, base_dim;
@@ -118,9 +120,17 @@ __device__ __forceinline__ void row_dot(const int *rowptr, const int *col, const
   for (int r = 0; r < S; ++r) s[r] = gsum<G>(s[r]);
 }
 
+// the threads running a phase: lanes / groups for the row loops, the team's
+// thread index and size for the element loops, and its barrier (0: the whole
+// block, __syncthreads; 1: the first nt threads only, a named barrier)
 struct Team {
-  int lane, grp, ngrp;
+  int lane, grp, ngrp, tid, nt, bar;
 };
+
+__device__ __forceinline__ void tsync(const Team &tm) {
+  if (tm.bar == 0) __syncthreads();
+  else asm volatile("bar.sync %0, %1;\n" ::"r"(tm.bar), "r"(tm.nt) : "memory");
+}
 
 // x -= A y ; acc += y (dmatmul_minus + dadd)
 template <class T, int S>
@@ -145,8 +155,8 @@ __device__ void c_spmv(const PL<T> &L, T *x, const T *y, T *acc, const Team &tm)
 
 // t = damp * D^{-1} b (l_jac + dscalx)
 template <class T, int S>
-__device__ void c_jac(const PL<T> &L, const SArgs &a) {
-  for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+__device__ void c_jac(const PL<T> &L, const SArgs &a, const Team &tm) {
+  for (int i = tm.tid; i < L.n; i += tm.nt) {
     if (!L.all_active && !(L.flags[i] & F_ACTIVE)) {
 #pragma unroll
       for (int r = 0; r < S; ++r) L.t[i * S + r] = T(0);
@@ -190,7 +200,7 @@ __device__ void c_gs(const PL<T> &L, const Team &tm) {
         }
       }
     }
-    __syncthreads();
+    tsync(tm);
   }
 }
 
@@ -213,7 +223,7 @@ __device__ void c_ilu(const PL<T> &L, const Team &tm) {
 #pragma unroll
         for (int r = 0; r < S; ++r) L.t[i * S + r] = act ? L.b[i * S + r] - s[r] : T(0);
     }
-    __syncthreads();
+    tsync(tm);
   }
   for (int w = 0; w < L.nuwave; ++w) {
     const int r0 = L.uptr[w], r1 = L.uptr[w + 1];
@@ -239,7 +249,7 @@ __device__ void c_ilu(const PL<T> &L, const Team &tm) {
         }
       }
     }
-    __syncthreads();
+    tsync(tm);
   }
 }
 
@@ -247,26 +257,26 @@ __device__ void c_ilu(const PL<T> &L, const Team &tm) {
 template <class T, int S, int SMO>
 __device__ void c_smooth(const PL<T> &L, const SArgs &a, const Team &tm) {
   if (SMO == 0) {
-    c_jac<T, S>(L, a);
-    __syncthreads();
+    c_jac<T, S>(L, a, tm);
+    tsync(tm);
   } else {
     if (SMO == 1) c_gs<T, S>(L, tm);
     else c_ilu<T, S>(L, tm);
     if (!a.unit_damp) {
-      for (int i = threadIdx.x; i < L.n; i += blockDim.x)
+      for (int i = tm.tid; i < L.n; i += tm.nt)
 #pragma unroll
         for (int r = 0; r < S; ++r) L.t[i * S + r] *= T(a.damp[r]);
-      __syncthreads();
+      tsync(tm);
     }
   }
   c_spmv<T, S>(L, L.b, L.t, L.c, tm);
-  __syncthreads();
+  tsync(tm);
 }
 
 // StandardRestrict into the level below, fused with lmgc's dset(c_{l-1}, 0)
 template <class T, int S>
-__device__ void c_restrict(const PL<T> &F, const PL<T> &Cl) {
-  for (int c = threadIdx.x; c < Cl.n; c += blockDim.x) {
+__device__ void c_restrict(const PL<T> &F, const PL<T> &Cl, const Team &tm) {
+  for (int c = tm.tid; c < Cl.n; c += tm.nt) {
     const bool reset = Cl.flags[c] & F_RESET;
     const int sk = Cl.skip[c];
     T acc[S];
@@ -289,8 +299,8 @@ __device__ void c_restrict(const PL<T> &F, const PL<T> &Cl) {
 
 // StandardInterpolateCorrection into t, fused with lmgc's dadd(c, t)
 template <class T, int S>
-__device__ void c_interp(const PL<T> &F, const PL<T> &Cl, const SArgs &a) {
-  for (int f = threadIdx.x; f < F.n; f += blockDim.x) {
+__device__ void c_interp(const PL<T> &F, const PL<T> &Cl, const SArgs &a, const Team &tm) {
+  for (int f = tm.tid; f < F.n; f += tm.nt) {
     const int sk = F.skip[f];
     T v[S];
 #pragma unroll
@@ -322,7 +332,7 @@ __device__ void c_base(const PL<T> &B, const SArgs &a, const double *ainv, const
   double acc[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) acc[r] = 0.0;
-  for (int i = threadIdx.x; i < B.n; i += blockDim.x)
+  for (int i = tm.tid; i < B.n; i += tm.nt)
 #pragma unroll
     for (int r = 0; r < S; ++r) {
       double v = double(B.b[i * S + r]);
@@ -332,29 +342,29 @@ __device__ void c_base(const PL<T> &B, const SArgs &a, const double *ainv, const
   for (int r = 0; r < S; ++r) {
     double v = acc[r];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((threadIdx.x & 31) == 0) red[r][threadIdx.x >> 5] = v;
+    if ((tm.tid & 31) == 0) red[r][tm.tid >> 5] = v;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  tsync(tm);
+  if (tm.tid == 0) {
     int below = 1;
     for (int r = 0; r < S; ++r) {
       double v = 0.0;
-      for (int w = 0; w < (int)(blockDim.x / 32); ++w) v += red[r][w];
+      for (int w = 0; w < (int)(tm.nt / 32); ++w) v += red[r][w];
       if (fabs(sqrt(v)) >= fabs(a.abslimit[r])) below = 0;
     }
     skip = below;
   }
-  __syncthreads();
+  tsync(tm);
   if (skip) return;
   const int N = B.n * S;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  for (int i = tm.tid; i < N; i += tm.nt) {
     double v = 0.0;
     for (int j = 0; j < N; ++j) v = fma(ainv[i * N + j], double(B.b[j]), v);
     B.t[i] = T(v);
   }
-  __syncthreads();
+  tsync(tm);
   c_spmv<T, S>(B, B.b, B.t, B.c, tm);
-  __syncthreads();
+  tsync(tm);
 }
 
 // the cycle over the fused levels, shared memory `sm` holding a's image
@@ -390,24 +400,41 @@ __device__ void cycle_body(const SArgs &a, char *sm) {
   }
   __syncthreads();
   constexpr int G = GL<S>::G;
-  Team tm{int(threadIdx.x & (G - 1)), int(threadIdx.x / G), int(blockDim.x / G)};
-  // down: pre-smoothing and restriction
-  for (int k = a.nl - 1; k >= 1; --k) {
+  const Team wide{int(threadIdx.x & (G - 1)), int(threadIdx.x / G), int(blockDim.x / G), int(threadIdx.x),
+                  int(blockDim.x), 0};
+  // the bottom levels 0..nn-1 (a few rows each) belong to a team of the first
+  // NARROW threads with its own barrier: the other warps skip their phases
+  // instead of passing ~25 block-wide barriers per level with nothing to do
+  const int nn = a.narrow;
+  const Team nar{int(threadIdx.x & (G - 1)), int(threadIdx.x / G), NARROW / G, int(threadIdx.x), NARROW, 1};
+  auto down = [&](int k, const Team &tm) {  // pre-smoothing and restriction
     const PL<T> L = make_pl<T>(a.L[k], sm);
     for (int it = 0; it < a.nu1; ++it) c_smooth<T, S, SMO>(L, a, tm);
-    c_restrict<T, S>(L, make_pl<T>(a.L[k - 1], sm));
-    __syncthreads();
-  }
-  c_base<T, S>(make_pl<T>(a.L[0], sm), a, reinterpret_cast<const double *>(sm + a.o_ainv), tm);
-  // up: interpolation, coarse-grid correction, post-smoothing
-  for (int k = 1; k < a.nl; ++k) {
+    c_restrict<T, S>(L, make_pl<T>(a.L[k - 1], sm), tm);
+    tsync(tm);
+  };
+  auto up = [&](int k, const Team &tm) {  // interpolation, coarse-grid correction, post-smoothing
     const PL<T> L = make_pl<T>(a.L[k], sm);
-    c_interp<T, S>(L, make_pl<T>(a.L[k - 1], sm), a);
-    __syncthreads();
+    c_interp<T, S>(L, make_pl<T>(a.L[k - 1], sm), a, tm);
+    tsync(tm);
     c_spmv<T, S>(L, L.b, L.t, nullptr, tm);
-    __syncthreads();
+    tsync(tm);
     for (int it = 0; it < a.nu2; ++it) c_smooth<T, S, SMO>(L, a, tm);
+  };
+  const double *ainv = reinterpret_cast<const double *>(sm + a.o_ainv);
+  const int k0 = nn > 1 ? nn : 1;  // lowest level visited by the whole block
+  for (int k = a.nl - 1; k >= k0; --k) down(k, wide);
+  if (nn > 0) {
+    if (threadIdx.x < NARROW) {
+      for (int k = nn - 1; k >= 1; --k) down(k, nar);
+      c_base<T, S>(make_pl<T>(a.L[0], sm), a, ainv, nar);
+      for (int k = 1; k < nn; ++k) up(k, nar);
+    }
+    __syncthreads();
+  } else {
+    c_base<T, S>(make_pl<T>(a.L[0], sm), a, ainv, wide);
   }
+  for (int k = k0; k < a.nl; ++k) up(k, wide);
   // write back b and c of every fused level
   for (int k = 0; k < a.nl; ++k) {
     const SLev &s = a.L[k];
@@ -706,6 +733,12 @@ static int make_single(gmg_mg *mg, int bl, int lc, int smo, CachedImage &e) {
   }
   std::vector<char> img;
   if (build_image<T>(mg, bl, nl, smo, LH, sub, false, -1, e.args, img, &e.smem)) return 1;
+  {  // the narrow team takes the levels from the base up with at most ~4 rows per lane group
+    const int G = mg->lev[bl].s == 1 ? 4 : 2;
+    int nn = 0;
+    while (nn < nl && e.args.L[nn].n <= 4 * (NARROW / G)) ++nn;
+    e.args.narrow = nn;
+  }
   GMG_CHECK(e.smem <= 227 * 1024, "fused coarse cycle needs %d bytes of shared memory", e.smem);
   GMG_CUDA(cudaMalloc(&e.dev, img.size()));
   GMG_CUDA(cudaMemcpy(e.dev, img.data(), img.size(), cudaMemcpyHostToDevice));
@@ -902,6 +935,7 @@ int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_v
     return 0;
   }
   SArgs a = ci->args;
+  if (!cfg.narrow) a.narrow = 0;
   a.nu1 = cfg.nu1;
   a.nu2 = cfg.nu2;
   a.unit_damp = unit;

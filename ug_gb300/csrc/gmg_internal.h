@@ -375,6 +375,7 @@ int k_bcgs_xb(gmg_mg *mg, long long len, double *x, const double *q, double *b, 
 // the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
 struct CoarseCfg {
   int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;
+  int narrow = 1;  // the smallest levels by a narrow team of threads (0: the whole block)
   double damp[GMG_MAX_S], cdamp[GMG_MAX_S], abslimit[GMG_MAX_S];
 };
 int k_coarse_cycle(gmg_mg *mg, int prec, const CoarseCfg &cfg, gmg_vec *c, gmg_vec *b, gmg_vec *t);

@@ -752,6 +752,7 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
   }
   if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 6000;
   if (!a.get_int("cluster", &cluster)) cluster = 16;
+  if (!a.get_int("narrow", &narrow)) narrow = 1;
   int bs = 0;
   batch_smem = a.get_int("bsmem", &bs) ? bs : BATCH_COARSE_SMEM_BUDGET;
   if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return NP_NOT_ACTIVE;
@@ -834,7 +835,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
     // this level and everything below it: one cluster kernel
     CoarseCfg cfg;
     cfg.bl = baselevel; cfg.lc = level; cfg.smoother = smo;
-    cfg.nu1 = nu1; cfg.nu2 = nu2; cfg.cluster = cluster;
+    cfg.nu1 = nu1; cfg.nu2 = nu2; cfg.cluster = cluster; cfg.narrow = narrow;
     const NPSmoother *sm = static_cast<const NPSmoother *>(PreSmooth);
     for (int r = 0; r < GMG_MAX_S; ++r) {
       cfg.damp[r] = sm->damp[r];

@@ -136,6 +136,7 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   // levels with at most fuse_rows VECTORs run as one fused cluster kernel
   // (gmg_coarse.cu); 0 disables.  cluster = CTAs of that kernel's cluster.
   int fuse_rows = 6000, cluster = 16;
+  int narrow = 1;  // $narrow 0: the fused cycle runs its smallest levels with the whole block
   // batched hierarchies: the fused cycle runs one block per instance, over
   // the levels whose largest instance image fits batch_smem bytes ($bsmem; 0 disables)
   long long batch_smem = BATCH_COARSE_SMEM_BUDGET;
