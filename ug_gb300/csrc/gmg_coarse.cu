@@ -139,15 +139,24 @@ __device__ void c_spmv(const PL<T> &L, T *x, const T *y, T *acc, const Team &tm)
   for (int base = 0; base < L.n; base += tm.ngrp) {
     const int i = base + tm.grp;
     const bool valid = i < L.n;
+    const bool own = valid && tm.lane == 0;
+    // the row's own entries first: they do not wait for the gathers
+    T xi[S], yi[S], ai[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+      xi[r] = own ? x[i * S + r] : T(0);
+      yi[r] = own && acc ? y[i * S + r] : T(0);
+      ai[r] = own && acc ? acc[i * S + r] : T(0);
+    }
     T s[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) s[r] = T(0);
     row_dot<T, S, G, false>(L.rowptr, L.col, L.val, y, i, 0, tm.lane, valid, s);
-    if (valid && tm.lane == 0) {
+    if (own) {
 #pragma unroll
       for (int r = 0; r < S; ++r) {
-        x[i * S + r] -= s[r];
-        if (acc) acc[i * S + r] += y[i * S + r];
+        x[i * S + r] = xi[r] - s[r];
+        if (acc) acc[i * S + r] = ai[r] + yi[r];
       }
     }
   }
@@ -183,19 +192,26 @@ __device__ void c_gs(const PL<T> &L, const Team &tm) {
       const bool valid = q < r1;
       const int i = valid ? L.wrows[q] : 0;
       const bool act = valid && (L.all_active || (L.flags[i] & F_ACTIVE));
+      const bool own = valid && tm.lane == 0;
+      // b and the inverse diagonal of the row before the gathers
+      T bi[S], di[S * S];
+#pragma unroll
+      for (int r = 0; r < S; ++r) bi[r] = own ? L.b[i * S + r] : T(0);
+#pragma unroll
+      for (int k = 0; k < S * S; ++k) di[k] = own ? L.dinv[i * S * S + k] : T(0);
       T s[S];
 #pragma unroll
       for (int r = 0; r < S; ++r) s[r] = T(0);
       row_dot<T, S, G, true>(L.rowptr, L.col, L.val, L.t, i, 1, tm.lane, act, s);
-      if (valid && tm.lane == 0) {
+      if (own) {
         T rhs[S];
 #pragma unroll
-        for (int r = 0; r < S; ++r) rhs[r] = L.b[i * S + r] - s[r];
+        for (int r = 0; r < S; ++r) rhs[r] = bi[r] - s[r];
 #pragma unroll
         for (int r = 0; r < S; ++r) {
           T v = T(0);
 #pragma unroll
-          for (int c = 0; c < S; ++c) v = fma(L.dinv[i * S * S + r * S + c], rhs[c], v);
+          for (int c = 0; c < S; ++c) v = fma(di[r * S + c], rhs[c], v);
           L.t[i * S + r] = act ? v : T(0);
         }
       }
