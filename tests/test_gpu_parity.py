@@ -85,7 +85,7 @@ def test_kernels_match_ug(G, oracle_mod, name, order):
 @pytest.mark.parametrize("name", NAMES)
 def test_solve_matches_ug(G, name, fuse):
     """fuse=0: one kernel per level operation; None: the small levels run as
-    one fused cluster kernel (here the whole hierarchy)."""
+    one fused single-CTA kernel (here the whole hierarchy)."""
     fx = load_golden(name)
     mg, _ = _setup(G, fx, 0)
     sm = fx["smoother"]

@@ -372,9 +372,9 @@ int k_bcgs_xs(gmg_mg *mg, long long len, double *x, const double *q, const doubl
 int k_bcgs_half_test(gmg_mg *mg, int s, const double *th, double *sc);
 int k_bcgs_xb(gmg_mg *mg, long long len, double *x, const double *q, double *b, const double *sv, const double *tn,
               const double *sc);
-// the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one cluster launch
+// the whole lmgc V-cycle (gamma = 1) over levels bl..lc in one launch of one CTA
 struct CoarseCfg {
-  int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1, cluster = 16;
+  int bl = 0, lc = 0, smoother = 0, nu1 = 1, nu2 = 1;
   int narrow = 1;  // the smallest levels by a narrow team of threads (0: the whole block)
   double damp[GMG_MAX_S], cdamp[GMG_MAX_S], abslimit[GMG_MAX_S];
 };

@@ -751,7 +751,6 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
     baselevel = i;
   }
   if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 6000;
-  if (!a.get_int("cluster", &cluster)) cluster = 16;
   if (!a.get_int("narrow", &narrow)) narrow = 1;
   int bs = 0;
   batch_smem = a.get_int("bsmem", &bs) ? bs : BATCH_COARSE_SMEM_BUDGET;
@@ -766,7 +765,7 @@ std::string NPLmgc::Display() const {
   std::ostringstream o;
   o << NPIter::Display() << "g = " << gamma << "\nn1 = " << nu1 << "\nn2 = " << nu2 << "\nbaselevel = " << baselevel
     << "\nfuse = " << fuse_rows << " (" << (fusable_smoother() >= 0 ? "fused coarse cycle" : "not fusable")
-    << ")\ncluster = " << cluster
+    << ")\nnarrow = " << narrow
     << "\nT = " << (Transfer ? Transfer->name : "---") << "\npre = " << (PreSmooth ? PreSmooth->name : "---")
     << "\npost = " << (PostSmooth ? PostSmooth->name : "---") << "\nbase = " << (BaseSolver ? BaseSolver->name : "---")
     << "\n";
@@ -832,10 +831,10 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   GMG_CHECK(t, "lmgc: temporary vector");
   const int smo = fusable_smoother();
   if (smo >= 0 && fuse_here(level, prec, smo)) {
-    // this level and everything below it: one cluster kernel
+    // this level and everything below it: one fused kernel (a single CTA)
     CoarseCfg cfg;
     cfg.bl = baselevel; cfg.lc = level; cfg.smoother = smo;
-    cfg.nu1 = nu1; cfg.nu2 = nu2; cfg.cluster = cluster; cfg.narrow = narrow;
+    cfg.nu1 = nu1; cfg.nu2 = nu2; cfg.narrow = narrow;
     const NPSmoother *sm = static_cast<const NPSmoother *>(PreSmooth);
     for (int r = 0; r < GMG_MAX_S; ++r) {
       cfg.damp[r] = sm->damp[r];

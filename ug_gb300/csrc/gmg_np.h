@@ -133,9 +133,9 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   NPLinearSolver *BaseSolver = nullptr;
   double damp[GMG_MAX_S];
   gmg_vec *t64 = nullptr, *t32 = nullptr;  // the temporary t of Lmgc (AllocVDFromVD)
-  // levels with at most fuse_rows VECTORs run as one fused cluster kernel
-  // (gmg_coarse.cu); 0 disables.  cluster = CTAs of that kernel's cluster.
-  int fuse_rows = 6000, cluster = 16;
+  // levels with at most fuse_rows VECTORs run as one fused kernel of one CTA
+  // (gmg_coarse.cu); 0 disables
+  int fuse_rows = 6000;
   int narrow = 1;  // $narrow 0: the fused cycle runs its smallest levels with the whole block
   // batched hierarchies: the fused cycle runs one block per instance, over
   // the levels whose largest instance image fits batch_smem bytes ($bsmem; 0 disables)
