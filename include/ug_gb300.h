@@ -310,6 +310,17 @@ int gmg_lgen_rhs(gmg_lgen *g, const double **rhs, long long *len);
 int gmg_lgen_coords(gmg_lgen *g, int level, const double **xyz);
 int gmg_lgen_destroy(gmg_lgen *g);
 
+/* ---- adaptation: incremental re-flattening ------------------------------
+ * After AdaptMultiGrid changed the levels from_level.. (their structure,
+ * values or vector classes), replace exactly those: levels[k] describes the
+ * new level from_level + k (count levels, so the top may move), flattened as
+ * for gmg_mg_create; the levels below from_level must be unchanged (VNCLASS of
+ * a level depends on the level above it: a level whose classes changed is
+ * part of the replaced range).  Kept levels keep their device arrays, factors
+ * and vector values; vectors start at zero on the new levels; numprocs redo
+ * their PreProcess at the next solve.  Not on batched hierarchies. */
+int gmg_mg_replace_levels(gmg_mg *mg, int from_level, const gmg_level_desc *levels, int count);
+
 /* ---- orderings: UG's order numprocs on a flattened level ----------------
  * UG orders a level's VECTOR list with its order numprocs (np/procs/order.cc:
  * order.lex, order.bw) before solving; Gauss-Seidel and ILU then visit the

@@ -237,3 +237,70 @@ def test_generated_local_krylov_vs_oracle(G, oracle_mod, solver):
     assert conv and lr.converged and abs(lr.iters - ito) <= 1
     assert rel(x, np.concatenate(xr)) <= 1e-8
     mg.close()
+
+
+def _same_level(a, b):
+    for k in ("n", "rowptr", "col", "val", "vclass", "vnclass", "skip", "prowptr", "pcol", "pw"):
+        x, y = a.get(k), b.get(k)
+        if (x is None) != (y is None) or (x is not None and not np.array_equal(np.asarray(x), np.asarray(y))):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("order,sm", [(0, "gs"), (1, "gs"), (2, "ilu"), (0, "ilu")])
+@pytest.mark.parametrize("nuni,nloc", [(3, 3), (2, 6)])
+def test_replace_levels_after_adaptation(G, nuni, nloc, order, sm):
+    """Incremental re-flattening: one more local refinement step toward the
+    corner changes the old top level (its VNCLASS) and adds a level above it;
+    gmg_mg_replace_levels swaps in exactly those levels on a hierarchy that
+    has already solved (ILU factors, fused images, captured loop built).  The
+    next solve of the refined problem equals, bit for bit, the solve on a
+    hierarchy created from scratch for it, and the kept levels' arrays are
+    untouched."""
+    a = G.LocalGenerator(nuni, nloc, seed=5)
+    b = G.LocalGenerator(nuni, nloc + 1, seed=5)
+    la = [a.level(l) for l in range(a.nlevels)]
+    lb = [b.level(l) for l in range(b.nlevels)]
+    first = next(l for l in range(len(la)) if not _same_level(la[l], lb[l]))
+    assert 1 <= first < len(la)
+
+    def solver(mg):
+        G.setup_lmgc(mg, sm, baselevel=0, damp=_damp(sm), red=1e-10, abslimit=1e-50)
+
+    fresh = G.MultiGrid(lb, order=order)
+    solver(fresh)
+    x_ref, lr_ref = fresh.solve_host("mgs", b.rhs)
+    fresh.close()
+
+    mg = G.MultiGrid(la, order=order)
+    solver(mg)
+    mg.solve_host("mgs", a.rhs)
+    kept = [mg.matrix(l) for l in range(first)]
+    mg.replace_levels(first, lb[first:])
+    assert mg.nlevels == len(lb) and mg.local
+    for l in range(first):
+        assert all(np.array_equal(u, v) for u, v in zip(mg.matrix(l), kept[l]))
+    x, lr = mg.solve_host("mgs", b.rhs)
+    assert lr.converged and lr.iters == lr_ref.iters
+    assert np.array_equal(x, x_ref)
+    # replacing the top with itself changes nothing
+    mg.replace_levels(mg.top, lb[-1:])
+    x2, lr2 = mg.solve_host("mgs", b.rhs)
+    assert lr2.iters == lr_ref.iters and np.array_equal(x2, x_ref)
+    mg.close()
+
+
+def test_replace_levels_errors(G):
+    gen = G.LocalGenerator(2, 2, seed=5)
+    levels = [gen.level(l) for l in range(gen.nlevels)]
+    mg = G.MultiGrid(levels)
+    with pytest.raises(G.GmgError, match="first level"):
+        mg.replace_levels(0, levels)
+    with pytest.raises(G.GmgError, match="first level"):
+        mg.replace_levels(len(levels) + 1, levels[-1:])
+    bad = dict(levels[-1])
+    bad["pcol"] = np.asarray(bad["pcol"]) + 10 ** 6
+    with pytest.raises(G.GmgError, match="coarse index"):
+        mg.replace_levels(mg.top, [bad])
+    assert mg.nlevels == len(levels)  # a failed replacement keeps the hierarchy
+    mg.close()

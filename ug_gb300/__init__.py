@@ -122,6 +122,7 @@ def lib(build_if_missing: bool = True):
         "gmg_lgen_rhs": ([P, P, P], I), "gmg_lgen_coords": ([P, I, P], I), "gmg_lgen_destroy": ([P], I),
         "gmg_gen_create": ([I, I, C.c_ulonglong, D, D, P], I), "gmg_gen_levels": ([P, P, P], I),
         "gmg_gen_rhs": ([P, P, P], I), "gmg_gen_coords": ([P, I, P], I), "gmg_gen_destroy": ([P], I),
+        "gmg_mg_replace_levels": ([P, I, P, I], I),
         "gmg_order_bw": ([P, P, P], I), "gmg_order_lex": ([P, I, P, I, C.c_char_p, D, P], I),
     }
     for name, (args, res) in sig.items():
@@ -408,11 +409,26 @@ class MultiGrid:
                 self.pack_off.append(po.value)
             self.block = self.size(0)[1]
             self.packed_len = (self.pack_off[-1] + self.inst_n[-1]) * self.block
-        # locally refined: the surface spans levels frl..top, host vectors hold every level
-        self.frl = L.gmg_mg_full_refine_level(h)
-        self.local = self.frl < self.top
-        self.level_len = [self.size(l)[0] * self.size(l)[1] for l in range(nl)]
+        self._refresh_levels()
         del keep  # the device holds its own copies
+
+    def _refresh_levels(self):
+        # locally refined: the surface spans levels frl..top, host vectors hold every level
+        self.nlevels = lib().gmg_mg_nlevels(self._h)
+        self.top = self.nlevels - 1
+        self.frl = lib().gmg_mg_full_refine_level(self._h)
+        self.local = self.frl < self.top
+        self.level_len = [self.size(l)[0] * self.size(l)[1] for l in range(self.nlevels)]
+
+    def replace_levels(self, from_level: int, levels) -> None:
+        """gmg_mg_replace_levels: levels from_level.. replaced by ``levels``
+        (level dicts, the new levels from_level, from_level+1, ...) after an
+        adaptation changed them; the levels below are kept as they are."""
+        keep: list = []
+        desc_arr, n = _desc_array(list(levels), keep)
+        if lib().gmg_mg_replace_levels(self._h, int(from_level), C.cast(desc_arr, C.c_void_p), n):
+            _err("gmg_mg_replace_levels")
+        self._refresh_levels()
 
     # ---- locally refined hierarchies
     def split_levels(self, flat) -> list:

@@ -47,8 +47,9 @@ enum : uint8_t {
 void par_copy(void *dst, const void *src, size_t bytes);
 
 // ---------------------------------------------------------------- device memory
-// All arrays of one hierarchy live in one allocation; sub-arrays are 256-byte
-// aligned so every row / block access can use 128-bit loads.
+// The arrays of one level live in one allocation (the level's arena);
+// sub-arrays are 256-byte aligned so every row / block access can use
+// 128-bit loads.
 struct Arena {
   char *base = nullptr;
   size_t size = 0, used = 0;
@@ -76,6 +77,7 @@ struct Sched {
 };
 
 struct Level {
+  Arena arena;                  // the level's device arrays (released with the level)
   int n = 0, s = 1;
   long long nnzb = 0;
   bool all_active = true;   // every row ACTIVE
@@ -186,7 +188,6 @@ struct gmg_mg {
   int device = 0;
   cudaStream_t stream = nullptr;
   gmg_mg_opts opts{};
-  gmg::Arena arena;
   std::vector<gmg::Level> lev;
   // FULLREFINELEVEL (gm/algebra.cc:2838): the lowest level holding a
   // FINE_GRID_DOF row; below the top level only on a locally refined
@@ -201,8 +202,9 @@ struct gmg_mg {
   double *partial = nullptr;   // GMG_REDUCE_BLOCKS * GMG_MAX_S
   double *norms_dev = nullptr; // GMG_MAX_S
   double *norms_host = nullptr;// pinned
-  void *stage_dev = nullptr;   // n_top*s doubles
-  double *stage_host = nullptr;// pinned, n_top*s doubles
+  void *stage_dev = nullptr;   // stage_len doubles
+  double *stage_host = nullptr;// pinned, stage_len doubles
+  size_t stage_len = 0;        // n_top*s (every level on a locally refined hierarchy)
   long long launches = 0;
   // bumped when device copies that captured iterations point into are
   // replaced (gmg_mg_update_values drops the fused coarse images): a CUDA

@@ -655,8 +655,10 @@ gmg_mg::~gmg_mg() {
   for (auto &L : lev) {
     for (void *p : L.own) cudaFree(p);
     if (L.ainv) cudaFree(L.ainv);
+    L.arena.release();
   }
-  arena.release();
+  if (partial) cudaFree(partial);
+  if (stage_dev) cudaFree(stage_dev);
   if (norms_host) cudaFreeHost(norms_host);
   if (stage_host) cudaFreeHost(stage_host);
   if (batch.conv_host) cudaFreeHost(batch.conv_host);
@@ -669,148 +671,107 @@ const char *gmg_last_error(void) { return gmg::last_error(); }
 
 }  // extern "C"
 
-// the device hierarchy of `levels`; `colours` optionally fixes each level's
-// colouring, `stage_min` is the least staging length (doubles) to allocate
-static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts &opts,
-                            const std::vector<std::vector<int>> *colours, size_t stage_min,
-                            std::unique_ptr<gmg_mg> &out) {
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return 1; }
-  GMG_CUDA(cudaSetDevice(opts.device));
-  const int s = levels[0].s;
-  std::vector<HostLevel> H(nlevels);
-  for (int l = 0; l < nlevels; ++l) {
-    GMG_CHECK(levels[l].s == s, "all levels must have the same block size");
-    if (build_host_level(levels[l], opts.order, H[l], colours ? &(*colours)[l] : nullptr)) return 1;
-    if (l > 0 && build_host_transfer(levels[l], H[l - 1], H[l])) return 1;
+// device arrays of one level in its own arena (nc = rows of level-1, or -1 on
+// level 0); the host copies the factorisations need move into the Level
+static int upload_level(HostLevel &h, int nc, bool f32, Level &L) {
+  const int s = h.s;
+  const size_t nnz = h.rowptr[h.n], ss = size_t(s) * s;
+  size_t bytes = al((h.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * 8) + (f32 ? al(nnz * ss * 4) : 0);
+  bytes += al(h.n * ss * 8) + (f32 ? al(h.n * ss * 4) : 0) + 2 * al(h.n) + 3 * al(h.n * 4);
+  bytes += al(h.lptr.size() * 4) + al(h.uptr.size() * 4);
+  if (!h.sptr.empty())
+    bytes += al(h.sptr.size() * 4) + al(h.scol.size() * 4) + al(h.sval.size() * 8) + (f32 ? al(h.sval.size() * 4) : 0);
+  if (nc >= 0) {
+    size_t pn = h.pcol.size(), rn = h.rcol.size();
+    bytes += al((h.n + 1) * 4) + al(pn * 4) + al(pn * 8) + (f32 ? al(pn * 4) : 0);
+    bytes += al((size_t(nc) + 1) * 4) + al(rn * 4) + al(rn * 8) + (f32 ? al(rn * 4) : 0);
   }
-  // plan the arena
-  const bool f32 = opts.fp32_copy != 0;
-  size_t bytes = 0;
-  for (int l = 0; l < nlevels; ++l) {
-    const HostLevel &h = H[l];
-    size_t nnz = h.rowptr[h.n], ss = size_t(s) * s;
-    bytes += al((h.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * 8) + (f32 ? al(nnz * ss * 4) : 0);
-    bytes += al(h.n * ss * 8) + (f32 ? al(h.n * ss * 4) : 0) + 2 * al(h.n) + 3 * al(h.n * 4);
-    bytes += al(h.lptr.size() * 4) + al(h.uptr.size() * 4);
-    if (!h.sptr.empty())
-      bytes += al(h.sptr.size() * 4) + al(h.scol.size() * 4) + al(h.sval.size() * 8) + (f32 ? al(h.sval.size() * 4) : 0);
-    if (l > 0) {
-      size_t pn = h.pcol.size(), rn = h.rcol.size();
-      bytes += al((h.n + 1) * 4) + al(pn * 4) + al(pn * 8) + (f32 ? al(pn * 4) : 0);
-      bytes += al((H[l - 1].n + 1) * 4) + al(rn * 4) + al(rn * 8) + (f32 ? al(rn * 4) : 0);
-    }
+  Arena &ar = L.arena;
+  if (ar.alloc(bytes)) return 1;
+  L.n = h.n; L.s = s; L.nnzb = nnz;
+  L.all_active = h.all_active; L.any_skip = h.any_skip;
+  L.A.nrows = h.n; L.A.nnz = nnz;
+  L.A.rowptr = ar.take_n<int>(h.n + 1);
+  L.A.col = ar.take_n<int>(nnz);
+  L.A.v64 = ar.take_n<double>(nnz * ss);
+  if (upload(L.A.rowptr, h.rowptr.data(), h.n + 1) || upload(L.A.col, h.col.data(), nnz) ||
+      upload(L.A.v64, h.val.data(), nnz * ss))
+    return 1;
+  L.dinv64 = ar.take_n<double>(h.n * ss);
+  if (upload(L.dinv64, h.dinv.data(), h.n * ss)) return 1;
+  if (f32) {
+    L.A.v32 = ar.take_n<float>(nnz * ss);
+    L.dinv32 = ar.take_n<float>(h.n * ss);
+    auto v = to_f32(h.val), dv = to_f32(h.dinv);
+    if (upload(L.A.v32, v.data(), v.size()) || upload(L.dinv32, dv.data(), dv.size())) return 1;
   }
-  auto mg = std::make_unique<gmg_mg>();
-  mg->device = opts.device;
-  mg->opts = opts;
-  // a stream of its own: the legacy default stream cannot be captured into graphs
-  GMG_CUDA(cudaStreamCreateWithFlags(&mg->stream, cudaStreamNonBlocking));
-  mg->own_stream = true;
-  if (mg->arena.alloc(bytes)) return 1;
-  mg->lev.resize(nlevels);
-  for (int l = 0; l < nlevels; ++l) {
-    HostLevel &h = H[l];
-    Level &L = mg->lev[l];
-    const size_t nnz = h.rowptr[h.n], ss = size_t(s) * s;
-    L.n = h.n; L.s = s; L.nnzb = nnz;
-    L.all_active = h.all_active; L.any_skip = h.any_skip;
-    L.A.nrows = h.n; L.A.nnz = nnz;
-    L.A.rowptr = mg->arena.take_n<int>(h.n + 1);
-    L.A.col = mg->arena.take_n<int>(nnz);
-    L.A.v64 = mg->arena.take_n<double>(nnz * ss);
-    if (upload(L.A.rowptr, h.rowptr.data(), h.n + 1) || upload(L.A.col, h.col.data(), nnz) ||
-        upload(L.A.v64, h.val.data(), nnz * ss))
+  L.flags = ar.take_n<uint8_t>(h.n);
+  L.skip = ar.take_n<uint8_t>(h.n);
+  L.perm_dev = ar.take_n<int>(h.n);
+  L.lower.rows = ar.take_n<int>(h.n);
+  L.upper.rows = ar.take_n<int>(h.n);
+  L.lower.ptr = h.lptr;
+  L.upper.ptr = h.uptr;
+  L.lower.ptr_dev = ar.take_n<int>(h.lptr.size());
+  L.upper.ptr_dev = ar.take_n<int>(h.uptr.size());
+  if (upload(L.lower.ptr_dev, h.lptr.data(), h.lptr.size()) || upload(L.upper.ptr_dev, h.uptr.data(), h.uptr.size()))
+    return 1;
+  if (upload(L.flags, h.flags.data(), h.n) || upload(L.skip, h.skip.data(), h.n) ||
+      upload(L.perm_dev, h.perm.data(), h.n) || upload(L.lower.rows, h.lrows.data(), h.n) ||
+      upload(L.upper.rows, h.urows.data(), h.n))
+    return 1;
+  if (nc >= 0) {
+    L.P.nrows = h.n; L.P.nnz = h.pcol.size();
+    L.P.rowptr = ar.take_n<int>(h.n + 1);
+    L.P.col = ar.take_n<int>(h.pcol.size());
+    L.P.v64 = ar.take_n<double>(h.pw.size());
+    L.R.nrows = nc; L.R.nnz = h.rcol.size();
+    L.R.rowptr = ar.take_n<int>(nc + 1);
+    L.R.col = ar.take_n<int>(h.rcol.size());
+    L.R.v64 = ar.take_n<double>(h.rw.size());
+    if (upload(L.P.rowptr, h.prow.data(), h.n + 1) || upload(L.P.col, h.pcol.data(), h.pcol.size()) ||
+        upload(L.P.v64, h.pw.data(), h.pw.size()) || upload(L.R.rowptr, h.rrow.data(), nc + 1) ||
+        upload(L.R.col, h.rcol.data(), h.rcol.size()) || upload(L.R.v64, h.rw.data(), h.rw.size()))
       return 1;
-    L.dinv64 = mg->arena.take_n<double>(h.n * ss);
-    if (upload(L.dinv64, h.dinv.data(), h.n * ss)) return 1;
     if (f32) {
-      L.A.v32 = mg->arena.take_n<float>(nnz * ss);
-      L.dinv32 = mg->arena.take_n<float>(h.n * ss);
-      auto v = to_f32(h.val), dv = to_f32(h.dinv);
-      if (upload(L.A.v32, v.data(), v.size()) || upload(L.dinv32, dv.data(), dv.size())) return 1;
+      L.P.v32 = ar.take_n<float>(h.pw.size());
+      L.R.v32 = ar.take_n<float>(h.rw.size());
+      auto pw = to_f32(h.pw), rw = to_f32(h.rw);
+      if (upload(L.P.v32, pw.data(), pw.size()) || upload(L.R.v32, rw.data(), rw.size())) return 1;
     }
-    L.flags = mg->arena.take_n<uint8_t>(h.n);
-    L.skip = mg->arena.take_n<uint8_t>(h.n);
-    L.perm_dev = mg->arena.take_n<int>(h.n);
-    L.lower.rows = mg->arena.take_n<int>(h.n);
-    L.upper.rows = mg->arena.take_n<int>(h.n);
-    L.lower.ptr = h.lptr;
-    L.upper.ptr = h.uptr;
-    L.lower.ptr_dev = mg->arena.take_n<int>(h.lptr.size());
-    L.upper.ptr_dev = mg->arena.take_n<int>(h.uptr.size());
-    if (upload(L.lower.ptr_dev, h.lptr.data(), h.lptr.size()) || upload(L.upper.ptr_dev, h.uptr.data(), h.uptr.size()))
-      return 1;
-    if (upload(L.flags, h.flags.data(), h.n) || upload(L.skip, h.skip.data(), h.n) ||
-        upload(L.perm_dev, h.perm.data(), h.n) || upload(L.lower.rows, h.lrows.data(), h.n) ||
-        upload(L.upper.rows, h.urows.data(), h.n))
-      return 1;
-    if (l > 0) {
-      const int nc = H[l - 1].n;
-      L.P.nrows = h.n; L.P.nnz = h.pcol.size();
-      L.P.rowptr = mg->arena.take_n<int>(h.n + 1);
-      L.P.col = mg->arena.take_n<int>(h.pcol.size());
-      L.P.v64 = mg->arena.take_n<double>(h.pw.size());
-      L.R.nrows = nc; L.R.nnz = h.rcol.size();
-      L.R.rowptr = mg->arena.take_n<int>(nc + 1);
-      L.R.col = mg->arena.take_n<int>(h.rcol.size());
-      L.R.v64 = mg->arena.take_n<double>(h.rw.size());
-      if (upload(L.P.rowptr, h.prow.data(), h.n + 1) || upload(L.P.col, h.pcol.data(), h.pcol.size()) ||
-          upload(L.P.v64, h.pw.data(), h.pw.size()) || upload(L.R.rowptr, h.rrow.data(), nc + 1) ||
-          upload(L.R.col, h.rcol.data(), h.rcol.size()) || upload(L.R.v64, h.rw.data(), h.rw.size()))
-        return 1;
-      if (f32) {
-        L.P.v32 = mg->arena.take_n<float>(h.pw.size());
-        L.R.v32 = mg->arena.take_n<float>(h.rw.size());
-        auto pw = to_f32(h.pw), rw = to_f32(h.rw);
-        if (upload(L.P.v32, pw.data(), pw.size()) || upload(L.R.v32, rw.data(), rw.size())) return 1;
-      }
-    }
-    L.tpr = pick_tpr(h);
-    L.waves_contiguous = h.contiguous;
-    if (!h.sptr.empty()) {
-      L.sell = true;
-      L.sell_nent = h.sptr.back();
-      L.sell_ptr = mg->arena.take_n<int>(h.sptr.size());
-      L.sell_col = mg->arena.take_n<int>(h.scol.size());
-      L.sell_v64 = mg->arena.take_n<double>(h.sval.size());
-      if (upload(L.sell_ptr, h.sptr.data(), h.sptr.size()) || upload(L.sell_col, h.scol.data(), h.scol.size()) ||
-          upload(L.sell_v64, h.sval.data(), h.sval.size()))
-        return 1;
-      if (f32) {
-        L.sell_v32 = mg->arena.take_n<float>(h.sval.size());
-        auto sv = to_f32(h.sval);
-        if (upload(L.sell_v32, sv.data(), sv.size())) return 1;
-      }
-      std::vector<int>().swap(h.sptr);
-      std::vector<int>().swap(h.scol);
-      std::vector<double>().swap(h.sval);
-    }
-    // keep host copies for the ILU / base factorisations and for export
-    L.perm = std::move(h.perm);
-    L.h_rowptr = std::move(h.rowptr);
-    L.h_col = std::move(h.col);
-    L.h_val = std::move(h.val);
-    L.h_flags = std::move(h.flags);
-    L.h_skip = std::move(h.skip);
   }
-  GMG_CHECK(mg->arena.used <= mg->arena.size, "arena overflow");
+  L.tpr = pick_tpr(h);
+  L.waves_contiguous = h.contiguous;
+  if (!h.sptr.empty()) {
+    L.sell = true;
+    L.sell_nent = h.sptr.back();
+    L.sell_ptr = ar.take_n<int>(h.sptr.size());
+    L.sell_col = ar.take_n<int>(h.scol.size());
+    L.sell_v64 = ar.take_n<double>(h.sval.size());
+    if (upload(L.sell_ptr, h.sptr.data(), h.sptr.size()) || upload(L.sell_col, h.scol.data(), h.scol.size()) ||
+        upload(L.sell_v64, h.sval.data(), h.sval.size()))
+      return 1;
+    if (f32) {
+      L.sell_v32 = ar.take_n<float>(h.sval.size());
+      auto sv = to_f32(h.sval);
+      if (upload(L.sell_v32, sv.data(), sv.size())) return 1;
+    }
+    std::vector<int>().swap(h.sptr);
+    std::vector<int>().swap(h.scol);
+    std::vector<double>().swap(h.sval);
+  }
+  GMG_CHECK(ar.used <= ar.size, "arena overflow");
   // son of every coarse row (the fine corner copy), for StandardProject
-  for (int l = 1; l < nlevels; ++l) {
-    HostLevel &h = H[l];
-    std::vector<int> son(H[l - 1].n, -1);
+  if (nc >= 0) {
+    std::vector<int> son(nc, -1);
     for (int f = 0; f < h.n; ++f)
       if (h.prow[f + 1] - h.prow[f] == 1 && h.pw[h.prow[f]] == 1.0) son[h.pcol[h.prow[f]]] = f;
-    Level &L = mg->lev[l];
     GMG_CUDA(cudaMalloc(&L.son, sizeof(int) * std::max<size_t>(son.size(), 1)));
     L.own.push_back(L.son);
     if (!son.empty()) GMG_CUDA(cudaMemcpy(L.son, son.data(), sizeof(int) * son.size(), cudaMemcpyHostToDevice));
   }
   // subdomain tables of the triangular sweeps
-  for (int l = 0; l < nlevels; ++l) {
-    HostLevel &h = H[l];
-    Level &L = mg->lev[l];
-    if (h.dom_nreg == 0) continue;
+  if (h.dom_nreg > 0) {
     L.dom_nreg = h.dom_nreg;
     L.dom_nint = h.dom_nint;
     L.dom_cptr = h.dom_cptr;
@@ -829,30 +790,86 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
         put(&L.dom_iface, iface))
       return 1;
   }
-  // FULLREFINELEVEL (SetSurfaceClasses, gm/algebra.cc:2905-2921)
+  // keep host copies for the ILU / base factorisations and for export
+  L.perm = std::move(h.perm);
+  L.h_rowptr = std::move(h.rowptr);
+  L.h_col = std::move(h.col);
+  L.h_val = std::move(h.val);
+  L.h_flags = std::move(h.flags);
+  L.h_skip = std::move(h.skip);
+  return 0;
+}
+
+// the device memory a Level owns (its arena, separately allocated arrays, the base inverse)
+static void free_level(Level &L) {
+  for (void *p : L.own) cudaFree(p);
+  L.own.clear();
+  if (L.ainv) cudaFree(L.ainv);
+  L.ainv = nullptr;
+  L.arena.release();
+}
+
+// FULLREFINELEVEL (SetSurfaceClasses, gm/algebra.cc:2905-2921) and the pinned
+// / device staging buffers (the top level, or every level of a locally refined
+// hierarchy, at least stage_min doubles)
+static int finish_hierarchy(gmg_mg *mg, size_t stage_min) {
+  const int nlevels = int(mg->lev.size()), s = mg->lev[0].s;
   mg->frl = nlevels - 1;
   for (int l = nlevels - 1; l >= 0; --l)
     for (uint8_t f : mg->lev[l].h_flags)
       if (f & F_FINE) { mg->frl = l; break; }
   GMG_CHECK(!mg->local() || nlevels <= SURF_MAX_LEVELS, "a locally refined hierarchy has at most %d levels",
             SURF_MAX_LEVELS);
-  // scratch
-  // reduction scratch: per-block partial sums, the norms, and the norm kernel's ticket counter
-  const size_t scratch = sizeof(double) * (REDUCE_BLOCKS * GMG_MAX_S + GMG_MAX_S + 1);
-  GMG_CUDA(cudaMalloc(&mg->partial, scratch));
-  GMG_CUDA(cudaMemset(mg->partial, 0, scratch));
-  mg->norms_dev = mg->partial + REDUCE_BLOCKS * GMG_MAX_S;
-  GMG_CUDA(cudaMallocHost(&mg->norms_host, sizeof(double) * GMG_MAX_S));
-  mg->lev.back().own.push_back(mg->partial);
   size_t top_len = std::max(size_t(mg->lev.back().n) * s, stage_min);
   if (mg->local()) {  // host vectors of a locally refined hierarchy hold every level
     size_t all = 0;
     for (const auto &L : mg->lev) all += size_t(L.n) * s;
     top_len = std::max(top_len, all);
   }
-  GMG_CUDA(cudaMallocHost(&mg->stage_host, sizeof(double) * (top_len ? top_len : 1)));
-  GMG_CUDA(cudaMalloc(&mg->stage_dev, sizeof(double) * (top_len ? top_len : 1)));
-  mg->lev.back().own.push_back(mg->stage_dev);
+  if (top_len == 0) top_len = 1;
+  if (top_len > mg->stage_len) {
+    if (mg->stage_host) cudaFreeHost(mg->stage_host);
+    if (mg->stage_dev) cudaFree(mg->stage_dev);
+    mg->stage_host = nullptr;
+    mg->stage_dev = nullptr;
+    GMG_CUDA(cudaMallocHost(&mg->stage_host, sizeof(double) * top_len));
+    GMG_CUDA(cudaMalloc(&mg->stage_dev, sizeof(double) * top_len));
+    mg->stage_len = top_len;
+  }
+  return 0;
+}
+
+// the device hierarchy of `levels`; `colours` optionally fixes each level's
+// colouring, `stage_min` is the least staging length (doubles) to allocate
+static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts &opts,
+                            const std::vector<std::vector<int>> *colours, size_t stage_min,
+                            std::unique_ptr<gmg_mg> &out) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return 1; }
+  GMG_CUDA(cudaSetDevice(opts.device));
+  const int s = levels[0].s;
+  std::vector<HostLevel> H(nlevels);
+  for (int l = 0; l < nlevels; ++l) {
+    GMG_CHECK(levels[l].s == s, "all levels must have the same block size");
+    if (build_host_level(levels[l], opts.order, H[l], colours ? &(*colours)[l] : nullptr)) return 1;
+    if (l > 0 && build_host_transfer(levels[l], H[l - 1], H[l])) return 1;
+  }
+  auto mg = std::make_unique<gmg_mg>();
+  mg->device = opts.device;
+  mg->opts = opts;
+  // a stream of its own: the legacy default stream cannot be captured into graphs
+  GMG_CUDA(cudaStreamCreateWithFlags(&mg->stream, cudaStreamNonBlocking));
+  mg->own_stream = true;
+  mg->lev.resize(nlevels);
+  for (int l = 0; l < nlevels; ++l)
+    if (upload_level(H[l], l > 0 ? H[l - 1].n : -1, opts.fp32_copy != 0, mg->lev[l])) return 1;
+  if (finish_hierarchy(mg.get(), stage_min)) return 1;
+  // reduction scratch: per-block partial sums, the norms, and the norm kernel's ticket counter
+  const size_t scratch = sizeof(double) * (REDUCE_BLOCKS * GMG_MAX_S + GMG_MAX_S + 1);
+  GMG_CUDA(cudaMalloc(&mg->partial, scratch));
+  GMG_CUDA(cudaMemset(mg->partial, 0, scratch));
+  mg->norms_dev = mg->partial + REDUCE_BLOCKS * GMG_MAX_S;
+  GMG_CUDA(cudaMallocHost(&mg->norms_host, sizeof(double) * GMG_MAX_S));
   mg->mats["MAT"] = std::make_unique<gmg_mat>();
   mg->mats["MAT"]->name = "MAT";
   mg->mats["MAT"]->mg = mg.get();
@@ -974,6 +991,71 @@ int gmg_mg_create(const gmg_level_desc *levels, int nlevels, const gmg_mg_opts *
   std::unique_ptr<gmg_mg> mg;
   if (create_hierarchy(levels, nlevels, opts, nullptr, 0, mg)) return 1;
   *out = mg.release();
+  return 0;
+}
+
+// Levels from_level.. after an adaptation: AdaptMultiGrid (gm/refine.cc)
+// changes the levels from the lowest one holding a refined or coarsened
+// element upward, and the flattener re-exports only those.  The levels below
+// keep every device array, ILU factor and base inverse; the new levels are
+// built as gmg_mg_create builds them.  Vectors keep their values on the kept
+// levels and start at zero on the new ones; fused coarse images are dropped
+// and captured iterations re-captured; every linear solver runs its
+// PreProcess again at its next solve (new ILU factors on the new levels).
+int gmg_mg_replace_levels(gmg_mg *mg, int from_level, const gmg_level_desc *levels, int count) {
+  if (!mg || !levels || count < 1) { set_error("gmg_mg_replace_levels: bad arguments"); return 1; }
+  GMG_CHECK(mg->batch.ninst == 0, "gmg_mg_replace_levels: not on a batched hierarchy");
+  const int old_n = int(mg->lev.size());
+  GMG_CHECK(from_level >= 1 && from_level <= old_n, "gmg_mg_replace_levels: first level %d not in 1..%d", from_level,
+            old_n);
+  const int s = mg->lev[0].s, nl = from_level + count;
+  GMG_CUDA(cudaSetDevice(mg->device));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));  // nothing in flight reads the old levels
+  // the kept level below, as the transfer builder sees it (its row count and
+  // the processing position of every list position)
+  HostLevel below;
+  {
+    const Level &C = mg->lev[from_level - 1];
+    below.n = C.n;
+    below.iperm.assign(C.n, 0);
+    for (int i = 0; i < C.n; ++i) below.iperm[C.perm[i]] = i;
+  }
+  std::vector<HostLevel> H(count);
+  for (int k = 0; k < count; ++k) {
+    GMG_CHECK(levels[k].s == s, "all levels must have the same block size");
+    if (build_host_level(levels[k], mg->opts.order, H[k], nullptr)) return 1;
+    if (build_host_transfer(levels[k], k ? H[k - 1] : below, H[k])) return 1;
+  }
+  std::vector<Level> fresh(count);
+  for (int k = 0; k < count; ++k)
+    if (upload_level(H[k], k ? H[k - 1].n : below.n, mg->opts.fp32_copy != 0, fresh[k])) {
+      for (auto &L : fresh) free_level(L);
+      return 1;
+    }
+  for (int l = from_level; l < old_n; ++l) free_level(mg->lev[l]);
+  mg->lev.resize(from_level);
+  for (auto &L : fresh) mg->lev.push_back(std::move(L));
+  for (auto &kv : mg->vecs) {
+    gmg_vec *v = kv.second.get();
+    for (int l = from_level; l < (int)v->lev.size(); ++l)
+      if (v->lev[l]) cudaFree(v->lev[l]);
+    v->lev.resize(nl, nullptr);
+    for (int l = from_level; l < nl; ++l) {
+      const size_t len = size_t(mg->lev[l].n) * s, bytes = (len ? len : 1) * (v->prec == GMG_PREC_FP64 ? 8 : 4);
+      GMG_CUDA(cudaMalloc(&v->lev[l], bytes));
+      GMG_CUDA(cudaMemsetAsync(v->lev[l], 0, bytes, mg->stream));
+    }
+  }
+  mg->coarse_images.clear();
+  mg->coarse_smem_cache.clear();
+  ++mg->graph_epoch;
+  for (auto &kv : mg->nps)
+    if (NPLs *ls = dynamic_cast<NPLs *>(kv.second.get())) ls->preprocessed = false;
+  if (finish_hierarchy(mg, 0)) return 1;
+  if (mg->opts.autotune)
+    for (int l = from_level; l < nl; ++l)
+      if (autotune_level(mg, mg->lev[l])) return 1;
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
   return 0;
 }
 
@@ -1216,7 +1298,8 @@ int gmg_mg_num_waves(const gmg_mg *mg, int level) {
 
 long long gmg_mg_device_bytes(const gmg_mg *mg) {
   if (!mg) return 0;
-  long long b = (long long)mg->arena.size;
+  long long b = 0;
+  for (const auto &L : mg->lev) b += (long long)L.arena.size;
   for (auto &kv : mg->vecs)
     for (size_t l = 0; l < kv.second->lev.size(); ++l)
       b += (long long)mg->lev[l].n * mg->lev[l].s * (kv.second->prec == GMG_PREC_FP64 ? 8 : 4);
