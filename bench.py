@@ -664,10 +664,12 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t0)
     e2e_ms = reduce_over_ranks(float(np.mean(e2e_t)) * 1e3)
 
-    # roofline of the dominant kernel (the Gauss-Seidel colour waves, sell_gs_kernel:
-    # ~44 % of the mixed solve's profiled time) -- one FP32 l_lgs sweep of the
-    # finest level = one launch per colour -- and of the finest-level dmatmul_minus,
-    # each HBM-cold, CUDA events on the launching stream
+    # roofline of the dominant streaming kernel: the finest level's Gauss-Seidel
+    # colour waves (in the solve as sell_gs_chain_kernel, whose launches also
+    # finish the previous colour's defect rows: ~19 % of the profiled cycle,
+    # profiles/launches_c2.md), measured as one FP32 l_lgs sweep of the finest
+    # level = one sell_gs_kernel launch per colour -- and the finest-level
+    # dmatmul_minus, each HBM-cold, CUDA events on the launching stream
     n, s, nnz = mg.size(top)
     nwaves_top = mg.num_waves(top)
     mg.createvector("ry", "rx")
@@ -747,7 +749,9 @@ def run_ours(args):
                          "achieved": ach_gs, "peak": peak, "unit": "GB/s", "frac": ach_gs / peak,
                          "peak_kind": peak_kind, "traffic": profiled_traffic("gs"),
                          "algorithmic_bytes": algo_gs / nwaves_top, "launch_ms": gs_ms / nwaves_top,
-                         "note": "latency-bound: each colour wave is a dependent gather chain of a few us",
+                         "note": "latency-bound: each colour wave is a dependent gather chain of a few us; "
+                                 "the solve runs the same waves as sell_gs_chain_kernel (~19% of the profiled "
+                                 "cycle) next to the one-CTA fused coarse cycle (~15%, shared-memory latency)",
                          "spmv_fp32": {"kernel": "sell_spmv_kernel<float> (finest-level dmatmul_minus)",
                                        "achieved": ach32, "frac": ach32 / peak, "algorithmic_bytes": algo[32],
                                        "launch_ms": kms[32], "traffic": profiled_traffic("spmv")},
