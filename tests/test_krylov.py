@@ -20,10 +20,11 @@ def G():
     return ug_gb300
 
 
-def _setup_cg(G, mg, sm, bl, red=1e-10, mixed=False, name="cgs"):
+def _setup_cg(G, mg, sm, bl, red=1e-10, mixed=False, name="cgs", dloop=True):
     G.setup_lmgc(mg, sm, baselevel=bl, damp=0.8 if sm == "jac" else 1.0, red=red, abslimit=1e-50)
     mg.npcreate(name, "linear_solver.gcg")
-    st = mg.npinit(name, f"$A MAT $x sol $b rhs $red {red} $abslimit 1e-50 $m 100 $I lmgc $mixed {int(mixed)}")
+    st = mg.npinit(name, f"$A MAT $x sol $b rhs $red {red} $abslimit 1e-50 $m 100 $I lmgc $mixed {int(mixed)}"
+                         f" $dloop {int(dloop)}")
     assert st == G.NP_EXECUTABLE
     return name
 
@@ -114,3 +115,25 @@ def test_bcgs_gs_vs_oracle_midsize(G, oracle_mod, order):
     assert conv and lr.converged and abs(lr.iters - ito) <= 1
     assert rel(x, xr) <= 1e-8
     mg.close()
+
+
+@pytest.mark.parametrize("name,order,mixed", [("p1k_gs", 1, False), ("el_ilu", 0, True), ("ls_gs", 0, False)])
+def test_cg_device_loop_matches_host_loop(G, name, order, mixed):
+    """cg's iterations after the first run as one conditional graph (the loop
+    test also watches CGUpdate's (A p, p) = 0 flag); the host loop ($dloop 0)
+    takes the same iterations to the same x, bit for bit."""
+    fx = load_golden(name)
+    levels = G.levels_from_ugfx(fx)
+    sm, bl = fx["smoother"], int(fx["baselevel"][0])
+    out = {}
+    for dloop in (True, False):
+        mg = G.MultiGrid(levels, order=order, fp32=True)
+        _setup_cg(G, mg, sm, bl, mixed=mixed, dloop=dloop)
+        x, lr = mg.solve_host("cgs", fx["rhs_all"] if mg.local else fx["rhs"])
+        out[dloop] = (x, lr, mg.npdisplay("cgs"))
+        mg.close()
+    (xd, ld, dd), (xh, lh, dh) = out[True], out[False]
+    assert "loop = device (built)" in dd and "loop = host" in dh
+    assert ld.converged and ld.iters == lh.iters
+    assert list(ld.last_defect) == list(lh.last_defect)
+    assert np.array_equal(xd, xh)

@@ -297,13 +297,15 @@ int k_axpy(gmg_mg *mg, int prec, void *x, const void *y, int n, int s, const dou
 int k_convert(gmg_mg *mg, int dst_prec, void *dst, int src_prec, const void *src, long long len);
 // ls's convergence loop on the device (ls.cc:680-730): one conditional WHILE
 // node replays the iteration; after each pass the test counts it, keeps the
-// defect norms, stops on a non-finite norm (bad = the iteration), on
+// defect norms, stops on the solver's error flag (flagged = the iteration;
+// cg's (A p, p) = 0), on a non-finite norm (bad = the iteration), on
 // convergence (sc_cmp against abslimit or the reduction target) or at maxit
 struct LsLoopState {
-  int it = 0, conv = 0, bad = 0, maxit = 0, s = 0, pad[3] = {0, 0, 0};
+  int it = 0, conv = 0, bad = 0, maxit = 0, s = 0, flagged = 0, pad[2] = {0, 0};
   double abs[GMG_MAX_S] = {0}, reach[GMG_MAX_S] = {0}, last[GMG_MAX_S] = {0};
 };
-int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, cudaGraphConditionalHandle h);
+// flag (device, may be null): a nonzero value ends the loop as an error
+int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, const double *flag, cudaGraphConditionalHandle h);
 int k_add_mixed(gmg_mg *mg, double *x64, int src_prec, const void *c, long long len);  // x64 += c
 // x -= A y (A in the precision of x/y); if acc != null also acc += y
 int k_matmul_minus(gmg_mg *mg, const Level &L, int prec, void *x, const void *y, void *acc);

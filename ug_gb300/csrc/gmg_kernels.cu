@@ -2622,10 +2622,16 @@ int k_scatter(gmg_mg *mg, int prec, double *dst, const void *src, const int *per
 
 // the test of ls's loop after one device-side iteration: the same
 // comparisons as the host loop (sc_cmp, npscan.cc:1027: every |d_r| < |lim_r|)
-__global__ void ls_loop_test_kernel(LsLoopState *st, const double *__restrict__ norms, cudaGraphConditionalHandle h) {
+__global__ void ls_loop_test_kernel(LsLoopState *st, const double *__restrict__ norms, const double *flag,
+                                    cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0) return;
   const int it = st->it + 1, s = st->s;
   st->it = it;
+  if (flag && *flag != 0.0) {
+    st->flagged = it;
+    cudaGraphSetConditional(h, 0);
+    return;
+  }
   bool finite = true, below_abs = true, below_reach = true;
   for (int r = 0; r < s; ++r) {
     const double d = norms[r];
@@ -2643,8 +2649,8 @@ __global__ void ls_loop_test_kernel(LsLoopState *st, const double *__restrict__ 
   cudaGraphSetConditional(h, (!st->conv && it < st->maxit) ? 1u : 0u);
 }
 
-int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, cudaGraphConditionalHandle h) {
-  ls_loop_test_kernel<<<1, 32, 0, mg->stream>>>(st, mg->norms_dev, h);
+int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, const double *flag, cudaGraphConditionalHandle h) {
+  ls_loop_test_kernel<<<1, 32, 0, mg->stream>>>(st, mg->norms_dev, flag, h);
   LAUNCH_CHECK(mg);
   return 0;
 }

@@ -1256,7 +1256,7 @@ int NPLs::build_loop(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am) {
   norm_to_host = false;
   int rc = iteration(level, xv, bv, Am, &err);
   norm_to_host = true;
-  if (!rc) rc = k_ls_loop_test(mg, loop_dev, h);
+  if (!rc) rc = k_ls_loop_test(mg, loop_dev, iteration_flag(), h);
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(mg->stream, &captured);
   loop_kernels = mg->launches - before;
@@ -1311,6 +1311,10 @@ int NPLs::device_loop(int i0, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, 
   GMG_CUDA(cudaMemcpyAsync(loop_host, loop_dev, sizeof(LsLoopState), cudaMemcpyDeviceToHost, mg->stream));
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
   mg->launches += (st.it - i0) * loop_kernels;
+  if (st.flagged) {  // the solver's own error, reported as the host loop reports it
+    if (fetch_iteration_flag() || check_iteration(st.flagged - 1)) return 1;
+    GMG_CHECK(false, "ls: iteration flag set in iteration %d", st.flagged);
+  }
   for (int r = 0; r < s; ++r) lr->last_defect[r] = st.last[r];
   GMG_CHECK(st.bad == 0, "ls: defect is not finite in iteration %d", st.bad);
   lr->converged = st.conv;
@@ -1521,8 +1525,10 @@ int NPCg::surface_cg_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am,
                 (const double *)vlev(t, l), sc))
       return 1;
   if (surface_norm(mg, level, bv)) return 1;
-  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
-  GMG_CUDA(cudaMemcpyAsync(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  if (norm_to_host) {
+    GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * s, cudaMemcpyDeviceToHost, mg->stream));
+    GMG_CUDA(cudaMemcpyAsync(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  }
   return 0;
 }
 
@@ -1554,8 +1560,15 @@ int NPCg::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) 
   if (k_set(mg, GMG_PREC_FP64, tt, len, 0.0) || k_matmul_minus(mg, L, GMG_PREC_FP64, tt, pp, nullptr)) return 1;
   if (k_cg_dot(mg, L, tt, pp, sc, 2, -1.0) || k_cg_xb(mg, len, x, pp, b, tt, sc)) return 1;
   if (k_nrm2x(mg, L, GMG_PREC_FP64, b)) return 1;
-  GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
-  GMG_CUDA(cudaMemcpyAsync(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  if (norm_to_host) {
+    GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * L.s, cudaMemcpyDeviceToHost, mg->stream));
+    GMG_CUDA(cudaMemcpyAsync(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  }
+  return 0;
+}
+
+int NPCg::fetch_iteration_flag() {
+  GMG_CUDA(cudaMemcpy(flag_host, sc + 3, sizeof(double), cudaMemcpyDeviceToHost));
   return 0;
 }
 

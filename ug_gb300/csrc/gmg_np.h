@@ -209,6 +209,10 @@ struct NPLs : NPLinearSolver {
   virtual int iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
   // after every synchronised iteration: nonzero stops the solver with an error
   virtual int check_iteration(int i) { return 0; }
+  // the device value check_iteration tests (null: none); on the device loop a
+  // nonzero value ends the loop and check_iteration reports it
+  virtual const double *iteration_flag() const { return nullptr; }
+  virtual int fetch_iteration_flag() { return 0; }  // the flag's value to the host
   // the base-solver shortcut of lmgc: `ls $m 1 $I ex` as one kernel
   bool is_exact_base() const;
   // iteration i of Solver's loop (graph replay after the first), synchronised
@@ -246,6 +250,8 @@ struct NPCg : NPLs {
   // locally refined hierarchies: CGUpdate on every level, products ON_SURFACE
   int surface_cg_iteration(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *err);
   int check_iteration(int i) override;
+  const double *iteration_flag() const override { return sc + 3; }
+  int fetch_iteration_flag() override;
   std::string Display() const override;
 };
 
