@@ -13,8 +13,12 @@ With --spmv / --lgs: only the finest level's dmatmul_minus / Gauss-Seidel
 sweep (l_lgs, one launch per colour) in FP32, --cycles times.
 With --local NUNI: the locally refined L-shaped elasticity workload (NUNI
 uniform + --nloc local refinements, block ILU(0) V(2,2)) instead.
+With --coarse L: only the fused coarse cycle (one launch of one CTA), lmgc
+Iter on levels 1..L of the 3D hierarchy, --cycles times each, FP32.
 """
 import argparse
+
+import numpy as np
 
 import ug_gb300 as G
 
@@ -33,6 +37,9 @@ def main():
     ap.add_argument("--pool", type=int, default=0, help="one request in a one-slot serving pool of this depth")
     ap.add_argument("--local", type=int, default=0, help="uniform refinements of the locally refined workload")
     ap.add_argument("--nloc", type=int, default=9)
+    ap.add_argument("--coarse", type=int, default=0,
+                    help="only the fused coarse cycle: lmgc Iter on levels 1..COARSE, --cycles times each (FP32)")
+    ap.add_argument("--narrow", type=int, default=1, help="$narrow of lmgc (0: the whole block on every level)")
     a = ap.parse_args()
     if a.local:
         gen = G.LocalGenerator(a.local, a.nloc, seed=2026)
@@ -55,6 +62,21 @@ def main():
                 pass
         print(f"{a.cycles} pool iterations, depth {a.pool}")
         p.close()
+        return
+    if a.coarse:
+        gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
+        mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
+        G.setup_lmgc(mg, "gs", baselevel=0, red=1e-8, mixed=True, graph=False, narrow=bool(a.narrow))
+        mg.createvector("cc", "bb", prec=G.FP32)
+        mg.iter_preprocess("lmgc", mg.top, "sol", "rhs")
+        for lev in range(1, a.coarse + 1):
+            mg.upload("bb", lev, np.linspace(-1.0, 1.0, mg.size(lev)[0] * mg.size(lev)[1]))
+            mg.dset(lev, "cc", 0.0)
+            for _ in range(a.cycles):
+                mg.iter_iter("lmgc", lev, "cc", "bb")
+        mg.sync()
+        print(f"fused coarse cycles on levels 1..{a.coarse}, {a.cycles} each, narrow={a.narrow}")
+        mg.close()
         return
     if a.spmv or a.lgs:
         gen = G.Generator(G.Generator.DIFFUSION3D, a.nref, seed=2026, corr=0.1, var=1.0)
