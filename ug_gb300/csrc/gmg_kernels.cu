@@ -64,6 +64,7 @@ constexpr long long STREAM_MIN_BYTES = 96ll << 20;
 inline bool use_prefetch(const Level &L, long long grid) {
   return L.prefetch < 0 ? grid <= PREFETCH_MAX_BLOCKS : L.prefetch != 0;
 }
+constexpr long long REFINE_STREAM_MIN_BYTES = 16ll << 20;
 inline bool use_stream(const Level &L, long long bytes) { return L.stream < 0 ? bytes > STREAM_MIN_BYTES : L.stream != 0; }
 template <bool ST, class T>
 __device__ __forceinline__ T ld_mat(const T *p) {
@@ -2179,8 +2180,11 @@ int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const floa
     if (k_add_mixed(mg, x, GMG_PREC_FP32, c, (long long)L.n * L.s)) return 1;
     return k_matmul_minus_mixed(mg, L, b, GMG_PREC_FP32, c);
   }
-  const bool pre = use_prefetch(L, grid_for(L.n));
-  const bool st = use_stream(L, sell_bytes<double>(L));
+  // the FP64 matrix is read once per ls iteration while the FP32 copies are
+  // reused by every smoothing step of the cycle: above REFINE_STREAM_MIN_BYTES
+  // it streams with evict-first loads so that it does not push them out of L2
+  const bool st = sell_bytes<double>(L) > REFINE_STREAM_MIN_BYTES || use_stream(L, sell_bytes<double>(L));
+  const bool pre = !st && use_prefetch(L, grid_for(L.n));
 #define RU(SS)                                                                                                   \
   if (pre)                                                                                                       \
     GMG_LAUNCH((sell_spmv_kernel<double, float, double, SS, true, PF<SS>::N>), grid_for(L.n), BLK, L.n,          \
