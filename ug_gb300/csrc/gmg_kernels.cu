@@ -2750,7 +2750,7 @@ int k_project(gmg_mg *mg, const Level &F, const Level &C, int prec, void *xc, co
 // handles row g - row0[l] of the level l with row0[l] <= g < row0[l+1].
 // OP 0: b -= A y, 1: b += A y, 2: b = -(A y), 3: b = A y on the selected rows (the
 // surface rows of `mask`, or every row where `all` is set)
-template <int S, class YT, int OP>
+template <int S, class YT, int OP, bool STREAM>
 __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
   pdl_prologue();
   const int total = t.row0[t.nlev];
@@ -2765,7 +2765,7 @@ __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
       for (int r = 0; r < S; ++r) acc[r] = 0.0;
       const int k1 = __ldg(t.rowptr[l] + i + 1);
       for (int k = __ldg(t.rowptr[l] + i); k < k1; ++k) {
-        const int j = __ldg(t.col[l] + k);
+        const int j = STREAM ? __ldcs(t.col[l] + k) : __ldg(t.col[l] + k);
         const double *m = t.val[l] + (size_t)k * (S * S);
         double yj[S];
 #pragma unroll
@@ -2773,7 +2773,7 @@ __global__ void __launch_bounds__(BLK) surf_update_kernel(SurfLevels t) {
 #pragma unroll
         for (int r = 0; r < S; ++r)
 #pragma unroll
-          for (int c = 0; c < S; ++c) acc[r] = fma(__ldg(m + r * S + c), yj[c], acc[r]);
+          for (int c = 0; c < S; ++c) acc[r] = fma(STREAM ? __ldcs(m + r * S + c) : __ldg(m + r * S + c), yj[c], acc[r]);
       }
 #pragma unroll
       for (int r = 0; r < S; ++r) {
@@ -2865,8 +2865,11 @@ __global__ void __launch_bounds__(BLK) surf_nrm_kernel(SurfLevels t, double *__r
 int k_surf_update(gmg_mg *mg, const SurfLevels &t, int yprec, int s, int op) {
   if (t.row0[t.nlev] == 0) return 0;
   const int g = vec_grid(t.row0[t.nlev]);
-#define SO(SS, OP) { if (yprec == GMG_PREC_FP64) GMG_LAUNCH((surf_update_kernel<SS, double, OP>), g, BLK, t); \
-                     else GMG_LAUNCH((surf_update_kernel<SS, float, OP>), g, BLK, t); }
+  // an FP32 y is the mixed iteration's correction: the FP64 matrices are then
+  // read once per ls iteration while the FP32 cycle reuses its copies, so they
+  // stream with evict-first loads
+#define SO(SS, OP) { if (yprec == GMG_PREC_FP64) GMG_LAUNCH((surf_update_kernel<SS, double, OP, false>), g, BLK, t); \
+                     else GMG_LAUNCH((surf_update_kernel<SS, float, OP, true>), g, BLK, t); }
 #define SU(SS) { if (op == 0) SO(SS, 0) else if (op == 1) SO(SS, 1) else if (op == 2) SO(SS, 2) else SO(SS, 3) }
   if (s == 1) SU(1) else if (s == 2) SU(2) else if (s == 3) SU(3)
   else { set_error("block size %d not compiled", s); return 1; }
