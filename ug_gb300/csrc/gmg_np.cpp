@@ -1203,7 +1203,9 @@ int NPLs::Solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double 
   int i;
   for (i = 0; i < maxiter; ++i) {
     if (lr->converged) break;
-    if (i > 0 && on_device) return device_loop(i, level, xv, bv, Am, abs_, reach, lr);
+    // the first iteration runs eagerly (it creates the temporaries and the
+    // loop is captured after it); once the loop graph exists it runs them all
+    if (on_device && (i > 0 || loop_graph)) return device_loop(i, level, xv, bv, Am, abs_, reach, lr);
     if (step(i, level, xv, bv, Am, lr) || check_iteration(i)) return 1;
     for (int r = 0; r < s; ++r) lr->last_defect[r] = mg->norms_host[r];
     for (int r = 0; r < s; ++r)
