@@ -138,6 +138,40 @@ def test_batched_converged_instances_stay(G):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mixed,maxit", [(True, 100), (False, 100), (True, 3)])
+def test_batched_device_loop_matches_host_loop(G, mixed, maxit):
+    """The batched ls loop after the first iteration (every later solve: all
+    of it) runs as one conditional graph whose test keeps every instance's
+    convergence, iteration count and last defect on the device; the host loop
+    ($dloop 0) gives the same per-instance results and the same x, bit for
+    bit, including an instance converged from the start and, with $m 3,
+    instances stopped unconverged."""
+    gens = _instances(G, 0, [3, 5, 2, 4, 6])
+    insts = [g.levels() for g in gens]
+    rhs = [g.rhs.copy() for g in gens]
+    rhs[2][:] = 0.0
+    out = {}
+    for dloop in (True, False):
+        mg = G.MultiGrid(insts, batched=True, fp32=True)
+        G.setup_lmgc(mg, "jac", red=1e-8, abslimit=1e-50, mixed=mixed, maxit=maxit, dloop=dloop)
+        runs = []
+        for _ in range(2):
+            x, lr = mg.solve_host("mgs", mg.pack(rhs))
+            r = [mg.instance_result("mgs", k) for k in range(len(gens))]
+            runs.append((x, lr.iters, lr.converged,
+                         [(q.iters, q.converged, list(q.last_defect)) for q in r]))
+        out[dloop] = (runs, mg.npdisplay("mgs"))
+        mg.close()
+    (dev, dev_disp), (host, host_disp) = out[True], out[False]
+    assert "loop = device (built)" in dev_disp and "loop = host" in host_disp
+    for (xd, itd, cd, rd), (xh, ith, ch, rh) in zip(dev, host):
+        assert itd == ith and cd == ch and rd == rh
+        assert np.array_equal(xd, xh)
+        assert rd[2][0] == 0 and rd[2][1]
+        assert cd == (maxit == 100)
+
+
+@pytest.mark.gpu
 def test_batched_many_small_instances(G, oracle_mod):
     """64 instances of levels 3..7 (the batched workload's size range, fewer
     instances): every instance meets its own stopping test."""

@@ -306,6 +306,16 @@ struct LsLoopState {
 };
 // flag (device, may be null): a nonzero value ends the loop as an error
 int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, const double *flag, cudaGraphConditionalHandle h);
+// the same on a batched hierarchy: every instance keeps its own convergence
+// (batch.conv_dev), iteration count and last defect; the loop ends when all
+// have converged, at maxit, or on a non-finite defect (bad_k = the lowest
+// such instance, bad_it the iteration)
+struct BatchLoopHead {
+  int it = 0, maxit = 0, ninst = 0, s = 0, bad_k = 0, bad_it = 0, pad[2] = {0, 0};
+  double abs[GMG_MAX_S] = {0};
+};
+int k_batch_loop_test(gmg_mg *mg, BatchLoopHead *hd, int *iters, double *last, const double *reach,
+                      cudaGraphConditionalHandle h);
 int k_add_mixed(gmg_mg *mg, double *x64, int src_prec, const void *c, long long len);  // x64 += c
 // x -= A y (A in the precision of x/y); if acc != null also acc += y
 int k_matmul_minus(gmg_mg *mg, const Level &L, int prec, void *x, const void *y, void *acc);

@@ -2659,6 +2659,54 @@ int k_ls_loop_test(gmg_mg *mg, LsLoopState *st, const double *flag, cudaGraphCon
   return 0;
 }
 
+// the per-instance test of the batched ls loop (the host loop's comparisons,
+// instance by instance); one block
+__global__ void __launch_bounds__(1024) batch_loop_test_kernel(BatchLoopHead *hd, const double *__restrict__ norms,
+                                                               uint8_t *conv, int *iters, double *last,
+                                                               const double *__restrict__ reach,
+                                                               cudaGraphConditionalHandle h) {
+  const int it = hd->it + 1, ni = hd->ninst, s = hd->s;
+  int all = 1;
+  for (int k = threadIdx.x; k < ni; k += blockDim.x) {
+    if (conv[k]) continue;
+    const double *d = norms + (size_t)k * GMG_MAX_S;
+    bool finite = true, below_abs = true, below_reach = true;
+    for (int r = 0; r < s; ++r) {
+      const double v = d[r];
+      finite = finite && isfinite(v);
+      below_abs = below_abs && fabs(v) < fabs(hd->abs[r]);
+      below_reach = below_reach && fabs(v) < fabs(reach[(size_t)k * GMG_MAX_S + r]);
+    }
+    if (!finite) {
+      atomicMin(&hd->bad_k, k);
+      all = 0;
+      continue;
+    }
+    for (int r = 0; r < s; ++r) last[(size_t)k * GMG_MAX_S + r] = d[r];
+    if (below_abs || below_reach) {
+      conv[k] = 1;
+      iters[k] = it;
+    } else {
+      all = 0;
+    }
+  }
+  all = __syncthreads_and(all);
+  if (threadIdx.x == 0) {
+    hd->it = it;
+    const bool bad = hd->bad_k < ni;
+    if (bad) hd->bad_it = it;
+    cudaGraphSetConditional(h, (!bad && !all && it < hd->maxit) ? 1u : 0u);
+  }
+}
+
+int k_batch_loop_test(gmg_mg *mg, BatchLoopHead *hd, int *iters, double *last, const double *reach,
+                      cudaGraphConditionalHandle h) {
+  batch_loop_test_kernel<<<1, 1024, 0, mg->stream>>>(hd, mg->batch.norms_dev, mg->batch.conv_dev, iters, last, reach,
+                                                     h);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 // daxpy, ugblas.cc:2875: x += a y (per component a), one rounding each
 template <class T, int S>
 __global__ void __launch_bounds__(BLK) axpy_kernel(long long n, T *__restrict__ x, const T *__restrict__ y,

@@ -917,6 +917,11 @@ NPLs::~NPLs() {
   if (loop_graph) cudaGraphExecDestroy(loop_graph);
   if (loop_dev) cudaFree(loop_dev);
   if (loop_host) cudaFreeHost(loop_host);
+  if (bhd_dev) cudaFree(bhd_dev);
+  if (bhd_host) cudaFreeHost(bhd_host);
+  if (biters_dev) cudaFree(biters_dev);
+  if (blast_dev) cudaFree(blast_dev);
+  if (breach_dev) cudaFree(breach_dev);
 }
 
 int NPLs::Init(const Args &a) {  // LinearSolverInit, ls.cc:788
@@ -1119,7 +1124,8 @@ int NPLs::batch_norms(gmg_vec *bv) {
 int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) {
   const auto &B = mg->batch;
   const int s = mg->lev[level].s;
-  GMG_CUDA(cudaMemcpyAsync(B.conv_dev, B.conv_host, B.ninst, cudaMemcpyHostToDevice, mg->stream));
+  // on the device loop the flags stay on the device (the loop test sets them)
+  if (norm_to_host) GMG_CUDA(cudaMemcpyAsync(B.conv_dev, B.conv_host, B.ninst, cudaMemcpyHostToDevice, mg->stream));
   if (!mixed) {
     // c below the deepest level is reset by every restriction of the cycle
     if (k_set(mg, cvec->prec, vlev(cvec, level), vlen(mg, level), 0.0)) return 1;
@@ -1133,8 +1139,9 @@ int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int 
     if (k_batch_widen(mg, c64, cvec) || k_batch_finish(mg, GMG_PREC_FP64, bv, xv, GMG_PREC_FP64, c64, true, s))
       return 1;
   }
-  GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
-                           mg->stream));
+  if (norm_to_host)
+    GMG_CUDA(cudaMemcpyAsync(B.norms_host, B.norms_dev, sizeof(double) * B.ninst * GMG_MAX_S, cudaMemcpyDeviceToHost,
+                             mg->stream));
   return 0;
 }
 
@@ -1230,6 +1237,20 @@ int NPLs::build_loop(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am) {
     GMG_CUDA(cudaMalloc(&loop_dev, sizeof(LsLoopState)));
     GMG_CUDA(cudaMallocHost(&loop_host, sizeof(LsLoopState)));
   }
+  const int ni = mg->batch.ninst;
+  if (batched(level) && bloop_n != ni) {
+    if (bhd_dev) cudaFree(bhd_dev);
+    if (bhd_host) cudaFreeHost(bhd_host);
+    if (biters_dev) cudaFree(biters_dev);
+    if (blast_dev) cudaFree(blast_dev);
+    if (breach_dev) cudaFree(breach_dev);
+    GMG_CUDA(cudaMalloc(&bhd_dev, sizeof(BatchLoopHead)));
+    GMG_CUDA(cudaMallocHost(&bhd_host, sizeof(BatchLoopHead)));
+    GMG_CUDA(cudaMalloc(&biters_dev, sizeof(int) * ni));
+    GMG_CUDA(cudaMalloc(&blast_dev, sizeof(double) * ni * GMG_MAX_S));
+    GMG_CUDA(cudaMalloc(&breach_dev, sizeof(double) * ni * GMG_MAX_S));
+    bloop_n = ni;
+  }
   cudaGraph_t g = nullptr;
   GMG_CUDA(cudaGraphCreate(&g, 0));
   auto unavailable = [&](const char *what, cudaError_t e) {
@@ -1258,7 +1279,9 @@ int NPLs::build_loop(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am) {
   norm_to_host = false;
   int rc = iteration(level, xv, bv, Am, &err);
   norm_to_host = true;
-  if (!rc) rc = k_ls_loop_test(mg, loop_dev, iteration_flag(), h);
+  if (!rc)
+    rc = batched(level) ? k_batch_loop_test(mg, bhd_dev, biters_dev, blast_dev, breach_dev, h)
+                        : k_ls_loop_test(mg, loop_dev, iteration_flag(), h);
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(mg->stream, &captured);
   loop_kernels = mg->launches - before;
@@ -1369,6 +1392,45 @@ int NPLs::step_async(int i, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, gm
   return 0;
 }
 
+int NPLs::batch_device_loop(int i0, int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const double *abs_,
+                            const std::vector<double> &reach, int *iters) {
+  auto &B = mg->batch;
+  const int s = mg->lev[level].s, ni = B.ninst;
+  *iters = -1;  // not run: the caller continues on the host
+  if (!loop_graph) {
+    if (build_loop(level, xv, bv, Am)) return 1;
+    if (!loop_graph) return 0;
+  }
+  BatchLoopHead &hd = *bhd_host;
+  hd = BatchLoopHead();
+  hd.it = i0;
+  hd.maxit = maxiter;
+  hd.ninst = ni;
+  hd.s = s;
+  hd.bad_k = ni;
+  for (int r = 0; r < s; ++r) hd.abs[r] = abs_[r];
+  for (int k = 0; k < ni; ++k) B.conv_host[k] = uint8_t(inst_conv[k]);
+  GMG_CUDA(cudaMemcpyAsync(bhd_dev, bhd_host, sizeof(BatchLoopHead), cudaMemcpyHostToDevice, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(B.conv_dev, B.conv_host, ni, cudaMemcpyHostToDevice, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(biters_dev, inst_iters.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(blast_dev, inst_last.data(), sizeof(double) * ni * GMG_MAX_S, cudaMemcpyHostToDevice,
+                           mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(breach_dev, reach.data(), sizeof(double) * ni * GMG_MAX_S, cudaMemcpyHostToDevice,
+                           mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));  // the host vectors above are pageable
+  GMG_CUDA(cudaGraphLaunch(loop_graph, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(bhd_host, bhd_dev, sizeof(BatchLoopHead), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaMemcpyAsync(B.conv_host, B.conv_dev, ni, cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  GMG_CUDA(cudaMemcpy(inst_iters.data(), biters_dev, sizeof(int) * ni, cudaMemcpyDeviceToHost));
+  GMG_CUDA(cudaMemcpy(inst_last.data(), blast_dev, sizeof(double) * ni * GMG_MAX_S, cudaMemcpyDeviceToHost));
+  mg->launches += (long long)(hd.it - i0) * loop_kernels;
+  GMG_CHECK(hd.bad_k >= ni, "ls: defect of instance %d is not finite in iteration %d", hd.bad_k, hd.bad_it);
+  for (int k = 0; k < ni; ++k) inst_conv[k] = B.conv_host[k];
+  *iters = hd.it;
+  return 0;
+}
+
 // LinearSolver on a batched hierarchy: every instance keeps its own first
 // defect, reduction target and convergence test (ls.cc:680-730); converged
 // instances stop updating x while the others iterate.  lr receives the
@@ -1396,6 +1458,10 @@ int NPLs::batch_solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const d
     }
     inst_conv[k] = sc_cmp(&inst_first[k * GMG_MAX_S], abs_, s);
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GMG_CUDA(cudaStreamIsCapturing(mg->stream, &cap));
+  const bool on_device = use_device_loop && use_graph && !loop_unavailable && IterNp->capturable() &&
+                         cap == cudaStreamCaptureStatusNone;
   int i;
   for (i = 0; i < maxiter; ++i) {
     bool all = true;
@@ -1404,6 +1470,14 @@ int NPLs::batch_solver(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, const d
       all = all && inst_conv[k];
     }
     if (all) break;
+    if (on_device && (i > 0 || loop_graph)) {  // the rest of the loop on the device
+      int run = -1;
+      if (batch_device_loop(i, level, xv, bv, Am, abs_, reach, &run)) return 1;
+      if (run >= 0) {
+        i = run;
+        break;
+      }
+    }
     if (step(i, level, xv, bv, Am, lr)) return 1;
     for (int k = 0; k < ni; ++k) {
       if (inst_conv[k]) continue;

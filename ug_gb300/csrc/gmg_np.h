@@ -191,6 +191,14 @@ struct NPLs : NPLinearSolver {
   cudaGraphExec_t loop_graph = nullptr;
   long long loop_kernels = 0;     // kernels per pass of the body, the test included
   LsLoopState *loop_dev = nullptr, *loop_host = nullptr;
+  // batched hierarchies: the per-instance loop state on the device
+  BatchLoopHead *bhd_dev = nullptr, *bhd_host = nullptr;
+  int *biters_dev = nullptr;
+  double *blast_dev = nullptr, *breach_dev = nullptr;
+  int bloop_n = 0;
+  // iterations i0+1.. of batch_solver on the device; *iters = iterations run in all
+  int batch_device_loop(int i0, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
+                        const std::vector<double> &reach, int *iters);
   int build_loop(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A);
   // iterations i0+1.. of Solver on the device; fills lr like the host loop
   int device_loop(int i0, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
