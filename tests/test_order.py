@@ -99,3 +99,44 @@ def test_order_errors(G):
     assert G.order_lex(lev, xyz, "ru", 1.0).tolist() == [0, 1, 2, 3]
     assert G.order_lex(lev, xyz, "ur", 1.0).tolist() == [0, 2, 1, 3]
     assert G.order_lex(lev, xyz, "ld", 1.0).tolist() == [3, 2, 1, 0]
+
+
+@pytest.mark.parametrize("name", ["q1_gs", "el_ilu", "ls_gs"])
+def test_permute_levels_round_trip(G, name):
+    """permute_levels by random permutations and then by their inverses gives
+    the hierarchy back; the permuted level matrix is P A P^T and the permuted
+    transfer is P_f T P_c^T (dense check on the small levels)."""
+    levels = G.levels_from_ugfx(load_golden(name))
+    rng = np.random.default_rng(3)
+    perms = [rng.permutation(lev["n"]) for lev in levels]
+    inv = [np.argsort(p) for p in perms]
+    there = G.permute_levels(levels, perms)
+    back = G.permute_levels(there, inv)
+    for a, b in zip(back, levels):
+        for k in KEYS:
+            if b.get(k) is not None:
+                assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+    s = int(levels[0]["s"])
+
+    def dense(rp, col, val, nr, nc, w):
+        m = np.zeros((nr * w, nc * w))
+        v = np.asarray(val).reshape(-1, w, w)
+        for i in range(nr):
+            for e in range(rp[i], rp[i + 1]):
+                m[i * w:(i + 1) * w, col[e] * w:(col[e] + 1) * w] += v[e]
+        return m
+
+    def blockperm(p, w):
+        return (np.asarray(p)[:, None] * w + np.arange(w)[None, :]).ravel()
+
+    for l in range(min(3, len(levels))):
+        a, t = levels[l], there[l]
+        A = dense(a["rowptr"], a["col"], a["val"], a["n"], a["n"], s)
+        At = dense(t["rowptr"], t["col"], t["val"], t["n"], t["n"], s)
+        q = blockperm(perms[l], s)
+        assert np.array_equal(At, A[np.ix_(q, q)])
+        if l > 0:
+            nc = levels[l - 1]["n"]
+            T = dense(a["prowptr"], a["pcol"], a["pw"], a["n"], nc, 1)
+            Tt = dense(t["prowptr"], t["pcol"], t["pw"], t["n"], nc, 1)
+            assert np.array_equal(Tt, T[np.ix_(perms[l], perms[l - 1])])
