@@ -2,7 +2,7 @@
  * multigrid path (ls + lmgc with jac / gs / ilu smoothers, the standard
  * transfer and the ex base solver) on a flattened hierarchy.
  *
- * TEST INFRASTRUCTURE ONLY.  It is the checker the CUDA path is compared
+ * TEST INFRASTRUCTURE ONLY.  It is the oracle the CUDA path is compared
  * against (tests/, __graft_entry__.smoke, and bench.py's CPU baseline leg);
  * the ug_gb300 product never calls it.  Its own correctness is pinned
  * against golden vectors produced by the UG reference itself

@@ -1,7 +1,7 @@
 """ctypes front end of the C restatement of UG's lmgc path (lmgc_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg as the checker the CUDA path is compared against.
+bench.py's CPU-baseline leg as the oracle the CUDA path is compared against.
 The ug_gb300 product never imports this module.
 
 Also reads the UGFX container written by oracle/ug_export.cc (the UG
