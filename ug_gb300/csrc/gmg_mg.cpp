@@ -1026,6 +1026,17 @@ int gmg_mg_replace_levels(gmg_mg *mg, int from_level, const gmg_level_desc *leve
     if (build_host_level(levels[k], mg->opts.order, H[k], nullptr)) return 1;
     if (build_host_transfer(levels[k], k ? H[k - 1] : below, H[k])) return 1;
   }
+  {  // a locally refined result must fit the surface tables: checked before anything changes
+    bool fine_below_top = false;
+    for (int l = 0; l < from_level && !fine_below_top; ++l)
+      for (uint8_t f : mg->lev[l].h_flags)
+        if (f & F_FINE) { fine_below_top = true; break; }
+    for (int k = 0; k + 1 < count && !fine_below_top; ++k)
+      for (uint8_t f : H[k].flags)
+        if (f & F_FINE) { fine_below_top = true; break; }
+    GMG_CHECK(!fine_below_top || nl <= SURF_MAX_LEVELS, "a locally refined hierarchy has at most %d levels",
+              SURF_MAX_LEVELS);
+  }
   std::vector<Level> fresh(count);
   for (int k = 0; k < count; ++k)
     if (upload_level(H[k], k ? H[k - 1].n : below.n, mg->opts.fp32_copy != 0, fresh[k])) {
