@@ -140,3 +140,23 @@ def test_permute_levels_round_trip(G, name):
             T = dense(a["prowptr"], a["pcol"], a["pw"], a["n"], nc, 1)
             Tt = dense(t["prowptr"], t["pcol"], t["pw"], t["n"], nc, 1)
             assert np.array_equal(Tt, T[np.ix_(perms[l], perms[l - 1])])
+
+
+@pytest.mark.parametrize("config", ["ru", "ur", "ld", "dl", "ruf", "bdl", "fru", "lub"])
+def test_order_lex_is_a_lexicographic_sort(G, config):
+    """On a lattice (distinct positions, spacing far above the 1e-3 tolerance)
+    order.lex is numpy's lexicographic sort with the last config letter as
+    the major key and each letter's direction."""
+    dim = len(config)
+    rng = np.random.default_rng(len(config) + ord(config[0]))
+    side = 5
+    pts = np.stack(np.meshgrid(*[np.arange(side)] * dim, indexing="ij"), -1).reshape(-1, dim).astype(float)
+    pts = pts[rng.permutation(len(pts))] * 0.25
+    n = len(pts)
+    lev = {"n": n, "s": 1, "rowptr": np.arange(n + 1), "col": np.arange(n), "val": np.ones(n),
+           "vclass": np.full(n, 3), "vnclass": np.full(n, 3), "skip": np.zeros(n)}
+    axis = {"r": (0, 1), "l": (0, -1), "u": (1, 1), "d": (1, -1), "f": (2, 1), "b": (2, -1)}
+    keys = [axis[c][1] * pts[:, axis[c][0]] for c in config]  # np.lexsort: last key is the primary one
+    want = np.lexsort(keys)
+    got = G.order_lex(lev, pts, config, 1.0)
+    assert got.tolist() == want.tolist()
