@@ -160,3 +160,32 @@ def test_order_lex_is_a_lexicographic_sort(G, config):
     want = np.lexsort(keys)
     got = G.order_lex(lev, pts, config, 1.0)
     assert got.tolist() == want.tolist()
+
+
+@pytest.mark.parametrize("name", ["q1_gs", "p1_gs", "el_ilu"])
+def test_order_bw_is_breadth_first(G, name):
+    """order.bw's order is a breadth-first order of the matrix graph: graph
+    distances from its first vector never decrease along it, and its first
+    vector is the one a breadth-first sweep from the level's first vector
+    reaches last."""
+    for lev in G.levels_from_ugfx(load_golden(name)):
+        n = lev["n"]
+        rp, col = np.asarray(lev["rowptr"]), np.asarray(lev["col"])
+        perm, _ = G.order_bw(lev)
+
+        def bfs(src):
+            dist = np.full(n, -1)
+            dist[src] = 0
+            q, h = [src], 0
+            while h < len(q):
+                v = q[h]; h += 1
+                for w in col[rp[v]:rp[v + 1]]:
+                    if dist[w] < 0:
+                        dist[w] = dist[v] + 1
+                        q.append(w)
+            return dist, q
+
+        _, first_sweep = bfs(0)
+        assert perm[0] == first_sweep[-1]
+        dist, _ = bfs(perm[0])
+        assert np.all(np.diff(dist[perm]) >= 0)
