@@ -189,3 +189,20 @@ def test_order_bw_is_breadth_first(G, name):
         assert perm[0] == first_sweep[-1]
         dist, _ = bfs(perm[0])
         assert np.all(np.diff(dist[perm]) >= 0)
+
+
+@pytest.mark.parametrize("name", sorted(ORDERED))
+def test_order_levels_reproduces_ug(G, name):
+    """order_levels (UG's `npexecute ord $a`) with the default radius (half
+    the extent of level 0) gives UG's reordered hierarchy."""
+    base_name, _ = ORDERED[name]
+    fx, base = load_golden(name), load_golden(base_name)
+    levels = G.levels_from_ugfx(base)
+    xyz = [_xyz(base, l) for l in range(len(levels))]
+    got, perms = G.order_levels(levels, str(fx["order"]), xyz=xyz)
+    for a, b in zip(got, G.levels_from_ugfx(fx)):
+        for k in KEYS:
+            if b.get(k) is not None:
+                assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), (name, k)
+    with pytest.raises(G.GmgError):
+        G.order_levels(levels, "so")

@@ -315,6 +315,29 @@ def lex_inv_mesh_size(level: int, n_level0: int, dim: int, radius: float) -> flo
     return float(2 ** level) * float(n_level0) ** (1.0 / dim) / radius
 
 
+def order_levels(levels: list[dict], order: str, xyz=None, radius: float | None = None):
+    """UG's `npexecute <order numproc> $a` on a flattened hierarchy: every
+    level renumbered by order.bw (``order="bw"``) or order.lex
+    (``order="lex:<config>"``, positions ``xyz[l]`` per level; the domain
+    radius defaults to half the largest extent of level 0).  Returns
+    (levels in the new order, the permutation of every level)."""
+    if order == "bw":
+        perms = [order_bw(d)[0] for d in levels]
+    elif order.startswith("lex:"):
+        config = order[4:]
+        dim = len(config)
+        if xyz is None:
+            raise GmgError("order lex needs the vector positions of every level")
+        pos = [np.asarray(x, np.float64).reshape(int(d["n"]), -1)[:, :dim] for x, d in zip(xyz, levels)]
+        if radius is None:
+            radius = 0.5 * float(np.max(pos[0].max(axis=0) - pos[0].min(axis=0)))
+        perms = [order_lex(d, pos[l], config, lex_inv_mesh_size(l, int(levels[0]["n"]), dim, radius))
+                 for l, d in enumerate(levels)]
+    else:
+        raise GmgError(f"unknown order {order!r} (bw or lex:<config>)")
+    return permute_levels(levels, perms), perms
+
+
 def permute_vector(v, perm, s: int = 1) -> np.ndarray:
     """A level vector (s components per row) in the order perm."""
     return np.asarray(v).reshape(-1, s)[np.asarray(perm)].ravel()
