@@ -94,6 +94,13 @@ def lib():
         L.orc_ls_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_cg_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_bcgs_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
+        L.orc_cube_create.argtypes = [C.c_int, C.c_ulonglong, C.c_double, C.c_double, C.c_int, C.POINTER(P)]
+        L.orc_cube_create.restype = C.c_int
+        L.orc_cube_level.argtypes = [P, C.c_int, C.POINTER(_Level), C.POINTER(C.POINTER(C.c_double))]
+        L.orc_cube_level.restype = C.c_int
+        L.orc_cube_rhs.argtypes = [P, C.POINTER(C.c_int)]
+        L.orc_cube_rhs.restype = C.POINTER(C.c_double)
+        L.orc_cube_destroy.argtypes = [P]
         L.orc_fullrefinelevel.argtypes = [P]
         L.orc_fullrefinelevel.restype = C.c_int
         L.orc_cg_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
@@ -107,6 +114,47 @@ def lib():
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def cube_levels(nref: int, seed: int, corr: float = 0.1, var: float = 1.0, threads: int | None = None):
+    """The 3D P1 diffusion workload's hierarchy from the oracle's own
+    generator (cube_gen.c): unit cube, six Kuhn tetrahedra refined nref times,
+    k = exp(g) per element, seeded right-hand side.  Returns (levels, rhs,
+    xyz): level dicts as Hierarchy takes them, the finest level's right-hand
+    side and every level's node coordinates (n x 3)."""
+    L = lib()
+    h = C.c_void_p()
+    nt = threads if threads else max(1, min(16, os.cpu_count() or 1))
+    rc = L.orc_cube_create(nref, seed, corr, var, nt, C.byref(h))
+    if rc:
+        raise RuntimeError(f"orc_cube_create failed ({rc})")
+    try:
+        levels, xyzs = [], []
+        for l in range(nref + 1):
+            lv = _Level()
+            xp = C.POINTER(C.c_double)()
+            assert L.orc_cube_level(h, l, C.byref(lv), C.byref(xp)) == 0
+            n = lv.n
+            nnz = np.ctypeslib.as_array(C.cast(lv.rowptr, C.POINTER(C.c_int)), (n + 1,))[-1]
+
+            def arr(ptr, cnt, t):
+                return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(t)), (int(cnt),)).copy()
+
+            d = {"n": n, "s": 1, "rowptr": arr(lv.rowptr, n + 1, C.c_int), "col": arr(lv.col, nnz, C.c_int),
+                 "val": arr(lv.val, nnz, C.c_double), "vclass": arr(lv.vclass, n, C.c_int),
+                 "vnclass": arr(lv.vnclass, n, C.c_int), "skip": arr(lv.skip, n, C.c_int)}
+            if l > 0:
+                d["prowptr"] = arr(lv.prowptr, n + 1, C.c_int)
+                d["pcol"] = arr(lv.pcol, d["prowptr"][-1], C.c_int)
+                d["pw"] = arr(lv.pw, d["prowptr"][-1], C.c_double)
+            levels.append(d)
+            xyzs.append(np.ctypeslib.as_array(xp, (n * 3,)).copy().reshape(n, 3))
+        ln = C.c_int()
+        rp = L.orc_cube_rhs(h, C.byref(ln))
+        rhs = np.ctypeslib.as_array(rp, (ln.value,)).copy()
+    finally:
+        L.orc_cube_destroy(h)
+    return levels, rhs, xyzs
 
 
 class Hierarchy:

@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures in this directory from the UG reference.
 
-Builds the reference with oracle/Makefile (needs the UG 3.12.1 sources at
-$REF, default /root/reference), runs oracle/_ref/ug_export{2d,3d} for each
+Builds the reference with oracle/Makefile (needs the UG 3.12.1 sources: set
+the environment variable REF to that tree), runs oracle/_ref/ug_export{2d,3d} for each
 case below and stores every record as a compressed .npz.  Each fixture holds
 the hierarchy exactly as UG's grid manager and assembly produced it, the
 known-answer vectors of UG's kernels on the finest level, and UG's own ls +
@@ -56,6 +56,8 @@ CASES = {
 
 def main():
     env = dict(os.environ)
+    if not env.get("REF"):
+        raise SystemExit("set REF to the UG 3.12.1 source tree")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"], check=True, env=env)
     only = set(sys.argv[1:])  # optional: the names to regenerate
     with tempfile.TemporaryDirectory() as tmp:
