@@ -38,9 +38,10 @@ RED = 1e-8
 
 def workload_config(extra=None):
     c = {"workload": "3D P1 diffusion k=exp(g) (corr 0.1, var 1), unit cube 6 Kuhn tets red x6, "
-                     "65^3=274625 unknowns, lmgc V(2,2) multicolour GS, base level 0, ls to 1e-8 rel defect",
-         "unknowns": 274625, "nnz": 4018753, "levels": NREF + 1, "smoother": "gs (multicolour)",
-         "l2": "flushed between timed steps (256 MB read); the hierarchy itself (~60 MB FP64) fits in L2"}
+                     "65^3=274625 unknowns, lmgc V(2,2) Gauss-Seidel, base level 0, ls to 1e-8 rel defect",
+         "unknowns": 274625, "nnz": 4018753, "levels": NREF + 1, "smoother": "gs",
+         "l2": "GPU arm: L2 flushed between timed steps (256 MB read); the hierarchy itself (~60 MB FP64) "
+               "fits in L2"}
     if extra:
         c.update(extra)
     return c
@@ -149,49 +150,56 @@ def profiled_traffic(kind="gs"):
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores.
 
-    The UG reference itself cannot run here (its sources are not present on
-    this host, and it does not build for aarch64 from this tree), so the
-    oracle port -- the C restatement of UG's ls + lmgc, pinned bit-for-bit
-    to UG's kernels and solves -- runs the same workload, one independent
-    solve per host thread, each step a batch of concurrent solves."""
+    UG itself cannot run on the GPU host (its sources are not there, and its
+    build needs them), so the oracle port -- the C restatement of UG's ls +
+    lmgc, pinned bit-for-bit to UG's kernels and solves -- solves the same
+    workload.  The hierarchy comes from the oracle's own generator
+    (oracle/cube_gen.c, bitwise equal to the one the GPU arm uses), so this
+    process loads nothing but the oracle library.  Each step runs one
+    complete solve to 1e-8 per host thread, all threads at once; the rate is
+    the solves of a step over its wall time.  The oracle sweeps the rows in
+    the generator's VECTOR-list order (UG's l_lgs), the GPU arm in
+    multicolour order: the same smoother, a different order (the `ordering`
+    key), both converging in 13 iterations."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import ctypes  # noqa: F401
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    import ug_gb300 as G
     oracle.build()
-    gen = G.Generator(G.Generator.DIFFUSION3D, NREF, seed=SEED, corr=CORR, var=VAR)
-    # UG's own order: the VECTOR list (lexicographic here), as l_lgs sweeps it
-    H = oracle.Hierarchy(gen.levels())
-    rhs = gen.rhs
+    levels, rhs, _ = oracle.cube_levels(NREF, SEED, CORR, VAR)
+    H = oracle.Hierarchy(levels)
     threads = max(1, min(os.cpu_count() or 1, 16))
+    results = [None] * threads
 
-    # warm-up: one complete solve gives the iteration count of the workload
-    t0 = time.perf_counter()
-    _, iters, conv, _ = H.ls_solve(rhs, smoother="gs", baselevel=0, red=RED)
-    t_full = time.perf_counter() - t0
-    # each timed step: `threads` concurrent solves of one ls iteration (defect,
-    # norm, one V-cycle), scaled by the iteration count of a complete solve
-    times = []
-    for _ in range(args.steps):
+    def solve(k):
+        _, it, conv, hist = H.ls_solve(rhs, smoother="gs", baselevel=0, red=RED, abslimit=1e-50)
+        results[k] = (it, conv, hist[-1, 0] / hist[0, 0])
+
+    def step():
+        th = [threading.Thread(target=solve, args=(k,)) for k in range(threads)]
         t0 = time.perf_counter()
-        th = [threading.Thread(target=lambda: H.ls_solve(rhs, smoother="gs", baselevel=0, red=RED, maxit=1))
-              for _ in range(threads)]
         [t.start() for t in th]
         [t.join() for t in th]
-        times.append(time.perf_counter() - t0)
-    per_step = float(np.mean(times)) * iters  # one batch of `threads` complete solves
+        dt = time.perf_counter() - t0
+        assert all(r is not None and r[1] for r in results), "an oracle solve did not converge"
+        return dt
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
+    per_step = float(np.mean(times))
     value = threads / per_step
+    iters = results[0][0]
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-            "config": workload_config({"iterations": iters, "smoother": "gs (UG VECTOR-list order, as l_lgs)"}),
+            "config": workload_config(),
+            "ordering": "VECTOR-list order (lexicographic), as UG's l_lgs sweeps it",
+            "iterations": iters, "final_rel_defect": float(results[0][2]),
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": f"{threads} concurrent FP64 solves (one per thread), each step one ls "
-                                       f"iteration of each, scaled by the {iters} iterations of a complete "
-                                       f"solve (single-thread complete solve: {t_full:.1f} s)"},
+                             "sample": f"each step: {threads} complete FP64 solves to 1e-8 ({iters} iterations "
+                                       f"each), one per host thread, run at once; {args.steps} steps timed"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -600,6 +608,78 @@ def run_serving(args, rank):
     return out
 
 
+# ---------------------------------------------------------------- roofline kernels of the C2 solve
+def c2_roofline(G, mg, stream, flush_l2, reps=20, skip=3):
+    """Roofline of the dominant streaming kernels of the C2 solve, each timed
+    HBM-cold (L2 flushed before every repetition) with CUDA events on the
+    launching stream:
+    * the finest level's smoothing as lmgc runs it (gmg_iter_smooth, 2 FP32
+      Gauss-Seidel steps): per colour one sell_gs_chain_kernel launch per
+      step, then one sell_upper_defect_kernel launch; algorithmic bytes per
+      smoothing = 2 (M + 6 V), M = nnz (4 + 4) + 4 (n + 1) the FP32 matrix
+      stream, V = 4 n a vector (the GS step with fused defect update);
+    * the finest level's dmatmul_minus (sell_spmv_kernel) in FP32 and FP64:
+      nnz (p + 4) + 4 (n + 1) + 3 n q."""
+    import torch
+    top = mg.top
+    n, s, nnz = mg.size(top)
+    nwaves = mg.num_waves(top)
+    for v in ("ry", "rx"):
+        try:
+            mg.vec(v)
+        except G.GmgError:
+            mg.createvector(v)
+    for v in ("ry32", "rx32", "st32", "sb32", "sc32"):
+        try:
+            mg.vec(v)
+        except G.GmgError:
+            mg.createvector(v, prec=G.FP32)
+    b0 = np.linspace(-1.0, 1.0, n * s)
+    mg.upload("sb32", top, b0)
+    mg.dset(top, "sc32", 0.0)
+    algo_smooth = 2 * ((nnz * (4 + 4) + 4 * (n + 1)) + 6 * n * s * 4)
+    launches_smooth = 2 * nwaves + 1
+    algo = {64: nnz * (8 + 4) + (n + 1) * 4 + 3 * n * 8, 32: nnz * (4 + 4) + (n + 1) * 4 + 3 * n * 4}
+
+    def event_ms(fn):
+        ts = []
+        for k in range(reps):
+            if k % 5 == 0:
+                mg.upload("sb32", top, b0)  # keep the defect away from denormals
+            flush_l2()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            if k >= skip:
+                ts.append(a.elapsed_time(b))
+        return float(np.mean(ts))
+
+    sm_ms = event_ms(lambda: mg.iter_smooth("smooth", top, "st32", "sb32", "sc32", 2))
+    kms = {64: event_ms(lambda: mg.dmatmul_minus(top, "rx", "ry")),
+           32: event_ms(lambda: mg.dmatmul_minus(top, "rx32", "ry32"))}
+    peak, peak_kind = measured_peak()
+    ach = algo_smooth / (sm_ms * 1e-3) / 1e9
+    ach32 = algo[32] / (kms[32] * 1e-3) / 1e9
+    ach64 = algo[64] / (kms[64] * 1e-3) / 1e9
+    tr = profiled_traffic("smooth")
+    return {"bound": "hbm",
+            "kernel": f"sell_gs_chain_kernel<float> + sell_upper_defect_kernel<float>: the finest level's "
+                      f"2 Gauss-Seidel smoothing steps as lmgc runs them ({launches_smooth} launches: "
+                      f"{nwaves} colours x 2 steps + 1 defect pass), HBM-cold; per launch",
+            "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind,
+            "traffic": tr, "algorithmic_bytes": algo_smooth / launches_smooth,
+            "launch_ms": sm_ms / launches_smooth, "smoothing_ms": sm_ms,
+            "note": "each colour wave is a dependent gather chain of a few us (latency-bound launches); rows "
+                    "store their lower entries first, so a forward wave streams only those",
+            "spmv_fp32": {"kernel": "sell_spmv_kernel<float> (finest-level dmatmul_minus)",
+                          "achieved": ach32, "frac": ach32 / peak, "algorithmic_bytes": algo[32],
+                          "launch_ms": kms[32], "traffic": profiled_traffic("spmv")},
+            "spmv_fp64": {"achieved": ach64, "frac": ach64 / peak, "algorithmic_bytes": algo[64],
+                          "launch_ms": kms[64]}}
+
+
 # ---------------------------------------------------------------- our arm
 def run_ours(args):
     import torch
@@ -612,6 +692,25 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     import ug_gb300 as G
 
+    # L2 flush between timed steps: READ 256 MB (twice the L2), which leaves
+    # only clean lines behind (a write would leave dirty lines whose
+    # write-back the next timed kernel would pay for)
+    flush = torch.ones(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    sink = torch.empty((), dtype=torch.float32, device="cuda")
+
+    def flush_l2():
+        torch.sum(flush, dim=0, out=sink)
+
+    single = {"c1": lambda: run_c1(args, stream, flush_l2, world, rank),
+              "local": lambda: run_local(args, stream, flush_l2, world, rank),
+              "batched": lambda: run_batched(args, stream, flush_l2, world, rank),
+              "serving": lambda: run_serving(args, rank)}
+    if args.only in single:  # one workload alone (profiling runs)
+        out = single[args.only]()
+        if rank == 0:
+            print(json.dumps({"only": args.only, args.only: out}), flush=True)
+        return
+
     gen = G.Generator(G.Generator.DIFFUSION3D, NREF, seed=SEED, corr=CORR, var=VAR)
     mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True, autotune=True, device=local)
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
@@ -622,14 +721,12 @@ def run_ours(args):
     top = mg.top
     mg.upload("rhs0", top, gen.rhs)
     mg.ls_preprocess("mgs64", top, "sol", "rhs")
-    # L2 flush between timed steps: READ 256 MB (twice the L2), which leaves
-    # only clean lines behind (a write would leave dirty lines whose
-    # write-back the next timed kernel would pay for)
-    flush = torch.ones(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    sink = torch.empty((), dtype=torch.float32, device="cuda")
-
-    def flush_l2():
-        torch.sum(flush, dim=0, out=sink)
+    if args.only == "roofline":  # the roofline kernels alone (profiling runs)
+        roof = c2_roofline(G, mg, stream, flush_l2, reps=args.warmup + args.steps, skip=args.warmup)
+        mg.close()
+        if rank == 0:
+            print(json.dumps({"only": "roofline", "roofline": roof}), flush=True)
+        return
 
     def step(solver):
         lr = G.LResult()
@@ -644,7 +741,7 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    results = {}
+    results, xs = {}, {}
     for solver in ("mgs64", "mgs32"):
         for _ in range(args.warmup):
             step(solver)
@@ -666,6 +763,7 @@ def run_ours(args):
             torch.cuda.synchronize(); barrier()
             wall = time.perf_counter() - t0
         ms = [a.elapsed_time(b) for a, b in ev]
+        xs[solver] = mg.download("sol", top)  # the last timed solve's solution (list order)
         ms_step = reduce_over_ranks(float(np.mean(ms)), "max")
         results[solver] = {"ms_per_step": ms_step, "iters": iters[-1], "launches_per_step": launches / args.steps,
                            "clocks": clk.summary(), "wall_s": wall}
@@ -684,45 +782,11 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t0)
     e2e_ms = reduce_over_ranks(float(np.mean(e2e_t)) * 1e3)
 
-    # roofline of the dominant streaming kernel: the finest level's Gauss-Seidel
-    # colour waves (in the solve as sell_gs_chain_kernel, whose launches also
-    # finish the previous colour's defect rows: ~19 % of the profiled cycle,
-    # profiles/launches_c2.md), measured as one FP32 l_lgs sweep of the finest
-    # level = one sell_gs_kernel launch per colour -- and the finest-level
-    # dmatmul_minus, each HBM-cold, CUDA events on the launching stream
     n, s, nnz = mg.size(top)
-    nwaves_top = mg.num_waves(top)
-    mg.createvector("ry", "rx")
-    mg.createvector("ry32", "rx32", prec=G.FP32)
-    nnz_lower = (nnz - n) // 2  # strictly lower entries (symmetric pattern)
-    # sweep: the lower triangle's values and columns, the inverse diagonal, b, t
-    # written and t gathered once per row (FP32)
-    algo_gs = nnz_lower * (4 + 4) + (n + 1) * 4 + n * 4 * 4
-    algo = {64: nnz * (8 + 4) + (n + 1) * 4 + 3 * n * 8, 32: nnz * (4 + 4) + (n + 1) * 4 + 3 * n * 4}
-
-    def event_ms(fn, reps=20, skip=3):
-        ts = []
-        for k in range(reps):
-            flush_l2()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            torch.cuda.synchronize()
-            if k >= skip:
-                ts.append(a.elapsed_time(b))
-        return float(np.mean(ts))
-
-    gs_ms = event_ms(lambda: mg.l_lgs(top, "rx32", "ry32"))
-    kms = {64: event_ms(lambda: mg.dmatmul_minus(top, "rx", "ry")),
-           32: event_ms(lambda: mg.dmatmul_minus(top, "rx32", "ry32"))}
-    peak, peak_kind = measured_peak()
-    ach_gs = algo_gs / (gs_ms * 1e-3) / 1e9
-    ach32 = algo[32] / (kms[32] * 1e-3) / 1e9
-    ach64 = algo[64] / (kms[64] * 1e-3) / 1e9
+    roof = c2_roofline(G, mg, stream, flush_l2)
 
     # CPU baseline: the oracle port, one FP64 solve on one core, bounded sample
-    cpu = None
+    cpu, accuracy = None, None
     if rank == 0:
         try:
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -734,16 +798,32 @@ def run_ours(args):
             dt = time.perf_counter() - t0
             cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
                    "sample": f"one full FP64 solve of the workload in UG's list order ({it_cpu} iterations, {dt:.1f} s)"}
+            # the timed solutions against FP64: their defect computed by the
+            # oracle in FP64, and their distance to the FP64 solution converged
+            # to 1e-12 (the discrete solution up to 1e-12 of the defect)
+            xt, it_t, conv_t, _ = H.ls_solve(gen.rhs, smoother="gs", baselevel=0, red=1e-12, abslimit=1e-50,
+                                             base_abslimit=1e-30)
+            nb = float(H.nrm2x(top, gen.rhs)[0])
+            accuracy = {"reference": f"oracle FP64 solve to 1e-12 rel defect ({it_t} iterations, converged "
+                                     f"{conv_t}); defects computed by the oracle in FP64"}
+            for key, solver in (("mixed", "mgs32"), ("fp64", "mgs64")):
+                d = H.matmul_minus(top, gen.rhs, xs[solver])
+                accuracy[key] = {"rel_defect_fp64": float(H.nrm2x(top, d)[0]) / nb,
+                                 "rel_error_vs_fp64_solution": float(np.max(np.abs(xs[solver] - xt)) /
+                                                                     np.max(np.abs(xt)))}
+            accuracy["mixed_vs_fp64_gpu"] = float(np.max(np.abs(xs["mgs32"] - xs["mgs64"])) /
+                                                  np.max(np.abs(xs["mgs64"])))
         except Exception as e:  # reported, not fatal
             cpu = {"value": None, "unit": "solves/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
 
     waves = [mg.num_waves(l) for l in range(mg.nlevels)]
     variants = [mg.level_variant(l) for l in range(mg.nlevels)]
     mg.close()
-    c1 = run_c1(args, stream, flush_l2, world, rank)
-    local_c3 = run_local(args, stream, flush_l2, world, rank) if not args.no_local else None
-    batched = run_batched(args, stream, flush_l2, world, rank) if not args.no_batched else None
-    serving = run_serving(args, rank) if not args.no_serving else None
+    rest = args.only != "c2"
+    c1 = run_c1(args, stream, flush_l2, world, rank) if rest else None
+    local_c3 = run_local(args, stream, flush_l2, world, rank) if rest and not args.no_local else None
+    batched = run_batched(args, stream, flush_l2, world, rank) if rest and not args.no_batched else None
+    serving = run_serving(args, rank) if rest and not args.no_serving else None
 
     if rank == 0:
         r32, r64 = results["mgs32"], results["mgs64"]
@@ -753,33 +833,24 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-in-f64 (mixed); f64 reported beside",
             "data": "synthetic (seeded)",
-            "config": workload_config({"iterations_mixed": r32["iters"], "iterations_fp64": r64["iters"],
-                                       "parallelism": "replicas" if world > 1 else "1 GPU",
-                                       "gs_waves_per_level": waves,
-                                       "kernel_variants_per_level (autotuned)": variants,
-                                       "launches_per_solve": r32["launches_per_step"]}),
+            "config": workload_config(),
+            "ordering": "multicolour (DSATUR colouring of every level)",
+            "run": {"iterations_mixed": r32["iters"], "iterations_fp64": r64["iters"],
+                    "parallelism": "replicas" if world > 1 else "1 GPU",
+                    "gs_waves_per_level": waves,
+                    "kernel_variants_per_level (autotuned)": variants,
+                    "launches_per_solve": r32["launches_per_step"]},
             "fp64": {"value": whole_job_rate(1, r64["ms_per_step"], world), "unit": "solves/s",
                      "ms_per_step": r64["ms_per_step"],
                      "iterations": r64["iters"]},
             "mixed_over_fp64": r64["ms_per_step"] / r32["ms_per_step"],
             "e2e": {"value": whole_job_rate(1, e2e_ms, world), "unit": "solves/s", "h2d_bytes_per_step": int(n * s * 8),
                     "d2h_bytes_per_step": int(n * s * 8), "ms_per_step": e2e_ms},
-            "roofline": {"bound": "hbm", "kernel": f"sell_gs_kernel<float> (finest-level Gauss-Seidel sweep, "
-                                                   f"{nwaves_top} colour launches, HBM-cold; per launch)",
-                         "achieved": ach_gs, "peak": peak, "unit": "GB/s", "frac": ach_gs / peak,
-                         "peak_kind": peak_kind, "traffic": profiled_traffic("gs"),
-                         "algorithmic_bytes": algo_gs / nwaves_top, "launch_ms": gs_ms / nwaves_top,
-                         "note": "latency-bound: each colour wave is a dependent gather chain of a few us; "
-                                 "the solve runs the same waves as sell_gs_chain_kernel (~19% of the profiled "
-                                 "cycle) next to the one-CTA fused coarse cycle (~15%, shared-memory latency)",
-                         "spmv_fp32": {"kernel": "sell_spmv_kernel<float> (finest-level dmatmul_minus)",
-                                       "achieved": ach32, "frac": ach32 / peak, "algorithmic_bytes": algo[32],
-                                       "launch_ms": kms[32], "traffic": profiled_traffic("spmv")},
-                         "spmv_fp64": {"achieved": ach64, "frac": ach64 / peak, "algorithmic_bytes": algo[64],
-                                       "launch_ms": kms[64]}},
+            "roofline": roof,
             "gpu_launches": int(r32["launches_per_step"] * args.steps),
             "clocks": r32["clocks"],
             "cpu_baseline": cpu,
+            "accuracy": accuracy,
             "config1": c1,
             "local_refinement": local_c3,
             "batched": batched,
@@ -801,6 +872,10 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH_N, help="instances of the batched workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests of the serving stream")
+    ap.add_argument("--only", default="all", choices=["all", "c2", "roofline", "c1", "local", "batched", "serving"],
+                    help="run one workload alone and print its JSON (profiling runs); c2: the headline solve "
+                         "without the other workloads; roofline: the C2 roofline kernels only, warmup + steps "
+                         "repetitions each")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

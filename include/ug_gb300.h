@@ -162,6 +162,11 @@ int gmg_np_display(gmg_np *np, char *buf, int buflen);
 int gmg_iter_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result);
 int gmg_iter_iter(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result);
 int gmg_iter_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
+/* lmgc's smoothing loop on one level (iter.cc:7811-7816 pre, 7903-7906 post):
+ * `steps` times { t = Iter(b) (b -= A t); c += t }, as lmgc runs it: with
+ * unit damping on a multicolour-ordered level the Gauss-Seidel steps are
+ * chained (the defect stays implicit between steps, b is written once). */
+int gmg_iter_smooth(gmg_np *np, int level, gmg_vec *t, gmg_vec *b, gmg_mat *A, gmg_vec *c, int steps, int *result);
 
 /* NP_TRANSFER (np/procs/transfer.h:79-166) */
 int gmg_transfer_preprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
@@ -227,7 +232,8 @@ int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_
  * a fixed array inside the library (about 20 KB per device, held until the
  * process exits); s above GMG_MAX_S is rejected.  The first call on a device
  * looks up that array's address with the device current: make it before any
- * stream capture.  All calls share the array, so calls that overlap on the
+ * stream capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset it is stale, so do not call this again in that process.  All calls share the array, so calls that overlap on the
  * GPU race; order them on one stream.  Enqueued on `stream` (cudaStream_t). */
 int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev, void *stream);
 

@@ -197,6 +197,36 @@ def test_full_size_p1_diffusion_gs(G, oracle_mod):
     mg.close()
 
 
+def test_full_size_p1_diffusion_mixed(G, oracle_mod):
+    """The benchmarked solve itself: 3D P1 diffusion 65^3 (274,625 unknowns,
+    k = exp(g), seed 2026), multicolour GS V(2,2), the FP32 V-cycle inside FP64
+    iterative refinement to 1e-8, autotuned kernels, as bench.py runs it.
+    Checked in FP64 by the oracle on the same (reordered) hierarchy: the
+    solution meets the stopping test (FP64 defect <= 1e-8 of the first), takes
+    the FP64 solve's iteration count +-1, and is within 1e-6 (relative,
+    max-norm) of the FP64 solution converged to 1e-12."""
+    gen = G.Generator(1, 6, seed=2026, corr=0.1, var=1.0)
+    levels = gen.levels()
+    mg = G.MultiGrid(levels, order=G.ORDER_COLOR, fp32=True, autotune=True)
+    G.setup_lmgc(mg, "gs", baselevel=0, red=1e-8, abslimit=1e-50)
+    mg.npcreate("mgs32", "linear_solver.gls")
+    mg.npinit("mgs32", "$A MAT $x sol $b rhs $red 1e-8 $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    x32, lr32 = mg.solve_host("mgs32", gen.rhs)
+    x32b, _ = mg.solve_host("mgs32", gen.rhs)  # a second solve on the warm hierarchy (graph replay)
+    H = oracle_mod.Hierarchy(permuted_levels(levels, mg))
+    perm = mg.order(mg.top)
+    b = gen.rhs[perm]
+    _, it8, conv8, _ = H.ls_solve(b, smoother="gs", baselevel=0, red=1e-8, abslimit=1e-50)
+    xt, _, convt, _ = H.ls_solve(b, smoother="gs", baselevel=0, red=1e-12, abslimit=1e-50, base_abslimit=1e-30)
+    mg.close()
+    xtl = np.empty_like(xt); xtl[perm] = xt
+    assert lr32.converged and conv8 and convt and abs(lr32.iters - it8) <= 1
+    assert np.array_equal(x32, x32b)
+    d = H.matmul_minus(6, b, x32[perm])
+    assert H.nrm2x(6, d)[0] <= 1.0000001e-8 * H.nrm2x(6, b)[0]
+    assert rel(x32, xtl) <= 1e-6
+
+
 MID = [  # generator kind, nref, smoother, baselevel, var
     (0, 6, "jac", 2, 0.0), (0, 6, "gs", 2, 0.0), (0, 6, "ilu", 2, 0.0),
     (1, 4, "gs", 0, 1.0), (1, 4, "ilu", 0, 1.0), (1, 4, "jac", 0, 1.0),

@@ -8,8 +8,9 @@ kernel's scratch lives in a fixed device array inside the library.  This test
 calls that entry point through the C ABI on buffers the caller owns and
 compares it with the library's ordinary entry point (gmg_dnrm2x, which uses
 the multigrid's allocated scratch) on two calls in a row, for one and two
-components per row; it also checks that a size beyond the fixed scratch is
-rejected with an error instead of being run.
+components per row, and with numpy for three and eight; it also checks that
+a size beyond the fixed scratch is rejected with an error instead of being
+run.
 
 Collected last (file name) so that a run stopping at the first failure has
 already run every other test; it passes alone in a fresh process as well.
@@ -51,6 +52,19 @@ def test_static_scratch_norms_match_dnrm2x():
             assert np.allclose(got, ref, rtol=1e-12, atol=0.0), (got, ref)
             assert np.allclose(got, np.sqrt((x.reshape(-1, s) ** 2).sum(axis=0)), rtol=1e-12, atol=0.0)
         mg.close()
+    # three and eight components per row (the largest the scratch holds) on
+    # synthetic device data, two calls in a row each
+    for s in (3, 8):
+        n = 40_000 + s
+        for _call in range(2):
+            x = rng.uniform(-1.0, 1.0, n * s)
+            xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+            out = torch.full((s,), -1.0, dtype=torch.float64, device="cuda")
+            rc = f(xd.data_ptr(), n, s, out.data_ptr(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+            assert rc == 0, lib.gmg_last_error()
+            torch.cuda.synchronize()
+            got = out.cpu().numpy()
+            assert np.allclose(got, np.sqrt((x.reshape(-1, s) ** 2).sum(axis=0)), rtol=1e-12, atol=0.0), (s, got)
     # more components than the fixed scratch holds: rejected, nothing launched
     out = torch.zeros(16, dtype=torch.float64, device="cuda")
     xd = torch.zeros(16 * 9, dtype=torch.float64, device="cuda")

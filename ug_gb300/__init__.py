@@ -88,7 +88,7 @@ def lib(build_if_missing: bool = True):
         "gmg_np_execute": ([P, C.c_char_p, C.c_char_p], I), "gmg_np_by_name": ([P, C.c_char_p], P),
         "gmg_np_display": ([P, C.c_char_p, I], I),
         "gmg_iter_preprocess": ([P, I, P, P, P, P, P], I), "gmg_iter_iter": ([P, I, P, P, P, P], I),
-        "gmg_iter_postprocess": ([P, I, P, P, P, P], I),
+        "gmg_iter_postprocess": ([P, I, P, P, P, P], I), "gmg_iter_smooth": ([P, I, P, P, P, P, I, P], I),
         "gmg_transfer_preprocess": ([P, P, I, P, P, P, P], I),
         "gmg_transfer_restrict_defect": ([P, I, P, P, P, P, P], I),
         "gmg_transfer_interpolate_correction": ([P, I, P, P, P, P, P], I),
@@ -612,6 +612,13 @@ class MultiGrid:
         res = C.c_int()
         if lib().gmg_iter_iter(self.np(obj), level, self.vec(c), self.vec(b), self.mat(A), C.byref(res)):
             _err(f"{obj} Iter")
+
+    def iter_smooth(self, obj, level, t, b, c, steps, A="MAT"):
+        """lmgc's smoothing loop: `steps` times t = Iter(b), c += t."""
+        res = C.c_int()
+        if lib().gmg_iter_smooth(self.np(obj), level, self.vec(t), self.vec(b), self.mat(A), self.vec(c), steps,
+                                 C.byref(res)):
+            _err(f"{obj} smoothing steps")
 
     def iter_postprocess(self, obj, level, x, b, A="MAT"):
         res = C.c_int()

@@ -133,6 +133,11 @@ struct Level {
   int *sell_col = nullptr;
   double *sell_v64 = nullptr;
   float *sell_v32 = nullptr;
+  // each row stores the diagonal, then its strictly lower blocks (sell_nl[i]
+  // of them), then the upper ones; sell_split: every count fits a byte
+  uint8_t *sell_nl = nullptr;
+  bool sell_split = false;
+  std::vector<int> h_sell_pos;  // sliced-ELLPACK entry of every CSR entry (processing order)
   // the forward schedule's wavefronts are contiguous row ranges (multicolour order)
   bool waves_contiguous = false;
   // subdomain order (GMG_ORDER_DOMAIN): rows 0..dom_nint are the interiors of

@@ -98,6 +98,43 @@ struct SellRow {
   }
 };
 
+// entries kb..ke-1 of sliced-ELLPACK row i (e0 = entry kb, w = ke - kb); the
+// first P held in registers.  Rows of a split level (Level::sell_split) store
+// the diagonal, their sell_nl[i] strictly lower blocks, then the upper ones:
+// part 0 = all off-diagonal entries, 1 = the lower ones, 2 = the upper ones
+// and the padding.  Unsplit levels keep every off-diagonal entry in each part
+// (the kernels test the column).
+template <class T, int S, int P_>
+struct SellPart {
+  static constexpr int P = P_;
+  int e0, w;
+  int col[P > 0 ? P : 1];
+  T val[P > 0 ? P : 1][S * S];
+  __device__ __forceinline__ void load(int i, int part, const int *__restrict__ sptr, const uint8_t *__restrict__ nl,
+                                       const int *__restrict__ scol, const T *__restrict__ sval) {
+    const int base = __ldg(sptr + (i >> 5));
+    const int wt = (__ldg(sptr + (i >> 5) + 1) - base) >> 5;
+    int kb = 1, ke = wt;
+    if (nl && part) {
+      const int m = 1 + __ldg(nl + i);
+      if (part == 1) ke = m;
+      else kb = m;
+    }
+    w = ke - kb;
+    e0 = base + (i & 31) + 32 * kb;
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      col[k] = 0;
+      if (k < w) {
+        const int e = e0 + 32 * k;
+        col[k] = __ldg(scol + e);
+#pragma unroll
+        for (int q = 0; q < S * S; ++q) val[k][q] = __ldg(sval + (size_t)e * (S * S) + q);
+      }
+    }
+  }
+};
+
 template <typename... KP, typename... A>
 inline void pdl_launch(gmg_mg *mg, void (*kern)(KP...), dim3 grid, dim3 block, A &&...args) {
   cudaLaunchConfig_t cfg = {};
@@ -333,16 +370,17 @@ __global__ void __launch_bounds__(BLK) sell_spmv_kernel(int n, const int *__rest
 // and the padding (j == i) are skipped.
 template <class T, int S, bool ALL_ACTIVE, int PN>
 __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int *__restrict__ sptr,
-                                                      const int *__restrict__ scol, const T *__restrict__ sval,
-                                                      const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
-                                                      const T *__restrict__ b, T *__restrict__ t) {
+                                                      const uint8_t *__restrict__ nl, const int *__restrict__ scol,
+                                                      const T *__restrict__ sval, const T *__restrict__ dinv,
+                                                      const uint8_t *__restrict__ flags, const T *__restrict__ b,
+                                                      T *__restrict__ t) {
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1) return;
   const bool act = ALL_ACTIVE || (__ldg(flags + i) & F_ACTIVE);
-  SellRow<T, S, PN> R;
+  SellPart<T, S, PN> R;
   T D[S * S];
   if (act) {
-    R.load(i, sptr, scol, sval);
+    R.load(i, 1, sptr, nl, scol, sval);
 #pragma unroll
     for (int q = 0; q < S * S; ++q) D[q] = __ldg(dinv + (size_t)i * S * S + q);
   }
@@ -356,7 +394,7 @@ __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int 
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = b[(size_t)i * S + r];
 #pragma unroll
-  for (int k = 1; k < PN; ++k) {
+  for (int k = 0; k < PN; ++k) {
     if (k < R.w && R.col[k] < i) {
 #pragma unroll
       for (int c = 0; c < S; ++c) {
@@ -366,9 +404,9 @@ __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int 
       }
     }
   }
-  int e = R.e0 + 32 * (PN > 1 ? PN : 1);
+  int e = R.e0 + 32 * (PN > 0 ? PN : 0);
 #pragma unroll 4
-  for (int k = PN > 1 ? PN : 1; k < R.w; ++k, e += 32) {
+  for (int k = PN > 0 ? PN : 0; k < R.w; ++k, e += 32) {
     const int j = __ldg(scol + e);
     if (j >= i) continue;
     const T *m = sval + (size_t)e * (S * S);
@@ -400,14 +438,15 @@ __global__ void __launch_bounds__(BLK) sell_gs_kernel(int r0, int r1, const int 
 // all-ACTIVE levels, unit damping and colour-contiguous waves.
 template <class T, int S, bool FIRST, int PN>
 __global__ void __launch_bounds__(BLK) sell_gs_chain_kernel(int r0, int r1, const int *__restrict__ sptr,
+                                                            const uint8_t *__restrict__ nl,
                                                             const int *__restrict__ scol, const T *__restrict__ sval,
                                                             const T *__restrict__ dinv, const T *__restrict__ b,
                                                             T *__restrict__ t, T *__restrict__ c) {
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1) return;
-  SellRow<T, S, PN> R;
+  SellPart<T, S, PN> R;
   T D[S * S];
-  R.load(i, sptr, scol, sval);
+  R.load(i, FIRST ? 1 : 0, sptr, nl, scol, sval);
 #pragma unroll
   for (int q = 0; q < S * S; ++q) D[q] = __ldg(dinv + (size_t)i * S * S + q);
   pdl_wait_then_trigger();
@@ -415,7 +454,7 @@ __global__ void __launch_bounds__(BLK) sell_gs_chain_kernel(int r0, int r1, cons
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = FIRST ? b[(size_t)i * S + r] : T(0);
 #pragma unroll
-  for (int k = 1; k < PN; ++k) {
+  for (int k = 0; k < PN; ++k) {
     if (k < R.w && (FIRST ? R.col[k] < i : R.col[k] != i)) {
 #pragma unroll
       for (int cc = 0; cc < S; ++cc) {
@@ -425,9 +464,9 @@ __global__ void __launch_bounds__(BLK) sell_gs_chain_kernel(int r0, int r1, cons
       }
     }
   }
-  int e = R.e0 + 32 * (PN > 1 ? PN : 1);
+  int e = R.e0 + 32 * (PN > 0 ? PN : 0);
 #pragma unroll 4
-  for (int k = PN > 1 ? PN : 1; k < R.w; ++k, e += 32) {
+  for (int k = PN > 0 ? PN : 0; k < R.w; ++k, e += 32) {
     const int j = __ldg(scol + e);
     if (FIRST ? j >= i : j == i) continue;
     const T *m = sval + (size_t)e * (S * S);
@@ -451,19 +490,20 @@ __global__ void __launch_bounds__(BLK) sell_gs_chain_kernel(int r0, int r1, cons
 // b = -U t: the defect after the last chained step (entries j > i)
 template <class T, int S, int PN>
 __global__ void __launch_bounds__(BLK) sell_upper_defect_kernel(int n, const int *__restrict__ sptr,
+                                                                const uint8_t *__restrict__ nl,
                                                                 const int *__restrict__ scol,
                                                                 const T *__restrict__ sval, const T *__restrict__ t,
                                                                 T *__restrict__ b) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  SellRow<T, S, PN> R;
-  R.load(i, sptr, scol, sval);
+  SellPart<T, S, PN> R;
+  R.load(i, 2, sptr, nl, scol, sval);
   pdl_wait_then_trigger();
   T s[S];
 #pragma unroll
   for (int r = 0; r < S; ++r) s[r] = T(0);
 #pragma unroll
-  for (int k = 1; k < PN; ++k) {
+  for (int k = 0; k < PN; ++k) {
     if (k < R.w && R.col[k] > i) {
 #pragma unroll
       for (int cc = 0; cc < S; ++cc) {
@@ -473,9 +513,9 @@ __global__ void __launch_bounds__(BLK) sell_upper_defect_kernel(int n, const int
       }
     }
   }
-  int e = R.e0 + 32 * (PN > 1 ? PN : 1);
+  int e = R.e0 + 32 * (PN > 0 ? PN : 0);
 #pragma unroll 4
-  for (int k = PN > 1 ? PN : 1; k < R.w; ++k, e += 32) {
+  for (int k = PN > 0 ? PN : 0; k < R.w; ++k, e += 32) {
     const int j = __ldg(scol + e);
     if (j <= i) continue;
     const T *m = sval + (size_t)e * (S * S);
@@ -2280,21 +2320,22 @@ int k_jac_step(gmg_mg *mg, const Level &L, int prec, void *bout, const void *bin
 template <class T, int S>
 int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
   const T *sv = sell_val<T>(L), *dinv = dinv_of<T>(L);
+  const uint8_t *nl = L.sell_split ? L.sell_nl : nullptr;
   for (int w = 0; w < L.lower.nwave(); ++w) {
     const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
     if (r1 <= r0) continue;
     const unsigned g = grid_for(r1 - r0);
     const bool pre = g <= PREFETCH_MAX_BLOCKS;  // per wave (the autotuner times whole-level launches)
     if (L.all_active && pre)
-      GMG_LAUNCH((sell_gs_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags,
+      GMG_LAUNCH((sell_gs_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, L.flags,
                  b, t);
     else if (L.all_active)
-      GMG_LAUNCH((sell_gs_kernel<T, S, true, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags, b, t);
+      GMG_LAUNCH((sell_gs_kernel<T, S, true, 0>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, L.flags, b, t);
     else if (pre)
-      GMG_LAUNCH((sell_gs_kernel<T, S, false, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags,
+      GMG_LAUNCH((sell_gs_kernel<T, S, false, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, L.flags,
                  b, t);
     else
-      GMG_LAUNCH((sell_gs_kernel<T, S, false, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, L.flags, b, t);
+      GMG_LAUNCH((sell_gs_kernel<T, S, false, 0>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, L.flags, b, t);
     LAUNCH_CHECK(mg);
   }
   return 0;
@@ -2303,6 +2344,7 @@ int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
 template <class T, int S>
 int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
   const T *sv = sell_val<T>(L), *dinv = dinv_of<T>(L);
+  const uint8_t *nl = L.sell_split ? L.sell_nl : nullptr;
   for (int st = 0; st < steps; ++st) {
     for (int w = 0; w < L.lower.nwave(); ++w) {
       const int r0 = L.lower.ptr[w], r1 = L.lower.ptr[w + 1];
@@ -2310,24 +2352,24 @@ int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
       const unsigned g = grid_for(r1 - r0);
       const bool pre = g <= PREFETCH_MAX_BLOCKS;  // per wave (the autotuner times whole-level launches)
       if (st == 0 && pre)
-        GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b,
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, b,
                    t, c);
       else if (st == 0)
-        GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b, t, c);
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, true, 0>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, b, t, c);
       else if (pre)
-        GMG_LAUNCH((sell_gs_chain_kernel<T, S, false, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b,
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, false, PF<S>::N>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, b,
                    t, c);
       else
-        GMG_LAUNCH((sell_gs_chain_kernel<T, S, false, 0>), g, BLK, r0, r1, L.sell_ptr, L.sell_col, sv, dinv, b, t,
+        GMG_LAUNCH((sell_gs_chain_kernel<T, S, false, 0>), g, BLK, r0, r1, L.sell_ptr, nl, L.sell_col, sv, dinv, b, t,
                    c);
       LAUNCH_CHECK(mg);
     }
   }
   const unsigned g = grid_for(L.n);
   if (use_prefetch(L, g))
-    GMG_LAUNCH((sell_upper_defect_kernel<T, S, PF<S>::N>), g, BLK, L.n, L.sell_ptr, L.sell_col, sv, t, b);
+    GMG_LAUNCH((sell_upper_defect_kernel<T, S, PF<S>::N>), g, BLK, L.n, L.sell_ptr, nl, L.sell_col, sv, t, b);
   else
-    GMG_LAUNCH((sell_upper_defect_kernel<T, S, 0>), g, BLK, L.n, L.sell_ptr, L.sell_col, sv, t, b);
+    GMG_LAUNCH((sell_upper_defect_kernel<T, S, 0>), g, BLK, L.n, L.sell_ptr, nl, L.sell_col, sv, t, b);
   LAUNCH_CHECK(mg);
   return 0;
 }

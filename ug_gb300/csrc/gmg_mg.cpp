@@ -385,10 +385,17 @@ struct HostLevel {
   std::vector<int> dom_region, dom_cptr, dom_fwbeg, dom_fwptr, dom_frows, dom_bwbeg, dom_bwptr, dom_brows;
   std::vector<int> sptr, scol;  // sliced ELLPACK (32-row slices)
   std::vector<double> sval;
+  std::vector<uint8_t> snl;     // strictly lower entries per row (stored right after the diagonal)
+  std::vector<int> spos;        // sliced-ELLPACK entry of every CSR entry
+  bool ssplit = false;          // every row's lower count fits snl
 };
 
 constexpr int SELL_MIN_ROWS = 2048;  // smaller levels keep the CSR kernels
 
+// Rows are stored as: the diagonal block, the strictly lower blocks (columns
+// j < i), the strictly upper blocks, each part in the row's MATRIX-list
+// order, then the padding.  A forward Gauss-Seidel wave then streams only
+// entries 1..snl[i], the upper-triangle defect pass only the rest.
 static void build_sell(HostLevel &H) {
   const int n = H.n, ss = H.s * H.s, ns = (n + 31) / 32;
   H.sptr.assign(ns + 1, 0);
@@ -399,15 +406,32 @@ static void build_sell(HostLevel &H) {
   }
   H.scol.assign(H.sptr[ns], 0);
   H.sval.assign(size_t(H.sptr[ns]) * ss, 0.0);
+  H.snl.assign(n, 0);
+  H.spos.assign(H.rowptr[n], 0);
+  H.ssplit = true;
+  std::vector<int> order;
   for (int sl = 0; sl < ns; ++sl) {
     const int w = (H.sptr[sl + 1] - H.sptr[sl]) / 32;
     for (int lane = 0; lane < 32; ++lane) {
       const int i = sl * 32 + lane;
+      order.clear();
+      if (i < n) {
+        const int k0 = H.rowptr[i], k1 = H.rowptr[i + 1];
+        order.push_back(k0);
+        for (int k = k0 + 1; k < k1; ++k)
+          if (H.col[k] < i) order.push_back(k);
+        const int nl = int(order.size()) - 1;
+        for (int k = k0 + 1; k < k1; ++k)
+          if (H.col[k] >= i) order.push_back(k);
+        if (nl > 255) H.ssplit = false;
+        H.snl[i] = uint8_t(std::min(nl, 255));
+      }
       for (int k = 0; k < w; ++k) {
         const size_t e = size_t(H.sptr[sl]) + size_t(k) * 32 + lane;
-        if (i < n && k < H.rowptr[i + 1] - H.rowptr[i]) {
-          H.scol[e] = H.col[H.rowptr[i] + k];
-          std::memcpy(&H.sval[e * ss], &H.val[size_t(H.rowptr[i] + k) * ss], sizeof(double) * ss);
+        if (k < int(order.size())) {
+          H.scol[e] = H.col[order[k]];
+          H.spos[order[k]] = int(e);
+          std::memcpy(&H.sval[e * ss], &H.val[size_t(order[k]) * ss], sizeof(double) * ss);
         } else {
           H.scol[e] = i < n ? i : 0;  // padding: zero block at the row itself
         }
@@ -680,7 +704,8 @@ static int upload_level(HostLevel &h, int nc, bool f32, Level &L) {
   bytes += al(h.n * ss * 8) + (f32 ? al(h.n * ss * 4) : 0) + 2 * al(h.n) + 3 * al(h.n * 4);
   bytes += al(h.lptr.size() * 4) + al(h.uptr.size() * 4);
   if (!h.sptr.empty())
-    bytes += al(h.sptr.size() * 4) + al(h.scol.size() * 4) + al(h.sval.size() * 8) + (f32 ? al(h.sval.size() * 4) : 0);
+    bytes += al(h.sptr.size() * 4) + al(h.scol.size() * 4) + al(h.sval.size() * 8) + (f32 ? al(h.sval.size() * 4) : 0) +
+             al(h.n);
   if (nc >= 0) {
     size_t pn = h.pcol.size(), rn = h.rcol.size();
     bytes += al((h.n + 1) * 4) + al(pn * 4) + al(pn * 8) + (f32 ? al(pn * 4) : 0);
@@ -756,6 +781,10 @@ static int upload_level(HostLevel &h, int nc, bool f32, Level &L) {
       auto sv = to_f32(h.sval);
       if (upload(L.sell_v32, sv.data(), sv.size())) return 1;
     }
+    L.sell_nl = ar.take_n<uint8_t>(h.n);
+    if (upload(L.sell_nl, h.snl.data(), h.n)) return 1;
+    L.sell_split = h.ssplit;
+    L.h_sell_pos = std::move(h.spos);
     std::vector<int>().swap(h.sptr);
     std::vector<int>().swap(h.scol);
     std::vector<double>().swap(h.sval);

@@ -17,6 +17,10 @@
 //   * the first call on a device looks up the scratch's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
 //     before any stream capture;
+//   * that address is kept per device ordinal for the life of the process and
+//     is not looked up again: after cudaDeviceReset (or any other teardown of
+//     the device's primary context) it is stale, so do not call this entry
+//     point again in that process;
 //   * every call shares the one scratch array: calls whose kernels overlap on
 //     the GPU (different streams, no ordering between them) race and give
 //     wrong norms; order them on one stream or synchronise between them;

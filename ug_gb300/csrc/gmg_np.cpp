@@ -1999,6 +1999,14 @@ int gmg_iter_iter(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int
   int dummy;
   return p->Iter(level, c, b, A, result ? result : &dummy);
 }
+int gmg_iter_smooth(gmg_np *np, int level, gmg_vec *t, gmg_vec *b, gmg_mat *A, gmg_vec *c, int steps,
+                    int *result) {
+  AS(NPIter, np, NPK_ITER);
+  GMG_CHECK(t && b && c && steps >= 0, "gmg_iter_smooth: vectors missing or negative step count");
+  GMG_CHECK(t->mg == p->mg && b->mg == p->mg && c->mg == p->mg, "gmg_iter_smooth: vectors of another multigrid");
+  int dummy;
+  return p->IterAccN(level, t, b, A, c, steps, result ? result : &dummy);
+}
 int gmg_iter_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPIter, np, NPK_ITER);
   int dummy;

@@ -123,11 +123,8 @@ int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int 
   for (int l = 0; l < nl; ++l) {
     Level &L = mg->lev[l];
     if (L.sell) {
-      const int ns = (L.n + 31) / 32;
-      std::vector<int> sptr(ns + 1), m(L.h_rowptr[L.n]);
-      GMG_CUDA(cudaMemcpy(sptr.data(), L.sell_ptr, sptr.size() * 4, cudaMemcpyDeviceToHost));
-      for (int i = 0; i < L.n; ++i)
-        for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k) m[k] = sptr[i >> 5] + (k - L.h_rowptr[i]) * 32 + (i & 31);
+      const std::vector<int> &m = L.h_sell_pos;
+      GMG_CHECK((long long)m.size() == L.nnzb, "pool: sliced-ELLPACK entry map missing");
       GMG_CUDA(cudaMalloc(&P->c2s[l], m.size() * 4));
       GMG_CUDA(cudaMemcpy(P->c2s[l], m.data(), m.size() * 4, cudaMemcpyHostToDevice));
     }
