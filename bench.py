@@ -580,6 +580,7 @@ def run_serving(args, rank):
            "throughput_req_s": st.throughput, "offered_req_s": SERVE_RATE, "makespan_s": st.makespan_s,
            "iterations_mean": st.iterations_mean, "all_converged": st.all_converged,
            "per_depth": {str(k): v for k, v in st.per_depth.items()},
+           "breakdown": st.breakdown,
            "pools": {str(L): {"pools": n, "slots_each": m} for L, (n, m) in srv.layout.items()},
            "setup_s": setup_s, "clocks": clk.summary(),
            "note": "latency = completion - arrival (queueing, on-device assembly, all iterations, "

@@ -219,6 +219,11 @@ int gmg_ddot(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, double *result);    
 int gmg_l_jac(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);                /* ugiter.cc:271 */
 int gmg_l_lgs(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);                /* ugiter.cc:412 */
 int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *M, const double *beta);            /* ugiter.cc:2252 */
+/* the factors l_ilubthdecomp left in its copy of the matrix (decomposed on the
+ * device): the level's matrix layout in processing order (gmg_mg_get_matrix),
+ * diagonal blocks inverted, L below the diagonal, U above; rows that are not
+ * ACTIVE keep A's values */
+int gmg_l_ilu_factors(gmg_mg *mg, int level, double *lu);
 int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);             /* ugiter.cc:4444 */
 int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp);            /* 462 */
 int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp); /* 529 */

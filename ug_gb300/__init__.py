@@ -106,6 +106,7 @@ def lib(build_if_missing: bool = True):
         "gmg_dscalx": ([P, I, P, P], I), "gmg_daxpy": ([P, I, P, P, P], I), "gmg_ddot": ([P, I, P, P, P], I),
         "gmg_l_jac": ([P, I, P, P, P], I), "gmg_l_lgs": ([P, I, P, P, P], I),
         "gmg_l_ilu_decomp": ([P, I, P, P], I), "gmg_l_luiter": ([P, I, P, P, P], I),
+        "gmg_l_ilu_factors": ([P, I, P], I),
         "gmg_standard_restrict": ([P, I, P, P, P], I), "gmg_standard_interpolate_correction": ([P, I, P, P, P], I),
         "gmg_solve_host": ([P, C.c_char_p, P, P, P], I),
         "gmg_mg_create_batched": ([P, P, I, P, P], I), "gmg_mg_num_instances": ([P], I),
@@ -755,6 +756,15 @@ class MultiGrid:
     def l_lgs(self, level, v, d, M="MAT"):
         if lib().gmg_l_lgs(self._h, level, self.vec(v), self.mat(M), self.vec(d)):
             _err("l_lgs")
+
+    def l_ilu_factors(self, level):
+        """The ILU(0) factors of a level as l_ilubthdecomp leaves them (the
+        device matrix layout of `matrix(level)`, processing order)."""
+        n, s, nnz = self.size(level)
+        lu = np.empty(nnz * s * s)
+        if lib().gmg_l_ilu_factors(self._h, level, lu.ctypes.data):
+            _err("l_ilu_factors")
+        return lu
 
     def l_ilu_decomp(self, level, beta=None, M="MAT"):
         b = _sc(beta, 0.0)

@@ -76,6 +76,15 @@ struct Sched {
   int nwave() const { return ptr.empty() ? 0 : int(ptr.size()) - 1; }
 };
 
+// work arrays of the device ILU(0) factorisation of one level: the combined
+// factor array (nnzb blocks, the level's CSR), per row its strictly lower
+// entries sorted by column (lsort[lsptr[i]..lsptr[i+1]], CSR positions) and
+// the smallest row whose pivot block was singular
+struct IluDev {
+  double *lu = nullptr;
+  int *lsptr = nullptr, *lsort = nullptr, *fail = nullptr;
+};
+
 struct Level {
   Arena arena;                  // the level's device arrays (released with the level)
   int n = 0, s = 1;
@@ -103,6 +112,7 @@ struct Level {
   DevCSR L, U;                  // strict lower (unit diagonal) / strict upper parts
   double *udinv64 = nullptr;    // inverted diagonal blocks of U
   float *udinv32 = nullptr;
+  IluDev ilu_dev;               // the device factorisation's work arrays
   std::vector<void *> own;      // cudaMalloc'd arrays owned outside the arena
   // transfer from level-1: P (rows = this level), R (rows = level-1 VECTORs)
   DevCSR P, R;
@@ -343,6 +353,11 @@ bool gs_chain_ok(const Level &L, int prec);
 int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps);
 // ILU forward / backward solve with the factors of L
 int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
+// ILU(0) factors of the level matrix with beta (l_ilubthdecomp) on the device,
+// written into L.L / L.U / L.udinv (FP64 and FP32 copies); synchronous.
+// *failed_row = the smallest processing-order row whose diagonal block was
+// singular (nothing written then), else -1
+int k_ilu_factor(gmg_mg *mg, Level &L, const double *beta, const IluDev &D, int *failed_row);
 // coarse = (reset ? 0 : coarse) + R (damp*fine), honouring coarse VECSKIP
 // (zero_coarse, if given, is set to 0 on the coarse level in the same pass)
 int k_restrict(gmg_mg *mg, const Level &fine, const Level &coarse, int prec, void *to, const void *from,

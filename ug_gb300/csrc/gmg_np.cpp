@@ -291,95 +291,6 @@ std::string NPIlu::Display() const {
   return NPSmoother::Display() + "beta = " + fmt_sc(beta, mg->lev.empty() ? 1 : mg->lev[0].s) + "\n";
 }
 
-// l_ilubthdecomp (ugiter.cc:2252-2625) without threshold / rest vector, on a
-// copy of A (ILUPreProcess, iter.cc:5444), in processing order.  The row's
-// diagonal block becomes its inverse (StoreInverse), each block (j,i) below
-// it the pivot A_ji D_i^{-1}, and pattern blocks (j,k), k>i, are updated.
-static int ilu_factor_host(const Level &L, const double *beta, std::vector<double> &lu) {
-  const int n = L.n, s = L.s, ss = s * s;
-  lu = L.h_val;
-  auto active = [&](int i) { return (L.h_flags[i] & F_ACTIVE) != 0; };
-  auto find = [&](int row, int col) {
-    for (int k = L.h_rowptr[row]; k < L.h_rowptr[row + 1]; ++k)
-      if (L.h_col[k] == col) return k;
-    return -1;
-  };
-  std::vector<double> inv(ss), pm(ss), cor(ss), rowsum(s);
-  for (int i = 0; i < n; ++i) {
-    if (!active(i)) continue;
-    const int kd = L.h_rowptr[i];
-    if (s == 1) {
-      double diag = lu[kd];
-      if (std::fabs(diag) < 2.220446049250313e-16 * 10 * 1e-20) return -(i + 1);
-      double invdiag = 1.0 / diag;
-      lu[kd] = invdiag;
-      for (int kij = kd + 1; kij < L.h_rowptr[i + 1]; ++kij) {
-        int j = L.h_col[kij];
-        if (!(active(j) && j > i)) continue;
-        int kji = find(j, i);
-        if (kji < 0) return -(i + 1);
-        double pivot = lu[kji] * invdiag;
-        lu[kji] = pivot;
-        if (pivot == 0.0) continue;
-        for (int kik = kd + 1; kik < L.h_rowptr[i + 1]; ++kik) {
-          int k = L.h_col[kik];
-          if (!(active(k) && k > i)) continue;
-          int kjk = find(j, k);
-          if (kjk >= 0) lu[kjk] -= pivot * lu[kik];
-          else lu[L.h_rowptr[j]] += beta[0] * std::fabs(pivot * lu[kik]);
-        }
-      }
-      continue;
-    }
-    if (invert_block(s, &lu[size_t(kd) * ss], inv.data())) return -(i + 1);
-    std::copy(inv.begin(), inv.end(), lu.begin() + size_t(kd) * ss);
-    for (int kij = kd + 1; kij < L.h_rowptr[i + 1]; ++kij) {
-      int j = L.h_col[kij];
-      if (!(active(j) && i < j)) continue;
-      std::fill(rowsum.begin(), rowsum.end(), 0.0);
-      int kji = find(j, i);
-      if (kji < 0) return -(i + 1);
-      double *piv = &lu[size_t(kji) * ss];
-      bool zero = true;
-      for (int r = 0; r < s; ++r)
-        for (int c = 0; c < s; ++c) {
-          double sum = 0.0;
-          for (int q = 0; q < s; ++q) sum += piv[r * s + q] * inv[q * s + c];
-          pm[r * s + c] = sum;
-          if (sum != 0.0) zero = false;
-        }
-      std::copy(pm.begin(), pm.end(), piv);
-      if (zero) continue;
-      for (int kik = kd + 1; kik < L.h_rowptr[i + 1]; ++kik) {
-        int k = L.h_col[kik];
-        if (!(active(k) && i < k)) continue;
-        const double *elm = &lu[size_t(kik) * ss];
-        bool cz = true;
-        for (int r = 0; r < s; ++r)
-          for (int c = 0; c < s; ++c) {
-            double sum = 0.0;
-            for (int q = 0; q < s; ++q) sum += pm[r * s + q] * elm[q * s + c];
-            cor[r * s + c] = sum;
-            if (sum != 0.0) cz = false;
-          }
-        if (cz) continue;
-        int kjk = find(j, k);
-        if (kjk >= 0) {
-          double *mat = &lu[size_t(kjk) * ss];
-          for (int q = 0; q < ss; ++q) mat[q] -= cor[q];
-        } else {
-          for (int r = 0; r < s; ++r)
-            for (int c = 0; c < s; ++c) rowsum[r] += std::fabs(cor[r * s + c]);
-        }
-      }
-      double *djj = &lu[size_t(L.h_rowptr[j]) * ss];
-      for (int r = 0; r < s; ++r)
-        for (int c = 0; c < s; ++c) djj[r * s + c] *= 1.0 + beta[c] * rowsum[c];
-    }
-  }
-  return 0;
-}
-
 template <class T>
 static int dev_copy(gmg::Level &L, T **dst, const std::vector<T> &src) {
   size_t n = src.empty() ? 1 : src.size();
@@ -436,71 +347,75 @@ int NPIlu::PreProcess(int level, gmg_vec *, gmg_vec *, gmg_mat *, int *baselevel
   Level &L = mg->lev[level];
   *baselevel = level;
   if (L.ilu_ready) return 0;
-  return ilu_build(mg, L, level, beta, false, result);
+  return ilu_build(mg, L, level, beta, L.L.rowptr != nullptr, result);
 }
 
-// the ILU(0) factors of level L with the given beta, split into the unit
-// lower factor, the strict upper factor and the inverted diagonal blocks;
-// in_place: the level's factor arrays exist (same structure) and are rewritten
+// the ILU(0) factors of level L with the given beta (l_ilubthdecomp on the
+// device, gmg_ilu.cu), split into the unit lower factor, the strict upper
+// factor and the inverted diagonal blocks; in_place: the level's factor
+// arrays exist (same structure) and only the values are recomputed
 static int ilu_build(gmg_mg *mg, Level &L, int level, const double *beta, bool in_place, int *result) {
-  std::vector<double> lu;
-  int rc = ilu_factor_host(L, beta, lu);
-  if (rc) {
-    *result = rc;
-    set_error("ILU decomposition failed in row %d of level %d", -rc - 1, level);
-    return 1;
-  }
   const int n = L.n, s = L.s, ss = s * s;
-  std::vector<int> lr(n + 1, 0), ur(n + 1, 0), lc, uc;
-  std::vector<double> lv, uv, ud(size_t(n) * ss, 0.0);
-  for (int i = 0; i < n; ++i) {
-    const bool act = L.h_flags[i] & F_ACTIVE;
-    for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k) {
-      int j = L.h_col[k];
-      if (j == i) {
-        if (act) std::copy(&lu[size_t(k) * ss], &lu[size_t(k) * ss] + ss, &ud[size_t(i) * ss]);
-        continue;
+  if (!in_place) {
+    // the factors' structure: active rows' strictly lower / upper entries
+    // between active rows, in CSR order; per row its lower entries by column
+    auto act = [&](int i) { return (L.h_flags[i] & F_ACTIVE) != 0; };
+    std::vector<int> lr(n + 1, 0), ur(n + 1, 0), lc, uc, lsptr(n + 1, 0), lsort;
+    std::vector<std::pair<int, int>> low;
+    for (int i = 0; i < n; ++i) {
+      low.clear();
+      for (int k = L.h_rowptr[i]; k < L.h_rowptr[i + 1]; ++k) {
+        const int j = L.h_col[k];
+        if (j < i) low.push_back({j, k});
+        if (j == i || !act(i) || !act(j)) continue;
+        (j < i ? lc : uc).push_back(j);
       }
-      if (!act || !(L.h_flags[j] & F_ACTIVE)) continue;
-      if (j < i) { lc.push_back(j); lv.insert(lv.end(), &lu[size_t(k) * ss], &lu[size_t(k) * ss] + ss); }
-      else { uc.push_back(j); uv.insert(uv.end(), &lu[size_t(k) * ss], &lu[size_t(k) * ss] + ss); }
+      std::sort(low.begin(), low.end());
+      for (auto &e : low) lsort.push_back(e.second);
+      lr[i + 1] = int(lc.size());
+      ur[i + 1] = int(uc.size());
+      lsptr[i + 1] = int(lsort.size());
     }
-    lr[i + 1] = int(lc.size());
-    ur[i + 1] = int(uc.size());
-  }
-  std::copy(beta, beta + GMG_MAX_S, L.ilu_beta);
-  if (in_place) {
-    GMG_CHECK(L.L.nnz == (long long)lc.size() && L.U.nnz == (long long)uc.size(), "ILU refresh: factor pattern changed");
-    auto put = [](void *dst, const void *src, size_t bytes) -> int {
-      if (bytes) GMG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    // UG's MATRIX entries come in pairs (MADJ): the elimination needs (i, j)
+    // wherever (j, i) is stored
+    for (int i = 0; i < n; ++i)
+      for (int k = L.h_rowptr[i] + 1; k < L.h_rowptr[i + 1]; ++k) {
+        const int j = L.h_col[k];
+        bool found = false;
+        for (int q = L.h_rowptr[j]; q < L.h_rowptr[j + 1] && !found; ++q) found = L.h_col[q] == i;
+        GMG_CHECK(found, "ILU: level %d: entry (%d, %d) has no transposed entry", level, L.perm[i], L.perm[j]);
+      }
+    auto dev_alloc = [&](auto **dst, size_t count) -> int {
+      GMG_CUDA(cudaMalloc(dst, std::max<size_t>(count, 1) * sizeof(**dst)));
+      L.own.push_back(*dst);
       return 0;
     };
-    if (put(L.L.v64, lv.data(), lv.size() * 8) || put(L.U.v64, uv.data(), uv.size() * 8) ||
-        put(L.udinv64, ud.data(), ud.size() * 8))
+    L.L.nrows = L.U.nrows = n;
+    L.L.nnz = lc.size();
+    L.U.nnz = uc.size();
+    if (dev_copy(L, &L.L.rowptr, lr) || dev_copy(L, &L.L.col, lc) || dev_alloc(&L.L.v64, lc.size() * ss) ||
+        dev_copy(L, &L.U.rowptr, ur) || dev_copy(L, &L.U.col, uc) || dev_alloc(&L.U.v64, uc.size() * ss) ||
+        dev_alloc(&L.udinv64, size_t(n) * ss) || dev_alloc(&L.ilu_dev.lu, size_t(L.nnzb) * ss) ||
+        dev_copy(L, &L.ilu_dev.lsptr, lsptr) || dev_copy(L, &L.ilu_dev.lsort, lsort) ||
+        dev_alloc(&L.ilu_dev.fail, 1))
       return 1;
-    if (mg->opts.fp32_copy) {
-      std::vector<float> lv32(lv.begin(), lv.end()), uv32(uv.begin(), uv.end()), ud32(ud.begin(), ud.end());
-      if (put(L.L.v32, lv32.data(), lv32.size() * 4) || put(L.U.v32, uv32.data(), uv32.size() * 4) ||
-          put(L.udinv32, ud32.data(), ud32.size() * 4))
-        return 1;
-    }
-    return 0;
+    if (mg->opts.fp32_copy &&
+        (dev_alloc(&L.L.v32, lc.size() * ss) || dev_alloc(&L.U.v32, uc.size() * ss) ||
+         dev_alloc(&L.udinv32, size_t(n) * ss)))
+      return 1;
+    if (L.dom_nreg > 0 &&
+        (region_tables(L, L.h_dom_fwbeg, L.h_dom_fwptr, L.h_dom_frows, lr, lc, true, L.dom_lt) ||
+         region_tables(L, L.h_dom_bwbeg, L.h_dom_bwptr, L.h_dom_brows, ur, uc, false, L.dom_ut)))
+      return 1;
   }
-  L.L.nrows = L.U.nrows = n;
-  L.L.nnz = lc.size();
-  L.U.nnz = uc.size();
-  if (dev_copy(L, &L.L.rowptr, lr) || dev_copy(L, &L.L.col, lc) || dev_copy(L, &L.L.v64, lv) ||
-      dev_copy(L, &L.U.rowptr, ur) || dev_copy(L, &L.U.col, uc) || dev_copy(L, &L.U.v64, uv) ||
-      dev_copy(L, &L.udinv64, ud))
+  int failed = -1;
+  if (k_ilu_factor(mg, L, beta, L.ilu_dev, &failed)) return 1;
+  if (failed >= 0) {
+    *result = -(failed + 1);
+    set_error("ILU decomposition failed in row %d of level %d", failed, level);
     return 1;
-  if (mg->opts.fp32_copy) {
-    std::vector<float> lv32(lv.begin(), lv.end()), uv32(uv.begin(), uv.end()), ud32(ud.begin(), ud.end());
-    if (dev_copy(L, &L.L.v32, lv32) || dev_copy(L, &L.U.v32, uv32) || dev_copy(L, &L.udinv32, ud32)) return 1;
   }
-  if (L.dom_nreg > 0 &&
-      (region_tables(L, L.h_dom_fwbeg, L.h_dom_fwptr, L.h_dom_frows, lr, lc, true, L.dom_lt) ||
-       region_tables(L, L.h_dom_bwbeg, L.h_dom_bwptr, L.h_dom_brows, ur, uc, false, L.dom_ut)))
-    return 1;
+  std::copy(beta, beta + GMG_MAX_S, L.ilu_beta);
   L.ilu_ready = true;
   return 0;
 }
@@ -2175,6 +2090,15 @@ int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *, const double *beta) {
   mg->coarse_images.clear();  // fused images hold copies of the factors
   int bl = 0, res = 0;
   return tmp.PreProcess(level, nullptr, nullptr, nullptr, &bl, &res);
+}
+int gmg_l_ilu_factors(gmg_mg *mg, int level, double *lu) {
+  MGV(mg, level);
+  const Level &L = mg->lev[level];
+  GMG_CHECK(lu, "gmg_l_ilu_factors: no output array");
+  GMG_CHECK(L.ilu_ready && L.ilu_dev.lu, "gmg_l_ilu_factors: level %d has no ILU factors", level);
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  GMG_CUDA(cudaMemcpy(lu, L.ilu_dev.lu, sizeof(double) * L.nnzb * L.s * L.s, cudaMemcpyDeviceToHost));
+  return 0;
 }
 int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
   MGV(mg, level);

@@ -22,6 +22,7 @@ iterations included); throughput = completed requests / makespan.
 from __future__ import annotations
 
 import ctypes as C
+import gc
 import time
 from dataclasses import dataclass, field
 
@@ -163,6 +164,7 @@ class ServeStats:
     iterations_mean: float
     all_converged: bool
     per_depth: dict = field(default_factory=dict)
+    breakdown: dict = field(default_factory=dict)
 
 
 class Server:
@@ -215,13 +217,30 @@ class Server:
                 p.solve(seed, self.corr, self.var)
 
     def run(self, requests: list[Request], keep_x: bool = False) -> ServeStats:
+        """Serve the stream; latency breakdown per request: queue wait
+        (admission - arrival) and service (completion - admission); the
+        loop's host calls are timed too (the longest ones are reported), so
+        a latency tail can be traced to queueing, a slow host call or the
+        device.  Python's cyclic garbage collector is paused during the
+        loop (a full collection over the process's objects is a pause of
+        tens to hundreds of ms that would land on every request in flight)."""
         pending = {L: [] for L in self.pools}
         order = sorted(requests, key=lambda r: r.arrival)
         nxt = 0
         done_count = 0
-        t0 = time.perf_counter()
+        host_ops = []  # (seconds, kind, depth) of every admit / launch / poll / fetch
+        gaps = []      # wall time of each pass of the loop
+        gc_was = gc.isenabled()
+        gc.collect()
+        gc.disable()
+        pc = time.perf_counter
+        t0 = pc()
+        tprev = t0
         while done_count < len(order):
-            now = time.perf_counter() - t0
+            tl = pc()
+            gaps.append(tl - tprev)
+            tprev = tl
+            now = tl - t0
             while nxt < len(order) and order[nxt].arrival <= now:
                 pending[order[nxt].nref].append(order[nxt])
                 nxt += 1
@@ -229,14 +248,18 @@ class Server:
             for L, pools in self.pools.items():
                 for pool in pools:
                     if pool.busy:
+                        ta = pc()
                         fin = pool.poll()
+                        host_ops.append((pc() - ta, "poll", L))
                         if fin is None:
                             continue
                         progressed = True
-                        tnow = time.perf_counter() - t0
+                        tnow = pc() - t0
                         for k in fin:
                             req = pool.active.pop(k)
+                            ta = pc()
                             x, lr = pool.fetch(k, keep_x)
+                            host_ops.append((pc() - ta, "fetch", L))
                             req.done, req.iters, req.converged = tnow, lr.iters, bool(lr.converged)
                             req.x = x
                             pool.free.append(k)
@@ -248,20 +271,42 @@ class Server:
                     while q and pool.free and not pool.busy:
                         req = q.pop(0)
                         k = pool.free.pop(0)
+                        ta = pc()
+                        req.start = ta - t0
                         pool.admit(k, req.seed, self.corr, self.var)
-                        req.start = time.perf_counter() - t0
+                        host_ops.append((pc() - ta, "admit", L))
                         pool.active[k] = req
                         progressed = True
                 for pool in pools:
                     if pool.active and not pool.busy:
+                        ta = pc()
                         pool.launch()
+                        host_ops.append((pc() - ta, "launch", L))
             if not progressed:
                 if nxt < len(order) and not any(p.busy for ps in self.pools.values() for p in ps):
                     wait = order[nxt].arrival - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(min(wait, 0.002))
+        if gc_was:
+            gc.enable()
         makespan = max(r.done for r in order)
         lat = np.array([(r.done - r.arrival) * 1e3 for r in order])
+        wait = np.array([(r.start - r.arrival) * 1e3 for r in order])
+        serv = np.array([(r.done - r.start) * 1e3 for r in order])
+        host_ops.sort(key=lambda o: -o[0])
+        by_kind = {}
+        for dt, kind, L in host_ops:
+            e = by_kind.setdefault(kind, [0, 0.0, 0.0])
+            e[0] += 1; e[1] += dt; e[2] = max(e[2], dt)
+        breakdown = {
+            "queue_wait_ms": {"p50": float(np.percentile(wait, 50)), "p99": float(np.percentile(wait, 99)),
+                              "max": float(wait.max())},
+            "service_ms": {"p50": float(np.percentile(serv, 50)), "p99": float(np.percentile(serv, 99)),
+                           "max": float(serv.max())},
+            "host_calls": {k: {"count": c, "total_ms": t * 1e3, "max_ms": m * 1e3} for k, (c, t, m) in by_kind.items()},
+            "longest_host_calls_ms": [[round(dt * 1e3, 3), kind, L] for dt, kind, L in host_ops[:5]],
+            "longest_loop_pass_ms": float(max(gaps) * 1e3) if gaps else 0.0,
+        }
         per = {}
         for L in self.pools:
             ls = np.array([(r.done - r.arrival) * 1e3 for r in order if r.nref == L])
@@ -270,7 +315,7 @@ class Server:
                           "p99_ms": float(np.percentile(ls, 99)), "pools_x_slots": list(self.layout[L])}
         return ServeStats(len(order), makespan, float(np.percentile(lat, 50)), float(np.percentile(lat, 99)),
                           float(lat.mean()), len(order) / makespan, float(np.mean([r.iters for r in order])),
-                          all(r.converged for r in order), per)
+                          all(r.converged for r in order), per, breakdown)
 
     def close(self):
         for ps in self.pools.values():
