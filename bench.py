@@ -569,6 +569,60 @@ def run_serving(args, rank):
     reqs = poisson_stream(args.serve_requests, SERVE_RATE, SERVE_LEVELS, seed=2026 + rank)
     with ClockSampler(torch.cuda.current_device()) as clk:
         st = srv.run(reqs)
+    # the admission's device work per depth (field, assembly of every level,
+    # right-hand side, first norm), timed alone after the stream, with the
+    # stream's FP32 field and with the FP64 field
+    admit_ms = {"fp32_field": {}, "fp64_field": {}}
+    for L, pools in srv.pools.items():
+        p = pools[0]
+        for key, prec in (("fp32_field", 1), ("fp64_field", 0)):
+            G.lib().gmg_pool_set_field_precision(p._h, prec)
+            ts = []
+            for rep in range(3):
+                slot = p.free[0]
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                p.admit(slot, 999 + rep, srv.corr, srv.var)
+                torch.cuda.synchronize()
+                ts.append((time.perf_counter() - t1) * 1e3)
+                while True:  # iterate the request to its end, which frees the slot
+                    p.launch()
+                    while (done := p.poll()) is None:
+                        pass
+                    if slot in done:
+                        break
+                p.fetch(slot, False)
+            admit_ms[key][str(L)] = float(np.median(ts))
+        G.lib().gmg_pool_set_field_precision(p._h, 0 if srv.field_fp64 else 1)
+    # accuracy of served results: a sample of the stream's requests solved again
+    # alone in a pool of their depth (bitwise the result they had in the mix,
+    # tests/test_serve.py), against FP64 oracle solutions converged to 1e-12 of
+    # (a) the problem the slot held (its matrices read back from the device)
+    # and (b) the host-assembled FP64 problem (depths up to 6 on the CPU)
+    served_err = {}
+    if rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        for L in range(SERVE_LEVELS[0], min(SERVE_LEVELS[1], 6) + 1):
+            sample = [r for r in reqs if r.nref == L][: (2 if L <= 5 else 1)]
+            e_slot, e_host, same_iters = [], [], True
+            p = srv.pools[L][0]
+            for r in sample:
+                slot = p.free[0]
+                x, lr = p.solve(r.seed, srv.corr, srv.var, slot=slot)
+                same_iters = same_iters and lr.iters == r.iters
+                levels, rhs, _ = oracle.cube_levels(L, r.seed, CORR, VAR)
+                xo, _, conv, _ = oracle.Hierarchy(levels).ls_solve(rhs, smoother="gs", baselevel=0, red=1e-12,
+                                                                   abslimit=1e-50, base_abslimit=1e-30)
+                e_host.append(float(np.max(np.abs(x - xo)) / np.max(np.abs(xo))) if conv else float("nan"))
+                held = [dict(d, val=p.slot_matrix(slot, l, d["val"].size)) for l, d in enumerate(levels)]
+                xs, _, conv, _ = oracle.Hierarchy(held).ls_solve(rhs, smoother="gs", baselevel=0, red=1e-12,
+                                                                 abslimit=1e-50, base_abslimit=1e-30)
+                e_slot.append(float(np.max(np.abs(x - xs)) / np.max(np.abs(xs))) if conv else float("nan"))
+            served_err[str(L)] = {"requests": len(sample), "same_iterations_as_served": same_iters,
+                                  "max_rel_error_vs_fp64_oracle_of_served_problem": max(e_slot),
+                                  "max_rel_error_vs_fp64_oracle_of_host_problem": max(e_host)}
     srv.close()
     # replicas: latencies of the slowest rank, throughput of all ranks
     st.p50_ms, st.p99_ms, st.mean_ms = (reduce_over_ranks(v) for v in (st.p50_ms, st.p99_ms, st.mean_ms))
@@ -580,7 +634,10 @@ def run_serving(args, rank):
            "throughput_req_s": st.throughput, "offered_req_s": SERVE_RATE, "makespan_s": st.makespan_s,
            "iterations_mean": st.iterations_mean, "all_converged": st.all_converged,
            "per_depth": {str(k): v for k, v in st.per_depth.items()},
-           "breakdown": st.breakdown,
+           "breakdown": st.breakdown, "admission_device_ms": admit_ms,
+           "field": "FP64" if srv.field_fp64 else "FP32 (fixed-point phases, FP32 cosines: k within ~1e-6 of the "
+                                                 "host generator's; the FP64 field is the pools' option)",
+           "accuracy_sample": served_err,
            "pools": {str(L): {"pools": n, "slots_each": m} for L, (n, m) in srv.layout.items()},
            "setup_s": setup_s, "clocks": clk.summary(),
            "note": "latency = completion - arrival (queueing, on-device assembly, all iterations, "

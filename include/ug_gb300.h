@@ -254,7 +254,8 @@ int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev,
  * corr, var as gmg_gen_create), its matrices on every level and its
  * right-hand side on the device; each launch is one ls iteration of all
  * slots; a poll tests every active slot against its own first defect, so
- * requests join and leave between iterations.  Pools run on their own
+ * requests join and leave between iterations (the field's precision:
+ * gmg_pool_set_field_precision).  Pools run on their own
  * streams and overlap on the GPU.  Admit, fetch and slot_matrix need the
  * pool idle (the last launch polled). */
 typedef struct gmg_pool gmg_pool;
@@ -265,6 +266,11 @@ int gmg_pool_set_stream(gmg_pool *pool, void *stream);
 /* slots, VECTORs of one slot's finest level, free slots */
 int gmg_pool_slots(const gmg_pool *pool, int *nslots, int *n_top, int *free_slots);
 int gmg_pool_admit(gmg_pool *pool, int slot, unsigned long long seed, double corr, double var);
+/* Precision of the coefficient field at admission: GMG_PREC_FP64 (the
+ * default: k within ~1e-14 of gmg_gen_create's, so a slot holds the FP64
+ * problem) or GMG_PREC_FP32 (fixed-point phases and FP32 cosines, ~1e-6
+ * relative in k, a cheaper admission).  Needs the pool idle. */
+int gmg_pool_set_field_precision(gmg_pool *pool, int precision);
 int gmg_pool_launch(gmg_pool *pool);
 /* 0: still running; 1: finished, *ndone slots done (listed in done[]); -1: error */
 int gmg_pool_poll(gmg_pool *pool, int *ndone, int *done);

@@ -11,12 +11,20 @@
 // diagonal); boundary rows become unit Dirichlet rows.  The right-hand side is
 // the position-keyed uniform load of fields.h.
 //
-// The field's phases are evaluated exactly in 32-bit fixed point (fractions
-// of a turn): for centroid lattice coordinates c (units of h/4) the phase is
-// phi + sum_d c_d theta_d modulo one turn, with theta_d = w_d h / 4 rounded to
-// 2^-32 turn, so no large argument reaches the sine and cosine; those, the
-// angle additions, the sum over features and exp run in FP32.  k then agrees
-// with the FP64 host generator to ~1e-6 relative.
+// Two evaluations of the field.  FP64 (the default of the serving pools):
+// the phase of feature m at the centroid (c + delta_p) h of tetrahedron p of
+// cell c is phi_m + w_m.c h + w_m.delta_p h, so cos of it is the real part of
+// the product of per-axis factors exp(i w_md c_d h) (tabulated per level and
+// feature, one sincos per table entry), the factor exp(i phi_m) and the
+// tetrahedron's exp(i w_m.delta_p h); a cell then costs two complex
+// products per feature and each of its six tetrahedra two FMAs, all in FP64:
+// k agrees with the host generator's direct evaluation to ~1e-14 relative
+// (both round the phase differently, by |phase| ulp at most).  FP32: the
+// phases exactly in 32-bit fixed point (fractions of a turn: for centroid
+// lattice coordinates c in units of h/4 the phase is phi + sum_d c_d theta_d
+// modulo one turn, theta_d = w_d h / 4 rounded to 2^-32 turn), the sines,
+// cosines, angle additions, the sum over features and exp in FP32: ~1e-6
+// relative in k, about 50x less FP64-free work.
 #include <cmath>
 #include <cstdint>
 #include <algorithm>
@@ -130,6 +138,84 @@ __global__ void __launch_bounds__(ABLK) cube_field_kernel(int Nc, const uint4 *_
   }
 }
 
+// FP64 field, per-axis tables of one level (Nc cells per axis, h = 1 / Nc),
+// phases at cell centres: X[m][i] = e^{i w_m0 (i + 1/2) h}, Y[m][j] =
+// e^{i w_m1 (j + 1/2) h}, ZP[m][k] = e^{i (phi_m + w_m2 (k + 1/2) h)}.  The
+// centroids of the tetrahedra pair up about the cell centre:
+// delta_p = 1/2 + eps_q for p = 0, 1, 2 (q = p) and delta = 1/2 - eps_q for
+// their partners 5, 3, 4, eps_q = (e_p0 - e_p2) / 4; U[m][q] = (cos, sin) of
+// w_m.eps_q h
+__global__ void __launch_bounds__(ABLK) cube_field64_tables_kernel(int Nc, double h, int M,
+                                                                   const double *__restrict__ w,
+                                                                   const double *__restrict__ phi,
+                                                                   double2 *__restrict__ X, double2 *__restrict__ Y,
+                                                                   double2 *__restrict__ ZP, double2 *__restrict__ U) {
+  const int per = 3 * Nc + 3;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M * per) return;
+  const int m = t / per, q = t % per;
+  double arg;
+  double2 *dst;
+  if (q < Nc) {
+    arg = w[m * 3] * ((q + 0.5) * h);
+    dst = X + (size_t)m * Nc + q;
+  } else if (q < 2 * Nc) {
+    arg = w[m * 3 + 1] * ((q - Nc + 0.5) * h);
+    dst = Y + (size_t)m * Nc + (q - Nc);
+  } else if (q < 3 * Nc) {
+    arg = phi[m] + w[m * 3 + 2] * ((q - 2 * Nc + 0.5) * h);
+    dst = ZP + (size_t)m * Nc + (q - 2 * Nc);
+  } else {
+    const int p = q - 3 * Nc;  // 0, 1, 2
+    arg = h * 0.25 * (w[m * 3 + c_perm[p][0]] - w[m * 3 + c_perm[p][2]]);
+    dst = U + (size_t)m * 3 + p;
+  }
+  double sn, cs;
+  sincos(arg, &sn, &cs);
+  *dst = make_double2(cs, sn);
+}
+
+// FP64 field: k of every tetrahedron of the level (element ((z Nc + y) Nc +
+// x) 6 + p).  One block per row (y, z) of cells: the row's factors Y ZP per
+// feature and the pair factors U in shared memory; per cell and feature E =
+// X YZ = e^{i a0} (a0 the phase at the cell centre), then for each pair
+// S += Re E cos u, D += Im E sin u: cos(a0 + u) = S - D, cos(a0 - u) = S + D
+__global__ void __launch_bounds__(128) cube_field64_kernel(int Nc, int M, double amp, const double2 *__restrict__ X,
+                                                           const double2 *__restrict__ Y,
+                                                           const double2 *__restrict__ ZP,
+                                                           const double2 *__restrict__ U,
+                                                           double *__restrict__ kelem) {
+  __shared__ double2 sYZ[GMG_FIELD_MAX_M];
+  __shared__ double2 sU[GMG_FIELD_MAX_M * 3];
+  const int row = blockIdx.x, j = row % Nc, k = row / Nc;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const double2 b = Y[(size_t)m * Nc + j], c = ZP[(size_t)m * Nc + k];
+    sYZ[m] = make_double2(b.x * c.x - b.y * c.y, b.x * c.y + b.y * c.x);
+  }
+  for (int q = threadIdx.x; q < M * 3; q += blockDim.x) sU[q] = U[q];
+  __syncthreads();
+  for (int i = threadIdx.x; i < Nc; i += blockDim.x) {
+    double S[3] = {0.0, 0.0, 0.0}, D[3] = {0.0, 0.0, 0.0};
+    for (int m = 0; m < M; ++m) {
+      const double2 a = __ldg(X + (size_t)m * Nc + i), yz = sYZ[m];
+      const double er = fma(a.x, yz.x, -a.y * yz.y), ei = fma(a.x, yz.y, a.y * yz.x);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        S[q] = fma(er, sU[m * 3 + q].x, S[q]);
+        D[q] = fma(ei, sU[m * 3 + q].y, D[q]);
+      }
+    }
+    double *ke = kelem + ((size_t)row * Nc + i) * 6;
+    // tetrahedra 0, 1, 2 at 1/2 + eps_q; their partners 5, 3, 4 at 1/2 - eps_q
+    ke[0] = exp(amp * (S[0] - D[0]));
+    ke[5] = exp(amp * (S[0] + D[0]));
+    ke[1] = exp(amp * (S[1] - D[1]));
+    ke[3] = exp(amp * (S[1] + D[1]));
+    ke[2] = exp(amp * (S[2] - D[2]));
+    ke[4] = exp(amp * (S[2] + D[2]));
+  }
+}
+
 __device__ __forceinline__ int lattice_code(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
 
 // the Kuhn tetrahedra as compile-time functions (kPerms above), so that the
@@ -167,10 +253,11 @@ __device__ __forceinline__ double pick27(const double (&acc)[27], int code) {
   return v;
 }
 
-// one slot's rows of one level
+// one slot's rows of one level (kelem: FP64 or FP32 field)
+template <class TK>
 __global__ void __launch_bounds__(ABLK) cube_assemble_kernel(
     int nrows, const int *__restrict__ rows, const int *__restrict__ perm, int off, int N,
-    const int *__restrict__ rowptr, const int *__restrict__ col, const float *__restrict__ kelem, double h,
+    const int *__restrict__ rowptr, const int *__restrict__ col, const TK *__restrict__ kelem, double h,
     double *__restrict__ v64, float *__restrict__ v32, const int *__restrict__ c2s, double *__restrict__ sv64,
     float *__restrict__ sv32, double *__restrict__ dinv64, float *__restrict__ dinv32) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -317,15 +404,40 @@ int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, 
   return 0;
 }
 
-int k_cube_assemble(gmg_mg *mg, const Level &L, const SlotLevel &sl, const float *kelem, double h,
-                    const int *c2s) {
+int k_cube_field64(gmg_mg *mg, int Nc, const double *w_dev, const double *phi_dev, int M, double amp,
+                   double2 *tables, double *kelem) {
+  GMG_CHECK(M <= GMG_FIELD_MAX_M, "field with %d features (at most %d)", M, GMG_FIELD_MAX_M);
+  if (upload_constants(mg->device)) return 1;
+  double2 *X = tables, *Y = X + (size_t)M * Nc, *ZP = Y + (size_t)M * Nc, *U = ZP + (size_t)M * Nc;
+  const int nt = M * (3 * Nc + 3);
+  cube_field64_tables_kernel<<<grid_of(nt), ABLK, 0, mg->stream>>>(Nc, 1.0 / double(Nc), M, w_dev, phi_dev, X, Y,
+                                                                    ZP, U);
+  ACHECK(mg);
+  const int bt = std::min(128, std::max(32, (Nc + 31) / 32 * 32));
+  cube_field64_kernel<<<unsigned(Nc) * unsigned(Nc), bt, 0, mg->stream>>>(Nc, M, amp, X, Y, ZP, U, kelem);
+  ACHECK(mg);
+  return 0;
+}
+
+template <class TK>
+static int assemble_t(gmg_mg *mg, const Level &L, const SlotLevel &sl, const TK *kelem, double h, const int *c2s) {
   GMG_CHECK(L.s == 1 && L.A.v32 && L.dinv32, "cube assembly: scalar level with FP32 copies expected");
   if (upload_constants(mg->device)) return 1;
-  cube_assemble_kernel<<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(
+  cube_assemble_kernel<TK><<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(
       sl.nrows, sl.rows, L.perm_dev, sl.off, sl.N, L.A.rowptr, L.A.col, kelem, h, L.A.v64, L.A.v32, c2s,
       L.sell_v64, L.sell_v32, L.dinv64, L.dinv32);
   ACHECK(mg);
   return 0;
+}
+
+int k_cube_assemble(gmg_mg *mg, const Level &L, const SlotLevel &sl, const float *kelem, double h,
+                    const int *c2s) {
+  return assemble_t(mg, L, sl, kelem, h, c2s);
+}
+
+int k_cube_assemble64(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *kelem, double h,
+                      const int *c2s) {
+  return assemble_t(mg, L, sl, kelem, h, c2s);
 }
 
 int k_cube_rhs(gmg_mg *mg, const Level &L, const SlotLevel &sl, uint64_t seed, double *b, double *x) {

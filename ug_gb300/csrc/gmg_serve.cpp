@@ -16,6 +16,7 @@
 #include <cstring>
 #include <memory>
 
+#include "fields.h"
 #include "gmg_internal.h"
 #include "gmg_np.h"
 #include "gmg_serve.h"
@@ -35,8 +36,12 @@ struct gmg_pool {
   std::vector<int *> c2s;                    // per level: CSR entry -> sliced ELLPACK entry
   std::vector<int *> rows;                   // per level: the slots' rows (slot k at blk_ptr[k])
   std::vector<std::vector<SlotLevel>> sl;    // [slot][level]
-  float *kelem = nullptr;                    // element coefficients of one level
-  uint32_t *prm_dev = nullptr, *prm_host = nullptr;  // field features, per slot and level
+  int field_prec = GMG_PREC_FP64;            // precision of the coefficient field at admission
+  float *kelem = nullptr;                    // element coefficients of one level (FP32 field)
+  double *kelem64 = nullptr;                 // ... (FP64 field)
+  double2 *ftab = nullptr;                   // FP64 field: phase tables of one level
+  double *fw_dev = nullptr, *fw_host = nullptr;  // FP64 field: w (M x 3) and phi (M) per slot
+  uint32_t *prm_dev = nullptr, *prm_host = nullptr;  // FP32 field features, per slot and level
   size_t prm_stride = 0;                     // uint32 per slot
   double *first_dev = nullptr, *first_host = nullptr;
   double *norm_scratch = nullptr;            // partial sums + ticket of the admission norm
@@ -50,6 +55,10 @@ struct gmg_pool {
     for (int *p : c2s) if (p) cudaFree(p);
     for (int *p : rows) if (p) cudaFree(p);
     if (kelem) cudaFree(kelem);
+    if (kelem64) cudaFree(kelem64);
+    if (ftab) cudaFree(ftab);
+    if (fw_dev) cudaFree(fw_dev);
+    if (fw_host) cudaFreeHost(fw_host);
     if (prm_dev) cudaFree(prm_dev);
     if (prm_host) cudaFreeHost(prm_host);
     if (first_dev) cudaFree(first_dev);
@@ -139,10 +148,10 @@ int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int 
     }
   }
   const long long nemax = 6LL << (3 * nref);
-  GMG_CUDA(cudaMalloc(&P->kelem, sizeof(float) * nemax));
-  P->prm_stride = size_t(nl) * GMG_FIELD_MAX_M * 4;
-  GMG_CUDA(cudaMalloc(&P->prm_dev, sizeof(uint32_t) * P->prm_stride * nslots));
-  GMG_CUDA(cudaMallocHost(&P->prm_host, sizeof(uint32_t) * P->prm_stride * nslots));
+  GMG_CUDA(cudaMalloc(&P->kelem64, sizeof(double) * nemax));
+  GMG_CUDA(cudaMalloc(&P->ftab, sizeof(double2) * GMG_FIELD_MAX_M * (3 * (1 << nref) + 6)));
+  GMG_CUDA(cudaMalloc(&P->fw_dev, sizeof(double) * GMG_FIELD_MAX_M * 4 * nslots));
+  GMG_CUDA(cudaMallocHost(&P->fw_host, sizeof(double) * GMG_FIELD_MAX_M * 4 * nslots));
   GMG_CUDA(cudaMalloc(&P->first_dev, sizeof(double) * GMG_MAX_S * nslots));
   GMG_CUDA(cudaMallocHost(&P->first_host, sizeof(double) * GMG_MAX_S * nslots));
   GMG_CUDA(cudaMalloc(&P->norm_scratch, sizeof(double) * (SLOT_NORM_BLOCKS * GMG_MAX_S + 1)));
@@ -188,24 +197,47 @@ int gmg_pool_admit(gmg_pool *p, int k, unsigned long long seed, double corr, dou
   GMG_CHECK(p->state[k] == SLOT_FREE, "gmg_pool_admit: slot %d is not free", k);
   gmg_mg *mg = p->mg;
   const int nl = p->nref + 1, top = p->nref;
-  uint32_t *ph = p->prm_host + p->prm_stride * k, *pd = p->prm_dev + p->prm_stride * k;
-  std::vector<float> amp(nl, 0.0f);
-  std::vector<int> M(nl, 0);
-  if (var > 0.0) {
-    std::vector<uint32_t> prm;
-    for (int l = 0; l < nl; ++l) {
-      cube_field_params(seed, corr, var, l, prm, &amp[l], &M[l]);
-      std::memcpy(ph + size_t(l) * GMG_FIELD_MAX_M * 4, prm.data(), prm.size() * 4);
-    }
-    GMG_CUDA(cudaMemcpyAsync(pd, ph, p->prm_stride * 4, cudaMemcpyHostToDevice, mg->stream));
-  }
-  for (int l = 0; l < nl; ++l) {
-    const float *ke = nullptr;
+  if (p->field_prec == GMG_PREC_FP64) {
+    // the field's features exactly as the host generator draws them
+    int M = 0;
+    double amp = 0.0;
+    double *fh = p->fw_host + size_t(k) * GMG_FIELD_MAX_M * 4, *fd = p->fw_dev + size_t(k) * GMG_FIELD_MAX_M * 4;
     if (var > 0.0) {
-      if (k_cube_field(mg, 1 << l, pd + size_t(l) * GMG_FIELD_MAX_M * 4, M[l], amp[l], p->kelem)) return 1;
-      ke = p->kelem;
+      ugfx::LogNormalField f(seed, 3, corr, var, GMG_FIELD_MAX_M);
+      M = f.M;
+      amp = f.amp;
+      std::memcpy(fh, f.w.data(), sizeof(double) * M * 3);
+      std::memcpy(fh + GMG_FIELD_MAX_M * 3, f.phi.data(), sizeof(double) * M);
+      GMG_CUDA(cudaMemcpyAsync(fd, fh, sizeof(double) * GMG_FIELD_MAX_M * 4, cudaMemcpyHostToDevice, mg->stream));
     }
-    if (k_cube_assemble(mg, mg->lev[l], p->sl[k][l], ke, 1.0 / double(1 << l), p->c2s[l])) return 1;
+    for (int l = 0; l < nl; ++l) {
+      const double *ke = nullptr;
+      if (var > 0.0) {
+        if (k_cube_field64(mg, 1 << l, fd, fd + GMG_FIELD_MAX_M * 3, M, amp, p->ftab, p->kelem64)) return 1;
+        ke = p->kelem64;
+      }
+      if (k_cube_assemble64(mg, mg->lev[l], p->sl[k][l], ke, 1.0 / double(1 << l), p->c2s[l])) return 1;
+    }
+  } else {
+    uint32_t *ph = p->prm_host + p->prm_stride * k, *pd = p->prm_dev + p->prm_stride * k;
+    std::vector<float> amp(nl, 0.0f);
+    std::vector<int> M(nl, 0);
+    if (var > 0.0) {
+      std::vector<uint32_t> prm;
+      for (int l = 0; l < nl; ++l) {
+        cube_field_params(seed, corr, var, l, prm, &amp[l], &M[l]);
+        std::memcpy(ph + size_t(l) * GMG_FIELD_MAX_M * 4, prm.data(), prm.size() * 4);
+      }
+      GMG_CUDA(cudaMemcpyAsync(pd, ph, p->prm_stride * 4, cudaMemcpyHostToDevice, mg->stream));
+    }
+    for (int l = 0; l < nl; ++l) {
+      const float *ke = nullptr;
+      if (var > 0.0) {
+        if (k_cube_field(mg, 1 << l, pd + size_t(l) * GMG_FIELD_MAX_M * 4, M[l], amp[l], p->kelem)) return 1;
+        ke = p->kelem;
+      }
+      if (k_cube_assemble(mg, mg->lev[l], p->sl[k][l], ke, 1.0 / double(1 << l), p->c2s[l])) return 1;
+    }
   }
   const Level &T = mg->lev[top];
   if (k_cube_rhs(mg, T, p->sl[k][top], seed, (double *)p->b->lev[top], (double *)p->x->lev[top])) return 1;
@@ -218,6 +250,24 @@ int gmg_pool_admit(gmg_pool *p, int k, unsigned long long seed, double corr, dou
   p->iters[k] = 0;
   p->conv[k] = 0;
   p->need_first[k] = 1;
+  return 0;
+}
+
+int gmg_pool_set_field_precision(gmg_pool *p, int precision) {
+  if (!p || (precision != GMG_PREC_FP64 && precision != GMG_PREC_FP32)) {
+    set_error("gmg_pool_set_field_precision: bad arguments");
+    return 1;
+  }
+  GMG_CHECK(!p->inflight, "gmg_pool_set_field_precision: an iteration is in flight (poll first)");
+  if (precision == GMG_PREC_FP32 && !p->kelem) {
+    const int nl = p->nref + 1;
+    const long long nemax = 6LL << (3 * p->nref);
+    GMG_CUDA(cudaMalloc(&p->kelem, sizeof(float) * nemax));
+    p->prm_stride = size_t(nl) * GMG_FIELD_MAX_M * 4;
+    GMG_CUDA(cudaMalloc(&p->prm_dev, sizeof(uint32_t) * p->prm_stride * p->nslots));
+    GMG_CUDA(cudaMallocHost(&p->prm_host, sizeof(uint32_t) * p->prm_stride * p->nslots));
+  }
+  p->field_prec = precision;
   return 0;
 }
 

@@ -2,6 +2,7 @@
 // of a batched hierarchy (gmg_assemble.cu), used by gmg_serve.cpp.
 #pragma once
 #include <cstdint>
+#include <cuda_runtime.h>
 #include <vector>
 
 #include "gmg_internal.h"
@@ -24,6 +25,14 @@ void cube_field_params(uint64_t seed, double corr, double var, int level, std::v
                        int *M);
 // k of every tetrahedron of a level with Nc cells per axis
 int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem);
+// the FP64 field of a level with Nc cells per axis from the features w (M x 3)
+// and phi (M) of LogNormalField: tables (M (3 Nc + 6) double2) of per-axis and
+// per-tetrahedron phase factors, then k of every tetrahedron
+int k_cube_field64(gmg_mg *mg, int Nc, const double *w_dev, const double *phi_dev, int M, double amp,
+                   double2 *tables, double *kelem);
+// ... assembly from an FP64 field
+int k_cube_assemble64(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *kelem, double h,
+                      const int *c2s);
 // the slot's rows of level L from k (kelem == nullptr: k = 1); c2s maps CSR
 // entries to sliced-ELLPACK entries (nullptr if the level has none)
 int k_cube_assemble(gmg_mg *mg, const Level &L, const SlotLevel &sl, const float *kelem, double h, const int *c2s);

@@ -69,15 +69,23 @@ def slot_bytes(nref: int) -> int:
     return int(total * 1.15)
 
 
+def pool_bytes(nref: int, nslots: int) -> int:
+    """Device bytes of a pool: its slots plus the admission's FP64 field of
+    the finest level (one coefficient per tetrahedron)."""
+    return nslots * slot_bytes(nref) + 6 * 8 ** nref * 8
+
+
 class Pool:
     """One gmg_pool: `nslots` slots of depth `nref`."""
 
     def __init__(self, nref: int, nslots: int, smoother: str = "gs", red: float = 1e-8, maxit: int = 100,
-                 device: int = 0, stream=None):
+                 device: int = 0, stream=None, field_fp64: bool = True):
         h = C.c_void_p()
         if lib().gmg_pool_create(nref, nslots, smoother.encode(), red, maxit, device, C.byref(h)):
             _err("gmg_pool_create")
         self._h = h
+        if not field_fp64 and lib().gmg_pool_set_field_precision(h, 1):
+            _err("gmg_pool_set_field_precision")
         self.nref, self.nslots = nref, nslots
         if stream is not None:
             lib().gmg_pool_set_stream(h, stream)
@@ -181,18 +189,23 @@ class Server:
 
     def __init__(self, depths=range(2, 8), layout=None, hbm_fraction: float = 0.5, smoother: str = "gs",
                  red: float = 1e-8, maxit: int = 100, corr: float = 0.1, var: float = 1.0, device: int = 0,
-                 slots=None):
+                 slots=None, field_fp64: bool = False):
+        """field_fp64: admissions evaluate the coefficient field in FP64 (the
+        host generator's problem to 1e-12; on GB300 ~23 ms of FP64 work per
+        depth-7 admission, more than a 200 req/s stream leaves) instead of
+        FP32 (~1 ms, k within ~1e-6)."""
         import torch
         self.corr, self.var = corr, var
+        self.field_fp64 = field_fp64
         depths = list(depths)
         if layout is None:
             layout = {L: ((1, slots[L]) if slots else self.DEFAULT.get(L, (2, 1))) for L in depths}
         budget = hbm_fraction * free_device_memory(device)
-        need = sum(slot_bytes(L) * n * m for L, (n, m) in layout.items())
+        need = sum(pool_bytes(L, m) * n for L, (n, m) in layout.items())
         if need > budget:  # shrink the largest depths' pool counts to the budget
             for L in sorted(layout, reverse=True):
                 while need > budget and layout[L][0] > 1:
-                    need -= slot_bytes(L) * layout[L][1]
+                    need -= pool_bytes(L, layout[L][1])
                     layout[L] = (layout[L][0] - 1, layout[L][1])
         if need > budget:
             raise GmgError(f"pools need {need / 1e9:.1f} GB, {budget / 1e9:.1f} GB available")
@@ -205,7 +218,7 @@ class Server:
             for _ in range(npools):
                 st = torch.cuda.Stream(device=device)
                 self.streams.append(st)
-                self.pools[L].append(Pool(L, nslots, smoother, red, maxit, device, st.cuda_stream))
+                self.pools[L].append(Pool(L, nslots, smoother, red, maxit, device, st.cuda_stream, field_fp64))
         self.slots = {L: n * m for L, (n, m) in layout.items()}
 
     def warm(self, seed: int = 1):
