@@ -196,6 +196,17 @@ int gmg_mg_set_new_vectors(gmg_mg *mg, int level, const int *vnew);
  * batched hierarchies. */
 int gmg_mg_update_values(gmg_mg *mg, int level, const double *val);
 
+/* The interpolation matrix of a fine level (UG's IMATRIX: the VISTART list
+ * of every VECTOR, built by AddInterpolationMatrix / CreateIMatrix,
+ * np/algebra/transgrid.cc:1028, gm/algebra.cc:7601), used by a transfer
+ * numproc in its matrix mode (`npinit <transfer> $M`, transfer.cc:564:
+ * RestrictByMatrix / InterpolateCorrectionByMatrix, transgrid.cc:1113, 1292):
+ * per VECTOR of `level` in list order (rowptr, n+1) the level-1 VECTORs it
+ * couples to (col, level-1 list order) with an s*s block each (val, row-major
+ * coarse component by fine component, as MVALUE of an interpolation matrix).
+ * Copied; replaces an earlier one.  Not for batched hierarchies. */
+int gmg_mg_set_imatrix(gmg_mg *mg, int level, const int *rowptr, const int *col, const double *val);
+
 /* NP_LINEAR_SOLVER (np/procs/ls.h:79-132); Solver takes (abslimit, reduction)
  * in the order of np/procs/ls.cc:637. */
 int gmg_ls_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *baselevel, int *result);
@@ -227,6 +238,9 @@ int gmg_l_ilu_factors(gmg_mg *mg, int level, double *lu);
 int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *M, gmg_vec *d);             /* ugiter.cc:4444 */
 int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp);            /* 462 */
 int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp); /* 529 */
+/* with the level's interpolation matrix (gmg_mg_set_imatrix): transgrid.cc:1113 / 1292 */
+int gmg_restrict_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp);
+int gmg_interpolate_correction_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp);
 
 /* ------------------------------------------------ allocation-free norm
  * No counterpart in the reference.  Per-component 2-norms of a device array

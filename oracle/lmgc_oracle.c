@@ -364,6 +364,70 @@ void orc_interpolate(const orc_level *fine, double *to, const double *from, cons
   }
 }
 
+/* RestrictByMatrix_General, np/algebra/transgrid.cc:1113-1247 (flag 0): the
+ * coarse vectors with VNCLASS >= NEWDEF_CLASS are reset; every fine vector
+ * with VCLASS >= NEWDEF_CLASS adds block * d to each coarse vector of its
+ * interpolation matrix, in the components that coarse vector's VECSKIP
+ * leaves free (block row i times the fine vector, summed over j first);
+ * then the reset coarse vectors are scaled by damp if any damp != 1.  (UG's
+ * CRITBIT filter is never set on these hierarchies.) */
+void orc_restrict_imat(const orc_level *fine, const orc_imat *M, const orc_level *coarse, double *to,
+                       const double *from, const double *damp) {
+  const int s = fine->s, ss = s * s;
+  for (int c = 0; c < coarse->n; ++c)
+    if (coarse->vnclass[c] >= NEWDEF_CLASS)
+      for (int r = 0; r < s; ++r) to[(size_t)c * s + r] = 0.0;
+  for (int f = 0; f < fine->n; ++f) {
+    if (fine->vclass[f] < NEWDEF_CLASS) continue;
+    const double *v = from + (size_t)f * s;
+    for (int k = M->rowptr[f]; k < M->rowptr[f + 1]; ++k) {
+      const int c = M->col[k], sk = coarse->skip[c];
+      const double *m = M->val + (size_t)k * ss;
+      for (int i = 0; i < s; ++i) {
+        if (sk & (1 << i)) continue;
+        double sum = 0.0;
+        for (int j = 0; j < s; ++j) sum += m[i * s + j] * v[j];
+        to[(size_t)c * s + i] += sum;
+      }
+    }
+  }
+  int scale = 0;
+  for (int r = 0; r < s; ++r) scale |= damp[r] != 1.0;
+  if (scale)
+    for (int c = 0; c < coarse->n; ++c)
+      if (coarse->vnclass[c] >= NEWDEF_CLASS)
+        for (int r = 0; r < s; ++r) to[(size_t)c * s + r] *= damp[r];
+}
+
+/* InterpolateCorrectionByMatrix_General, transgrid.cc:1292-1386 (flag 0):
+ * the fine level is reset; every fine vector takes, in each component its
+ * VECSKIP leaves free, the transposed blocks of its interpolation matrix
+ * times the coarse vectors (sum over the coarse components first, coarse
+ * vectors in list order); then every fine vector is scaled by damp if any
+ * damp != 1. */
+void orc_interpolate_imat(const orc_level *fine, const orc_imat *M, double *to, const double *from,
+                          const double *damp) {
+  const int s = fine->s, ss = s * s;
+  memset(to, 0, sizeof(double) * (size_t)fine->n * s);
+  for (int f = 0; f < fine->n; ++f) {
+    const int sk = fine->skip[f];
+    for (int k = M->rowptr[f]; k < M->rowptr[f + 1]; ++k) {
+      const double *m = M->val + (size_t)k * ss, *w = from + (size_t)M->col[k] * s;
+      for (int i = 0; i < s; ++i) {
+        if (sk & (1 << i)) continue;
+        double sum = 0.0;
+        for (int j = 0; j < s; ++j) sum += m[j * s + i] * w[j];
+        to[(size_t)f * s + i] += sum;
+      }
+    }
+  }
+  int scale = 0;
+  for (int r = 0; r < s; ++r) scale |= damp[r] != 1.0;
+  if (scale)
+    for (int f = 0; f < fine->n; ++f)
+      for (int r = 0; r < s; ++r) to[(size_t)f * s + r] *= damp[r];
+}
+
 /* StandardIntNewNodeVector, np/algebra/transgrid.cc:354-430: every fine
  * vector with VNEW set takes the coarse values through its transfer row (a
  * corner copy, or the father element's shape functions GNs), every
@@ -485,11 +549,17 @@ static int lmgc(orc_ws *w, int l) {
   const orc_level *Lc = &mg->lev[l - 1];
   double one[ORC_MAX_S];
   for (int r = 0; r < ORC_MAX_S; ++r) one[r] = 1.0;
-  orc_restrict(L, Lc, w->b[l - 1], b, one);
+  if (mg->imat)
+    orc_restrict_imat(L, &mg->imat[l], Lc, w->b[l - 1], b, one);
+  else
+    orc_restrict(L, Lc, w->b[l - 1], b, one);
   memset(w->c[l - 1], 0, sizeof(double) * (size_t)Lc->n * Lc->s);
   for (int g = 0; g < mg->gamma; ++g)
     if ((rc = lmgc(w, l - 1))) return rc;
-  orc_interpolate(L, t, w->c[l - 1], mg->cdamp);
+  if (mg->imat)
+    orc_interpolate_imat(L, &mg->imat[l], t, w->c[l - 1], mg->cdamp);
+  else
+    orc_interpolate(L, t, w->c[l - 1], mg->cdamp);
   vadd(c, t, len);
   orc_matmul_minus(L, b, t);
   for (int i = 0; i < mg->nu2; ++i) {

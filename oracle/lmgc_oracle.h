@@ -39,6 +39,17 @@ typedef struct {
 
 enum { ORC_JAC = 0, ORC_GS = 1, ORC_ILU = 2 };
 
+/* An interpolation matrix of a fine level (UG's IMATRIX: the VISTART list of
+ * every fine VECTOR): per fine vector (CSR over the fine level, list order)
+ * the coarse vectors it couples to, each with an s x s block stored coarse
+ * component major (val[k*s*s + i*s + j]: coarse component i, fine
+ * component j), as MVALUE of an interpolation matrix. */
+typedef struct {
+  const int *rowptr;  /* fine n + 1 */
+  const int *col;     /* coarse vector index */
+  const double *val;  /* rowptr[n] * s * s */
+} orc_imat;
+
 typedef struct {
   int nlevels;            /* levels 0..nlevels-1 */
   const orc_level *lev;
@@ -52,6 +63,10 @@ typedef struct {
    * component of the base-level defect is already below its abslimit
    * (default ABS_LIMIT = 1e-10, np/procs/ls.cc:66, 389-391, 689) */
   double base_abslimit[ORC_MAX_S];
+  /* the transfer's matrix mode (`npinit transfer $M`): imat[l] is level l's
+   * interpolation matrix (l >= 1), used for RestrictDefect and
+   * InterpolateCorrection instead of the standard weights; NULL = standard */
+  const orc_imat *imat;
 } orc_mg;
 
 /* ---- kernels (one level) ---- */
@@ -68,6 +83,10 @@ void orc_interpolate(const orc_level *fine, double *to_fine, const double *from_
 void orc_interpolate_new(const orc_level *fine, const int *vnew, double *x_fine,
                          const double *x_coarse);                                 /* StandardIntNewNodeVector */
 void orc_project(const orc_level *fine, double *x_coarse, const double *x_fine);  /* StandardProject */
+void orc_restrict_imat(const orc_level *fine, const orc_imat *M, const orc_level *coarse, double *to_coarse,
+                       const double *from_fine, const double *damp);              /* RestrictByMatrix */
+void orc_interpolate_imat(const orc_level *fine, const orc_imat *M, double *to_fine, const double *from_coarse,
+                          const double *damp);                                    /* InterpolateCorrectionByMatrix */
 
 /* ---- solver ----
  * Solves A x = b on level top = nlevels-1 with ls + lmgc.  x (finest, n*s)

@@ -67,7 +67,12 @@ class _MG(C.Structure):
     _fields_ = [("nlevels", C.c_int), ("lev", C.c_void_p), ("baselevel", C.c_int),
                 ("nu1", C.c_int), ("nu2", C.c_int), ("gamma", C.c_int), ("smoother", C.c_int),
                 ("damp", C.c_double * MAX_S), ("beta", C.c_double * MAX_S),
-                ("cdamp", C.c_double * MAX_S), ("base_abslimit", C.c_double * MAX_S)]
+                ("cdamp", C.c_double * MAX_S), ("base_abslimit", C.c_double * MAX_S),
+                ("imat", C.c_void_p)]
+
+
+class _Imat(C.Structure):
+    _fields_ = [("rowptr", C.c_void_p), ("col", C.c_void_p), ("val", C.c_void_p)]
 
 
 _lib = None
@@ -90,6 +95,8 @@ def lib():
         L.orc_interpolate.argtypes = [P, P, P, P]
         L.orc_interpolate_new.argtypes = [P, P, P, P]
         L.orc_project.argtypes = [P, P, P]
+        L.orc_restrict_imat.argtypes = [P, P, P, P, P, P]
+        L.orc_interpolate_imat.argtypes = [P, P, P, P, P]
         L.orc_ls_solve.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_ls_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_cg_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
@@ -164,7 +171,19 @@ class Hierarchy:
     and (l >= 1) prowptr, pcol, pw.  The C structs point into these arrays, so
     the object keeps them alive."""
 
-    def __init__(self, levels: list[dict]):
+    def __init__(self, levels: list[dict], imat: list | None = None):
+        """imat: per level an interpolation matrix {rowptr, col, val} (UG's
+        IMATRIX; None on level 0), used by the transfer's matrix mode."""
+        self.imat = None
+        if imat is not None:
+            self.imat = [None if m is None else {"rowptr": np.ascontiguousarray(m["rowptr"], np.int32),
+                                                 "col": np.ascontiguousarray(m["col"], np.int32),
+                                                 "val": np.ascontiguousarray(m["val"], np.float64)}
+                         for m in imat]
+            self._ci = (_Imat * len(self.imat))()
+            for i, m in enumerate(self.imat):
+                if m is not None:
+                    self._ci[i] = _Imat(_p(m["rowptr"]), _p(m["col"]), _p(m["val"]))
         self.levels = []
         for L in levels:
             d = {"n": int(L["n"]), "s": int(L["s"])}
@@ -192,7 +211,11 @@ class Hierarchy:
                 q = f"P{l}_"
                 L.update(prowptr=fx[q + "rowptr"], pcol=fx[q + "col"], pw=fx[q + "w"])
             levels.append(L)
-        return cls(levels)
+        imat = None
+        if int(fx.get("imat", [0])[0]):
+            imat = [None] + [{"rowptr": fx[f"M{l}_rowptr"], "col": fx[f"M{l}_col"], "val": fx[f"M{l}_val"]}
+                             for l in range(1, len(levels))]
+        return cls(levels, imat)
 
     def lev(self, l):
         return C.byref(self._c[l])
@@ -235,6 +258,21 @@ class Hierarchy:
         to = np.zeros(L["n"] * L["s"]); fr = np.ascontiguousarray(from_coarse, np.float64)
         dm = np.ones(MAX_S) if damp is None else np.resize(np.asarray(damp, np.float64), MAX_S)
         lib().orc_interpolate(self.lev(l), _p(to), _p(fr), _p(dm)); return to
+
+    def restrict_imat(self, l, to_coarse, from_fine, damp=None):
+        """RestrictByMatrix with level l's interpolation matrix."""
+        to = np.array(to_coarse, np.float64); fr = np.ascontiguousarray(from_fine, np.float64)
+        dm = np.ones(MAX_S) if damp is None else np.resize(np.asarray(damp, np.float64), MAX_S)
+        lib().orc_restrict_imat(self.lev(l), C.byref(self._ci[l]), self.lev(l - 1), _p(to), _p(fr), _p(dm))
+        return to
+
+    def interpolate_imat(self, l, from_coarse, damp=None):
+        """InterpolateCorrectionByMatrix with level l's interpolation matrix."""
+        L = self.levels[l]
+        to = np.zeros(L["n"] * L["s"]); fr = np.ascontiguousarray(from_coarse, np.float64)
+        dm = np.ones(MAX_S) if damp is None else np.resize(np.asarray(damp, np.float64), MAX_S)
+        lib().orc_interpolate_imat(self.lev(l), C.byref(self._ci[l]), _p(to), _p(fr), _p(dm))
+        return to
 
     def interpolate_new(self, l, vnew, x_fine, x_coarse):
         """StandardIntNewNodeVector: fine vectors with VNEW take P x_coarse."""
@@ -319,8 +357,11 @@ class Hierarchy:
         return x, it, bool(conv.value), hist[: (it + 1) * s].reshape(it + 1, s)
 
     def _mg(self, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None, beta=None, cdamp=None,
-            base_abslimit=1e-10):
+            base_abslimit=1e-10, matrix_transfer=False):
         mg = _MG()
+        if matrix_transfer:
+            assert self.imat is not None, "no interpolation matrices"
+            mg.imat = C.addressof(self._ci)
         mg.nlevels = len(self.levels); mg.lev = C.addressof(self._c)
         mg.baselevel, mg.nu1, mg.nu2, mg.gamma = baselevel, nu1, nu2, gamma
         mg.smoother = SMOOTHERS[smoother] if isinstance(smoother, str) else smoother
@@ -333,12 +374,16 @@ class Hierarchy:
 
     def ls_solve(self, rhs, *, smoother="jac", baselevel=0, nu1=2, nu2=2, gamma=1, damp=None,
                  beta=None, cdamp=None, red=1e-10, abslimit=1e-50, maxit=100, x0=None,
-                 base_abslimit=1e-10, _solver="ls"):
+                 base_abslimit=1e-10, _solver="ls", matrix_transfer=False):
         """ls + lmgc as configured by `npinit lmgc $n1 $n2 $g $b` and `npinit ls
-        $red $abslimit $m`.  Returns (x, iterations, converged, history)."""
+        $red $abslimit $m` (matrix_transfer: `npinit transfer $M`).  Returns
+        (x, iterations, converged, history)."""
         top = len(self.levels) - 1
         s = self.levels[top]["s"]
         mg = _MG()
+        if matrix_transfer:
+            assert self.imat is not None, "no interpolation matrices"
+            mg.imat = C.addressof(self._ci)
         mg.nlevels = len(self.levels); mg.lev = C.addressof(self._c)
         mg.baselevel, mg.nu1, mg.nu2, mg.gamma = baselevel, nu1, nu2, gamma
         mg.smoother = SMOOTHERS[smoother] if isinstance(smoother, str) else smoother

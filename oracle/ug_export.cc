@@ -21,10 +21,15 @@
 //     replaying the ls loop (dset, Lmgc, dadd, dnrm2x) through the same
 //     numprocs;
 //   * the same problem solved with UG's cg and bcgs (ls.cc:901, 1711)
-//     preconditioned by the same lmgc: iterations, defects, solution.
+//     preconditioned by the same lmgc: iterations, defects, solution;
+//   * with imat = block: an interpolation matrix (IMATRIX, VISTART lists) on
+//     every fine level, the standard transfer's weights times a seeded block
+//     near the identity, its known-answer vectors of RestrictByMatrix and
+//     InterpolateCorrectionByMatrix (transgrid.cc:1113, 1292), and every
+//     solve above with the transfer in its matrix mode (`$M`).
 //
 // usage: ug_export{2d,3d} <problem> <nref> <baselevel> <smoother> <seed> <out>
-//        [maxit] [local_levels]
+//        [maxit] [local_levels] [order] [imat]
 //   problem  : poisson  (2D: one Q1 quad; 3D: six Kuhn tets of the unit cube)
 //              diffusion (3D only: P1 with k = exp(g) per element, corr 0.1, var 1)
 //              elasticity (2D only: P1 triangles, plane strain E=1 nu=0.3, 2x2 blocks)
@@ -194,6 +199,8 @@ int main(int argc, char **argv) {
   // UG's ordering numprocs (order.cc:931) applied to every level after the
   // assembly: "bw" (order.bw) or "lex:<config>" (order.lex $config <config>)
   std::string order = argc > 9 ? argv[9] : "none";
+  // "block": IMATRIX on every fine level and the transfer in `$M` mode
+  const bool imat = argc > 10 && std::string(argv[10]) == "block";
   char cmd[512];
   int ug_argc = 1;
   char *ug_argv0 = argv[0];
@@ -210,7 +217,9 @@ int main(int argc, char **argv) {
   CreateBoundaryValueProblem("bvp", BndCond, 0, NULL, 0, NULL);
   if (lshape && create_lshape_domain()) { fprintf(stderr, "L-shaped domain\n"); return 1; }
   run(lshape ? "configure bvp $d LShape;" : DIMX == 2 ? "configure bvp $d Quadrilateral;" : "configure bvp $d Hexahedron;");
-  run(s == 1 ? "newformat fmt $V n1: vt 20 $M implicit(vt): mt 4;" : "newformat fmt $V n2: vt 20 $M implicit(vt): mt 4;");
+  if (imat) run(s == 1 ? "newformat fmt $V n1: vt 20 $M implicit(vt): mt 4 $I n1;"
+                       : "newformat fmt $V n2: vt 20 $M implicit(vt): mt 4 $I n2;");
+  else run(s == 1 ? "newformat fmt $V n1: vt 20 $M implicit(vt): mt 4;" : "newformat fmt $V n2: vt 20 $M implicit(vt): mt 4;");
   run("new mg $b bvp $f fmt $h 4000M;");
   if (lshape) {
     // three unit squares, each split by its diagonal through the re-entrant corner (node 2)
@@ -440,6 +449,53 @@ int main(int argc, char **argv) {
     putd("rhs_all", ball);  // every level, levels concatenated
   }
 
+  // ---- interpolation matrices (IMATRIX): for every fine vector and every
+  // coarse vector of its standard transfer row (weight c), the block
+  // c (I + 0.2 (U - 1/2)), U uniform[0,1) per entry from a seeded sequence
+  // (coarse-component-major, as MVALUE of an interpolation matrix); exported
+  // per level in VISTART order
+  if (imat) {
+    ugfx::SplitMix irng(seed * 104729 + 3);
+    for (int l = 1; l <= top; ++l) {
+      GRID *g = GRID_ON_LEVEL(mg, l);
+      for (NODE *nd = FIRSTNODE(g); nd; nd = SUCCN(nd)) {
+        VECTOR *v = NVECTOR(nd);
+        std::vector<std::pair<VECTOR *, double>> row;
+        if (CORNERTYPE(nd)) {
+          row.push_back({NVECTOR((NODE *)NFATHER(nd)), 1.0});
+        } else {
+          VERTEX *vx = MYVERTEX(nd);
+          ELEMENT *fe = VFATHER(vx);
+          int nc = CORNERS_OF_ELEM(fe);
+          DOUBLE c[MAX_CORNERS_OF_ELEM];
+          GNs(nc, LCVECT(vx), c);
+          for (int i = 0; i < nc; ++i)
+            if (c[i] != 0.0) row.push_back({NVECTOR(CORNER(fe, i)), c[i]});
+        }
+        for (auto &e : row) {
+          MATRIX *im = CreateIMatrix(g, v, e.first);
+          if (!im) { fprintf(stderr, "CreateIMatrix failed\n"); return 1; }
+          for (int i = 0; i < s; ++i)
+            for (int j = 0; j < s; ++j)
+              MVALUEPTR(im, 0)[i * s + j] = e.second * ((i == j ? 1.0 : 0.0) + 0.2 * (irng.uniform() - 0.5));
+        }
+      }
+      auto &L = g_lev[l];
+      std::vector<int> mptr(1, 0), mcol;
+      std::vector<double> mval;
+      for (VECTOR *v : L.vecs) {
+        for (MATRIX *im = VISTART(v); im; im = MNEXT(im)) {
+          mcol.push_back(g_lev[l - 1].idx.at(MDEST(im)));
+          for (int k = 0; k < s * s; ++k) mval.push_back(MVALUEPTR(im, 0)[k]);
+        }
+        mptr.push_back((int)mcol.size());
+      }
+      std::string q = "M" + std::to_string(l) + "_";
+      puti(q + "rowptr", mptr); puti(q + "col", mcol); putd(q + "val", mval);
+    }
+  }
+  put1i("imat", imat ? 1 : 0);
+
   // ---- kernel known-answer vectors on the finest level
   ugfx::SplitMix rng(seed * 7919 + 17);
   GRID *gt = GRID_ON_LEVEL(mg, top);
@@ -493,10 +549,29 @@ int main(int argc, char **argv) {
     putd("kat_interp_coarse", grab(kc, top - 1));
     if (StandardInterpolateCorrection(gt, kt, kc, one)) return 1;
     putd("kat_interp", grab(kt, top));
+    if (imat) {  // the matrix-mode transfers, plain and damped
+      VEC_SCALAR dm;
+      for (int i = 0; i < MAX_VEC_COMP; ++i) dm[i] = 0.7 - 0.1 * i;
+      fill(kc, gc);
+      putd("kat_mrestrict_pre", grab(kc, top - 1));
+      if (RestrictByMatrix(gt, kc, kd, one)) return 1;
+      putd("kat_mrestrict", grab(kc, top - 1));
+      fill(kc, gc);
+      putd("kat_mrestrict_damp_pre", grab(kc, top - 1));
+      if (RestrictByMatrix(gt, kc, kd, dm)) return 1;
+      putd("kat_mrestrict_damp", grab(kc, top - 1));
+      fill(kc, gc); fill(kt, gt);
+      putd("kat_minterp_coarse", grab(kc, top - 1));
+      if (InterpolateCorrectionByMatrix(gt, kt, kc, one)) return 1;
+      putd("kat_minterp", grab(kt, top));
+      fill(kt, gt);
+      if (InterpolateCorrectionByMatrix(gt, kt, kc, dm)) return 1;
+      putd("kat_minterp_damp", grab(kt, top));
+    }
   }
 
   // ---- full solve through UG's numprocs
-  run("npcreate transfer $c transfer; npinit transfer;");
+  run(imat ? "npcreate transfer $c transfer; npinit transfer $M;" : "npcreate transfer $c transfer; npinit transfer;");
   // ---- the transfer numproc's solution operations on every level
   // (transfer.cc:775 InterpolateNewVectors -> StandardIntNewNodeVector,
   // transfer.cc:794 ProjectSolution -> StandardProject), with VNEW of the

@@ -18,8 +18,13 @@ def pytest_configure(config):
 
 def golden_names(kind="uniform"):
     """Fixture names: "uniform" (uniformly refined hierarchies, the surface is
-    the top level), "local" (the ls_* cases, locally refined) or "all"."""
+    the top level), "local" (the ls_* cases, locally refined), "all" (both),
+    or "imat" (the im_* cases: interpolation matrices on every fine level and
+    UG's transfer in its matrix mode, uniform and local)."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    if kind == "imat":
+        return [n for n in names if n.startswith("im_")]
+    names = [n for n in names if not n.startswith("im_")]
     if kind == "all":
         return names
     return [n for n in names if n.startswith("ls_") == (kind == "local")]

@@ -29,9 +29,10 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 
-# name: (dimension, problem, nref, baselevel, smoother, seed[, nloc[, order]]);
+# name: (dimension, problem, nref, baselevel, smoother, seed[, nloc[, order[, imat]]]);
 # order = one of UG's order numprocs run on every level after the assembly
-# ("bw" = order.bw, "lex:<config>" = order.lex $config <config>)
+# ("bw" = order.bw, "lex:<config>" = order.lex $config <config>); imat =
+# "block": interpolation matrices and the transfer's matrix mode
 CASES = {
     "q1_jac": (2, "poisson", 5, 2, "jac", 11),
     "q1_gs": (2, "poisson", 5, 2, "gs", 11),
@@ -51,6 +52,12 @@ CASES = {
     "p1lex_gs": (3, "poisson", 3, 0, "gs", 12, 0, "lex:dfl"),
     "elbw_ilu": (2, "elasticity", 4, 1, "ilu", 14, 0, "bw"),
     "ls_bw_gs": (2, "lshape", 2, 0, "gs", 22, 6, "bw"),
+    # the transfer in UG's matrix mode (`$M`) on seeded block interpolation
+    # matrices (IMATRIX) near the standard transfer
+    "im_q1_gs": (2, "poisson", 5, 2, "gs", 11, 0, "none", "block"),
+    "im_el_ilu": (2, "elasticity", 4, 1, "ilu", 14, 0, "none", "block"),
+    "im_p1k_jac": (3, "diffusion", 3, 0, "jac", 13, 0, "none", "block"),
+    "im_ls_gs": (2, "lshape", 2, 0, "gs", 22, 6, "none", "block"),
 }
 
 
@@ -68,7 +75,8 @@ def main():
             raw = os.path.join(tmp, name + ".bin")
             nloc = rest[0] if rest else 0
             order = rest[1] if len(rest) > 1 else "none"
-            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw, "100", str(nloc), order],
+            imat = rest[2] if len(rest) > 2 else "none"
+            subprocess.run([exe, problem, str(nref), str(base), sm, str(seed), raw, "100", str(nloc), order, imat],
                            check=True, stdout=subprocess.DEVNULL)
             fx = oracle.read_ugfx(raw)
             arrays = {k: (np.array(v) if not isinstance(v, str) else np.array(v)) for k, v in fx.items()}

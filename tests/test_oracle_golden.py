@@ -177,3 +177,34 @@ def test_surface_krylov_matches_ug(name, solver, oracle_mod):
     assert conv == bool(fx[f"{solver}_converged"][0]) and it == int(fx[f"{solver}_iters"][0])
     assert rel(x, fx[f"{solver}_x_all"]) <= 1e-12
     assert rel(hist[-1], fx[f"{solver}_last"]) <= 1e-10
+
+
+IMAT = golden_names("imat")
+
+
+@pytest.mark.parametrize("name", IMAT)
+def test_oracle_matrix_transfer_matches_ug(oracle_mod, name):
+    """The transfer's matrix mode (`npinit transfer $M`): RestrictByMatrix and
+    InterpolateCorrectionByMatrix on UG's interpolation matrices, plain and
+    damped, bit for bit, and UG's solves in that mode (iterations, defect
+    history, solution), on uniform and locally refined hierarchies."""
+    fx = load_golden(name)
+    H = oracle_mod.Hierarchy.from_ugfx(fx)
+    top = len(H.levels) - 1
+    dm = [0.7 - 0.1 * i for i in range(8)]
+    assert np.array_equal(H.restrict_imat(top, fx["kat_mrestrict_pre"], fx["kat_d"]), fx["kat_mrestrict"])
+    assert np.array_equal(H.restrict_imat(top, fx["kat_mrestrict_damp_pre"], fx["kat_d"], dm),
+                          fx["kat_mrestrict_damp"])
+    assert np.array_equal(H.interpolate_imat(top, fx["kat_minterp_coarse"]), fx["kat_minterp"])
+    assert np.array_equal(H.interpolate_imat(top, fx["kat_minterp_coarse"], dm), fx["kat_minterp_damp"])
+    sm = str(fx["smoother"])
+    kw = dict(smoother=sm, baselevel=int(fx["baselevel"][0]), damp=0.8 if sm == "jac" else 1.0, red=1e-10,
+              matrix_transfer=True)
+    if name.startswith("im_ls"):
+        x, it, conv, hist = H.ls_solve_surface(fx["rhs_all"], **kw)
+        assert rel(x, fx["ls_x_all"]) <= 1e-14
+    else:
+        x, it, conv, hist = H.ls_solve(fx["rhs"], **kw)
+        assert rel(x, fx["ls_x"]) <= 1e-14
+    assert it == int(fx["ls_iters"][0]) and conv == bool(fx["ls_converged"][0])
+    assert rel(hist.ravel(), fx["ls_hist"]) <= 1e-14

@@ -9,7 +9,7 @@ class roles, argument syntax and error behaviour as UG 3.12.1:
 
     mg = MultiGrid(levels)                   # flattened hierarchy (grid change)
     mg.createvector("sol", "rhs")
-    mg.npcreate("transfer", "transfer.gtransfer"); mg.npinit("transfer", "")
+    mg.npcreate("transfer", "transfer.gtransfer"); mg.npinit("transfer", transfer)
     mg.npcreate("smooth", "iter.gjac");     mg.npinit("smooth", "$damp 0.8")
     ...
     mg.npexecute("mgs", "$i $d $r $s $p")
@@ -106,7 +106,8 @@ def lib(build_if_missing: bool = True):
         "gmg_dscalx": ([P, I, P, P], I), "gmg_daxpy": ([P, I, P, P, P], I), "gmg_ddot": ([P, I, P, P, P], I),
         "gmg_l_jac": ([P, I, P, P, P], I), "gmg_l_lgs": ([P, I, P, P, P], I),
         "gmg_l_ilu_decomp": ([P, I, P, P], I), "gmg_l_luiter": ([P, I, P, P, P], I),
-        "gmg_l_ilu_factors": ([P, I, P], I),
+        "gmg_l_ilu_factors": ([P, I, P], I), "gmg_mg_set_imatrix": ([P, I, P, P, P], I),
+        "gmg_restrict_by_matrix": ([P, I, P, P, P], I), "gmg_interpolate_correction_by_matrix": ([P, I, P, P, P], I),
         "gmg_standard_restrict": ([P, I, P, P, P], I), "gmg_standard_interpolate_correction": ([P, I, P, P, P], I),
         "gmg_solve_host": ([P, C.c_char_p, P, P, P], I),
         "gmg_mg_create_batched": ([P, P, I, P, P], I), "gmg_mg_num_instances": ([P], I),
@@ -757,6 +758,25 @@ class MultiGrid:
         if lib().gmg_l_lgs(self._h, level, self.vec(v), self.mat(M), self.vec(d)):
             _err("l_lgs")
 
+    def set_imatrix(self, level, rowptr, col, val):
+        """The level's interpolation matrix (UG's IMATRIX, list order, s x s
+        blocks coarse component major) for the transfer's matrix mode ($M)."""
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        cl = np.ascontiguousarray(col, np.int32)
+        vl = np.ascontiguousarray(val, np.float64)
+        if lib().gmg_mg_set_imatrix(self._h, level, rp.ctypes.data, cl.ctypes.data, vl.ctypes.data):
+            _err("set_imatrix")
+
+    def restrict_by_matrix(self, level, to, frm, damp=None):
+        d = _sc(damp)
+        if lib().gmg_restrict_by_matrix(self._h, level, self.vec(to), self.vec(frm), _ptr(d)):
+            _err("RestrictByMatrix")
+
+    def interpolate_correction_by_matrix(self, level, to, frm, damp=None):
+        d = _sc(damp)
+        if lib().gmg_interpolate_correction_by_matrix(self._h, level, self.vec(to), self.vec(frm), _ptr(d)):
+            _err("InterpolateCorrectionByMatrix")
+
     def l_ilu_factors(self, level):
         """The ILU(0) factors of a level as l_ilubthdecomp leaves them (the
         device matrix layout of `matrix(level)`, processing order)."""
@@ -812,11 +832,17 @@ class MultiGrid:
             pass
 
 
+def imatrices_from_ugfx(fx: dict) -> list:
+    """The interpolation matrices of a UG export (None on level 0)."""
+    n = int(fx["nlevels"][0])
+    return [None] + [(fx[f"M{l}_rowptr"], fx[f"M{l}_col"], fx[f"M{l}_val"]) for l in range(1, n)]
+
+
 def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: int = 2, nu2: int = 2,
                damp: float | None = None, red: float = 1e-10, abslimit: float = 1e-50, maxit: int = 100,
                mixed: bool = False, x: str = "sol", b: str = "rhs", name: str = "mgs",
                fuse: int | None = None, graph: bool = True, bsmem: int | None = None,
-               dloop: bool = True, narrow: bool = True) -> str:
+               dloop: bool = True, narrow: bool = True, transfer: str = "") -> str:
     """The standard script of the workloads, as UG numproc commands:
 
         npcreate transfer $c gtransfer; npcreate smooth $c g<smoother>;
@@ -828,7 +854,7 @@ def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: in
             mg.vec(v)
         except GmgError:
             mg.createvector(v)
-    mg.npcreate("transfer", "transfer.gtransfer"); mg.npinit("transfer", "")
+    mg.npcreate("transfer", "transfer.gtransfer"); mg.npinit("transfer", transfer)
     mg.npcreate("smooth", f"iter.g{smoother}")
     if damp is None:
         damp = 0.8 if smoother == "jac" else 1.0

@@ -116,6 +116,12 @@ struct Level {
   std::vector<void *> own;      // cudaMalloc'd arrays owned outside the arena
   // transfer from level-1: P (rows = this level), R (rows = level-1 VECTORs)
   DevCSR P, R;
+  // the level's interpolation matrix (UG's IMATRIX, gmg_mg_set_imatrix) for
+  // the transfer's matrix mode: IP rows = this level's vectors, IR rows =
+  // level-1 vectors (its transpose restricted to NEWDEF rows); s x s blocks,
+  // coarse component major
+  bool has_imat = false;
+  DevCSR IP, IR;
   // son of every level-1 row: the row of this level that is its corner copy
   // (a transfer row with the single weight 1), -1 if none (StandardProject)
   int *son = nullptr;
@@ -358,6 +364,12 @@ int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // *failed_row = the smallest processing-order row whose diagonal block was
 // singular (nothing written then), else -1
 int k_ilu_factor(gmg_mg *mg, Level &L, const double *beta, const IluDev &D, int *failed_row);
+// RestrictByMatrix / InterpolateCorrectionByMatrix with the fine level's
+// interpolation matrix (F.has_imat); zero_coarse / acc as for the standard ones
+int k_restrict_imat(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from,
+                    const double *damp, void *zero_coarse = nullptr);
+int k_interpolate_imat(gmg_mg *mg, const Level &F, int prec, void *to, const void *from, const double *damp,
+                       void *acc);
 // coarse = (reset ? 0 : coarse) + R (damp*fine), honouring coarse VECSKIP
 // (zero_coarse, if given, is set to 0 on the coarse level in the same pass)
 int k_restrict(gmg_mg *mg, const Level &fine, const Level &coarse, int prec, void *to, const void *from,

@@ -2439,6 +2439,145 @@ int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b) {
   return 1;
 }
 
+// ------------------------------------------------------------ transfer by interpolation matrix
+// RestrictByMatrix (transgrid.cc:1113-1247) as a gather over the transposed
+// interpolation matrix (rows = coarse vectors, blocks coarse-component major):
+// reset rows (VNCLASS >= NEWDEF) start from zero, the others keep their value;
+// each block adds M d_v in the components the coarse VECSKIP leaves free; the
+// reset rows are then scaled by damp (if any damp != 1, SCALE).  zc (optional)
+// is set to zero on the coarse level in the same pass.
+template <class T, int S, bool SCALE>
+__global__ void __launch_bounds__(BLK) restrict_imat_kernel(int nc, const int *__restrict__ rrow,
+                                                            const int *__restrict__ rcol, const T *__restrict__ rval,
+                                                            const uint8_t *__restrict__ cflags,
+                                                            const uint8_t *__restrict__ cskip,
+                                                            const T *__restrict__ from, T *__restrict__ to, Damp<T> dm,
+                                                            T *__restrict__ zc) {
+  pdl_prologue();
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nc) return;
+  const bool reset = __ldg(cflags + w) & F_RESET;
+  const int sk = __ldg(cskip + w);
+  T acc[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) acc[i] = reset ? T(0) : to[(size_t)w * S + i];
+  for (int k = __ldg(rrow + w); k < __ldg(rrow + w + 1); ++k) {
+    const int v = __ldg(rcol + k);
+    const T *m = rval + (size_t)k * S * S;
+    T d[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) d[j] = from[(size_t)v * S + j];
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (sk & (1 << i)) continue;
+      T sum = T(0);
+#pragma unroll
+      for (int j = 0; j < S; ++j) sum = fma(__ldg(m + i * S + j), d[j], sum);
+      acc[i] += sum;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    to[(size_t)w * S + i] = (SCALE && reset) ? acc[i] * dm.d[i] : acc[i];
+    if (zc) zc[(size_t)w * S + i] = T(0);
+  }
+}
+
+// InterpolateCorrectionByMatrix (transgrid.cc:1292-1386): every fine vector
+// takes the transposed blocks of its interpolation matrix times the coarse
+// vectors in the components its VECSKIP leaves free (0 in the others), times
+// damp; ACC: acc += t as well (lmgc's dadd(c, t))
+template <class T, int S, bool ACC>
+__global__ void __launch_bounds__(BLK) interp_imat_kernel(int nf, const int *__restrict__ prow,
+                                                          const int *__restrict__ pcol, const T *__restrict__ pval,
+                                                          const uint8_t *__restrict__ fskip,
+                                                          const T *__restrict__ from, T *__restrict__ to, Damp<T> dm,
+                                                          T *__restrict__ acc) {
+  pdl_prologue();
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nf) return;
+  const int sk = __ldg(fskip + v);
+  T t[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) t[i] = T(0);
+  for (int k = __ldg(prow + v); k < __ldg(prow + v + 1); ++k) {
+    const int w = __ldg(pcol + k);
+    const T *m = pval + (size_t)k * S * S;
+    T c[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) c[j] = from[(size_t)w * S + j];
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      T sum = T(0);
+#pragma unroll
+      for (int j = 0; j < S; ++j) sum = fma(__ldg(m + j * S + i), c[j], sum);
+      t[i] += sum;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    const T r = (sk & (1 << i)) ? T(0) : t[i] * dm.d[i];
+    to[(size_t)v * S + i] = r;
+    if (ACC) acc[(size_t)v * S + i] += r;
+  }
+}
+
+int k_restrict_imat(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from,
+                    const double *damp, void *zero_coarse) {
+  GMG_CHECK(F.has_imat, "RestrictByMatrix: no interpolation matrix on this level");
+  if (C.n == 0) return 0;
+  bool scale = false;
+  for (int r = 0; r < F.s; ++r) scale = scale || damp[r] != 1.0;
+#define RM(TT, SS)                                                                                            \
+  do {                                                                                                        \
+    if (scale)                                                                                                \
+      GMG_LAUNCH((restrict_imat_kernel<TT, SS, true>), grid_for(C.n), BLK, C.n, F.IR.rowptr, F.IR.col,       \
+                 mval<TT>(F.IR), C.flags, C.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS),        \
+                 (TT *)zero_coarse);                                                                          \
+    else                                                                                                      \
+      GMG_LAUNCH((restrict_imat_kernel<TT, SS, false>), grid_for(C.n), BLK, C.n, F.IR.rowptr, F.IR.col,      \
+                 mval<TT>(F.IR), C.flags, C.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS),        \
+                 (TT *)zero_coarse);                                                                          \
+  } while (0)
+#define RMS(TT)                                 \
+  if (F.s == 1) RM(TT, 1);                      \
+  else if (F.s == 2) RM(TT, 2);                 \
+  else if (F.s == 3) RM(TT, 3);                 \
+  else { set_error("block size %d not compiled", F.s); return 1; }
+  if (prec == GMG_PREC_FP64) { RMS(double) }
+  else { GMG_CHECK(F.IR.v32, "FP32 interpolation matrix not built"); RMS(float) }
+#undef RMS
+#undef RM
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
+int k_interpolate_imat(gmg_mg *mg, const Level &F, int prec, void *to, const void *from, const double *damp,
+                       void *acc) {
+  GMG_CHECK(F.has_imat, "InterpolateCorrectionByMatrix: no interpolation matrix on this level");
+  if (F.n == 0) return 0;
+#define IM(TT, SS)                                                                                             \
+  do {                                                                                                         \
+    if (acc)                                                                                                   \
+      GMG_LAUNCH((interp_imat_kernel<TT, SS, true>), grid_for(F.n), BLK, F.n, F.IP.rowptr, F.IP.col,          \
+                 mval<TT>(F.IP), F.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS), (TT *)acc);      \
+    else                                                                                                       \
+      GMG_LAUNCH((interp_imat_kernel<TT, SS, false>), grid_for(F.n), BLK, F.n, F.IP.rowptr, F.IP.col,         \
+                 mval<TT>(F.IP), F.skip, (const TT *)from, (TT *)to, make_damp<TT>(damp, SS), (TT *)acc);      \
+  } while (0)
+#define IMS(TT)                                 \
+  if (F.s == 1) IM(TT, 1);                      \
+  else if (F.s == 2) IM(TT, 2);                 \
+  else if (F.s == 3) IM(TT, 3);                 \
+  else { set_error("block size %d not compiled", F.s); return 1; }
+  if (prec == GMG_PREC_FP64) { IMS(double) }
+  else { GMG_CHECK(F.IP.v32, "FP32 interpolation matrix not built"); IMS(float) }
+#undef IMS
+#undef IM
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_restrict(gmg_mg *mg, const Level &F, const Level &C, int prec, void *to, const void *from, const double *damp,
                void *zero_coarse) {
   if (C.n == 0) return 0;

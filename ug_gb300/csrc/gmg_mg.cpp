@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -936,6 +937,77 @@ extern "C" {
 // and base-level inverse if built); the fused coarse images are dropped and
 // rebuilt on their next use, and iterations captured as CUDA graphs are
 // re-captured.
+// an interpolation matrix for the transfer's matrix mode (UG's IMATRIX lists)
+int gmg_mg_set_imatrix(gmg_mg *mg, int level, const int *rowptr, const int *col, const double *val) {
+  GMG_CHECK(mg && rowptr && col && val, "gmg_mg_set_imatrix: bad arguments");
+  GMG_CHECK(level >= 1 && level < int(mg->lev.size()), "gmg_mg_set_imatrix: level %d has no coarser level", level);
+  GMG_CHECK(mg->batch.ninst == 0, "gmg_mg_set_imatrix: not for batched hierarchies");
+  Level &F = mg->lev[level];
+  const Level &C = mg->lev[level - 1];
+  const int nf = F.n, nc = C.n, s = F.s, ss = s * s;
+  std::vector<int> ifp(nf), icp(nc);
+  for (int i = 0; i < nf; ++i) ifp[F.perm[i]] = i;
+  for (int i = 0; i < nc; ++i) icp[C.perm[i]] = i;
+  const int nnz = rowptr[nf];
+  for (int o = 0; o < nf; ++o)
+    GMG_CHECK(rowptr[o] <= rowptr[o + 1], "gmg_mg_set_imatrix: row pointers decrease at row %d", o);
+  for (int k = 0; k < nnz; ++k)
+    GMG_CHECK(col[k] >= 0 && col[k] < nc, "gmg_mg_set_imatrix: coarse index %d out of range", col[k]);
+  // IP: fine rows in processing order, entries in their given order
+  std::vector<int> pr(nf + 1, 0), pc;
+  std::vector<double> pv;
+  pc.reserve(nnz);
+  pv.reserve(size_t(nnz) * ss);
+  for (int i = 0; i < nf; ++i) {
+    const int o = F.perm[i];
+    for (int k = rowptr[o]; k < rowptr[o + 1]; ++k) {
+      pc.push_back(icp[col[k]]);
+      pv.insert(pv.end(), val + size_t(k) * ss, val + size_t(k + 1) * ss);
+    }
+    pr[i + 1] = int(pc.size());
+  }
+  // IR: coarse rows in processing order; the NEWDEF fine rows' entries in
+  // fine list order (the order RestrictByMatrix accumulates them in)
+  std::vector<int> rr(nc + 1, 0), rc;
+  std::vector<double> rv;
+  for (int o = 0; o < nf; ++o)
+    if (F.h_flags[ifp[o]] & F_NEWDEF)
+      for (int k = rowptr[o]; k < rowptr[o + 1]; ++k) rr[icp[col[k]] + 1]++;
+  for (int w = 0; w < nc; ++w) rr[w + 1] += rr[w];
+  rc.resize(rr[nc]);
+  rv.resize(size_t(rr[nc]) * ss);
+  std::vector<int> fill(rr.begin(), rr.end() - 1);
+  for (int o = 0; o < nf; ++o)
+    if (F.h_flags[ifp[o]] & F_NEWDEF)
+      for (int k = rowptr[o]; k < rowptr[o + 1]; ++k) {
+        const int q = fill[icp[col[k]]]++;
+        rc[q] = ifp[o];
+        std::copy(val + size_t(k) * ss, val + size_t(k + 1) * ss, rv.begin() + size_t(q) * ss);
+      }
+  auto put = [&](auto **dst, const auto &src) -> int {
+    using E = typename std::remove_reference<decltype(src)>::type::value_type;
+    GMG_CUDA(cudaMalloc(dst, std::max<size_t>(src.size(), 1) * sizeof(E)));
+    F.own.push_back(*dst);
+    if (!src.empty()) GMG_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(E), cudaMemcpyHostToDevice));
+    return 0;
+  };
+  DevCSR P, R;
+  P.nrows = nf; P.nnz = pc.size();
+  R.nrows = nc; R.nnz = rc.size();
+  if (put(&P.rowptr, pr) || put(&P.col, pc) || put(&P.v64, pv) || put(&R.rowptr, rr) || put(&R.col, rc) ||
+      put(&R.v64, rv))
+    return 1;
+  if (mg->opts.fp32_copy) {
+    std::vector<float> pv32(pv.begin(), pv.end()), rv32(rv.begin(), rv.end());
+    if (put(&P.v32, pv32) || put(&R.v32, rv32)) return 1;
+  }
+  F.IP = P;
+  F.IR = R;
+  F.has_imat = true;
+  ++mg->graph_epoch;
+  return 0;
+}
+
 int gmg_mg_update_values(gmg_mg *mg, int level, const double *val) {
   if (!mg || level < 0 || level >= int(mg->lev.size()) || !val) {
     set_error("gmg_mg_update_values: bad arguments");

@@ -578,8 +578,10 @@ int NPTransfer::Init(const Args &a) {  // TransferInit / NPTransferInit
   a.get_int("baselevel", &baselevel);
   for (double &d : damp) d = 1.0;
   a.get_sc("damp", damp);
-  GMG_CHECK(!a.option("M") && !a.option("S") && !a.option("D"),
-            "transfer: only the standard (shape-function) mode is implemented");
+  imat = a.option("M");
+  GMG_CHECK(!a.option("R"), "transfer: $R (RestrictByMatrix_s) is not implemented");
+  GMG_CHECK(!a.option("S") && !a.option("D"),
+            "transfer: the scaled ($S) and Dirichlet re-assembly ($D) modes are not implemented");
   GMG_CHECK(!a.option("l"), "transfer: $l (MinimizeLevel in AdaptCorrection) is not implemented");
   return (!A && !b && !x && !c) ? NP_ACTIVE : NP_EXECUTABLE;
 }
@@ -592,6 +594,9 @@ int NPTransfer::RestrictDefect(int level, gmg_vec *to, gmg_vec *from, gmg_mat *,
   if (check_level(mg, level)) return 1;
   GMG_CHECK(level >= 1, "RestrictDefect: no coarser grid below level %d", level);
   GMG_CHECK(to->prec == from->prec, "RestrictDefect: precision mismatch");
+  if (imat)  // RestrictByMatrix, transgrid.cc:1113
+    return k_restrict_imat(mg, mg->lev[level], mg->lev[level - 1], to->prec, vlev(to, level - 1), vlev(from, level),
+                           dmp);
   return k_restrict(mg, mg->lev[level], mg->lev[level - 1], to->prec, vlev(to, level - 1), vlev(from, level), dmp);
 }
 
@@ -601,12 +606,15 @@ int NPTransfer::InterpolateCorrection(int level, gmg_vec *to, gmg_vec *from, gmg
   if (check_level(mg, level)) return 1;
   GMG_CHECK(level >= 1, "InterpolateCorrection: no coarser grid below level %d", level);
   GMG_CHECK(to->prec == from->prec, "InterpolateCorrection: precision mismatch");
+  if (imat)  // InterpolateCorrectionByMatrix, transgrid.cc:1292
+    return k_interpolate_imat(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), dmp, nullptr);
   return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), dmp, nullptr);
 }
 
 // InterpolateNewVectors, transfer.cc:775: StandardIntNewNodeVector on levels fl+1..tl
 int NPTransfer::InterpolateNewVectors(int fl, int tl, gmg_vec *xv, int *result) {
   GMG_CHECK(xv && fl >= 0 && tl < int(mg->lev.size()), "InterpolateNewVectors: bad arguments");
+  GMG_CHECK(!imat, "InterpolateNewVectors: the matrix mode (InterpolateNewVectorsByMatrix) is not implemented");
   for (int l = fl + 1; l <= tl; ++l)
     if (k_interpolate_new(mg, mg->lev[l], xv->prec, vlev(xv, l), vlev(xv, l - 1))) return 1;
   return 0;
@@ -639,6 +647,8 @@ int NPTransfer::Execute(const Args &a) {
 }
 
 std::string NPTransfer::Display() const {
+  if (imat)
+    return "class " + cls + "\nRestrict = RestrictByMatrix\nInterpolateCor = InterpolateCorrectionByMatrix\n";
   return "class " + cls + "\nRestrict = StandardRestrict\nInterpolateCor = StandardInterpolateCorrection\n";
 }
 
@@ -689,7 +699,7 @@ std::string NPLmgc::Display() const {
 
 int NPLmgc::fusable_smoother() const {
   if (fuse_rows <= 0 || gamma != 1 || !Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return -1;
-  if (typeid(*Transfer) != typeid(NPTransfer)) return -1;
+  if (typeid(*Transfer) != typeid(NPTransfer) || Transfer->imat) return -1;
   const NPLs *bls = dynamic_cast<const NPLs *>(BaseSolver);
   if (!bls || !bls->is_exact_base()) return -1;
   if (typeid(*PreSmooth) != typeid(*PostSmooth)) return -1;
@@ -761,9 +771,11 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   if (PreSmooth->IterAccN(level, t, bv, Am, cv, nu1, result)) return 1;
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};  // Factor_One
   if (typeid(*Transfer) == typeid(NPTransfer)) {
-    // StandardRestrict and dset(c_{l-1}, 0) in one pass
-    if (k_restrict(mg, mg->lev[level], mg->lev[level - 1], prec, vlev(bv, level - 1), vlev(bv, level), one,
-                   vlev(cv, level - 1)))
+    // StandardRestrict (or RestrictByMatrix) and dset(c_{l-1}, 0) in one pass
+    if (Transfer->imat ? k_restrict_imat(mg, mg->lev[level], mg->lev[level - 1], prec, vlev(bv, level - 1),
+                                         vlev(bv, level), one, vlev(cv, level - 1))
+                       : k_restrict(mg, mg->lev[level], mg->lev[level - 1], prec, vlev(bv, level - 1),
+                                    vlev(bv, level), one, vlev(cv, level - 1)))
       return 1;
   } else {
     if (Transfer->RestrictDefect(level, bv, bv, Am, one, result)) return 1;
@@ -773,7 +785,11 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
     if (Iter(level - 1, cv, bv, Am, result)) return 1;
   // t = P c_{l-1} * damp; c += t (fused); b -= A t
   if (dynamic_cast<NPTransfer *>(Transfer) && typeid(*Transfer) == typeid(NPTransfer)) {
-    if (k_interpolate(mg, mg->lev[level], prec, vlev(t, level), vlev(cv, level - 1), damp, vlev(cv, level))) return 1;
+    if (Transfer->imat ? k_interpolate_imat(mg, mg->lev[level], prec, vlev(t, level), vlev(cv, level - 1), damp,
+                                            vlev(cv, level))
+                       : k_interpolate(mg, mg->lev[level], prec, vlev(t, level), vlev(cv, level - 1), damp,
+                                       vlev(cv, level)))
+      return 1;
   } else {
     if (Transfer->InterpolateCorrection(level, t, cv, Am, damp, result)) return 1;
     if (k_add(mg, prec, vlev(cv, level), vlev(t, level), vlen(mg, level))) return 1;
@@ -2116,6 +2132,24 @@ int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_
   GMG_CHECK(level >= 1, "no coarser grid");
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
   return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), damp ? damp : one, nullptr);
+}
+
+int gmg_restrict_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
+  MGV(mg, level);
+  GMG_CHECK(level >= 1, "no coarser grid");
+  GMG_CHECK(to && from && to->prec == from->prec, "RestrictByMatrix: vectors missing or of different precision");
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
+  return k_restrict_imat(mg, mg->lev[level], mg->lev[level - 1], to->prec, vlev(to, level - 1), vlev(from, level),
+                         damp ? damp : one);
+}
+int gmg_interpolate_correction_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
+  MGV(mg, level);
+  GMG_CHECK(level >= 1, "no coarser grid");
+  GMG_CHECK(to && from && to->prec == from->prec,
+            "InterpolateCorrectionByMatrix: vectors missing or of different precision");
+  static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
+  return k_interpolate_imat(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), damp ? damp : one,
+                            nullptr);
 }
 
 int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double *x_host, gmg_lresult *lr) {

@@ -107,6 +107,9 @@ struct NPTransfer : gmg_np {
   gmg_mat *A = nullptr;
   double damp[GMG_MAX_S];
   int baselevel = 0;
+  // `$M` (IMAT_MODE, transfer.cc:564): restriction and interpolation by the
+  // levels' interpolation matrices (gmg_mg_set_imatrix)
+  bool imat = false;
   int kind() const override { return NPK_TRANSFER; }
   int Init(const Args &a) override;  // TransferInit + NPTransferInit, transfer.cc:553, 296
   virtual int PreProcess(int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result);
