@@ -773,9 +773,11 @@ def run_ours(args):
     mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True, autotune=True, device=local)
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     mg.createvector("sol", "rhs", "rhs0")
-    G.setup_lmgc(mg, "gs", baselevel=0, red=RED, abslimit=1e-50, name="mgs64")
+    graph = not args.no_graph
+    G.setup_lmgc(mg, "gs", baselevel=0, red=RED, abslimit=1e-50, name="mgs64", graph=graph, dloop=graph)
     mg.npcreate("mgs32", "linear_solver.gls")
-    mg.npinit("mgs32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    mg.npinit("mgs32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1"
+                       f" $graph {int(graph)} $dloop {int(graph)}")
     top = mg.top
     mg.upload("rhs0", top, gen.rhs)
     mg.ls_preprocess("mgs64", top, "sol", "rhs")
@@ -930,6 +932,9 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH_N, help="instances of the batched workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests of the serving stream")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="C2 solvers without CUDA graphs ($graph 0 $dloop 0): every kernel an individual launch, "
+                         "for profilers that do not see inside conditional graphs; not a benchmark setting")
     ap.add_argument("--only", default="all", choices=["all", "c2", "roofline", "c1", "local", "batched", "serving"],
                     help="run one workload alone and print its JSON (profiling runs); c2: the headline solve "
                          "without the other workloads; roofline: the C2 roofline kernels only, warmup + steps "
