@@ -553,22 +553,36 @@ def run_batched(args, stream, flush_l2, world, rank):
 SERVE_RATE, SERVE_LEVELS = 200.0, (2, 7)
 
 
-def run_serving(args, rank):
+def run_serving(args, rank, mixed=(), extras=True):
     """The request loop: a seeded Poisson stream (mean 200 req/s) of 3D P1
     diffusion solves, depths U{2..7} (125 .. 2,146,689 unknowns), log-normal
     k (corr 0.1, var 1), FP32 multicolour-GS V(2,2) in FP64 refinement to
-    1e-8, admitted into resident pools by free device memory."""
+    1e-8, admitted into resident pools by free device memory.  mixed: groups
+    of depths that share mixed pools (their V-cycles batched level by level
+    across mesh sizes); extras: also time admissions, sample the served
+    results' accuracy and time the CPU baseline."""
     import torch
     import ug_gb300 as G
     from ug_gb300.serve import Server, poisson_stream
     t0 = time.perf_counter()
-    srv = Server(depths=range(SERVE_LEVELS[0], SERVE_LEVELS[1] + 1), device=torch.cuda.current_device())
+    srv = Server(depths=range(SERVE_LEVELS[0], SERVE_LEVELS[1] + 1), device=torch.cuda.current_device(),
+                 mixed=mixed, grow_after_ms=50.0)
     srv.warm()  # every pool's temporaries and CUDA graph
     setup_s = time.perf_counter() - t0
     srv.run(poisson_stream(max(24, args.warmup * 12), SERVE_RATE, SERVE_LEVELS, seed=77))
     reqs = poisson_stream(args.serve_requests, SERVE_RATE, SERVE_LEVELS, seed=2026 + rank)
     with ClockSampler(torch.cuda.current_device()) as clk:
         st = srv.run(reqs)
+    if not extras:
+        srv.close()
+        st.p50_ms, st.p99_ms, st.mean_ms = (reduce_over_ranks(v) for v in (st.p50_ms, st.p99_ms, st.mean_ms))
+        st.throughput = reduce_over_ranks(st.throughput, "sum")
+        return {"workload": "the stream of `serving` (same requests)", "mixed_pools": [list(g) for g in mixed],
+                "requests": st.completed, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
+                "throughput_req_s": st.throughput, "all_converged": st.all_converged,
+                "per_depth": {str(k): v for k, v in st.per_depth.items()},
+                "queue_wait_ms": st.breakdown["queue_wait_ms"], "service_ms": st.breakdown["service_ms"],
+                "setup_s": setup_s, "clocks": clk.summary()}
     # the admission's device work per depth (field, assembly of every level,
     # right-hand side, first norm), timed alone after the stream, with the
     # stream's FP32 field and with the FP64 field
@@ -579,7 +593,7 @@ def run_serving(args, rank):
             G.lib().gmg_pool_set_field_precision(p._h, prec)
             ts = []
             for rep in range(3):
-                slot = p.free[0]
+                slot = p.free_slot(L)
                 torch.cuda.synchronize()
                 t1 = time.perf_counter()
                 p.admit(slot, 999 + rep, srv.corr, srv.var)
@@ -609,7 +623,7 @@ def run_serving(args, rank):
             e_slot, e_host, same_iters = [], [], True
             p = srv.pools[L][0]
             for r in sample:
-                slot = p.free[0]
+                slot = p.free_slot(L)
                 x, lr = p.solve(r.seed, srv.corr, srv.var, slot=slot)
                 same_iters = same_iters and lr.iters == r.iters
                 levels, rhs, _ = oracle.cube_levels(L, r.seed, CORR, VAR)
@@ -639,7 +653,9 @@ def run_serving(args, rank):
                                                  "host generator's; the FP64 field is the pools' option)",
            "accuracy_sample": served_err,
            "pools": {str(L): {"pools": n, "slots_each": m} for L, (n, m) in srv.layout.items()},
+           "mixed_pools": [list(g) for g in mixed],
            "setup_s": setup_s, "clocks": clk.summary(),
+           "pools_grown_while_serving": [[round(t, 3), L] for t, L in srv.grown],
            "note": "latency = completion - arrival (queueing, on-device assembly, all iterations, "
                    "solution not copied back); the published stream has 20k requests"}
     if rank == 0:
@@ -760,6 +776,7 @@ def run_ours(args):
         torch.sum(flush, dim=0, out=sink)
 
     single = {"c1": lambda: run_c1(args, stream, flush_l2, world, rank),
+              "serving_mixed": lambda: run_serving(args, rank, mixed=[(2, 3, 4, 5)], extras=False),
               "local": lambda: run_local(args, stream, flush_l2, world, rank),
               "batched": lambda: run_batched(args, stream, flush_l2, world, rank),
               "serving": lambda: run_serving(args, rank)}
@@ -884,6 +901,8 @@ def run_ours(args):
     local_c3 = run_local(args, stream, flush_l2, world, rank) if rest and not args.no_local else None
     batched = run_batched(args, stream, flush_l2, world, rank) if rest and not args.no_batched else None
     serving = run_serving(args, rank) if rest and not args.no_serving else None
+    serving_mixed = run_serving(args, rank, mixed=[(2, 3, 4, 5)], extras=False) if rest and not args.no_serving \
+        else None
 
     if rank == 0:
         r32, r64 = results["mgs32"], results["mgs64"]
@@ -915,6 +934,7 @@ def run_ours(args):
             "local_refinement": local_c3,
             "batched": batched,
             "serving": serving,
+            "serving_mixed_pools": serving_mixed,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -935,7 +955,8 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="C2 solvers without CUDA graphs ($graph 0 $dloop 0): every kernel an individual launch, "
                          "for profilers that do not see inside conditional graphs; not a benchmark setting")
-    ap.add_argument("--only", default="all", choices=["all", "c2", "roofline", "c1", "local", "batched", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "c2", "roofline", "c1", "local", "batched", "serving",
+                                                      "serving_mixed"],
                     help="run one workload alone and print its JSON (profiling runs); c2: the headline solve "
                          "without the other workloads; roofline: the C2 roofline kernels only, warmup + steps "
                          "repetitions each")

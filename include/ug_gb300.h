@@ -274,11 +274,20 @@ int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev,
  * pool idle (the last launch polled). */
 typedef struct gmg_pool gmg_pool;
 int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int maxit, int device, gmg_pool **out);
+/* A pool whose slots hold cubes of different depths (slot k refined
+ * depths[k] times, 1..9): one batched hierarchy whose level l holds level l
+ * of every slot that reaches it, so one ls iteration of the pool runs the
+ * V-cycles of requests of different mesh sizes together, level by level
+ * (each request still iterates and converges on its own). */
+int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, double red, int maxit, int device,
+                          gmg_pool **out);
 int gmg_pool_destroy(gmg_pool *pool);
 gmg_mg *gmg_pool_multigrid(gmg_pool *pool);
 int gmg_pool_set_stream(gmg_pool *pool, void *stream);
-/* slots, VECTORs of one slot's finest level, free slots */
+/* slots, VECTORs of the largest slot's finest level, free slots */
 int gmg_pool_slots(const gmg_pool *pool, int *nslots, int *n_top, int *free_slots);
+/* a slot's refinements and the VECTORs of its finest level */
+int gmg_pool_slot_info(const gmg_pool *pool, int slot, int *nref, int *n_top);
 int gmg_pool_admit(gmg_pool *pool, int slot, unsigned long long seed, double corr, double var);
 /* Precision of the coefficient field at admission: GMG_PREC_FP64 (the
  * default: k within ~1e-14 of gmg_gen_create's, so a slot holds the FP64

@@ -48,3 +48,15 @@ def test_generator_sizes():
         if top["skip"][i]:
             k0, k1 = top["rowptr"][i], top["rowptr"][i + 1]
             assert top["val"][k0] == 1.0 and not top["val"][k0 + 1:k1].any()
+
+
+def test_python_binding_declares_every_entry_point():
+    """The ctypes front end (ug_gb300/__init__.py) gives every entry point of
+    include/ug_gb300.h its argument and result types (a missing declaration
+    makes ctypes pass doubles as ints); gmg_nrm2x_static, which takes raw
+    device pointers, is declared by its caller."""
+    import re
+    hdr = open(os.path.join(ROOT, "include", "ug_gb300.h")).read()
+    src = open(os.path.join(ROOT, "ug_gb300", "__init__.py")).read()
+    names = set(re.findall(r"\b(gmg_\w+)\s*\(", hdr)) - {"gmg_nrm2x_static"}
+    assert sorted(n for n in names if f'"{n}"' not in src) == []

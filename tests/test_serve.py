@@ -136,3 +136,91 @@ def test_server_stream(G):
             xa, lra = p.solve(r.seed, slot=0)
             assert lra.iters == r.iters and np.array_equal(xa, r.x), (L, r.rid)
         p.close()
+
+
+@pytest.mark.gpu
+def test_mixed_pool_batches_depths(G):
+    """A mixed pool (slots of depths 2, 2, 3, 3, 4 in one batched hierarchy,
+    every iteration one V-cycle over all of them, level by level): a depth-3
+    request gives bitwise the same result alone in such a pool and joining it
+    while depth-2 and depth-4 requests come and go; and the same iterations
+    and solution to 1e-10 as in a pool of depth-3 slots only."""
+    from ug_gb300.serve import Pool
+    dep = [2, 2, 3, 3, 4]
+    seed = 515
+    alone = Pool(0, 0, depths=dep)
+    xa, lra = alone.solve(seed, slot=3)
+    alone.close()
+    mix = Pool(0, 0, depths=dep)
+    mix.free = []
+    mix.admit(0, 21, 0.1, 1.0)
+    mix.admit(4, 22, 0.1, 1.0)
+    mix.active = {0: 21, 4: 22}
+    got, it, joined = {}, 0, False
+    while mix.active:
+        if it == 2 and not joined:
+            mix.admit(3, seed, 0.1, 1.0)
+            mix.active[3] = seed
+            joined = True
+        mix.launch()
+        while (done := mix.poll()) is None:
+            pass
+        it += 1
+        for k in done:
+            s = mix.active.pop(k)
+            got[s] = mix.fetch(k)
+            if s == 21:
+                mix.admit(1, 23, 0.1, 1.0)  # another depth-2 request in the other depth-2 slot
+                mix.active[1] = 23
+    mix.close()
+    xm, lrm = got[seed]
+    assert lrm.converged and lrm.iters == lra.iters and np.array_equal(xm, xa)
+    assert all(got[q][1].converged for q in (21, 22, 23))
+    assert len(got[22][0]) == 17 ** 3 and len(got[21][0]) == 5 ** 3
+    uni = Pool(3, 2)
+    xu, lru = uni.solve(seed)
+    uni.close()
+    assert lru.iters == lrm.iters and rel(xm, xu) <= 1e-10
+
+
+@pytest.mark.gpu
+def test_server_stream_mixed_pools(G):
+    """The server with depths 1..3 sharing mixed pools: every request converges
+    and matches its solution in a pool of its own depth to 1e-10."""
+    from ug_gb300.serve import Pool, Server, poisson_stream
+    reqs = poisson_stream(18, 3000.0, levels=(1, 3), seed=10)
+    srv = Server(depths=range(1, 4), slots={1: 2, 2: 3, 3: 2}, mixed=[(1, 2, 3)])
+    assert len(srv.all_pools) == 1 and sorted(srv.all_pools[0].depths) == [1, 1, 2, 2, 2, 3, 3]
+    st = srv.run(reqs, keep_x=True)
+    srv.close()
+    assert st.completed == 18 and st.all_converged
+    for L, n in ((1, 2), (2, 3), (3, 2)):
+        p = Pool(L, n, field_fp64=srv.field_fp64)
+        for r in [q for q in reqs if q.nref == L][:3]:
+            xa, lra = p.solve(r.seed, slot=0)
+            assert lra.iters == r.iters and rel(r.x, xa) <= 1e-10, (L, r.rid)
+        p.close()
+
+
+@pytest.mark.gpu
+def test_server_grows_pools_by_free_memory(G):
+    """Demand-driven growth: one one-slot pool of depth 3 and a burst of
+    requests; once requests have waited, the server creates (on a helper
+    thread, the loop serving on) another pool of that shape because the
+    device's free memory allows it, and the burst finishes with every
+    request converged and equal to its alone solution."""
+    from ug_gb300.serve import Pool, Server, poisson_stream
+    reqs = [r for r in poisson_stream(400, 3000.0, levels=(3, 3), seed=12)][:120]
+    srv = Server(depths=[3], layout={3: (1, 1)}, grow_after_ms=5.0)
+    assert srv._may_grow(3)
+    st = srv.run(reqs, keep_x=True)
+    grown = list(srv.grown)
+    npools = len(srv.pools[3])
+    srv.close()
+    assert st.completed == len(reqs) and st.all_converged
+    assert grown and npools == 1 + len(grown) and all(L == 3 for _, L in grown)
+    p = Pool(3, 1, field_fp64=srv.field_fp64)
+    for r in reqs[:3]:
+        xa, lra = p.solve(r.seed)
+        assert lra.iters == r.iters and np.array_equal(xa, r.x)
+    p.close()

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 
 #include "fields.h"
@@ -26,9 +27,10 @@ using namespace gmg;
 enum { SLOT_FREE = 0, SLOT_ACTIVE = 1, SLOT_DONE = 2 };
 
 struct gmg_pool {
-  int nref = 0, nslots = 0, s = 1, maxit = 100;
+  int nref = 0, nslots = 0, s = 1, maxit = 100;  // nref: the deepest slot's refinements
   double red = 1e-8, abslimit = 1e-50;
-  gmg_gen *tmpl = nullptr;
+  std::vector<int> depth;                    // refinements of every slot's cube
+  std::map<int, gmg_gen *> tmpl;             // the cached topology of every depth
   gmg_mg *mg = nullptr;
   NPLs *ls = nullptr;
   gmg_vec *x = nullptr, *b = nullptr;
@@ -65,7 +67,7 @@ struct gmg_pool {
     if (norm_scratch) cudaFree(norm_scratch);
     if (first_host) cudaFreeHost(first_host);
     if (mg) gmg_mg_destroy(mg);
-    if (tmpl) gmg_gen_destroy(tmpl);
+    for (auto &kv : tmpl) gmg_gen_destroy(kv.second);
   }
 };
 
@@ -84,24 +86,44 @@ static int np(gmg_mg *mg, const char *name, const char *cls, const char *args) {
 extern "C" {
 
 int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int maxit, int device, gmg_pool **out) {
-  if (!out || nref < 1 || nref > 9 || nslots < 1 || !smoother) {
+  if (nslots < 1 || nslots > (1 << 20)) {
+    set_error("gmg_pool_create: bad arguments");
+    return 1;
+  }
+  std::vector<int> d(nslots, nref);
+  return gmg_pool_create_mixed(d.data(), nslots, smoother, red, maxit, device, out);
+}
+
+int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, double red, int maxit, int device,
+                          gmg_pool **out) {
+  if (!out || !depths || nslots < 1 || !smoother) {
     set_error("gmg_pool_create: bad arguments");
     return 1;
   }
   *out = nullptr;
+  for (int k = 0; k < nslots; ++k)
+    GMG_CHECK(depths[k] >= 1 && depths[k] <= 9, "gmg_pool_create: slot %d has %d refinements (1..9)", k, depths[k]);
   const std::string sm(smoother);
   GMG_CHECK(sm == "gs" || sm == "jac", "gmg_pool_create: smoother %s (gs or jac)", smoother);
   auto P = std::make_unique<gmg_pool>();
+  P->depth.assign(depths, depths + nslots);
+  const int nref = *std::max_element(depths, depths + nslots);
   P->nref = nref;
   P->nslots = nslots;
   P->red = red;
   P->maxit = maxit;
-  if (gmg_gen_create(1, nref, 0, 0.1, 0.0, &P->tmpl)) return 1;
-  const gmg_level_desc *levels = nullptr;
-  int nl = 0;
-  gmg_gen_levels(P->tmpl, &levels, &nl);
-  std::vector<const gmg_level_desc *> inst(nslots, levels);
-  std::vector<int> nls(nslots, nl);
+  std::vector<const gmg_level_desc *> inst(nslots);
+  std::vector<int> nls(nslots);
+  for (int k = 0; k < nslots; ++k) {
+    gmg_gen *&g = P->tmpl[depths[k]];
+    if (!g && gmg_gen_create(1, depths[k], 0, 0.1, 0.0, &g)) return 1;
+    const gmg_level_desc *levels = nullptr;
+    int nlk = 0;
+    gmg_gen_levels(g, &levels, &nlk);
+    inst[k] = levels;
+    nls[k] = nlk;
+  }
+  const int nl = nref + 1;
   gmg_mg_opts o{};
   o.order = GMG_ORDER_COLOR;
   o.fp32_copy = 1;
@@ -139,12 +161,15 @@ int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int 
     }
     GMG_CUDA(cudaMalloc(&P->rows[l], L.blk_rows.size() * 4));
     GMG_CUDA(cudaMemcpy(P->rows[l], L.blk_rows.data(), L.blk_rows.size() * 4, cudaMemcpyHostToDevice));
-    for (int k = 0; k < nslots; ++k) {
+    // blocks of this level: the slots that reach it, in slot order
+    for (int k = 0, blk = 0; k < nslots; ++k) {
+      if (P->depth[k] < l) continue;
       SlotLevel &q = P->sl[k][l];
       q.N = (1 << l) + 1;
       q.off = mg->batch.list_off[l][k];
-      q.nrows = L.blk_ptr[k + 1] - L.blk_ptr[k];
-      q.rows = P->rows[l] + L.blk_ptr[k];
+      q.nrows = L.blk_ptr[blk + 1] - L.blk_ptr[blk];
+      q.rows = P->rows[l] + L.blk_ptr[blk];
+      ++blk;
     }
   }
   const long long nemax = 6LL << (3 * nref);
@@ -184,8 +209,15 @@ int gmg_pool_set_stream(gmg_pool *p, void *stream) {
 int gmg_pool_slots(const gmg_pool *p, int *nslots, int *n_top, int *free_slots) {
   if (!p) return 1;
   if (nslots) *nslots = p->nslots;
-  if (n_top) *n_top = p->mg->batch.nrows_top[0];
+  if (n_top) *n_top = *std::max_element(p->mg->batch.nrows_top.begin(), p->mg->batch.nrows_top.end());
   if (free_slots) *free_slots = int(std::count(p->state.begin(), p->state.end(), int(SLOT_FREE)));
+  return 0;
+}
+
+int gmg_pool_slot_info(const gmg_pool *p, int k, int *nref, int *n_top) {
+  if (!p || k < 0 || k >= p->nslots) { set_error("gmg_pool_slot_info: bad slot"); return 1; }
+  if (nref) *nref = p->depth[k];
+  if (n_top) *n_top = p->mg->batch.nrows_top[k];
   return 0;
 }
 
@@ -196,7 +228,7 @@ int gmg_pool_admit(gmg_pool *p, int k, unsigned long long seed, double corr, dou
   GMG_CHECK(!p->inflight, "gmg_pool_admit: an iteration is in flight (poll first)");
   GMG_CHECK(p->state[k] == SLOT_FREE, "gmg_pool_admit: slot %d is not free", k);
   gmg_mg *mg = p->mg;
-  const int nl = p->nref + 1, top = p->nref;
+  const int nl = p->depth[k] + 1, top = p->depth[k];  // the slot's own levels
   if (p->field_prec == GMG_PREC_FP64) {
     // the field's features exactly as the host generator draws them
     int M = 0;
@@ -337,14 +369,19 @@ int gmg_pool_fetch(gmg_pool *p, int k, double *x_host, gmg_lresult *lr) {
   GMG_CHECK(p->state[k] == SLOT_DONE, "gmg_pool_fetch: slot %d has not finished", k);
   gmg_mg *mg = p->mg;
   const auto &B = mg->batch;
-  const auto &tl = B.tops[0];
   const int s = mg->lev[0].s, n = B.nrows_top[k];
   if (x_host) {
-    std::vector<int> ptr(tl.ninst + 1);
-    // instance k's rows in the top level's instance-major lists start at ptr[k]
-    GMG_CUDA(cudaMemcpy(ptr.data(), tl.ptr_dev, ptr.size() * 4, cudaMemcpyDeviceToHost));
-    if (k_pack_scatter_range(mg, GMG_PREC_FP64, (double *)mg->stage_dev, p->x->lev[p->nref], tl.rows_dev + ptr[k],
-                             tl.pack_dev + ptr[k], n, s))
+    // slot k's top level and its place in that level's instance-major lists
+    const gmg_mg::Batch::TopLevel *tl = nullptr;
+    int kl = -1;
+    for (const auto &t : B.tops)
+      for (int q = 0; q < t.ninst && kl < 0; ++q)
+        if (t.ids[q] == k) { tl = &t; kl = q; }
+    GMG_CHECK(tl, "gmg_pool_fetch: slot %d has no top level", k);
+    std::vector<int> ptr(tl->ninst + 1);
+    GMG_CUDA(cudaMemcpy(ptr.data(), tl->ptr_dev, ptr.size() * 4, cudaMemcpyDeviceToHost));
+    if (k_pack_scatter_range(mg, GMG_PREC_FP64, (double *)mg->stage_dev, p->x->lev[p->depth[k]],
+                             tl->rows_dev + ptr[kl], tl->pack_dev + ptr[kl], n, s))
       return 1;
     const size_t o = size_t(B.pack_off[k]) * s;
     GMG_CUDA(cudaMemcpyAsync(mg->stage_host + o, (double *)mg->stage_dev + o, sizeof(double) * n * s,
@@ -368,7 +405,7 @@ int gmg_pool_fetch(gmg_pool *p, int k, double *x_host, gmg_lresult *lr) {
 // the matrix of slot k on one level as the device holds it, in the template's
 // CSR order (instance list order, entries as in gmg_gen_levels)
 int gmg_pool_slot_matrix(gmg_pool *p, int k, int level, double *val) {
-  if (!p || k < 0 || k >= p->nslots || level < 0 || level > p->nref || !val) {
+  if (!p || k < 0 || k >= p->nslots || level < 0 || level > p->depth[k] || !val) {
     set_error("gmg_pool_slot_matrix: bad arguments");
     return 1;
   }

@@ -76,26 +76,46 @@ def pool_bytes(nref: int, nslots: int) -> int:
 
 
 class Pool:
-    """One gmg_pool: `nslots` slots of depth `nref`."""
+    """One gmg_pool: `nslots` slots of depth `nref`, or (depths given) one slot
+    per entry of `depths`, each of its own depth: a mixed pool, whose every
+    iteration runs the V-cycles of all its requests level by level together."""
 
     def __init__(self, nref: int, nslots: int, smoother: str = "gs", red: float = 1e-8, maxit: int = 100,
-                 device: int = 0, stream=None, field_fp64: bool = True):
+                 device: int = 0, stream=None, field_fp64: bool = True, depths=None):
         h = C.c_void_p()
-        if lib().gmg_pool_create(nref, nslots, smoother.encode(), red, maxit, device, C.byref(h)):
-            _err("gmg_pool_create")
+        if depths is not None:
+            d = np.ascontiguousarray(depths, np.int32)
+            if lib().gmg_pool_create_mixed(d.ctypes.data, len(d), smoother.encode(), red, maxit, device,
+                                           C.byref(h)):
+                _err("gmg_pool_create_mixed")
+            self.depths = [int(x) for x in d]
+        else:
+            if lib().gmg_pool_create(nref, nslots, smoother.encode(), red, maxit, device, C.byref(h)):
+                _err("gmg_pool_create")
+            self.depths = [nref] * nslots
         self._h = h
         if not field_fp64 and lib().gmg_pool_set_field_precision(h, 1):
             _err("gmg_pool_set_field_precision")
-        self.nref, self.nslots = nref, nslots
+        self.nref, self.nslots = max(self.depths), len(self.depths)
         if stream is not None:
             lib().gmg_pool_set_stream(h, stream)
-        ns, nt, fr = C.c_int(), C.c_int(), C.c_int()
-        lib().gmg_pool_slots(h, C.byref(ns), C.byref(nt), C.byref(fr))
-        self.n_top = nt.value
-        self.free = list(range(nslots))
+        self.n_top_of = []
+        for k in range(self.nslots):
+            dk, nt = C.c_int(), C.c_int()
+            lib().gmg_pool_slot_info(h, k, C.byref(dk), C.byref(nt))
+            self.n_top_of.append(nt.value)
+        self.n_top = max(self.n_top_of)
+        self.free = list(range(self.nslots))
         self.active: dict[int, object] = {}
         self.busy = False
-        self._done = np.zeros(nslots, np.int32)
+        self._done = np.zeros(self.nslots, np.int32)
+
+    def free_slot(self, depth: int):
+        """A free slot of this depth, or None."""
+        for k in self.free:
+            if self.depths[k] == depth:
+                return k
+        return None
 
     def admit(self, slot: int, seed: int, corr: float, var: float):
         if lib().gmg_pool_admit(self._h, slot, seed, corr, var):
@@ -119,7 +139,7 @@ class Pool:
 
     def fetch(self, slot: int, want_x: bool = True):
         lr = LResult()
-        x = np.empty(self.n_top) if want_x else None
+        x = np.empty(self.n_top_of[slot]) if want_x else None
         if lib().gmg_pool_fetch(self._h, slot, None if x is None else x.ctypes.data, C.byref(lr)):
             _err("gmg_pool_fetch")
         return x, lr
@@ -130,9 +150,10 @@ class Pool:
             _err("gmg_pool_slot_matrix")
         return v
 
-    def solve(self, seed: int, corr: float = 0.1, var: float = 1.0, slot: int | None = None):
+    def solve(self, seed: int, corr: float = 0.1, var: float = 1.0, slot: int | None = None, depth=None):
         """One request alone in this pool (blocking): (x, LResult)."""
-        slot = self.free[0] if slot is None else slot
+        if slot is None:
+            slot = self.free_slot(self.depths[0] if depth is None else depth)
         self.free.remove(slot)
         self.admit(slot, seed, corr, var)
         while True:
@@ -176,27 +197,42 @@ class ServeStats:
 
 
 class Server:
-    """Pools per depth, sized from free device memory, and the event loop.
+    """Pools sized from free device memory, and the event loop.
 
-    layout[L] = (pools, slots per pool).  Large depths get one-slot pools
-    (one instance saturates the GPU's bandwidth and a pool iterates all of
-    its slots, busy or not); small depths share few pools of many slots
+    layout[L] = (pools, slots per pool) per depth.  Large depths get one-slot
+    pools (one instance saturates the GPU's bandwidth and a pool iterates all
+    of its slots, busy or not); small depths share few pools of many slots
     (their cycles are latency-bound, so batching them is what pays).  Two or
     more pools per depth let a request start while another pool of its depth
-    is mid-iteration."""
+    is mid-iteration.  `mixed` lists groups of depths whose pools are shared:
+    a group's pools are mixed pools holding, per depth of the group, that
+    depth's slots per pool (the group has the largest pool count of its
+    depths), so requests of different mesh sizes run their V-cycles level by
+    level in the same iterations."""
 
     DEFAULT = {1: (2, 8), 2: (2, 8), 3: (2, 8), 4: (2, 8), 5: (2, 4), 6: (3, 1), 7: (4, 1), 8: (2, 1)}
 
     def __init__(self, depths=range(2, 8), layout=None, hbm_fraction: float = 0.5, smoother: str = "gs",
                  red: float = 1e-8, maxit: int = 100, corr: float = 0.1, var: float = 1.0, device: int = 0,
-                 slots=None, field_fp64: bool = False):
+                 slots=None, field_fp64: bool = False, mixed=(), grow_after_ms: float | None = None,
+                 grow_reserve: float = 0.1):
         """field_fp64: admissions evaluate the coefficient field in FP64 (the
-        host generator's problem to 1e-12; on GB300 ~23 ms of FP64 work per
+        host generator's problem to 1e-12; on GB300 ~12 ms of FP64 work per
         depth-7 admission, more than a 200 req/s stream leaves) instead of
-        FP32 (~1 ms, k within ~1e-6)."""
+        FP32 (~2 ms, k within ~1e-6).
+
+        grow_after_ms: a depth whose requests have waited this long for a
+        free slot gets one more pool of its layout's shape, if the device's
+        free memory (queried at that moment) covers it with grow_reserve of
+        the device left over; the pool is created and warmed on a helper
+        thread while the loop keeps serving, and joins the loop when ready
+        (None: the pools are fixed)."""
         import torch
         self.corr, self.var = corr, var
         self.field_fp64 = field_fp64
+        self.grow_after_ms, self.grow_reserve = grow_after_ms, grow_reserve
+        self._args = (smoother, red, maxit, device)
+        self.grown = []  # (seconds into the stream, depth) of every pool added while serving
         depths = list(depths)
         if layout is None:
             layout = {L: ((1, slots[L]) if slots else self.DEFAULT.get(L, (2, 1))) for L in depths}
@@ -210,24 +246,54 @@ class Server:
         if need > budget:
             raise GmgError(f"pools need {need / 1e9:.1f} GB, {budget / 1e9:.1f} GB available")
         self.layout = dict(layout)
-        self.pools = {}
+        groups = [tuple(g) for g in mixed if all(L in layout for L in g)]
+        grouped = {L for g in groups for L in g}
+        self.mixed_depths = grouped
+        groups += [(L,) for L in depths if L not in grouped]
+        self.groups = groups
+        self.pools = {L: [] for L in depths}  # depth -> the pools with slots of that depth
+        self.all_pools = []
         self.streams = []
-        for L in depths:
-            npools, nslots = layout[L]
-            self.pools[L] = []
-            for _ in range(npools):
+        for g in groups:
+            for _ in range(max(layout[L][0] for L in g)):
                 st = torch.cuda.Stream(device=device)
                 self.streams.append(st)
-                self.pools[L].append(Pool(L, nslots, smoother, red, maxit, device, st.cuda_stream, field_fp64))
-        self.slots = {L: n * m for L, (n, m) in layout.items()}
+                if len(g) == 1:
+                    pool = Pool(g[0], layout[g[0]][1], smoother, red, maxit, device, st.cuda_stream, field_fp64)
+                else:
+                    dep = [L for L in g for _ in range(layout[L][1])]
+                    pool = Pool(0, 0, smoother, red, maxit, device, st.cuda_stream, field_fp64, depths=dep)
+                self.all_pools.append(pool)
+                for L in g:
+                    self.pools[L].append(pool)
+        self.slots = {L: sum(p.depths.count(L) for p in self.pools[L]) for L in depths}
 
     def warm(self, seed: int = 1):
-        """One request through every pool: its first iteration allocates the
-        solver's temporaries and its second captures the iteration's CUDA
-        graph -- work that must not stall the event loop later."""
-        for pools in self.pools.values():
-            for p in pools:
-                p.solve(seed, self.corr, self.var)
+        """One request of each of its depths through every pool: the first
+        iteration allocates the solver's temporaries and the second captures
+        the iteration's CUDA graph -- work that must not stall the event loop
+        later."""
+        for p in self.all_pools:
+            for d in sorted(set(p.depths)):
+                p.solve(seed, self.corr, self.var, depth=d)
+
+    def _grow(self, L: int, ready: list):
+        """Create and warm one more pool of depth L (helper thread); the
+        event loop adds it from `ready`."""
+        import torch
+        smoother, red, maxit, device = self._args
+        torch.cuda.set_device(device)
+        st = torch.cuda.Stream(device=device)
+        pool = Pool(L, self.layout[L][1], smoother, red, maxit, device, st.cuda_stream, self.field_fp64)
+        pool.solve(1, self.corr, self.var)
+        torch.cuda.current_stream(device).synchronize()
+        ready.append((L, pool, st))
+
+    def _may_grow(self, L: int) -> bool:
+        import torch
+        smoother, red, maxit, device = self._args
+        free, total = torch.cuda.mem_get_info(device)
+        return free - pool_bytes(L, self.layout[L][1]) >= self.grow_reserve * total
 
     def run(self, requests: list[Request], keep_x: bool = False) -> ServeStats:
         """Serve the stream; latency breakdown per request: queue wait
@@ -249,54 +315,78 @@ class Server:
         pc = time.perf_counter
         t0 = pc()
         tprev = t0
+        ready, growing, waiting_since = [], set(), {}
+        import threading
         while done_count < len(order):
             tl = pc()
             gaps.append(tl - tprev)
             tprev = tl
             now = tl - t0
+            while ready:  # pools a helper thread finished
+                L, pool, st = ready.pop()
+                self.streams.append(st)
+                self.all_pools.append(pool)
+                self.pools[L].append(pool)
+                self.slots[L] += pool.nslots
+                growing.discard(L)
+                self.grown.append((now, L))
             while nxt < len(order) and order[nxt].arrival <= now:
                 pending[order[nxt].nref].append(order[nxt])
                 nxt += 1
             progressed = False
-            for L, pools in self.pools.items():
-                for pool in pools:
-                    if pool.busy:
+            for pool in self.all_pools:
+                if pool.busy:
+                    ta = pc()
+                    fin = pool.poll()
+                    host_ops.append((pc() - ta, "poll", pool.nref))
+                    if fin is None:
+                        continue
+                    progressed = True
+                    tnow = pc() - t0
+                    for k in fin:
+                        req = pool.active.pop(k)
                         ta = pc()
-                        fin = pool.poll()
-                        host_ops.append((pc() - ta, "poll", L))
-                        if fin is None:
-                            continue
-                        progressed = True
-                        tnow = pc() - t0
-                        for k in fin:
-                            req = pool.active.pop(k)
-                            ta = pc()
-                            x, lr = pool.fetch(k, keep_x)
-                            host_ops.append((pc() - ta, "fetch", L))
-                            req.done, req.iters, req.converged = tnow, lr.iters, bool(lr.converged)
-                            req.x = x
-                            pool.free.append(k)
-                            done_count += 1
-                # admissions between two iterations (pools already iterating
-                # first, so requests batch), then the next iterations
-                q = pending[L]
-                for pool in sorted(pools, key=lambda p: -len(p.active)):
-                    while q and pool.free and not pool.busy:
+                        x, lr = pool.fetch(k, keep_x)
+                        host_ops.append((pc() - ta, "fetch", pool.depths[k]))
+                        req.done, req.iters, req.converged = tnow, lr.iters, bool(lr.converged)
+                        req.x = x
+                        pool.free.append(k)
+                        done_count += 1
+            # admissions between two iterations (pools already iterating
+            # first, so requests batch), then the next iterations
+            for L, q in pending.items():
+                if not q:
+                    continue
+                for pool in sorted(self.pools[L], key=lambda p: -len(p.active)):
+                    while q and not pool.busy:
+                        k = pool.free_slot(L)
+                        if k is None:
+                            break
                         req = q.pop(0)
-                        k = pool.free.pop(0)
+                        pool.free.remove(k)
                         ta = pc()
                         req.start = ta - t0
                         pool.admit(k, req.seed, self.corr, self.var)
                         host_ops.append((pc() - ta, "admit", L))
                         pool.active[k] = req
                         progressed = True
-                for pool in pools:
-                    if pool.active and not pool.busy:
-                        ta = pc()
-                        pool.launch()
-                        host_ops.append((pc() - ta, "launch", L))
+            for pool in self.all_pools:
+                if pool.active and not pool.busy:
+                    ta = pc()
+                    pool.launch()
+                    host_ops.append((pc() - ta, "launch", pool.nref))
+            if self.grow_after_ms is not None:  # demand-driven growth by free device memory
+                for L, q in pending.items():
+                    if not q:
+                        waiting_since.pop(L, None)
+                        continue
+                    w0 = waiting_since.setdefault(L, now)
+                    if L not in growing and L not in self.mixed_depths and (now - w0) * 1e3 >= self.grow_after_ms \
+                            and self._may_grow(L):
+                        growing.add(L)
+                        threading.Thread(target=self._grow, args=(L, ready), daemon=True).start()
             if not progressed:
-                if nxt < len(order) and not any(p.busy for ps in self.pools.values() for p in ps):
+                if nxt < len(order) and not any(p.busy for p in self.all_pools):
                     wait = order[nxt].arrival - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(min(wait, 0.002))
@@ -325,12 +415,12 @@ class Server:
             ls = np.array([(r.done - r.arrival) * 1e3 for r in order if r.nref == L])
             if ls.size:
                 per[L] = {"count": int(ls.size), "p50_ms": float(np.percentile(ls, 50)),
-                          "p99_ms": float(np.percentile(ls, 99)), "pools_x_slots": list(self.layout[L])}
+                          "p99_ms": float(np.percentile(ls, 99)), "pools": len(self.pools[L]),
+                          "slots": self.slots[L]}
         return ServeStats(len(order), makespan, float(np.percentile(lat, 50)), float(np.percentile(lat, 99)),
                           float(lat.mean()), len(order) / makespan, float(np.mean([r.iters for r in order])),
                           all(r.converged for r in order), per, breakdown)
 
     def close(self):
-        for ps in self.pools.values():
-            for p in ps:
-                p.close()
+        for p in self.all_pools:
+            p.close()
