@@ -34,12 +34,21 @@ sys.path.insert(0, ROOT)
 METRIC = "solves/s to 1e-8 rel defect, mixed vs FP64 GPU; HBM GB/s; serve p50/p99 ms"
 NREF, SEED, CORR, VAR = 6, 2026, 0.1, 1.0
 RED = 1e-8
+# the tetrahedra of the refined cube: "ug" = UG's red rules (shortest interior
+# diagonal, UG's own mesh), "freudenthal" = the Freudenthal triangulation
+MESH = "ug"
+MESHES = {"ug": "UG red rules (shortest interior diagonal)", "freudenthal": "Freudenthal triangulation"}
+
+
+def gen_kind(G):
+    return G.Generator.DIFFUSION3D_UG if MESH == "ug" else G.Generator.DIFFUSION3D
 
 
 def workload_config(extra=None):
-    c = {"workload": "3D P1 diffusion k=exp(g) (corr 0.1, var 1), unit cube 6 Kuhn tets red x6, "
-                     "65^3=274625 unknowns, lmgc V(2,2) Gauss-Seidel, base level 0, ls to 1e-8 rel defect",
-         "unknowns": 274625, "nnz": 4018753, "levels": NREF + 1, "smoother": "gs",
+    c = {"workload": f"3D P1 diffusion k=exp(g) (corr 0.1, var 1), unit cube 6 Kuhn tets red x{NREF} "
+                     f"({MESHES[MESH]}), 65^3=274625 unknowns, lmgc V(2,2) Gauss-Seidel, base level 0, "
+                     "ls to 1e-8 rel defect",
+         "mesh": MESH, "unknowns": 274625, "nnz": 4018753, "levels": NREF + 1, "smoother": "gs",
          "l2": "GPU arm: L2 flushed between timed steps (256 MB read); the hierarchy itself (~60 MB FP64) "
                "fits in L2"}
     if extra:
@@ -167,7 +176,7 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    levels, rhs, _ = oracle.cube_levels(NREF, SEED, CORR, VAR)
+    levels, rhs, _ = oracle.cube_levels(NREF, SEED, CORR, VAR, ug_rules=MESH == "ug")
     H = oracle.Hierarchy(levels)
     threads = max(1, min(os.cpu_count() or 1, 16))
     results = [None] * threads
@@ -786,7 +795,7 @@ def run_ours(args):
             print(json.dumps({"only": args.only, args.only: out}), flush=True)
         return
 
-    gen = G.Generator(G.Generator.DIFFUSION3D, NREF, seed=SEED, corr=CORR, var=VAR)
+    gen = G.Generator(gen_kind(G), NREF, seed=SEED, corr=CORR, var=VAR)
     mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True, autotune=True, device=local)
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     mg.createvector("sol", "rhs", "rhs0")
@@ -942,6 +951,7 @@ def run_ours(args):
 
 
 def main():
+    global MESH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -960,7 +970,11 @@ def main():
                     help="run one workload alone and print its JSON (profiling runs); c2: the headline solve "
                          "without the other workloads; roofline: the C2 roofline kernels only, warmup + steps "
                          "repetitions each")
+    ap.add_argument("--mesh", default=MESH, choices=sorted(MESHES),
+                    help="tetrahedra of the headline workload (both arms): ug = UG's red rules, UG's own mesh; "
+                         "freudenthal = the Freudenthal triangulation (same nodes and edge counts)")
     args = ap.parse_args()
+    MESH = args.mesh
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -325,7 +325,12 @@ int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double 
  * with `mark $a; refine`, assembled as in the workloads:
  *   kind 0: 2D Q1 Poisson;   kind 1: 3D P1 diffusion, k = exp(g) per element
  *   (exponential covariance, correlation `corr`, variance `var`; var=0 gives k=1);
- *   kind 2: 2D P1 plane-strain elasticity (E=1, nu=0.3) on two triangles, 2x2 blocks.
+ *   kind 2: 2D P1 plane-strain elasticity (E=1, nu=0.3) on two triangles, 2x2 blocks;
+ *   kind 3: kind 1's problem on the cube refined by UG's red rules with the
+ *   shortest interior diagonal and UG's tie-break (gm/rm.cc:1567): UG's own
+ *   3D hierarchy, node for node (kind 1 refines along the diagonal that keeps
+ *   the Freudenthal triangulation: same nodes and edge counts, other edges);
+ *   nref <= 7.
  * Homogeneous Dirichlet boundary (unit rows, VECSKIP); the right-hand side is
  * uniform[-1,1] keyed by lattice position and `seed`, scaled by h^dim.
  * Node order per level: lexicographic.  The generator owns all arrays. */

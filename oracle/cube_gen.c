@@ -29,11 +29,26 @@
  * even layers first, then odd ones; in a layer y, x, then the six tetrahedra
  * of a cell), which fixes the rounding of every entry.
  *
- * Tetrahedra: the Freudenthal triangulation of the lattice (cell (i,j,k)
- * split into the six tetrahedra x_s1 >= x_s2 >= x_s3 of its local
+ * Tetrahedra, rule 0: the Freudenthal triangulation of the lattice (cell
+ * (i,j,k) split into the six tetrahedra x_s1 >= x_s2 >= x_s3 of its local
  * coordinates), which is what red refinement of the Kuhn tetrahedra gives
  * when every octahedron is cut along the diagonal that keeps that
- * triangulation. */
+ * triangulation.
+ *
+ * Rule 1: UG's own refinement.  The six coarse tetrahedra as the workload
+ * inserts them (cube corners (0,1,2,6), (0,2,3,6), (0,3,7,6), (0,7,4,6),
+ * (0,4,5,6), (0,5,1,6), cube corners numbered as UG's hexahedron domain
+ * numbers them), refined by UG's red rules: the rule of the shortest
+ * interior diagonal (ShortestInteriorEdge, gm/rm.cc:1567, its comparisons
+ * and tie cases), the sons and their corner orders from UG's rule table
+ * (TetrahedronRules, gm/rm.cc:494, rules 2-4: TET_RED_2_4, _0_5, _1_3,
+ * gm/rm.h:183-186), edges numbered as UG numbers a tetrahedron's edges
+ * (gm/elements.cc).  Every son lies in one lattice cell; rows list the
+ * neighbours in the 26-direction order of kOffs26 (the 14 of rule 0 first),
+ * elements are summed per z layer of cells (even layers, then odd), in a
+ * layer by cell (y, x) and then by the sorted node numbers of the
+ * element; a fine node off the coarse lattice interpolates from the ends of
+ * the one coarse edge through it. */
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -288,8 +303,266 @@ static int build_level(orc_cube *C, int l, const field *F, int nthreads) {
   return 0;
 }
 
+/* ---- rule 1: UG's red refinement ----------------------------------------- */
+static const int kEdge[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+/* sons of TET_RED_2_4, TET_RED_0_5, TET_RED_1_3: corners 0..3 of the father,
+ * 4 + e the midpoint of edge e */
+static const int kSons[3][8][4] = {
+    {{0, 4, 6, 7}, {4, 5, 8, 1}, {5, 6, 9, 2}, {7, 8, 9, 3}, {4, 6, 7, 8}, {4, 5, 6, 8}, {5, 6, 8, 9}, {6, 7, 8, 9}},
+    {{5, 6, 9, 2}, {4, 5, 8, 1}, {7, 8, 9, 3}, {0, 4, 6, 7}, {4, 5, 6, 9}, {5, 8, 9, 4}, {4, 7, 8, 9}, {4, 6, 7, 9}},
+    {{7, 8, 9, 3}, {4, 5, 8, 1}, {0, 4, 6, 7}, {5, 6, 9, 2}, {5, 7, 8, 9}, {4, 5, 7, 8}, {4, 5, 6, 7}, {5, 6, 7, 9}}};
+static int kOffs26[26][3];
+static void init_offs26(void) {
+  for (int q = 0; q < 14; ++q)
+    for (int d = 0; d < 3; ++d) kOffs26[q][d] = kOffs[q][d];
+  int q = 14;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        int nonneg = dx >= 0 && dy >= 0 && dz >= 0, nonpos = dx <= 0 && dy <= 0 && dz <= 0;
+        if (nonneg || nonpos) continue; /* the origin and the 14 above */
+        kOffs26[q][0] = dx; kOffs26[q][1] = dy; kOffs26[q][2] = dz; ++q;
+      }
+}
+static int dir26(int dx, int dy, int dz) {
+  for (int q = 0; q < 26; ++q)
+    if (kOffs26[q][0] == dx && kOffs26[q][1] == dy && kOffs26[q][2] == dz) return q;
+  return -1;
+}
+
+typedef struct { int c[4][3]; } tet;
+
+/* index into kSons of the rule UG takes for a tetrahedron whose corners
+ * and edge midpoints (in units of the son lattice) are P[0..9] */
+static int shortest_interior_edge(int P[10][3]) {
+  long long d[3] = {0, 0, 0}; /* squared lengths of the diagonals 0-5, 1-3, 2-4 */
+  static const int ends[3][2] = {{4, 9}, {5, 7}, {6, 8}};
+  for (int g = 0; g < 3; ++g)
+    for (int x = 0; x < 3; ++x) {
+      long long t = P[ends[g][0]][x] - P[ends[g][1]][x];
+      d[g] += t * t;
+    }
+  int flags = (d[0] < d[1]) | ((d[1] < d[2]) << 1) | ((d[2] < d[0]) << 2);
+  if (flags == 2 || flags == 6) return 2; /* TET_RED_1_3 */
+  if (flags == 4 || flags == 5) return 0; /* TET_RED_2_4 */
+  return 1;                               /* TET_RED_0_5 */
+}
+
+typedef struct { int z, y, x, ids[4]; int t; } elem_key;
+static int cmp_int(const void *a, const void *b) { return *(const int *)a - *(const int *)b; }
+static int cmp_key(const void *pa, const void *pb) {
+  const elem_key *a = (const elem_key *)pa, *b = (const elem_key *)pb;
+  if (a->z != b->z) return a->z < b->z ? -1 : 1;
+  if (a->y != b->y) return a->y < b->y ? -1 : 1;
+  if (a->x != b->x) return a->x < b->x ? -1 : 1;
+  for (int i = 0; i < 4; ++i)
+    if (a->ids[i] != b->ids[i]) return a->ids[i] < b->ids[i] ? -1 : 1;
+  return 0;
+}
+
+typedef struct { const field *F; double h; const tet *T; const elem_key *K; size_t e0, e1; double *kc; } ug_field_job;
+static void *ug_field_range(void *arg) {
+  ug_field_job *J = (ug_field_job *)arg;
+  for (size_t e = J->e0; e < J->e1; ++e) {
+    const tet *t = &J->T[J->K[e].t];
+    double xc[3] = {0, 0, 0};
+    for (int a = 0; a < 4; ++a)
+      for (int d = 0; d < 3; ++d) xc[d] += (t->c[a][d] * J->h) / 4;
+    J->kc[e] = field_k(J->F, xc);
+  }
+  return NULL;
+}
+
+/* level l of rule 1 from its tetrahedra; nb[] receives the 26-bit
+ * neighbour masks, cnb[] holds level l-1's */
+static int build_level_ug(orc_cube *C, int l, const tet *T, size_t nt_el, const uint32_t *cnb, uint32_t *nb,
+                          const field *F, int nthreads) {
+  level *L = &C->lev[l];
+  const int N = (1 << l) + 1, n = N * N * N, nc = N - 1;
+  const double h = 1.0 / (N - 1);
+  L->N = N;
+  L->n = n;
+  memset(nb, 0, sizeof(uint32_t) * (size_t)n);
+  for (size_t e = 0; e < nt_el; ++e)
+    for (int g = 0; g < 6; ++g) {
+      const int *a = T[e].c[kEdge[g][0]], *b = T[e].c[kEdge[g][1]];
+      int fwd = dir26(b[0] - a[0], b[1] - a[1], b[2] - a[2]), bwd = dir26(a[0] - b[0], a[1] - b[1], a[2] - b[2]);
+      if (fwd < 0 || bwd < 0) return 1; /* an edge longer than one lattice step */
+      nb[(a[2] * N + a[1]) * N + a[0]] |= 1u << fwd;
+      nb[(b[2] * N + b[1]) * N + b[0]] |= 1u << bwd;
+    }
+  size_t nnz = 0;
+  for (int r = 0; r < n; ++r) nnz += 1 + (size_t)__builtin_popcount(nb[r]);
+  L->rowptr = (int *)malloc(sizeof(int) * (n + 1));
+  L->col = (int *)malloc(sizeof(int) * nnz);
+  L->xyz = (double *)malloc(sizeof(double) * (size_t)n * 3);
+  int *pos = (int *)malloc(sizeof(int) * (size_t)n * 26);
+  if (!L->rowptr || !L->col || !L->xyz || !pos) { free(pos); return 1; }
+  int q = 0;
+  L->rowptr[0] = 0;
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        int r = (k * N + j) * N + i;
+        L->xyz[(size_t)r * 3] = i * h; L->xyz[(size_t)r * 3 + 1] = j * h; L->xyz[(size_t)r * 3 + 2] = k * h;
+        L->col[q++] = r;
+        for (int o = 0; o < 26; ++o) {
+          pos[(size_t)r * 26 + o] = -1;
+          if (!(nb[r] >> o & 1u)) continue;
+          pos[(size_t)r * 26 + o] = q;
+          L->col[q++] = ((k + kOffs26[o][2]) * N + j + kOffs26[o][1]) * N + i + kOffs26[o][0];
+        }
+        L->rowptr[r + 1] = q;
+      }
+  /* elements in summation order */
+  elem_key *K = (elem_key *)malloc(sizeof(elem_key) * (nt_el ? nt_el : 1));
+  double *kc = (double *)malloc(sizeof(double) * (nt_el ? nt_el : 1));
+  L->val = (double *)calloc((size_t)q, sizeof(double));
+  if (!K || !kc || !L->val) { free(K); free(kc); free(pos); return 1; }
+  for (size_t e = 0; e < nt_el; ++e) {
+    elem_key *k = &K[e];
+    k->x = k->y = k->z = 1 << 30;
+    for (int a = 0; a < 4; ++a) {
+      const int *v = T[e].c[a];
+      if (v[0] < k->x) k->x = v[0];
+      if (v[1] < k->y) k->y = v[1];
+      if (v[2] < k->z) k->z = v[2];
+      k->ids[a] = (v[2] * N + v[1]) * N + v[0];
+    }
+    qsort(k->ids, 4, sizeof(int), cmp_int);
+    k->t = (int)e;
+  }
+  qsort(K, nt_el, sizeof(elem_key), cmp_key);
+  int nt = nthreads < 1 ? 1 : nthreads > 64 ? 64 : nthreads;
+  pthread_t th[64];
+  ug_field_job jobs[64];
+  for (int w = 0; w < nt; ++w) {
+    jobs[w].F = F; jobs[w].h = h; jobs[w].T = T; jobs[w].K = K; jobs[w].kc = kc;
+    jobs[w].e0 = nt_el * w / nt; jobs[w].e1 = nt_el * (w + 1) / nt;
+  }
+  for (int w = 1; w < nt; ++w) pthread_create(&th[w], NULL, ug_field_range, &jobs[w]);
+  ug_field_range(&jobs[0]);
+  for (int w = 1; w < nt; ++w) pthread_join(th[w], NULL);
+  for (int parity = 0; parity < 2; ++parity)
+    for (size_t e = 0; e < nt_el; ++e) {
+      if ((K[e].z & 1) != parity) continue;
+      const tet *t = &T[K[e].t];
+      double X[4][3], Ke[16];
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) X[a][d] = t->c[a][d] * h;
+      p1_stiffness(X, kc[e], Ke);
+      for (int a = 0; a < 4; ++a) {
+        const int *va = t->c[a];
+        int r = (va[2] * N + va[1]) * N + va[0];
+        for (int b = 0; b < 4; ++b) {
+          const int *vb = t->c[b];
+          int ent = a == b ? L->rowptr[r] : pos[(size_t)r * 26 + dir26(vb[0] - va[0], vb[1] - va[1], vb[2] - va[2])];
+          L->val[ent] += Ke[a * 4 + b];
+        }
+      }
+    }
+  free(K);
+  free(kc);
+  free(pos);
+  L->vclass = (int *)malloc(sizeof(int) * n);
+  L->vnclass = (int *)malloc(sizeof(int) * n);
+  L->skip = (int *)calloc(n, sizeof(int));
+  if (!L->vclass || !L->vnclass || !L->skip) return 1;
+  for (int r = 0; r < n; ++r) { L->vclass[r] = 3; L->vnclass[r] = l < C->nref ? 3 : 0; }
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        if (!(i == 0 || j == 0 || k == 0 || i == N - 1 || j == N - 1 || k == N - 1)) continue;
+        int r = (k * N + j) * N + i;
+        L->skip[r] = 1;
+        for (int e = L->rowptr[r]; e < L->rowptr[r + 1]; ++e) L->val[e] = e == L->rowptr[r] ? 1.0 : 0.0;
+      }
+  L->prow = L->pcol = NULL;
+  L->pw = NULL;
+  if (l == 0) return 0;
+  const int Nc = (1 << (l - 1)) + 1;
+  L->prow = (int *)malloc(sizeof(int) * (n + 1));
+  L->pcol = (int *)malloc(sizeof(int) * (size_t)n * 2);
+  L->pw = (double *)malloc(sizeof(double) * (size_t)n * 2);
+  if (!L->prow || !L->pcol || !L->pw) return 1;
+  int m = 0;
+  L->prow[0] = 0;
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        int r = (k * N + j) * N + i, p[3] = {i, j, k};
+        if (!(i & 1) && !(j & 1) && !(k & 1)) {
+          L->pcol[m] = ((k / 2) * Nc + j / 2) * Nc + i / 2; L->pw[m++] = 1.0;
+          L->prow[r + 1] = m;
+          continue;
+        }
+        /* the coarse edges through p: for each odd axis, the end a steps
+         * down (sign bit 0) or up (bit 1) and the end b the other way */
+        int found = 0;
+        for (int sg = 0; sg < 8 && !found; ++sg) {
+          int a[3], b[3], ok = 1;
+          for (int d = 0; d < 3; ++d) {
+            if (!(p[d] & 1)) { if (sg >> d & 1) ok = 0; a[d] = b[d] = p[d] / 2; continue; }
+            int s = (sg >> d & 1) ? -1 : 1;
+            a[d] = (p[d] - s) / 2;
+            b[d] = (p[d] + s) / 2;
+          }
+          if (!ok) continue;
+          int o = dir26(b[0] - a[0], b[1] - a[1], b[2] - a[2]);
+          if (o < 0 || !(cnb[(a[2] * Nc + a[1]) * Nc + a[0]] >> o & 1u)) continue;
+          L->pcol[m] = (a[2] * Nc + a[1]) * Nc + a[0]; L->pw[m++] = 0.5;
+          L->pcol[m] = (b[2] * Nc + b[1]) * Nc + b[0]; L->pw[m++] = 0.5;
+          found = 1;
+        }
+        if (!found) return 1;
+        L->prow[r + 1] = m;
+      }
+  return 0;
+}
+
+static int build_ug(orc_cube *C, const field *F, int nthreads) {
+  static const int cube[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  static const int coarse[6][4] = {{0, 1, 2, 6}, {0, 2, 3, 6}, {0, 3, 7, 6}, {0, 7, 4, 6}, {0, 4, 5, 6}, {0, 5, 1, 6}};
+  init_offs26();
+  size_t ne = 6, nmax = (size_t)6 << (3 * C->nref);
+  const size_t nn = (size_t)((1 << C->nref) + 1) * ((1 << C->nref) + 1) * ((1 << C->nref) + 1);
+  tet *T = (tet *)malloc(sizeof(tet) * nmax), *S = (tet *)malloc(sizeof(tet) * nmax);
+  uint32_t *nb = (uint32_t *)malloc(sizeof(uint32_t) * nn), *cnb = (uint32_t *)malloc(sizeof(uint32_t) * nn);
+  int rc = !T || !S || !nb || !cnb;
+  if (!rc) {
+    for (int e = 0; e < 6; ++e)
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) T[e].c[a][d] = cube[coarse[e][a]][d];
+    rc = build_level_ug(C, 0, T, ne, NULL, nb, F, nthreads);
+  }
+  for (int l = 1; l <= C->nref && !rc; ++l) {
+    for (size_t e = 0; e < ne; ++e) {
+      int P[10][3];
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) P[a][d] = 2 * T[e].c[a][d];
+      for (int g = 0; g < 6; ++g)
+        for (int d = 0; d < 3; ++d) P[4 + g][d] = T[e].c[kEdge[g][0]][d] + T[e].c[kEdge[g][1]][d];
+      const int r = shortest_interior_edge(P);
+      for (int s = 0; s < 8; ++s)
+        for (int a = 0; a < 4; ++a)
+          for (int d = 0; d < 3; ++d) S[e * 8 + s].c[a][d] = P[kSons[r][s][a]][d];
+    }
+    ne *= 8;
+    tet *x = T; T = S; S = x;
+    uint32_t *y = cnb; cnb = nb; nb = y;
+    rc = build_level_ug(C, l, T, ne, cnb, nb, F, nthreads);
+  }
+  free(T); free(S); free(nb); free(cnb);
+  return rc;
+}
+
 int orc_cube_create(int nref, unsigned long long seed, double corr, double var, int nthreads, orc_cube **out) {
-  if (!out || nref < 0 || nref > 8) return 1;
+  return orc_cube_create_rule(0, nref, seed, corr, var, nthreads, out);
+}
+
+int orc_cube_create_rule(int rule, int nref, unsigned long long seed, double corr, double var, int nthreads,
+                         orc_cube **out) {
+  if (!out || rule < 0 || rule > 1 || nref < 0 || nref > (rule ? 7 : 8)) return 1;
   init_offs();
   orc_cube *C = (orc_cube *)calloc(1, sizeof *C);
   if (!C) return 1;
@@ -298,8 +571,12 @@ int orc_cube_create(int nref, unsigned long long seed, double corr, double var, 
   field *F = (field *)malloc(sizeof(field));
   if (!C->lev || !F) { free(F); orc_cube_destroy(C); return 1; }
   field_init(F, seed, corr, var);
-  for (int l = 0; l <= nref; ++l)
-    if (build_level(C, l, F, nthreads)) { free(F); orc_cube_destroy(C); return 1; }
+  if (rule == 1) {
+    if (build_ug(C, F, nthreads)) { free(F); orc_cube_destroy(C); return 1; }
+  } else {
+    for (int l = 0; l <= nref; ++l)
+      if (build_level(C, l, F, nthreads)) { free(F); orc_cube_destroy(C); return 1; }
+  }
   free(F);
   const level *T = &C->lev[nref];
   const double scale = (double)(1 << nref), hd = pow(1.0 / scale, 3);

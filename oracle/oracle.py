@@ -103,6 +103,9 @@ def lib():
         L.orc_bcgs_solve_levels.argtypes = [P, P, P, P, P, C.c_int, P, P]
         L.orc_cube_create.argtypes = [C.c_int, C.c_ulonglong, C.c_double, C.c_double, C.c_int, C.POINTER(P)]
         L.orc_cube_create.restype = C.c_int
+        L.orc_cube_create_rule.argtypes = [C.c_int, C.c_int, C.c_ulonglong, C.c_double, C.c_double, C.c_int,
+                                           C.POINTER(P)]
+        L.orc_cube_create_rule.restype = C.c_int
         L.orc_cube_level.argtypes = [P, C.c_int, C.POINTER(_Level), C.POINTER(C.POINTER(C.c_double))]
         L.orc_cube_level.restype = C.c_int
         L.orc_cube_rhs.argtypes = [P, C.POINTER(C.c_int)]
@@ -123,16 +126,19 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
-def cube_levels(nref: int, seed: int, corr: float = 0.1, var: float = 1.0, threads: int | None = None):
+def cube_levels(nref: int, seed: int, corr: float = 0.1, var: float = 1.0, threads: int | None = None,
+                ug_rules: bool = False):
     """The 3D P1 diffusion workload's hierarchy from the oracle's own
-    generator (cube_gen.c): unit cube, six Kuhn tetrahedra refined nref times,
-    k = exp(g) per element, seeded right-hand side.  Returns (levels, rhs,
-    xyz): level dicts as Hierarchy takes them, the finest level's right-hand
-    side and every level's node coordinates (n x 3)."""
+    generator (cube_gen.c): unit cube, six Kuhn tetrahedra refined nref times
+    (ug_rules: by UG's red rules with the shortest interior diagonal, UG's
+    own mesh; else the Freudenthal triangulation), k = exp(g) per element,
+    seeded right-hand side.  Returns (levels, rhs, xyz): level dicts as
+    Hierarchy takes them, the finest level's right-hand side and every
+    level's node coordinates (n x 3)."""
     L = lib()
     h = C.c_void_p()
     nt = threads if threads else max(1, min(16, os.cpu_count() or 1))
-    rc = L.orc_cube_create(nref, seed, corr, var, nt, C.byref(h))
+    rc = L.orc_cube_create_rule(int(bool(ug_rules)), nref, seed, corr, var, nt, C.byref(h))
     if rc:
         raise RuntimeError(f"orc_cube_create failed ({rc})")
     try:

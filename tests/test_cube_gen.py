@@ -15,11 +15,13 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+@pytest.mark.parametrize("ug_rules", [False, True], ids=["freudenthal", "ug_red_rules"])
 @pytest.mark.parametrize("nref,var,seed", [(2, 1.0, 7), (3, 1.0, 2026), (3, 0.0, 12), (4, 0.5, 5)])
-def test_oracle_generator_equals_product_generator(oracle_mod, nref, var, seed):
+def test_oracle_generator_equals_product_generator(oracle_mod, nref, var, seed, ug_rules):
     import ug_gb300 as G
-    levels, rhs, xyz = oracle_mod.cube_levels(nref, seed, 0.1, var, threads=3)
-    gen = G.Generator(G.Generator.DIFFUSION3D, nref, seed=seed, corr=0.1, var=var)
+    levels, rhs, xyz = oracle_mod.cube_levels(nref, seed, 0.1, var, threads=3, ug_rules=ug_rules)
+    kind = G.Generator.DIFFUSION3D_UG if ug_rules else G.Generator.DIFFUSION3D
+    gen = G.Generator(kind, nref, seed=seed, corr=0.1, var=var)
     assert gen.nlevels == len(levels) == nref + 1
     for l in range(nref + 1):
         g, o = gen.level(l), levels[l]

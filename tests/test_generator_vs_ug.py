@@ -5,13 +5,14 @@ side agree with the UG-exported golden fixtures once vectors are matched by
 their coordinates (UG numbers them in refinement order, the generator
 lexicographically).  Runs on the CPU: the generator needs no GPU.
 
-In 3D the match is exact on the coarse grid (six Kuhn tetrahedra) and in the
-level sizes (unknowns, nonzeros) of every level: UG's red rule for
-tetrahedra picks the octahedron's shortest interior diagonal and breaks the
-tie between the two equally short ones of a Kuhn tetrahedron by its local
-edge numbering (ShortestInteriorEdge, gm/rm.cc:1567), while the generator
-always takes the one that keeps the Freudenthal triangulation.  Both are red
-refinements with the same vertices and the same number of edges."""
+In 3D, kind 3 is UG's own hierarchy and matches on every level: UG's red
+rule for tetrahedra picks the octahedron's shortest interior diagonal and
+breaks the tie between the two equally short ones of a Kuhn tetrahedron by
+its local edge numbering (ShortestInteriorEdge, gm/rm.cc:1567), which kind 3
+follows through the sons' corner orders of UG's rule table.  Kind 1 always
+takes the diagonal that keeps the Freudenthal triangulation: it matches on
+the coarse grid and in the level sizes (unknowns, nonzeros) of every level
+(both are red refinements with the same vertices and edge counts)."""
 import numpy as np
 import pytest
 
@@ -21,6 +22,8 @@ CASES = [  # fixture, generator kind, nref, seed, corr, var
     ("q1_jac", 0, 5, 11, 0.1, 0.0),
     ("p1_gs", 1, 3, 12, 0.1, 0.0),
     ("p1k_jac", 1, 3, 13, 0.1, 1.0),
+    ("p1_gs", 3, 3, 12, 0.1, 0.0),
+    ("p1k_jac", 3, 3, 13, 0.1, 1.0),
     ("el_jac", 2, 4, 14, 0.1, 0.0),
 ]
 
@@ -29,11 +32,36 @@ def _keys(xyz, scale):
     return [tuple(int(round(c * scale)) for c in p) for p in np.asarray(xyz).reshape(-1, 3)]
 
 
+class _OracleCube:
+    """The oracle's generator (oracle/cube_gen.c) behind the Generator
+    interface the checks below read."""
+
+    def __init__(self, oracle_mod, nref, seed, corr, var):
+        self._lv, self.rhs, xyz = oracle_mod.cube_levels(nref, seed, corr, var, threads=2, ug_rules=True)
+        for d, x in zip(self._lv, xyz):
+            d["xyz"] = x
+        self.nlevels = len(self._lv)
+
+    def level(self, l):
+        return self._lv[l]
+
+
 @pytest.mark.parametrize("name,kind,nref,seed,corr,var", CASES)
 def test_generator_matches_ug(name, kind, nref, seed, corr, var):
     import ug_gb300 as G
+    _check_against_ug(name, G.Generator(kind, nref, seed=seed, corr=corr, var=var), kind, nref)
+
+
+@pytest.mark.parametrize("name,nref,seed,corr,var", [c[:1] + c[2:] for c in CASES if c[1] == 3])
+def test_oracle_ug_rules_match_ug(oracle_mod, name, nref, seed, corr, var):
+    """The oracle's restatement of UG's red refinement, pinned on its own
+    against UG's exported 3D hierarchies (every level, pattern, values,
+    transfer, right-hand side)."""
+    _check_against_ug(name, _OracleCube(oracle_mod, nref, seed, corr, var), 3, nref)
+
+
+def _check_against_ug(name, gen, kind, nref):
     fx = load_golden(name)
-    gen = G.Generator(kind, nref, seed=seed, corr=corr, var=var)
     assert gen.nlevels == int(fx["nlevels"][0])
     s = int(fx["blocksize"][0])
     scale = 1 << nref

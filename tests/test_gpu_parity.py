@@ -197,15 +197,17 @@ def test_full_size_p1_diffusion_gs(G, oracle_mod):
     mg.close()
 
 
-def test_full_size_p1_diffusion_mixed(G, oracle_mod):
+@pytest.mark.parametrize("kind", [1, 3], ids=["freudenthal", "ug_red_rules"])
+def test_full_size_p1_diffusion_mixed(G, oracle_mod, kind):
     """The benchmarked solve itself: 3D P1 diffusion 65^3 (274,625 unknowns,
     k = exp(g), seed 2026), multicolour GS V(2,2), the FP32 V-cycle inside FP64
-    iterative refinement to 1e-8, autotuned kernels, as bench.py runs it.
+    iterative refinement to 1e-8, autotuned kernels, as bench.py runs it, on
+    both tetrahedral meshes of the cube (UG's red rules, Freudenthal).
     Checked in FP64 by the oracle on the same (reordered) hierarchy: the
     solution meets the stopping test (FP64 defect <= 1e-8 of the first), takes
     the FP64 solve's iteration count +-1, and is within 1e-6 (relative,
     max-norm) of the FP64 solution converged to 1e-12."""
-    gen = G.Generator(1, 6, seed=2026, corr=0.1, var=1.0)
+    gen = G.Generator(kind, 6, seed=2026, corr=0.1, var=1.0)
     levels = gen.levels()
     mg = G.MultiGrid(levels, order=G.ORDER_COLOR, fp32=True, autotune=True)
     G.setup_lmgc(mg, "gs", baselevel=0, red=1e-8, abslimit=1e-50)
@@ -230,6 +232,7 @@ def test_full_size_p1_diffusion_mixed(G, oracle_mod):
 MID = [  # generator kind, nref, smoother, baselevel, var
     (0, 6, "jac", 2, 0.0), (0, 6, "gs", 2, 0.0), (0, 6, "ilu", 2, 0.0),
     (1, 4, "gs", 0, 1.0), (1, 4, "ilu", 0, 1.0), (1, 4, "jac", 0, 1.0),
+    (3, 4, "gs", 0, 1.0), (3, 4, "ilu", 0, 1.0), (3, 5, "gs", 0, 1.0),
     (2, 6, "gs", 1, 0.0), (2, 6, "ilu", 1, 0.0), (2, 6, "jac", 1, 0.0),
 ]
 

@@ -159,9 +159,12 @@ class Generator:
     kind 0: 2D Q1 Poisson on the unit square (one quad refined nref times);
     kind 1: 3D P1 diffusion on the unit cube (six Kuhn tets refined nref
     times), k = exp(g) with correlation ``corr`` and variance ``var``;
-    kind 2: 2D P1 plane-strain elasticity, 2x2 blocks."""
+    kind 2: 2D P1 plane-strain elasticity, 2x2 blocks;
+    kind 3: kind 1's problem on the tetrahedra UG's red rules produce (the
+    octahedron cut along its shortest interior diagonal, UG's tie-break;
+    kind 1 keeps the Freudenthal triangulation instead)."""
 
-    POISSON2D, DIFFUSION3D, ELASTICITY2D = 0, 1, 2
+    POISSON2D, DIFFUSION3D, ELASTICITY2D, DIFFUSION3D_UG = 0, 1, 2, 3
 
     def __init__(self, kind: int, nref: int, seed: int = 1, corr: float = 0.1, var: float = 0.0):
         L = lib()

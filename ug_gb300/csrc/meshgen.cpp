@@ -293,10 +293,257 @@ static int build_level(gmg_gen *G, int l, const ugfx::LogNormalField &field) {
   return 0;
 }
 
+// ------------------------------------------------------------ kind 3: UG's red refinement
+// The six Kuhn tetrahedra of the unit cube, in the corner order the workload
+// inserts them (corner ids of the cube 0..7 as the Hexahedron domain numbers
+// them; every one positively oriented, so UG keeps the order), refined by
+// UG's red rules: each tetrahedron splits into its four corner tetrahedra and
+// the four of its octahedron cut along the shortest interior diagonal,
+// ties broken as UG breaks them; sons carry their corners in the order of
+// UG's rule table, which fixes the next refinement's edge numbering.
+namespace {
+
+// edges of a tetrahedron and the sons of the red rules that cut the
+// octahedron along the diagonal between the midpoints of edges (2, 4),
+// (0, 5) and (1, 3); son corners 0..3 = the father's corners, 4 + e = the
+// midpoint of edge e
+const int kTetEdge[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+const int kRedSons[3][8][4] = {
+    {{0, 4, 6, 7}, {4, 5, 8, 1}, {5, 6, 9, 2}, {7, 8, 9, 3}, {4, 6, 7, 8}, {4, 5, 6, 8}, {5, 6, 8, 9}, {6, 7, 8, 9}},
+    {{5, 6, 9, 2}, {4, 5, 8, 1}, {7, 8, 9, 3}, {0, 4, 6, 7}, {4, 5, 6, 9}, {5, 8, 9, 4}, {4, 7, 8, 9}, {4, 6, 7, 9}},
+    {{7, 8, 9, 3}, {4, 5, 8, 1}, {0, 4, 6, 7}, {5, 6, 9, 2}, {5, 7, 8, 9}, {4, 5, 7, 8}, {4, 5, 6, 7}, {5, 6, 7, 9}}};
+const int kCube[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+const int kCoarse[6][4] = {{0, 1, 2, 6}, {0, 2, 3, 6}, {0, 3, 7, 6}, {0, 7, 4, 6}, {0, 4, 5, 6}, {0, 5, 1, 6}};
+
+struct Tet {
+  int v[4][3];  // lattice coordinates of the corners, UG's corner order
+};
+
+// the rule of the shortest interior diagonal (gm/rm.cc:1567): index into
+// kRedSons; lengths compared exactly on the lattice
+int red_rule(const int P[10][3]) {
+  auto d2 = [&](int a, int b) {
+    long long t = 0;
+    for (int d = 0; d < 3; ++d) t += (long long)(P[a][d] - P[b][d]) * (P[a][d] - P[b][d]);
+    return t;
+  };
+  const long long d05 = d2(4, 9), d13 = d2(5, 7), d24 = d2(6, 8);
+  const int flags = int(d05 < d13) | (int(d13 < d24) << 1) | (int(d24 < d05) << 2);
+  switch (flags) {
+    case 2: case 6: return 2;  // 1_3
+    case 4: case 5: return 0;  // 2_4
+    default: return 1;         // 0_5 (flags 0, 1, 3)
+  }
+}
+
+std::vector<Tet> refine_red(const std::vector<Tet> &in) {
+  std::vector<Tet> out(in.size() * 8);
+  for (size_t t = 0; t < in.size(); ++t) {
+    int P[10][3];
+    for (int c = 0; c < 4; ++c)
+      for (int d = 0; d < 3; ++d) P[c][d] = 2 * in[t].v[c][d];
+    for (int e = 0; e < 6; ++e)
+      for (int d = 0; d < 3; ++d) P[4 + e][d] = in[t].v[kTetEdge[e][0]][d] + in[t].v[kTetEdge[e][1]][d];
+    const int r = red_rule(P);
+    for (int q = 0; q < 8; ++q)
+      for (int c = 0; c < 4; ++c)
+        for (int d = 0; d < 3; ++d) out[t * 8 + q].v[c][d] = P[kRedSons[r][q][c]][d];
+  }
+  return out;
+}
+
+// the 26 lattice directions: the 14 of the Freudenthal stencil first (for
+// m = 1..7 with bits x, y, z: +m, -m), then the other 12
+std::vector<std::array<int, 3>> offsets26() {
+  std::vector<std::array<int, 3>> o;
+  for (int m = 1; m < 8; ++m) {
+    const int a = m & 1, b = (m >> 1) & 1, c = (m >> 2) & 1;
+    o.push_back({a, b, c});
+    o.push_back({-a, -b, -c});
+  }
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dx && !dy && !dz) continue;
+        const bool same = (dx >= 0 && dy >= 0 && dz >= 0) || (dx <= 0 && dy <= 0 && dz <= 0);
+        if (!same) o.push_back({dx, dy, dz});
+      }
+  return o;
+}
+int off_index(const std::vector<std::array<int, 3>> &o, int dx, int dy, int dz) {
+  for (int q = 0; q < int(o.size()); ++q)
+    if (o[q][0] == dx && o[q][1] == dy && o[q][2] == dz) return q;
+  return -1;
+}
+
+// one level of the UG-refined cube from its tetrahedra; `coarse_mask` (the
+// level below's neighbour masks, null on level 0) gives the transfer
+int build_ug_level(gmg_gen *G, int l, std::vector<Tet> &tets, const std::vector<uint32_t> *coarse_mask,
+                   std::vector<uint32_t> &mask, const ugfx::LogNormalField &field) {
+  static const std::vector<std::array<int, 3>> O = offsets26();
+  GenLevel &L = G->lev[l];
+  const int N = (1 << l) + 1, n = N * N * N, nc = N - 1;
+  L.N = N; L.s = 1; L.n = n;
+  const double h = 1.0 / nc;
+  auto id = [&](const int *v) { return (v[2] * N + v[1]) * N + v[0]; };
+  // the neighbours of every node: the edges of the tetrahedra
+  mask.assign(n, 0u);
+  for (const Tet &t : tets)
+    for (auto &e : kTetEdge) {
+      const int *a = t.v[e[0]], *b = t.v[e[1]];
+      mask[id(a)] |= 1u << off_index(O, b[0] - a[0], b[1] - a[1], b[2] - a[2]);
+      mask[id(b)] |= 1u << off_index(O, a[0] - b[0], a[1] - b[1], a[2] - b[2]);
+    }
+  // rows: the diagonal, then the neighbours in the order of O
+  std::vector<int> slot(size_t(n) * 26, -1);
+  L.rowptr.assign(n + 1, 0);
+  L.col.clear();
+  L.xyz.assign(size_t(n) * 3, 0.0);
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        const int r = (k * N + j) * N + i;
+        L.xyz[size_t(r) * 3] = i * h; L.xyz[size_t(r) * 3 + 1] = j * h; L.xyz[size_t(r) * 3 + 2] = k * h;
+        L.col.push_back(r);
+        for (int o = 0; o < 26; ++o) {
+          if (!(mask[r] & (1u << o))) continue;
+          slot[size_t(r) * 26 + o] = int(L.col.size());
+          L.col.push_back(((k + O[o][2]) * N + (j + O[o][1])) * N + (i + O[o][0]));
+        }
+        L.rowptr[r + 1] = int(L.col.size());
+      }
+  L.val.assign(L.col.size(), 0.0);
+  // every tetrahedron lies in one lattice cell (its corners differ by at most
+  // one step): sorted by cell (z, y, x), then by its sorted corner ids, the
+  // contributions to every entry are summed in one fixed order -- z layers of
+  // cells with even index first, then odd ones (no two layers of one parity
+  // share a node, so they are assembled in parallel)
+  struct Key { int z, y, x; std::array<int, 4> ids; size_t t; };
+  std::vector<Key> keys(tets.size());
+  for (size_t t = 0; t < tets.size(); ++t) {
+    Key &kk = keys[t];
+    kk.x = std::min({tets[t].v[0][0], tets[t].v[1][0], tets[t].v[2][0], tets[t].v[3][0]});
+    kk.y = std::min({tets[t].v[0][1], tets[t].v[1][1], tets[t].v[2][1], tets[t].v[3][1]});
+    kk.z = std::min({tets[t].v[0][2], tets[t].v[1][2], tets[t].v[2][2], tets[t].v[3][2]});
+    for (int c = 0; c < 4; ++c) kk.ids[c] = id(tets[t].v[c]);
+    std::sort(kk.ids.begin(), kk.ids.end());
+    kk.t = t;
+  }
+  std::sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) {
+    if (a.z != b.z) return a.z < b.z;
+    if (a.y != b.y) return a.y < b.y;
+    if (a.x != b.x) return a.x < b.x;
+    return a.ids < b.ids;
+  });
+  std::vector<size_t> zbeg(nc + 1, 0);
+  for (const Key &kk : keys) zbeg[kk.z + 1]++;
+  for (int z = 0; z < nc; ++z) zbeg[z + 1] += zbeg[z];
+  auto do_slab = [&](int z) {
+    double K[16];
+    for (size_t q = zbeg[z]; q < zbeg[z + 1]; ++q) {
+      const Tet &T = tets[keys[q].t];
+      double X[4][3], xc[3] = {0, 0, 0};
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) { X[a][d] = T.v[a][d] * h; xc[d] += X[a][d] / 4; }
+      p1_stiffness(3, X, field.k(xc), K);
+      for (int a = 0; a < 4; ++a) {
+        const int r = id(T.v[a]);
+        for (int b = 0; b < 4; ++b) {
+          const int e = a == b ? L.rowptr[r]
+                               : slot[size_t(r) * 26 + off_index(O, T.v[b][0] - T.v[a][0], T.v[b][1] - T.v[a][1],
+                                                                  T.v[b][2] - T.v[a][2])];
+          L.val[e] += K[a * 4 + b];
+        }
+      }
+    }
+  };
+  const int nt = std::max(1, std::min(nthreads(), nc));
+  for (int parity = 0; parity < 2; ++parity) {
+    std::vector<std::thread> th;
+    for (int w = 0; w < nt; ++w)
+      th.emplace_back([&, w]() {
+        for (int z = parity + 2 * w; z < nc; z += 2 * nt) do_slab(z);
+      });
+    for (auto &x : th) x.join();
+  }
+  // classes, Dirichlet rows
+  L.vclass.assign(n, 3);
+  L.vnclass.assign(n, l < G->nref ? 3 : 0);
+  L.skip.assign(n, 0);
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        if (!(i == 0 || j == 0 || k == 0 || i == N - 1 || j == N - 1 || k == N - 1)) continue;
+        const int r = (k * N + j) * N + i;
+        L.skip[r] = 1;
+        for (int q = L.rowptr[r]; q < L.rowptr[r + 1]; ++q) L.val[q] = q == L.rowptr[r] ? 1.0 : 0.0;
+      }
+  // standard transfer: a corner copies its father; any other node is the
+  // midpoint of the one coarse edge among the segments through it
+  if (coarse_mask) {
+    const int Nc = (1 << (l - 1)) + 1;
+    L.prow.assign(n + 1, 0);
+    L.pcol.clear();
+    L.pw.clear();
+    for (int k = 0; k < N; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          const int r = (k * N + j) * N + i, odd[3] = {i & 1, j & 1, k & 1}, c[3] = {i / 2, j / 2, k / 2};
+          if (!odd[0] && !odd[1] && !odd[2]) {
+            L.pcol.push_back((c[2] * Nc + c[1]) * Nc + c[0]);
+            L.pw.push_back(1.0);
+          } else {
+            int found = 0;
+            for (int sg = 0; sg < 8 && !found; ++sg) {  // the low end of the segment: (p - e) / 2 per odd axis
+              int lo[3], hi[3];
+              bool ok = true;
+              for (int d = 0; d < 3; ++d) {
+                const int pd = d == 0 ? i : d == 1 ? j : k;
+                if (!odd[d]) { lo[d] = hi[d] = pd / 2; if ((sg >> d) & 1) ok = false; continue; }
+                const int sgn = ((sg >> d) & 1) ? -1 : 1;
+                lo[d] = (pd - sgn) / 2;
+                hi[d] = (pd + sgn) / 2;
+              }
+              if (!ok) continue;
+              const int a = (lo[2] * Nc + lo[1]) * Nc + lo[0];
+              const int q = off_index(O, hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]);
+              if (q >= 0 && ((*coarse_mask)[a] & (1u << q))) {
+                L.pcol.push_back(a); L.pw.push_back(0.5);
+                L.pcol.push_back((hi[2] * Nc + hi[1]) * Nc + hi[0]); L.pw.push_back(0.5);
+                found = 1;
+              }
+            }
+            if (!found) {
+              gmg::set_error("UG cube level %d: node (%d,%d,%d) is on no coarse edge", l, i, j, k);
+              return 1;
+            }
+          }
+          L.prow[r + 1] = int(L.pcol.size());
+        }
+  }
+  return 0;
+}
+
+int build_ug_cube(gmg_gen *G, const ugfx::LogNormalField &field) {
+  std::vector<Tet> tets(6);
+  for (int t = 0; t < 6; ++t)
+    for (int c = 0; c < 4; ++c)
+      for (int d = 0; d < 3; ++d) tets[t].v[c][d] = kCube[kCoarse[t][c]][d];
+  std::vector<uint32_t> mask, prev;
+  for (int l = 0; l <= G->nref; ++l) {
+    if (l > 0) tets = refine_red(tets);
+    if (build_ug_level(G, l, tets, l > 0 ? &prev : nullptr, mask, field)) return 1;
+    prev.swap(mask);
+  }
+  return 0;
+}
+
+}  // namespace
+
 extern "C" {
 
 int gmg_gen_create(int kind, int nref, unsigned long long seed, double corr, double var, gmg_gen **out) {
-  if (!out || kind < 0 || kind > 2 || nref < 0 || nref > (kind == 1 ? 9 : 12)) {
+  if (!out || kind < 0 || kind > 3 || nref < 0 || nref > (kind == 1 ? 9 : kind == 3 ? 7 : 12)) {
     gmg::set_error("gmg_gen_create: bad arguments (kind %d, nref %d)", kind, nref);
     return 1;
   }
@@ -304,11 +551,15 @@ int gmg_gen_create(int kind, int nref, unsigned long long seed, double corr, dou
   G->kind = kind;
   G->nref = nref;
   G->lev.resize(nref + 1);
-  const int dim = kind == 1 ? 3 : 2;
+  const int dim = kind == 1 || kind == 3 ? 3 : 2;
   ugfx::LogNormalField field;
   if (var > 0.0 && kind != 2) field = ugfx::LogNormalField(seed, dim, corr, var);
-  for (int l = 0; l <= nref; ++l)
-    if (build_level(G.get(), l, field)) return 1;
+  if (kind == 3) {
+    if (build_ug_cube(G.get(), field)) return 1;
+  } else {
+    for (int l = 0; l <= nref; ++l)
+      if (build_level(G.get(), l, field)) return 1;
+  }
   G->desc.resize(nref + 1);
   for (int l = 0; l <= nref; ++l) {
     GenLevel &L = G->lev[l];
