@@ -99,6 +99,13 @@ int gmg_mg_num_waves(const gmg_mg *mg, int level);
  * evict-first matrix stream (1 / 0, -1 = chosen by size); set by the
  * autotuner (gmg_mg_opts.autotune) at creation. */
 int gmg_mg_level_variant(const gmg_mg *mg, int level, int *tpr, int *prefetch, int *stream);
+/* Chained Gauss-Seidel steps of a small multicolour level (at most 48
+ * colours, its t and c within 200 KB) in ONE thread block, the colour waves
+ * separated by block barriers instead of kernel launches; bit-identical to
+ * the per-wave launches.  The autotuner turns it on where it is faster; set
+ * it (1 / 0) before the first solve that captures a CUDA graph. */
+int gmg_mg_level_cta_chain(const gmg_mg *mg, int level, int *on);
+int gmg_mg_set_level_cta_chain(gmg_mg *mg, int level, int on);
 /* Device bytes held by the hierarchy. */
 long long gmg_mg_device_bytes(const gmg_mg *mg);
 /* Kernel launches issued by mg since creation (or the last reset). */

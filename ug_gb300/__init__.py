@@ -97,6 +97,7 @@ def lib(build_if_missing: bool = True):
         "gmg_transfer_project_solution": ([P, I, I, P, P], I),
         "gmg_transfer_adapt_correction": ([P, I, P, P, P, P], I), "gmg_mg_set_new_vectors": ([P, I, P], I),
         "gmg_mg_update_values": ([P, I, P], I), "gmg_mg_level_variant": ([P, I, P, P, P], I),
+    "gmg_mg_level_cta_chain": ([P, I, P], I), "gmg_mg_set_level_cta_chain": ([P, I, I], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -656,7 +657,16 @@ class MultiGrid:
         t, p, st = C.c_int(), C.c_int(), C.c_int()
         if lib().gmg_mg_level_variant(self._h, level, C.byref(t), C.byref(p), C.byref(st)):
             _err("level_variant")
-        return {"tpr": t.value, "prefetch": p.value, "stream": st.value}
+        on = C.c_int()
+        if lib().gmg_mg_level_cta_chain(self._h, level, C.byref(on)):
+            _err("level_cta_chain")
+        return {"tpr": t.value, "prefetch": p.value, "stream": st.value, "cta_chain": on.value}
+
+    def set_cta_chain(self, level: int, on: bool):
+        """Run the level's chained Gauss-Seidel steps in one thread block (on)
+        or as one launch per colour wave; before the first graph-captured solve."""
+        if lib().gmg_mg_set_level_cta_chain(self._h, level, int(bool(on))):
+            _err("set_cta_chain")
 
     def update_values(self, level: int, val):
         """New matrix values of a level (gmg_level_desc layout), structure unchanged."""

@@ -140,6 +140,8 @@ struct Level {
   // kernel variants of the level (autotuner; -1: by size): prefetch the
   // rows' structure before the launch wait; evict-first matrix stream
   int prefetch = -1, stream = -1;
+  // chained Gauss-Seidel steps in one thread block (gs_chain_cta_ok levels)
+  int cta_chain = 0;
   // sliced ELLPACK copy of A (slices of 32 consecutive rows stored column by
   // column, padded to the slice's longest row with zero blocks pointing at the
   // row itself): one thread per row, coalesced 32-row loads, no reductions
@@ -357,6 +359,16 @@ int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // qualifies (sliced ELLPACK, colour-contiguous waves, every row ACTIVE)
 bool gs_chain_ok(const Level &L, int prec);
 int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps);
+// the chained steps of a level in one thread block (Level::cta_chain): at
+// most CTA_CHAIN_MAXW waves, t and c of the level in shared memory
+constexpr int CTA_CHAIN_MAXW = 48;
+constexpr long long CTA_CHAIN_SMEM = 200 * 1024;
+struct CtaWaves {
+  int n, nwave, steps;
+  int ptr[CTA_CHAIN_MAXW + 1];
+};
+long long gs_chain_cta_smem(const Level &L, int prec);
+bool gs_chain_cta_ok(const Level &L, int prec);
 // ILU forward / backward solve with the factors of L
 int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // ILU(0) factors of the level matrix with beta (l_ilubthdecomp) on the device,

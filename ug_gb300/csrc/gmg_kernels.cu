@@ -12,6 +12,7 @@
 // results agree with the reference to rounding (the summation order inside a
 // row follows the shuffle tree instead of the MATRIX list).
 #include <cstdio>
+#include <map>
 #include <utility>
 
 #include "gmg_internal.h"
@@ -528,6 +529,138 @@ __global__ void __launch_bounds__(BLK) sell_upper_defect_kernel(int n, const int
   }
 #pragma unroll
   for (int r = 0; r < S; ++r) b[(size_t)i * S + r] = s[r];
+}
+
+// ------------------------------------------------------------ chained steps in one block
+// The chained steps and the closing b = -U t of one small sliced-ELLPACK
+// level (a few thousand rows) run by ONE thread block. Each colour wave of a
+// level that small keeps a few warps busy, and as separate launches every
+// wave pays a kernel handoff (~1.3 us) plus an L2 gather. Here the waves are
+// separated by __syncthreads. t and c live in shared memory for the whole
+// call. The matrix streams from L2 in its sliced-ELLPACK layout. Each
+// thread's first row of the next wave (and, in the first step, its b) is
+// loaded before the barrier, so the barrier hides those loads. Every row does
+// the arithmetic of sell_gs_chain_kernel / sell_upper_defect_kernel in the
+// same order, so the results are bit-identical to the per-wave launches.
+template <class T, int S, int PN, int NT>
+__global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_constant__ CtaWaves W,
+                                                                  const int *__restrict__ sptr,
+                                                                  const uint8_t *__restrict__ nl,
+                                                                  const int *__restrict__ scol,
+                                                                  const T *__restrict__ sval,
+                                                                  const T *__restrict__ dinv, T *__restrict__ b,
+                                                                  T *__restrict__ t, T *__restrict__ c) {
+  extern __shared__ __align__(16) unsigned char cta_smem[];
+  T *ts = reinterpret_cast<T *>(cta_smem);  // t, n * S
+  T *cs = ts + (size_t)W.n * S;             // c, n * S
+  const int tid = threadIdx.x;
+  SellPart<T, S, PN> R;
+  T D[S * S], bi[S];
+  // the static part of a row: its entries of step st and its inverse diagonal
+  auto load_row = [&](int i, int st) {
+    R.load(i, st == 0 ? 1 : 0, sptr, nl, scol, sval);
+#pragma unroll
+    for (int q = 0; q < S * S; ++q) D[q] = __ldg(dinv + (size_t)i * S * S + q);
+  };
+  auto load_b = [&](int i) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) bi[r] = b[(size_t)i * S + r];
+  };
+  int first = W.ptr[0] + tid;
+  if (first < W.ptr[1]) load_row(first, 0);
+  pdl_wait_then_trigger();
+  for (int k = tid; k < W.n * S; k += NT) cs[k] = c[k];
+  if (first < W.ptr[1]) load_b(first);
+  __syncthreads();
+  for (int st = 0; st < W.steps; ++st) {
+    for (int w = 0; w < W.nwave; ++w) {
+      const int r0 = W.ptr[w], r1 = W.ptr[w + 1];
+      for (int i = r0 + tid; i < r1; i += NT) {
+        if (i != r0 + tid) {
+          load_row(i, st);
+          if (st == 0) load_b(i);
+        }
+        T s[S];
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = st == 0 ? bi[r] : T(0);
+#pragma unroll
+        for (int k = 0; k < PN; ++k) {
+          if (k < R.w && (st == 0 ? R.col[k] < i : R.col[k] != i)) {
+#pragma unroll
+            for (int cc = 0; cc < S; ++cc) {
+              const T tv = ts[(size_t)R.col[k] * S + cc];
+#pragma unroll
+              for (int r = 0; r < S; ++r) s[r] = fma(-R.val[k][r * S + cc], tv, s[r]);
+            }
+          }
+        }
+        int e = R.e0 + 32 * (PN > 0 ? PN : 0);
+        for (int k = PN > 0 ? PN : 0; k < R.w; ++k, e += 32) {
+          const int j = __ldg(scol + e);
+          if (st == 0 ? j >= i : j == i) continue;
+          const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+          for (int cc = 0; cc < S; ++cc) {
+            const T tv = ts[(size_t)j * S + cc];
+#pragma unroll
+            for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + cc), tv, s[r]);
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+          T v = T(0);
+#pragma unroll
+          for (int cc = 0; cc < S; ++cc) v = fma(D[r * S + cc], s[cc], v);
+          ts[(size_t)i * S + r] = v;
+          cs[(size_t)i * S + r] += v;
+        }
+      }
+      // this thread's first row of the next wave, before the barrier
+      const int w2 = w + 1 < W.nwave ? w + 1 : 0, st2 = w + 1 < W.nwave ? st : st + 1;
+      const int i2 = W.ptr[w2] + tid;
+      if (st2 < W.steps && i2 < W.ptr[w2 + 1]) {
+        load_row(i2, st2);
+        if (st2 == 0) load_b(i2);
+      }
+      __syncthreads();
+    }
+  }
+  // b = -U t, then t and c back to global memory
+  for (int i = tid; i < W.n; i += NT) {
+    R.load(i, 2, sptr, nl, scol, sval);
+    T s[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) s[r] = T(0);
+#pragma unroll
+    for (int k = 0; k < PN; ++k) {
+      if (k < R.w && R.col[k] > i) {
+#pragma unroll
+        for (int cc = 0; cc < S; ++cc) {
+          const T tv = ts[(size_t)R.col[k] * S + cc];
+#pragma unroll
+          for (int r = 0; r < S; ++r) s[r] = fma(-R.val[k][r * S + cc], tv, s[r]);
+        }
+      }
+    }
+    int e = R.e0 + 32 * (PN > 0 ? PN : 0);
+    for (int k = PN > 0 ? PN : 0; k < R.w; ++k, e += 32) {
+      const int j = __ldg(scol + e);
+      if (j <= i) continue;
+      const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+      for (int cc = 0; cc < S; ++cc) {
+        const T tv = ts[(size_t)j * S + cc];
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + cc), tv, s[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < S; ++r) b[(size_t)i * S + r] = s[r];
+  }
+  for (int k = tid; k < W.n * S; k += NT) {
+    t[k] = ts[k];
+    c[k] = cs[k];
+  }
 }
 
 // ------------------------------------------------------------ l_jac
@@ -2378,8 +2511,59 @@ bool gs_chain_ok(const Level &L, int prec) {
   return L.sell && L.waves_contiguous && L.all_active && (prec == GMG_PREC_FP64 || (L.sell_v32 && L.dinv32));
 }
 
+long long gs_chain_cta_smem(const Level &L, int prec) {
+  return 2ll * L.n * L.s * (prec == GMG_PREC_FP64 ? 8 : 4);
+}
+
+bool gs_chain_cta_ok(const Level &L, int prec) {
+  return gs_chain_ok(L, prec) && L.lower.nwave() <= CTA_CHAIN_MAXW && gs_chain_cta_smem(L, prec) <= CTA_CHAIN_SMEM;
+}
+
+template <class T, int S>
+static int gs_chain_cta(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
+  constexpr int NT = S == 1 && sizeof(T) == 4 ? 1024 : 512;  // 64 / 128 registers a thread
+  CtaWaves W{};
+  W.n = L.n;
+  W.nwave = L.lower.nwave();
+  W.steps = steps;
+  for (int w = 0; w <= W.nwave; ++w) W.ptr[w] = L.lower.ptr[w];
+  const int smem = int(gs_chain_cta_smem(L, sizeof(T) == 8 ? GMG_PREC_FP64 : GMG_PREC_FP32));
+  auto kern = sell_gs_chain_cta_kernel<T, S, PF<S>::N, NT>;
+  static thread_local std::map<void *, int> smem_set;
+  if (smem_set[(void *)kern] < smem) {
+    GMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    smem_set[(void *)kern] = smem;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(1);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = mg->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = mg->opts.disable_pdl ? 0 : 1;
+  const uint8_t *nl = L.sell_split ? L.sell_nl : nullptr;
+  cudaLaunchKernelEx(&cfg, kern, W, (const int *)L.sell_ptr, nl, (const int *)L.sell_col, sell_val<T>(L),
+                     dinv_of<T>(L), b, t, c);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps) {
   GMG_CHECK(gs_chain_ok(L, prec) && steps >= 1, "chained Gauss-Seidel steps need a colour-ordered SELL level");
+  if (L.cta_chain && gs_chain_cta_ok(L, prec)) {
+    if (prec == GMG_PREC_FP64) {
+      if (L.s == 1) return gs_chain_cta<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+      if (L.s == 2) return gs_chain_cta<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+      if (L.s == 3) return gs_chain_cta<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+    } else {
+      if (L.s == 1) return gs_chain_cta<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+      if (L.s == 2) return gs_chain_cta<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+      if (L.s == 3) return gs_chain_cta<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+    }
+  }
   if (prec == GMG_PREC_FP64) {
     if (L.s == 1) return gs_chain<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps);
     if (L.s == 2) return gs_chain<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps);

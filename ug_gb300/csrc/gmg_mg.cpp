@@ -599,16 +599,20 @@ static int pick_tpr(const HostLevel &H) {
 // evict-first matrix stream where the matrix exceeds half of L2); on CSR
 // levels the threads per row.
 // Median of 3 timed chains after one warm-up, in the precision the V-cycle
-// uses (FP32 when the hierarchy has FP32 copies).
+// uses (FP32 when the hierarchy has FP32 copies).  Levels that can run their
+// chained Gauss-Seidel steps in one thread block (gs_chain_cta_ok) also time
+// two chained steps both ways, as lmgc's pre-smoothing runs them.
 static int autotune_level(gmg_mg *mg, Level &L) {
   if (L.n < 256) return 0;
   const int prec = mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64;
-  void *x = nullptr, *y = nullptr;
+  void *x = nullptr, *y = nullptr, *z = nullptr;
   size_t len = size_t(L.n) * L.s;
   GMG_CUDA(cudaMalloc(&x, len * sizeof(double)));
   GMG_CUDA(cudaMalloc(&y, len * sizeof(double)));
+  GMG_CUDA(cudaMalloc(&z, len * sizeof(double)));
   cudaMemsetAsync(x, 0, len * sizeof(double), mg->stream);
   cudaMemsetAsync(y, 0, len * sizeof(double), mg->stream);
+  cudaMemsetAsync(z, 0, len * sizeof(double), mg->stream);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -616,12 +620,12 @@ static int autotune_level(gmg_mg *mg, Level &L) {
   // each kernel's pre-wait part overlap its predecessor, which an isolated
   // launch would not show
   constexpr int CHAIN = 8;
-  auto time_it = [&]() -> float {
+  auto time_op = [&](auto op) -> float {
     std::vector<float> ts;
     for (int rep = 0; rep < 4; ++rep) {
       cudaEventRecord(e0, mg->stream);
       for (int k = 0; k < CHAIN; ++k)
-        if (k_matmul_minus(mg, L, prec, x, y, nullptr)) return 1e30f;
+        if (op()) return 1e30f;
       cudaEventRecord(e1, mg->stream);
       cudaEventSynchronize(e1);
       float ms = 0;
@@ -631,6 +635,15 @@ static int autotune_level(gmg_mg *mg, Level &L) {
     std::sort(ts.begin(), ts.end());
     return ts[ts.size() / 2];
   };
+  auto time_it = [&]() -> float { return time_op([&]() { return k_matmul_minus(mg, L, prec, x, y, nullptr); }); };
+  if (gs_chain_cta_ok(L, prec)) {
+    auto chain = [&]() { return k_gs_chain(mg, L, prec, x, y, z, 2); };
+    L.cta_chain = 0;
+    const float waves_ms = time_op(chain);
+    L.cta_chain = 1;
+    const float cta_ms = time_op(chain);
+    L.cta_chain = cta_ms < 0.95f * waves_ms;
+  }
   float best_ms = 1e30f;
   if (L.sell) {
     // the size-based default first; another variant must be 5 % faster to
@@ -665,6 +678,8 @@ static int autotune_level(gmg_mg *mg, Level &L) {
   cudaEventDestroy(e1);
   cudaFree(x);
   cudaFree(y);
+  cudaFree(z);
+  GMG_CUDA(cudaGetLastError());
   return 0;
 }
 
@@ -1060,6 +1075,32 @@ int gmg_mg_update_values(gmg_mg *mg, int level, const double *val) {
 // the kernel variant of a level: threads per row (CSR levels), prefetch
 // before the launch wait and evict-first stream (sliced-ELLPACK levels; -1 =
 // chosen by size)
+int gmg_mg_level_cta_chain(const gmg_mg *mg, int level, int *on) {
+  if (!mg || !on || level < 0 || level >= int(mg->lev.size())) {
+    set_error("gmg_mg_level_cta_chain: bad arguments");
+    return 1;
+  }
+  *on = mg->lev[level].cta_chain;
+  return 0;
+}
+
+int gmg_mg_set_level_cta_chain(gmg_mg *mg, int level, int on) {
+  if (!mg || level < 0 || level >= int(mg->lev.size()) || (on != 0 && on != 1)) {
+    set_error("gmg_mg_set_level_cta_chain: bad arguments");
+    return 1;
+  }
+  Level &L = mg->lev[level];
+  if (on && !gs_chain_cta_ok(L, mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64)) {
+    set_error("gmg_mg_set_level_cta_chain: level %d cannot run its chained steps in one thread block "
+              "(needs a multicolour sliced-ELLPACK level, all rows active, at most %d colours, t and c in %lld "
+              "bytes of shared memory)",
+              level, CTA_CHAIN_MAXW, CTA_CHAIN_SMEM);
+    return 1;
+  }
+  L.cta_chain = on;
+  return 0;
+}
+
 int gmg_mg_level_variant(const gmg_mg *mg, int level, int *tpr, int *prefetch, int *stream) {
   if (!mg || level < 0 || level >= int(mg->lev.size())) { set_error("gmg_mg_level_variant: bad arguments"); return 1; }
   const Level &L = mg->lev[level];
