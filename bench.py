@@ -40,6 +40,33 @@ MESH = "ug"
 MESHES = {"ug": "UG red rules (shortest interior diagonal)", "freudenthal": "Freudenthal triangulation"}
 
 
+# CUDA graphs for the ls iterations of every workload ($graph / $dloop);
+# --no-graph turns them off so that profilers see every kernel launch
+GRAPH = 1
+
+
+class nvtx_range:
+    """An NVTX range around one region (`ncu --nvtx --nvtx-include name/`
+    then captures only its kernels); a no-op where NVTX is unavailable."""
+
+    def __init__(self, name: str, on: bool = True):
+        self.name, self.on = name, on
+
+    def __enter__(self):
+        if self.on:
+            try:
+                import torch
+                torch.cuda.nvtx.range_push(self.name)
+            except Exception:
+                self.on = False
+        return self
+
+    def __exit__(self, *a):
+        if self.on:
+            import torch
+            torch.cuda.nvtx.range_pop()
+
+
 def gen_kind(G):
     return G.Generator.DIFFUSION3D_UG if MESH == "ug" else G.Generator.DIFFUSION3D
 
@@ -281,9 +308,10 @@ def run_local(args, stream, flush_l2, world, rank):
     t0 = time.perf_counter()
     mg = G.MultiGrid(gen, order=G.ORDER_DOMAIN, fp32=True, autotune=True, device=torch.cuda.current_device())
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
-    G.setup_lmgc(mg, "ilu", baselevel=0, red=RED, abslimit=1e-50, name="loc64")
+    G.setup_lmgc(mg, "ilu", baselevel=0, red=RED, abslimit=1e-50, name="loc64", graph=GRAPH, dloop=GRAPH)
     mg.npcreate("loc32", "linear_solver.gls")
-    mg.npinit("loc32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    mg.npinit("loc32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1"
+                       f" $graph {GRAPH} $dloop {GRAPH}")
     top = mg.top
     mg.createvector("b0")
     mg.upload_levels("b0", gen.rhs)
@@ -319,14 +347,15 @@ def run_local(args, stream, flush_l2, world, rank):
         for _ in range(args.warmup):
             step(solver)
         ms, launches = [], 0
-        for _ in range(args.steps):
+        for k in range(args.steps):
             flush_l2()
             mg.launch_count(reset=True)
             a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            lr = step(solver)
-            e.record(stream)
-            torch.cuda.synchronize()
+            with nvtx_range("c3_mixed_solve", solver == "loc32" and k == args.steps - 1):
+                a.record(stream)
+                lr = step(solver)
+                e.record(stream)
+                torch.cuda.synchronize()
             launches += mg.launch_count()
             assert lr.converged, f"{solver} did not converge"
             ms.append(a.elapsed_time(e))
@@ -408,9 +437,10 @@ def run_batched(args, stream, flush_l2, world, rank):
     mg = G.MultiGrid(gens, batched=True, order=G.ORDER_LIST, fp32=True, autotune=True,
                      device=torch.cuda.current_device())
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
-    G.setup_lmgc(mg, "jac", baselevel=0, red=RED, abslimit=1e-50, name="bat64")
+    G.setup_lmgc(mg, "jac", baselevel=0, red=RED, abslimit=1e-50, name="bat64", graph=GRAPH, dloop=GRAPH)
     mg.npcreate("bat32", "linear_solver.gls")
-    mg.npinit("bat32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1")
+    mg.npinit("bat32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1"
+                       f" $graph {GRAPH} $dloop {GRAPH}")
     b = mg.pack([g.rhs for g in gens])
     x = np.empty_like(b)
     unknowns = int(b.size)
@@ -425,11 +455,12 @@ def run_batched(args, stream, flush_l2, world, rank):
             mg.solve_host(solver, b, x)
         ms, iters, launches = [], 0, 0
         with ClockSampler(torch.cuda.current_device()) as clk:
-            for _ in range(args.steps):
+            for k in range(args.steps):
                 flush_l2(); torch.cuda.synchronize()
                 mg.launch_count(reset=True)
                 t0 = time.perf_counter()
-                _, lr = mg.solve_host(solver, b, x)
+                with nvtx_range("c4_batch", solver == "bat32" and k == args.steps - 1):
+                    _, lr = mg.solve_host(solver, b, x)
                 ms.append((time.perf_counter() - t0) * 1e3)
                 launches += mg.launch_count()
                 assert lr.converged, f"batched {solver} did not converge"
@@ -724,24 +755,25 @@ def c2_roofline(G, mg, stream, flush_l2, reps=20, skip=3):
     launches_smooth = 2 * nwaves + 1
     algo = {64: nnz * (8 + 4) + (n + 1) * 4 + 3 * n * 8, 32: nnz * (4 + 4) + (n + 1) * 4 + 3 * n * 4}
 
-    def event_ms(fn):
+    def event_ms(fn, name):
         ts = []
         for k in range(reps):
             if k % 5 == 0:
                 mg.upload("sb32", top, b0)  # keep the defect away from denormals
             flush_l2()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            torch.cuda.synchronize()
+            with nvtx_range(name, k == reps - 1):
+                a.record(stream)
+                fn()
+                b.record(stream)
+                torch.cuda.synchronize()
             if k >= skip:
                 ts.append(a.elapsed_time(b))
         return float(np.mean(ts))
 
-    sm_ms = event_ms(lambda: mg.iter_smooth("smooth", top, "st32", "sb32", "sc32", 2))
-    kms = {64: event_ms(lambda: mg.dmatmul_minus(top, "rx", "ry")),
-           32: event_ms(lambda: mg.dmatmul_minus(top, "rx32", "ry32"))}
+    sm_ms = event_ms(lambda: mg.iter_smooth("smooth", top, "st32", "sb32", "sc32", 2), "c2_smooth")
+    kms = {64: event_ms(lambda: mg.dmatmul_minus(top, "rx", "ry"), "c2_spmv64"),
+           32: event_ms(lambda: mg.dmatmul_minus(top, "rx32", "ry32"), "c2_spmv32")}
     peak, peak_kind = measured_peak()
     ach = algo_smooth / (sm_ms * 1e-3) / 1e9
     ach32 = algo[32] / (kms[32] * 1e-3) / 1e9
@@ -764,6 +796,47 @@ def c2_roofline(G, mg, stream, flush_l2, reps=20, skip=3):
 
 
 # ---------------------------------------------------------------- our arm
+def mesh_comparison(args, stream, flush_l2, world):
+    """The same mixed solve on the Freudenthal triangulation of the cube (same
+    nodes, same edge count, 4 colours on every level where UG's red rules
+    need up to 9): what the colour count costs.  Device-timed like `value`."""
+    import torch
+    import ug_gb300 as G
+    gen = G.Generator(G.Generator.DIFFUSION3D, NREF, seed=SEED, corr=CORR, var=VAR)
+    mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True, autotune=True)
+    G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
+    mg.createvector("sol", "rhs", "rhs0")
+    G.setup_lmgc(mg, "gs", baselevel=0, red=RED, abslimit=1e-50, name="mgs64")
+    mg.npcreate("mgs32", "linear_solver.gls")
+    mg.npinit("mgs32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1 $graph 1 $dloop 1")
+    top = mg.top
+    mg.upload("rhs0", top, gen.rhs)
+    mg.ls_preprocess("mgs32", top, "sol", "rhs")
+    ms, it = [], 0
+    for k in range(args.warmup + args.steps):
+        flush_l2()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lr = G.LResult()
+        e0.record(stream)
+        mg.dcopy(top, "rhs", "rhs0")
+        mg.dset(top, "sol", 0.0)
+        mg.ls_defect("mgs32", top, "sol", "rhs")
+        mg.ls_residuum("mgs32", 0, top, "sol", "rhs", lr)
+        mg.ls_solver("mgs32", top, "sol", "rhs", lr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        assert lr.converged
+        it = lr.iters
+        if k >= args.warmup:
+            ms.append(e0.elapsed_time(e1))
+    waves = [mg.num_waves(l) for l in range(mg.nlevels)]
+    mg.close()
+    ms_step = reduce_over_ranks(float(np.mean(ms)), "max")
+    return {"value": whole_job_rate(1, ms_step, world), "unit": "solves/s", "ms_per_step": ms_step,
+            "iterations": it, "gs_waves_per_level": waves,
+            "note": "mixed solve of the same problem on the Freudenthal triangulation (not UG's mesh)"}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -799,7 +872,7 @@ def run_ours(args):
     mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True, autotune=True, device=local)
     G.lib().gmg_mg_set_stream(mg._h, stream.cuda_stream)
     mg.createvector("sol", "rhs", "rhs0")
-    graph = not args.no_graph
+    graph = bool(GRAPH)
     G.setup_lmgc(mg, "gs", baselevel=0, red=RED, abslimit=1e-50, name="mgs64", graph=graph, dloop=graph)
     mg.npcreate("mgs32", "linear_solver.gls")
     mg.npinit("mgs32", f"$A MAT $x sol $b rhs $red {RED} $abslimit 1e-50 $m 100 $I lmgc $mixed 1"
@@ -807,12 +880,6 @@ def run_ours(args):
     top = mg.top
     mg.upload("rhs0", top, gen.rhs)
     mg.ls_preprocess("mgs64", top, "sol", "rhs")
-    if args.only == "roofline":  # the roofline kernels alone (profiling runs)
-        roof = c2_roofline(G, mg, stream, flush_l2, reps=args.warmup + args.steps, skip=args.warmup)
-        mg.close()
-        if rank == 0:
-            print(json.dumps({"only": "roofline", "roofline": roof}), flush=True)
-        return
 
     def step(solver):
         lr = G.LResult()
@@ -822,6 +889,35 @@ def run_ours(args):
         mg.ls_residuum(solver, 0, top, "sol", "rhs", lr)
         mg.ls_solver(solver, top, "sol", "rhs", lr)
         return lr
+
+    if args.only == "c2mixed":  # the headline mixed solve alone (profiling runs)
+        ms = []
+        mg.launch_count(reset=True)
+        for k in range(args.warmup + args.steps):
+            flush_l2()
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with nvtx_range("c2_mixed_solve", k == args.warmup + args.steps - 1):
+                a.record(stream)
+                lr = step("mgs32")
+                e.record(stream)
+                torch.cuda.synchronize()
+            assert lr.converged
+            if k >= args.warmup:
+                ms.append(a.elapsed_time(e))
+        out = {"ms_per_step": float(np.mean(ms)), "iterations": lr.iters,
+               "launches_per_solve": mg.launch_count() / (args.warmup + args.steps), "graph": graph,
+               "mesh": MESH, "gs_waves_per_level": [mg.num_waves(l) for l in range(mg.nlevels)],
+               "variants": [mg.level_variant(l) for l in range(mg.nlevels)]}
+        mg.close()
+        if rank == 0:
+            print(json.dumps({"only": "c2mixed", "c2mixed": out}), flush=True)
+        return
+    if args.only == "roofline":  # the roofline kernels alone (profiling runs)
+        roof = c2_roofline(G, mg, stream, flush_l2, reps=args.warmup + args.steps, skip=args.warmup)
+        mg.close()
+        if rank == 0:
+            print(json.dumps({"only": "roofline", "roofline": roof}), flush=True)
+        return
 
     def barrier():
         if world > 1:
@@ -905,6 +1001,7 @@ def run_ours(args):
     waves = [mg.num_waves(l) for l in range(mg.nlevels)]
     variants = [mg.level_variant(l) for l in range(mg.nlevels)]
     mg.close()
+    other_mesh = mesh_comparison(args, stream, flush_l2, world) if MESH == "ug" else None
     rest = args.only != "c2"
     c1 = run_c1(args, stream, flush_l2, world, rank) if rest else None
     local_c3 = run_local(args, stream, flush_l2, world, rank) if rest and not args.no_local else None
@@ -939,6 +1036,7 @@ def run_ours(args):
             "clocks": r32["clocks"],
             "cpu_baseline": cpu,
             "accuracy": accuracy,
+            "freudenthal_mesh": other_mesh,
             "config1": c1,
             "local_refinement": local_c3,
             "batched": batched,
@@ -951,7 +1049,7 @@ def run_ours(args):
 
 
 def main():
-    global MESH
+    global MESH, GRAPH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -963,10 +1061,10 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests of the serving stream")
     ap.add_argument("--no-graph", action="store_true",
-                    help="C2 solvers without CUDA graphs ($graph 0 $dloop 0): every kernel an individual launch, "
+                    help="ls solvers without CUDA graphs ($graph 0 $dloop 0): every kernel an individual launch, "
                          "for profilers that do not see inside conditional graphs; not a benchmark setting")
-    ap.add_argument("--only", default="all", choices=["all", "c2", "roofline", "c1", "local", "batched", "serving",
-                                                      "serving_mixed"],
+    ap.add_argument("--only", default="all", choices=["all", "c2", "c2mixed", "roofline", "c1", "local", "batched",
+                                                      "serving", "serving_mixed"],
                     help="run one workload alone and print its JSON (profiling runs); c2: the headline solve "
                          "without the other workloads; roofline: the C2 roofline kernels only, warmup + steps "
                          "repetitions each")
@@ -975,6 +1073,7 @@ def main():
                          "freudenthal = the Freudenthal triangulation (same nodes and edge counts)")
     args = ap.parse_args()
     MESH = args.mesh
+    GRAPH = 0 if args.no_graph else 1
     if args.impl == "reference":
         run_reference(args)
     else:
