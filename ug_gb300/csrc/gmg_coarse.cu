@@ -44,6 +44,7 @@ constexpr int NARROW = 128; // threads of the team that runs the smallest levels
 struct SLev {
   int n, all_active, nwave, nuwave;
   int o_rowptr, o_col, o_val, o_dinv, o_flags, o_skip;
+  int o_lend;  // per row: end of its lower entries (rows stored diagonal | lower | upper)
   int o_wptr, o_wrows, o_uptr, o_urows;
   int o_lrow, o_lcol, o_lval, o_urow, o_ucol, o_uval, o_udinv;
   int o_prow, o_pcol, o_pw, o_rrow, o_rcol, o_rw;
@@ -66,7 +67,8 @@ struct SArgs {
 template <class T>
 struct PL {
   int n, all_active, nwave, nuwave;
-  const int *rowptr, *col, *wptr, *wrows, *uptr, *urows, *lrow, *lcol, *urow, *ucol, *prow, *pcol, *rrow, *rcol;
+  const int *rowptr, *lend, *col, *wptr, *wrows, *uptr, *urows, *lrow, *lcol, *urow, *ucol, *prow, *pcol, *rrow,
+      *rcol;
   const T *val, *dinv, *lval, *uval, *udinv, *pw, *rw;
   const uint8_t *flags, *skip;
   T *b, *c, *t;
@@ -78,7 +80,8 @@ __device__ PL<T> make_pl(const SLev &s, char *sm) {
   p.n = s.n; p.all_active = s.all_active; p.nwave = s.nwave; p.nuwave = s.nuwave;
   auto I = [&](int o) { return o >= 0 ? (const int *)(sm + o) : nullptr; };
   auto V = [&](int o) { return o >= 0 ? (const T *)(sm + o) : nullptr; };
-  p.rowptr = I(s.o_rowptr); p.col = I(s.o_col); p.wptr = I(s.o_wptr); p.wrows = I(s.o_wrows);
+  p.rowptr = I(s.o_rowptr); p.lend = I(s.o_lend); p.col = I(s.o_col); p.wptr = I(s.o_wptr);
+  p.wrows = I(s.o_wrows);
   p.uptr = I(s.o_uptr); p.urows = I(s.o_urows); p.lrow = I(s.o_lrow); p.lcol = I(s.o_lcol);
   p.urow = I(s.o_urow); p.ucol = I(s.o_ucol); p.prow = I(s.o_prow); p.pcol = I(s.o_pcol);
   p.rrow = I(s.o_rrow); p.rcol = I(s.o_rcol);
@@ -101,15 +104,16 @@ __device__ __forceinline__ T gsum(T v) {
   return v;
 }
 
-// s += sum over the lane's share of `row` (entries j < lim when LOWER) of m_k * v_j
+// s += sum over the lane's share of `row` of m_k * v_j: the whole row, or
+// (LOWER, with the row's lower end `lend`) its strictly lower entries, which
+// the image stores right after the diagonal
 template <class T, int S, int G, bool LOWER>
-__device__ __forceinline__ void row_dot(const int *rowptr, const int *col, const T *val, const T *v, int row,
-                                        int first, int lane, bool on, T *s) {
-  const int k1 = on ? rowptr[row + 1] : 0;
+__device__ __forceinline__ void row_dot(const int *rowptr, const int *lend, const int *col, const T *val,
+                                        const T *v, int row, int first, int lane, bool on, T *s) {
+  const int k1 = on ? (LOWER ? lend[row] : rowptr[row + 1]) : 0;
 #pragma unroll 4
   for (int k = on ? rowptr[row] + first + lane : 0; k < k1; k += G) {
     const int j = col[k];
-    if (LOWER && j >= row) continue;
     const T *m = val + (size_t)k * S * S;
 #pragma unroll
     for (int r = 0; r < S; ++r)
@@ -151,7 +155,7 @@ __device__ void c_spmv(const PL<T> &L, T *x, const T *y, T *acc, const Team &tm)
     T s[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) s[r] = T(0);
-    row_dot<T, S, G, false>(L.rowptr, L.col, L.val, y, i, 0, tm.lane, valid, s);
+    row_dot<T, S, G, false>(L.rowptr, L.lend, L.col, L.val, y, i, 0, tm.lane, valid, s);
     if (own) {
 #pragma unroll
       for (int r = 0; r < S; ++r) {
@@ -202,7 +206,7 @@ __device__ void c_gs(const PL<T> &L, const Team &tm) {
       T s[S];
 #pragma unroll
       for (int r = 0; r < S; ++r) s[r] = T(0);
-      row_dot<T, S, G, true>(L.rowptr, L.col, L.val, L.t, i, 1, tm.lane, act, s);
+      row_dot<T, S, G, true>(L.rowptr, L.lend, L.col, L.val, L.t, i, 1, tm.lane, act, s);
       if (own) {
         T rhs[S];
 #pragma unroll
@@ -234,7 +238,7 @@ __device__ void c_ilu(const PL<T> &L, const Team &tm) {
       T s[S];
 #pragma unroll
       for (int r = 0; r < S; ++r) s[r] = T(0);
-      row_dot<T, S, G, false>(L.lrow, L.lcol, L.lval, L.t, i, 0, tm.lane, act, s);
+      row_dot<T, S, G, false>(L.lrow, nullptr, L.lcol, L.lval, L.t, i, 0, tm.lane, act, s);
       if (valid && tm.lane == 0)
 #pragma unroll
         for (int r = 0; r < S; ++r) L.t[i * S + r] = act ? L.b[i * S + r] - s[r] : T(0);
@@ -251,7 +255,7 @@ __device__ void c_ilu(const PL<T> &L, const Team &tm) {
       T s[S];
 #pragma unroll
       for (int r = 0; r < S; ++r) s[r] = T(0);
-      row_dot<T, S, G, false>(L.urow, L.ucol, L.uval, L.t, i, 0, tm.lane, act, s);
+      row_dot<T, S, G, false>(L.urow, nullptr, L.ucol, L.uval, L.t, i, 0, tm.lane, act, s);
       if (act && tm.lane == 0) {
         T rhs[S];
 #pragma unroll
@@ -652,6 +656,25 @@ int build_image(gmg_mg *mg, int bl, int nl, int smo, const std::vector<LevelHost
     }
     d.all_active = all;
     sub_csr(L.h_rowptr, L.h_col, R, loc[k], rp, cl, src);
+    {  // every row as diagonal | strictly lower | upper, each part in stored order
+      std::vector<int> c2(cl.size()), s2(src.size()), lend(n);
+      for (int q = 0; q < n; ++q) {
+        int o = rp[q];
+        for (int part = 0; part < 3; ++part) {
+          for (int e = rp[q]; e < rp[q + 1]; ++e) {
+            const int p = cl[e] == q ? 0 : (cl[e] < q ? 1 : 2);
+            if (p != part) continue;
+            c2[o] = cl[e];
+            s2[o] = src[e];
+            ++o;
+          }
+          if (part == 1) lend[q] = o;
+        }
+      }
+      cl.swap(c2);
+      src.swap(s2);
+      d.o_lend = im.add(lend.data(), lend.size() * 4);
+    }
     d.o_rowptr = im.add(rp.data(), rp.size() * 4);
     d.o_col = im.add(cl.data(), cl.size() * 4);
     auto v = gather_blocks<T>(L.h_val.data(), src, ss);
@@ -877,7 +900,8 @@ long long coarse_smem_bytes(const gmg_mg *mg_c, int bl, int lc, int prec, int sm
   for (int l = bl; l <= lc; ++l) {
     const Level &L = mg->lev[l];
     const size_t nnz = L.h_rowptr[L.n];
-    b += al((L.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * T) + al(size_t(L.n) * ss * T) + 2 * al(L.n);
+    b += al((L.n + 1) * 4) + al(size_t(L.n) * 4) + al(nnz * 4) + al(nnz * ss * T) + al(size_t(L.n) * ss * T) +
+         2 * al(L.n);
     b += al(L.lower.ptr.size() * 4) + al(L.upper.ptr.size() * 4) + 2 * al(size_t(L.n) * 4);
     if (smo == 2 && l > bl) b += 2 * (al((L.n + 1) * 4) + al(nnz * 4) + al(nnz * ss * T)) + al(size_t(L.n) * ss * T);
     if (l > bl)
