@@ -379,11 +379,15 @@ def run_local(args, stream, flush_l2, world, rank):
     # off-diagonal blocks of L and U (nnz - n) and the n inverse diagonal blocks
     lu_bytes = (nnz_t - n_t) * (s_t * s_t * 4 + 4) + n_t * s_t * s_t * 4 + 2 * (n_t + 1) * 4 + 3 * n_t * s_t * 4
     peak, peak_kind = measured_peak()
-    out["ilu_sweep"] = {"kernel": "l_luiter FP32 on the finest level (subdomain interiors + 6+6 interface colours), "
-                                  "HBM-cold", "launch_ms": lu_ms, "algorithmic_bytes": int(lu_bytes),
+    dom = mg.domain_info(top)
+    nc = dom["interface_colours"]
+    out["ilu_sweep"] = {"kernel": f"l_luiter FP32 on the finest level ({dom['subdomains']} subdomain interiors, "
+                                  f"{dom['interior_rows']} rows, + {nc}+{nc} interface colours), HBM-cold",
+                        "launch_ms": lu_ms, "algorithmic_bytes": int(lu_bytes),
                         "achieved": lu_bytes / (lu_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": lu_bytes / (lu_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
-                        "note": "latency-bound: ~18 interior wavefronts per subdomain block, 12 dependent colour launches"}
+                        "note": f"latency-bound: ~18 interior wavefronts per subdomain block, {2 * nc} dependent "
+                                "interface-colour launches"}
     b_host = np.ascontiguousarray(gen.rhs)
     x_host = np.empty_like(b_host)
     mg.solve_host("loc32", b_host, x_host)

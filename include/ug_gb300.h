@@ -94,6 +94,9 @@ int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm);
 int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val);
 /* Number of multicolour classes (wavefronts of the gs/ilu schedule) on a level. */
 int gmg_mg_num_waves(const gmg_mg *mg, int level);
+/* Subdomain order (GMG_ORDER_DOMAIN) of a level: subdomains, interior rows
+ * and interface colours (all 0 in the other orders). */
+int gmg_mg_domain_info(const gmg_mg *mg, int level, int *nsub, int *ninterior, int *ncolours);
 /* The kernel variant a level runs: threads per row (CSR levels, 0 on
  * sliced-ELLPACK levels), row structure prefetched before the launch wait and
  * evict-first matrix stream (1 / 0, -1 = chosen by size); set by the

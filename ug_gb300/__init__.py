@@ -98,6 +98,7 @@ def lib(build_if_missing: bool = True):
         "gmg_transfer_adapt_correction": ([P, I, P, P, P, P], I), "gmg_mg_set_new_vectors": ([P, I, P], I),
         "gmg_mg_update_values": ([P, I, P], I), "gmg_mg_level_variant": ([P, I, P, P, P], I),
     "gmg_mg_level_cta_chain": ([P, I, P], I), "gmg_mg_set_level_cta_chain": ([P, I, I], I),
+    "gmg_mg_domain_info": ([P, I, P, P, P], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -661,6 +662,13 @@ class MultiGrid:
         if lib().gmg_mg_level_cta_chain(self._h, level, C.byref(on)):
             _err("level_cta_chain")
         return {"tpr": t.value, "prefetch": p.value, "stream": st.value, "cta_chain": on.value}
+
+    def domain_info(self, level: int) -> dict:
+        """Subdomain order of a level: subdomains, interior rows, interface colours."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        if lib().gmg_mg_domain_info(self._h, level, C.byref(a), C.byref(b), C.byref(c)):
+            _err("domain_info")
+        return {"subdomains": a.value, "interior_rows": b.value, "interface_colours": c.value}
 
     def set_cta_chain(self, level: int, on: bool):
         """Run the level's chained Gauss-Seidel steps in one thread block (on)

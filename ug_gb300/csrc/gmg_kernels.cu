@@ -556,32 +556,9 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_c
   const int tid = threadIdx.x;
   SellPart<T, S, PN> R;
   T D[S * S], bi[S];
-  // a row's entries of `part` into R, leaving the unrolled loop after the
-  // row's last entry (one SM issues every instruction of this kernel, and a
-  // lower or upper half is about half of PN)
-  auto load_part = [&](int i, int part) {
-    const int base = __ldg(sptr + (i >> 5));
-    const int wt = (__ldg(sptr + (i >> 5) + 1) - base) >> 5;
-    int kb = 1, ke = wt;
-    if (nl && part) {
-      const int m = 1 + __ldg(nl + i);
-      if (part == 1) ke = m;
-      else kb = m;
-    }
-    R.w = ke - kb;
-    R.e0 = base + (i & 31) + 32 * kb;
-#pragma unroll
-    for (int k = 0; k < PN; ++k) {
-      if (k >= R.w) break;
-      const int e = R.e0 + 32 * k;
-      R.col[k] = __ldg(scol + e);
-#pragma unroll
-      for (int q = 0; q < S * S; ++q) R.val[k][q] = __ldg(sval + (size_t)e * (S * S) + q);
-    }
-  };
   // the static part of a row: its entries of step st and its inverse diagonal
   auto load_row = [&](int i, int st) {
-    load_part(i, st == 0 ? 1 : 0);
+    R.load(i, st == 0 ? 1 : 0, sptr, nl, scol, sval);
 #pragma unroll
     for (int q = 0; q < S * S; ++q) D[q] = __ldg(dinv + (size_t)i * S * S + q);
   };
@@ -608,8 +585,7 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_c
         for (int r = 0; r < S; ++r) s[r] = st == 0 ? bi[r] : T(0);
 #pragma unroll
         for (int k = 0; k < PN; ++k) {
-          if (k >= R.w) break;
-          if (st == 0 ? R.col[k] < i : R.col[k] != i) {
+          if (k < R.w && (st == 0 ? R.col[k] < i : R.col[k] != i)) {
 #pragma unroll
             for (int cc = 0; cc < S; ++cc) {
               const T tv = ts[(size_t)R.col[k] * S + cc];
@@ -651,14 +627,13 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_c
   }
   // b = -U t, then t and c back to global memory
   for (int i = tid; i < W.n; i += NT) {
-    load_part(i, 2);
+    R.load(i, 2, sptr, nl, scol, sval);
     T s[S];
 #pragma unroll
     for (int r = 0; r < S; ++r) s[r] = T(0);
 #pragma unroll
     for (int k = 0; k < PN; ++k) {
-      if (k >= R.w) break;
-      if (R.col[k] > i) {
+      if (k < R.w && R.col[k] > i) {
 #pragma unroll
         for (int cc = 0; cc < S; ++cc) {
           const T tv = ts[(size_t)R.col[k] * S + cc];

@@ -1565,6 +1565,18 @@ int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double
   return 0;
 }
 
+int gmg_mg_domain_info(const gmg_mg *mg, int level, int *nsub, int *ninterior, int *ncolours) {
+  if (!mg || level < 0 || level >= (int)mg->lev.size() || !nsub || !ninterior || !ncolours) {
+    set_error("gmg_mg_domain_info: bad arguments");
+    return 1;
+  }
+  const Level &L = mg->lev[level];
+  *nsub = L.dom_nreg;
+  *ninterior = L.dom_nint;
+  *ncolours = L.dom_cptr.empty() ? 0 : int(L.dom_cptr.size()) - 1;
+  return 0;
+}
+
 int gmg_mg_num_waves(const gmg_mg *mg, int level) {
   if (!mg || level < 0 || level >= (int)mg->lev.size()) return -1;
   return mg->lev[level].lower.nwave();
