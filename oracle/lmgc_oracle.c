@@ -428,6 +428,37 @@ void orc_interpolate_imat(const orc_level *fine, const orc_imat *M, double *to, 
       for (int r = 0; r < s; ++r) to[(size_t)f * s + r] *= damp[r];
 }
 
+/* InterpolateNewVectorsByMatrix, transgrid.cc:1425-1490: every fine vector
+ * with VNEW set takes the product of its interpolation-matrix row with the
+ * coarse vector.  One component per vector (the scalar descriptor branch,
+ * 1436-1453): only vectors with VECSKIP 0, each entry added to x directly.
+ * Blocks (1456-1488): VECSKIP not consulted, per entry the block's
+ * transposed product (m[j s + i], as InterpolateCorrectionByMatrix) summed
+ * into one value and then added.  The other fine vectors keep theirs. */
+void orc_interpolate_new_imat(const orc_level *fine, const orc_imat *M, const int *vnew, double *x_fine,
+                              const double *x_coarse) {
+  const int s = fine->s, ss = s * s;
+  for (int f = 0; f < fine->n; ++f) {
+    if (!vnew[f]) continue;
+    double *v = x_fine + (size_t)f * s;
+    if (s == 1) {
+      if (fine->skip[f]) continue;
+      v[0] = 0.0;
+      for (int k = M->rowptr[f]; k < M->rowptr[f + 1]; ++k) v[0] += M->val[k] * x_coarse[M->col[k]];
+      continue;
+    }
+    for (int i = 0; i < s; ++i) v[i] = 0.0;
+    for (int k = M->rowptr[f]; k < M->rowptr[f + 1]; ++k) {
+      const double *m = M->val + (size_t)k * ss, *w = x_coarse + (size_t)M->col[k] * s;
+      for (int i = 0; i < s; ++i) {
+        double sum = 0.0;
+        for (int j = 0; j < s; ++j) sum += m[j * s + i] * w[j];
+        v[i] += sum;
+      }
+    }
+  }
+}
+
 /* StandardIntNewNodeVector, np/algebra/transgrid.cc:354-430: every fine
  * vector with VNEW set takes the coarse values through its transfer row (a
  * corner copy, or the father element's shape functions GNs), every

@@ -86,7 +86,11 @@ void orc_project(const orc_level *fine, double *x_coarse, const double *x_fine);
 void orc_restrict_imat(const orc_level *fine, const orc_imat *M, const orc_level *coarse, double *to_coarse,
                        const double *from_fine, const double *damp);              /* RestrictByMatrix */
 void orc_interpolate_imat(const orc_level *fine, const orc_imat *M, double *to_fine, const double *from_coarse,
-                          const double *damp);                                    /* InterpolateCorrectionByMatrix */
+                          const double *damp);
+/* InterpolateNewVectorsByMatrix (transgrid.cc:1425): the VNEW fine vectors
+ * from the coarse level through the interpolation matrix */
+void orc_interpolate_new_imat(const orc_level *fine, const orc_imat *M, const int *vnew, double *x_fine,
+                              const double *x_coarse);                                    /* InterpolateCorrectionByMatrix */
 
 /* ---- solver ----
  * Solves A x = b on level top = nlevels-1 with ls + lmgc.  x (finest, n*s)

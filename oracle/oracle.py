@@ -94,6 +94,7 @@ def lib():
         L.orc_restrict.argtypes = [P, P, P, P, P]
         L.orc_interpolate.argtypes = [P, P, P, P]
         L.orc_interpolate_new.argtypes = [P, P, P, P]
+        L.orc_interpolate_new_imat.argtypes = [P, P, P, P, P]
         L.orc_project.argtypes = [P, P, P]
         L.orc_restrict_imat.argtypes = [P, P, P, P, P, P]
         L.orc_interpolate_imat.argtypes = [P, P, P, P, P]
@@ -281,10 +282,16 @@ class Hierarchy:
         return to
 
     def interpolate_new(self, l, vnew, x_fine, x_coarse):
-        """StandardIntNewNodeVector: fine vectors with VNEW take P x_coarse."""
+        """StandardIntNewNodeVector: fine vectors with VNEW take P x_coarse;
+        with interpolation matrices (the transfer's `$M` mode)
+        InterpolateNewVectorsByMatrix instead."""
         xf = np.array(x_fine, np.float64); xc = np.ascontiguousarray(x_coarse, np.float64)
         vn = np.ascontiguousarray(vnew, np.int32)
-        lib().orc_interpolate_new(self.lev(l), _p(vn), _p(xf), _p(xc)); return xf
+        if self.imat is not None:
+            lib().orc_interpolate_new_imat(self.lev(l), C.byref(self._ci[l]), _p(vn), _p(xf), _p(xc))
+        else:
+            lib().orc_interpolate_new(self.lev(l), _p(vn), _p(xf), _p(xc))
+        return xf
 
     def project(self, l, x_coarse, x_fine):
         """StandardProject: coarse vectors with a son node take its values."""

@@ -12,6 +12,8 @@ the identity, uniform and locally refined hierarchies).
   same iterations and solution to 1e-8);
 * the FP32 V-cycle in FP64 refinement with the matrix-mode transfer meets the
   FP64 stopping test;
+* InterpolateNewVectors in the matrix mode (InterpolateNewVectorsByMatrix,
+  transgrid.cc:1425) over every level: UG's values bit for bit;
 * errors: the matrix mode without interpolation matrices, and $R (not
   implemented) leaving the numproc not active."""
 import numpy as np
@@ -97,6 +99,25 @@ def test_matrix_transfer_mixed_precision(G, oracle_mod, name):
     top = len(H.levels) - 1
     d = H.matmul_minus(top, fx["rhs"], x)
     assert np.all(H.nrm2x(top, d) <= 1.0000001e-8 * H.nrm2x(top, fx["rhs"]))
+    mg.close()
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+@pytest.mark.parametrize("name", IMAT)
+def test_matrix_mode_new_vectors_match_ug(G, name, order):
+    fx = load_golden(name)
+    mg = _mg(G, fx, order=order)
+    mg.createvector("x")
+    mg.npcreate("tr", "transfer.gtransfer")
+    mg.npinit("tr", "$M")
+    n = mg.nlevels
+    offs = np.cumsum([0] + mg.level_len)
+    for l in range(n):
+        mg.set_new_vectors(l, fx[f"L{l}_vnew"])
+        mg.upload("x", l, fx["kat_newvec_pre"][offs[l]:offs[l + 1]])
+    mg.transfer_interpolate_new_vectors("tr", 0, n - 1, "x")
+    got = np.concatenate([mg.download("x", l) for l in range(n)])
+    assert np.array_equal(got, fx["kat_newvec"])
     mg.close()
 
 

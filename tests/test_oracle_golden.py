@@ -186,11 +186,15 @@ IMAT = golden_names("imat")
 def test_oracle_matrix_transfer_matches_ug(oracle_mod, name):
     """The transfer's matrix mode (`npinit transfer $M`): RestrictByMatrix and
     InterpolateCorrectionByMatrix on UG's interpolation matrices, plain and
-    damped, bit for bit, and UG's solves in that mode (iterations, defect
+    damped, bit for bit, InterpolateNewVectorsByMatrix over every level as
+    the `$M` transfer numproc runs it (transfer.cc:775 through its intnew,
+    transgrid.cc:1425), and UG's solves in that mode (iterations, defect
     history, solution), on uniform and locally refined hierarchies."""
     fx = load_golden(name)
     H = oracle_mod.Hierarchy.from_ugfx(fx)
     top = len(H.levels) - 1
+    vnew = [fx[f"L{l}_vnew"] for l in range(top + 1)]
+    assert np.array_equal(H.interpolate_new_vectors(0, top, fx["kat_newvec_pre"], vnew), fx["kat_newvec"])
     dm = [0.7 - 0.1 * i for i in range(8)]
     assert np.array_equal(H.restrict_imat(top, fx["kat_mrestrict_pre"], fx["kat_d"]), fx["kat_mrestrict"])
     assert np.array_equal(H.restrict_imat(top, fx["kat_mrestrict_damp_pre"], fx["kat_d"], dm),

@@ -396,6 +396,7 @@ int k_interpolate(gmg_mg *mg, const Level &fine, int prec, void *to, const void 
 int refresh_factors(gmg_mg *mg, int level);
 // StandardIntNewNodeVector: fine rows with F_VNEW take P x_coarse (every component)
 int k_interpolate_new(gmg_mg *mg, const Level &fine, int prec, void *x_fine, const void *x_coarse);
+int k_interpolate_new_imat(gmg_mg *mg, const Level &fine, int prec, void *x_fine, const void *x_coarse);
 // StandardProject: coarse rows with a son take the son's values
 int k_project(gmg_mg *mg, const Level &fine, const Level &coarse, int prec, void *x_coarse, const void *x_fine);
 // per-component 2-norms of the NEW_DEFECT rows into mg->norms_dev (device)

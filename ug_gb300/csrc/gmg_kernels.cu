@@ -3143,6 +3143,60 @@ int k_interpolate_new(gmg_mg *mg, const Level &F, int prec, void *xf, const void
   return 0;
 }
 
+// InterpolateNewVectorsByMatrix (transgrid.cc:1425-1490): VNEW fine vectors
+// take their interpolation-matrix row times the coarse vector, in double with
+// unfused products and sums in the row's entry order.  One component: rows
+// with a VECSKIP bit keep their value, each entry adds to x directly.
+// Blocks: VECSKIP not consulted, per entry the transposed block product
+// summed first, then added.
+template <class T, int S>
+__global__ void __launch_bounds__(BLK) interp_new_imat_kernel(int nf, const int *__restrict__ prow,
+                                                              const int *__restrict__ pcol,
+                                                              const double *__restrict__ pval,
+                                                              const uint8_t *__restrict__ flags,
+                                                              const uint8_t *__restrict__ skip, T *xf,
+                                                              const T *__restrict__ xc) {
+  pdl_prologue();
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    if (!(flags[f] & F_VNEW)) continue;
+    if (S == 1 && skip[f]) continue;
+    double v[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) v[i] = 0.0;
+    for (int k = prow[f]; k < prow[f + 1]; ++k) {
+      const double *m = pval + (size_t)k * S * S;
+      const T *w = xc + (size_t)pcol[k] * S;
+      if (S == 1) {
+        v[0] = __dadd_rn(v[0], __dmul_rn(m[0], double(w[0])));
+        continue;
+      }
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        double sum = 0.0;
+#pragma unroll
+        for (int j = 0; j < S; ++j) sum = __dadd_rn(sum, __dmul_rn(m[j * S + i], double(w[j])));
+        v[i] = __dadd_rn(v[i], sum);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < S; ++i) xf[(size_t)f * S + i] = T(v[i]);
+  }
+}
+
+int k_interpolate_new_imat(gmg_mg *mg, const Level &F, int prec, void *xf, const void *xc) {
+  GMG_CHECK(F.has_imat, "InterpolateNewVectorsByMatrix: no interpolation matrix on this level");
+  if (F.n == 0) return 0;
+#define NI(TT, SS) GMG_LAUNCH((interp_new_imat_kernel<TT, SS>), vec_grid(F.n), BLK, F.n, F.IP.rowptr, F.IP.col, \
+                              F.IP.v64, F.flags, F.skip, (TT *)xf, (const TT *)xc)
+  if (prec == GMG_PREC_FP64) { if (F.s == 1) NI(double, 1); else if (F.s == 2) NI(double, 2); else if (F.s == 3) NI(double, 3);
+                               else { set_error("block size %d not compiled", F.s); return 1; } }
+  else { if (F.s == 1) NI(float, 1); else if (F.s == 2) NI(float, 2); else if (F.s == 3) NI(float, 3);
+         else { set_error("block size %d not compiled", F.s); return 1; } }
+#undef NI
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_project(gmg_mg *mg, const Level &F, const Level &C, int prec, void *xc, const void *xf) {
   if (C.n == 0) return 0;
 #define PJ(TT, SS) GMG_LAUNCH((project_kernel<TT, SS>), vec_grid(C.n), BLK, C.n, F.son, (TT *)xc, (const TT *)xf)

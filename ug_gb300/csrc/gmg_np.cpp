@@ -611,12 +611,16 @@ int NPTransfer::InterpolateCorrection(int level, gmg_vec *to, gmg_vec *from, gmg
   return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), dmp, nullptr);
 }
 
-// InterpolateNewVectors, transfer.cc:775: StandardIntNewNodeVector on levels fl+1..tl
+// InterpolateNewVectors, transfer.cc:775: the transfer's intnew on levels
+// fl+1..tl -- StandardIntNewNodeVector, or InterpolateNewVectorsByMatrix
+// (transgrid.cc:1425) in the matrix mode
 int NPTransfer::InterpolateNewVectors(int fl, int tl, gmg_vec *xv, int *result) {
   GMG_CHECK(xv && fl >= 0 && tl < int(mg->lev.size()), "InterpolateNewVectors: bad arguments");
-  GMG_CHECK(!imat, "InterpolateNewVectors: the matrix mode (InterpolateNewVectorsByMatrix) is not implemented");
-  for (int l = fl + 1; l <= tl; ++l)
-    if (k_interpolate_new(mg, mg->lev[l], xv->prec, vlev(xv, l), vlev(xv, l - 1))) return 1;
+  for (int l = fl + 1; l <= tl; ++l) {
+    const int rc = imat ? k_interpolate_new_imat(mg, mg->lev[l], xv->prec, vlev(xv, l), vlev(xv, l - 1))
+                        : k_interpolate_new(mg, mg->lev[l], xv->prec, vlev(xv, l), vlev(xv, l - 1));
+    if (rc) return 1;
+  }
   return 0;
 }
 
