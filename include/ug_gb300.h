@@ -94,6 +94,11 @@ int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm);
 int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val);
 /* Number of multicolour classes (wavefronts of the gs/ilu schedule) on a level. */
 int gmg_mg_num_waves(const gmg_mg *mg, int level);
+/* The colouring GMG_ORDER_COLOR uses, on the host (no device needed):
+ * DSATUR on the symmetrised graph of the CSR pattern (rowptr[n+1], col),
+ * then a bounded, deterministic tabu search removing colours while it can.
+ * colour[i] in 0..*ncolours-1; adjacent rows never share a colour. */
+int gmg_colour_graph(int n, const int *rowptr, const int *col, int *colour, int *ncolours);
 /* Subdomain order (GMG_ORDER_DOMAIN) of a level: subdomains, interior rows
  * and interface colours (all 0 in the other orders). */
 int gmg_mg_domain_info(const gmg_mg *mg, int level, int *nsub, int *ninterior, int *ncolours);

@@ -98,7 +98,7 @@ def lib(build_if_missing: bool = True):
         "gmg_transfer_adapt_correction": ([P, I, P, P, P, P], I), "gmg_mg_set_new_vectors": ([P, I, P], I),
         "gmg_mg_update_values": ([P, I, P], I), "gmg_mg_level_variant": ([P, I, P, P, P], I),
     "gmg_mg_level_cta_chain": ([P, I, P], I), "gmg_mg_set_level_cta_chain": ([P, I, I], I),
-    "gmg_mg_domain_info": ([P, I, P, P, P], I),
+    "gmg_mg_domain_info": ([P, I, P, P, P], I), "gmg_colour_graph": ([I, P, P, P, P], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -153,6 +153,19 @@ def _sc(v, default=1.0):
         v = np.atleast_1d(np.asarray(v, np.float64))
         a[:] = np.resize(v, MAX_S)
     return a
+
+
+def colour_graph(rowptr, col):
+    """The multicolour order's colouring of a CSR pattern (gmg_colour_graph):
+    DSATUR, then tabu search for fewer colours.  Returns (colour, ncolours)."""
+    rp = np.ascontiguousarray(rowptr, np.int32)
+    cl = np.ascontiguousarray(col, np.int32)
+    n = len(rp) - 1
+    colour = np.empty(max(n, 1), np.int32)
+    nc = C.c_int()
+    if lib().gmg_colour_graph(n, _ptr(rp), _ptr(cl), _ptr(colour), C.byref(nc)):
+        _err("gmg_colour_graph")
+    return colour[:n], nc.value
 
 
 class Generator:

@@ -1565,6 +1565,24 @@ int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double
   return 0;
 }
 
+int gmg_colour_graph(int n, const int *rowptr, const int *col, int *colour, int *ncolours) {
+  if (n < 0 || (n > 0 && (!rowptr || !col || !colour)) || !ncolours) {
+    set_error("gmg_colour_graph: bad arguments");
+    return 1;
+  }
+  for (int i = 0; i < n; ++i)
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+      if (col[k] < 0 || col[k] >= n) {
+        set_error("gmg_colour_graph: row %d: column %d out of range", i, col[k]);
+        return 1;
+      }
+  int nc = 0;
+  const std::vector<int> c = colour_graph(n, sym_adjacency(n, rowptr, col), &nc);
+  std::copy(c.begin(), c.end(), colour);
+  *ncolours = nc;
+  return 0;
+}
+
 int gmg_mg_domain_info(const gmg_mg *mg, int level, int *nsub, int *ninterior, int *ncolours) {
   if (!mg || level < 0 || level >= (int)mg->lev.size() || !nsub || !ninterior || !ncolours) {
     set_error("gmg_mg_domain_info: bad arguments");
