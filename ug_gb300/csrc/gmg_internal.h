@@ -45,6 +45,11 @@ enum : uint8_t {
 
 // memcpy for large host buffers (several threads)
 void par_copy(void *dst, const void *src, size_t bytes);
+// host vector <-> stage_dev: `n` doubles from `host` into stage_dev + off
+// (queued on mg's stream; the host buffer may be reused on return), and
+// stage_dev + off into `host` (returns when the copy is complete)
+int stage_in(gmg_mg *mg, const double *host, size_t off, size_t n);
+int stage_out(gmg_mg *mg, double *host, size_t off, size_t n);
 
 // ---------------------------------------------------------------- device memory
 // The arrays of one level live in one allocation (the level's arena);
@@ -228,6 +233,10 @@ struct gmg_mg {
   void *stage_dev = nullptr;   // stage_len doubles
   double *stage_host = nullptr;// pinned, stage_len doubles
   size_t stage_len = 0;        // n_top*s (every level on a locally refined hierarchy)
+  // the device reads and writes pageable host memory through the host's page
+  // tables (Grace: NVLink-C2C): host vectors are copied straight from / to
+  // the caller's memory instead of through stage_host
+  bool direct_host = false;
   long long launches = 0;
   // bumped when device copies that captured iterations point into are
   // replaced (gmg_mg_update_values drops the fused coarse images): a CUDA

@@ -113,6 +113,32 @@ void par_copy(void *dst, const void *src, size_t bytes) {
   CopyPool::get().run(static_cast<char *>(dst), static_cast<const char *>(src), bytes, parts);
 }
 
+// Measured on GB300 with Grace (2.2 MB): pageable cudaMemcpyAsync 21-23 us
+// each way, through the pinned buffer (host memcpy + copy) 124-153 us.
+int stage_in(gmg_mg *mg, const double *host, size_t off, size_t n) {
+  double *dev = (double *)mg->stage_dev + off;
+  if (mg->direct_host) {
+    GMG_CUDA(cudaMemcpyAsync(dev, host, n * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+    return 0;
+  }
+  par_copy(mg->stage_host + off, host, n * sizeof(double));
+  GMG_CUDA(cudaMemcpyAsync(dev, mg->stage_host + off, n * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+  return 0;
+}
+
+int stage_out(gmg_mg *mg, double *host, size_t off, size_t n) {
+  const double *dev = (const double *)mg->stage_dev + off;
+  if (mg->direct_host) {
+    GMG_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+    GMG_CUDA(cudaStreamSynchronize(mg->stream));
+    return 0;
+  }
+  GMG_CUDA(cudaMemcpyAsync(mg->stage_host + off, dev, n * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
+  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  par_copy(host, mg->stage_host + off, n * sizeof(double));
+  return 0;
+}
+
 int Arena::alloc(size_t bytes) {
   size = bytes;
   used = 0;
@@ -1013,6 +1039,8 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return 1; }
   GMG_CUDA(cudaSetDevice(opts.device));
+  int pma_host_tables = 0;
+  GMG_CUDA(cudaDeviceGetAttribute(&pma_host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, opts.device));
   const int s = levels[0].s;
   std::vector<HostLevel> H(nlevels);
   for (int l = 0; l < nlevels; ++l) {
@@ -1022,6 +1050,7 @@ static int create_hierarchy(const gmg_level_desc *levels, int nlevels, const gmg
   }
   auto mg = std::make_unique<gmg_mg>();
   mg->device = opts.device;
+  mg->direct_host = pma_host_tables != 0;
   mg->opts = opts;
   // a stream of its own: the legacy default stream cannot be captured into graphs
   GMG_CUDA(cudaStreamCreateWithFlags(&mg->stream, cudaStreamNonBlocking));

@@ -1848,16 +1848,20 @@ gmg_mat *gmg_mat_by_name(gmg_mg *mg, const char *name) {
   return it == mg->mats.end() ? nullptr : it->second.get();
 }
 
-int gmg_vec_upload(gmg_vec *v, int level, const double *host) {
-  if (!v || !host) { set_error("gmg_vec_upload: bad arguments"); return 1; }
+// host -> level of v, queued on mg's stream (the host buffer is consumed on return)
+static int upload_async(gmg_vec *v, int level, const double *host) {
   gmg_mg *mg = v->mg;
   if (check_level(mg, level)) return 1;
   const Level &L = mg->lev[level];
   const size_t len = size_t(L.n) * L.s;
-  par_copy(mg->stage_host, host, len * sizeof(double));
-  GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
-  if (k_gather(mg, v->prec, vlev(v, level), (const double *)mg->stage_dev, L.perm_dev, L.n, L.s)) return 1;
-  GMG_CUDA(cudaStreamSynchronize(mg->stream));
+  if (stage_in(mg, host, 0, len)) return 1;
+  return k_gather(mg, v->prec, vlev(v, level), (const double *)mg->stage_dev, L.perm_dev, L.n, L.s);
+}
+
+int gmg_vec_upload(gmg_vec *v, int level, const double *host) {
+  if (!v || !host) { set_error("gmg_vec_upload: bad arguments"); return 1; }
+  if (upload_async(v, level, host)) return 1;
+  GMG_CUDA(cudaStreamSynchronize(v->mg->stream));
   return 0;
 }
 
@@ -1868,10 +1872,7 @@ int gmg_vec_download(gmg_vec *v, int level, double *host) {
   const Level &L = mg->lev[level];
   const size_t len = size_t(L.n) * L.s;
   if (k_scatter(mg, v->prec, (double *)mg->stage_dev, vlev(v, level), L.perm_dev, L.n, L.s)) return 1;
-  GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, len * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
-  GMG_CUDA(cudaStreamSynchronize(mg->stream));
-  par_copy(host, mg->stage_host, len * sizeof(double));
-  return 0;
+  return stage_out(mg, host, 0, len);
 }
 
 int gmg_vec_device_ptr(gmg_vec *v, int level, void **ptr) {
@@ -2178,7 +2179,8 @@ int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double 
     for (int l = 0; l <= top; ++l)
       if (k_set(mg, ls->x->prec, vlev(ls->x, l), vlen(mg, l), 0.0)) return 1;
   } else {
-    if (gmg_vec_upload(ls->b, top, b_host)) return 1;
+    // queued: the solve runs on the same stream and the copy has consumed b_host
+    if (upload_async(ls->b, top, b_host)) return 1;
     if (k_set(mg, ls->x->prec, vlev(ls->x, top), vlen(mg, top), 0.0)) return 1;
   }
   if (ls->Defect(top, ls->x, ls->b, ls->A, &res)) return 1;
@@ -2195,8 +2197,7 @@ int gmg_vec_upload_levels(gmg_vec *v, const double *host) {
   size_t len = 0;
   for (const auto &L : mg->lev) len += size_t(L.n) * L.s;
   GMG_CHECK(mg->local(), "gmg_vec_upload_levels: not a locally refined hierarchy");
-  par_copy(mg->stage_host, host, len * sizeof(double));
-  GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+  if (stage_in(mg, host, 0, len)) return 1;
   size_t off = 0;
   for (int l = 0; l < int(mg->lev.size()); ++l) {
     const Level &L = mg->lev[l];
@@ -2217,10 +2218,7 @@ int gmg_vec_download_levels(gmg_vec *v, double *host) {
     if (k_scatter(mg, v->prec, (double *)mg->stage_dev + off, vlev(v, l), L.perm_dev, L.n, L.s)) return 1;
     off += size_t(L.n) * L.s;
   }
-  GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, off * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
-  GMG_CUDA(cudaStreamSynchronize(mg->stream));
-  par_copy(host, mg->stage_host, off * sizeof(double));
-  return 0;
+  return stage_out(mg, host, 0, off);
 }
 
 int gmg_mg_full_refine_level(const gmg_mg *mg) { return mg ? mg->frl : -1; }
@@ -2234,8 +2232,7 @@ int gmg_vec_upload_packed(gmg_vec *v, const double *host) {
   gmg_mg *mg = v->mg;
   GMG_CHECK(mg->batch.ninst > 0, "gmg_vec_upload_packed: not a batched hierarchy");
   const size_t len = size_t(packed_len(mg));
-  par_copy(mg->stage_host, host, len * sizeof(double));
-  GMG_CUDA(cudaMemcpyAsync(mg->stage_dev, mg->stage_host, len * sizeof(double), cudaMemcpyHostToDevice, mg->stream));
+  if (stage_in(mg, host, 0, len)) return 1;
   for (const auto &tl : mg->batch.tops)
     if (k_pack_gather(mg, v->prec, vlev(v, tl.level), (const double *)mg->stage_dev, tl, mg->lev[0].s)) return 1;
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
@@ -2249,10 +2246,7 @@ int gmg_vec_download_packed(gmg_vec *v, double *host) {
   const size_t len = size_t(packed_len(mg));
   for (const auto &tl : mg->batch.tops)
     if (k_pack_scatter(mg, v->prec, (double *)mg->stage_dev, vlev(v, tl.level), tl, mg->lev[0].s)) return 1;
-  GMG_CUDA(cudaMemcpyAsync(mg->stage_host, mg->stage_dev, len * sizeof(double), cudaMemcpyDeviceToHost, mg->stream));
-  GMG_CUDA(cudaStreamSynchronize(mg->stream));
-  par_copy(host, mg->stage_host, len * sizeof(double));
-  return 0;
+  return stage_out(mg, host, 0, len);
 }
 
 int gmg_ls_instance_result(gmg_np *np, int k, gmg_lresult *lr) {

@@ -384,10 +384,7 @@ int gmg_pool_fetch(gmg_pool *p, int k, double *x_host, gmg_lresult *lr) {
                              tl->rows_dev + ptr[kl], tl->pack_dev + ptr[kl], n, s))
       return 1;
     const size_t o = size_t(B.pack_off[k]) * s;
-    GMG_CUDA(cudaMemcpyAsync(mg->stage_host + o, (double *)mg->stage_dev + o, sizeof(double) * n * s,
-                             cudaMemcpyDeviceToHost, mg->stream));
-    GMG_CUDA(cudaStreamSynchronize(mg->stream));
-    par_copy(x_host, mg->stage_host + o, sizeof(double) * n * s);
+    if (stage_out(mg, x_host, o, size_t(n) * s)) return 1;
   }
   if (lr) {
     *lr = gmg_lresult{};
