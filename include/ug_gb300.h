@@ -94,6 +94,13 @@ int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm);
 int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val);
 /* Number of multicolour classes (wavefronts of the gs/ilu schedule) on a level. */
 int gmg_mg_num_waves(const gmg_mg *mg, int level);
+/* Interface sweeps of the subdomain order (ILU in GMG_ORDER_DOMAIN): all
+ * interface colours of a direction in one cooperative launch, rows waiting
+ * on their earlier-colour neighbours' completion flags, or one launch per
+ * colour.  mode 0: per colour; 1 (default): one launch for FP64 sweeps, per
+ * colour for FP32 ones (faster there); 2: one launch for both.
+ * Bit-identical; set before the first graph-captured solve. */
+int gmg_mg_set_iface_sweep(gmg_mg *mg, int mode);
 /* The colouring GMG_ORDER_COLOR uses, on the host (no device needed):
  * DSATUR on the symmetrised graph of the CSR pattern (rowptr[n+1], col),
  * then a bounded, deterministic tabu search removing colours while it can.

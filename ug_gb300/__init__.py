@@ -99,6 +99,7 @@ def lib(build_if_missing: bool = True):
         "gmg_mg_update_values": ([P, I, P], I), "gmg_mg_level_variant": ([P, I, P, P, P], I),
     "gmg_mg_level_cta_chain": ([P, I, P], I), "gmg_mg_set_level_cta_chain": ([P, I, I], I),
     "gmg_mg_domain_info": ([P, I, P, P, P], I), "gmg_colour_graph": ([I, P, P, P, P], I),
+    "gmg_mg_set_iface_sweep": ([P, I], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -682,6 +683,13 @@ class MultiGrid:
         if lib().gmg_mg_domain_info(self._h, level, C.byref(a), C.byref(b), C.byref(c)):
             _err("domain_info")
         return {"subdomains": a.value, "interior_rows": b.value, "interface_colours": c.value}
+
+    def set_iface_sweep(self, mode: int):
+        """Interface ILU sweeps of the subdomain order: 0 one launch per
+        colour, 1 (default) one cooperative launch per direction for FP64
+        sweeps, 2 for FP32 sweeps as well."""
+        if lib().gmg_mg_set_iface_sweep(self._h, int(mode)):
+            _err("set_iface_sweep")
 
     def set_cta_chain(self, level: int, on: bool):
         """Run the level's chained Gauss-Seidel steps in one thread block (on)

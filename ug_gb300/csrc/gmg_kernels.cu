@@ -949,6 +949,118 @@ __global__ void __launch_bounds__(BLK) ilu_fwd_kernel(const int *__restrict__ ro
   }
 }
 
+// The interface part of the ILU solve in subdomain order, all colours of one
+// direction in ONE cooperative launch.  Items are the interface rows colour
+// after colour (forward 0..nc-1, backward nc-2..0), each colour padded to
+// whole warps, TPR threads per row, grid-stride; a thread's rows never go
+// back in colour, and no warp holds two colours.  A row whose factor entry
+// points at an interface row solved in this launch waits for that row's
+// completion flag (acquire; the writer stores t, then the flag with release
+// semantics), reading t through L2.  Flags hold the launch's epoch + 1: the
+// last block to finish advances the epoch, so flags are never reset.  Every
+// row does ilu_fwd_kernel's / ilu_bwd_kernel's arithmetic in the same order
+// (bit-identical).  A wait gives up after a bounded number of polls: the
+// row's result becomes NaN (the ls loop's non-finite test then fails the
+// solve) and *err is set.
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+constexpr int IFACE_MAX_POLLS = 1 << 16;
+
+template <class T, int S, int TPR, bool ALL_ACTIVE, bool FWD>
+__global__ void __launch_bounds__(BLK) ilu_iface_kernel(const int *__restrict__ items, int nitems, int nint,
+                                                        int last_lo, const int *__restrict__ rowptr,
+                                                        const int *__restrict__ col, const T *__restrict__ val,
+                                                        const T *__restrict__ dinv, const uint8_t *__restrict__ flags,
+                                                        const T *__restrict__ b, T *__restrict__ t,
+                                                        unsigned *__restrict__ done, unsigned *__restrict__ ctr,
+                                                        int *__restrict__ err) {
+  const unsigned target = *(volatile unsigned *)ctr + 1u;
+  const long long total = (long long)nitems * TPR, stride = (long long)gridDim.x * blockDim.x;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += stride) {
+    const int q = int(g / TPR), lane = int(g & (TPR - 1));
+    const int row = __ldg(items + q);
+    const bool valid = row >= 0;
+    const bool active = valid && (ALL_ACTIVE || (flags[row] & F_ACTIVE));
+    bool ok = true;
+    T s[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) s[r] = T(0);
+    if (active) {
+      const int k1 = __ldg(rowptr + row + 1);
+      for (int k = __ldg(rowptr + row) + lane; k < k1; k += TPR) {
+        const int j = __ldg(col + k);
+        if (FWD ? j >= nint : j < last_lo) {  // solved in this launch
+          int it = 0;
+          while (ld_acquire_u32(done + (j - nint)) != target && ++it < IFACE_MAX_POLLS) __nanosleep(32);
+          if (it >= IFACE_MAX_POLLS) ok = false;
+        }
+        const T *m = val + (size_t)k * (S * S);
+        T yv[S];
+#pragma unroll
+        for (int c = 0; c < S; ++c) yv[c] = __ldcg(t + (size_t)j * S + c);
+#pragma unroll
+        for (int r = 0; r < S; ++r)
+#pragma unroll
+          for (int c = 0; c < S; ++c) s[r] = fma(__ldg(m + r * S + c), yv[c], s[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < S; ++r) s[r] = group_sum<TPR>(s[r]);
+    ok = __all_sync(0xffffffffu, ok) != 0;  // the row group's lanes (whole warp: one colour)
+    if (valid && lane == 0) {
+      if (!ok) {
+        atomicExch(err, 1);
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = T(NAN);
+      }
+      if (FWD) {
+        if (row >= last_lo && active) {  // the last colour: no upper entries, backward step at once
+          T rhs[S];
+#pragma unroll
+          for (int r = 0; r < S; ++r) rhs[r] = b[(size_t)row * S + r] - s[r];
+#pragma unroll
+          for (int r = 0; r < S; ++r) {
+            T v = T(0);
+#pragma unroll
+            for (int c = 0; c < S; ++c) v = fma(__ldg(dinv + (size_t)row * S * S + r * S + c), rhs[c], v);
+            t[(size_t)row * S + r] = v;
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < S; ++r) t[(size_t)row * S + r] = active ? b[(size_t)row * S + r] - s[r] : T(0);
+        }
+      } else if (active) {
+        T rhs[S];
+#pragma unroll
+        for (int r = 0; r < S; ++r) rhs[r] = __ldcg(t + (size_t)row * S + r) - s[r];
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+          T v = T(0);
+#pragma unroll
+          for (int c = 0; c < S; ++c) v = fma(__ldg(dinv + (size_t)row * S * S + r * S + c), rhs[c], v);
+          t[(size_t)row * S + r] = v;
+        }
+      }
+      st_release_u32(done + (row - nint), target);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(ctr + 1, 1u) == gridDim.x - 1) {
+      ctr[1] = 0;
+      __threadfence();
+      atomicAdd(ctr, 1u);
+    }
+  }
+}
+
 template <class T, int S, int TPR, bool ALL_ACTIVE>
 __global__ void __launch_bounds__(BLK) ilu_bwd_kernel(const int *__restrict__ rows, int nrows,
                                                       const int *__restrict__ rowptr, const int *__restrict__ col,
@@ -2094,6 +2206,39 @@ int gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
   return 0;
 }
 
+// one cooperative launch of ilu_iface_kernel (grid: every block resident)
+template <class T, int S, int TPR, bool ALL, bool FWD>
+int iface_launch(gmg_mg *mg, const Level &L, const T *val, const T *dinv, T *t, const T *b) {
+  auto kern = ilu_iface_kernel<T, S, TPR, ALL, FWD>;
+  static thread_local std::map<void *, int> max_grid;
+  int &mgrid = max_grid[(void *)kern];
+  if (mgrid == 0) {
+    int per_sm = 0, nsm = 0, dev = 0;
+    GMG_CUDA(cudaGetDevice(&dev));
+    GMG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    GMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLK, 0));
+    mgrid = std::max(1, per_sm * nsm);
+  }
+  const int nitems = FWD ? L.iface_fw_n : L.iface_bw_n;
+  const long long need = ((long long)nitems * TPR + BLK - 1) / BLK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(std::max<long long>(1, std::min<long long>(need, mgrid))));
+  cfg.blockDim = dim3(BLK);
+  cfg.stream = mg->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const int nc = int(L.dom_cptr.size()) - 1;
+  cudaLaunchKernelEx(&cfg, kern, (const int *)(FWD ? L.iface_fw_items : L.iface_bw_items), nitems, L.dom_nint,
+                     L.dom_cptr[nc - 1], (const int *)(FWD ? L.L.rowptr : L.U.rowptr),
+                     (const int *)(FWD ? L.L.col : L.U.col), val, dinv, (const uint8_t *)L.flags, b, t,
+                     L.iface_flags + (FWD ? 0 : (L.n - L.dom_nint)), L.iface_ctr + (FWD ? 0 : 2), L.iface_err);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 // the ILU solve in subdomain order: interiors (one block per subdomain), the
 // interface colours forward; the interface colours backward, interiors
 template <class T, int S, int TPR, bool ALL>
@@ -2110,6 +2255,11 @@ int ilu_domain(gmg_mg *mg, const Level &L, T *t, const T *b) {
     GMG_LAUNCH((ilu_region_kernel<T, S, TPR, ALL, true>), L.dom_nreg, REGION_BLK, L.dom_fwbeg, L.dom_fwptr,
                L.dom_frows, L.L.rowptr, L.L.col, lv, (const T *)nullptr, L.flags, b, t);
   LAUNCH_CHECK(mg);
+  if (L.iface_coop && (mg->iface_sweep == 2 || (mg->iface_sweep == 1 && sizeof(T) == 8))) {
+    if (iface_launch<T, S, TPR, ALL, true>(mg, L, lv, ud, t, b) ||
+        iface_launch<T, S, TPR, ALL, false>(mg, L, uv, ud, t, (const T *)nullptr))
+      return 1;
+  } else {
   // the last colour's rows have no upper entries: its forward and backward
   // steps are one launch
   for (int c = 0; c < nc; ++c) {
@@ -2129,6 +2279,7 @@ int ilu_domain(gmg_mg *mg, const Level &L, T *t, const T *b) {
     GMG_LAUNCH((ilu_bwd_kernel<T, S, TPR, ALL>), grid_for((long long)nr * TPR), BLK, L.dom_iface + (r0 - L.dom_nint),
                nr, L.U.rowptr, L.U.col, uv, ud, L.flags, t);
     LAUNCH_CHECK(mg);
+  }
   }
   if (smem)
     pdl_launch_smem(mg, ilu_region_smem_kernel<T, S, ALL, false>, dim3(L.dom_nreg), dim3(REGION_BLK), bsm,

@@ -981,6 +981,32 @@ static int upload_level(HostLevel &h, int nc, bool f32, Level &L) {
         put(&L.dom_bwbeg, h.dom_bwbeg) || put(&L.dom_bwptr, h.dom_bwptr) || put(&L.dom_brows, h.dom_brows) ||
         put(&L.dom_iface, iface))
       return 1;
+    // the interface sweeps in one launch per direction: colours padded to
+    // multiples of 8 rows (whole warps at 4 or 8 threads per row)
+    const int nc = int(h.dom_cptr.size()) - 1;
+    if (nc >= 2) {
+      std::vector<int> fw, bw;
+      auto add = [](std::vector<int> &v, int r0, int r1) {
+        for (int r = r0; r < r1; ++r) v.push_back(r);
+        while (v.size() % 8) v.push_back(-1);
+      };
+      for (int c = 0; c < nc; ++c) add(fw, h.dom_cptr[c], h.dom_cptr[c + 1]);
+      for (int c = nc - 2; c >= 0; --c) add(bw, h.dom_cptr[c], h.dom_cptr[c + 1]);
+      L.iface_fw_n = int(fw.size());
+      L.iface_bw_n = int(bw.size());
+      const size_t ni = size_t(h.n - h.dom_nint);
+      if (put(&L.iface_fw_items, fw) || put(&L.iface_bw_items, bw)) return 1;
+      GMG_CUDA(cudaMalloc(&L.iface_flags, sizeof(unsigned) * 2 * std::max<size_t>(ni, 1)));
+      L.own.push_back(L.iface_flags);
+      GMG_CUDA(cudaMemset(L.iface_flags, 0, sizeof(unsigned) * 2 * std::max<size_t>(ni, 1)));
+      GMG_CUDA(cudaMalloc(&L.iface_ctr, sizeof(unsigned) * 4));
+      L.own.push_back(L.iface_ctr);
+      GMG_CUDA(cudaMemset(L.iface_ctr, 0, sizeof(unsigned) * 4));
+      GMG_CUDA(cudaMalloc(&L.iface_err, sizeof(int)));
+      L.own.push_back(L.iface_err);
+      GMG_CUDA(cudaMemset(L.iface_err, 0, sizeof(int)));
+      L.iface_coop = true;
+    }
   }
   // keep host copies for the ILU / base factorisations and for export
   L.perm = std::move(h.perm);
@@ -1591,6 +1617,15 @@ int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double
   if (rowptr) std::copy(L.h_rowptr.begin(), L.h_rowptr.end(), rowptr);
   if (col) std::copy(L.h_col.begin(), L.h_col.end(), col);
   if (val) std::copy(L.h_val.begin(), L.h_val.end(), val);
+  return 0;
+}
+
+int gmg_mg_set_iface_sweep(gmg_mg *mg, int mode) {
+  if (!mg || mode < 0 || mode > 2) {
+    set_error("gmg_mg_set_iface_sweep: bad arguments");
+    return 1;
+  }
+  mg->iface_sweep = mode;
   return 0;
 }
 
