@@ -94,6 +94,11 @@ int gmg_mg_get_order(const gmg_mg *mg, int level, int *perm);
 int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double *val);
 /* Number of multicolour classes (wavefronts of the gs/ilu schedule) on a level. */
 int gmg_mg_num_waves(const gmg_mg *mg, int level);
+/* Host vectors (uploads, downloads, gmg_solve_host): 1 = copied straight
+ * from / to the caller's pageable memory, the default where the device reads
+ * host memory through the host's page tables (Grace); 0 = through a pinned
+ * staging buffer, the default elsewhere.  Same results. */
+int gmg_mg_set_direct_host(gmg_mg *mg, int on);
 /* Interface sweeps of the subdomain order (ILU in GMG_ORDER_DOMAIN): all
  * interface colours of a direction in one cooperative launch, rows waiting
  * on their earlier-colour neighbours' completion flags, or one launch per

@@ -420,3 +420,32 @@ def test_blas_level_operations(G, name):
     mg.upload("x", top, x0)
     assert abs(mg.ddot(top, "x", "y") - float(x0 @ y)) <= 1e-12 * np.sum(np.abs(x0 * y))
     mg.close()
+
+
+def test_host_copy_paths_agree(G):
+    """Host vectors through pinned staging (the path of hosts whose GPU cannot
+    read pageable memory) and, where the device reads host page tables,
+    straight from / to pageable memory: the same solution and iterations,
+    bit for bit, through gmg_solve_host and the per-level upload / download."""
+    fx = load_golden("p1k_jac")
+    levels = G.levels_from_ugfx(fx)
+    out = []
+    for direct in (False, True):
+        mg = G.MultiGrid(levels, order=1)
+        try:
+            mg.set_direct_host(direct)
+        except G.GmgError:
+            mg.close()
+            assert direct  # only the direct path can be unavailable
+            continue
+        G.setup_lmgc(mg, "jac", baselevel=0, damp=0.8, red=1e-10)
+        x, lr = mg.solve_host("mgs", fx["rhs"])
+        mg.createvector("v")
+        mg.upload("v", mg.top, fx["rhs"])
+        back = mg.download("v", mg.top)
+        out.append((x, lr.iters, back))
+        mg.close()
+    assert np.array_equal(out[0][2], fx["rhs"])
+    if len(out) == 2:
+        assert out[0][1] == out[1][1] and np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[1][2], fx["rhs"])

@@ -99,7 +99,7 @@ def lib(build_if_missing: bool = True):
         "gmg_mg_update_values": ([P, I, P], I), "gmg_mg_level_variant": ([P, I, P, P, P], I),
     "gmg_mg_level_cta_chain": ([P, I, P], I), "gmg_mg_set_level_cta_chain": ([P, I, I], I),
     "gmg_mg_domain_info": ([P, I, P, P, P], I), "gmg_colour_graph": ([I, P, P, P, P], I),
-    "gmg_mg_set_iface_sweep": ([P, I], I),
+    "gmg_mg_set_iface_sweep": ([P, I], I), "gmg_mg_set_direct_host": ([P, I], I),
         "gmg_ls_preprocess": ([P, I, P, P, P, P, P], I), "gmg_ls_defect": ([P, I, P, P, P, P], I),
         "gmg_ls_residuum": ([P, I, I, P, P, P, P], I), "gmg_ls_solver": ([P, I, P, P, P, P, P, P], I),
         "gmg_ls_postprocess": ([P, I, P, P, P, P], I),
@@ -683,6 +683,12 @@ class MultiGrid:
         if lib().gmg_mg_domain_info(self._h, level, C.byref(a), C.byref(b), C.byref(c)):
             _err("domain_info")
         return {"subdomains": a.value, "interior_rows": b.value, "interface_colours": c.value}
+
+    def set_direct_host(self, on: bool):
+        """Host vectors straight from / to pageable memory (True; needs a
+        device that reads host page tables) or through pinned staging."""
+        if lib().gmg_mg_set_direct_host(self._h, int(bool(on))):
+            _err("set_direct_host")
 
     def set_iface_sweep(self, mode: int):
         """Interface ILU sweeps of the subdomain order: 0 one launch per

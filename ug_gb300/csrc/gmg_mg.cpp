@@ -1620,6 +1620,20 @@ int gmg_mg_get_matrix(const gmg_mg *mg, int level, int *rowptr, int *col, double
   return 0;
 }
 
+int gmg_mg_set_direct_host(gmg_mg *mg, int on) {
+  if (!mg || (on != 0 && on != 1)) {
+    set_error("gmg_mg_set_direct_host: bad arguments");
+    return 1;
+  }
+  if (on) {
+    int v = 0;
+    GMG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, mg->device));
+    GMG_CHECK(v, "gmg_mg_set_direct_host: the device does not read pageable host memory through the host page tables");
+  }
+  mg->direct_host = on != 0;
+  return 0;
+}
+
 int gmg_mg_set_iface_sweep(gmg_mg *mg, int mode) {
   if (!mg || mode < 0 || mode > 2) {
     set_error("gmg_mg_set_iface_sweep: bad arguments");
