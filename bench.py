@@ -610,7 +610,7 @@ def run_serving(args, rank, mixed=(), extras=True):
     from ug_gb300.serve import Server, poisson_stream
     t0 = time.perf_counter()
     srv = Server(depths=range(SERVE_LEVELS[0], SERVE_LEVELS[1] + 1), device=torch.cuda.current_device(),
-                 mixed=mixed, grow_after_ms=50.0)
+                 mixed=mixed, grow_after_ms=None, mesh=gen_kind(G))
     srv.warm()  # every pool's temporaries and CUDA graph
     setup_s = time.perf_counter() - t0
     srv.run(poisson_stream(max(24, args.warmup * 12), SERVE_RATE, SERVE_LEVELS, seed=77))
@@ -670,7 +670,7 @@ def run_serving(args, rank, mixed=(), extras=True):
                 slot = p.free_slot(L)
                 x, lr = p.solve(r.seed, srv.corr, srv.var, slot=slot)
                 same_iters = same_iters and lr.iters == r.iters
-                levels, rhs, _ = oracle.cube_levels(L, r.seed, CORR, VAR)
+                levels, rhs, _ = oracle.cube_levels(L, r.seed, CORR, VAR, ug_rules=MESH == "ug")
                 xo, _, conv, _ = oracle.Hierarchy(levels).ls_solve(rhs, smoother="gs", baselevel=0, red=1e-12,
                                                                    abslimit=1e-50, base_abslimit=1e-30)
                 e_host.append(float(np.max(np.abs(x - xo)) / np.max(np.abs(xo))) if conv else float("nan"))
@@ -686,8 +686,8 @@ def run_serving(args, rank, mixed=(), extras=True):
     st.p50_ms, st.p99_ms, st.mean_ms = (reduce_over_ranks(v) for v in (st.p50_ms, st.p99_ms, st.mean_ms))
     st.throughput = reduce_over_ranks(st.throughput, "sum")
     out = {"workload": f"{args.serve_requests} requests, Poisson arrivals mean {SERVE_RATE:.0f}/s, 3D P1 cube "
-                       f"levels U{{{SERVE_LEVELS[0]}..{SERVE_LEVELS[1]}}} (125..2146689 unknowns), k=exp(g) corr 0.1 "
-                       f"var 1, FP32 GS V(2,2) in FP64 refinement to 1e-8",
+                       f"levels U{{{SERVE_LEVELS[0]}..{SERVE_LEVELS[1]}}} (125..2146689 unknowns, {MESHES[MESH]}), "
+                       f"k=exp(g) corr 0.1 var 1, FP32 GS V(2,2) in FP64 refinement to 1e-8",
            "requests": st.completed, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
            "throughput_req_s": st.throughput, "offered_req_s": SERVE_RATE, "makespan_s": st.makespan_s,
            "iterations_mean": st.iterations_mean, "all_converged": st.all_converged,
@@ -709,7 +709,7 @@ def run_serving(args, rank, mixed=(), extras=True):
             oracle.build()
             per = {}
             for L in range(SERVE_LEVELS[0], min(SERVE_LEVELS[1], 6) + 1):
-                gen = G.Generator(G.Generator.DIFFUSION3D, L, seed=31 + L, corr=CORR, var=VAR)
+                gen = G.Generator(gen_kind(G), L, seed=31 + L, corr=CORR, var=VAR)
                 H = oracle.Hierarchy(gen.levels())
                 t1 = time.perf_counter()
                 H.ls_solve(gen.rhs, smoother="gs", baselevel=0, red=RED)

@@ -287,8 +287,8 @@ int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev,
 /* Continuous batching of solves on resident hierarchies (no UG counterpart:
  * the request loop around UG's ls).  A pool holds `nslots` instances of one
  * cached topology -- the 3D diffusion workload's unit cube (six Kuhn
- * tetrahedra) refined `nref` times, the hierarchy gmg_gen_create(1, nref, ...)
- * builds -- as one batched hierarchy with an ls (FP32 lmgc V(2,2) with
+ * tetrahedra) refined `nref` (1..7) times by UG's red rules, the hierarchy
+ * gmg_gen_create(3, nref, ...) builds -- as one batched hierarchy with an ls (FP32 lmgc V(2,2) with
  * `smoother` "gs" (multicolour) or "jac", base level 0, inside FP64
  * iterative refinement to `red`, at most `maxit` iterations).  A request is
  * admitted into a free slot by assembling its coefficient k = exp(g) (seed,
@@ -302,12 +302,17 @@ int gmg_nrm2x_static(const double *x_dev, long long n, int s, double *norms_dev,
 typedef struct gmg_pool gmg_pool;
 int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int maxit, int device, gmg_pool **out);
 /* A pool whose slots hold cubes of different depths (slot k refined
- * depths[k] times, 1..9): one batched hierarchy whose level l holds level l
+ * depths[k] times, 1..7): one batched hierarchy whose level l holds level l
  * of every slot that reaches it, so one ls iteration of the pool runs the
  * V-cycles of requests of different mesh sizes together, level by level
  * (each request still iterates and converges on its own). */
 int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, double red, int maxit, int device,
                           gmg_pool **out);
+/* Either of the above on a chosen mesh: `mesh` 3 = UG's red rules (what
+ * gmg_pool_create / _mixed build), 1 = the Freudenthal triangulation
+ * (gmg_gen_create kind 1, depths 1..9). */
+int gmg_pool_create_mesh(int mesh, const int *depths, int nslots, const char *smoother, double red, int maxit,
+                         int device, gmg_pool **out);
 int gmg_pool_destroy(gmg_pool *pool);
 gmg_mg *gmg_pool_multigrid(gmg_pool *pool);
 int gmg_pool_set_stream(gmg_pool *pool, void *stream);

@@ -1,7 +1,9 @@
 """Serving pools and the continuous-batching loop (ug_gb300/serve.py,
 ug_gb300/csrc/gmg_serve.cpp, gmg_assemble.cu).
 
-* On-device assembly reproduces the host generator's matrices: exactly up to
+* On-device assembly reproduces the host generator's matrices, on both
+  cube meshes (UG's red rules, the pools' default, and the Freudenthal
+  triangulation): exactly up to
   rounding (1e-13 relative) for k = 1, and to 1e-12 relative with the
   log-normal field evaluated in FP64 (the pools' default), so a slot holds
   the FP64 problem; with the optional FP32 field (phases in 32-bit fixed
@@ -40,15 +42,16 @@ def test_stream_is_seeded(G):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mesh", [3, 1], ids=["ug_red_rules", "freudenthal"])
 @pytest.mark.parametrize("var,fp64,tol", [(0.0, True, 1e-13), (1.0, True, 1e-12), (1.0, False, 2e-5)])
 @pytest.mark.parametrize("nref", [3, 5])
-def test_device_assembly_matches_generator(G, var, fp64, tol, nref):
+def test_device_assembly_matches_generator(G, var, fp64, tol, nref, mesh):
     from ug_gb300.serve import Pool
     seed = 77
-    pool = Pool(nref, 2, field_fp64=fp64)
+    pool = Pool(nref, 2, field_fp64=fp64, mesh=mesh)
     pool.free.remove(1)
     pool.admit(1, seed, 0.1, var)
-    gen = G.Generator(G.Generator.DIFFUSION3D, nref, seed=seed, corr=0.1, var=var)
+    gen = G.Generator(mesh, nref, seed=seed, corr=0.1, var=var)
     for l in range(nref + 1):
         ref = gen.level(l)["val"]
         got = pool.slot_matrix(1, l, ref.size)
@@ -61,8 +64,8 @@ def test_device_assembly_matches_generator(G, var, fp64, tol, nref):
     pool.close()
 
 
-def _mixed_solo(G, nref, seed, var):
-    gen = G.Generator(G.Generator.DIFFUSION3D, nref, seed=seed, corr=0.1, var=var)
+def _mixed_solo(G, nref, seed, var, mesh=3):
+    gen = G.Generator(mesh, nref, seed=seed, corr=0.1, var=var)
     mg = G.MultiGrid(gen, order=G.ORDER_COLOR, fp32=True)
     G.setup_lmgc(mg, "gs", red=1e-8, abslimit=1e-50, mixed=True)
     x, lr = mg.solve_host("mgs", gen.rhs)
@@ -114,7 +117,7 @@ def test_alone_equals_in_the_mix(G):
     # ... and its FP64 oracle solution
     import oracle
     oracle.build()
-    gen = G.Generator(G.Generator.DIFFUSION3D, nref, seed=seed, corr=0.1, var=1.0)
+    gen = G.Generator(G.Generator.DIFFUSION3D_UG, nref, seed=seed, corr=0.1, var=1.0)
     H = oracle.Hierarchy(gen.levels())
     xo, _, conv, _ = H.ls_solve(gen.rhs, smoother="gs", baselevel=0, red=1e-12, abslimit=1e-50, base_abslimit=1e-30)
     assert conv and rel(xm, xo) <= 1e-6

@@ -122,6 +122,7 @@ def lib(build_if_missing: bool = True):
         "gmg_pool_poll": ([P, P, P], I), "gmg_pool_fetch": ([P, I, P, P], I),
         "gmg_pool_slot_matrix": ([P, I, I, P], I), "gmg_pool_set_field_precision": ([P, I], I),
         "gmg_pool_create_mixed": ([P, I, C.c_char_p, D, I, I, P], I), "gmg_pool_slot_info": ([P, I, P, P], I),
+        "gmg_pool_create_mesh": ([I, P, I, C.c_char_p, D, I, I, P], I),
         "gmg_mg_full_refine_level": ([P], I), "gmg_vec_upload_levels": ([P, P], I),
         "gmg_vec_download_levels": ([P, P], I),
         "gmg_lgen_create": ([I, I, C.c_ulonglong, P], I), "gmg_lgen_levels": ([P, P, P], I),

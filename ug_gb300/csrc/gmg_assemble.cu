@@ -43,6 +43,21 @@ constexpr int ABLK = 256;
 __constant__ double c_kref[6][16];  // stiffness of the unit Kuhn tetrahedra (h = 1, k = 1)
 __constant__ int c_perm[6][3];      // the axis order of each tetrahedron's path from (0,0,0) to (1,1,1)
 
+// UG's red refinement (generator kind 3): the six tetrahedra of a lattice
+// cell differ from cell to cell and come as masks of the cell's corners (bit
+// dx | dy << 1 | dz << 2).  d_ug_shape[mask]: the stiffness of the unit
+// tetrahedron on those corners (vertices in ascending corner order, h = 1,
+// k = 1), its corners, and the code of its centroid in the cell: 4 delta_d
+// in 1..3 per axis, code (4 dx - 1) + 3 (4 dy - 1) + 9 (4 dz - 1).  Masks
+// that are no tetrahedron stay zero.
+struct UgShape {
+  double K[16];
+  int corner[4];
+  int dcode;
+};
+__device__ UgShape d_ug_shape[256];
+constexpr int UG_DCODES = 27;
+
 // the Kuhn tetrahedra of the unit cube: vertices 0, e_a, e_a + e_b, (1,1,1)
 const int kPerms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
@@ -92,6 +107,32 @@ int upload_constants(int device) {
   }
   GMG_CUDA(cudaMemcpyToSymbol(c_kref, K, sizeof K));
   GMG_CUDA(cudaMemcpyToSymbol(c_perm, kPerms, sizeof kPerms));
+  std::vector<UgShape> sh(256);
+  std::memset(sh.data(), 0, sizeof(UgShape) * 256);
+  for (int mask = 0; mask < 256; ++mask) {
+    if (__builtin_popcount(unsigned(mask)) != 4) continue;
+    double V[4][3];
+    int a = 0, sum[3] = {0, 0, 0};
+    for (int c = 0; c < 8; ++c) {
+      if (!((mask >> c) & 1)) continue;
+      sh[mask].corner[a] = c;
+      for (int d = 0; d < 3; ++d) {
+        V[a][d] = double((c >> d) & 1);
+        sum[d] += (c >> d) & 1;
+      }
+      ++a;
+    }
+    double J[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) J[r][c] = V[c + 1][r] - V[0][r];
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    if (det == 0.0) continue;  // four corners of one face
+    tet_stiffness(V, sh[mask].K);
+    sh[mask].dcode = (sum[0] - 1) + 3 * (sum[1] - 1) + 9 * (sum[2] - 1);
+  }
+  GMG_CUDA(cudaMemcpyToSymbol(d_ug_shape, sh.data(), sizeof(UgShape) * 256));
   if ((int)done.size() <= device) done.resize(device + 1, 0);
   done[device] = 1;
   return 0;
@@ -217,6 +258,157 @@ __global__ void __launch_bounds__(128) cube_field64_kernel(int Nc, int M, double
 }
 
 __device__ __forceinline__ int lattice_code(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
+
+// UG's mesh, FP32 field: as cube_field_kernel, with the offset of each
+// tetrahedron's centroid from its cell's origin looked up by its code (the
+// 27 offsets of every feature in shared memory)
+__global__ void __launch_bounds__(ABLK) ug_field_kernel(int Nc, const uint4 *__restrict__ prm, int M, float amp,
+                                                        const uint8_t *__restrict__ masks,
+                                                        float *__restrict__ kelem) {
+  extern __shared__ float2 sdu[];  // [M][27]: (cos, sin) of the centroid offsets
+  __shared__ uint4 sp[GMG_FIELD_MAX_M];
+  for (int q = threadIdx.x; q < M * UG_DCODES; q += blockDim.x) {
+    const int m = q / UG_DCODES, c = q % UG_DCODES;
+    const uint4 v = prm[m];
+    if (c == 0) sp[m] = v;
+    const uint32_t d = uint32_t(c % 3 + 1) * v.y + uint32_t((c / 3) % 3 + 1) * v.z + uint32_t(c / 9 + 1) * v.w;
+    float sn, cs;
+    sincospif(__uint2float_rn(d) * 4.656612873077392578125e-10f, &sn, &cs);
+    sdu[q] = make_float2(cs, sn);
+  }
+  __syncthreads();
+  const long long nc = (long long)Nc * Nc * Nc;
+  for (long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x; cell < nc;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const uint32_t cx = uint32_t(cell % Nc) * 4u, cy = uint32_t((cell / Nc) % Nc) * 4u,
+                   cz = uint32_t(cell / ((long long)Nc * Nc)) * 4u;
+    int code[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) code[t] = d_ug_shape[masks[cell * 6 + t]].dcode;
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int m = 0; m < M; ++m) {
+      const uint32_t ph = sp[m].x + cx * sp[m].y + cy * sp[m].z + cz * sp[m].w;
+      float s0, c0;
+      sincospif(__uint2float_rn(ph) * 4.656612873077392578125e-10f, &s0, &c0);
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        const float2 o = sdu[m * UG_DCODES + code[t]];
+        g[t] += c0 * o.x - s0 * o.y;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 6; ++t) kelem[cell * 6 + t] = expf(amp * g[t]);
+  }
+}
+
+// UG's mesh, FP64 field: V[m][code] = (cos, sin) of w_m.eps h, eps = delta -
+// 1/2 the centroid's offset from the cell centre (-1/4, 0 or 1/4 per axis)
+__global__ void __launch_bounds__(ABLK) ug_field64_offsets_kernel(double h, int M, const double *__restrict__ w,
+                                                                  double2 *__restrict__ V) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= M * UG_DCODES) return;
+  const int m = q / UG_DCODES, c = q % UG_DCODES;
+  const double ex = 0.25 * double(c % 3 - 1), ey = 0.25 * double((c / 3) % 3 - 1), ez = 0.25 * double(c / 9 - 1);
+  const double arg = h * (ex * w[m * 3] + ey * w[m * 3 + 1] + ez * w[m * 3 + 2]);
+  double sn, cs;
+  sincos(arg, &sn, &cs);
+  V[q] = make_double2(cs, sn);
+}
+
+// UG's mesh, FP64 field: one block per row (y, z) of cells; per cell and
+// feature E = e^{i a0} at the cell centre, then for each tetrahedron
+// cos(a0 + u) = Re E cos u - Im E sin u, u its centroid's offset phase
+__global__ void __launch_bounds__(128) ug_field64_kernel(int Nc, int M, double amp, const double2 *__restrict__ X,
+                                                         const double2 *__restrict__ Y, const double2 *__restrict__ ZP,
+                                                         const double2 *__restrict__ V,
+                                                         const uint8_t *__restrict__ masks,
+                                                         double *__restrict__ kelem) {
+  extern __shared__ double2 sV[];  // [M][27]
+  __shared__ double2 sYZ[GMG_FIELD_MAX_M];
+  const int row = blockIdx.x, j = row % Nc, k = row / Nc;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const double2 b = Y[(size_t)m * Nc + j], c = ZP[(size_t)m * Nc + k];
+    sYZ[m] = make_double2(b.x * c.x - b.y * c.y, b.x * c.y + b.y * c.x);
+  }
+  for (int q = threadIdx.x; q < M * UG_DCODES; q += blockDim.x) sV[q] = V[q];
+  __syncthreads();
+  for (int i = threadIdx.x; i < Nc; i += blockDim.x) {
+    const size_t cell = (size_t)row * Nc + i;
+    int code[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) code[t] = d_ug_shape[masks[cell * 6 + t]].dcode;
+    double S[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, D[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int m = 0; m < M; ++m) {
+      const double2 a = __ldg(X + (size_t)m * Nc + i), yz = sYZ[m];
+      const double er = fma(a.x, yz.x, -a.y * yz.y), ei = fma(a.x, yz.y, a.y * yz.x);
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        const double2 v = sV[m * UG_DCODES + code[t]];
+        S[t] = fma(er, v.x, S[t]);
+        D[t] = fma(ei, v.y, D[t]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 6; ++t) kelem[cell * 6 + t] = exp(amp * (S[t] - D[t]));
+  }
+}
+
+// UG's mesh: one slot's rows of one level, each row summing the tetrahedra
+// of its eight cells that contain its node (as cube_assemble_kernel; the
+// cells' tetrahedra come from their corner masks)
+template <class TK>
+__global__ void __launch_bounds__(ABLK) ug_assemble_kernel(
+    int nrows, const int *__restrict__ rows, const int *__restrict__ perm, int off, int N,
+    const int *__restrict__ rowptr, const int *__restrict__ col, const uint8_t *__restrict__ masks,
+    const TK *__restrict__ kelem, double h, double *__restrict__ v64, float *__restrict__ v32,
+    const int *__restrict__ c2s, double *__restrict__ sv64, float *__restrict__ sv32, double *__restrict__ dinv64,
+    float *__restrict__ dinv32) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrows) return;
+  const int i = rows[q], j = perm[i] - off;
+  const int x = j % N, y = (j / N) % N, z = j / (N * N);
+  const bool bnd = x == 0 || y == 0 || z == 0 || x == N - 1 || y == N - 1 || z == N - 1;
+  double acc[27];
+#pragma unroll
+  for (int t = 0; t < 27; ++t) acc[t] = 0.0;
+  if (!bnd) {
+    const int Nc = N - 1;
+    for (int cc = 0; cc < 8; ++cc) {  // the cells around the node; the node is their corner cc
+      const long long cell = ((long long)(z - ((cc >> 2) & 1)) * Nc + (y - ((cc >> 1) & 1))) * Nc + (x - (cc & 1));
+      for (int t = 0; t < 6; ++t) {
+        const int mask = masks[cell * 6 + t];
+        if (!((mask >> cc) & 1)) continue;
+        const UgShape &sh = d_ug_shape[mask];
+        const int m = __popc(unsigned(mask) & ((1u << cc) - 1u));
+        const double ke = kelem ? double(kelem[cell * 6 + t]) : 1.0;
+        for (int b = 0; b < 4; ++b) {
+          const int ct = sh.corner[b];
+          acc[lattice_code((ct & 1) - (cc & 1), ((ct >> 1) & 1) - ((cc >> 1) & 1), ((ct >> 2) & 1) - ((cc >> 2) & 1))] +=
+              ke * sh.K[m * 4 + b];
+        }
+      }
+    }
+  }
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    double v;
+    if (bnd) {
+      v = k == rowptr[i] ? 1.0 : 0.0;
+    } else {
+      const int jc = perm[col[k]] - off;
+      v = h * acc[lattice_code(jc % N - x, (jc / N) % N - y, jc / (N * N) - z)];
+    }
+    v64[k] = v;
+    v32[k] = float(v);
+    if (c2s) {
+      sv64[c2s[k]] = v;
+      sv32[c2s[k]] = float(v);
+    }
+    if (k == rowptr[i]) {
+      dinv64[i] = 1.0 / v;
+      dinv32[i] = float(1.0 / v);
+    }
+  }
+}
 
 // the Kuhn tetrahedra as compile-time functions (kPerms above), so that the
 // unrolled assembly loops index the row accumulators with constants
@@ -394,18 +586,38 @@ void cube_field_params(uint64_t seed, double corr, double var, int level, std::v
   *M = f.M;
 }
 
-int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem) {
+template <class KERN>
+static int allow_smem(KERN kern, int bytes) {
+  static std::mutex mu;
+  static std::vector<std::pair<void *, int>> set;
+  std::lock_guard<std::mutex> lk(mu);
+  for (auto &e : set)
+    if (e.first == (void *)kern && e.second >= bytes) return 0;
+  GMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  set.emplace_back((void *)kern, bytes);
+  return 0;
+}
+
+int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem,
+                 const uint8_t *masks) {
   GMG_CHECK(M <= GMG_FIELD_MAX_M, "field with %d features (at most %d)", M, GMG_FIELD_MAX_M);
   if (upload_constants(mg->device)) return 1;
   const long long nc = (long long)Nc * Nc * Nc;
   const unsigned g = unsigned(std::min<long long>((nc + ABLK - 1) / ABLK, 152LL * 8));
-  cube_field_kernel<<<g, ABLK, 0, mg->stream>>>(Nc, reinterpret_cast<const uint4 *>(prm_dev), M, amp, kelem);
+  if (masks) {
+    const int smem = M * UG_DCODES * int(sizeof(float2));
+    if (allow_smem(ug_field_kernel, smem)) return 1;
+    ug_field_kernel<<<g, ABLK, smem, mg->stream>>>(Nc, reinterpret_cast<const uint4 *>(prm_dev), M, amp, masks,
+                                                   kelem);
+  } else {
+    cube_field_kernel<<<g, ABLK, 0, mg->stream>>>(Nc, reinterpret_cast<const uint4 *>(prm_dev), M, amp, kelem);
+  }
   ACHECK(mg);
   return 0;
 }
 
 int k_cube_field64(gmg_mg *mg, int Nc, const double *w_dev, const double *phi_dev, int M, double amp,
-                   double2 *tables, double *kelem) {
+                   double2 *tables, double *kelem, const uint8_t *masks) {
   GMG_CHECK(M <= GMG_FIELD_MAX_M, "field with %d features (at most %d)", M, GMG_FIELD_MAX_M);
   if (upload_constants(mg->device)) return 1;
   double2 *X = tables, *Y = X + (size_t)M * Nc, *ZP = Y + (size_t)M * Nc, *U = ZP + (size_t)M * Nc;
@@ -414,7 +626,16 @@ int k_cube_field64(gmg_mg *mg, int Nc, const double *w_dev, const double *phi_de
                                                                     ZP, U);
   ACHECK(mg);
   const int bt = std::min(128, std::max(32, (Nc + 31) / 32 * 32));
-  cube_field64_kernel<<<unsigned(Nc) * unsigned(Nc), bt, 0, mg->stream>>>(Nc, M, amp, X, Y, ZP, U, kelem);
+  if (masks) {
+    double2 *V = U + (size_t)M * 3;  // M x 27
+    ug_field64_offsets_kernel<<<grid_of(M * UG_DCODES), ABLK, 0, mg->stream>>>(1.0 / double(Nc), M, w_dev, V);
+    ACHECK(mg);
+    const int smem = M * UG_DCODES * int(sizeof(double2));
+    if (allow_smem(ug_field64_kernel, smem)) return 1;
+    ug_field64_kernel<<<unsigned(Nc) * unsigned(Nc), bt, smem, mg->stream>>>(Nc, M, amp, X, Y, ZP, V, masks, kelem);
+  } else {
+    cube_field64_kernel<<<unsigned(Nc) * unsigned(Nc), bt, 0, mg->stream>>>(Nc, M, amp, X, Y, ZP, U, kelem);
+  }
   ACHECK(mg);
   return 0;
 }
@@ -423,9 +644,14 @@ template <class TK>
 static int assemble_t(gmg_mg *mg, const Level &L, const SlotLevel &sl, const TK *kelem, double h, const int *c2s) {
   GMG_CHECK(L.s == 1 && L.A.v32 && L.dinv32, "cube assembly: scalar level with FP32 copies expected");
   if (upload_constants(mg->device)) return 1;
-  cube_assemble_kernel<TK><<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(
-      sl.nrows, sl.rows, L.perm_dev, sl.off, sl.N, L.A.rowptr, L.A.col, kelem, h, L.A.v64, L.A.v32, c2s,
-      L.sell_v64, L.sell_v32, L.dinv64, L.dinv32);
+  if (sl.masks)
+    ug_assemble_kernel<TK><<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(
+        sl.nrows, sl.rows, L.perm_dev, sl.off, sl.N, L.A.rowptr, L.A.col, sl.masks, kelem, h, L.A.v64, L.A.v32,
+        c2s, L.sell_v64, L.sell_v32, L.dinv64, L.dinv32);
+  else
+    cube_assemble_kernel<TK><<<grid_of(sl.nrows), ABLK, 0, mg->stream>>>(
+        sl.nrows, sl.rows, L.perm_dev, sl.off, sl.N, L.A.rowptr, L.A.col, kelem, h, L.A.v64, L.A.v32, c2s,
+        L.sell_v64, L.sell_v32, L.dinv64, L.dinv32);
   ACHECK(mg);
   return 0;
 }

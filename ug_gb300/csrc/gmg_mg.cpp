@@ -354,6 +354,48 @@ static std::vector<int> colour_graph(int n, const std::vector<std::vector<int>> 
   return colour;
 }
 
+static std::vector<std::vector<int>> sym_adjacency(int n, const int *rowptr, const int *col);
+
+// colour_graph of a CSR pattern, remembered for the process: hierarchies of
+// one topology (the pools of a server, repeated creations) colour it once.
+// Keyed by n, nnz and a 64-bit hash of the pattern; a hit is used only after
+// checking that it is a proper colouring of this pattern.
+static std::vector<int> colour_pattern(int n, const int *rowptr, const int *col,
+                                       const std::vector<std::vector<int>> *adj, int *ncol) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, uint64_t>, std::pair<std::vector<int>, int>> cache;
+  const int nnz = n > 0 ? rowptr[n] : 0;
+  uint64_t h = 0x9e3779b97f4a7c15ull ^ uint64_t(n);
+  auto mix = [&](uint64_t v) {
+    h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    h *= 0xff51afd7ed558ccdull;
+    h ^= h >> 33;
+  };
+  for (int i = 0; i <= n; ++i) mix(uint64_t(uint32_t(rowptr[i])));
+  for (int k = 0; k < nnz; ++k) mix(uint64_t(uint32_t(col[k])));
+  const auto key = std::make_tuple(n, nnz, h);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      const std::vector<int> &c = it->second.first;
+      bool ok = int(c.size()) == n;
+      for (int i = 0; ok && i < n; ++i)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+          if (col[k] != i && c[col[k]] == c[i]) { ok = false; break; }
+      if (ok) {
+        *ncol = it->second.second;
+        return c;
+      }
+    }
+  }
+  std::vector<int> c = adj ? colour_graph(n, *adj, ncol) : colour_graph(n, sym_adjacency(n, rowptr, col), ncol);
+  std::lock_guard<std::mutex> lk(mu);
+  if (cache.size() >= 64) cache.erase(cache.begin());
+  cache[key] = {c, *ncol};
+  return c;
+}
+
 static std::vector<std::vector<int>> sym_adjacency(int n, const int *rowptr, const int *col) {
   std::vector<std::vector<int>> adj(n);
   for (int i = 0; i < n; ++i)
@@ -612,7 +654,7 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
       colour = *colour_in;
       H.ncolour = 1 + *std::max_element(colour.begin(), colour.end());
     } else {
-      colour = colour_graph(n, adj, &H.ncolour);
+      colour = colour_pattern(n, d.rowptr, d.col, &adj, &H.ncolour);
     }
     std::stable_sort(H.perm.begin(), H.perm.end(), [&](int a, int b) { return colour[a] < colour[b]; });
     // the wavefronts are the colour classes: contiguous ranges of the processing order
@@ -1457,7 +1499,7 @@ int gmg_mg_create_batched(const gmg_level_desc *const *instances, const int *ins
         auto it = colour_memo.find(key);
         if (it == colour_memo.end()) {
           int nc = 0;
-          it = colour_memo.emplace(key, colour_graph(e.n, sym_adjacency(e.n, e.rowptr, e.col), &nc)).first;
+          it = colour_memo.emplace(key, colour_pattern(e.n, e.rowptr, e.col, nullptr, &nc)).first;
         }
         colours[l].insert(colours[l].end(), it->second.begin(), it->second.end());
       }

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 
 #include "fields.h"
 #include "gmg_internal.h"
@@ -28,9 +29,11 @@ enum { SLOT_FREE = 0, SLOT_ACTIVE = 1, SLOT_DONE = 2 };
 
 struct gmg_pool {
   int nref = 0, nslots = 0, s = 1, maxit = 100;  // nref: the deepest slot's refinements
+  int mesh = 3;                              // generator kind of the cubes: 3 UG's red rules, 1 Freudenthal
+  std::vector<uint8_t *> masks;              // per level (UG's mesh): the tetrahedra of every cell
   double red = 1e-8, abslimit = 1e-50;
   std::vector<int> depth;                    // refinements of every slot's cube
-  std::map<int, gmg_gen *> tmpl;             // the cached topology of every depth
+  std::map<int, std::shared_ptr<gmg_gen>> tmpl;  // the topology of every depth (shared between pools)
   gmg_mg *mg = nullptr;
   NPLs *ls = nullptr;
   gmg_vec *x = nullptr, *b = nullptr;
@@ -56,6 +59,7 @@ struct gmg_pool {
     if (ev) cudaEventDestroy(ev);
     for (int *p : c2s) if (p) cudaFree(p);
     for (int *p : rows) if (p) cudaFree(p);
+    for (uint8_t *p : masks) if (p) cudaFree(p);
     if (kelem) cudaFree(kelem);
     if (kelem64) cudaFree(kelem64);
     if (ftab) cudaFree(ftab);
@@ -67,7 +71,6 @@ struct gmg_pool {
     if (norm_scratch) cudaFree(norm_scratch);
     if (first_host) cudaFreeHost(first_host);
     if (mg) gmg_mg_destroy(mg);
-    for (auto &kv : tmpl) gmg_gen_destroy(kv.second);
   }
 };
 
@@ -75,6 +78,22 @@ static int sc_less(const double *x, const double *y, int s) {  // sc_cmp, npscan
   for (int i = 0; i < s; ++i)
     if (std::fabs(x[i]) >= std::fabs(y[i])) return 0;
   return 1;
+}
+
+// The cube topologies of the pools, one per (mesh, depth) while any pool uses
+// it: generating UG's refinement of a depth-7 cube takes seconds on the host,
+// and a server holds several pools of one depth.
+static std::shared_ptr<gmg_gen> topology(int mesh, int depth) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::weak_ptr<gmg_gen>> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  std::weak_ptr<gmg_gen> &w = cache[{mesh, depth}];
+  if (auto g = w.lock()) return g;
+  gmg_gen *raw = nullptr;
+  if (gmg_gen_create(mesh, depth, 0, 0.1, 0.0, &raw)) return nullptr;
+  std::shared_ptr<gmg_gen> g(raw, [](gmg_gen *p) { gmg_gen_destroy(p); });
+  w = g;
+  return g;
 }
 
 static int np(gmg_mg *mg, const char *name, const char *cls, const char *args) {
@@ -91,21 +110,29 @@ int gmg_pool_create(int nref, int nslots, const char *smoother, double red, int 
     return 1;
   }
   std::vector<int> d(nslots, nref);
-  return gmg_pool_create_mixed(d.data(), nslots, smoother, red, maxit, device, out);
+  return gmg_pool_create_mesh(3, d.data(), nslots, smoother, red, maxit, device, out);
 }
 
 int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, double red, int maxit, int device,
                           gmg_pool **out) {
-  if (!out || !depths || nslots < 1 || !smoother) {
+  return gmg_pool_create_mesh(3, depths, nslots, smoother, red, maxit, device, out);
+}
+
+int gmg_pool_create_mesh(int mesh, const int *depths, int nslots, const char *smoother, double red, int maxit,
+                         int device, gmg_pool **out) {
+  if (!out || !depths || nslots < 1 || !smoother || (mesh != 1 && mesh != 3)) {
     set_error("gmg_pool_create: bad arguments");
     return 1;
   }
   *out = nullptr;
+  const int maxd = mesh == 3 ? 7 : 9;
   for (int k = 0; k < nslots; ++k)
-    GMG_CHECK(depths[k] >= 1 && depths[k] <= 9, "gmg_pool_create: slot %d has %d refinements (1..9)", k, depths[k]);
+    GMG_CHECK(depths[k] >= 1 && depths[k] <= maxd, "gmg_pool_create: slot %d has %d refinements (1..%d)", k,
+              depths[k], maxd);
   const std::string sm(smoother);
   GMG_CHECK(sm == "gs" || sm == "jac", "gmg_pool_create: smoother %s (gs or jac)", smoother);
   auto P = std::make_unique<gmg_pool>();
+  P->mesh = mesh;
   P->depth.assign(depths, depths + nslots);
   const int nref = *std::max_element(depths, depths + nslots);
   P->nref = nref;
@@ -115,11 +142,11 @@ int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, d
   std::vector<const gmg_level_desc *> inst(nslots);
   std::vector<int> nls(nslots);
   for (int k = 0; k < nslots; ++k) {
-    gmg_gen *&g = P->tmpl[depths[k]];
-    if (!g && gmg_gen_create(1, depths[k], 0, 0.1, 0.0, &g)) return 1;
+    std::shared_ptr<gmg_gen> &g = P->tmpl[depths[k]];
+    if (!g && !(g = topology(mesh, depths[k]))) return 1;
     const gmg_level_desc *levels = nullptr;
     int nlk = 0;
-    gmg_gen_levels(g, &levels, &nlk);
+    gmg_gen_levels(g.get(), &levels, &nlk);
     inst[k] = levels;
     nls[k] = nlk;
   }
@@ -147,9 +174,21 @@ int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, d
   const int top = nl - 1;
   int bl = 0, res = 0;
   if (P->ls->PreProcess(top, P->x, P->b, P->A, &bl, &res) || P->ls->prepare_temps(P->b)) return 1;
-  // per-level maps and slot tables
+  // per-level maps and slot tables; UG's mesh: every level's cells with their
+  // tetrahedra (the same on every depth that reaches the level)
   P->c2s.assign(nl, nullptr);
   P->rows.assign(nl, nullptr);
+  P->masks.assign(nl, nullptr);
+  if (mesh == 3) {
+    const gmg_gen *deep = P->tmpl[nref].get();
+    for (int l = 0; l < nl; ++l) {
+      const uint8_t *m = gen_cell_masks(deep, l);
+      GMG_CHECK(m, "pool: no cell tetrahedra on level %d", l);
+      const size_t bytes = size_t(6) << (3 * l);
+      GMG_CUDA(cudaMalloc(&P->masks[l], bytes));
+      GMG_CUDA(cudaMemcpy(P->masks[l], m, bytes, cudaMemcpyHostToDevice));
+    }
+  }
   P->sl.assign(nslots, std::vector<SlotLevel>(nl));
   for (int l = 0; l < nl; ++l) {
     Level &L = mg->lev[l];
@@ -169,12 +208,14 @@ int gmg_pool_create_mixed(const int *depths, int nslots, const char *smoother, d
       q.off = mg->batch.list_off[l][k];
       q.nrows = L.blk_ptr[blk + 1] - L.blk_ptr[blk];
       q.rows = P->rows[l] + L.blk_ptr[blk];
+      q.masks = P->masks[l];
       ++blk;
     }
   }
   const long long nemax = 6LL << (3 * nref);
   GMG_CUDA(cudaMalloc(&P->kelem64, sizeof(double) * nemax));
-  GMG_CUDA(cudaMalloc(&P->ftab, sizeof(double2) * GMG_FIELD_MAX_M * (3 * (1 << nref) + 6)));
+  // FP64 field tables: X, Y, ZP (Nc each), three Kuhn pair factors and 27 centroid offsets per feature
+  GMG_CUDA(cudaMalloc(&P->ftab, sizeof(double2) * GMG_FIELD_MAX_M * (3 * (1 << nref) + 3 + 27)));
   GMG_CUDA(cudaMalloc(&P->fw_dev, sizeof(double) * GMG_FIELD_MAX_M * 4 * nslots));
   GMG_CUDA(cudaMallocHost(&P->fw_host, sizeof(double) * GMG_FIELD_MAX_M * 4 * nslots));
   GMG_CUDA(cudaMalloc(&P->first_dev, sizeof(double) * GMG_MAX_S * nslots));
@@ -245,7 +286,8 @@ int gmg_pool_admit(gmg_pool *p, int k, unsigned long long seed, double corr, dou
     for (int l = 0; l < nl; ++l) {
       const double *ke = nullptr;
       if (var > 0.0) {
-        if (k_cube_field64(mg, 1 << l, fd, fd + GMG_FIELD_MAX_M * 3, M, amp, p->ftab, p->kelem64)) return 1;
+        if (k_cube_field64(mg, 1 << l, fd, fd + GMG_FIELD_MAX_M * 3, M, amp, p->ftab, p->kelem64, p->sl[k][l].masks))
+          return 1;
         ke = p->kelem64;
       }
       if (k_cube_assemble64(mg, mg->lev[l], p->sl[k][l], ke, 1.0 / double(1 << l), p->c2s[l])) return 1;
@@ -265,7 +307,9 @@ int gmg_pool_admit(gmg_pool *p, int k, unsigned long long seed, double corr, dou
     for (int l = 0; l < nl; ++l) {
       const float *ke = nullptr;
       if (var > 0.0) {
-        if (k_cube_field(mg, 1 << l, pd + size_t(l) * GMG_FIELD_MAX_M * 4, M[l], amp[l], p->kelem)) return 1;
+        if (k_cube_field(mg, 1 << l, pd + size_t(l) * GMG_FIELD_MAX_M * 4, M[l], amp[l], p->kelem,
+                         p->sl[k][l].masks))
+          return 1;
         ke = p->kelem;
       }
       if (k_cube_assemble(mg, mg->lev[l], p->sl[k][l], ke, 1.0 / double(1 << l), p->c2s[l])) return 1;

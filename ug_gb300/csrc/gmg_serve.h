@@ -17,6 +17,7 @@ struct SlotLevel {
   int off = 0;            // first union list position of the slot
   int nrows = 0;          // rows of the slot (N^3)
   const int *rows = nullptr;  // device: the slot's rows (processing order)
+  const uint8_t *masks = nullptr;  // device: UG's mesh, the tetrahedra of every cell (nullptr: Freudenthal)
 };
 
 // field features of LogNormalField(seed, 3, corr, var) for a level with h =
@@ -24,12 +25,19 @@ struct SlotLevel {
 void cube_field_params(uint64_t seed, double corr, double var, int level, std::vector<uint32_t> &prm, float *amp,
                        int *M);
 // k of every tetrahedron of a level with Nc cells per axis
-int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem);
+// (masks: UG's mesh, every cell's six tetrahedra as corner masks; nullptr:
+// the Freudenthal triangulation)
+int k_cube_field(gmg_mg *mg, int Nc, const uint32_t *prm_dev, int M, float amp, float *kelem,
+                 const uint8_t *masks = nullptr);
 // the FP64 field of a level with Nc cells per axis from the features w (M x 3)
-// and phi (M) of LogNormalField: tables (M (3 Nc + 6) double2) of per-axis and
+// and phi (M) of LogNormalField: tables (M (3 Nc + 30) double2) of per-axis and
 // per-tetrahedron phase factors, then k of every tetrahedron
 int k_cube_field64(gmg_mg *mg, int Nc, const double *w_dev, const double *phi_dev, int M, double amp,
-                   double2 *tables, double *kelem);
+                   double2 *tables, double *kelem, const uint8_t *masks = nullptr);
+// the tetrahedra of every cell of a UG-refined cube level (generator kind 3),
+// host memory owned by the generator; nullptr for the other kinds
+const uint8_t *gen_cell_masks(const gmg_gen *g, int level);
+int gen_kind(const gmg_gen *g);
 // ... assembly from an FP64 field
 int k_cube_assemble64(gmg_mg *mg, const Level &L, const SlotLevel &sl, const double *kelem, double h,
                       const int *c2s);

@@ -37,6 +37,9 @@ struct GenLevel {
   int n = 0, s = 1, N = 0;  // N = points per axis
   std::vector<int> rowptr, col, vclass, vnclass, skip, prow, pcol;
   std::vector<double> val, pw, xyz;
+  // kind 3: the six tetrahedra of every lattice cell ((z Nc + y) Nc + x) as
+  // masks of the cell's corners (bit dx | dy << 1 | dz << 2), ascending
+  std::vector<uint8_t> cell_masks;
 };
 
 struct Offs {
@@ -435,6 +438,32 @@ int build_ug_level(gmg_gen *G, int l, std::vector<Tet> &tets, const std::vector<
     if (a.x != b.x) return a.x < b.x;
     return a.ids < b.ids;
   });
+  // every cell holds six tetrahedra of volume h^3 / 6 (6 8^l of them fill the
+  // 8^l cells, and a tetrahedron on cube corners has volume 1/6 or 1/3 of it):
+  // their corner masks, the device assembly's description of the mesh
+  L.cell_masks.assign(size_t(nc) * nc * nc * 6, 0);
+  {
+    std::vector<uint8_t> fill(size_t(nc) * nc * nc, 0);
+    for (const Key &kk : keys) {
+      const Tet &T = tets[kk.t];
+      int mask = 0;
+      for (int a = 0; a < 4; ++a)
+        mask |= 1 << ((T.v[a][0] - kk.x) | ((T.v[a][1] - kk.y) << 1) | ((T.v[a][2] - kk.z) << 2));
+      const size_t cell = (size_t(kk.z) * nc + kk.y) * nc + kk.x;
+      if (fill[cell] >= 6) {
+        gmg::set_error("UG cube level %d: more than six tetrahedra in cell (%d,%d,%d)", l, kk.x, kk.y, kk.z);
+        return 1;
+      }
+      L.cell_masks[cell * 6 + fill[cell]++] = uint8_t(mask);
+    }
+    for (size_t c = 0; c < fill.size(); ++c) {
+      if (fill[c] != 6) {
+        gmg::set_error("UG cube level %d: cell %zu holds %d tetrahedra", l, c, int(fill[c]));
+        return 1;
+      }
+      std::sort(L.cell_masks.begin() + c * 6, L.cell_masks.begin() + c * 6 + 6);
+    }
+  }
   std::vector<size_t> zbeg(nc + 1, 0);
   for (const Key &kk : keys) zbeg[kk.z + 1]++;
   for (int z = 0; z < nc; ++z) zbeg[z + 1] += zbeg[z];
@@ -539,6 +568,14 @@ int build_ug_cube(gmg_gen *G, const ugfx::LogNormalField &field) {
 }
 
 }  // namespace
+
+namespace gmg {
+const uint8_t *gen_cell_masks(const gmg_gen *g, int level) {
+  if (!g || level < 0 || level > g->nref || g->lev[level].cell_masks.empty()) return nullptr;
+  return g->lev[level].cell_masks.data();
+}
+int gen_kind(const gmg_gen *g) { return g ? g->kind : -1; }
+}  // namespace gmg
 
 extern "C" {
 

@@ -78,21 +78,19 @@ def pool_bytes(nref: int, nslots: int) -> int:
 class Pool:
     """One gmg_pool: `nslots` slots of depth `nref`, or (depths given) one slot
     per entry of `depths`, each of its own depth: a mixed pool, whose every
-    iteration runs the V-cycles of all its requests level by level together."""
+    iteration runs the V-cycles of all its requests level by level together.
+    mesh: 3 the cubes UG's red rules refine (UG's own hierarchies), 1 the
+    Freudenthal triangulation."""
 
     def __init__(self, nref: int, nslots: int, smoother: str = "gs", red: float = 1e-8, maxit: int = 100,
-                 device: int = 0, stream=None, field_fp64: bool = True, depths=None):
+                 device: int = 0, stream=None, field_fp64: bool = True, depths=None, mesh: int = 3):
         h = C.c_void_p()
-        if depths is not None:
-            d = np.ascontiguousarray(depths, np.int32)
-            if lib().gmg_pool_create_mixed(d.ctypes.data, len(d), smoother.encode(), red, maxit, device,
-                                           C.byref(h)):
-                _err("gmg_pool_create_mixed")
-            self.depths = [int(x) for x in d]
-        else:
-            if lib().gmg_pool_create(nref, nslots, smoother.encode(), red, maxit, device, C.byref(h)):
-                _err("gmg_pool_create")
-            self.depths = [nref] * nslots
+        d = np.ascontiguousarray(depths if depths is not None else [nref] * nslots, np.int32)
+        if lib().gmg_pool_create_mesh(mesh, d.ctypes.data, len(d), smoother.encode(), red, maxit, device,
+                                      C.byref(h)):
+            _err("gmg_pool_create_mesh")
+        self.depths = [int(x) for x in d]
+        self.mesh = mesh
         self._h = h
         if not field_fp64 and lib().gmg_pool_set_field_precision(h, 1):
             _err("gmg_pool_set_field_precision")
@@ -215,7 +213,7 @@ class Server:
     def __init__(self, depths=range(2, 8), layout=None, hbm_fraction: float = 0.5, smoother: str = "gs",
                  red: float = 1e-8, maxit: int = 100, corr: float = 0.1, var: float = 1.0, device: int = 0,
                  slots=None, field_fp64: bool = False, mixed=(), grow_after_ms: float | None = None,
-                 grow_reserve: float = 0.1):
+                 grow_reserve: float = 0.1, mesh: int = 3):
         """field_fp64: admissions evaluate the coefficient field in FP64 (the
         host generator's problem to 1e-12; on GB300 ~12 ms of FP64 work per
         depth-7 admission, more than a 200 req/s stream leaves) instead of
@@ -226,10 +224,14 @@ class Server:
         free memory (queried at that moment) covers it with grow_reserve of
         the device left over; the pool is created and warmed on a helper
         thread while the loop keeps serving, and joins the loop when ready
-        (None: the pools are fixed)."""
+        (None: the pools are fixed).
+
+        mesh: 3 (default) the cubes refined by UG's red rules, 1 the
+        Freudenthal triangulation."""
         import torch
         self.corr, self.var = corr, var
         self.field_fp64 = field_fp64
+        self.mesh = mesh
         self.grow_after_ms, self.grow_reserve = grow_after_ms, grow_reserve
         self._args = (smoother, red, maxit, device)
         self.grown = []  # (seconds into the stream, depth) of every pool added while serving
@@ -259,10 +261,12 @@ class Server:
                 st = torch.cuda.Stream(device=device)
                 self.streams.append(st)
                 if len(g) == 1:
-                    pool = Pool(g[0], layout[g[0]][1], smoother, red, maxit, device, st.cuda_stream, field_fp64)
+                    pool = Pool(g[0], layout[g[0]][1], smoother, red, maxit, device, st.cuda_stream, field_fp64,
+                                mesh=mesh)
                 else:
                     dep = [L for L in g for _ in range(layout[L][1])]
-                    pool = Pool(0, 0, smoother, red, maxit, device, st.cuda_stream, field_fp64, depths=dep)
+                    pool = Pool(0, 0, smoother, red, maxit, device, st.cuda_stream, field_fp64, depths=dep,
+                                mesh=mesh)
                 self.all_pools.append(pool)
                 for L in g:
                     self.pools[L].append(pool)
@@ -284,7 +288,8 @@ class Server:
         smoother, red, maxit, device = self._args
         torch.cuda.set_device(device)
         st = torch.cuda.Stream(device=device)
-        pool = Pool(L, self.layout[L][1], smoother, red, maxit, device, st.cuda_stream, self.field_fp64)
+        pool = Pool(L, self.layout[L][1], smoother, red, maxit, device, st.cuda_stream, self.field_fp64,
+                    mesh=self.mesh)
         pool.solve(1, self.corr, self.var)
         torch.cuda.current_stream(device).synchronize()
         ready.append((L, pool, st))
