@@ -131,7 +131,8 @@ long long gmg_mg_device_bytes(const gmg_mg *mg);
 /* Kernel launches issued by mg since creation (or the last reset). */
 long long gmg_mg_launch_count(const gmg_mg *mg, int reset);
 const char *gmg_last_error(void);
-/* Synchronise mg's stream; returns nonzero if a kernel failed. */
+/* Synchronise mg's stream; returns nonzero if a kernel failed or a bounded
+ * device-side wait (the one-launch interface ILU sweeps) gave up. */
 int gmg_mg_sync(gmg_mg *mg);
 
 /* ------------------------------------------------ batched hierarchies */

@@ -1741,6 +1741,19 @@ int gmg_mg_sync(gmg_mg *mg) {
   if (!mg) return 1;
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
   GMG_CUDA(cudaGetLastError());
+  // a one-launch interface ILU sweep whose completion wait ran out (its rows
+  // became NaN): report it once and clear the flag
+  for (size_t l = 0; l < mg->lev.size(); ++l) {
+    const Level &L = mg->lev[l];
+    if (!L.iface_err) continue;
+    int e = 0;
+    GMG_CUDA(cudaMemcpy(&e, L.iface_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+      GMG_CUDA(cudaMemset(L.iface_err, 0, sizeof(int)));
+      set_error("level %zu: an interface ILU sweep gave up waiting for a neighbour row (results are NaN)", l);
+      return 1;
+    }
+  }
   return 0;
 }
 
