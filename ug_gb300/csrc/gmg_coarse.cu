@@ -94,7 +94,10 @@ __device__ PL<T> make_pl(const SLev &s, char *sm) {
 
 template <int S>
 struct GL {
-  static constexpr int G = S == 1 ? 4 : 2;  // lanes per row
+  // lanes per row; measured on the C2 cube (one mixed solve): 1 / 2 / 4 / 8
+  // lanes 5.36 / 5.36 / 5.44 / 5.52 ms on UG's mesh, 3.09 / 3.13 / 3.19 /
+  // 3.30 ms on the Freudenthal triangulation
+  static constexpr int G = S == 1 ? 1 : 2;
 };
 
 template <int G, class T>
@@ -773,7 +776,7 @@ static int make_single(gmg_mg *mg, int bl, int lc, int smo, CachedImage &e) {
   std::vector<char> img;
   if (build_image<T>(mg, bl, nl, smo, LH, sub, false, -1, e.args, img, &e.smem)) return 1;
   {  // the narrow team takes the levels from the base up with at most ~4 rows per lane group
-    const int G = mg->lev[bl].s == 1 ? 4 : 2;
+    const int G = mg->lev[bl].s == 1 ? GL<1>::G : GL<2>::G;
     int nn = 0;
     while (nn < nl && e.args.L[nn].n <= 4 * (NARROW / G)) ++nn;
     e.args.narrow = nn;
