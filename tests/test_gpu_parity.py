@@ -159,6 +159,15 @@ def test_numproc_status_and_errors(G):
         mg.npcreate("bad", "iter.nosuchclass")
     with pytest.raises(G.GmgError):
         mg.npexecute("lmgc", "$s")                                  # not executable
+    # the function-table entries refuse a numproc whose init failed or that
+    # was never initialised (its $I / $S / $T partners are missing)
+    with pytest.raises(G.GmgError, match="not initialised"):
+        mg.ls_preprocess("ls", mg.top, "sol", "rhs")
+    with pytest.raises(G.GmgError, match="not initialised"):
+        mg.solve_host("ls", fx["rhs"])
+    mg.npcreate("j", "iter.gjac")
+    with pytest.raises(G.GmgError, match="not initialised"):
+        mg.iter_iter("j", mg.top, "sol", "rhs")
     G.setup_lmgc(mg, "jac", baselevel=2)
     assert "n1 = 2" in mg.npdisplay("lmgc") and "baselevel = 2" in mg.npdisplay("lmgc")
     mg.upload("rhs", mg.top, fx["rhs"])

@@ -1921,9 +1921,17 @@ int gmg_np_display(gmg_np *np, char *buf, int buflen) {
   return 0;
 }
 
-#define AS(T, np, k)                                                  \
-  T *p = (np && np->kind() == k) ? static_cast<T *>(np) : nullptr;    \
-  if (!p) { set_error("%s: numproc of the wrong class", __func__); return 1; }
+// the function-table entries take a numproc of their class whose init
+// found its partners ($I, $S, $T; status NP_ACTIVE or NP_EXECUTABLE), as
+// UG's parents only call numprocs that initialised
+#define AS(T, np, k)                                                                               \
+  T *p = (np && np->kind() == k) ? static_cast<T *>(np) : nullptr;                                 \
+  if (!p) { set_error("%s: numproc of the wrong class", __func__); return 1; }                     \
+  if (p->status < NP_ACTIVE) {                                                                     \
+    set_error("%s: numproc %s is not initialised (status %d; npinit it with the objects it names " \
+              "created first)", __func__, p->name.c_str(), p->status);                             \
+    return 1;                                                                                      \
+  }
 
 int gmg_iter_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *bl, int *result) {
   AS(NPIter, np, NPK_ITER);
@@ -2161,6 +2169,7 @@ int gmg_solve_host(gmg_mg *mg, const char *solver, const double *b_host, double 
   if (!mg || !solver || !b_host || !x_host || !lr) { set_error("gmg_solve_host: bad arguments"); return 1; }
   gmg_np *np = gmg_np_by_name(mg, solver);
   GMG_CHECK(np && np->kind() == NPK_LS, "no linear solver %s", solver);
+  GMG_CHECK(np->status >= NP_ACTIVE, "linear solver %s is not initialised (status %d)", solver, np->status);
   NPLinearSolver *ls = static_cast<NPLinearSolver *>(np);
   NPLs *gls = dynamic_cast<NPLs *>(ls);
   GMG_CHECK(ls->x && ls->b && ls->A, "solver %s has no x, b or A", solver);
