@@ -119,11 +119,16 @@ int gmg_mg_domain_info(const gmg_mg *mg, int level, int *nsub, int *ninterior, i
  * evict-first matrix stream (1 / 0, -1 = chosen by size); set by the
  * autotuner (gmg_mg_opts.autotune) at creation. */
 int gmg_mg_level_variant(const gmg_mg *mg, int level, int *tpr, int *prefetch, int *stream);
-/* Chained Gauss-Seidel steps of a small multicolour level (at most 48
- * colours, its t and c within 200 KB) in ONE thread block, the colour waves
- * separated by block barriers instead of kernel launches; bit-identical to
- * the per-wave launches.  The autotuner turns it on where it is faster; set
- * it (1 / 0) before the first solve that captures a CUDA graph. */
+/* How the chained Gauss-Seidel steps of a multicolour level (at most 48
+ * colours) run: 0 = one launch per colour wave; 1 = ONE thread block, the
+ * colour waves separated by block barriers (t and c within 200 KB of shared
+ * memory); 2, 4, 8 or 16 = one thread-block cluster of that many blocks,
+ * each holding all of t in shared memory (within 227 KB with its rows' c),
+ * the waves separated by cluster barriers, new values sent to every block
+ * through distributed shared memory.  All forms are bit-identical to the
+ * per-wave launches.  The autotuner picks the fastest; set it before the
+ * first solve that captures a CUDA graph.  Refused (1) for a level or device
+ * where the form cannot run. */
 int gmg_mg_level_cta_chain(const gmg_mg *mg, int level, int *on);
 int gmg_mg_set_level_cta_chain(gmg_mg *mg, int level, int on);
 /* Device bytes held by the hierarchy. */

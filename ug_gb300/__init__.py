@@ -698,10 +698,11 @@ class MultiGrid:
         if lib().gmg_mg_set_iface_sweep(self._h, int(mode)):
             _err("set_iface_sweep")
 
-    def set_cta_chain(self, level: int, on: bool):
-        """Run the level's chained Gauss-Seidel steps in one thread block (on)
-        or as one launch per colour wave; before the first graph-captured solve."""
-        if lib().gmg_mg_set_level_cta_chain(self._h, level, int(bool(on))):
+    def set_cta_chain(self, level: int, blocks):
+        """Run the level's chained Gauss-Seidel steps as one launch per colour
+        wave (0 / False), in one thread block (1 / True) or in one cluster of
+        2, 4, 8 or 16 blocks; before the first graph-captured solve."""
+        if lib().gmg_mg_set_level_cta_chain(self._h, level, int(blocks)):
             _err("set_cta_chain")
 
     def update_values(self, level: int, val):

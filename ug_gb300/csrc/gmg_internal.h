@@ -145,7 +145,9 @@ struct Level {
   // kernel variants of the level (autotuner; -1: by size): prefetch the
   // rows' structure before the launch wait; evict-first matrix stream
   int prefetch = -1, stream = -1;
-  // chained Gauss-Seidel steps in one thread block (gs_chain_cta_ok levels)
+  // chained Gauss-Seidel steps run by: 0 one launch per colour wave, 1 one
+  // thread block (gs_chain_cta_ok), cw > 1 a cluster of cw blocks
+  // (gs_chain_cluster_ok)
   int cta_chain = 0;
   // sliced ELLPACK copy of A (slices of 32 consecutive rows stored column by
   // column, padded to the slice's longest row with zero blocks pointing at the
@@ -153,6 +155,7 @@ struct Level {
   bool sell = false;
   int *sell_ptr = nullptr;  // nslices+1 entry offsets
   long long sell_nent = 0;  // stored entries (padding included)
+  int sell_wmax = 0;        // entries of the widest slice's rows (diagonal included)
   int *sell_col = nullptr;
   double *sell_v64 = nullptr;
   float *sell_v32 = nullptr;
@@ -384,16 +387,24 @@ int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // qualifies (sliced ELLPACK, colour-contiguous waves, every row ACTIVE)
 bool gs_chain_ok(const Level &L, int prec);
 int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps);
-// the chained steps of a level in one thread block (Level::cta_chain): at
-// most CTA_CHAIN_MAXW waves, t and c of the level in shared memory
+// the chained steps of a level in one thread block (Level::cta_chain = 1):
+// at most CTA_CHAIN_MAXW waves, t and c of the level in shared memory
 constexpr int CTA_CHAIN_MAXW = 48;
 constexpr long long CTA_CHAIN_SMEM = 200 * 1024;
 struct CtaWaves {
   int n, nwave, steps;
+  int own, wm;  // cluster form: slots of the block with the most rows; stored off-diagonal entries a row
   int ptr[CTA_CHAIN_MAXW + 1];
 };
 long long gs_chain_cta_smem(const Level &L, int prec);
 bool gs_chain_cta_ok(const Level &L, int prec);
+// ... or in one thread-block cluster of cw = 2, 4, 8 or 16 blocks
+// (Level::cta_chain = cw): every block holds all of t in shared memory
+// (CLUSTER_CHAIN_SMEM with its c slots); also false where the device cannot
+// co-schedule such a cluster
+constexpr long long CLUSTER_CHAIN_SMEM = 227 * 1024;
+long long gs_chain_cluster_smem(const Level &L, int prec, int cw);
+bool gs_chain_cluster_ok(const Level &L, int prec, int cw);
 // ILU forward / backward solve with the factors of L
 int k_luiter(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // ILU(0) factors of the level matrix with beta (l_ilubthdecomp) on the device,

@@ -11,8 +11,10 @@
 // The arithmetic of each kernel follows the UG routine named in its comment;
 // results agree with the reference to rounding (the summation order inside a
 // row follows the shuffle tree instead of the MATRIX list).
+#include <algorithm>
 #include <cstdio>
 #include <map>
+#include <mutex>
 #include <utility>
 
 #include "gmg_internal.h"
@@ -111,6 +113,21 @@ struct SellPart {
   int e0, w;
   int col[P > 0 ? P : 1];
   T val[P > 0 ? P : 1][S * S];
+  // the w entries from entry e0_ on (their start already known)
+  __device__ __forceinline__ void load_at(int e0_, int w_, const int *__restrict__ scol, const T *__restrict__ sval) {
+    e0 = e0_;
+    w = w_;
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      col[k] = 0;
+      if (k < w) {
+        const int e = e0 + 32 * k;
+        col[k] = __ldg(scol + e);
+#pragma unroll
+        for (int q = 0; q < S * S; ++q) val[k][q] = __ldg(sval + (size_t)e * (S * S) + q);
+      }
+    }
+  }
   __device__ __forceinline__ void load(int i, int part, const int *__restrict__ sptr, const uint8_t *__restrict__ nl,
                                        const int *__restrict__ scol, const T *__restrict__ sval) {
     const int base = __ldg(sptr + (i >> 5));
@@ -660,6 +677,256 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_c
   for (int k = tid; k < W.n * S; k += NT) {
     t[k] = ts[k];
     c[k] = cs[k];
+  }
+}
+
+// ------------------------------------------------------------ chained steps in one cluster
+// The same chained steps spread over a thread-block cluster of cw blocks on
+// cw SMs.  Each colour wave is cut into chunks of 32 rows (one sliced-ELLPACK
+// slice) dealt to the blocks in turn; a block's rows of a wave are numbered
+// L = 0..cnt-1 and row L is done by thread L mod NT, its c_i kept in the
+// block's slot of the row.  Every block holds the whole of t in its shared
+// memory: a new t_i is stored into every block's copy through distributed
+// shared memory, and the waves are separated by cluster barriers (release
+// on arrive, acquire on wait).  With RS the matrix entries of the block's
+// rows are staged in its shared memory once per call (before the launch
+// wait), so the waves read no global memory; without it the rows stream from
+// L2 and each thread's next row is fetched between arrive and wait.  The
+// arithmetic of every row is that of sell_gs_chain_kernel, in the same order,
+// so the results are bit-identical to the per-wave launches.
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+// the shared::cluster address of shared::cta address `a` in block q
+__device__ __forceinline__ uint32_t cluster_map(uint32_t a, unsigned q) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(q));
+  return r;
+}
+__device__ __forceinline__ void st_cluster(uint32_t a, float v) {
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+// rows of a wave of len rows that block `rank` of cw takes (chunks rank,
+// rank + cw, ...; the last chunk of the wave may be partial)
+__host__ __device__ inline int cluster_share(int len, int cw, int rank) {
+  const int nch = (len + 31) / 32;
+  if (rank >= nch) return 0;
+  const int mine = (nch - 1 - rank) / cw + 1;
+  const int last = rank + (mine - 1) * cw;
+  return (mine - 1) * 32 + (last == nch - 1 ? len - last * 32 : 32);
+}
+// the wave row of the block's row L: its chunk L / 32 is chunk (L / 32) cw + rank
+__device__ __forceinline__ int cluster_row(int r0, int L, unsigned cw, unsigned rank) {
+  return r0 + ((L >> 5) * int(cw) + int(rank)) * 32 + (L & 31);
+}
+
+template <class T, int S, int PN, int NT, bool RS>
+__global__ void __launch_bounds__(NT, 1) sell_gs_chain_cluster_kernel(const __grid_constant__ CtaWaves W,
+                                                                      const int *__restrict__ sptr,
+                                                                      const uint8_t *__restrict__ nl,
+                                                                      const int *__restrict__ scol,
+                                                                      const T *__restrict__ sval,
+                                                                      const T *__restrict__ dinv, T *__restrict__ b,
+                                                                      T *__restrict__ t, T *__restrict__ c) {
+  // t (n S) | c slots (own S) | inverse diagonals (own S S) | RS: values
+  // (wm own S S), columns (wm own) | widths (own: off-diagonal entries |
+  // lower ones << 16) | streamed: first off-diagonal entry (own) | first
+  // slot of each wave (nwave + 1).  Slot q's entry k sits at k own + q.
+  extern __shared__ __align__(16) unsigned char cl_smem[];
+  T *ts = reinterpret_cast<T *>(cl_smem);
+  T *cs = ts + (size_t)W.n * S;
+  T *md = cs + (size_t)W.own * S;
+  T *mv = md + (size_t)W.own * S * S;
+  int *mc = reinterpret_cast<int *>(mv + (RS ? (size_t)W.wm * W.own * S * S : 0));
+  int *mw = mc + (RS ? (size_t)W.wm * W.own : 0);
+  int *me = mw + W.own;
+  int *wb = me + (RS ? 0 : W.own);
+  const uint32_t ts_sa = uint32_t(__cvta_generic_to_shared(ts));
+  const unsigned cw = cluster_size(), rank = cluster_rank();
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    int q = 0;
+    for (int w = 0; w < W.nwave; ++w) {
+      wb[w] = q;
+      q += cluster_share(W.ptr[w + 1] - W.ptr[w], int(cw), int(rank));
+    }
+    wb[W.nwave] = q;
+  }
+  __syncthreads();
+  const int nown = wb[W.nwave];
+  // slot q of the block: its wave and row
+  auto slot_row = [&](int q) {
+    int w = 0;
+    while (wb[w + 1] <= q) ++w;
+    return cluster_row(W.ptr[w], q - wb[w], cw, rank);
+  };
+  // the entries kb..ke-1 (of the off-diagonal ones) of a part of slot q's
+  // row: 0 all, 1 the lower, 2 the upper ones and the padding
+  auto part_range = [&](int q, int part, int &kb, int &ke) {
+    const int meta = mw[q], wt1 = meta & 0xffff, nlw = meta >> 16;
+    kb = 0;
+    ke = wt1;
+    if (nl && part == 1) ke = nlw;
+    if (nl && part == 2) kb = nlw;
+  };
+  // the static part of every slot's row, before the launch wait (slot q by
+  // thread q mod NT)
+  for (int q = tid; q < nown; q += NT) {
+    const int i = slot_row(q);
+    const int base = __ldg(sptr + (i >> 5));
+    const int wt1 = ((__ldg(sptr + (i >> 5) + 1) - base) >> 5) - 1;
+    mw[q] = wt1 | (nl ? int(__ldg(nl + i)) << 16 : 0);
+#pragma unroll
+    for (int z = 0; z < S * S; ++z) md[(size_t)q * S * S + z] = __ldg(dinv + (size_t)i * S * S + z);
+    if constexpr (RS) {
+      for (int k = 0; k < wt1; ++k) {
+        const int e = base + (i & 31) + 32 * (k + 1);
+        mc[(size_t)k * W.own + q] = __ldg(scol + e);
+#pragma unroll
+        for (int z = 0; z < S * S; ++z) mv[((size_t)k * W.own + q) * S * S + z] = __ldg(sval + (size_t)e * S * S + z);
+      }
+    } else {
+      me[q] = base + (i & 31) + 32;
+    }
+  }
+  SellPart<T, S, RS ? 1 : PN> R;
+  T bi[S];
+  auto load_row = [&](int q, int part) {
+    if constexpr (!RS) {
+      int kb, ke;
+      part_range(q, part, kb, ke);
+      R.load_at(me[q] + 32 * kb, ke - kb, scol, sval);
+    }
+  };
+  auto load_b = [&](int i) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) bi[r] = b[(size_t)i * S + r];
+  };
+  const int first = wb[1] > tid ? cluster_row(W.ptr[0], tid, cw, rank) : -1;
+  if (first >= 0) load_row(tid, 1);  // slot tid, staged by this thread
+  pdl_wait_then_trigger();
+  for (int q = tid; q < nown; q += NT) {
+    const int i = slot_row(q);
+#pragma unroll
+    for (int r = 0; r < S; ++r) cs[(size_t)q * S + r] = c[(size_t)i * S + r];
+  }
+  if (first >= 0) load_b(first);
+  // every block has started and staged its rows before any stores into it
+  cluster_arrive();
+  cluster_wait();
+  // s -= (a part of slot q's row) t, the entries failing the column test left out
+  auto row_dot = [&](T *s, int i, int q, int st, int part) {
+    if constexpr (RS) {
+      int kb, ke;
+      part_range(q, part, kb, ke);
+      for (int k = kb; k < ke; ++k) {
+        const int j = mc[(size_t)k * W.own + q];
+        if (part == 2 ? j <= i : st == 0 ? j >= i : j == i) continue;
+        const T *m = mv + ((size_t)k * W.own + q) * S * S;
+#pragma unroll
+        for (int cc = 0; cc < S; ++cc) {
+          const T tv = ts[(size_t)j * S + cc];
+#pragma unroll
+          for (int r = 0; r < S; ++r) s[r] = fma(-m[r * S + cc], tv, s[r]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < PN; ++k) {
+        if (k < R.w && (part == 2 ? R.col[k] > i : st == 0 ? R.col[k] < i : R.col[k] != i)) {
+#pragma unroll
+          for (int cc = 0; cc < S; ++cc) {
+            const T tv = ts[(size_t)R.col[k] * S + cc];
+#pragma unroll
+            for (int r = 0; r < S; ++r) s[r] = fma(-R.val[k][r * S + cc], tv, s[r]);
+          }
+        }
+      }
+      int e = R.e0 + 32 * (PN > 0 ? PN : 0);
+      for (int k = PN > 0 ? PN : 0; k < R.w; ++k, e += 32) {
+        const int j = __ldg(scol + e);
+        if (part == 2 ? j <= i : st == 0 ? j >= i : j == i) continue;
+        const T *m = sval + (size_t)e * (S * S);
+#pragma unroll
+        for (int cc = 0; cc < S; ++cc) {
+          const T tv = ts[(size_t)j * S + cc];
+#pragma unroll
+          for (int r = 0; r < S; ++r) s[r] = fma(-__ldg(m + r * S + cc), tv, s[r]);
+        }
+      }
+    }
+  };
+  for (int st = 0; st < W.steps; ++st) {
+    for (int w = 0; w < W.nwave; ++w) {
+      const int r0 = W.ptr[w], cnt = wb[w + 1] - wb[w];
+      // this thread's first row of the next wave, fetched while the new
+      // values travel and the cluster gathers
+      const int w2 = w + 1 < W.nwave ? w + 1 : 0, st2 = w + 1 < W.nwave ? st : st + 1;
+      bool fetched = false;
+      auto fetch_next = [&]() {
+        fetched = true;
+        if (st2 < W.steps && tid < wb[w2 + 1] - wb[w2]) {
+          load_row(wb[w2] + tid, st2 == 0 ? 1 : 0);
+          if (st2 == 0) load_b(cluster_row(W.ptr[w2], tid, cw, rank));
+        }
+      };
+      for (int L = tid; L < cnt; L += NT) {
+        const int i = cluster_row(r0, L, cw, rank), q = wb[w] + L;
+        if (L != tid) {
+          load_row(q, st == 0 ? 1 : 0);
+          if (st == 0) load_b(i);
+        }
+        T s[S], v[S];
+#pragma unroll
+        for (int r = 0; r < S; ++r) s[r] = st == 0 ? bi[r] : T(0);
+        row_dot(s, i, q, st, st == 0 ? 1 : 0);
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+          v[r] = T(0);
+#pragma unroll
+          for (int cc = 0; cc < S; ++cc) v[r] = fma(md[(size_t)q * S * S + r * S + cc], s[cc], v[r]);
+        }
+        if (L + NT >= cnt) fetch_next();
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+          const uint32_t off = ts_sa + uint32_t(((size_t)i * S + r) * sizeof(T));
+          for (unsigned p = 0; p < cw; ++p) st_cluster(cluster_map(off, p), v[r]);
+          cs[(size_t)q * S + r] += v[r];
+        }
+      }
+      if (!fetched) fetch_next();
+      cluster_arrive();
+      cluster_wait();
+    }
+  }
+  // b = -U t on the block's rows; t and c back to global memory
+  for (int q = tid; q < nown; q += NT) {
+    const int i = slot_row(q);
+    load_row(q, 2);
+    T s[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) s[r] = T(0);
+    row_dot(s, i, q, 1, 2);
+#pragma unroll
+    for (int r = 0; r < S; ++r) b[(size_t)i * S + r] = s[r];
+  }
+  for (int k = int(rank) * NT + tid; k < W.n * S; k += int(cw) * NT) t[k] = ts[k];
+  for (int q = tid; q < nown; q += NT) {
+    const int i = slot_row(q);
+#pragma unroll
+    for (int r = 0; r < S; ++r) c[(size_t)i * S + r] = cs[(size_t)q * S + r];
   }
 }
 
@@ -2702,9 +2969,164 @@ static int gs_chain_cta(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps)
   return 0;
 }
 
+template <class T, int S>
+constexpr int cluster_chain_nt() {
+  return S == 1 && sizeof(T) == 4 ? 1024 : 512;  // 64 / 128 registers a thread
+}
+
+// slots of the block of a cw-cluster with the most rows
+static int cluster_chain_own(const Level &L, int cw) {
+  int own = 0;
+  for (int r = 0; r < cw; ++r) {
+    int q = 0;
+    for (int w = 0; w < L.lower.nwave(); ++w) q += cluster_share(L.lower.ptr[w + 1] - L.lower.ptr[w], cw, r);
+    own = std::max(own, q);
+  }
+  return own;
+}
+
+// shared memory of the cluster form with the block's rows staged (rs) or streamed
+static long long cluster_chain_bytes(const Level &L, int prec, int cw, bool rs) {
+  const long long el = prec == GMG_PREC_FP64 ? 8 : 4, own = cluster_chain_own(L, cw), wm = std::max(L.sell_wmax - 1, 0);
+  const long long s = L.s;
+  return el * s * (L.n + own + own * s + (rs ? wm * own * s : 0)) +
+         4 * ((rs ? wm * own : 0) + own + (rs ? 0 : own) + L.lower.nwave() + 1);
+}
+
+// 2: rows staged in shared memory, 1: rows streamed, 0: no cluster form
+static int cluster_chain_form(const Level &L, int prec, int cw, int *smem) {
+  if (!(cw == 2 || cw == 4 || cw == 8 || cw == 16)) return 0;
+  if (!gs_chain_ok(L, prec) || L.lower.nwave() > CTA_CHAIN_MAXW) return 0;
+  for (int rs = 1; rs >= 0; --rs) {
+    const long long b = cluster_chain_bytes(L, prec, cw, rs != 0);
+    if (b <= CLUSTER_CHAIN_SMEM) {
+      *smem = int(b);
+      return rs ? 2 : 1;
+    }
+  }
+  return 0;
+}
+
+long long gs_chain_cluster_smem(const Level &L, int prec, int cw) {
+  int smem = 0;
+  return cluster_chain_form(L, prec, cw, &smem) ? smem : cluster_chain_bytes(L, prec, cw, false);
+}
+
+// the kernel with its launch attributes set for `smem` bytes; false where the
+// device cannot co-schedule a cluster of cw such blocks (remembered)
+template <class T, int S, bool RS>
+static bool cluster_chain_prepare(int cw, int smem) {
+  constexpr int NT = cluster_chain_nt<T, S>();
+  auto kern = sell_gs_chain_cluster_kernel<T, S, PF<S>::N, NT, RS>;
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, bool> fits;
+  static int smem_set = 0, nonportable = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = fits.find({cw, smem});
+  if (it != fits.end()) return it->second;
+  bool ok = true;
+  if (smem_set < smem) {
+    ok = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
+    if (ok) smem_set = smem;
+  }
+  if (ok && cw > 8 && !nonportable) {
+    ok = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+    if (ok) nonportable = 1;
+  }
+  if (ok) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cw);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cw;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters > 0;
+  }
+  cudaGetLastError();
+  fits[{cw, smem}] = ok;
+  return ok;
+}
+
+template <class T, int S>
+static bool cluster_chain_prepare(int form, int cw, int smem) {
+  return form == 2 ? cluster_chain_prepare<T, S, true>(cw, smem) : cluster_chain_prepare<T, S, false>(cw, smem);
+}
+
+bool gs_chain_cluster_ok(const Level &L, int prec, int cw) {
+  int smem = 0;
+  const int form = cluster_chain_form(L, prec, cw, &smem);
+  if (!form) return false;
+  if (prec == GMG_PREC_FP64) {
+    if (L.s == 1) return cluster_chain_prepare<double, 1>(form, cw, smem);
+    if (L.s == 2) return cluster_chain_prepare<double, 2>(form, cw, smem);
+    if (L.s == 3) return cluster_chain_prepare<double, 3>(form, cw, smem);
+  } else {
+    if (L.s == 1) return cluster_chain_prepare<float, 1>(form, cw, smem);
+    if (L.s == 2) return cluster_chain_prepare<float, 2>(form, cw, smem);
+    if (L.s == 3) return cluster_chain_prepare<float, 3>(form, cw, smem);
+  }
+  return false;
+}
+
+template <class T, int S>
+static int gs_chain_cluster(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps, int cw) {
+  constexpr int NT = cluster_chain_nt<T, S>();
+  int smem = 0;
+  const int form = cluster_chain_form(L, sizeof(T) == 8 ? GMG_PREC_FP64 : GMG_PREC_FP32, cw, &smem);
+  GMG_CHECK(form, "no cluster form of %d blocks for this level", cw);
+  CtaWaves W{};
+  W.n = L.n;
+  W.nwave = L.lower.nwave();
+  W.steps = steps;
+  W.own = cluster_chain_own(L, cw);
+  W.wm = std::max(L.sell_wmax - 1, 0);
+  for (int w = 0; w <= W.nwave; ++w) W.ptr[w] = L.lower.ptr[w];
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cw);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = mg->stream;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cw;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = mg->opts.disable_pdl ? 1 : 2;
+  const uint8_t *nl = L.sell_split ? L.sell_nl : nullptr;
+  if (form == 2)
+    cudaLaunchKernelEx(&cfg, sell_gs_chain_cluster_kernel<T, S, PF<S>::N, NT, true>, W, (const int *)L.sell_ptr, nl,
+                       (const int *)L.sell_col, sell_val<T>(L), dinv_of<T>(L), b, t, c);
+  else
+    cudaLaunchKernelEx(&cfg, sell_gs_chain_cluster_kernel<T, S, PF<S>::N, NT, false>, W, (const int *)L.sell_ptr, nl,
+                       (const int *)L.sell_col, sell_val<T>(L), dinv_of<T>(L), b, t, c);
+  LAUNCH_CHECK(mg);
+  return 0;
+}
+
 int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps) {
   GMG_CHECK(gs_chain_ok(L, prec) && steps >= 1, "chained Gauss-Seidel steps need a colour-ordered SELL level");
-  if (L.cta_chain && gs_chain_cta_ok(L, prec)) {
+  if (L.cta_chain > 1 && gs_chain_cluster_ok(L, prec, L.cta_chain)) {
+    const int cw = L.cta_chain;
+    if (prec == GMG_PREC_FP64) {
+      if (L.s == 1) return gs_chain_cluster<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw);
+      if (L.s == 2) return gs_chain_cluster<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw);
+      if (L.s == 3) return gs_chain_cluster<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw);
+    } else {
+      if (L.s == 1) return gs_chain_cluster<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw);
+      if (L.s == 2) return gs_chain_cluster<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw);
+      if (L.s == 3) return gs_chain_cluster<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw);
+    }
+  }
+  if (L.cta_chain == 1 && gs_chain_cta_ok(L, prec)) {
     if (prec == GMG_PREC_FP64) {
       if (L.s == 1) return gs_chain_cta<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps);
       if (L.s == 2) return gs_chain_cta<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps);

@@ -788,9 +788,11 @@ static int pick_tpr(const HostLevel &H) {
 // evict-first matrix stream where the matrix exceeds half of L2); on CSR
 // levels the threads per row.
 // Median of 3 timed chains after one warm-up, in the precision the V-cycle
-// uses (FP32 when the hierarchy has FP32 copies).  Levels that can run their
-// chained Gauss-Seidel steps in one thread block (gs_chain_cta_ok) also time
-// two chained steps both ways, as lmgc's pre-smoothing runs them.
+// uses (FP32 when the hierarchy has FP32 copies).  Levels that run chained
+// Gauss-Seidel steps also time two chained steps, as lmgc's pre-smoothing
+// runs them, as per-wave launches, in one thread block (gs_chain_cta_ok) and
+// in clusters of 2-16 blocks (gs_chain_cluster_ok); a form must be 5 %
+// faster than the best before it to be taken.
 static int autotune_level(gmg_mg *mg, Level &L) {
   if (L.n < 256) return 0;
   const int prec = mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64;
@@ -825,13 +827,24 @@ static int autotune_level(gmg_mg *mg, Level &L) {
     return ts[ts.size() / 2];
   };
   auto time_it = [&]() -> float { return time_op([&]() { return k_matmul_minus(mg, L, prec, x, y, nullptr); }); };
-  if (gs_chain_cta_ok(L, prec)) {
+  std::vector<int> forms;
+  for (int cw : {1, 2, 4, 8, 16})
+    if (cw == 1 ? gs_chain_cta_ok(L, prec) : gs_chain_cluster_ok(L, prec, cw)) forms.push_back(cw);
+  if (!forms.empty()) {
     auto chain = [&]() { return k_gs_chain(mg, L, prec, x, y, z, 2); };
     L.cta_chain = 0;
-    const float waves_ms = time_op(chain);
-    L.cta_chain = 1;
-    const float cta_ms = time_op(chain);
-    L.cta_chain = cta_ms < 0.95f * waves_ms;
+    float best = time_op(chain);
+    int pick = 0;
+    for (int cw : forms) {
+      L.cta_chain = cw;
+      const float ms = time_op(chain);
+      if (ms < 0.95f * best) {
+        best = ms;
+        pick = cw;
+      }
+    }
+    L.cta_chain = pick;
+    if (pick > 1) gs_chain_cluster_ok(L, GMG_PREC_FP64, pick);
   }
   float best_ms = 1e30f;
   if (L.sell) {
@@ -975,6 +988,8 @@ static int upload_level(HostLevel &h, int nc, bool f32, Level &L) {
   if (!h.sptr.empty()) {
     L.sell = true;
     L.sell_nent = h.sptr.back();
+    L.sell_wmax = 0;
+    for (size_t q = 0; q + 1 < h.sptr.size(); ++q) L.sell_wmax = std::max(L.sell_wmax, (h.sptr[q + 1] - h.sptr[q]) / 32);
     L.sell_ptr = ar.take_n<int>(h.sptr.size());
     L.sell_col = ar.take_n<int>(h.scol.size());
     L.sell_v64 = ar.take_n<double>(h.sval.size());
@@ -1303,18 +1318,30 @@ int gmg_mg_level_cta_chain(const gmg_mg *mg, int level, int *on) {
 }
 
 int gmg_mg_set_level_cta_chain(gmg_mg *mg, int level, int on) {
-  if (!mg || level < 0 || level >= int(mg->lev.size()) || (on != 0 && on != 1)) {
+  if (!mg || level < 0 || level >= int(mg->lev.size()) ||
+      !(on == 0 || on == 1 || on == 2 || on == 4 || on == 8 || on == 16)) {
     set_error("gmg_mg_set_level_cta_chain: bad arguments");
     return 1;
   }
   Level &L = mg->lev[level];
-  if (on && !gs_chain_cta_ok(L, mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64)) {
+  const int prec = mg->opts.fp32_copy ? GMG_PREC_FP32 : GMG_PREC_FP64;
+  if (on == 1 && !gs_chain_cta_ok(L, prec)) {
     set_error("gmg_mg_set_level_cta_chain: level %d cannot run its chained steps in one thread block "
               "(needs a multicolour sliced-ELLPACK level, all rows active, at most %d colours, t and c in %lld "
               "bytes of shared memory)",
               level, CTA_CHAIN_MAXW, CTA_CHAIN_SMEM);
     return 1;
   }
+  if (on > 1 && !gs_chain_cluster_ok(L, prec, on)) {
+    set_error("gmg_mg_set_level_cta_chain: level %d cannot run its chained steps in one cluster of %d thread "
+              "blocks (needs a multicolour sliced-ELLPACK level, all rows active, at most %d colours, t and the "
+              "c slots in %lld bytes of shared memory per block, and a device that co-schedules the cluster)",
+              level, on, CTA_CHAIN_MAXW, CLUSTER_CHAIN_SMEM);
+    return 1;
+  }
+  // the FP64 cycle of a mixed hierarchy dispatches on its own fit; decide it
+  // here, outside any graph capture
+  if (on > 1) gs_chain_cluster_ok(L, GMG_PREC_FP64, on);
   L.cta_chain = on;
   return 0;
 }
