@@ -176,6 +176,35 @@ def test_numproc_status_and_errors(G):
     mg.close()
 
 
+def test_vectors_of_another_multigrid_are_refused(G):
+    """The BLAS entries and the numproc function-table entries refuse a
+    missing vector and a vector of another hierarchy (whose levels and
+    lengths differ) instead of handing its pointers to a kernel."""
+    fx = load_golden("q1_jac")
+    mg, _ = _setup(G, fx, 0)
+    other, _ = _setup(G, fx, 0)
+    mg.createvector("sol", "rhs")
+    other.createvector("sol")
+    L = G.lib()
+    assert L.gmg_dset(mg._h, mg.top, other.vec("sol"), 1.0) != 0
+    assert b"another multigrid" in L.gmg_last_error()
+    assert L.gmg_dset(mg._h, mg.top, None, 1.0) != 0
+    assert b"vector missing" in L.gmg_last_error()
+    assert L.gmg_dcopy(mg._h, mg.top, mg.vec("sol"), other.vec("sol")) != 0
+    assert L.gmg_dnrm2x(mg._h, mg.top, other.vec("sol"), None) != 0
+    G.setup_lmgc(mg, "jac", baselevel=2)
+    assert L.gmg_iter_iter(mg.np("lmgc"), mg.top, other.vec("sol"), mg.vec("rhs"), mg.mat(), None) != 0
+    assert b"another multigrid" in L.gmg_last_error()
+    assert L.gmg_ls_defect(mg.np("mgs"), mg.top, mg.vec("sol"), None, mg.mat(), None) != 0
+    assert b"vector missing" in L.gmg_last_error()
+    # the hierarchy still solves afterwards
+    mg.upload("rhs", mg.top, fx["rhs"])
+    mg.npexecute("mgs", "$i $d $r $s $p")
+    assert rel(mg.download("sol", mg.top), fx["ls_x"]) <= 1e-10
+    mg.close()
+    other.close()
+
+
 def test_full_size_q1_jacobi(G, oracle_mod):
     """2D Q1 Poisson 257x257 (66,049 unknowns), V(2,2) jac 0.8, base 4x4, red 1e-10."""
     gen = G.Generator(0, 8, seed=1)

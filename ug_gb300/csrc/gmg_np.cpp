@@ -5,6 +5,7 @@
 // multigrid's stream.  Nothing here synchronises with the device except the
 // ls convergence test (one 8-byte-per-component read per iteration) and the
 // explicit upload / download calls.
+#include <initializer_list>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1921,6 +1922,26 @@ int gmg_np_display(gmg_np *np, char *buf, int buflen) {
   return 0;
 }
 
+static int check_vecs(const gmg_mg *mg, const char *fn, std::initializer_list<const gmg_vec *> vs, bool optional) {
+  for (const gmg_vec *v : vs) {
+    if (!v) {
+      if (optional) continue;
+      set_error("%s: vector missing", fn);
+      return 1;
+    }
+    if (v->mg != mg) {
+      set_error("%s: vector of another multigrid", fn);
+      return 1;
+    }
+  }
+  return 0;
+}
+// vectors of a numproc's multigrid, required / or left out (nullptr)
+#define NP_VECS(...) \
+  if (check_vecs(p->mg, __func__, {__VA_ARGS__}, false)) return 1;
+#define NP_VECS_OPT(...) \
+  if (check_vecs(p->mg, __func__, {__VA_ARGS__}, true)) return 1;
+
 // the function-table entries take a numproc of their class whose init
 // found its partners ($I, $S, $T; status NP_ACTIVE or NP_EXECUTABLE), as
 // UG's parents only call numprocs that initialised
@@ -1935,11 +1956,13 @@ int gmg_np_display(gmg_np *np, char *buf, int buflen) {
 
 int gmg_iter_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *bl, int *result) {
   AS(NPIter, np, NPK_ITER);
+  NP_VECS_OPT(x, b)
   int dummy;
   return p->PreProcess(level, x, b, A, bl ? bl : &dummy, result ? result : &dummy);
 }
 int gmg_iter_iter(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPIter, np, NPK_ITER);
+  NP_VECS(c, b)
   int dummy;
   return p->Iter(level, c, b, A, result ? result : &dummy);
 }
@@ -1953,69 +1976,83 @@ int gmg_iter_smooth(gmg_np *np, int level, gmg_vec *t, gmg_vec *b, gmg_mat *A, g
 }
 int gmg_iter_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPIter, np, NPK_ITER);
+  NP_VECS_OPT(x, b)
   int dummy;
   return p->PostProcess(level, x, b, A, result ? result : &dummy);
 }
 int gmg_transfer_preprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS_OPT(x, b)
   int dummy = 0, f0 = 0;
   return p->PreProcess(fl ? fl : &f0, tl, x, b, A, result ? result : &dummy);
 }
 int gmg_transfer_restrict_defect(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A, const double *damp,
                                  int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS(to, from)
   int dummy;
   return p->RestrictDefect(level, to, from, A, damp ? damp : p->damp, result ? result : &dummy);
 }
 int gmg_transfer_interpolate_correction(gmg_np *np, int level, gmg_vec *to, gmg_vec *from, gmg_mat *A,
                                         const double *damp, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS(to, from)
   int dummy;
   return p->InterpolateCorrection(level, to, from, A, damp ? damp : p->damp, result ? result : &dummy);
 }
 int gmg_transfer_interpolate_new_vectors(gmg_np *np, int fl, int tl, gmg_vec *x, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS(x)
   int dummy = 0;
   return p->InterpolateNewVectors(fl, tl, x, result ? result : &dummy);
 }
 int gmg_transfer_project_solution(gmg_np *np, int fl, int tl, gmg_vec *x, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS(x)
   int dummy = 0;
   return p->ProjectSolution(fl, tl, x, result ? result : &dummy);
 }
 int gmg_transfer_adapt_correction(gmg_np *np, int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS_OPT(c, b)
   int dummy = 0;
   return p->AdaptCorrection(level, c, b, A, result ? result : &dummy);
 }
 int gmg_transfer_postprocess(gmg_np *np, int *fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPTransfer, np, NPK_TRANSFER);
+  NP_VECS_OPT(x, b)
   int dummy = 0, f0 = 0;
   return p->PostProcess(fl ? fl : &f0, tl, x, b, A, result ? result : &dummy);
 }
 int gmg_ls_preprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *bl, int *result) {
   AS(NPLinearSolver, np, NPK_LS);
+  NP_VECS_OPT(x, b)
   int dummy = 0;
   return p->PreProcess(level, x, b, A, bl ? bl : &dummy, result ? result : &dummy);
 }
 int gmg_ls_defect(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPLinearSolver, np, NPK_LS);
+  NP_VECS(x, b)
   int dummy;
   return p->Defect(level, x, b, A, result ? result : &dummy);
 }
 int gmg_ls_residuum(gmg_np *np, int fl, int tl, gmg_vec *x, gmg_vec *b, gmg_mat *A, gmg_lresult *lr) {
   AS(NPLinearSolver, np, NPK_LS);
+  NP_VECS(b)
+  NP_VECS_OPT(x)
   GMG_CHECK(lr, "gmg_ls_residuum: lr is NULL");
   return p->Residuum(fl, tl, x, b, A, lr);
 }
 int gmg_ls_solver(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, const double *abslimit,
                   const double *reduction, gmg_lresult *lr) {
   AS(NPLinearSolver, np, NPK_LS);
+  NP_VECS(x, b)
   GMG_CHECK(lr, "gmg_ls_solver: lr is NULL");
   return p->Solver(level, x, b, A, abslimit ? abslimit : p->abslimit, reduction ? reduction : p->reduction, lr);
 }
 int gmg_ls_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) {
   AS(NPLinearSolver, np, NPK_LS);
+  NP_VECS_OPT(x, b)
   int dummy;
   return p->PostProcess(level, x, b, A, result ? result : &dummy);
 }
@@ -2024,23 +2061,31 @@ int gmg_ls_postprocess(gmg_np *np, int level, gmg_vec *x, gmg_vec *b, gmg_mat *A
 #define MGV(mg, level)                                        \
   if (!mg) { set_error("%s: no multigrid", __func__); return 1; } \
   if (check_level(mg, level)) return 1;
+// the vectors an entry works on: present and of this multigrid (a vector of
+// another hierarchy has other levels and lengths)
+#define VECS(...) \
+  if (check_vecs(mg, __func__, {__VA_ARGS__}, false)) return 1;
 
 int gmg_dset(gmg_mg *mg, int level, gmg_vec *x, double a) {
   MGV(mg, level);
+  VECS(x)
   return k_set(mg, x->prec, vlev(x, level), vlen(mg, level), a);
 }
 int gmg_dcopy(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y) {
   MGV(mg, level);
+  VECS(x, y)
   return k_convert(mg, x->prec, vlev(x, level), y->prec, vlev(y, level), vlen(mg, level));
 }
 int gmg_dadd(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y) {
   MGV(mg, level);
+  VECS(x, y)
   if (x->prec == GMG_PREC_FP64) return k_add_mixed(mg, (double *)vlev(x, level), y->prec, vlev(y, level), vlen(mg, level));
   GMG_CHECK(y->prec == x->prec, "dadd: precision mismatch");
   return k_add(mg, x->prec, vlev(x, level), vlev(y, level), vlen(mg, level));
 }
 int gmg_dmatmul_minus(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) {
   MGV(mg, level);
+  VECS(x, y)
   if (x->prec == GMG_PREC_FP64) return k_matmul_minus_mixed(mg, mg->lev[level], (double *)vlev(x, level), y->prec, vlev(y, level));
   GMG_CHECK(y->prec == x->prec, "dmatmul_minus: precision mismatch");
   return k_matmul_minus(mg, mg->lev[level], x->prec, vlev(x, level), vlev(y, level), nullptr);
@@ -2057,15 +2102,18 @@ static int matmul_op(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, int op) {
 }
 int gmg_dmatmul(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) {
   MGV(mg, level);
+  VECS(x, y)
   return matmul_op(mg, level, x, y, 3);
 }
 int gmg_dmatmul_add(gmg_mg *mg, int level, gmg_vec *x, gmg_mat *, gmg_vec *y) {
   MGV(mg, level);
+  VECS(x, y)
   return matmul_op(mg, level, x, y, 1);
 }
 // dscalx, ugblas.cc:2510: x *= a per component
 int gmg_dscalx(gmg_mg *mg, int level, gmg_vec *x, const double *a) {
   MGV(mg, level);
+  VECS(x)
   GMG_CHECK(a, "dscalx: no factors");
   double f[GMG_MAX_S];
   for (int r = 0; r < GMG_MAX_S; ++r) f[r] = r < mg->lev[level].s ? a[r] : 1.0;
@@ -2074,12 +2122,14 @@ int gmg_dscalx(gmg_mg *mg, int level, gmg_vec *x, const double *a) {
 // daxpyx, ugblas.cc:2875: x += a y per component
 int gmg_daxpy(gmg_mg *mg, int level, gmg_vec *x, const double *a, gmg_vec *y) {
   MGV(mg, level);
+  VECS(x, y)
   GMG_CHECK(a && x->prec == y->prec, "daxpy: no factors or precision mismatch");
   return k_axpy(mg, x->prec, vlev(x, level), vlev(y, level), mg->lev[level].n, mg->lev[level].s, a);
 }
 // ddot, ugblas.cc:3104: the sum over every row and component (FP64)
 int gmg_ddot(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, double *result) {
   MGV(mg, level);
+  VECS(x, y)
   GMG_CHECK(result && x->prec == GMG_PREC_FP64 && y->prec == GMG_PREC_FP64, "ddot: FP64 vectors and a result");
   SurfLevels t;
   surf_table(mg, level, level, level, t);
@@ -2095,6 +2145,7 @@ int gmg_ddot(gmg_mg *mg, int level, gmg_vec *x, gmg_vec *y, double *result) {
 }
 int gmg_dnrm2x(gmg_mg *mg, int level, gmg_vec *x, double *norms) {
   MGV(mg, level);
+  VECS(x)
   if (k_nrm2x(mg, mg->lev[level], x->prec, vlev(x, level))) return 1;
   GMG_CUDA(cudaMemcpyAsync(mg->norms_host, mg->norms_dev, sizeof(double) * mg->lev[level].s, cudaMemcpyDeviceToHost, mg->stream));
   GMG_CUDA(cudaStreamSynchronize(mg->stream));
@@ -2103,11 +2154,13 @@ int gmg_dnrm2x(gmg_mg *mg, int level, gmg_vec *x, double *norms) {
 }
 int gmg_l_jac(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
   MGV(mg, level);
+  VECS(v, d)
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
   return k_jac(mg, mg->lev[level], v->prec, vlev(v, level), vlev(d, level), one);
 }
 int gmg_l_lgs(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
   MGV(mg, level);
+  VECS(v, d)
   return k_gs(mg, mg->lev[level], v->prec, vlev(v, level), vlev(d, level));
 }
 int gmg_l_ilu_decomp(gmg_mg *mg, int level, gmg_mat *, const double *beta) {
@@ -2131,10 +2184,12 @@ int gmg_l_ilu_factors(gmg_mg *mg, int level, double *lu) {
 }
 int gmg_l_luiter(gmg_mg *mg, int level, gmg_vec *v, gmg_mat *, gmg_vec *d) {
   MGV(mg, level);
+  VECS(v, d)
   return k_luiter(mg, mg->lev[level], v->prec, vlev(v, level), vlev(d, level));
 }
 int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
   MGV(mg, level);
+  VECS(to, from)
   GMG_CHECK(level >= 1, "no coarser grid");
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
   return k_restrict(mg, mg->lev[level], mg->lev[level - 1], to->prec, vlev(to, level - 1), vlev(from, level),
@@ -2142,6 +2197,7 @@ int gmg_standard_restrict(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, con
 }
 int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
   MGV(mg, level);
+  VECS(to, from)
   GMG_CHECK(level >= 1, "no coarser grid");
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
   return k_interpolate(mg, mg->lev[level], to->prec, vlev(to, level), vlev(from, level - 1), damp ? damp : one, nullptr);
@@ -2149,6 +2205,7 @@ int gmg_standard_interpolate_correction(gmg_mg *mg, int level, gmg_vec *to, gmg_
 
 int gmg_restrict_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
   MGV(mg, level);
+  VECS(to, from)
   GMG_CHECK(level >= 1, "no coarser grid");
   GMG_CHECK(to && from && to->prec == from->prec, "RestrictByMatrix: vectors missing or of different precision");
   static const double one[GMG_MAX_S] = {1, 1, 1, 1, 1, 1, 1, 1};
@@ -2157,6 +2214,7 @@ int gmg_restrict_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, co
 }
 int gmg_interpolate_correction_by_matrix(gmg_mg *mg, int level, gmg_vec *to, gmg_vec *from, const double *damp) {
   MGV(mg, level);
+  VECS(to, from)
   GMG_CHECK(level >= 1, "no coarser grid");
   GMG_CHECK(to && from && to->prec == from->prec,
             "InterpolateCorrectionByMatrix: vectors missing or of different precision");
