@@ -95,6 +95,7 @@ struct Level {
   int n = 0, s = 1;
   long long nnzb = 0;
   bool all_active = true;   // every row ACTIVE
+  bool all_reset = true;    // every row F_RESET: a restriction into the level overwrites all of its b
   bool any_skip = false;
   // host copies in processing order
   std::vector<int> perm;       // perm[i] = UG list position of processed row i
@@ -386,7 +387,9 @@ int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);
 // defect on return, t the last step's correction.  gs_chain_ok: the level
 // qualifies (sliced ELLPACK, colour-contiguous waves, every row ACTIVE)
 bool gs_chain_ok(const Level &L, int prec);
-int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps);
+// want_b false: the caller never reads the final defect (lmgc's post-smoothing
+// where the next restriction overwrites b), so it is not computed
+int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps, bool want_b = true);
 // the chained steps of a level in one thread block (Level::cta_chain = 1):
 // at most CTA_CHAIN_MAXW waves, t and c of the level in shared memory
 constexpr int CTA_CHAIN_MAXW = 48;
@@ -394,6 +397,7 @@ constexpr long long CTA_CHAIN_SMEM = 200 * 1024;
 struct CtaWaves {
   int n, nwave, steps;
   int own, wm;  // cluster form: slots of the block with the most rows; stored off-diagonal entries a row
+  int want_b;   // write the final defect b = -U t
   int ptr[CTA_CHAIN_MAXW + 1];
 };
 long long gs_chain_cta_smem(const Level &L, int prec);

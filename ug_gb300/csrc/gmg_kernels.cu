@@ -642,8 +642,8 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_c
       __syncthreads();
     }
   }
-  // b = -U t, then t and c back to global memory
-  for (int i = tid; i < W.n; i += NT) {
+  // b = -U t (unless the caller never reads it), then t and c back to global memory
+  for (int i = tid; W.want_b && i < W.n; i += NT) {
     R.load(i, 2, sptr, nl, scol, sval);
     T s[S];
 #pragma unroll
@@ -911,8 +911,9 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cluster_kernel(const __gr
       cluster_wait();
     }
   }
-  // b = -U t on the block's rows; t and c back to global memory
-  for (int q = tid; q < nown; q += NT) {
+  // b = -U t on the block's rows (unless the caller never reads it); t and c
+  // back to global memory
+  for (int q = tid; W.want_b && q < nown; q += NT) {
     const int i = slot_row(q);
     load_row(q, 2);
     T s[S];
@@ -2893,7 +2894,7 @@ int sell_gs_waves(gmg_mg *mg, const Level &L, T *t, const T *b) {
 }
 
 template <class T, int S>
-int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
+int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps, bool want_b) {
   const T *sv = sell_val<T>(L), *dinv = dinv_of<T>(L);
   const uint8_t *nl = L.sell_split ? L.sell_nl : nullptr;
   for (int st = 0; st < steps; ++st) {
@@ -2916,6 +2917,7 @@ int gs_chain(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
       LAUNCH_CHECK(mg);
     }
   }
+  if (!want_b) return 0;
   const unsigned g = grid_for(L.n);
   if (use_prefetch(L, g))
     GMG_LAUNCH((sell_upper_defect_kernel<T, S, PF<S>::N>), g, BLK, L.n, L.sell_ptr, nl, L.sell_col, sv, t, b);
@@ -2938,12 +2940,13 @@ bool gs_chain_cta_ok(const Level &L, int prec) {
 }
 
 template <class T, int S>
-static int gs_chain_cta(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps) {
+static int gs_chain_cta(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps, bool want_b) {
   constexpr int NT = S == 1 && sizeof(T) == 4 ? 1024 : 512;  // 64 / 128 registers a thread
   CtaWaves W{};
   W.n = L.n;
   W.nwave = L.lower.nwave();
   W.steps = steps;
+  W.want_b = want_b;
   for (int w = 0; w <= W.nwave; ++w) W.ptr[w] = L.lower.ptr[w];
   const int smem = int(gs_chain_cta_smem(L, sizeof(T) == 8 ? GMG_PREC_FP64 : GMG_PREC_FP32));
   auto kern = sell_gs_chain_cta_kernel<T, S, PF<S>::N, NT>;
@@ -3075,7 +3078,7 @@ bool gs_chain_cluster_ok(const Level &L, int prec, int cw) {
 }
 
 template <class T, int S>
-static int gs_chain_cluster(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps, int cw) {
+static int gs_chain_cluster(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int steps, int cw, bool want_b) {
   constexpr int NT = cluster_chain_nt<T, S>();
   int smem = 0;
   const int form = cluster_chain_form(L, sizeof(T) == 8 ? GMG_PREC_FP64 : GMG_PREC_FP32, cw, &smem);
@@ -3085,6 +3088,7 @@ static int gs_chain_cluster(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int st
   W.nwave = L.lower.nwave();
   W.steps = steps;
   W.own = cluster_chain_own(L, cw);
+  W.want_b = want_b;
   W.wm = std::max(L.sell_wmax - 1, 0);
   for (int w = 0; w <= W.nwave; ++w) W.ptr[w] = L.lower.ptr[w];
   cudaLaunchConfig_t cfg = {};
@@ -3112,39 +3116,39 @@ static int gs_chain_cluster(gmg_mg *mg, const Level &L, T *t, T *b, T *c, int st
   return 0;
 }
 
-int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps) {
+int k_gs_chain(gmg_mg *mg, const Level &L, int prec, void *t, void *b, void *c, int steps, bool want_b) {
   GMG_CHECK(gs_chain_ok(L, prec) && steps >= 1, "chained Gauss-Seidel steps need a colour-ordered SELL level");
   if (L.cta_chain > 1 && gs_chain_cluster_ok(L, prec, L.cta_chain)) {
     const int cw = L.cta_chain;
     if (prec == GMG_PREC_FP64) {
-      if (L.s == 1) return gs_chain_cluster<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw);
-      if (L.s == 2) return gs_chain_cluster<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw);
-      if (L.s == 3) return gs_chain_cluster<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw);
+      if (L.s == 1) return gs_chain_cluster<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw, want_b);
+      if (L.s == 2) return gs_chain_cluster<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw, want_b);
+      if (L.s == 3) return gs_chain_cluster<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps, cw, want_b);
     } else {
-      if (L.s == 1) return gs_chain_cluster<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw);
-      if (L.s == 2) return gs_chain_cluster<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw);
-      if (L.s == 3) return gs_chain_cluster<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw);
+      if (L.s == 1) return gs_chain_cluster<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw, want_b);
+      if (L.s == 2) return gs_chain_cluster<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw, want_b);
+      if (L.s == 3) return gs_chain_cluster<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps, cw, want_b);
     }
   }
   if (L.cta_chain == 1 && gs_chain_cta_ok(L, prec)) {
     if (prec == GMG_PREC_FP64) {
-      if (L.s == 1) return gs_chain_cta<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps);
-      if (L.s == 2) return gs_chain_cta<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps);
-      if (L.s == 3) return gs_chain_cta<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+      if (L.s == 1) return gs_chain_cta<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps, want_b);
+      if (L.s == 2) return gs_chain_cta<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps, want_b);
+      if (L.s == 3) return gs_chain_cta<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps, want_b);
     } else {
-      if (L.s == 1) return gs_chain_cta<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps);
-      if (L.s == 2) return gs_chain_cta<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps);
-      if (L.s == 3) return gs_chain_cta<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+      if (L.s == 1) return gs_chain_cta<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps, want_b);
+      if (L.s == 2) return gs_chain_cta<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps, want_b);
+      if (L.s == 3) return gs_chain_cta<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps, want_b);
     }
   }
   if (prec == GMG_PREC_FP64) {
-    if (L.s == 1) return gs_chain<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps);
-    if (L.s == 2) return gs_chain<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps);
-    if (L.s == 3) return gs_chain<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps);
+    if (L.s == 1) return gs_chain<double, 1>(mg, L, (double *)t, (double *)b, (double *)c, steps, want_b);
+    if (L.s == 2) return gs_chain<double, 2>(mg, L, (double *)t, (double *)b, (double *)c, steps, want_b);
+    if (L.s == 3) return gs_chain<double, 3>(mg, L, (double *)t, (double *)b, (double *)c, steps, want_b);
   } else {
-    if (L.s == 1) return gs_chain<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps);
-    if (L.s == 2) return gs_chain<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps);
-    if (L.s == 3) return gs_chain<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps);
+    if (L.s == 1) return gs_chain<float, 1>(mg, L, (float *)t, (float *)b, (float *)c, steps, want_b);
+    if (L.s == 2) return gs_chain<float, 2>(mg, L, (float *)t, (float *)b, (float *)c, steps, want_b);
+    if (L.s == 3) return gs_chain<float, 3>(mg, L, (float *)t, (float *)b, (float *)c, steps, want_b);
   }
   set_error("block size %d not compiled", L.s);
   return 1;

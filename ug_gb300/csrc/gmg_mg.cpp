@@ -568,7 +568,7 @@ struct HostLevel {
   std::vector<int> lptr, lrows, uptr, urows;
   std::vector<int> prow, pcol, rrow, rcol;
   std::vector<double> pw, rw;
-  bool all_active = true, any_skip = false, contiguous = false;
+  bool all_active = true, all_reset = true, any_skip = false, contiguous = false;
   int ncolour = 0;
   // subdomain order: per-subdomain interior waves (forward / backward), interface colours
   int dom_nreg = 0, dom_nint = 0;
@@ -702,7 +702,7 @@ static int build_host_level(const gmg_level_desc &d, int order, HostLevel &H,
     uint8_t f = 0;
     if (vc >= 3) f |= F_ACTIVE; else H.all_active = false;
     if (vc >= 2) f |= F_NEWDEF;
-    if (vn >= 2) f |= F_RESET;
+    if (vn >= 2) f |= F_RESET; else H.all_reset = false;
     if (vc >= 2 && vn <= 1) f |= F_FINE;
     H.flags[i] = f;
     H.skip[i] = uint8_t(sk & 0xff);
@@ -932,7 +932,7 @@ static int upload_level(HostLevel &h, int nc, bool f32, Level &L) {
   Arena &ar = L.arena;
   if (ar.alloc(bytes)) return 1;
   L.n = h.n; L.s = s; L.nnzb = nnz;
-  L.all_active = h.all_active; L.any_skip = h.any_skip;
+  L.all_active = h.all_active; L.all_reset = h.all_reset; L.any_skip = h.any_skip;
   L.A.nrows = h.n; L.A.nnz = nnz;
   L.A.rowptr = ar.take_n<int>(h.n + 1);
   L.A.col = ar.take_n<int>(nnz);

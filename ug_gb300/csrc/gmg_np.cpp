@@ -172,7 +172,8 @@ int NPIter::IterAcc(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, gmg_vec *a
   return k_add(mg, acc->prec, vlev(acc, level), vlev(cv, level), vlen(mg, level));
 }
 
-int NPIter::IterAccN(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result) {
+int NPIter::IterAccN(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result,
+                     bool) {
   for (int i = 0; i < steps; ++i)
     if (IterAcc(level, cv, bv, Am, acc, result)) return 1;
   return 0;
@@ -247,7 +248,8 @@ int NPJac::IterAcc(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc
   return k_matmul_minus(mg, L, x->prec, vlev(bv, level), vlev(x, level), vlev(acc, level));
 }
 
-int NPJac::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result) {
+int NPJac::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result,
+                    bool) {
   if (check_level(mg, level)) return 1;
   // FP32 only: recomputing D^{-1} b per stored entry triples the FP64
   // arithmetic per entry, and GB300's FP64 rate makes that slower than the
@@ -271,14 +273,15 @@ int NPGs::Step(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *, int *) {
   return k_gs(mg, mg->lev[level], x->prec, vlev(x, level), vlev(bv, level));
 }
 
-int NPGs::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result) {
+int NPGs::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result,
+                   bool want_b) {
   if (check_level(mg, level)) return 1;
   const Level &L = mg->lev[level];
   bool unit = true;
   for (int r = 0; r < L.s; ++r) unit = unit && damp[r] == 1.0;
   if (!unit || steps < 2 || acc->prec != x->prec || bv->prec != x->prec || !gs_chain_ok(L, x->prec))
     return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
-  return k_gs_chain(mg, L, x->prec, vlev(x, level), vlev(bv, level), vlev(acc, level), steps);
+  return k_gs_chain(mg, L, x->prec, vlev(x, level), vlev(bv, level), vlev(acc, level), steps, want_b);
 }
 
 // ilu: ILUInit (iter.cc:5415) reads $beta (and $mindiag, unused by the decomposition)
@@ -743,6 +746,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   if (check_level(mg, level)) return 1;
   GMG_CHECK(cv->prec == bv->prec, "lmgc: c and b differ in precision");
   const int prec = cv->prec;
+  const bool b_unused = defect_unused;
   if (level <= baselevel) {
     NPLs *bls = dynamic_cast<NPLs *>(BaseSolver);
     if (bls && bls->is_exact_base()) {
@@ -786,8 +790,17 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
     if (Transfer->RestrictDefect(level, bv, bv, Am, one, result)) return 1;
     if (k_set(mg, prec, vlev(cv, level - 1), vlen(mg, level - 1), 0.0)) return 1;
   }
-  for (int i = 0; i < gamma; ++i)
-    if (Iter(level - 1, cv, bv, Am, result)) return 1;
+  // the defect the last coarse recursion leaves is never read when the next
+  // restriction overwrites all of it (StandardRestrict onto rows that all
+  // reset, one hierarchy, not surface-based): its post-smoothing may skip it
+  const bool coarse_b_dead = typeid(*Transfer) == typeid(NPTransfer) && !Transfer->imat && !mg->local() &&
+                             mg->batch.ninst == 0 && mg->lev[level - 1].all_reset;
+  for (int i = 0; i < gamma; ++i) {
+    defect_unused = coarse_b_dead && i == gamma - 1;
+    const int rc = Iter(level - 1, cv, bv, Am, result);
+    defect_unused = b_unused;
+    if (rc) return 1;
+  }
   // t = P c_{l-1} * damp; c += t (fused); b -= A t
   if (dynamic_cast<NPTransfer *>(Transfer) && typeid(*Transfer) == typeid(NPTransfer)) {
     if (Transfer->imat ? k_interpolate_imat(mg, mg->lev[level], prec, vlev(t, level), vlev(cv, level - 1), damp,
@@ -800,7 +813,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
     if (k_add(mg, prec, vlev(cv, level), vlev(t, level), vlen(mg, level))) return 1;
   }
   if (k_matmul_minus(mg, mg->lev[level], prec, vlev(bv, level), vlev(t, level), nullptr)) return 1;
-  if (PostSmooth->IterAccN(level, t, bv, Am, cv, nu2, result)) return 1;
+  if (PostSmooth->IterAccN(level, t, bv, Am, cv, nu2, result, !b_unused)) return 1;
   return 0;
 }
 
@@ -1098,7 +1111,12 @@ int NPLs::iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int *err) 
     if (k_refine_prepare(mg, (float *)vlev(b32, level), (float *)vlev(cvec, level), (const double *)vlev(bv, level),
                          len))
       return 1;
-    if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    // the FP32 defect the cycle leaves is rebuilt from the FP64 one next time
+    NPLmgc *lm = dynamic_cast<NPLmgc *>(IterNp);
+    if (lm) lm->defect_unused = true;
+    const int rc = IterNp->Iter(level, cvec, b32, Am, err);
+    if (lm) lm->defect_unused = false;
+    if (rc) return 1;
     if (k_refine_update(mg, L, (double *)vlev(bv, level), (double *)vlev(xv, level), (const float *)vlev(cvec, level)))
       return 1;
   }

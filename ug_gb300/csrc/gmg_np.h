@@ -57,8 +57,11 @@ struct NPIter : gmg_np {
   // Iter followed by acc += c (lmgc's dadd after each smoothing step);
   // smoothers fuse the addition into their defect update
   virtual int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result);
-  // `steps` of IterAcc in a row (lmgc's nu1 / nu2 smoothing loops)
-  virtual int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result);
+  // `steps` of IterAcc in a row (lmgc's nu1 / nu2 smoothing loops); want_b
+  // false: the caller never reads b afterwards, which a smoother may then
+  // leave without its final defect update
+  virtual int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result,
+                       bool want_b = true);
   int Execute(const Args &a) override;  // NPIterExecute, iter.cc:702
   std::string Display() const override;
 };
@@ -78,14 +81,17 @@ struct NPJac : NPSmoother {  // jac, iter.cc:894-942
   int Iter(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, int *result) override;
   int IterAcc(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int *result) override;
   // each step one fused kernel, the defect alternating between b and a scratch copy
-  int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result) override;
+  int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result,
+               bool want_b = true) override;
 };
 
 struct NPGs : NPSmoother {  // gs, iter.cc:974-1086
   int Step(int level, gmg_vec *x, gmg_vec *b, gmg_mat *A, int *result) override;
   // on colour-ordered sliced-ELLPACK levels with unit damping: the steps
   // chained, one launch per colour and step plus one for the final defect
-  int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result) override;
+  // (left out when the caller does not want it)
+  int IterAccN(int level, gmg_vec *c, gmg_vec *b, gmg_mat *A, gmg_vec *acc, int steps, int *result,
+               bool want_b = true) override;
 };
 
 struct NPIlu : NPSmoother {  // ilu, iter.cc:5383-5524
@@ -139,6 +145,11 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   // levels with at most fuse_rows VECTORs run as one fused kernel of one CTA
   // (gmg_coarse.cu); 0 disables
   int fuse_rows = 6000;
+  // the caller of the current Iter never reads the defect it leaves on its
+  // level (the parent's last coarse recursion of a V-cycle where the next
+  // restriction overwrites it; the top of a uniform mixed ls iteration,
+  // whose FP32 defect is rebuilt from the FP64 one)
+  bool defect_unused = false;
   int narrow = 1;  // $narrow 0: the fused cycle runs its smallest levels with the whole block
   // batched hierarchies: the fused cycle runs one block per instance, over
   // the levels whose largest instance image fits batch_smem bytes ($bsmem; 0 disables)
