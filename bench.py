@@ -549,7 +549,10 @@ def run_batched(args, stream, flush_l2, world, rank):
         "fp64_one_at_a_time": {"value": world * args.batch / solo_batch_s, "unit": "solves/s",
                                "sample": f"{len(sample)} instances solved one after another "
                                          f"({solo_per_s:.0f} instance solves/s), scaled to the batch by unknowns"},
+        # batching and precision together (the plain FP64 path, one instance at
+        # a time) / precision alone (both arms batched)
         "mixed_batched_over_fp64_one_at_a_time": solo_batch_s / (ms32 * 1e-3),
+        "mixed_over_fp64_batched": ms64 / ms32,
         "roofline_large_launch": roof_large,
         "h2d_bytes_per_batch": int(unknowns * 8), "d2h_bytes_per_batch": int(unknowns * 8),
     })
