@@ -1,7 +1,7 @@
 """The UG-side binding (ug_gb300/ug_glue/gpu_numprocs.cc) compiled into UG
 3.12.1 itself: oracle/Makefile builds it against UG's headers, links it with
 UG's library and libug_gb300 (oracle/_ref/ug_glue_test2d, part of the
-reference build), and the driver runs UG's own script commands on a 2D
+reference build), and that program runs UG's own script commands on a 2D
 hierarchy.  Checked here, on a host without a GPU: the classes register
 with CreateClass, `npcreate mgs $c gls` / `npinit ...` resolve to the
 forwarding classes (the objects are UG numprocs of those classes, status
