@@ -792,9 +792,11 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   }
   // the defect the last coarse recursion leaves is never read when the next
   // restriction overwrites all of it (StandardRestrict onto rows that all
-  // reset, one hierarchy, not surface-based): its post-smoothing may skip it
+  // reset, not surface-based; a batched level that is some instance's top
+  // keeps that instance's rows, VNCLASS < 2, so it never qualifies): its
+  // post-smoothing may skip it
   const bool coarse_b_dead = typeid(*Transfer) == typeid(NPTransfer) && !Transfer->imat && !mg->local() &&
-                             mg->batch.ninst == 0 && mg->lev[level - 1].all_reset;
+                             mg->lev[level - 1].all_reset;
   for (int i = 0; i < gamma; ++i) {
     defect_unused = coarse_b_dead && i == gamma - 1;
     const int rc = Iter(level - 1, cv, bv, Am, result);
@@ -1082,7 +1084,12 @@ int NPLs::batch_iteration(int level, gmg_vec *xv, gmg_vec *bv, gmg_mat *Am, int 
     if (k_batch_finish(mg, bv->prec, bv, xv, cvec->prec, cvec, false, s)) return 1;
   } else {
     if (k_batch_refine_prepare(mg, b32, cvec, bv)) return 1;
-    if (IterNp->Iter(level, cvec, b32, Am, err)) return 1;
+    // the FP32 defect the cycle leaves on the top is rebuilt from the FP64 one next time
+    NPLmgc *lm = dynamic_cast<NPLmgc *>(IterNp);
+    if (lm) lm->defect_unused = true;
+    const int rc = IterNp->Iter(level, cvec, b32, Am, err);
+    if (lm) lm->defect_unused = false;
+    if (rc) return 1;
     // the FP64 refinement defect reads c in FP64: one conversion per row
     // instead of one per stored entry (conversions run on GB300's FP64 pipe)
     if (k_batch_widen(mg, c64, cvec) || k_batch_finish(mg, GMG_PREC_FP64, bv, xv, GMG_PREC_FP64, c64, true, s))

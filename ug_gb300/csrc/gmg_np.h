@@ -147,8 +147,8 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   int fuse_rows = 6000;
   // the caller of the current Iter never reads the defect it leaves on its
   // level (the parent's last coarse recursion of a V-cycle where the next
-  // restriction overwrites it; the top of a uniform mixed ls iteration,
-  // whose FP32 defect is rebuilt from the FP64 one)
+  // restriction overwrites it; the top of a uniform or batched mixed ls
+  // iteration, whose FP32 defect is rebuilt from the FP64 one)
   bool defect_unused = false;
   int narrow = 1;  // $narrow 0: the fused cycle runs its smallest levels with the whole block
   // batched hierarchies: the fused cycle runs one block per instance, over
