@@ -249,18 +249,26 @@ int NPJac::IterAcc(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc
 }
 
 int NPJac::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result,
-                    bool) {
+                    bool want_b) {
   if (check_level(mg, level)) return 1;
+  const Level &L = mg->lev[level];
+  // without a reader of the final defect the last step only adds its
+  // correction to acc (the step's t is not kept either: lmgc's t is dead
+  // after its post-smoothing)
+  const bool last_acc_only = !want_b && steps >= 1 && acc->prec == bv->prec;
   // FP32 only: recomputing D^{-1} b per stored entry triples the FP64
   // arithmetic per entry, and GB300's FP64 rate makes that slower than the
   // two-pass step
-  if (x->prec != GMG_PREC_FP32 || acc->prec != x->prec || bv->prec != x->prec || steps < 2)
-    return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
+  if (x->prec != GMG_PREC_FP32 || acc->prec != x->prec || bv->prec != x->prec || steps < 2) {
+    if (!last_acc_only) return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
+    if (NPIter::IterAccN(level, x, bv, Am, acc, steps - 1, result)) return 1;
+    return k_jac_acc(mg, L, acc->prec, vlev(acc, level), vlev(bv, level), damp);
+  }
   gmg_vec *pp = temp_vec(mg, "__jac_pp" + std::to_string(x->prec), x->prec);
   GMG_CHECK(pp, "jac: temporary vector");
-  const Level &L = mg->lev[level];
   void *src = vlev(bv, level), *dst = vlev(pp, level);
   for (int i = 0; i < steps; ++i) {
+    if (i == steps - 1 && last_acc_only) return k_jac_acc(mg, L, x->prec, vlev(acc, level), src, damp);
     if (k_jac_step(mg, L, x->prec, dst, src, vlev(acc, level), damp)) return 1;
     std::swap(src, dst);
   }
