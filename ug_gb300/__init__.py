@@ -893,7 +893,7 @@ def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: in
                damp: float | None = None, red: float = 1e-10, abslimit: float = 1e-50, maxit: int = 100,
                mixed: bool = False, x: str = "sol", b: str = "rhs", name: str = "mgs",
                fuse: int | None = None, graph: bool = True, bsmem: int | None = None,
-               dloop: bool = True, narrow: bool = True, transfer: str = "") -> str:
+               dloop: bool = True, narrow: bool = True, transfer: str = "", defect: bool = False) -> str:
     """The standard script of the workloads, as UG numproc commands:
 
         npcreate transfer $c gtransfer; npcreate smooth $c g<smoother>;
@@ -915,6 +915,7 @@ def setup_lmgc(mg: MultiGrid, smoother: str = "jac", baselevel: int = 0, nu1: in
     mg.npcreate("lmgc", "iter.glmgc")
     fz = ("" if fuse is None else f" $fuse {int(fuse)}") + ("" if bsmem is None else f" $bsmem {int(bsmem)}")
     fz += "" if narrow else " $narrow 0"
+    fz += " $defect 1" if defect else ""
     mg.npinit("lmgc", f"$S smooth smooth basesolver $T transfer $n1 {nu1} $n2 {nu2} $b {baselevel}{fz}")
     mg.npcreate(name, "linear_solver.gls")
     st = mg.npinit(name, f"$A MAT $x {x} $b {b} $red {red} $abslimit {abslimit} $m {maxit} $I lmgc"

@@ -379,9 +379,6 @@ int k_refine_update(gmg_mg *mg, const Level &L, double *b, double *x, const floa
 int k_jac(gmg_mg *mg, const Level &L, int prec, void *t, const void *b, const double *damp);
 // one damped Jacobi smoothing step in one pass: t = damp D^{-1} bin (0 off
 // ACTIVE rows), bout = bin - A t, c += t (bout must not alias bin)
-// c += damp D^{-1} b on ACTIVE rows: a Jacobi step's correction without its
-// defect update (same bits as k_jac_step's c)
-int k_jac_acc(gmg_mg *mg, const Level &L, int prec, void *c, const void *b, const double *damp);
 int k_jac_step(gmg_mg *mg, const Level &L, int prec, void *bout, const void *bin, void *c, const double *damp);
 // forward Gauss-Seidel in processing order over the wavefronts; t is overwritten
 int k_gs(gmg_mg *mg, const Level &L, int prec, void *t, const void *b);

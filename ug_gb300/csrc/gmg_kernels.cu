@@ -1036,22 +1036,6 @@ __global__ void __launch_bounds__(BLK) sell_jac_step_kernel(int n, const int *__
   }
 }
 
-// The correction of one damped Jacobi step alone, c += damp D^{-1} b: the
-// last step of a smoothing whose final defect nothing reads.  jac_value's
-// arithmetic, so c is bit for bit that of the fused or two-pass step.
-template <class T, int S, bool ALL_ACTIVE>
-__global__ void __launch_bounds__(BLK) jac_acc_kernel(int n, const T *__restrict__ dinv,
-                                                      const uint8_t *__restrict__ flags, const T *__restrict__ b,
-                                                      T *__restrict__ c, Damp<T> dm) {
-  pdl_prologue();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  T ti[S];
-  jac_value<T, S, ALL_ACTIVE>(dinv, flags, b, i, dm, ti);
-#pragma unroll
-  for (int r = 0; r < S; ++r) c[(size_t)i * S + r] += ti[r];
-}
-
 template <class T, int S, int TPR, bool ALL_ACTIVE>
 __global__ void __launch_bounds__(BLK) jac_step_kernel(int n, const int *__restrict__ rowptr,
                                                        const int *__restrict__ col, const T *__restrict__ val,
@@ -2859,24 +2843,6 @@ int jac_step_dispatch(gmg_mg *mg, const Level &L, T *bout, const T *bin, T *c, D
 #undef CASE
     default: set_error("bad threads-per-row %d", L.tpr); return 1;
   }
-  LAUNCH_CHECK(mg);
-  return 0;
-}
-
-int k_jac_acc(gmg_mg *mg, const Level &L, int prec, void *c, const void *b, const double *damp) {
-  if (L.n == 0) return 0;
-#define JA(TT, SS, ALL)                                                                                    \
-  GMG_LAUNCH((jac_acc_kernel<TT, SS, ALL>), grid_for(L.n), BLK, L.n, dinv_of<TT>(L), L.flags, (const TT *)b, \
-             (TT *)c, make_damp<TT>(damp, SS))
-#define JS(TT)                                                                      \
-  if (L.s == 1) { if (L.all_active) JA(TT, 1, true); else JA(TT, 1, false); }       \
-  else if (L.s == 2) { if (L.all_active) JA(TT, 2, true); else JA(TT, 2, false); }  \
-  else if (L.s == 3) { if (L.all_active) JA(TT, 3, true); else JA(TT, 3, false); }  \
-  else { set_error("block size %d not compiled", L.s); return 1; }
-  if (prec == GMG_PREC_FP64) { JS(double) }
-  else { GMG_CHECK(L.dinv32, "FP32 copy not built"); JS(float) }
-#undef JS
-#undef JA
   LAUNCH_CHECK(mg);
   return 0;
 }

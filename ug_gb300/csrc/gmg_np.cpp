@@ -249,26 +249,18 @@ int NPJac::IterAcc(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc
 }
 
 int NPJac::IterAccN(int level, gmg_vec *x, gmg_vec *bv, gmg_mat *Am, gmg_vec *acc, int steps, int *result,
-                    bool want_b) {
+                    bool) {
   if (check_level(mg, level)) return 1;
-  const Level &L = mg->lev[level];
-  // without a reader of the final defect the last step only adds its
-  // correction to acc (the step's t is not kept either: lmgc's t is dead
-  // after its post-smoothing)
-  const bool last_acc_only = !want_b && steps >= 1 && acc->prec == bv->prec;
   // FP32 only: recomputing D^{-1} b per stored entry triples the FP64
   // arithmetic per entry, and GB300's FP64 rate makes that slower than the
   // two-pass step
-  if (x->prec != GMG_PREC_FP32 || acc->prec != x->prec || bv->prec != x->prec || steps < 2) {
-    if (!last_acc_only) return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
-    if (NPIter::IterAccN(level, x, bv, Am, acc, steps - 1, result)) return 1;
-    return k_jac_acc(mg, L, acc->prec, vlev(acc, level), vlev(bv, level), damp);
-  }
+  if (x->prec != GMG_PREC_FP32 || acc->prec != x->prec || bv->prec != x->prec || steps < 2)
+    return NPIter::IterAccN(level, x, bv, Am, acc, steps, result);
   gmg_vec *pp = temp_vec(mg, "__jac_pp" + std::to_string(x->prec), x->prec);
   GMG_CHECK(pp, "jac: temporary vector");
+  const Level &L = mg->lev[level];
   void *src = vlev(bv, level), *dst = vlev(pp, level);
   for (int i = 0; i < steps; ++i) {
-    if (i == steps - 1 && last_acc_only) return k_jac_acc(mg, L, x->prec, vlev(acc, level), src, damp);
     if (k_jac_step(mg, L, x->prec, dst, src, vlev(acc, level), damp)) return 1;
     std::swap(src, dst);
   }
@@ -693,6 +685,7 @@ int NPLmgc::Init(const Args &a) {  // LmgcInit, iter.cc:7613
   }
   if (!a.get_int("fuse", &fuse_rows)) fuse_rows = 6000;
   if (!a.get_int("narrow", &narrow)) narrow = 1;
+  if (!a.get_int("defect", &keep_defect)) keep_defect = 0;
   int bs = 0;
   batch_smem = a.get_int("bsmem", &bs) ? bs : BATCH_COARSE_SMEM_BUDGET;
   if (!Transfer || !PreSmooth || !PostSmooth || !BaseSolver) return NP_NOT_ACTIVE;
@@ -706,7 +699,7 @@ std::string NPLmgc::Display() const {
   std::ostringstream o;
   o << NPIter::Display() << "g = " << gamma << "\nn1 = " << nu1 << "\nn2 = " << nu2 << "\nbaselevel = " << baselevel
     << "\nfuse = " << fuse_rows << " (" << (fusable_smoother() >= 0 ? "fused coarse cycle" : "not fusable")
-    << ")\nnarrow = " << narrow
+    << ")\nnarrow = " << narrow << "\ndefect = " << (keep_defect ? "every level" : "where read")
     << "\nT = " << (Transfer ? Transfer->name : "---") << "\npre = " << (PreSmooth ? PreSmooth->name : "---")
     << "\npost = " << (PostSmooth ? PostSmooth->name : "---") << "\nbase = " << (BaseSolver ? BaseSolver->name : "---")
     << "\n";
@@ -754,7 +747,7 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   if (check_level(mg, level)) return 1;
   GMG_CHECK(cv->prec == bv->prec, "lmgc: c and b differ in precision");
   const int prec = cv->prec;
-  const bool b_unused = defect_unused;
+  const bool b_unused = defect_unused && !keep_defect;
   if (level <= baselevel) {
     NPLs *bls = dynamic_cast<NPLs *>(BaseSolver);
     if (bls && bls->is_exact_base()) {
@@ -803,8 +796,8 @@ int NPLmgc::Iter(int level, gmg_vec *cv, gmg_vec *bv, gmg_mat *Am, int *result) 
   // reset, not surface-based; a batched level that is some instance's top
   // keeps that instance's rows, VNCLASS < 2, so it never qualifies): its
   // post-smoothing may skip it
-  const bool coarse_b_dead = typeid(*Transfer) == typeid(NPTransfer) && !Transfer->imat && !mg->local() &&
-                             mg->lev[level - 1].all_reset;
+  const bool coarse_b_dead = !keep_defect && typeid(*Transfer) == typeid(NPTransfer) && !Transfer->imat &&
+                             !mg->local() && mg->lev[level - 1].all_reset;
   for (int i = 0; i < gamma; ++i) {
     defect_unused = coarse_b_dead && i == gamma - 1;
     const int rc = Iter(level - 1, cv, bv, Am, result);

@@ -150,6 +150,7 @@ struct NPLmgc : NPIter {  // lmgc, iter.cc:7578-8000
   // restriction overwrites it; the top of a uniform or batched mixed ls
   // iteration, whose FP32 defect is rebuilt from the FP64 one)
   bool defect_unused = false;
+  int keep_defect = 0;  // $defect 1: every post-smoothing computes its final defect (as UG does)
   int narrow = 1;  // $narrow 0: the fused cycle runs its smallest levels with the whole block
   // batched hierarchies: the fused cycle runs one block per instance, over
   // the levels whose largest instance image fits batch_smem bytes ($bsmem; 0 disables)
