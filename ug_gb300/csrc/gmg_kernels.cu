@@ -689,11 +689,13 @@ __global__ void __launch_bounds__(NT, 1) sell_gs_chain_cta_kernel(const __grid_c
 // memory: a new t_i is stored into every block's copy through distributed
 // shared memory, and the waves are separated by cluster barriers (release
 // on arrive, acquire on wait).  With RS the matrix entries of the block's
-// rows are staged in its shared memory once per call (before the launch
-// wait), so the waves read no global memory; without it the rows stream from
-// L2 and each thread's next row is fetched between arrive and wait.  The
-// arithmetic of every row is that of sell_gs_chain_kernel, in the same order,
-// so the results are bit-identical to the per-wave launches.
+// rows and their inverse diagonals are staged in its shared memory once per
+// call (before the launch wait), so the waves read no global memory; without
+// it only each row's inverse diagonal, first entry and widths are staged, the
+// entries stream from L2, and each thread fetches its next row before it
+// sends its new values.  The arithmetic of every row is that of
+// sell_gs_chain_kernel, in the same order, so the results are bit-identical
+// to the per-wave launches.
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
